@@ -1,0 +1,271 @@
+/*
+ * swgb.h -- C-ABI of the GB300-native draw path (vertex transform + clipping,
+ * triangle setup, fixed-point span rasterisation, attribute interpolation,
+ * SamplerCore texture filtering, depth test, colour blend/write).
+ *
+ * This boundary replaces, for the triangle-list FILL path only:
+ *   void sw::Renderer::draw(const vk::GraphicsPipeline *, const vk::DynamicState &,
+ *                           unsigned count, int baseVertex, CountedEvent *,
+ *                           int instanceID, int layer, void *indexBuffer,
+ *                           const VkRect2D &renderArea,
+ *                           const vk::Pipeline::PushConstantStorage &, bool update)
+ *   (src/Device/Renderer.hpp:211-213, body src/Device/Renderer.cpp:183-490)
+ * and sw::Renderer::synchronize() (src/Device/Renderer.hpp:218,
+ * src/Device/Renderer.cpp:664-671).
+ *
+ * The vk::GraphicsPipeline state the reference consumes (vk::GraphicsState,
+ * src/Device/Context.hpp:443-496; vk::Attachments :112-129; vk::Inputs :132-157;
+ * sw::DrawData src/Device/Renderer.hpp:58-113) is flattened into the POD
+ * swgb_pipeline_state below.  Enumerants reuse the numeric values of the
+ * Vulkan enums they stand for (VkFormat, VkCompareOp, VkBlendFactor, VkBlendOp,
+ * VkCullModeFlagBits, VkFrontFace, VkIndexType, VkFilter,
+ * VkSamplerMipmapMode, VkSamplerAddressMode), so a Vulkan-side caller copies
+ * its create-info fields straight across.
+ *
+ * All buffer pointers handed to swgb_draw / swgb_draw_batch are DEVICE
+ * pointers (cudaMalloc'd, this process, the context's device).  The caller owns
+ * them.  The library owns only its scratch memory (post-transform vertices,
+ * per-triangle records, bin lists), sized on demand inside the context.
+ *
+ * Every entry point returns a swgb_status; none aborts the process.
+ */
+#ifndef SWGB_H
+#define SWGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SWGB_ABI_VERSION 1
+
+typedef enum swgb_status {
+    SWGB_OK = 0,
+    SWGB_UNSUPPORTED_STATE = 1, /* state the GB300 path does not implement (reference: UNSUPPORTED()) */
+    SWGB_INVALID_ARG = 2,       /* null pointer, zero-sized attachment, out-of-range enum   */
+    SWGB_OOM = 3,               /* scratch allocation failed                                 */
+    SWGB_DEVICE_TIMEOUT = 4,    /* a bounded device-side wait gave up                        */
+    SWGB_DEVICE_ERROR = 5,      /* a CUDA call failed; swgb_last_error() has the text        */
+    SWGB_NO_DEVICE = 6          /* no CUDA device visible                                    */
+} swgb_status;
+
+/* --- Vulkan enumerant values used by the path (subset) ------------------ */
+/* VkFormat */
+#define SWGB_FORMAT_UNDEFINED 0
+#define SWGB_FORMAT_R8G8B8A8_UNORM 37
+#define SWGB_FORMAT_R16G16B16A16_SFLOAT 97
+#define SWGB_FORMAT_R32G32_SFLOAT 103
+#define SWGB_FORMAT_R32G32B32A32_SFLOAT 109
+#define SWGB_FORMAT_D32_SFLOAT 126
+/* VkPrimitiveTopology */
+#define SWGB_TOPOLOGY_TRIANGLE_LIST 3
+/* VkIndexType (0xFFFFFFFF = non-indexed draw) */
+#define SWGB_INDEX_TYPE_UINT16 0
+#define SWGB_INDEX_TYPE_UINT32 1
+#define SWGB_INDEX_TYPE_NONE 0xFFFFFFFFu
+/* VkCullModeFlagBits */
+#define SWGB_CULL_NONE 0
+#define SWGB_CULL_FRONT 1
+#define SWGB_CULL_BACK 2
+#define SWGB_CULL_FRONT_AND_BACK 3
+/* VkFrontFace */
+#define SWGB_FRONT_FACE_COUNTER_CLOCKWISE 0
+#define SWGB_FRONT_FACE_CLOCKWISE 1
+/* VkCompareOp */
+#define SWGB_COMPARE_NEVER 0
+#define SWGB_COMPARE_LESS 1
+#define SWGB_COMPARE_EQUAL 2
+#define SWGB_COMPARE_LESS_OR_EQUAL 3
+#define SWGB_COMPARE_GREATER 4
+#define SWGB_COMPARE_NOT_EQUAL 5
+#define SWGB_COMPARE_GREATER_OR_EQUAL 6
+#define SWGB_COMPARE_ALWAYS 7
+/* VkBlendFactor */
+#define SWGB_BLEND_ZERO 0
+#define SWGB_BLEND_ONE 1
+#define SWGB_BLEND_SRC_COLOR 2
+#define SWGB_BLEND_ONE_MINUS_SRC_COLOR 3
+#define SWGB_BLEND_DST_COLOR 4
+#define SWGB_BLEND_ONE_MINUS_DST_COLOR 5
+#define SWGB_BLEND_SRC_ALPHA 6
+#define SWGB_BLEND_ONE_MINUS_SRC_ALPHA 7
+#define SWGB_BLEND_DST_ALPHA 8
+#define SWGB_BLEND_ONE_MINUS_DST_ALPHA 9
+/* VkBlendOp */
+#define SWGB_BLEND_OP_ADD 0
+#define SWGB_BLEND_OP_SUBTRACT 1
+#define SWGB_BLEND_OP_REVERSE_SUBTRACT 2
+#define SWGB_BLEND_OP_MIN 3
+#define SWGB_BLEND_OP_MAX 4
+/* VkFilter / VkSamplerMipmapMode / VkSamplerAddressMode */
+#define SWGB_FILTER_NEAREST 0
+#define SWGB_FILTER_LINEAR 1
+#define SWGB_MIPMAP_MODE_NEAREST 0
+#define SWGB_MIPMAP_MODE_LINEAR 1
+#define SWGB_ADDRESS_REPEAT 0
+#define SWGB_ADDRESS_MIRRORED_REPEAT 1
+#define SWGB_ADDRESS_CLAMP_TO_EDGE 2
+
+/* The fixed shaders the path runs in place of SPIR-V modules.
+ * VS_MVP_PASSTHROUGH: gl_Position = mvp * attribute[0] (OpMatrixTimesVector,
+ *   src/Pipeline/SpirvShaderArithmetic.cpp:39-55); output location k = input
+ *   attribute k+1 unchanged.
+ * FS_VCOLOR:          outColor = in[0]                       (vec4 colour)
+ * FS_TEX_X_VCOLOR:    outColor = texture(tex, in[1].xy) * in[0] (OpFMul) */
+#define SWGB_VS_MVP_PASSTHROUGH 1
+#define SWGB_FS_VCOLOR 1
+#define SWGB_FS_TEX_X_VCOLOR 2
+
+/* Precision profiles of the reference (src/Vulkan/VkConfig.hpp:23-24,101-103).
+ * Only the standalone CMake profile (8 sub-pixel bits, fused mulAdd, 16-bit
+ * UNORM8 filtering) is implemented; the GN/Chromium legacy profile returns
+ * SWGB_UNSUPPORTED_STATE. */
+#define SWGB_PRECISION_CMAKE 0
+#define SWGB_PRECISION_LEGACY 1
+
+#define SWGB_MAX_ATTRIBS 4
+#define SWGB_MAX_MIP_LEVELS 15 /* sw::MIPMAP_LEVELS, src/Device/Config.hpp:23 */
+
+typedef struct swgb_vertex_attrib {
+    uint32_t format;   /* R32G32B32A32_SFLOAT or R32G32_SFLOAT                  */
+    uint32_t binding;  /* index into swgb_pipeline_state.bindings               */
+    uint32_t offset;   /* byte offset of the attribute inside one vertex        */
+    uint32_t reserved;
+} swgb_vertex_attrib;
+
+typedef struct swgb_vertex_binding {
+    const void *buffer; /* device pointer to vertex 0                           */
+    uint32_t stride;    /* bytes between consecutive vertices                   */
+    uint32_t reserved;
+} swgb_vertex_binding;
+
+typedef struct swgb_texture_level {
+    const void *buffer;    /* device pointer to texel (0,0) of this level        */
+    uint32_t width;
+    uint32_t height;
+    uint32_t pitch_texels; /* row pitch in texels (Mipmap::pitchP)               */
+    uint32_t reserved;
+} swgb_texture_level;
+
+/* A combined image sampler (VkDescriptorImageInfo + VkSamplerCreateInfo
+ * subset).  Level i of levels[] is image-view level i; entries past
+ * level_count are ignored (the descriptor replicates the last level,
+ * src/Vulkan/VkDescriptorSetLayout.cpp:468-470). */
+typedef struct swgb_texture {
+    uint32_t format;      /* R8G8B8A8_UNORM, R16G16B16A16_SFLOAT or R32G32B32A32_SFLOAT */
+    uint32_t level_count;
+    swgb_texture_level levels[SWGB_MAX_MIP_LEVELS];
+    uint32_t mag_filter, min_filter, mipmap_mode;
+    uint32_t address_u, address_v;
+    float mip_lod_bias, min_lod, max_lod;
+} swgb_texture;
+
+typedef struct swgb_pipeline_state {
+    /* vertex input interface (vk::VertexInputInterfaceState) */
+    uint32_t topology;
+    uint32_t attrib_count;
+    swgb_vertex_attrib attribs[SWGB_MAX_ATTRIBS];
+    swgb_vertex_binding bindings[SWGB_MAX_ATTRIBS];
+    /* shaders + push constants */
+    uint32_t vertex_shader;
+    uint32_t fragment_shader;
+    float mvp[16]; /* column-major, the push-constant block of the fixed VS */
+    /* pre-rasterization (vk::PreRasterizationState) */
+    float viewport_x, viewport_y, viewport_width, viewport_height;
+    float viewport_min_depth, viewport_max_depth;
+    int32_t scissor_x, scissor_y;
+    uint32_t scissor_width, scissor_height;
+    uint32_t cull_mode, front_face;
+    uint32_t depth_clip_enable;  /* VK_EXT_depth_clip_enable; default true   */
+    uint32_t depth_clamp_enable; /* must be 0                                 */
+    float depth_bias_constant, depth_bias_slope, depth_bias_clamp; /* must be 0 */
+    /* fragment (vk::FragmentState) */
+    uint32_t depth_test_enable, depth_write_enable, depth_compare_op;
+    /* fragment output interface (vk::FragmentOutputInterfaceState) */
+    uint32_t color_format;
+    uint32_t blend_enable;
+    uint32_t src_color_factor, dst_color_factor, color_blend_op;
+    uint32_t src_alpha_factor, dst_alpha_factor, alpha_blend_op;
+    uint32_t color_write_mask; /* VkColorComponentFlags, 0xF = RGBA        */
+    uint32_t sample_count;     /* 1 (4 = MSAA, not yet implemented)        */
+    /* attachments (vk::Attachments -> DrawData colorBuffer/depthBuffer) */
+    void *color;
+    uint32_t color_pitch_bytes;
+    uint32_t reserved0;
+    uint64_t color_slice_bytes;
+    void *depth;
+    uint32_t depth_pitch_bytes;
+    uint32_t reserved1;
+    uint64_t depth_slice_bytes;
+    uint32_t framebuffer_width, framebuffer_height;
+    /* the fragment shader's combined image sampler (FS_TEX_X_VCOLOR) */
+    swgb_texture texture;
+    uint32_t precision_profile;
+    uint32_t reserved2;
+} swgb_pipeline_state;
+
+/* The per-draw arguments of sw::Renderer::draw. */
+typedef struct swgb_draw_args {
+    uint32_t count;        /* number of triangles (Renderer::draw 'count')              */
+    int32_t base_vertex;   /* added to every vertex index ('baseVertex')                */
+    uint32_t first_vertex; /* non-indexed draws: index of the first vertex              */
+    uint32_t index_type;   /* SWGB_INDEX_TYPE_UINT16/UINT32, or SWGB_INDEX_TYPE_NONE    */
+    const void *indices;   /* device pointer to the first index of the draw             */
+    uint32_t vertex_count; /* indexed draws: vertices addressable after base_vertex;
+                              every index must be < vertex_count                       */
+    int32_t instance_id, layer;
+    int32_t render_area_x, render_area_y;
+    uint32_t render_area_width, render_area_height;
+    uint32_t reserved;
+} swgb_draw_args;
+
+/* Device-side counters of one draw (the reference keeps occlusion counts per
+ * cluster, src/Device/Renderer.cpp:413-419,524-531).  Accumulated across
+ * draws until swgb_reset_counters. */
+typedef struct swgb_counters {
+    uint64_t triangles_in;       /* triangles submitted                               */
+    uint64_t triangles_rejected; /* trivially rejected, clipped away or culled        */
+    uint64_t triangles_clipped;  /* triangles that went through the clipper           */
+    uint64_t triangles_visible;  /* setup returned a primitive (SetupRoutine 'Return(1)') */
+    uint64_t quads;              /* 2x2 quads with non-empty coverage that were shaded */
+    uint64_t fragments_tested;   /* covered samples that reached the depth test       */
+    uint64_t fragments_passed;   /* samples that passed and were written              */
+    uint64_t reserved;
+} swgb_counters;
+
+typedef struct swgb_ctx swgb_ctx;
+
+/* Library / context management. 'stream' is a cudaStream_t (NULL = the
+ * context creates its own non-blocking stream). */
+int swgb_abi_version(void);
+const char *swgb_last_error(void);
+swgb_status swgb_ctx_create(int device, void *stream, swgb_ctx **out);
+swgb_status swgb_ctx_destroy(swgb_ctx *ctx);
+swgb_status swgb_ctx_set_stream(swgb_ctx *ctx, void *stream);
+
+/* Validates and bakes the pipeline state, then enqueues one draw on the
+ * context's stream.  Returns before the draw completes (Renderer::draw also
+ * returns before its marl tasks finish). */
+swgb_status swgb_draw(swgb_ctx *ctx, const swgb_pipeline_state *state, const swgb_draw_args *args);
+
+/* N independent draws (own state, own attachments) enqueued as one persistent
+ * launch fed by a device work queue. */
+swgb_status swgb_draw_batch(swgb_ctx *ctx, const swgb_pipeline_state *states, const swgb_draw_args *args, uint32_t n);
+
+/* Waits for every draw enqueued so far (Renderer::synchronize). */
+swgb_status swgb_sync(swgb_ctx *ctx);
+
+/* Counters: copies the device counters to *out (synchronises the stream). */
+swgb_status swgb_get_counters(swgb_ctx *ctx, swgb_counters *out);
+swgb_status swgb_reset_counters(swgb_ctx *ctx);
+
+/* Number of kernel launches this context has issued since creation. */
+uint64_t swgb_launch_count(swgb_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SWGB_H */

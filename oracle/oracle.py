@@ -1,0 +1,102 @@
+"""TEST INFRASTRUCTURE ONLY: Python loader for the CPU oracle.
+
+Only tests/, __graft_entry__.smoke() and bench.py (cpu_baseline leg and
+--impl reference) import this module.  The swiftshader_gb300 package never
+does.  ``build()`` compiles swgb_oracle.c with gcc; ``render()`` runs one draw
+of a scene on host buffers and returns the attachments and counters.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "libswgb_oracle.so")
+SRC = os.path.join(HERE, "swgb_oracle.c")
+CFLAGS = ["-O2", "-fPIC", "-shared", "-std=c11", "-fwrapv", "-ffp-contract=off", "-fno-fast-math",
+          "-Wall", "-Wextra"]
+
+_lib = None
+
+
+def build(force=False):
+    os.makedirs(BUILD, exist_ok=True)
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(
+            os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "swgb_oracle.h"))):
+        return LIB
+    tmp = LIB + ".tmp%d" % os.getpid()
+    subprocess.check_call(["gcc"] + CFLAGS + ["-o", tmp, SRC, "-lm", "-lpthread"])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        import sys
+        sys.path.insert(0, os.path.dirname(HERE))
+        from swiftshader_gb300 import abi
+        build()
+        L = C.CDLL(LIB)
+        L.oracle_draw.argtypes = [C.POINTER(abi.PipelineState), C.POINTER(abi.DrawArgs), C.c_int,
+                                  C.POINTER(abi.Counters)]
+        L.oracle_draw.restype = C.c_int
+        L.oracle_round_int.argtypes = [C.c_float]
+        L.oracle_round_int.restype = C.c_int32
+        L.oracle_round_int_clamped.argtypes = [C.c_float]
+        L.oracle_round_int_clamped.restype = C.c_int32
+        L.oracle_trunc_int.argtypes = [C.c_float]
+        L.oracle_trunc_int.restype = C.c_int32
+        L.oracle_mulhigh_u16.argtypes = [C.c_uint16, C.c_uint16]
+        L.oracle_mulhigh_u16.restype = C.c_uint16
+        L.oracle_mulhigh_s16.argtypes = [C.c_int16, C.c_int16]
+        L.oracle_mulhigh_s16.restype = C.c_int16
+        L.oracle_fmuladd.argtypes = [C.c_float, C.c_float, C.c_float]
+        L.oracle_fmuladd.restype = C.c_float
+        L.oracle_log2sqrt.argtypes = [C.c_float]
+        L.oracle_log2sqrt.restype = C.c_float
+        L.oracle_ftz.argtypes = [C.c_float]
+        L.oracle_ftz.restype = C.c_float
+        L.oracle_vertex.argtypes = [C.POINTER(abi.PipelineState), C.POINTER(abi.DrawArgs), C.c_uint32,
+                                    C.POINTER(C.c_float), C.POINTER(C.c_int32)]
+        L.oracle_vertex.restype = C.c_int
+        L.oracle_setup.argtypes = [C.POINTER(abi.PipelineState), C.POINTER(abi.DrawArgs), C.c_uint32,
+                                   C.POINTER(C.c_int32), C.POINTER(C.c_uint16), C.c_int, C.POINTER(C.c_float)]
+        L.oracle_setup.restype = C.c_int
+        L.oracle_sample_quad.argtypes = [C.POINTER(abi.Texture), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                         C.POINTER(C.c_float)]
+        L.oracle_sample_quad.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data if a is not None else None
+
+
+def host_state(scene, color, depth):
+    """PipelineState + DrawArgs whose pointers address host numpy arrays."""
+    from swiftshader_gb300 import scenes
+    verts = np.ascontiguousarray(scene.vertices, np.float32)
+    levels = [np.ascontiguousarray(l) for l in scene.texture_levels]
+    st = scenes.build_state(scene, _ptr(color), _ptr(depth), _ptr(verts), [_ptr(l) for l in levels])
+    idx = None if scene.indices is None else np.ascontiguousarray(scene.indices, np.uint32)
+    args = scenes.build_args(scene, _ptr(idx))
+    keep = (verts, levels, idx)
+    return st, args, keep
+
+
+def render(scene, nthreads=1, color=None, depth=None):
+    """Runs one draw of 'scene' on the CPU oracle; returns (color, depth, counters dict)."""
+    from swiftshader_gb300 import abi, scenes
+    if color is None or depth is None:
+        color, depth = scenes.clear_buffers(scene)
+    st, args, keep = host_state(scene, color, depth)
+    cnt = abi.Counters()
+    s = lib().oracle_draw(C.byref(st), C.byref(args), nthreads, C.byref(cnt))
+    if s != 0:
+        raise RuntimeError("oracle_draw failed: %s" % abi.STATUS_NAMES.get(s, s))
+    del keep
+    return color, depth, cnt.as_dict()

@@ -1,0 +1,120 @@
+"""ctypes mirror of include/swgb.h.
+
+The structs here are byte-for-byte the C-ABI structs; ``tests/test_abi.py``
+checks their sizes and offsets against the header.  The same structs drive the
+GB300 library (device pointers) and the CPU oracle used by the tests (host
+pointers).
+"""
+import ctypes as C
+
+# swgb_status
+OK = 0
+UNSUPPORTED_STATE = 1
+INVALID_ARG = 2
+OOM = 3
+DEVICE_TIMEOUT = 4
+DEVICE_ERROR = 5
+NO_DEVICE = 6
+STATUS_NAMES = {0: "OK", 1: "UNSUPPORTED_STATE", 2: "INVALID_ARG", 3: "OOM",
+                4: "DEVICE_TIMEOUT", 5: "DEVICE_ERROR", 6: "NO_DEVICE"}
+
+# VkFormat subset
+FORMAT_R8G8B8A8_UNORM = 37
+FORMAT_R16G16B16A16_SFLOAT = 97
+FORMAT_R32G32_SFLOAT = 103
+FORMAT_R32G32B32A32_SFLOAT = 109
+FORMAT_D32_SFLOAT = 126
+TOPOLOGY_TRIANGLE_LIST = 3
+INDEX_TYPE_UINT16 = 0
+INDEX_TYPE_UINT32 = 1
+INDEX_TYPE_NONE = 0xFFFFFFFF
+CULL_NONE, CULL_FRONT, CULL_BACK, CULL_FRONT_AND_BACK = 0, 1, 2, 3
+FRONT_FACE_CCW, FRONT_FACE_CW = 0, 1
+(COMPARE_NEVER, COMPARE_LESS, COMPARE_EQUAL, COMPARE_LESS_OR_EQUAL, COMPARE_GREATER,
+ COMPARE_NOT_EQUAL, COMPARE_GREATER_OR_EQUAL, COMPARE_ALWAYS) = range(8)
+(BLEND_ZERO, BLEND_ONE, BLEND_SRC_COLOR, BLEND_ONE_MINUS_SRC_COLOR, BLEND_DST_COLOR,
+ BLEND_ONE_MINUS_DST_COLOR, BLEND_SRC_ALPHA, BLEND_ONE_MINUS_SRC_ALPHA, BLEND_DST_ALPHA,
+ BLEND_ONE_MINUS_DST_ALPHA) = range(10)
+BLEND_OP_ADD, BLEND_OP_SUBTRACT, BLEND_OP_REVERSE_SUBTRACT, BLEND_OP_MIN, BLEND_OP_MAX = range(5)
+FILTER_NEAREST, FILTER_LINEAR = 0, 1
+MIPMAP_MODE_NEAREST, MIPMAP_MODE_LINEAR = 0, 1
+ADDRESS_REPEAT, ADDRESS_MIRRORED_REPEAT, ADDRESS_CLAMP_TO_EDGE = 0, 1, 2
+VS_MVP_PASSTHROUGH = 1
+FS_VCOLOR = 1
+FS_TEX_X_VCOLOR = 2
+PRECISION_CMAKE = 0
+PRECISION_LEGACY = 1
+MAX_ATTRIBS = 4
+MAX_MIP_LEVELS = 15
+
+
+class VertexAttrib(C.Structure):
+    _fields_ = [("format", C.c_uint32), ("binding", C.c_uint32),
+                ("offset", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class VertexBinding(C.Structure):
+    _fields_ = [("buffer", C.c_void_p), ("stride", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class TextureLevel(C.Structure):
+    _fields_ = [("buffer", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("pitch_texels", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class Texture(C.Structure):
+    _fields_ = [("format", C.c_uint32), ("level_count", C.c_uint32),
+                ("levels", TextureLevel * MAX_MIP_LEVELS),
+                ("mag_filter", C.c_uint32), ("min_filter", C.c_uint32), ("mipmap_mode", C.c_uint32),
+                ("address_u", C.c_uint32), ("address_v", C.c_uint32),
+                ("mip_lod_bias", C.c_float), ("min_lod", C.c_float), ("max_lod", C.c_float)]
+
+
+class PipelineState(C.Structure):
+    _fields_ = [
+        ("topology", C.c_uint32), ("attrib_count", C.c_uint32),
+        ("attribs", VertexAttrib * MAX_ATTRIBS), ("bindings", VertexBinding * MAX_ATTRIBS),
+        ("vertex_shader", C.c_uint32), ("fragment_shader", C.c_uint32),
+        ("mvp", C.c_float * 16),
+        ("viewport_x", C.c_float), ("viewport_y", C.c_float),
+        ("viewport_width", C.c_float), ("viewport_height", C.c_float),
+        ("viewport_min_depth", C.c_float), ("viewport_max_depth", C.c_float),
+        ("scissor_x", C.c_int32), ("scissor_y", C.c_int32),
+        ("scissor_width", C.c_uint32), ("scissor_height", C.c_uint32),
+        ("cull_mode", C.c_uint32), ("front_face", C.c_uint32),
+        ("depth_clip_enable", C.c_uint32), ("depth_clamp_enable", C.c_uint32),
+        ("depth_bias_constant", C.c_float), ("depth_bias_slope", C.c_float), ("depth_bias_clamp", C.c_float),
+        ("depth_test_enable", C.c_uint32), ("depth_write_enable", C.c_uint32), ("depth_compare_op", C.c_uint32),
+        ("color_format", C.c_uint32), ("blend_enable", C.c_uint32),
+        ("src_color_factor", C.c_uint32), ("dst_color_factor", C.c_uint32), ("color_blend_op", C.c_uint32),
+        ("src_alpha_factor", C.c_uint32), ("dst_alpha_factor", C.c_uint32), ("alpha_blend_op", C.c_uint32),
+        ("color_write_mask", C.c_uint32), ("sample_count", C.c_uint32),
+        ("color", C.c_void_p), ("color_pitch_bytes", C.c_uint32), ("reserved0", C.c_uint32),
+        ("color_slice_bytes", C.c_uint64),
+        ("depth", C.c_void_p), ("depth_pitch_bytes", C.c_uint32), ("reserved1", C.c_uint32),
+        ("depth_slice_bytes", C.c_uint64),
+        ("framebuffer_width", C.c_uint32), ("framebuffer_height", C.c_uint32),
+        ("texture", Texture),
+        ("precision_profile", C.c_uint32), ("reserved2", C.c_uint32),
+    ]
+
+
+class DrawArgs(C.Structure):
+    _fields_ = [
+        ("count", C.c_uint32), ("base_vertex", C.c_int32), ("first_vertex", C.c_uint32),
+        ("index_type", C.c_uint32), ("indices", C.c_void_p), ("vertex_count", C.c_uint32),
+        ("instance_id", C.c_int32), ("layer", C.c_int32),
+        ("render_area_x", C.c_int32), ("render_area_y", C.c_int32),
+        ("render_area_width", C.c_uint32), ("render_area_height", C.c_uint32),
+        ("reserved", C.c_uint32),
+    ]
+
+
+class Counters(C.Structure):
+    _fields_ = [("triangles_in", C.c_uint64), ("triangles_rejected", C.c_uint64),
+                ("triangles_clipped", C.c_uint64), ("triangles_visible", C.c_uint64),
+                ("quads", C.c_uint64), ("fragments_tested", C.c_uint64),
+                ("fragments_passed", C.c_uint64), ("reserved", C.c_uint64)]
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k, _ in self._fields_ if k != "reserved"}

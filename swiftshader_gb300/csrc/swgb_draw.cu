@@ -1,0 +1,1578 @@
+// swgb_draw.cu -- GB300 (sm_103a) kernels and C-ABI of the draw hot path.
+//
+// Pipeline per draw (all on the context's stream, no host round trip):
+//   k_vertex  : one thread per vertex -- fetch, fixed VS (MVP), clip flags,
+//               projection + viewport snap.  Post-transform vertices stay in
+//               HBM/L2 like the reference's vertex cache
+//               (src/Pipeline/VertexRoutine.cpp:43-87,116-154,570-707).
+//   k_setup   : one thread per triangle, 256-triangle chunks -- trivial
+//               reject, homogeneous clipping, cull, sub-pixel polygon, y range,
+//               empty-row trimming, pixel bounding box; block-reduced chunk
+//               boxes drive the binning (src/Device/Renderer.cpp:733-776,
+//               src/Device/Clipper.cpp, src/Pipeline/SetupRoutine.cpp:36-294).
+//   k_raster  : one CTA per 32x32-pixel bin -- depth and colour of the bin are
+//               staged in shared memory; the chunk boxes and triangle boxes are
+//               tested in primitive order (warp ballot + prefix compaction);
+//               each batch of triangles regenerates its span rows with the
+//               reference's integer DDA, expands into 2x2 quad fragments,
+//               shades them in parallel (interpolation, SamplerCore filtering,
+//               fixed FS), and resolves depth test + blend per quad in
+//               primitive order; the bin is written back with 128-bit stores
+//               (src/Device/QuadRasterizer.cpp:36-250,
+//               src/Pipeline/PixelRoutine.cpp:97-358,494-739,1225-2700,
+//               src/Pipeline/PixelProgram.cpp:138-364,
+//               src/Pipeline/SamplerCore.cpp).
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+#include <string>
+
+#include "../../include/swgb.h"
+#include "swgb_numeric.cuh"
+
+using namespace swgb;
+
+namespace {
+
+constexpr int MAXV = 7;          // varying components carried per vertex
+constexpr int BIN = 32;          // bin side in pixels
+constexpr int BIN_QUADS = (BIN / 2) * (BIN / 2);
+constexpr int RASTER_THREADS = 256;
+constexpr int BATCH = 128;       // triangles staged per raster batch
+constexpr int CHUNK = 256;       // triangles per setup block / chunk box
+constexpr int MAX_POLY = 16;     // clipped polygon capacity (Polygon::B, src/Device/Polygon.hpp:45)
+
+enum { CLIP_RIGHT = 1 << 0, CLIP_TOP = 1 << 1, CLIP_FAR = 1 << 2, CLIP_LEFT = 1 << 3,
+       CLIP_BOTTOM = 1 << 4, CLIP_NEAR = 1 << 5, CLIP_FRUSTUM = 0x3F, CLIP_FINITE = 1 << 7 };
+
+enum { OP_ZERO_EXT = 1000, OP_SRC_EXT = 1001, OP_DST_EXT = 1002 };
+
+enum { ERR_INDEX_RANGE = 1, ERR_POLY_OVERFLOW = 2 };
+
+struct TexLevel {
+    const uint8_t *buf;
+    uint32_t w, h, pitch;
+    uint32_t uHalf, vHalf;
+};
+
+// Per-triangle record written by k_setup (16 bytes).
+struct TriRec {
+    int16_t x0, y0, x1, y1;  // pixel box; y0/y1 are the trimmed [yMin, yMax)
+    uint32_t info;           // bits 0-4: polygon vertex count (0 = no primitive), bit 5: winding d, bit 6: clipped
+    uint32_t slot;           // clipped polygon slot
+};
+
+// Everything a draw's kernels read, baked on the host from the pipeline state
+// (the analog of sw::DrawData plus the processors' state hashes).
+struct DrawParams {
+    // vertex input
+    const uint8_t *vbuf[SWGB_MAX_ATTRIBS];
+    uint32_t vstride[SWGB_MAX_ATTRIBS];
+    uint32_t voff[SWGB_MAX_ATTRIBS];
+    uint32_t vcomp[SWGB_MAX_ATTRIBS];
+    int nattr;
+    int nv;
+    float mvp[16];
+    const void *indices;
+    uint32_t indexType;
+    uint32_t firstVertex;
+    int32_t baseVertex;
+    uint32_t vertexCount;  // post-transform vertices
+    uint32_t count;        // triangles
+    // DrawData
+    float WxF, HxF, X0xF, Y0xF, depthRange, depthNear;
+    int sx0, sx1, sy0, sy1;
+    int depthClip;
+    uint32_t cullMode, frontFace;
+    // pixel state
+    int depthTest, depthWrite, compareOp;
+    float minDepthClamp, maxDepthClamp;
+    int blend;
+    uint32_t srcC, dstC, opC, srcA, dstA, opA;
+    uint32_t writeMask;
+    int fs;
+    uint8_t *color;
+    uint32_t colorPitch;
+    uint8_t *depth;
+    uint32_t depthPitch;
+    int vec16;  // attachments allow 16-byte row accesses
+    // texture
+    TexLevel lv[SWGB_MAX_MIP_LEVELS];
+    int levelCount;
+    float texW, texH;
+    float minLod, maxLod, lodBias;
+    int texLinear, mipLinear;
+    uint32_t addrU, addrV;
+    // bins
+    int binX0, binY0, binsX, binsY;
+    int nchunks;
+    // scratch
+    float4 *ptv;          // 4 x float4 per vertex
+    TriRec *tris;
+    short4 *chunkBox;     // x0, y0, x1, y1 per chunk
+    int2 *poly;           // MAX_POLY per slot
+    uint32_t *polyCount;
+    uint32_t polyCapacity;
+    unsigned long long *counters;
+    int *error;
+};
+
+// ------------------------------------------------------------------------
+// Vertex stage
+// ------------------------------------------------------------------------
+
+__device__ __forceinline__ void read_attrib(const DrawParams &D, int a, uint32_t index, float out[4])
+{
+    const float *p = (const float *)(D.vbuf[a] + (size_t)index * D.vstride[a] + D.voff[a]);
+    out[0] = __ldg(p + 0);
+    out[1] = __ldg(p + 1);
+    if(D.vcomp[a] == 4)
+    {
+        out[2] = __ldg(p + 2);
+        out[3] = __ldg(p + 3);
+    }
+    else
+    {
+        out[2] = 0.0f;
+        out[3] = 1.0f;  // readStream: componentCount < 4 -> w = 1 (VertexRoutine.cpp:565)
+    }
+}
+
+// Post-transform vertex: float4[0] = clip position; float4[1] = (X bits, Y
+// bits, clipFlags bits, projected z); float4[2] = (rhw, v0, v1, v2);
+// float4[3] = (v3, v4, v5, v6).
+__global__ void k_vertex(const __grid_constant__ DrawParams D, uint32_t nverts)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i == 0) *D.polyCount = 0;
+    if(i >= nverts) return;
+    uint32_t index = (D.indexType == SWGB_INDEX_TYPE_NONE ? D.firstVertex + i : i) + (uint32_t)D.baseVertex;
+    float p[4];
+    read_attrib(D, 0, index, p);
+    // OpMatrixTimesVector (src/Pipeline/SpirvShaderArithmetic.cpp:39-55), column-major.
+    float r[4];
+#pragma unroll
+    for(int row = 0; row < 4; row++)
+    {
+        float v = D.mvp[row] * p[0];
+        v = mul_add(D.mvp[4 + row], p[1], v);
+        v = mul_add(D.mvp[8 + row], p[2], v);
+        v = mul_add(D.mvp[12 + row], p[3], v);
+        r[row] = v;
+    }
+    float x = r[0], y = r[1], z = r[2], w = r[3];
+    // computeClipFlags (VertexRoutine.cpp:116-154)
+    int f = 0;
+    if(w < x) f |= CLIP_RIGHT;
+    if(w < y) f |= CLIP_TOP;
+    if(!(-w <= x)) f |= CLIP_LEFT;
+    if(!(-w <= y)) f |= CLIP_BOTTOM;
+    if(D.depthClip)
+    {
+        if(w < z) f |= CLIP_FAR;
+        if(!(0.0f <= z)) f |= CLIP_NEAR;
+    }
+    const float maxPos = __int_as_float(0x7F7FFFFF);
+    if(fabsf(x) <= maxPos && fabsf(y) <= maxPos && fabsf(z) <= maxPos) f |= CLIP_FINITE;
+    // writeCache projection (VertexRoutine.cpp:599-612)
+    uint32_t wb = __float_as_uint(w);
+    if(w == 0.0f) wb |= 0x3F800000u;
+    float rhw = 1.0f / __uint_as_float(wb);
+    int32_t X = round_int_clamped(D.X0xF + (x * rhw) * D.WxF);
+    int32_t Y = round_int_clamped(D.Y0xF + (y * rhw) * D.HxF);
+    float v[MAXV + 1] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int k = 0;
+    for(int a = 1; a < D.nattr; a++)
+    {
+        float t[4];
+        read_attrib(D, a, index, t);
+        for(int c = 0; c < (int)D.vcomp[a] && k < MAXV; c++) v[k++] = t[c];
+    }
+    float4 *o = D.ptv + (size_t)i * 4;
+    o[0] = make_float4(x, y, z, w);
+    o[1] = make_float4(__int_as_float(X), __int_as_float(Y), __int_as_float(f), z * rhw);
+    o[2] = make_float4(rhw, v[0], v[1], v[2]);
+    o[3] = make_float4(v[3], v[4], v[5], v[6]);
+}
+
+// ------------------------------------------------------------------------
+// Setup stage
+// ------------------------------------------------------------------------
+
+__device__ __forceinline__ uint32_t fetch_index(const DrawParams &D, uint32_t k)
+{
+    if(D.indexType == SWGB_INDEX_TYPE_NONE) return k;
+    if(D.indexType == SWGB_INDEX_TYPE_UINT16) return __ldg((const uint16_t *)D.indices + k);
+    return __ldg((const uint32_t *)D.indices + k);
+}
+
+struct CVert { float x, y, z, w; };
+
+__device__ __forceinline__ float plane_dist(const CVert &v, int plane)
+{
+    switch(plane)
+    {
+    case 0: return v.z;
+    case 1: return v.w - v.z;
+    case 2: return v.w + v.x;
+    case 3: return v.w - v.x;
+    case 4: return v.w - v.y;
+    default: return v.w + v.y;
+    }
+}
+
+// clipEdge (src/Device/Clipper.cpp:22-30)
+__device__ __forceinline__ CVert clip_edge(const CVert &Vi, const CVert &Vj, float di, float dj)
+{
+    float D = 1.0f / (dj - di);
+    CVert o;
+    o.x = (dj * Vi.x - di * Vj.x) * D;
+    o.y = (dj * Vi.y - di * Vj.y) * D;
+    o.z = (dj * Vi.z - di * Vj.z) * D;
+    o.w = (dj * Vi.w - di * Vj.w) * D;
+    return o;
+}
+
+// Clipper::Clip (src/Device/Clipper.cpp:271-299): NEAR, FAR, LEFT, RIGHT,
+// TOP, BOTTOM, each Sutherland-Hodgman pass as clipNear..clipBottom (:32-265).
+__device__ int clip_polygon(CVert *P, int n, int flagsOr)
+{
+    const int order[6] = {CLIP_NEAR, CLIP_FAR, CLIP_LEFT, CLIP_RIGHT, CLIP_TOP, CLIP_BOTTOM};
+    CVert T[MAX_POLY];
+    for(int k = 0; k < 6; k++)
+    {
+        if(n < 3) break;
+        if(!(flagsOr & order[k])) continue;
+        int t = 0;
+        for(int i = 0; i < n; i++)
+        {
+            int j = i == n - 1 ? 0 : i + 1;
+            float di = plane_dist(P[i], k);
+            float dj = plane_dist(P[j], k);
+            if(di >= 0.0f)
+            {
+                if(t < MAX_POLY) T[t] = P[i];
+                t++;
+                if(dj < 0.0f)
+                {
+                    if(t < MAX_POLY) T[t] = clip_edge(P[i], P[j], di, dj);
+                    t++;
+                }
+            }
+            else if(dj > 0.0f)
+            {
+                if(t < MAX_POLY) T[t] = clip_edge(P[j], P[i], dj, di);
+                t++;
+            }
+        }
+        n = t < MAX_POLY ? t : MAX_POLY;
+        for(int i = 0; i < n; i++) P[i] = T[i];
+    }
+    return n;
+}
+
+// Span x of one polygon edge at row y (SetupRoutine::edge, src/Pipeline/SetupRoutine.cpp:550-621):
+// the DDA value after (y - y1) steps, computed in closed form.  Returns false
+// when the edge does not write row y.  *isRight tells which span it writes.
+struct EdgeDDA {
+    int32_t y1, yMin, yMax;  // rows written: [yMin, yMax)
+    int32_t x, d, Q, R, D;   // state at row y1
+    bool right;
+};
+
+__device__ __forceinline__ bool edge_setup(const DrawParams &D, int32_t Xa, int32_t Ya, int32_t Xb, int32_t Yb, EdgeDDA &e)
+{
+    if(Ya == Yb) return false;
+    bool swap = Yb < Ya;
+    int32_t X1 = swap ? Xb : Xa, X2 = swap ? Xa : Xb;
+    int32_t Y1 = swap ? Yb : Ya, Y2 = swap ? Ya : Yb;
+    int32_t y1 = (Y1 + 0xFF) >> 8;
+    int32_t y2 = (Y2 + 0xFF) >> 8;
+    e.y1 = y1;
+    e.yMin = max(y1, D.sy0);
+    e.yMax = min(y2, D.sy1);
+    if(!(e.yMin < e.yMax)) return false;
+    e.right = swap;
+    int32_t DX12 = X2 - X1, DY12 = Y2 - Y1;
+    int32_t FDX12 = (int32_t)((uint32_t)DX12 << 8), FDY12 = (int32_t)((uint32_t)DY12 << 8);
+    int32_t X = (int32_t)((uint32_t)DX12 * (uint32_t)(((uint32_t)y1 << 8) - (uint32_t)Y1) + (uint32_t)(X1 & 0xFF) * (uint32_t)DY12);
+    int32_t x = (X1 >> 8) + X / FDY12;
+    int32_t d = X % FDY12;
+    int32_t c = (-d) >> 31;
+    x -= c;
+    d -= c & FDY12;
+    int32_t Q = FDX12 / FDY12, R = FDX12 % FDY12;
+    int32_t fl = R >> 31;
+    Q += fl;
+    R += fl & FDY12;
+    e.x = x; e.d = d; e.Q = Q; e.R = R; e.D = FDY12;
+    return true;
+}
+
+// x of the edge at row y (y1 <= y): x_k = x0 + k*Q + ceil((d0 + k*R) / D),
+// identical to k iterations of the reference's DDA step.
+__device__ __forceinline__ int32_t edge_x_at(const EdgeDDA &e, int32_t y, int32_t *dOut)
+{
+    int32_t k = y - e.y1;
+    if(k == 0)
+    {
+        if(dOut) *dOut = e.d;
+        return e.x;
+    }
+    long long num = (long long)e.d + (long long)k * e.R;  // > -D
+    long long m = num > 0 ? (num + e.D - 1) / e.D : 0;
+    if(dOut) *dOut = (int32_t)(num - m * e.D);
+    return (int32_t)((uint32_t)e.x + (uint32_t)k * (uint32_t)e.Q + (uint32_t)m);
+}
+
+__device__ __forceinline__ int32_t clamp_x(const DrawParams &D, int32_t x) { return min(max(x, D.sx0), D.sx1); }
+
+// Span (left, right) of a polygon at row y: the last edge (in edge order)
+// that writes the row wins, as in the reference's outline buffer.
+__device__ void span_at(const DrawParams &D, const int32_t *X, const int32_t *Y, int n, int dW, int32_t y, int32_t &l, int32_t &r)
+{
+    l = 0; r = 0;
+    for(int i = 0; i < n; i++)
+    {
+        int ia = i + 1 - dW, ib = i + dW;
+        ia = ia == n ? 0 : ia;
+        ib = ib == n ? 0 : ib;
+        EdgeDDA e;
+        if(!edge_setup(D, X[ia], Y[ia], X[ib], Y[ib], e)) continue;
+        if(y < e.yMin || y >= e.yMax) continue;
+        int32_t x = clamp_x(D, edge_x_at(e, y, nullptr));
+        if(e.right) r = x; else l = x;
+    }
+}
+
+__device__ __forceinline__ short4 empty_box() { return make_short4(0x7FFF, 0x7FFF, -0x8000, -0x8000); }
+
+__global__ void __launch_bounds__(CHUNK) k_setup(const __grid_constant__ DrawParams D)
+{
+    uint32_t t = blockIdx.x * CHUNK + threadIdx.x;
+    TriRec rec;
+    rec.x0 = rec.y0 = rec.x1 = rec.y1 = 0;
+    rec.info = 0;
+    rec.slot = 0;
+    int cntIn = 0, cntRej = 0, cntClip = 0, cntVis = 0;
+    if(t < D.count)
+    {
+        cntIn = 1;
+        uint32_t i0 = fetch_index(D, 3 * t + 0), i1 = fetch_index(D, 3 * t + 1), i2 = fetch_index(D, 3 * t + 2);
+        bool ok = true;
+        if(D.indexType != SWGB_INDEX_TYPE_NONE)
+        {
+            if(i0 >= D.vertexCount || i1 >= D.vertexCount || i2 >= D.vertexCount)
+            {
+                atomicOr(D.error, ERR_INDEX_RANGE);
+                ok = false;
+            }
+        }
+        else
+        {
+            i0 = 3 * t + 0; i1 = 3 * t + 1; i2 = 3 * t + 2;
+        }
+        int visible = 0, clipped = 0;
+        if(ok)
+        {
+            float4 c0 = D.ptv[(size_t)i0 * 4], c1 = D.ptv[(size_t)i1 * 4], c2 = D.ptv[(size_t)i2 * 4];
+            float4 p0 = D.ptv[(size_t)i0 * 4 + 1], p1 = D.ptv[(size_t)i1 * 4 + 1], p2 = D.ptv[(size_t)i2 * 4 + 1];
+            int f0 = __float_as_int(p0.z), f1 = __float_as_int(p1.z), f2 = __float_as_int(p2.z);
+            int32_t X[MAX_POLY + 1], Y[MAX_POLY + 1];
+            X[0] = __float_as_int(p0.x); X[1] = __float_as_int(p1.x); X[2] = __float_as_int(p2.x);
+            Y[0] = __float_as_int(p0.y); Y[1] = __float_as_int(p1.y); Y[2] = __float_as_int(p2.y);
+            int n = 3;
+            // setupSolidTriangles trivial reject (src/Device/Renderer.cpp:749-765)
+            if((f0 & f1 & f2) == CLIP_FINITE)
+            {
+                int flagsOr = f0 | f1 | f2;
+                bool keep = true;
+                CVert P[MAX_POLY];
+                if(flagsOr != CLIP_FINITE)
+                {
+                    clipped = 1;
+                    P[0] = {c0.x, c0.y, c0.z, c0.w};
+                    P[1] = {c1.x, c1.y, c1.z, c1.w};
+                    P[2] = {c2.x, c2.y, c2.z, c2.w};
+                    n = clip_polygon(P, 3, flagsOr);
+                    keep = n >= 3;
+                }
+                if(keep)
+                {
+                    // Culling (SetupRoutine.cpp:73-120)
+                    float x0 = (float)X[0], x1 = (float)X[1], x2 = (float)X[2];
+                    float y0 = (float)Y[0], y1 = (float)Y[1], y2 = (float)Y[2];
+                    float A = ((y0 - y2) * x1 + (y2 - y1) * x0) + (y1 - y0) * x2;
+                    int32_t w0w1w2 = __float_as_int(c0.w) ^ __float_as_int(c1.w) ^ __float_as_int(c2.w);
+                    if(w0w1w2 < 0) A = -A;
+                    bool front = D.frontFace == SWGB_FRONT_FACE_COUNTER_CLOCKWISE ? (A >= 0.0f) : (A <= 0.0f);
+                    if((D.cullMode & SWGB_CULL_FRONT) && front) keep = false;
+                    if((D.cullMode & SWGB_CULL_BACK) && !front) keep = false;
+                    int dW = A > 0.0f ? 1 : 0;
+                    if(keep && clipped)
+                    {
+                        // reproject the clipped polygon (SetupRoutine.cpp:125-145)
+                        for(int i = 0; i < n; i++)
+                        {
+                            float w = P[i].w;
+                            float rhw = w != 0.0f ? 1.0f / w : 1.0f;
+                            X[i] = round_int(D.X0xF + (P[i].x * rhw) * D.WxF);
+                            Y[i] = round_int(D.Y0xF + (P[i].y * rhw) * D.HxF);
+                        }
+                    }
+                    if(keep)
+                    {
+                        int32_t yMin = Y[0], yMax = Y[0], xMinS = X[0], xMaxS = X[0];
+                        for(int i = 1; i < n; i++)
+                        {
+                            yMin = min(yMin, Y[i]); yMax = max(yMax, Y[i]);
+                            xMinS = min(xMinS, X[i]); xMaxS = max(xMaxS, X[i]);
+                        }
+                        yMin = max((yMin + 0xFF) >> 8, D.sy0);
+                        yMax = min((yMax + 0xFF) >> 8, D.sy1);
+                        if(yMin < yMax)
+                        {
+                            // Trim empty rows at the top and bottom (SetupRoutine.cpp:243-264)
+                            int32_t l, r;
+                            while(yMin < yMax)
+                            {
+                                span_at(D, X, Y, n, dW, yMin, l, r);
+                                if(l != r) break;
+                                yMin++;
+                            }
+                            while(yMax > yMin)
+                            {
+                                span_at(D, X, Y, n, dW, yMax - 1, l, r);
+                                if(l != r) break;
+                                yMax--;
+                            }
+                            if(yMin < yMax)
+                            {
+                                int32_t bx0 = max(D.sx0, (xMinS + 0xFF) >> 8);
+                                int32_t bx1 = min(D.sx1, (xMaxS + 0xFF) >> 8);
+                                visible = 1;
+                                rec.x0 = (int16_t)bx0; rec.x1 = (int16_t)max(bx1, bx0);
+                                rec.y0 = (int16_t)yMin; rec.y1 = (int16_t)yMax;
+                                rec.info = (uint32_t)n | ((uint32_t)dW << 5) | ((uint32_t)clipped << 6);
+                                if(clipped)
+                                {
+                                    uint32_t slot = atomicAdd(D.polyCount, 1u);
+                                    if(slot < D.polyCapacity)
+                                    {
+                                        rec.slot = slot;
+                                        for(int i = 0; i < n; i++) D.poly[(size_t)slot * MAX_POLY + i] = make_int2(X[i], Y[i]);
+                                    }
+                                    else
+                                    {
+                                        atomicOr(D.error, ERR_POLY_OVERFLOW);
+                                        visible = 0;
+                                        rec.info = 0;
+                                    }
+                                }
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        cntClip = clipped;
+        cntVis = visible;
+        cntRej = visible ? 0 : 1;
+    }
+    D.tris[t] = rec;  // capacity is a whole number of chunks
+    // chunk box + counters (block reduction)
+    __shared__ int sbox[4][CHUNK / 32];
+    __shared__ int scnt[4][CHUNK / 32];
+    bool has = rec.info != 0;
+    int bx0 = has ? rec.x0 : 0x7FFF, by0 = has ? rec.y0 : 0x7FFF;
+    int bx1 = has ? rec.x1 : -0x8000, by1 = has ? rec.y1 : -0x8000;
+    for(int o = 16; o > 0; o >>= 1)
+    {
+        bx0 = min(bx0, __shfl_xor_sync(0xFFFFFFFFu, bx0, o));
+        by0 = min(by0, __shfl_xor_sync(0xFFFFFFFFu, by0, o));
+        bx1 = max(bx1, __shfl_xor_sync(0xFFFFFFFFu, bx1, o));
+        by1 = max(by1, __shfl_xor_sync(0xFFFFFFFFu, by1, o));
+        cntIn += __shfl_xor_sync(0xFFFFFFFFu, cntIn, o);
+        cntRej += __shfl_xor_sync(0xFFFFFFFFu, cntRej, o);
+        cntClip += __shfl_xor_sync(0xFFFFFFFFu, cntClip, o);
+        cntVis += __shfl_xor_sync(0xFFFFFFFFu, cntVis, o);
+    }
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if(lane == 0)
+    {
+        sbox[0][warp] = bx0; sbox[1][warp] = by0; sbox[2][warp] = bx1; sbox[3][warp] = by1;
+        scnt[0][warp] = cntIn; scnt[1][warp] = cntRej; scnt[2][warp] = cntClip; scnt[3][warp] = cntVis;
+    }
+    __syncthreads();
+    if(threadIdx.x == 0)
+    {
+        for(int w = 1; w < CHUNK / 32; w++)
+        {
+            bx0 = min(bx0, sbox[0][w]); by0 = min(by0, sbox[1][w]);
+            bx1 = max(bx1, sbox[2][w]); by1 = max(by1, sbox[3][w]);
+            cntIn += scnt[0][w]; cntRej += scnt[1][w]; cntClip += scnt[2][w]; cntVis += scnt[3][w];
+        }
+        D.chunkBox[blockIdx.x] = make_short4((short)bx0, (short)by0, (short)bx1, (short)by1);
+        atomicAdd(&D.counters[0], (unsigned long long)cntIn);
+        atomicAdd(&D.counters[1], (unsigned long long)cntRej);
+        atomicAdd(&D.counters[2], (unsigned long long)cntClip);
+        atomicAdd(&D.counters[3], (unsigned long long)cntVis);
+    }
+}
+
+// ------------------------------------------------------------------------
+// SamplerCore 16-bit path for R8G8B8A8_UNORM (src/Pipeline/SamplerCore.cpp)
+// ------------------------------------------------------------------------
+
+// address() 16-bit (SamplerCore.cpp:2399-2435)
+__device__ __forceinline__ uint32_t address16(float uw, uint32_t mode)
+{
+    if(mode == SWGB_ADDRESS_CLAMP_TO_EDGE)
+    {
+        float c = rmin(rmax(uw, 0.0f), 65535.0f / 65536.0f);
+        return (uint32_t)trunc_int(c * 65536.0f) & 0xFFFFu;
+    }
+    if(mode == SWGB_ADDRESS_MIRRORED_REPEAT)
+    {
+        int32_t convert = trunc_int(uw * 65536.0f);
+        int32_t mirror = (int32_t)((uint32_t)convert << 15) >> 31;
+        convert ^= mirror;
+        return (uint32_t)convert & 0xFFFFu;
+    }
+    return (uint32_t)trunc_int(uw * 65536.0f) & 0xFFFFu;
+}
+
+// offsetSample (SamplerCore.cpp:278-313)
+__device__ __forceinline__ uint32_t offset_sample(uint32_t uvw, uint32_t half, bool wrap, int count)
+{
+    if(wrap) return (count < 0 ? uvw - half : uvw + half) & 0xFFFFu;
+    return count < 0 ? subsat_u16(uvw, half) : addsat_u16(uvw, half);
+}
+
+// computeIndices + 8-bit unpack (SamplerCore.cpp:1593-1643,1747-1788): returns the texel as 4 bytes.
+__device__ __forceinline__ uint32_t texel_rgba8(const TexLevel &lv, uint32_t u, uint32_t v)
+{
+    uint32_t xi = mulhi_u16(u, lv.w);
+    uint32_t yi = mulhi_u16(v, lv.h);
+    int32_t index = (int32_t)(int16_t)xi + (int32_t)(int16_t)yi * (int32_t)(int16_t)lv.pitch;  // pmaddwd
+    return __ldg((const uint32_t *)lv.buf + (uint32_t)index);
+}
+
+// sampleQuad2D for one lane, 16-bit channel values c << 8 (SamplerCore.cpp:668-909).
+__device__ __forceinline__ void sample_quad_2d(const DrawParams &D, float u, float v, float lod, int second, uint32_t out[4])
+{
+    int ilod = D.mipLinear ? trunc_int(lod) : round_int(lod);  // selectMipmap (:2357-2379)
+    int li = ilod + second;
+    li = li < 0 ? 0 : (li > D.levelCount - 1 ? D.levelCount - 1 : li);
+    const TexLevel &lv = D.lv[li];
+    uint32_t uu = address16(u, D.addrU);
+    uint32_t vv = address16(v, D.addrV);
+    if(!D.texLinear)
+    {
+        uint32_t t = texel_rgba8(lv, uu, vv);
+#pragma unroll
+        for(int c = 0; c < 4; c++) out[c] = ((t >> (8 * c)) & 0xFFu) << 8;
+        return;
+    }
+    bool wu = D.addrU == SWGB_ADDRESS_REPEAT, wv = D.addrV == SWGB_ADDRESS_REPEAT;
+    uint32_t u0 = offset_sample(uu, lv.uHalf, wu, -1), v0 = offset_sample(vv, lv.vHalf, wv, -1);
+    uint32_t u1 = offset_sample(uu, lv.uHalf, wu, +1), v1 = offset_sample(vv, lv.vHalf, wv, +1);
+    uint32_t t00 = texel_rgba8(lv, u0, v0), t10 = texel_rgba8(lv, u1, v0);
+    uint32_t t01 = texel_rgba8(lv, u0, v1), t11 = texel_rgba8(lv, u1, v1);
+    // bilinearInterpolate, unsigned 8-bit components (:516-575)
+    uint32_t f0u = (u0 * lv.w) & 0xFFFFu, f0v = (v0 * lv.h) & 0xFFFFu;
+    uint32_t f1u = (~f0u) & 0xFFFFu, f1v = (~f0v) & 0xFFFFu;
+    uint32_t f0u0v = mulhi_u16(f0u, f0v), f1u0v = mulhi_u16(f1u, f0v);
+    uint32_t f0u1v = mulhi_u16(f0u, f1v), f1u1v = mulhi_u16(f1u, f1v);
+#pragma unroll
+    for(int c = 0; c < 4; c++)
+    {
+        uint32_t a = mulhi_u16(((t00 >> (8 * c)) & 0xFFu) << 8, f1u1v);
+        uint32_t b = mulhi_u16(((t10 >> (8 * c)) & 0xFFu) << 8, f0u1v);
+        uint32_t e = mulhi_u16(((t01 >> (8 * c)) & 0xFFu) << 8, f1u0v);
+        uint32_t g = mulhi_u16(((t11 >> (8 * c)) & 0xFFu) << 8, f0u0v);
+        out[c] = (((a + b) & 0xFFFFu) + ((e + g) & 0xFFFFu)) & 0xFFFFu;
+    }
+}
+
+// sampleTexture128 on the 16-bit path (SamplerCore.cpp:59-253) with the implicit
+// LOD of computeLod2D (:1376-1422); result scaled by 1 / 0xFF00.
+__device__ void sample_texture_quad(const DrawParams &D, const float u[4], const float v[4], float out[4][4])
+{
+    float lod;
+    if(D.minLod == D.maxLod)
+        lod = D.minLod;
+    else
+    {
+        float dudx = u[1] - u[0], dudy = u[2] - u[0];
+        float dvdx = v[1] - v[0], dvdy = v[2] - v[0];
+        float a = dudx * D.texW, b = dudy * D.texW, c = dvdx * D.texH, e = dvdy * D.texH;
+        a = a * a; b = b * b; c = c * c; e = e * e;
+        lod = log2sqrt(rmax(a + c, b + e));
+        lod = lod + D.lodBias;
+        lod = rmax(lod, D.minLod);
+        lod = rmin(lod, D.maxLod);
+    }
+    const float scale = 1.0f / 65280.0f;
+    uint32_t utri = 0;
+    if(D.mipLinear) utri = (uint32_t)trunc_int(lod * 65536.0f) & 0xFFFFu;
+#pragma unroll
+    for(int lane = 0; lane < 4; lane++)
+    {
+        uint32_t c[4];
+        sample_quad_2d(D, u[lane], v[lane], lod, 0, c);
+        if(D.mipLinear)  // sampleFilter trilinear blend (:324-379)
+        {
+            uint32_t cc[4];
+            sample_quad_2d(D, u[lane], v[lane], lod, 1, cc);
+#pragma unroll
+            for(int k = 0; k < 4; k++) c[k] = (mulhi_u16(c[k], (~utri) & 0xFFFFu) + mulhi_u16(cc[k], utri)) & 0xFFFFu;
+        }
+#pragma unroll
+        for(int k = 0; k < 4; k++) out[lane][k] = __uint2float_rn(c[k]) * scale;
+    }
+}
+
+// ------------------------------------------------------------------------
+// Raster stage
+// ------------------------------------------------------------------------
+
+__device__ __forceinline__ float blend_factor(uint32_t f, const float *src, const float *dst, int comp)
+{
+    bool alpha = comp == 3;
+    switch(f)
+    {
+    case SWGB_BLEND_ZERO: return 0.0f;
+    case SWGB_BLEND_ONE: return 1.0f;
+    case SWGB_BLEND_SRC_COLOR: return alpha ? src[3] : src[comp];
+    case SWGB_BLEND_ONE_MINUS_SRC_COLOR: return 1.0f - (alpha ? src[3] : src[comp]);
+    case SWGB_BLEND_DST_COLOR: return alpha ? dst[3] : dst[comp];
+    case SWGB_BLEND_ONE_MINUS_DST_COLOR: return 1.0f - (alpha ? dst[3] : dst[comp]);
+    case SWGB_BLEND_SRC_ALPHA: return src[3];
+    case SWGB_BLEND_ONE_MINUS_SRC_ALPHA: return 1.0f - src[3];
+    case SWGB_BLEND_DST_ALPHA: return dst[3];
+    case SWGB_BLEND_ONE_MINUS_DST_ALPHA: return 1.0f - dst[3];
+    default: return 0.0f;
+    }
+}
+
+__device__ __forceinline__ float blend_op(uint32_t op, float s, float sf, float d, float df)
+{
+    switch(op)
+    {
+    case SWGB_BLEND_OP_ADD: return s * sf + d * df;
+    case SWGB_BLEND_OP_SUBTRACT: return s * sf - d * df;
+    case SWGB_BLEND_OP_REVERSE_SUBTRACT: return d * df - s * sf;
+    case SWGB_BLEND_OP_MIN: return rmin(s, d);
+    case SWGB_BLEND_OP_MAX: return rmax(s, d);
+    case OP_SRC_EXT: return s;
+    case OP_DST_EXT: return d;
+    case OP_ZERO_EXT: return 0.0f;
+    default: return s;
+    }
+}
+
+__device__ __forceinline__ bool depth_pass(uint32_t op, float zb, float z)
+{
+    switch(op)
+    {
+    case SWGB_COMPARE_NEVER: return false;
+    case SWGB_COMPARE_LESS: return !(zb <= z);
+    case SWGB_COMPARE_EQUAL: return zb == z;
+    case SWGB_COMPARE_LESS_OR_EQUAL: return !(zb < z);
+    case SWGB_COMPARE_GREATER: return zb < z;
+    case SWGB_COMPARE_NOT_EQUAL: return !(zb == z);
+    case SWGB_COMPARE_GREATER_OR_EQUAL: return zb <= z;
+    default: return true;
+    }
+}
+
+// Number of per-triangle plane-equation floats staged for a batch:
+// x0, y0, z(A,B,C), w(A,B,C), V[k](A,B,C).
+constexpr int PLANES = 8 + 3 * MAXV;
+
+struct RasterShared {
+    float depth[BIN * BIN];
+    uint32_t color[BIN * BIN];
+    float plane[PLANES][BATCH];
+    uint32_t span[BATCH][BIN];        // left | right << 16 per bin row (0 = empty)
+    int16_t qx0[BATCH][BIN / 2];      // first quad x per quad row
+    uint16_t qpre[BATCH][BIN / 2 + 1];
+    int triStart[BATCH + 1];
+    int chunkList[RASTER_THREADS];
+    int triList[CHUNK];
+    int claim[BIN_QUADS];
+    int warpCount[RASTER_THREADS / 32];
+};
+
+// Block-wide ordered compaction: returns this thread's slot among the
+// flagged threads (thread order) and the flagged total.
+__device__ __forceinline__ int ordered_compact(bool flag, int *warpCount, int &total)
+{
+    unsigned b = __ballot_sync(0xFFFFFFFFu, flag);
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if(lane == 0) warpCount[warp] = __popc(b);
+    __syncthreads();
+    int before = 0;
+    total = 0;
+#pragma unroll
+    for(int w = 0; w < RASTER_THREADS / 32; w++)
+    {
+        int c = warpCount[w];
+        if(w < warp) before += c;
+        total += c;
+    }
+    __syncthreads();
+    return flag ? before + __popc(b & ((1u << lane) - 1u)) : -1;
+}
+
+__device__ __forceinline__ float vary(const float4 &a, const float4 &b, int k)
+{
+    // varying k of a post-transform vertex: float4[2].yzw then float4[3].xyzw
+    switch(k)
+    {
+    case 0: return a.y;
+    case 1: return a.z;
+    case 2: return a.w;
+    case 3: return b.x;
+    case 4: return b.y;
+    case 5: return b.z;
+    default: return b.w;
+    }
+}
+
+// R1: setup of one batch triangle -- spans of the bin rows (reference DDA),
+// quad rows, plane equations (SetupRoutine.cpp:270-548).  Returns its quads.
+__device__ int setup_batch_triangle(const DrawParams &D, RasterShared &S, int ti, uint32_t tIdx, int bx0, int by0)
+{
+    TriRec r = D.tris[tIdx];
+    int n = r.info & 31, dW = (r.info >> 5) & 1;
+    uint32_t iv[3];
+    if(D.indexType == SWGB_INDEX_TYPE_NONE) { iv[0] = 3 * tIdx; iv[1] = 3 * tIdx + 1; iv[2] = 3 * tIdx + 2; }
+    else { iv[0] = fetch_index(D, 3 * tIdx); iv[1] = fetch_index(D, 3 * tIdx + 1); iv[2] = fetch_index(D, 3 * tIdx + 2); }
+    float4 V0[3], V1[3], V2[3], V3[3];
+#pragma unroll
+    for(int k = 0; k < 3; k++)
+    {
+        const float4 *p = D.ptv + (size_t)iv[k] * 4;
+        V0[k] = p[0]; V1[k] = p[1]; V2[k] = p[2]; V3[k] = p[3];
+    }
+    int32_t X[MAX_POLY], Y[MAX_POLY];
+    if(r.info & 64)
+    {
+        for(int i = 0; i < n; i++)
+        {
+            int2 q = D.poly[(size_t)r.slot * MAX_POLY + i];
+            X[i] = q.x; Y[i] = q.y;
+        }
+    }
+    else
+    {
+#pragma unroll
+        for(int k = 0; k < 3; k++) { X[k] = __float_as_int(V1[k].x); Y[k] = __float_as_int(V1[k].y); }
+    }
+    // spans of the bin rows inside [yMin, yMax); the last edge writing a row wins
+    const int rowLo = max((int)r.y0, by0), rowHi = min((int)r.y1, by0 + BIN);
+    for(int y = 0; y < BIN; y++) S.span[ti][y] = 0u;
+    for(int i = 0; i < n; i++)
+    {
+        int ia = i + 1 - dW, ib = i + dW;
+        ia = ia == n ? 0 : ia;
+        ib = ib == n ? 0 : ib;
+        EdgeDDA e;
+        if(!edge_setup(D, X[ia], Y[ia], X[ib], Y[ib], e)) continue;
+        int ys = max(e.yMin, rowLo), ye = min(e.yMax, rowHi);
+        if(ys >= ye) continue;
+        int32_t dd;
+        int32_t x = edge_x_at(e, ys, &dd);
+        for(int y = ys; y < ye; y++)
+        {
+            uint32_t xc = (uint32_t)clamp_x(D, x);
+            uint32_t s = S.span[ti][y - by0];
+            S.span[ti][y - by0] = e.right ? ((s & 0xFFFFu) | (xc << 16)) : ((s & 0xFFFF0000u) | xc);
+            x += e.Q;
+            dd += e.R;
+            int32_t of = (-dd) >> 31;
+            dd -= e.D & of;
+            x -= of;
+        }
+    }
+    // quad rows: x range of the row pair (QuadRasterizer.cpp:96-123), clipped to the bin
+    int pre = 0;
+    for(int qr = 0; qr < BIN / 2; qr++)
+    {
+        S.qpre[ti][qr] = (uint16_t)pre;
+        uint32_t s0 = S.span[ti][2 * qr], s1 = S.span[ti][2 * qr + 1];
+        int l0 = s0 & 0xFFFF, r0 = s0 >> 16, l1 = s1 & 0xFFFF, r1 = s1 >> 16;
+        bool e0 = l0 >= r0, e1 = l1 >= r1;
+        int xa = 0, cnt = 0;
+        if(!(e0 && e1))
+        {
+            xa = e0 ? l1 : (e1 ? l0 : min(l0, l1));
+            int xb = e0 ? r1 : (e1 ? r0 : max(r0, r1));
+            xa = max(xa & ~1, bx0);
+            xb = min(xb, bx0 + BIN);
+            cnt = xb > xa ? (xb - xa + 1) >> 1 : 0;
+        }
+        S.qx0[ti][qr] = (int16_t)xa;
+        pre += cnt;
+    }
+    S.qpre[ti][BIN / 2] = (uint16_t)pre;
+
+    // sort by minimum y, then maximum w (SetupRoutine.cpp:270-294)
+    int o0 = 0, o1 = 1, o2 = 2, t;
+    {
+        float y0 = V0[0].y, y1 = V0[1].y, y2 = V0[2].y;
+        float ym = rmin(rmin(y0, y1), y2);
+        if(ym == y1) { t = o0; o0 = o1; o1 = o2; o2 = t; }
+        if(ym == y2) { t = o2; o2 = o1; o1 = o0; o0 = t; }
+    }
+    {
+        float w0 = V0[o0].w, w1 = V0[o1].w, w2 = V0[o2].w;
+        float wm = rmax(rmax(w0, w1), w2);
+        if(wm == w1) { t = o0; o0 = o1; o1 = o2; o2 = t; }
+        if(wm == w2) { t = o2; o2 = o1; o1 = o0; o0 = t; }
+    }
+    const float w1 = V0[o1].w, w2 = V0[o2].w;
+    const float rhw0 = V2[o0].x;
+    int32_t X0 = __float_as_int(V1[o0].x), X1 = __float_as_int(V1[o1].x), X2 = __float_as_int(V1[o2].x);
+    int32_t Y0 = __float_as_int(V1[o0].y), Y1 = __float_as_int(V1[o1].y), Y2 = __float_as_int(V1[o2].y);
+    const float inv = 1.0f / 256.0f;
+    S.plane[0][ti] = (float)X0 * inv;
+    S.plane[1][ti] = (float)Y0 * inv;
+    X1 -= X0; Y1 -= Y0; X2 -= X0; Y2 -= Y0;
+    float x1 = (w1 * inv) * (float)X1, y1 = (w1 * inv) * (float)Y1;
+    float x2 = (w2 * inv) * (float)X2, y2 = (w2 * inv) * (float)Y2;
+    float a = x1 * y2 - x2 * y1;
+    float M0x = 0.0f, M0y = 0.0f, M1x = 0.0f, M1y = 0.0f, M2x = 0.0f, M2y = 0.0f;
+    const float M0z = rhw0, M1z = 0.0f, M2z = 0.0f;
+    if(a != 0.0f)
+    {
+        float A = 1.0f / a;
+        float Dd = A * rhw0;
+        M0x = (y1 * w2 - y2 * w1) * Dd;
+        M0y = (x2 * w1 - x1 * w2) * Dd;
+        M1x = y2 * A;
+        M1y = (-x2) * A;
+        M2x = (-y1) * A;
+        M2y = x1 * A;
+    }
+    S.plane[5][ti] = (M0x + M1x) + M2x;
+    S.plane[6][ti] = (M0y + M1y) + M2y;
+    S.plane[7][ti] = (M0z + M1z) + M2z;
+    if(D.depthTest)
+    {
+        float z0 = V1[o0].w, z1 = V1[o1].w - z0, z2 = V1[o2].w - z0;
+        float fx1 = (float)X1 * inv, fy1 = (float)Y1 * inv;
+        float fx2 = (float)X2 * inv, fy2 = (float)Y2 * inv;
+        float Dz = D.depthRange / (fx1 * fy2 - fx2 * fy1);
+        S.plane[2][ti] = (fy2 * z1 - fy1 * z2) * Dz;
+        S.plane[3][ti] = (fx1 * z2 - fx2 * z1) * Dz;
+        S.plane[4][ti] = z0 * D.depthRange + D.depthNear;
+    }
+    for(int k = 0; k < D.nv; k++)
+    {
+        float i0 = vary(V2[o0], V3[o0], k), i1 = vary(V2[o1], V3[o1], k), i2 = vary(V2[o2], V3[o2], k);
+        S.plane[8 + 3 * k + 0][ti] = (i0 * M0x + i1 * M1x) + i2 * M2x;
+        S.plane[8 + 3 * k + 1][ti] = (i0 * M0y + i1 * M1y) + i2 * M2y;
+        S.plane[8 + 3 * k + 2][ti] = (i0 * M0z + i1 * M1z) + i2 * M2z;
+    }
+    return pre;
+}
+
+// R2: interpolation + fixed fragment shader of one 2x2 quad
+// (PixelRoutine::quad :124-261, PixelProgram::executeShader/clampColor).
+__device__ __forceinline__ void shade_quad(const DrawParams &D, const RasterShared &S, int ti, int qx, int y, float zq[4], float col[4][4])
+{
+    const float x0p = S.plane[0][ti], y0p = S.plane[1][ti];
+    float xF[4], yF[4];
+#pragma unroll
+    for(int i = 0; i < 4; i++)
+    {
+        xF[i] = ((float)qx + (float)(i & 1)) - x0p;
+        yF[i] = ((float)y + (float)(i >> 1)) - y0p;
+    }
+    if(D.depthTest)
+    {
+        const float zA = S.plane[2][ti], zB = S.plane[3][ti], zC = S.plane[4][ti];
+#pragma unroll
+        for(int i = 0; i < 4; i++)
+        {
+            float z = mul_add(xF[i], zA, zC + yF[i] * zB);
+            zq[i] = rmin(rmax(z, D.minDepthClamp), D.maxDepthClamp);  // clampDepth
+        }
+    }
+    float rhw[4];
+    {
+        const float wA = S.plane[5][ti], wB = S.plane[6][ti], wC = S.plane[7][ti];
+#pragma unroll
+        for(int i = 0; i < 4; i++) rhw[i] = 1.0f / mul_add(xF[i], wA, wC + yF[i] * wB);
+    }
+    float vin[MAXV][4];
+#pragma unroll
+    for(int k = 0; k < MAXV; k++)
+    {
+        if(k >= D.nv) break;
+        const float A = S.plane[8 + 3 * k][ti], B = S.plane[9 + 3 * k][ti], C = S.plane[10 + 3 * k][ti];
+#pragma unroll
+        for(int i = 0; i < 4; i++) vin[k][i] = mul_add(xF[i], A, C + yF[i] * B) * rhw[i];
+    }
+    if(D.fs == SWGB_FS_TEX_X_VCOLOR)
+    {
+        float tex[4][4];
+        sample_texture_quad(D, vin[4], vin[5], tex);
+#pragma unroll
+        for(int i = 0; i < 4; i++)
+#pragma unroll
+            for(int k = 0; k < 4; k++) col[i][k] = tex[i][k] * vin[k][i];
+    }
+    else
+    {
+#pragma unroll
+        for(int i = 0; i < 4; i++)
+#pragma unroll
+            for(int k = 0; k < 4; k++) col[i][k] = vin[k][i];
+    }
+#pragma unroll
+    for(int i = 0; i < 4; i++)
+#pragma unroll
+        for(int k = 0; k < 4; k++) col[i][k] = rmin(rmax(col[i][k], 0.0f), 1.0f);  // UNORM target
+}
+
+// R3: depth test/write, blend and RGBA8 write of the covered lanes of one quad
+// into the staged bin (PixelRoutine.cpp:494-574,660-685,1653-1961,1975-1993,2609-2650).
+__device__ __forceinline__ void rop_quad(const DrawParams &D, RasterShared &S, int lx, int ly, int cMask, const float zq[4],
+                                         const float col[4][4], unsigned long long &nTested, unsigned long long &nPassed)
+{
+#pragma unroll
+    for(int i = 0; i < 4; i++)
+    {
+        if(!(cMask & (1 << i))) continue;
+        int idx = (ly + (i >> 1)) * BIN + lx + (i & 1);
+        if(D.depthTest)
+        {
+            nTested++;
+            if(!depth_pass(D.compareOp, S.depth[idx], zq[i])) continue;
+            if(D.depthWrite) S.depth[idx] = zq[i];
+        }
+        nPassed++;
+        float out[4];
+        uint32_t old = S.color[idx];
+        if(D.blend)
+        {
+            float dst[4];
+#pragma unroll
+            for(int c = 0; c < 4; c++) dst[c] = (float)(((old >> (8 * c)) & 0xFFu) * 257u) * (1.0f / 0xFFFF);
+            float sf[4], df[4];
+#pragma unroll
+            for(int c = 0; c < 3; c++)
+            {
+                sf[c] = blend_factor(D.srcC, col[i], dst, c);
+                df[c] = blend_factor(D.dstC, col[i], dst, c);
+            }
+            sf[3] = blend_factor(D.srcA, col[i], dst, 3);
+            df[3] = blend_factor(D.dstA, col[i], dst, 3);
+#pragma unroll
+            for(int c = 0; c < 3; c++) out[c] = blend_op(D.opC, col[i][c], sf[c], dst[c], df[c]);
+            out[3] = blend_op(D.opA, col[i][3], sf[3], dst[3], df[3]);
+        }
+        else
+        {
+#pragma unroll
+            for(int c = 0; c < 4; c++) out[c] = col[i][c];
+        }
+        uint32_t packed = old;
+#pragma unroll
+        for(int c = 0; c < 4; c++)
+        {
+            float v = rmin(rmax(out[c], 0.0f), 1.0f);
+            int32_t r = round_int(v * 255.0f);
+            int32_t s16 = (int32_t)(int16_t)r;
+            uint32_t b = s16 < 0 ? 0u : (s16 > 255 ? 255u : (uint32_t)s16);  // PackUnsigned
+            if(D.writeMask & (1u << c)) packed = (packed & ~(0xFFu << (8 * c))) | (b << (8 * c));
+        }
+        S.color[idx] = packed;
+    }
+}
+
+__global__ void __launch_bounds__(RASTER_THREADS) k_raster(const __grid_constant__ DrawParams D)
+{
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    RasterShared &S = *reinterpret_cast<RasterShared *>(smem_raw);
+    const int tid = threadIdx.x;
+    const int bx0 = D.binX0 + (int)blockIdx.x * BIN;
+    const int by0 = D.binY0 + (int)blockIdx.y * BIN;
+
+    // ---- stage the bin's depth and colour in shared memory (16-byte rows) ----
+    for(int i = tid; i < BIN * BIN / 4; i += RASTER_THREADS)
+    {
+        int ly = i / (BIN / 4), lx = (i % (BIN / 4)) * 4;
+        int px = bx0 + lx, py = by0 + ly;
+        float4 dz = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+        uint4 cc = make_uint4(0, 0, 0, 0);
+        if(py < D.sy1 && px < D.sx1)
+        {
+            const uint8_t *drow = D.depth + (size_t)py * D.depthPitch;
+            const uint8_t *crow = D.color + (size_t)py * D.colorPitch;
+            if(D.vec16 && px + 4 <= D.sx1)
+            {
+                if(D.depthTest) dz = *(const float4 *)(drow + (size_t)px * 4);
+                cc = *(const uint4 *)(crow + (size_t)px * 4);
+            }
+            else
+            {
+                float dv[4] = {1.0f, 1.0f, 1.0f, 1.0f};
+                uint32_t cv[4] = {0, 0, 0, 0};
+                for(int k = 0; k < 4 && px + k < D.sx1; k++)
+                {
+                    if(D.depthTest) dv[k] = *(const float *)(drow + (size_t)(px + k) * 4);
+                    cv[k] = *(const uint32_t *)(crow + (size_t)(px + k) * 4);
+                }
+                dz = make_float4(dv[0], dv[1], dv[2], dv[3]);
+                cc = make_uint4(cv[0], cv[1], cv[2], cv[3]);
+            }
+        }
+        *(float4 *)&S.depth[ly * BIN + lx] = dz;
+        *(uint4 *)&S.color[ly * BIN + lx] = cc;
+    }
+    for(int i = tid; i < BIN_QUADS; i += RASTER_THREADS) S.claim[i] = 0x7FFFFFFF;
+    __syncthreads();
+
+    unsigned long long nQuads = 0, nTested = 0, nPassed = 0;
+
+    // ---- chunks in primitive order ----------------------------------------
+    for(int cbase = 0; cbase < D.nchunks; cbase += RASTER_THREADS)
+    {
+        int c = cbase + tid;
+        bool hit = false;
+        if(c < D.nchunks)
+        {
+            short4 b = D.chunkBox[c];
+            hit = b.x < b.z && b.x < bx0 + BIN && b.z > bx0 && b.y < by0 + BIN && b.w > by0;
+        }
+        int nHit;
+        int slot = ordered_compact(hit, S.warpCount, nHit);
+        if(hit) S.chunkList[slot] = c;
+        __syncthreads();
+        for(int h = 0; h < nHit; h++)
+        {
+            const int chunk = S.chunkList[h];
+            const uint32_t tri = (uint32_t)chunk * CHUNK + tid;
+            bool th = false;
+            if(tri < D.count)
+            {
+                TriRec r = D.tris[tri];
+                th = r.info != 0 && r.x0 < bx0 + BIN && r.x1 > bx0 && r.y0 < by0 + BIN && r.y1 > by0;
+            }
+            int nTri;
+            int ts = ordered_compact(th, S.warpCount, nTri);
+            if(th) S.triList[ts] = (int)tri;
+            __syncthreads();
+            for(int b0 = 0; b0 < nTri; b0 += BATCH)
+            {
+                const int nb = min(BATCH, nTri - b0);
+                int myQuads = 0;
+                if(tid < nb) myQuads = setup_batch_triangle(D, S, tid, (uint32_t)S.triList[b0 + tid], bx0, by0);
+                // exclusive scan of quad counts (primitive order)
+                {
+                    int lane = tid & 31, warp = tid >> 5;
+                    int v = myQuads;
+#pragma unroll
+                    for(int o = 1; o < 32; o <<= 1)
+                    {
+                        int u = __shfl_up_sync(0xFFFFFFFFu, v, o);
+                        if(lane >= o) v += u;
+                    }
+                    if(lane == 31) S.warpCount[warp] = v;
+                    __syncthreads();
+                    int before = 0;
+                    for(int w = 0; w < warp; w++) before += S.warpCount[w];
+                    if(tid < nb) S.triStart[tid] = before + v - myQuads;
+                    if(tid == RASTER_THREADS - 1) S.triStart[BATCH] = before + v;
+                    __syncthreads();
+                }
+                const int totalQuads = S.triStart[BATCH];
+                for(int f0 = 0; f0 < totalQuads; f0 += RASTER_THREADS)
+                {
+                    const int f = f0 + tid;
+                    int cMask = 0, lx = 0, ly = 0;
+                    float zq[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+                    float col[4][4];
+                    if(f < totalQuads)
+                    {
+                        int lo = 0, hi = nb - 1;
+                        while(lo < hi)
+                        {
+                            int mid = (lo + hi + 1) >> 1;
+                            if(S.triStart[mid] <= f) lo = mid; else hi = mid - 1;
+                        }
+                        const int ti = lo;
+                        const int local = f - S.triStart[ti];
+                        int qr = 0;
+                        while(qr < BIN / 2 - 1 && (int)S.qpre[ti][qr + 1] <= local) qr++;
+                        const int qx = S.qx0[ti][qr] + 2 * (local - (int)S.qpre[ti][qr]);
+                        const int y = by0 + 2 * qr;
+                        uint32_t s0 = S.span[ti][2 * qr], s1 = S.span[ti][2 * qr + 1];
+                        int l0 = s0 & 0xFFFF, r0 = s0 >> 16, l1 = s1 & 0xFFFF, r1 = s1 >> 16;
+                        // per-lane coverage: left <= x < right (QuadRasterizer.cpp:184-209)
+                        if(qx >= l0 && qx < r0) cMask |= 1;
+                        if(qx + 1 >= l0 && qx + 1 < r0) cMask |= 2;
+                        if(qx >= l1 && qx < r1) cMask |= 4;
+                        if(qx + 1 >= l1 && qx + 1 < r1) cMask |= 8;
+                        lx = qx - bx0;
+                        ly = 2 * qr;
+                        if(cMask)
+                        {
+                            nQuads++;
+                            shade_quad(D, S, ti, qx, y, zq, col);
+                        }
+                    }
+                    // ordered resolve: per quad, fragments apply in primitive order
+                    const int qIndex = (ly >> 1) * (BIN / 2) + (lx >> 1);
+                    bool pending = cMask != 0;
+                    for(;;)
+                    {
+                        if(pending) atomicMin(&S.claim[qIndex], f);
+                        __syncthreads();
+                        if(pending && S.claim[qIndex] == f)
+                        {
+                            rop_quad(D, S, lx, ly, cMask, zq, col, nTested, nPassed);
+                            S.claim[qIndex] = 0x7FFFFFFF;
+                            pending = false;
+                        }
+                        if(!__syncthreads_or(pending)) break;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        __syncthreads();
+    }
+
+    // ---- write the bin back ------------------------------------------------
+    for(int i = tid; i < BIN * BIN / 4; i += RASTER_THREADS)
+    {
+        int ly = i / (BIN / 4), lx = (i % (BIN / 4)) * 4;
+        int px = bx0 + lx, py = by0 + ly;
+        if(py >= D.sy1 || px >= D.sx1 || px < D.sx0 || py < D.sy0) continue;
+        uint8_t *drow = D.depth + (size_t)py * D.depthPitch;
+        uint8_t *crow = D.color + (size_t)py * D.colorPitch;
+        if(D.vec16 && px + 4 <= D.sx1)
+        {
+            if(D.depthWrite) *(float4 *)(drow + (size_t)px * 4) = *(const float4 *)&S.depth[ly * BIN + lx];
+            *(uint4 *)(crow + (size_t)px * 4) = *(const uint4 *)&S.color[ly * BIN + lx];
+        }
+        else
+        {
+            for(int k = 0; k < 4 && px + k < D.sx1; k++)
+            {
+                if(D.depthWrite) *(float *)(drow + (size_t)(px + k) * 4) = S.depth[ly * BIN + lx + k];
+                *(uint32_t *)(crow + (size_t)(px + k) * 4) = S.color[ly * BIN + lx + k];
+            }
+        }
+    }
+
+    // ---- counters ----------------------------------------------------------
+    for(int o = 16; o > 0; o >>= 1)
+    {
+        nQuads += __shfl_xor_sync(0xFFFFFFFFu, nQuads, o);
+        nTested += __shfl_xor_sync(0xFFFFFFFFu, nTested, o);
+        nPassed += __shfl_xor_sync(0xFFFFFFFFu, nPassed, o);
+    }
+    if((tid & 31) == 0 && (nQuads | nTested | nPassed))
+    {
+        atomicAdd(&D.counters[4], nQuads);
+        atomicAdd(&D.counters[5], nTested);
+        atomicAdd(&D.counters[6], nPassed);
+    }
+}
+
+}  // namespace
+
+// ==========================================================================
+// Host side: context, state baking, C-ABI
+// ==========================================================================
+
+struct swgb_ctx {
+    int device;
+    cudaStream_t stream;
+    bool ownStream;
+    float4 *ptv;
+    size_t ptvCap;
+    TriRec *tris;
+    size_t trisCap;
+    short4 *chunkBox;
+    size_t chunkCap;
+    int2 *poly;
+    size_t polyCap;
+    uint32_t *polyCount;
+    unsigned long long *counters;
+    int *error;
+    uint64_t launches;
+    bool rasterAttr;
+};
+
+namespace {
+
+thread_local std::string g_error;
+
+swgb_status set_error(swgb_status s, const char *msg)
+{
+    g_error = msg;
+    return s;
+}
+
+swgb_status cuda_check(cudaError_t e, const char *what)
+{
+    if(e == cudaSuccess) return SWGB_OK;
+    g_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? SWGB_OOM : SWGB_DEVICE_ERROR;
+}
+
+template<typename T>
+swgb_status ensure(T *&ptr, size_t &cap, size_t need, const char *what)
+{
+    if(need <= cap && ptr) return SWGB_OK;
+    if(ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+    size_t n = need < 1 ? 1 : need;
+    swgb_status s = cuda_check(cudaMalloc((void **)&ptr, n * sizeof(T)), what);
+    if(s != SWGB_OK) return s;
+    cap = n;
+    return SWGB_OK;
+}
+
+uint32_t simplify_op(uint32_t op, uint32_t sf, uint32_t df)
+{
+    // vk::FragmentOutputInterfaceState::blendOperation (src/Device/Context.cpp:1181-1270)
+    switch(op)
+    {
+    case SWGB_BLEND_OP_ADD:
+        if(sf == SWGB_BLEND_ZERO)
+        {
+            if(df == SWGB_BLEND_ZERO) return OP_ZERO_EXT;
+            if(df == SWGB_BLEND_ONE) return OP_DST_EXT;
+        }
+        else if(sf == SWGB_BLEND_ONE && df == SWGB_BLEND_ZERO)
+            return OP_SRC_EXT;
+        break;
+    case SWGB_BLEND_OP_SUBTRACT:
+        if(sf == SWGB_BLEND_ZERO) return OP_ZERO_EXT;  // UNORM target: negative clamps to zero
+        if(sf == SWGB_BLEND_ONE && df == SWGB_BLEND_ZERO) return OP_SRC_EXT;
+        break;
+    case SWGB_BLEND_OP_REVERSE_SUBTRACT:
+        if(sf == SWGB_BLEND_ZERO)
+        {
+            if(df == SWGB_BLEND_ZERO) return OP_ZERO_EXT;
+            if(df == SWGB_BLEND_ONE) return OP_DST_EXT;
+        }
+        break;
+    default: break;
+    }
+    return op;
+}
+
+// Validates the state and bakes DrawParams (Renderer::draw, src/Device/Renderer.cpp:183-490).
+swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawParams &D)
+{
+    memset(&D, 0, sizeof(D));
+    if(st->precision_profile != SWGB_PRECISION_CMAKE) return set_error(SWGB_UNSUPPORTED_STATE, "only the CMake precision profile is implemented");
+    if(st->topology != SWGB_TOPOLOGY_TRIANGLE_LIST) return set_error(SWGB_UNSUPPORTED_STATE, "topology");
+    if(st->sample_count != 1) return set_error(SWGB_UNSUPPORTED_STATE, "sample_count");
+    if(st->vertex_shader != SWGB_VS_MVP_PASSTHROUGH) return set_error(SWGB_UNSUPPORTED_STATE, "vertex_shader");
+    if(st->fragment_shader != SWGB_FS_VCOLOR && st->fragment_shader != SWGB_FS_TEX_X_VCOLOR) return set_error(SWGB_UNSUPPORTED_STATE, "fragment_shader");
+    if(st->depth_clamp_enable || st->depth_bias_constant != 0.0f || st->depth_bias_slope != 0.0f) return set_error(SWGB_UNSUPPORTED_STATE, "depth clamp / bias");
+    if(st->color_format != SWGB_FORMAT_R8G8B8A8_UNORM) return set_error(SWGB_UNSUPPORTED_STATE, "color_format");
+    if(!st->color) return set_error(SWGB_INVALID_ARG, "color attachment is null");
+    if(st->attrib_count < 1 || st->attrib_count > SWGB_MAX_ATTRIBS) return set_error(SWGB_INVALID_ARG, "attrib_count");
+    if(st->color_blend_op > SWGB_BLEND_OP_MAX || st->alpha_blend_op > SWGB_BLEND_OP_MAX) return set_error(SWGB_UNSUPPORTED_STATE, "blend op");
+    if(st->framebuffer_width > 16384 || st->framebuffer_height > 16384) return set_error(SWGB_UNSUPPORTED_STATE, "framebuffer larger than 16384");
+    D.nattr = (int)st->attrib_count;
+    D.nv = 0;
+    for(int i = 0; i < D.nattr; i++)
+    {
+        const swgb_vertex_attrib &at = st->attribs[i];
+        if(at.binding >= SWGB_MAX_ATTRIBS || !st->bindings[at.binding].buffer) return set_error(SWGB_INVALID_ARG, "vertex binding");
+        if(at.format != SWGB_FORMAT_R32G32B32A32_SFLOAT && at.format != SWGB_FORMAT_R32G32_SFLOAT) return set_error(SWGB_UNSUPPORTED_STATE, "vertex format");
+        D.vbuf[i] = (const uint8_t *)st->bindings[at.binding].buffer;
+        D.vstride[i] = st->bindings[at.binding].stride;
+        D.voff[i] = at.offset;
+        D.vcomp[i] = at.format == SWGB_FORMAT_R32G32_SFLOAT ? 2 : 4;
+        if(i > 0) D.nv += (int)D.vcomp[i];
+    }
+    if(D.nv > MAXV) return set_error(SWGB_UNSUPPORTED_STATE, "too many varyings");
+    if(D.nattr < 2 || D.vcomp[1] != 4) return set_error(SWGB_INVALID_ARG, "the fixed FS reads a vec4 colour at location 0");
+    D.fs = (int)st->fragment_shader;
+    if(D.fs == SWGB_FS_TEX_X_VCOLOR && (D.nattr < 3 || D.nv < 6)) return set_error(SWGB_INVALID_ARG, "textured FS needs a uv varying");
+    memcpy(D.mvp, st->mvp, sizeof(D.mvp));
+
+    D.count = a->count;
+    D.indexType = a->index_type;
+    D.indices = a->indices;
+    D.firstVertex = a->first_vertex;
+    D.baseVertex = a->base_vertex;
+    if(a->index_type == SWGB_INDEX_TYPE_NONE)
+        D.vertexCount = 3u * a->count;
+    else
+    {
+        if(a->index_type != SWGB_INDEX_TYPE_UINT16 && a->index_type != SWGB_INDEX_TYPE_UINT32) return set_error(SWGB_INVALID_ARG, "index_type");
+        if(!a->indices) return set_error(SWGB_INVALID_ARG, "indices");
+        if(a->vertex_count == 0) return set_error(SWGB_INVALID_ARG, "indexed draws need vertex_count");
+        D.vertexCount = a->vertex_count;
+    }
+
+    // Viewport and scissor (Renderer.cpp:300-345)
+    float W = 0.5f * st->viewport_width, H = 0.5f * st->viewport_height;
+    float X0 = st->viewport_x + W, Y0 = st->viewport_y + H;
+    D.WxF = W * 256.0f;
+    D.HxF = H * 256.0f;
+    D.X0xF = X0 * 256.0f - 128.0f;
+    D.Y0xF = Y0 * 256.0f - 128.0f;
+    D.depthRange = st->viewport_max_depth - st->viewport_min_depth;
+    D.depthNear = st->viewport_min_depth;
+    int rx0 = a->render_area_x, ry0 = a->render_area_y;
+    int rx1 = rx0 + (int)a->render_area_width, ry1 = ry0 + (int)a->render_area_height;
+    auto clampi = [](int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); };
+    D.sx0 = clampi(st->scissor_x, rx0, rx1);
+    D.sx1 = clampi(st->scissor_x + (int)st->scissor_width, rx0, rx1);
+    D.sy0 = clampi(st->scissor_y, ry0, ry1);
+    D.sy1 = clampi(st->scissor_y + (int)st->scissor_height, ry0, ry1);
+    if(D.sx0 < 0 || D.sy0 < 0 || D.sx1 > (int)st->framebuffer_width || D.sy1 > (int)st->framebuffer_height)
+        return set_error(SWGB_INVALID_ARG, "render area outside the framebuffer");
+    D.depthClip = st->depth_clip_enable ? 1 : 0;
+    D.cullMode = st->cull_mode;
+    D.frontFace = st->front_face;
+
+    D.depthTest = st->depth && st->depth_test_enable;
+    D.depthWrite = D.depthTest && st->depth_write_enable;
+    D.compareOp = st->depth_compare_op;
+    D.minDepthClamp = 0.0f;  // no VK_EXT_depth_range_unrestricted: clamp to [0,1] (PixelProcessor.cpp:106-128)
+    D.maxDepthClamp = 1.0f;
+    uint32_t opC = simplify_op(st->color_blend_op, st->src_color_factor, st->dst_color_factor);
+    uint32_t opA = simplify_op(st->alpha_blend_op, st->src_alpha_factor, st->dst_alpha_factor);
+    D.blend = st->blend_enable && (opC != OP_SRC_EXT || opA != OP_SRC_EXT) && st->color_write_mask != 0;
+    D.srcC = st->src_color_factor; D.dstC = st->dst_color_factor; D.opC = opC;
+    D.srcA = st->src_alpha_factor; D.dstA = st->dst_alpha_factor; D.opA = opA;
+    D.writeMask = st->color_write_mask & 0xFu;
+    D.color = (uint8_t *)st->color;
+    D.colorPitch = st->color_pitch_bytes;
+    D.depth = (uint8_t *)st->depth;
+    D.depthPitch = st->depth_pitch_bytes;
+    D.vec16 = ((uintptr_t)D.color % 16 == 0) && (D.colorPitch % 16 == 0) &&
+              (!D.depthTest || (((uintptr_t)D.depth % 16 == 0) && (D.depthPitch % 16 == 0)));
+
+    if(D.fs == SWGB_FS_TEX_X_VCOLOR)
+    {
+        const swgb_texture &t = st->texture;
+        if(t.format != SWGB_FORMAT_R8G8B8A8_UNORM) return set_error(SWGB_UNSUPPORTED_STATE, "texture format");
+        if(t.level_count < 1 || t.level_count > SWGB_MAX_MIP_LEVELS) return set_error(SWGB_INVALID_ARG, "texture level_count");
+        if(t.mag_filter != t.min_filter) return set_error(SWGB_UNSUPPORTED_STATE, "mixed min/mag filters");
+        if(t.address_u > SWGB_ADDRESS_CLAMP_TO_EDGE || t.address_v > SWGB_ADDRESS_CLAMP_TO_EDGE) return set_error(SWGB_UNSUPPORTED_STATE, "address mode");
+        D.levelCount = (int)t.level_count;
+        for(uint32_t i = 0; i < t.level_count; i++)
+        {
+            const swgb_texture_level &l = t.levels[i];
+            if(!l.buffer || l.width == 0 || l.height == 0 || l.width > 32768 || l.height > 32768 || l.pitch_texels > 32767)
+                return set_error(SWGB_INVALID_ARG, "texture level");
+            D.lv[i].buf = (const uint8_t *)l.buffer;
+            D.lv[i].w = l.width;
+            D.lv[i].h = l.height;
+            D.lv[i].pitch = l.pitch_texels;
+            D.lv[i].uHalf = (0x8000u / l.width) & 0xFFFFu;  // WriteTextureLevelInfo (VkDescriptorSetLayout.cpp:316-321)
+            D.lv[i].vHalf = (0x8000u / l.height) & 0xFFFFu;
+        }
+        D.texW = (float)t.levels[0].width;
+        D.texH = (float)t.levels[0].height;
+        auto clampLod = [](float l) { return l < 0.0f ? 0.0f : (l > 13.0f ? 13.0f : l); };  // vk::Sampler ClampLod
+        D.minLod = clampLod(t.min_lod);
+        D.maxLod = clampLod(t.max_lod);
+        if(t.level_count == 1) { D.minLod = 0.0f; D.maxLod = 0.0f; }  // SpirvShaderSampling.cpp:88-99
+        D.lodBias = t.mip_lod_bias;
+        D.texLinear = t.mag_filter == SWGB_FILTER_LINEAR;
+        D.mipLinear = t.mipmap_mode == SWGB_MIPMAP_MODE_LINEAR;
+        D.addrU = t.address_u;
+        D.addrV = t.address_v;
+    }
+    D.binX0 = D.sx0 & ~(BIN - 1);
+    D.binY0 = D.sy0 & ~(BIN - 1);
+    D.binsX = (D.sx1 - D.binX0 + BIN - 1) / BIN;
+    D.binsY = (D.sy1 - D.binY0 + BIN - 1) / BIN;
+    D.nchunks = (int)((a->count + CHUNK - 1) / CHUNK);
+    return SWGB_OK;
+}
+
+swgb_status enqueue(swgb_ctx *ctx, DrawParams &D)
+{
+    if(D.count == 0) return SWGB_OK;  // Renderer.cpp:187
+    swgb_status s;
+    if((s = ensure(ctx->ptv, ctx->ptvCap, (size_t)D.vertexCount * 4, "ptv")) != SWGB_OK) return s;
+    if((s = ensure(ctx->tris, ctx->trisCap, (size_t)D.nchunks * CHUNK, "tris")) != SWGB_OK) return s;
+    if((s = ensure(ctx->chunkBox, ctx->chunkCap, (size_t)D.nchunks, "chunk boxes")) != SWGB_OK) return s;
+    size_t polyNeed = (size_t)D.count * MAX_POLY;
+    if((s = ensure(ctx->poly, ctx->polyCap, polyNeed, "clip polygons")) != SWGB_OK) return s;
+    D.ptv = ctx->ptv;
+    D.tris = ctx->tris;
+    D.chunkBox = ctx->chunkBox;
+    D.poly = ctx->poly;
+    D.polyCount = ctx->polyCount;
+    D.polyCapacity = (uint32_t)(ctx->polyCap / MAX_POLY);
+    D.counters = ctx->counters;
+    D.error = ctx->error;
+    if(!ctx->rasterAttr)
+    {
+        if((s = cuda_check(cudaFuncSetAttribute(k_raster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(RasterShared)), "raster smem attribute")) != SWGB_OK) return s;
+        ctx->rasterAttr = true;
+    }
+    const uint32_t nv = D.vertexCount;
+    k_vertex<<<(nv + 255) / 256, 256, 0, ctx->stream>>>(D, nv);
+    k_setup<<<D.nchunks, CHUNK, 0, ctx->stream>>>(D);
+    if(D.binsX > 0 && D.binsY > 0)
+    {
+        dim3 grid(D.binsX, D.binsY);
+        k_raster<<<grid, RASTER_THREADS, sizeof(RasterShared), ctx->stream>>>(D);
+        ctx->launches += 1;
+    }
+    ctx->launches += 2;
+    return cuda_check(cudaGetLastError(), "kernel launch");
+}
+
+}  // namespace
+
+extern "C" {
+
+int swgb_abi_version(void) { return SWGB_ABI_VERSION; }
+
+const char *swgb_last_error(void) { return g_error.c_str(); }
+
+swgb_status swgb_ctx_create(int device, void *stream, swgb_ctx **out)
+{
+    if(!out) return set_error(SWGB_INVALID_ARG, "out is null");
+    *out = nullptr;
+    int n = 0;
+    if(cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return set_error(SWGB_NO_DEVICE, "no CUDA device");
+    if(device < 0 || device >= n) return set_error(SWGB_INVALID_ARG, "device index");
+    swgb_status s = cuda_check(cudaSetDevice(device), "cudaSetDevice");
+    if(s != SWGB_OK) return s;
+    swgb_ctx *c = new swgb_ctx();
+    memset(c, 0, sizeof(*c));
+    c->device = device;
+    if(stream)
+        c->stream = (cudaStream_t)stream;
+    else
+    {
+        if((s = cuda_check(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream")) != SWGB_OK) { delete c; return s; }
+        c->ownStream = true;
+    }
+    if((s = cuda_check(cudaMalloc((void **)&c->polyCount, sizeof(uint32_t)), "polyCount")) != SWGB_OK ||
+       (s = cuda_check(cudaMalloc((void **)&c->counters, 8 * sizeof(unsigned long long)), "counters")) != SWGB_OK ||
+       (s = cuda_check(cudaMalloc((void **)&c->error, sizeof(int)), "error")) != SWGB_OK)
+    {
+        swgb_ctx_destroy(c);
+        return s;
+    }
+    cudaMemset(c->counters, 0, 8 * sizeof(unsigned long long));
+    cudaMemset(c->error, 0, sizeof(int));
+    cudaMemset(c->polyCount, 0, sizeof(uint32_t));
+    *out = c;
+    return SWGB_OK;
+}
+
+swgb_status swgb_ctx_destroy(swgb_ctx *c)
+{
+    if(!c) return SWGB_INVALID_ARG;
+    cudaSetDevice(c->device);
+    if(c->stream) cudaStreamSynchronize(c->stream);
+    cudaFree(c->ptv);
+    cudaFree(c->tris);
+    cudaFree(c->chunkBox);
+    cudaFree(c->poly);
+    cudaFree(c->polyCount);
+    cudaFree(c->counters);
+    cudaFree(c->error);
+    if(c->ownStream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return SWGB_OK;
+}
+
+swgb_status swgb_ctx_set_stream(swgb_ctx *c, void *stream)
+{
+    if(!c) return SWGB_INVALID_ARG;
+    if(c->ownStream && c->stream)
+    {
+        cudaStreamSynchronize(c->stream);
+        cudaStreamDestroy(c->stream);
+    }
+    c->ownStream = false;
+    c->stream = (cudaStream_t)stream;
+    return SWGB_OK;
+}
+
+swgb_status swgb_draw(swgb_ctx *ctx, const swgb_pipeline_state *st, const swgb_draw_args *args)
+{
+    if(!ctx || !st || !args) return set_error(SWGB_INVALID_ARG, "null argument");
+    if(args->count == 0) return SWGB_OK;
+    DrawParams D;
+    swgb_status s = bake(st, args, D);
+    if(s != SWGB_OK) return s;
+    cudaSetDevice(ctx->device);
+    return enqueue(ctx, D);
+}
+
+swgb_status swgb_draw_batch(swgb_ctx *ctx, const swgb_pipeline_state *states, const swgb_draw_args *args, uint32_t n)
+{
+    if(!ctx || (!states && n) || (!args && n)) return set_error(SWGB_INVALID_ARG, "null argument");
+    for(uint32_t i = 0; i < n; i++)
+    {
+        swgb_status s = swgb_draw(ctx, &states[i], &args[i]);
+        if(s != SWGB_OK) return s;
+    }
+    return SWGB_OK;
+}
+
+swgb_status swgb_sync(swgb_ctx *ctx)
+{
+    if(!ctx) return SWGB_INVALID_ARG;
+    swgb_status s = cuda_check(cudaStreamSynchronize(ctx->stream), "stream sync");
+    if(s != SWGB_OK) return s;
+    int err = 0;
+    if((s = cuda_check(cudaMemcpy(&err, ctx->error, sizeof(int), cudaMemcpyDeviceToHost), "error word")) != SWGB_OK) return s;
+    if(err)
+    {
+        cudaMemset(ctx->error, 0, sizeof(int));
+        if(err & ERR_INDEX_RANGE) return set_error(SWGB_INVALID_ARG, "an index was >= vertex_count; its triangle was dropped");
+        return set_error(SWGB_DEVICE_ERROR, "clipped-polygon scratch overflow");
+    }
+    return SWGB_OK;
+}
+
+swgb_status swgb_get_counters(swgb_ctx *ctx, swgb_counters *out)
+{
+    if(!ctx || !out) return SWGB_INVALID_ARG;
+    swgb_status s = cuda_check(cudaStreamSynchronize(ctx->stream), "stream sync");
+    if(s != SWGB_OK) return s;
+    unsigned long long h[8];
+    if((s = cuda_check(cudaMemcpy(h, ctx->counters, sizeof(h), cudaMemcpyDeviceToHost), "counters")) != SWGB_OK) return s;
+    out->triangles_in = h[0];
+    out->triangles_rejected = h[1];
+    out->triangles_clipped = h[2];
+    out->triangles_visible = h[3];
+    out->quads = h[4];
+    out->fragments_tested = h[5];
+    out->fragments_passed = h[6];
+    out->reserved = 0;
+    return SWGB_OK;
+}
+
+swgb_status swgb_reset_counters(swgb_ctx *ctx)
+{
+    if(!ctx) return SWGB_INVALID_ARG;
+    return cuda_check(cudaMemsetAsync(ctx->counters, 0, 8 * sizeof(unsigned long long), ctx->stream), "counters reset");
+}
+
+uint64_t swgb_launch_count(swgb_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+}  // extern "C"

@@ -1,0 +1,91 @@
+// swgb_numeric.cuh -- device restatement of the Reactor numeric primitives the
+// draw path depends on (src/Reactor/LLVMReactor.cpp, src/Reactor/Reactor.cpp).
+//
+// The translation unit is compiled with -ftz=true -prec-div=true
+// -prec-sqrt=true -fmad=false, so:
+//   * every f32 add/sub/mul/div flushes subnormal inputs and results to a zero
+//     of the same sign, as the reference's worker threads do (FTZ+DAZ,
+//     src/System/SwiftConfig.cpp:136-139);
+//   * a / b is the IEEE-rounded quotient (Rcp with relaxedPrecision = false is
+//     1.0f / x on x86, src/Reactor/Reactor.cpp:4812-4851);
+//   * no multiply-add is contracted unless written as mul_add() below, which
+//     stands for Reactor's MulAdd / ShaderCore mulAdd (llvm.fmuladd, fused when
+//     the JIT host has FMA; src/Pipeline/ShaderCore.cpp:714-722).
+#pragma once
+
+#include <stdint.h>
+
+namespace swgb {
+
+__device__ __forceinline__ float mul_add(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+
+// Max(x, y) = x > y ? x : y, Min(x, y) = x < y ? x : y
+// (src/Reactor/Reactor.cpp:3980-3988, LLVMReactor.cpp:4443-4453).
+__device__ __forceinline__ float rmax(float x, float y) { return x > y ? x : y; }
+__device__ __forceinline__ float rmin(float x, float y) { return x < y ? x : y; }
+
+// RoundInt: cvtss2si / cvtps2dq -- round half to even, 0x80000000 when the
+// value does not fit (LLVMReactor.cpp:2373-2381,2684-2692).
+__device__ __forceinline__ int32_t round_int(float x)
+{
+    return (x >= -2147483648.0f && x < 2147483648.0f) ? __float2int_rn(x) : INT32_MIN;
+}
+
+// RoundIntClamped on SIMD::Float: nearbyint + fptosi.sat (LLVMReactor.cpp:4264-4281).
+// cvt.rni.s32.f32 saturates and maps NaN to 0, which is fptosi.sat.
+__device__ __forceinline__ int32_t round_int_clamped(float x) { return __float2int_rn(x); }
+
+// Int(Float) / Int4(Float4): cvttss2si / cvttps2dq -- truncation, 0x80000000
+// when the value does not fit.
+__device__ __forceinline__ int32_t trunc_int(float x)
+{
+    return (x >= -2147483648.0f && x < 2147483648.0f) ? __float2int_rz(x) : INT32_MIN;
+}
+
+// MulHigh (pmulhuw, LLVMReactor.cpp:2229-2237).
+__device__ __forceinline__ uint32_t mulhi_u16(uint32_t a, uint32_t b) { return ((a & 0xFFFFu) * (b & 0xFFFFu)) >> 16; }
+
+__device__ __forceinline__ uint32_t addsat_u16(uint32_t a, uint32_t b)
+{
+    uint32_t s = a + b;
+    return s > 0xFFFFu ? 0xFFFFu : s;
+}
+__device__ __forceinline__ uint32_t subsat_u16(uint32_t a, uint32_t b) { return a > b ? a - b : 0u; }
+
+// log2(sqrt(x)) by the exponent-bit trick of SamplerCore (src/Pipeline/SamplerCore.cpp:1333-1341).
+__device__ __forceinline__ float log2sqrt(float lod)
+{
+    lod = lod * lod;
+    lod = __int2float_rn(__float_as_int(lod)) - 1065353216.0f;  // Float(As<Int>(lod)) - Float(0x3F800000)
+    lod = lod * __int_as_float(0x33000000);                     // * 0.25 * 2^-23
+    return lod;
+}
+
+// halfToFloatBits / floatToHalfBits (src/Pipeline/ShaderCore.cpp:627-671).
+__device__ __forceinline__ float half_to_float(uint32_t h)
+{
+    uint32_t sign16 = h & 0x8000u, man16 = h & 0x03FFu, exp16 = h & 0x7C00u;
+    uint32_t sign32 = sign16 << 16, man32 = man16 << 13, exp32 = (exp16 + 0x1C000u) << 13;
+    uint32_t norm32 = (man32 | exp32) | (exp16 == 0x7C00u ? 0x7F800000u : 0u);
+    const uint32_t magic = 126u << 23;
+    uint32_t denorm32 = __float_as_uint(__uint_as_float(magic + man16) - __uint_as_float(magic));
+    return __uint_as_float(sign32 | (exp16 == 0 ? denorm32 : norm32));
+}
+
+__device__ __forceinline__ uint32_t float_to_half(float f)
+{
+    uint32_t bits = __float_as_uint(f);
+    uint32_t sign = bits & 0x80000000u, ab = bits & 0x7FFFFFFFu;
+    bool normal = ab > 0x38800000u;
+    uint32_t mantissa = (ab & 0x007FFFFFu) | 0x00800000u;
+    uint32_t e = 113u - (ab >> 23);
+    uint32_t denormal = e < 24u ? (mantissa >> e) : 0u;
+    uint32_t base = normal ? ab : denormal;
+    uint32_t bias = normal ? 0xC8000000u : 0u;
+    uint32_t rounded = base + bias + 0x00000FFFu + ((base >> 13) & 1u);
+    uint32_t fp16u = rounded >> 13;
+    if(ab > 0x47FFEFFFu) fp16u |= 0x7FFFu;
+    return ((sign >> 16) | fp16u) & 0xFFFFu;
+}
+
+}  // namespace swgb

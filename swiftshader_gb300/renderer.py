@@ -1,0 +1,100 @@
+"""Host-side mirror of sw::Renderer for the triangle-list FILL path.
+
+``Renderer.draw(state, args)`` is the reference's
+``sw::Renderer::draw(pipeline, dynamicState, count, baseVertex, events,
+instanceID, layer, indexBuffer, renderArea, pushConstants)``
+(src/Device/Renderer.hpp:211-213) with the pipeline state flattened into
+``abi.PipelineState`` and the per-draw arguments into ``abi.DrawArgs``;
+``Renderer.synchronize()`` is ``sw::Renderer::synchronize()``
+(src/Device/Renderer.cpp:664-671).  Like the reference, ``draw`` returns before
+the work completes; errors the device detects surface at ``synchronize``.
+
+Every call goes through libswgb.so.  There is no CPU path: without the built
+library or a CUDA device, construction raises.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import abi, scenes
+from ._lib import check, load
+
+
+class Renderer:
+    def __init__(self, device=0, stream=None):
+        self._L = load()
+        ctx = C.c_void_p()
+        handle = None
+        if stream is not None:
+            handle = C.c_void_p(stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream))
+        check(self._L.swgb_ctx_create(int(device), handle, C.byref(ctx)), "swgb_ctx_create")
+        self._ctx = ctx
+
+    def draw(self, state, args):
+        check(self._L.swgb_draw(self._ctx, C.byref(state), C.byref(args)), "swgb_draw")
+
+    def draw_batch(self, states, args):
+        n = len(states)
+        S = (abi.PipelineState * n)(*states)
+        A = (abi.DrawArgs * n)(*args)
+        check(self._L.swgb_draw_batch(self._ctx, S, A, n), "swgb_draw_batch")
+
+    def synchronize(self):
+        check(self._L.swgb_sync(self._ctx), "swgb_sync")
+
+    def counters(self):
+        c = abi.Counters()
+        check(self._L.swgb_get_counters(self._ctx, C.byref(c)), "swgb_get_counters")
+        return c.as_dict()
+
+    def reset_counters(self):
+        check(self._L.swgb_reset_counters(self._ctx), "swgb_reset_counters")
+
+    def launch_count(self):
+        return int(self._L.swgb_launch_count(self._ctx))
+
+    def set_stream(self, stream):
+        check(self._L.swgb_ctx_set_stream(self._ctx, C.c_void_p(stream.cuda_stream)), "swgb_ctx_set_stream")
+
+    def close(self):
+        if getattr(self, "_ctx", None):
+            self._L.swgb_ctx_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class DeviceScene:
+    """A scene's buffers resident in device memory (torch tensors), plus the
+    C-ABI state that points at them."""
+
+    def __init__(self, scene, device="cuda"):
+        import torch
+        self.scene = scene
+        self.device = torch.device(device)
+        self.vertices = torch.from_numpy(np.ascontiguousarray(scene.vertices)).to(self.device)
+        self.indices = None if scene.indices is None else torch.from_numpy(
+            np.ascontiguousarray(scene.indices).view(np.int32)).to(self.device)
+        self.levels = [torch.from_numpy(np.ascontiguousarray(l)).to(self.device) for l in scene.texture_levels]
+        h, w = scene.height, scene.width
+        cdtype = {abi.FORMAT_R8G8B8A8_UNORM: torch.uint8, abi.FORMAT_R32G32B32A32_SFLOAT: torch.float32,
+                  abi.FORMAT_R16G16B16A16_SFLOAT: torch.float16}[scene.color_format]
+        self.color = torch.empty((h, w, 4), dtype=cdtype, device=self.device)
+        self.depth = torch.empty((h, w), dtype=torch.float32, device=self.device)
+        self.clear()
+
+    def clear(self):
+        import torch
+        self.color[...] = torch.tensor(self.scene.clear_color, dtype=self.color.dtype, device=self.device)
+        self.depth.fill_(self.scene.clear_depth)
+
+    def state(self):
+        return scenes.build_state(self.scene, self.color.data_ptr(), self.depth.data_ptr(), self.vertices.data_ptr(),
+                                  [l.data_ptr() for l in self.levels])
+
+    def args(self):
+        return scenes.build_args(self.scene, None if self.indices is None else self.indices.data_ptr())

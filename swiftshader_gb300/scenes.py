@@ -1,0 +1,263 @@
+"""Seeded synthetic scenes for the five draw workloads the path is measured on.
+
+Every generator is deterministic: ``seed = 0x53570000 + workload index`` feeds
+numpy's PCG64 generator.  A scene is host data only (numpy arrays plus pipeline
+state values); ``Renderer`` uploads it, and the tests hand the same arrays to
+the CPU oracle.
+
+Vertex layout (AoS, 40 bytes): position R32G32B32A32_SFLOAT at 0, colour
+R32G32B32A32_SFLOAT at 16, uv R32G32_SFLOAT at 32.
+"""
+from dataclasses import dataclass, field
+import math
+
+import numpy as np
+
+from . import abi
+
+SEED_BASE = 0x53570000
+VERTEX_FLOATS = 10
+VERTEX_STRIDE = VERTEX_FLOATS * 4
+
+
+@dataclass
+class Scene:
+    name: str
+    width: int
+    height: int
+    vertices: np.ndarray              # float32 [N, 10]
+    indices: np.ndarray = None        # uint32 [3T] or None (non-indexed)
+    tri_count: int = 0
+    mvp: np.ndarray = None            # float32 [4, 4] row-major math matrix
+    fragment_shader: int = abi.FS_VCOLOR
+    texture_levels: list = field(default_factory=list)  # uint8 [h, w, 4] per level
+    sampler: dict = field(default_factory=dict)
+    blend: tuple = None               # (srcC, dstC, opC, srcA, dstA, opA) or None
+    cull_mode: int = abi.CULL_NONE
+    front_face: int = abi.FRONT_FACE_CCW
+    depth_compare: int = abi.COMPARE_LESS
+    clear_color: tuple = (0, 0, 0, 0)
+    clear_depth: float = 1.0
+    color_format: int = abi.FORMAT_R8G8B8A8_UNORM
+    viewport: tuple = None            # (x, y, w, h) default full framebuffer
+    scissor: tuple = None             # (x, y, w, h)
+
+    @property
+    def vertex_count(self):
+        return int(self.vertices.shape[0])
+
+    def mvp_column_major(self):
+        m = np.eye(4, dtype=np.float32) if self.mvp is None else np.asarray(self.mvp, np.float32)
+        return m.T.reshape(-1).copy()
+
+
+def _rng(index):
+    return np.random.Generator(np.random.PCG64(SEED_BASE + index))
+
+
+def random_triangles(rng, n, textured=False):
+    """n independent triangles, uniform in clip space: x,y in [-1,1],
+    z in [0.1,0.9], w = 1; RGBA uniform in [0,1]; uv uniform in [0,1]."""
+    v = np.zeros((3 * n, VERTEX_FLOATS), np.float32)
+    v[:, 0:2] = rng.uniform(-1.0, 1.0, (3 * n, 2))
+    v[:, 2] = rng.uniform(0.1, 0.9, 3 * n)
+    v[:, 3] = 1.0
+    v[:, 4:8] = rng.uniform(0.0, 1.0, (3 * n, 4))
+    if textured:
+        v[:, 8:10] = rng.uniform(0.0, 1.0, (3 * n, 2))
+    return v
+
+
+def box_mip_chain(level0):
+    """Full box-filtered mip chain of an RGBA8 image (rounded average of 2x2)."""
+    levels = [np.ascontiguousarray(level0)]
+    cur = level0.astype(np.uint32)
+    while cur.shape[0] > 1 or cur.shape[1] > 1:
+        h, w = cur.shape[:2]
+        h2, w2 = max(1, h // 2), max(1, w // 2)
+        if h > 1 and w > 1:
+            s = cur[0:2 * h2:2, 0:2 * w2:2] + cur[1:2 * h2:2, 0:2 * w2:2] + cur[0:2 * h2:2, 1:2 * w2:2] + cur[1:2 * h2:2, 1:2 * w2:2]
+            cur = (s + 2) // 4
+        elif h > 1:
+            cur = (cur[0:2 * h2:2] + cur[1:2 * h2:2] + 1) // 2
+        else:
+            cur = (cur[:, 0:2 * w2:2] + cur[:, 1:2 * w2:2] + 1) // 2
+        levels.append(np.ascontiguousarray(cur.astype(np.uint8)))
+    return levels
+
+
+def perspective_vk(fovy_deg, aspect, near, far):
+    """Vulkan clip space (y down, depth [0,1]) perspective matrix."""
+    f = 1.0 / math.tan(math.radians(fovy_deg) / 2.0)
+    return np.array([[f / aspect, 0, 0, 0],
+                     [0, -f, 0, 0],
+                     [0, 0, far / (near - far), near * far / (near - far)],
+                     [0, 0, -1, 0]], np.float64)
+
+
+def translate(x, y, z):
+    m = np.eye(4)
+    m[:3, 3] = (x, y, z)
+    return m
+
+
+def scene_small(n_tris=1000, width=256, height=256, seed_index=0):
+    """Plain forward, small: independent Gouraud triangles, identity MVP,
+    RGBA8 + D32F, depth LESS, no blending, no texture."""
+    rng = _rng(seed_index)
+    return Scene(name="tris%d_%dx%d" % (n_tris, width, height), width=width, height=height,
+                 vertices=random_triangles(rng, n_tris), tri_count=n_tris,
+                 fragment_shader=abi.FS_VCOLOR, clear_color=(0, 0, 0, 0), clear_depth=1.0)
+
+
+def scene_heightfield(quads_x=1000, quads_y=500, width=1920, height=1080, tex_size=2048, seed_index=1):
+    """Plain forward, large textured: a (quads_x x quads_y)-quad height-field
+    grid (2 triangles per quad, uint32 indices), heights uniform in [0,0.2],
+    perspective fov 60 deg, near 0.1, far 100, camera 2 units back.  UVs span
+    [0,4]^2 with REPEAT; tex_size^2 RGBA8 uniform texels with a box-filtered mip
+    chain, trilinear; colour = texel * vertex colour; depth LESS; blend
+    SRC_ALPHA / ONE_MINUS_SRC_ALPHA with vertex alpha in [0.5,1]."""
+    rng = _rng(seed_index)
+    nx, ny = quads_x + 1, quads_y + 1
+    aspect = width / height
+    half_h = 2.0 * math.tan(math.radians(30.0)) * 1.08   # slightly wider than the view: edges get clipped
+    half_w = half_h * aspect
+    gx = np.linspace(-half_w, half_w, nx, dtype=np.float64)
+    gy = np.linspace(-half_h, half_h, ny, dtype=np.float64)
+    X, Y = np.meshgrid(gx, gy)
+    Z = rng.uniform(0.0, 0.2, (ny, nx))
+    v = np.zeros((ny * nx, VERTEX_FLOATS), np.float32)
+    v[:, 0] = X.reshape(-1)
+    v[:, 1] = Y.reshape(-1)
+    v[:, 2] = Z.reshape(-1)
+    v[:, 3] = 1.0
+    v[:, 4:7] = rng.uniform(0.0, 1.0, (ny * nx, 3))
+    v[:, 7] = rng.uniform(0.5, 1.0, ny * nx)
+    U, V = np.meshgrid(np.linspace(0.0, 4.0, nx), np.linspace(0.0, 4.0, ny))
+    v[:, 8] = U.reshape(-1)
+    v[:, 9] = V.reshape(-1)
+    # indices: quad (i, j) -> (a, b, c), (c, b, d) with a=(j,i) b=(j,i+1) c=(j+1,i) d=(j+1,i+1)
+    j, i = np.meshgrid(np.arange(quads_y, dtype=np.uint32), np.arange(quads_x, dtype=np.uint32), indexing="ij")
+    a = (j * nx + i).reshape(-1)
+    b = a + 1
+    c = a + nx
+    d = c + 1
+    idx = np.stack([a, b, c, c, b, d], axis=1).reshape(-1).astype(np.uint32)
+    tex0 = rng.integers(0, 256, (tex_size, tex_size, 4), dtype=np.uint8)
+    mvp = perspective_vk(60.0, aspect, 0.1, 100.0) @ translate(0.0, 0.0, -2.0)
+    return Scene(name="heightfield%dk_%dx%d" % (len(idx) // 3 // 1000, width, height),
+                 width=width, height=height, vertices=v, indices=idx, tri_count=len(idx) // 3,
+                 mvp=mvp.astype(np.float32), fragment_shader=abi.FS_TEX_X_VCOLOR,
+                 texture_levels=box_mip_chain(tex0),
+                 sampler=dict(mag_filter=abi.FILTER_LINEAR, min_filter=abi.FILTER_LINEAR,
+                              mipmap_mode=abi.MIPMAP_MODE_LINEAR, address_u=abi.ADDRESS_REPEAT,
+                              address_v=abi.ADDRESS_REPEAT, mip_lod_bias=0.0, min_lod=0.0, max_lod=1000.0),
+                 blend=(abi.BLEND_SRC_ALPHA, abi.BLEND_ONE_MINUS_SRC_ALPHA, abi.BLEND_OP_ADD,
+                        abi.BLEND_SRC_ALPHA, abi.BLEND_ONE_MINUS_SRC_ALPHA, abi.BLEND_OP_ADD),
+                 clear_color=(26, 51, 77, 255), clear_depth=1.0)
+
+
+def scene_textured_small(n_tris=200, width=128, height=96, tex_size=64, mip=True, address=abi.ADDRESS_REPEAT,
+                         blend=True, seed_index=5):
+    """Small textured case for parity tests: random triangles with uv in
+    [-1.5, 2.5] so wrap/clamp addressing is exercised, optional mips/blend."""
+    rng = _rng(seed_index)
+    v = random_triangles(rng, n_tris, textured=True)
+    v[:, 8:10] = rng.uniform(-1.5, 2.5, (3 * n_tris, 2))
+    v[:, 7] = rng.uniform(0.3, 1.0, 3 * n_tris)
+    tex0 = rng.integers(0, 256, (tex_size, tex_size, 4), dtype=np.uint8)
+    levels = box_mip_chain(tex0) if mip else [tex0]
+    s = Scene(name="textured%d" % n_tris, width=width, height=height, vertices=v, tri_count=n_tris,
+              fragment_shader=abi.FS_TEX_X_VCOLOR, texture_levels=levels,
+              sampler=dict(mag_filter=abi.FILTER_LINEAR, min_filter=abi.FILTER_LINEAR,
+                           mipmap_mode=abi.MIPMAP_MODE_LINEAR if mip else abi.MIPMAP_MODE_NEAREST,
+                           address_u=address, address_v=address, mip_lod_bias=0.0, min_lod=0.0,
+                           max_lod=1000.0),
+              clear_color=(10, 20, 30, 40))
+    if blend:
+        s.blend = (abi.BLEND_SRC_ALPHA, abi.BLEND_ONE_MINUS_SRC_ALPHA, abi.BLEND_OP_ADD,
+                   abi.BLEND_SRC_ALPHA, abi.BLEND_ONE_MINUS_SRC_ALPHA, abi.BLEND_OP_ADD)
+    return s
+
+
+def build_state(scene, color_ptr, depth_ptr, vertex_ptr, level_ptrs=None, color_pitch=None, depth_pitch=None):
+    """PipelineState for a scene given buffer addresses (device pointers for
+    the GB300 path, host pointers for the oracle)."""
+    st = abi.PipelineState()
+    st.topology = abi.TOPOLOGY_TRIANGLE_LIST
+    st.attrib_count = 3
+    st.attribs[0] = abi.VertexAttrib(abi.FORMAT_R32G32B32A32_SFLOAT, 0, 0, 0)
+    st.attribs[1] = abi.VertexAttrib(abi.FORMAT_R32G32B32A32_SFLOAT, 0, 16, 0)
+    st.attribs[2] = abi.VertexAttrib(abi.FORMAT_R32G32_SFLOAT, 0, 32, 0)
+    st.bindings[0] = abi.VertexBinding(vertex_ptr, VERTEX_STRIDE, 0)
+    st.vertex_shader = abi.VS_MVP_PASSTHROUGH
+    st.fragment_shader = scene.fragment_shader
+    for k, val in enumerate(scene.mvp_column_major()):
+        st.mvp[k] = float(val)
+    vx, vy, vw, vh = scene.viewport or (0, 0, scene.width, scene.height)
+    st.viewport_x, st.viewport_y, st.viewport_width, st.viewport_height = float(vx), float(vy), float(vw), float(vh)
+    st.viewport_min_depth, st.viewport_max_depth = 0.0, 1.0
+    sx, sy, sw, sh = scene.scissor or (0, 0, scene.width, scene.height)
+    st.scissor_x, st.scissor_y, st.scissor_width, st.scissor_height = sx, sy, sw, sh
+    st.cull_mode = scene.cull_mode
+    st.front_face = scene.front_face
+    st.depth_clip_enable = 1
+    st.depth_test_enable = 1
+    st.depth_write_enable = 1
+    st.depth_compare_op = scene.depth_compare
+    st.color_format = scene.color_format
+    if scene.blend is not None:
+        st.blend_enable = 1
+        (st.src_color_factor, st.dst_color_factor, st.color_blend_op,
+         st.src_alpha_factor, st.dst_alpha_factor, st.alpha_blend_op) = scene.blend
+    st.color_write_mask = 0xF
+    st.sample_count = 1
+    bpp = {abi.FORMAT_R8G8B8A8_UNORM: 4, abi.FORMAT_R16G16B16A16_SFLOAT: 8,
+           abi.FORMAT_R32G32B32A32_SFLOAT: 16}[scene.color_format]
+    st.color = color_ptr
+    st.color_pitch_bytes = color_pitch or scene.width * bpp
+    st.color_slice_bytes = st.color_pitch_bytes * scene.height
+    st.depth = depth_ptr
+    st.depth_pitch_bytes = depth_pitch or scene.width * 4
+    st.depth_slice_bytes = st.depth_pitch_bytes * scene.height
+    st.framebuffer_width, st.framebuffer_height = scene.width, scene.height
+    if scene.fragment_shader == abi.FS_TEX_X_VCOLOR:
+        t = st.texture
+        t.format = abi.FORMAT_R8G8B8A8_UNORM
+        t.level_count = len(scene.texture_levels)
+        for i, lv in enumerate(scene.texture_levels):
+            t.levels[i] = abi.TextureLevel(level_ptrs[i], lv.shape[1], lv.shape[0], lv.shape[1], 0)
+        for k, val in scene.sampler.items():
+            setattr(t, k, val)
+    st.precision_profile = abi.PRECISION_CMAKE
+    return st
+
+
+def build_args(scene, index_ptr=None):
+    a = abi.DrawArgs()
+    a.count = scene.tri_count
+    a.base_vertex = 0
+    a.first_vertex = 0
+    if scene.indices is None:
+        a.index_type = abi.INDEX_TYPE_NONE
+        a.indices = None
+    else:
+        a.index_type = abi.INDEX_TYPE_UINT32
+        a.indices = index_ptr
+    a.vertex_count = scene.vertex_count
+    a.render_area_x, a.render_area_y = 0, 0
+    a.render_area_width, a.render_area_height = scene.width, scene.height
+    return a
+
+
+def clear_buffers(scene):
+    """Host colour (uint8/float) and depth (float32) attachments, cleared."""
+    if scene.color_format == abi.FORMAT_R8G8B8A8_UNORM:
+        color = np.empty((scene.height, scene.width, 4), np.uint8)
+    elif scene.color_format == abi.FORMAT_R32G32B32A32_SFLOAT:
+        color = np.empty((scene.height, scene.width, 4), np.float32)
+    else:
+        color = np.empty((scene.height, scene.width, 4), np.float16)
+    color[...] = np.asarray(scene.clear_color, color.dtype)
+    depth = np.full((scene.height, scene.width), scene.clear_depth, np.float32)
+    return color, depth
