@@ -232,13 +232,14 @@ typedef struct swgb_counters {
     uint64_t quads;              /* 2x2 quads with non-empty coverage that were shaded */
     uint64_t fragments_tested;   /* covered samples that reached the depth test       */
     uint64_t fragments_passed;   /* samples that passed and were written              */
-    uint64_t reserved;
+    uint64_t texture_levels_mask; /* bit i set: mip level i was sampled (OR across draws) */
 } swgb_counters;
 
 typedef struct swgb_ctx swgb_ctx;
 
-/* Library / context management. 'stream' is a cudaStream_t (NULL = the
- * context creates its own non-blocking stream). */
+/* Library / context management. 'stream' is a cudaStream_t: NULL makes the
+ * context create its own non-blocking stream; pass cudaStreamLegacy
+ * ((void *)1) to order draws on the legacy default stream. */
 int swgb_abi_version(void);
 const char *swgb_last_error(void);
 swgb_status swgb_ctx_create(int device, void *stream, swgb_ctx **out);
@@ -263,6 +264,18 @@ swgb_status swgb_reset_counters(swgb_ctx *ctx);
 
 /* Number of kernel launches this context has issued since creation. */
 uint64_t swgb_launch_count(swgb_ctx *ctx);
+
+/* Kernel timing for benchmarks: with enable = 1 the context records a CUDA
+ * event pair on its stream around every kernel launch.  swgb_get_kernel_times
+ * synchronises, sums the elapsed milliseconds per kernel kind
+ * (SWGB_KERNEL_*) into ms[] and the launch counts into launches[], then
+ * forgets the recorded pairs. */
+#define SWGB_KERNEL_VERTEX 0
+#define SWGB_KERNEL_SETUP 1
+#define SWGB_KERNEL_RASTER 2
+#define SWGB_KERNEL_KINDS 8
+swgb_status swgb_set_kernel_timing(swgb_ctx *ctx, int enable);
+swgb_status swgb_get_kernel_times(swgb_ctx *ctx, double ms[SWGB_KERNEL_KINDS], uint32_t launches[SWGB_KERNEL_KINDS]);
 
 #ifdef __cplusplus
 }

@@ -739,10 +739,11 @@ static void texel_rgba8(const swgb_texture_level *lv, uint16_t u, uint16_t v, ui
 }
 
 /* sampleQuad2D for one lane (SamplerCore.cpp:668-909) */
-static void sample_quad_2d(const OSampler *s, float u, float v, float lod, int secondLOD, uint16_t out[4])
+static void sample_quad_2d(const OSampler *s, float u, float v, float lod, int secondLOD, uint16_t out[4], uint32_t *lvMask)
 {
     int ilod = s->mipLinear ? trunc_int(lod) : round_int(lod); /* selectMipmap (:2357-2379) */
     const swgb_texture_level *lv = level_at(s, ilod + secondLOD);
+    if(lvMask) *lvMask |= 1u << (uint32_t)(lv - s->t->levels);
     uint16_t uuuu = address16(u, s->t->address_u);
     uint16_t vvvv = address16(v, s->t->address_v);
     if(!s->linearFilter)
@@ -797,7 +798,7 @@ static float lod_2d(const OSampler *s, const float u[4], const float v[4])
 
 /* sampleTexture128 for the 16-bit path (SamplerCore.cpp:59-253): returns
  * 4 lanes x RGBA, scaled by 1/getComponentScale() = 1/0xFF00. */
-static void sample_texture_quad(const OSampler *s, const float u[4], const float v[4], float out[4][4])
+static void sample_texture_quad(const OSampler *s, const float u[4], const float v[4], float out[4][4], uint32_t *lvMask)
 {
     float lod;
     if(s->minLod == s->maxLod)
@@ -813,11 +814,11 @@ static void sample_texture_quad(const OSampler *s, const float u[4], const float
     for(int lane = 0; lane < 4; lane++)
     {
         uint16_t c[4];
-        sample_quad_2d(s, u[lane], v[lane], lod, 0, c);
+        sample_quad_2d(s, u[lane], v[lane], lod, 0, c, lvMask);
         if(s->mipLinear) /* sampleFilter trilinear (:324-379) */
         {
             uint16_t cc[4];
-            sample_quad_2d(s, u[lane], v[lane], lod, 1, cc);
+            sample_quad_2d(s, u[lane], v[lane], lod, 1, cc, lvMask);
             float l = fmul(lod, 65536.0f);
             uint16_t utri = (uint16_t)trunc_int(l);
             for(int k = 0; k < 4; k++) cc[k] = mulhi_u16(cc[k], utri);
@@ -834,7 +835,7 @@ swgb_status oracle_sample_quad(const swgb_texture *tex, const float u[4], const 
     OSampler s;
     sampler_init(&s, tex);
     float o[4][4];
-    sample_texture_quad(&s, u, v, o);
+    sample_texture_quad(&s, u, v, o, NULL);
     for(int l = 0; l < 4; l++)
         for(int c = 0; c < 4; c++) out[l * 4 + c] = o[l][c];
     return SWGB_OK;
@@ -999,7 +1000,9 @@ static void pixel_quad(const ODraw *d, const OSampler *smp, const OPrim *pr, int
     if(st->fragment_shader == SWGB_FS_TEX_X_VCOLOR)
     {
         float tex[4][4];
-        sample_texture_quad(smp, vin[4], vin[5], tex);
+        uint32_t m = 0;
+        sample_texture_quad(smp, vin[4], vin[5], tex, &m);
+        if(cnt) cnt->texture_levels_mask |= m;
         for(int i = 0; i < 4; i++)
             for(int k = 0; k < 4; k++) c[i][k] = fmul(tex[i][k], vin[k][i]);
     }
@@ -1242,6 +1245,7 @@ swgb_status oracle_draw(const swgb_pipeline_state *st, const swgb_draw_args *a, 
             cnt->quads += j.local[t].quads;
             cnt->fragments_tested += j.local[t].fragments_tested;
             cnt->fragments_passed += j.local[t].fragments_passed;
+            cnt->texture_levels_mask |= j.local[t].texture_levels_mask;
         }
     pthread_mutex_destroy(&j.mu);
     free(j.prims);

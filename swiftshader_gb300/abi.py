@@ -114,7 +114,7 @@ class Counters(C.Structure):
     _fields_ = [("triangles_in", C.c_uint64), ("triangles_rejected", C.c_uint64),
                 ("triangles_clipped", C.c_uint64), ("triangles_visible", C.c_uint64),
                 ("quads", C.c_uint64), ("fragments_tested", C.c_uint64),
-                ("fragments_passed", C.c_uint64), ("reserved", C.c_uint64)]
+                ("fragments_passed", C.c_uint64), ("texture_levels_mask", C.c_uint64)]
 
     def as_dict(self):
-        return {k: int(getattr(self, k)) for k, _ in self._fields_ if k != "reserved"}
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}

@@ -25,10 +25,11 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
-#include <mutex>
 #include <string>
+#include <vector>
 
 #include "../../include/swgb.h"
 #include "swgb_numeric.cuh"
@@ -42,7 +43,8 @@ constexpr int BIN = 32;          // bin side in pixels
 constexpr int BIN_QUADS = (BIN / 2) * (BIN / 2);
 constexpr int RASTER_THREADS = 256;
 constexpr int BATCH = 128;       // triangles staged per raster batch
-constexpr int CHUNK = 256;       // triangles per setup block / chunk box
+constexpr int SETUP_THREADS = 256;
+constexpr int CHUNK = 64;        // triangles per chunk box
 constexpr int MAX_POLY = 16;     // clipped polygon capacity (Polygon::B, src/Device/Polygon.hpp:45)
 
 enum { CLIP_RIGHT = 1 << 0, CLIP_TOP = 1 << 1, CLIP_FAR = 1 << 2, CLIP_LEFT = 1 << 3,
@@ -58,11 +60,13 @@ struct TexLevel {
     uint32_t uHalf, vHalf;
 };
 
-// Per-triangle record written by k_setup (16 bytes).
-struct TriRec {
-    int16_t x0, y0, x1, y1;  // pixel box; y0/y1 are the trimmed [yMin, yMax)
-    uint32_t info;           // bits 0-4: polygon vertex count (0 = no primitive), bit 5: winding d, bit 6: clipped
-    uint32_t slot;           // clipped polygon slot
+// Per-triangle record written by k_setup next to its pixel box (a short4
+// x0, y0, x1, y1 with y0/y1 the trimmed [yMin, yMax); x0 >= x1 = no primitive).
+struct TriInfo {
+    uint32_t info;     // bits 0-4: polygon vertex count, bit 5: winding d, bit 6: clipped, bit 7: spans stored
+    uint32_t slot;     // clipped polygon slot
+    uint32_t spanOff;  // span-buffer index of row y0 (when stored)
+    uint32_t pad;
 };
 
 // Everything a draw's kernels read, baked on the host from the pipeline state
@@ -111,8 +115,12 @@ struct DrawParams {
     int nchunks;
     // scratch
     float4 *ptv;          // 4 x float4 per vertex
-    TriRec *tris;
-    short4 *chunkBox;     // x0, y0, x1, y1 per chunk
+    short4 *triBox;       // pixel box per triangle
+    TriInfo *triInfo;
+    short4 *chunkBox;     // union of the boxes of CHUNK consecutive triangles
+    uint32_t *spans;      // left | right << 16 per triangle row
+    unsigned long long *spanCount;
+    uint64_t spanCapacity;
     int2 *poly;           // MAX_POLY per slot
     uint32_t *polyCount;
     uint32_t polyCapacity;
@@ -147,7 +155,11 @@ __device__ __forceinline__ void read_attrib(const DrawParams &D, int a, uint32_t
 __global__ void k_vertex(const __grid_constant__ DrawParams D, uint32_t nverts)
 {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if(i == 0) *D.polyCount = 0;
+    if(i == 0)
+    {
+        *D.polyCount = 0;
+        *D.spanCount = 0;
+    }
     if(i >= nverts) return;
     uint32_t index = (D.indexType == SWGB_INDEX_TYPE_NONE ? D.firstVertex + i : i) + (uint32_t)D.baseVertex;
     float p[4];
@@ -348,23 +360,54 @@ __device__ void span_at(const DrawParams &D, const int32_t *X, const int32_t *Y,
     }
 }
 
-__device__ __forceinline__ short4 empty_box() { return make_short4(0x7FFF, 0x7FFF, -0x8000, -0x8000); }
-
-__global__ void __launch_bounds__(CHUNK) k_setup(const __grid_constant__ DrawParams D)
+// Writes the spans of rows [yMin, yMax) of a polygon into sp[0 .. yMax-yMin)
+// (left | right << 16), edge by edge in the reference's order, so that the
+// last edge writing a row wins exactly as in the outline buffer
+// (SetupRoutine.cpp:230-240,550-621).  Every row in the range is written by at
+// least one edge per side: the polygon is closed.
+__device__ void write_spans(const DrawParams &D, const int32_t *X, const int32_t *Y, int n, int dW, int32_t yMin, uint32_t *sp)
 {
-    uint32_t t = blockIdx.x * CHUNK + threadIdx.x;
-    TriRec rec;
-    rec.x0 = rec.y0 = rec.x1 = rec.y1 = 0;
-    rec.info = 0;
-    rec.slot = 0;
-    int cntIn = 0, cntRej = 0, cntClip = 0, cntVis = 0;
+    for(int i = 0; i < n; i++)
+    {
+        int ia = i + 1 - dW, ib = i + dW;
+        ia = ia == n ? 0 : ia;
+        ib = ib == n ? 0 : ib;
+        EdgeDDA e;
+        if(!edge_setup(D, X[ia], Y[ia], X[ib], Y[ib], e)) continue;
+        int32_t dd;
+        int32_t x = edge_x_at(e, e.yMin, &dd);
+        uint16_t *h = reinterpret_cast<uint16_t *>(sp) + (e.right ? 1 : 0);
+        for(int32_t y = e.yMin; y < e.yMax; y++)
+        {
+            h[2 * (y - yMin)] = (uint16_t)clamp_x(D, x);
+            x += e.Q;
+            dd += e.R;
+            int32_t of = (-dd) >> 31;
+            dd -= e.D & of;
+            x -= of;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(SETUP_THREADS) k_setup(const __grid_constant__ DrawParams D)
+{
+    const uint32_t t = blockIdx.x * SETUP_THREADS + threadIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    short4 box = make_short4(0, 0, 0, 0);
+    TriInfo inf = {0u, 0u, 0u, 0u};
+    int cntIn = 0, cntClip = 0, cntVis = 0;
+    bool cand = false;
+    int n = 3, dW = 1;
+    int32_t X[MAX_POLY + 1], Y[MAX_POLY + 1];
+    int32_t yMin = 0, yMax = 0, xMinS = 0, xMaxS = 0;
     if(t < D.count)
     {
         cntIn = 1;
-        uint32_t i0 = fetch_index(D, 3 * t + 0), i1 = fetch_index(D, 3 * t + 1), i2 = fetch_index(D, 3 * t + 2);
+        uint32_t i0, i1, i2;
         bool ok = true;
         if(D.indexType != SWGB_INDEX_TYPE_NONE)
         {
+            i0 = fetch_index(D, 3 * t + 0); i1 = fetch_index(D, 3 * t + 1); i2 = fetch_index(D, 3 * t + 2);
             if(i0 >= D.vertexCount || i1 >= D.vertexCount || i2 >= D.vertexCount)
             {
                 atomicOr(D.error, ERR_INDEX_RANGE);
@@ -375,25 +418,22 @@ __global__ void __launch_bounds__(CHUNK) k_setup(const __grid_constant__ DrawPar
         {
             i0 = 3 * t + 0; i1 = 3 * t + 1; i2 = 3 * t + 2;
         }
-        int visible = 0, clipped = 0;
         if(ok)
         {
-            float4 c0 = D.ptv[(size_t)i0 * 4], c1 = D.ptv[(size_t)i1 * 4], c2 = D.ptv[(size_t)i2 * 4];
-            float4 p0 = D.ptv[(size_t)i0 * 4 + 1], p1 = D.ptv[(size_t)i1 * 4 + 1], p2 = D.ptv[(size_t)i2 * 4 + 1];
-            int f0 = __float_as_int(p0.z), f1 = __float_as_int(p1.z), f2 = __float_as_int(p2.z);
-            int32_t X[MAX_POLY + 1], Y[MAX_POLY + 1];
+            const float4 p0 = D.ptv[(size_t)i0 * 4 + 1], p1 = D.ptv[(size_t)i1 * 4 + 1], p2 = D.ptv[(size_t)i2 * 4 + 1];
+            const int f0 = __float_as_int(p0.z), f1 = __float_as_int(p1.z), f2 = __float_as_int(p2.z);
             X[0] = __float_as_int(p0.x); X[1] = __float_as_int(p1.x); X[2] = __float_as_int(p2.x);
             Y[0] = __float_as_int(p0.y); Y[1] = __float_as_int(p1.y); Y[2] = __float_as_int(p2.y);
-            int n = 3;
             // setupSolidTriangles trivial reject (src/Device/Renderer.cpp:749-765)
             if((f0 & f1 & f2) == CLIP_FINITE)
             {
-                int flagsOr = f0 | f1 | f2;
+                const float4 c0 = D.ptv[(size_t)i0 * 4], c1 = D.ptv[(size_t)i1 * 4], c2 = D.ptv[(size_t)i2 * 4];
+                const int flagsOr = f0 | f1 | f2;
                 bool keep = true;
                 CVert P[MAX_POLY];
                 if(flagsOr != CLIP_FINITE)
                 {
-                    clipped = 1;
+                    cntClip = 1;
                     P[0] = {c0.x, c0.y, c0.z, c0.w};
                     P[1] = {c1.x, c1.y, c1.z, c1.w};
                     P[2] = {c2.x, c2.y, c2.z, c2.w};
@@ -411,84 +451,141 @@ __global__ void __launch_bounds__(CHUNK) k_setup(const __grid_constant__ DrawPar
                     bool front = D.frontFace == SWGB_FRONT_FACE_COUNTER_CLOCKWISE ? (A >= 0.0f) : (A <= 0.0f);
                     if((D.cullMode & SWGB_CULL_FRONT) && front) keep = false;
                     if((D.cullMode & SWGB_CULL_BACK) && !front) keep = false;
-                    int dW = A > 0.0f ? 1 : 0;
-                    if(keep && clipped)
+                    dW = A > 0.0f ? 1 : 0;
+                }
+                if(keep && cntClip)
+                {
+                    // reproject the clipped polygon (SetupRoutine.cpp:125-145)
+                    for(int i = 0; i < n; i++)
                     {
-                        // reproject the clipped polygon (SetupRoutine.cpp:125-145)
-                        for(int i = 0; i < n; i++)
-                        {
-                            float w = P[i].w;
-                            float rhw = w != 0.0f ? 1.0f / w : 1.0f;
-                            X[i] = round_int(D.X0xF + (P[i].x * rhw) * D.WxF);
-                            Y[i] = round_int(D.Y0xF + (P[i].y * rhw) * D.HxF);
-                        }
+                        float w = P[i].w;
+                        float rhw = w != 0.0f ? 1.0f / w : 1.0f;
+                        X[i] = round_int(D.X0xF + (P[i].x * rhw) * D.WxF);
+                        Y[i] = round_int(D.Y0xF + (P[i].y * rhw) * D.HxF);
                     }
-                    if(keep)
+                }
+                if(keep)
+                {
+                    yMin = Y[0]; yMax = Y[0]; xMinS = X[0]; xMaxS = X[0];
+                    for(int i = 1; i < n; i++)
                     {
-                        int32_t yMin = Y[0], yMax = Y[0], xMinS = X[0], xMaxS = X[0];
-                        for(int i = 1; i < n; i++)
-                        {
-                            yMin = min(yMin, Y[i]); yMax = max(yMax, Y[i]);
-                            xMinS = min(xMinS, X[i]); xMaxS = max(xMaxS, X[i]);
-                        }
-                        yMin = max((yMin + 0xFF) >> 8, D.sy0);
-                        yMax = min((yMax + 0xFF) >> 8, D.sy1);
-                        if(yMin < yMax)
-                        {
-                            // Trim empty rows at the top and bottom (SetupRoutine.cpp:243-264)
-                            int32_t l, r;
-                            while(yMin < yMax)
-                            {
-                                span_at(D, X, Y, n, dW, yMin, l, r);
-                                if(l != r) break;
-                                yMin++;
-                            }
-                            while(yMax > yMin)
-                            {
-                                span_at(D, X, Y, n, dW, yMax - 1, l, r);
-                                if(l != r) break;
-                                yMax--;
-                            }
-                            if(yMin < yMax)
-                            {
-                                int32_t bx0 = max(D.sx0, (xMinS + 0xFF) >> 8);
-                                int32_t bx1 = min(D.sx1, (xMaxS + 0xFF) >> 8);
-                                visible = 1;
-                                rec.x0 = (int16_t)bx0; rec.x1 = (int16_t)max(bx1, bx0);
-                                rec.y0 = (int16_t)yMin; rec.y1 = (int16_t)yMax;
-                                rec.info = (uint32_t)n | ((uint32_t)dW << 5) | ((uint32_t)clipped << 6);
-                                if(clipped)
-                                {
-                                    uint32_t slot = atomicAdd(D.polyCount, 1u);
-                                    if(slot < D.polyCapacity)
-                                    {
-                                        rec.slot = slot;
-                                        for(int i = 0; i < n; i++) D.poly[(size_t)slot * MAX_POLY + i] = make_int2(X[i], Y[i]);
-                                    }
-                                    else
-                                    {
-                                        atomicOr(D.error, ERR_POLY_OVERFLOW);
-                                        visible = 0;
-                                        rec.info = 0;
-                                    }
-                                }
-                            }
-                        }
+                        yMin = min(yMin, Y[i]); yMax = max(yMax, Y[i]);
+                        xMinS = min(xMinS, X[i]); xMaxS = max(xMaxS, X[i]);
+                    }
+                    // Vertical range (SetupRoutine.cpp:147-186)
+                    yMin = max((yMin + 0xFF) >> 8, D.sy0);
+                    yMax = min((yMax + 0xFF) >> 8, D.sy1);
+                    cand = yMin < yMax;
+                }
+            }
+        }
+    }
+
+    // ---- allocate span rows: block scan + one atomic per block ----------
+    __shared__ uint32_t sWarp[SETUP_THREADS / 32];
+    __shared__ unsigned long long sBase;
+    uint32_t rows = cand ? (uint32_t)(yMax - yMin) : 0u;
+    uint32_t incl = rows;
+#pragma unroll
+    for(int o = 1; o < 32; o <<= 1)
+    {
+        uint32_t u = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if(lane >= o) incl += u;
+    }
+    if(lane == 31) sWarp[warp] = incl;
+    __syncthreads();
+    if(threadIdx.x == 0)
+    {
+        uint32_t tot = 0;
+        for(int w = 0; w < SETUP_THREADS / 32; w++)
+        {
+            uint32_t c = sWarp[w];
+            sWarp[w] = tot;
+            tot += c;
+        }
+        sBase = tot ? atomicAdd(D.spanCount, (unsigned long long)tot) : 0ull;
+    }
+    __syncthreads();
+    const uint64_t off = (uint64_t)sBase + sWarp[warp] + (incl - rows);
+
+    if(cand)
+    {
+        bool stored = off + rows <= (uint64_t)D.spanCapacity;
+        if(stored)
+        {
+            uint32_t *sp = D.spans + off;
+            write_spans(D, X, Y, n, dW, yMin, sp);
+            // Trim empty rows at the top and bottom (SetupRoutine.cpp:243-264)
+            const int32_t y0 = yMin;
+            while(yMin < yMax)
+            {
+                uint32_t s = sp[yMin - y0];
+                if((s & 0xFFFFu) != (s >> 16)) break;
+                yMin++;
+            }
+            while(yMax > yMin)
+            {
+                uint32_t s = sp[yMax - 1 - y0];
+                if((s & 0xFFFFu) != (s >> 16)) break;
+                yMax--;
+            }
+            inf.spanOff = (uint32_t)(off + (uint64_t)(yMin - y0));
+        }
+        else
+        {
+            // span scratch full: trim by direct evaluation; k_raster walks the
+            // edges itself for this triangle
+            int32_t l, r;
+            while(yMin < yMax)
+            {
+                span_at(D, X, Y, n, dW, yMin, l, r);
+                if(l != r) break;
+                yMin++;
+            }
+            while(yMax > yMin)
+            {
+                span_at(D, X, Y, n, dW, yMax - 1, l, r);
+                if(l != r) break;
+                yMax--;
+            }
+        }
+        if(yMin < yMax)
+        {
+            // pixel box: covered x satisfy ceil(Xmin/256) <= left <= x < right <= ceil(Xmax/256)
+            int32_t bx0 = max(D.sx0, (xMinS + 0xFF) >> 8);
+            int32_t bx1 = max(bx0, min(D.sx1, (xMaxS + 0xFF) >> 8));
+            {
+                cntVis = 1;
+                box = make_short4((short)bx0, (short)yMin, (short)bx1, (short)yMax);
+                inf.info = (uint32_t)n | ((uint32_t)dW << 5) | ((uint32_t)cntClip << 6) | ((uint32_t)stored << 7);
+                if(cntClip)
+                {
+                    uint32_t slot = atomicAdd(D.polyCount, 1u);
+                    if(slot < D.polyCapacity)
+                    {
+                        inf.slot = slot;
+                        for(int i = 0; i < n; i++) D.poly[(size_t)slot * MAX_POLY + i] = make_int2(X[i], Y[i]);
+                    }
+                    else
+                    {
+                        atomicOr(D.error, ERR_POLY_OVERFLOW);
+                        cntVis = 0;
+                        box = make_short4(0, 0, 0, 0);
+                        inf.info = 0;
                     }
                 }
             }
         }
-        cntClip = clipped;
-        cntVis = visible;
-        cntRej = visible ? 0 : 1;
     }
-    D.tris[t] = rec;  // capacity is a whole number of chunks
-    // chunk box + counters (block reduction)
-    __shared__ int sbox[4][CHUNK / 32];
-    __shared__ int scnt[4][CHUNK / 32];
-    bool has = rec.info != 0;
-    int bx0 = has ? rec.x0 : 0x7FFF, by0 = has ? rec.y0 : 0x7FFF;
-    int bx1 = has ? rec.x1 : -0x8000, by1 = has ? rec.y1 : -0x8000;
+    D.triBox[t] = box;  // capacity is a whole number of setup blocks
+    D.triInfo[t] = inf;
+
+    // ---- chunk boxes (64 triangles = 2 warps) and counters ------------------
+    const bool has = cntVis != 0;
+    int bx0 = has ? box.x : 0x7FFF, by0 = has ? box.y : 0x7FFF;
+    int bx1 = has ? box.z : -0x8000, by1 = has ? box.w : -0x8000;
+    int cntRej = cntIn - cntVis;
+#pragma unroll
     for(int o = 16; o > 0; o >>= 1)
     {
         bx0 = min(bx0, __shfl_xor_sync(0xFFFFFFFFu, bx0, o));
@@ -500,26 +597,33 @@ __global__ void __launch_bounds__(CHUNK) k_setup(const __grid_constant__ DrawPar
         cntClip += __shfl_xor_sync(0xFFFFFFFFu, cntClip, o);
         cntVis += __shfl_xor_sync(0xFFFFFFFFu, cntVis, o);
     }
-    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __shared__ short4 sBox[SETUP_THREADS / 32];
+    __shared__ int sCnt[4][SETUP_THREADS / 32];
     if(lane == 0)
     {
-        sbox[0][warp] = bx0; sbox[1][warp] = by0; sbox[2][warp] = bx1; sbox[3][warp] = by1;
-        scnt[0][warp] = cntIn; scnt[1][warp] = cntRej; scnt[2][warp] = cntClip; scnt[3][warp] = cntVis;
+        sBox[warp] = make_short4((short)bx0, (short)by0, (short)bx1, (short)by1);
+        sCnt[0][warp] = cntIn; sCnt[1][warp] = cntRej; sCnt[2][warp] = cntClip; sCnt[3][warp] = cntVis;
     }
     __syncthreads();
-    if(threadIdx.x == 0)
+    if(threadIdx.x < SETUP_THREADS / CHUNK)
     {
+        const int w0 = threadIdx.x * (CHUNK / 32);
+        short4 b = sBox[w0];
         for(int w = 1; w < CHUNK / 32; w++)
         {
-            bx0 = min(bx0, sbox[0][w]); by0 = min(by0, sbox[1][w]);
-            bx1 = max(bx1, sbox[2][w]); by1 = max(by1, sbox[3][w]);
-            cntIn += scnt[0][w]; cntRej += scnt[1][w]; cntClip += scnt[2][w]; cntVis += scnt[3][w];
+            short4 c = sBox[w0 + w];
+            b.x = min(b.x, c.x); b.y = min(b.y, c.y); b.z = max(b.z, c.z); b.w = max(b.w, c.w);
         }
-        D.chunkBox[blockIdx.x] = make_short4((short)bx0, (short)by0, (short)bx1, (short)by1);
-        atomicAdd(&D.counters[0], (unsigned long long)cntIn);
-        atomicAdd(&D.counters[1], (unsigned long long)cntRej);
-        atomicAdd(&D.counters[2], (unsigned long long)cntClip);
-        atomicAdd(&D.counters[3], (unsigned long long)cntVis);
+        D.chunkBox[blockIdx.x * (SETUP_THREADS / CHUNK) + threadIdx.x] = b;
+    }
+    if(threadIdx.x == 0)
+    {
+        int a = 0, b = 0, c = 0, d = 0;
+        for(int w = 0; w < SETUP_THREADS / 32; w++) { a += sCnt[0][w]; b += sCnt[1][w]; c += sCnt[2][w]; d += sCnt[3][w]; }
+        atomicAdd(&D.counters[0], (unsigned long long)a);
+        atomicAdd(&D.counters[1], (unsigned long long)b);
+        atomicAdd(&D.counters[2], (unsigned long long)c);
+        atomicAdd(&D.counters[3], (unsigned long long)d);
     }
 }
 
@@ -562,11 +666,12 @@ __device__ __forceinline__ uint32_t texel_rgba8(const TexLevel &lv, uint32_t u, 
 }
 
 // sampleQuad2D for one lane, 16-bit channel values c << 8 (SamplerCore.cpp:668-909).
-__device__ __forceinline__ void sample_quad_2d(const DrawParams &D, float u, float v, float lod, int second, uint32_t out[4])
+__device__ __forceinline__ void sample_quad_2d(const DrawParams &D, float u, float v, float lod, int second, uint32_t out[4], uint32_t &lvMask)
 {
     int ilod = D.mipLinear ? trunc_int(lod) : round_int(lod);  // selectMipmap (:2357-2379)
     int li = ilod + second;
     li = li < 0 ? 0 : (li > D.levelCount - 1 ? D.levelCount - 1 : li);
+    lvMask |= 1u << li;
     const TexLevel &lv = D.lv[li];
     uint32_t uu = address16(u, D.addrU);
     uint32_t vv = address16(v, D.addrV);
@@ -600,8 +705,10 @@ __device__ __forceinline__ void sample_quad_2d(const DrawParams &D, float u, flo
 
 // sampleTexture128 on the 16-bit path (SamplerCore.cpp:59-253) with the implicit
 // LOD of computeLod2D (:1376-1422); result scaled by 1 / 0xFF00.
-__device__ void sample_texture_quad(const DrawParams &D, const float u[4], const float v[4], float out[4][4])
+__device__ void sample_texture_quad(const DrawParams &D, const float u[4], const float v[4], int laneMask, float out[4][4], uint32_t &lvMask)
 {
+    // The LOD comes from all four lanes of the quad, covered or not; only the
+    // lanes in laneMask are filtered (the others are never written).
     float lod;
     if(D.minLod == D.maxLod)
         lod = D.minLod;
@@ -619,15 +726,16 @@ __device__ void sample_texture_quad(const DrawParams &D, const float u[4], const
     const float scale = 1.0f / 65280.0f;
     uint32_t utri = 0;
     if(D.mipLinear) utri = (uint32_t)trunc_int(lod * 65536.0f) & 0xFFFFu;
-#pragma unroll
+#pragma unroll 1
     for(int lane = 0; lane < 4; lane++)
     {
+        if(!(laneMask >> lane & 1)) continue;
         uint32_t c[4];
-        sample_quad_2d(D, u[lane], v[lane], lod, 0, c);
+        sample_quad_2d(D, u[lane], v[lane], lod, 0, c, lvMask);
         if(D.mipLinear)  // sampleFilter trilinear blend (:324-379)
         {
             uint32_t cc[4];
-            sample_quad_2d(D, u[lane], v[lane], lod, 1, cc);
+            sample_quad_2d(D, u[lane], v[lane], lod, 1, cc, lvMask);
 #pragma unroll
             for(int k = 0; k < 4; k++) c[k] = (mulhi_u16(c[k], (~utri) & 0xFFFFu) + mulhi_u16(cc[k], utri)) & 0xFFFFu;
         }
@@ -690,22 +798,36 @@ __device__ __forceinline__ bool depth_pass(uint32_t op, float zb, float z)
     }
 }
 
-// Number of per-triangle plane-equation floats staged for a batch:
+// ------------------------------------------------------------------------
+// Raster stage
+// ------------------------------------------------------------------------
+
+// Per-triangle plane-equation floats staged for a batch:
 // x0, y0, z(A,B,C), w(A,B,C), V[k](A,B,C).
 constexpr int PLANES = 8 + 3 * MAXV;
+
+struct QuadEntry {
+    int f;        // fragment sequence number within the batch (primitive order)
+    int16_t ti, qx, y;
+    int16_t mask;
+};
 
 struct RasterShared {
     float depth[BIN * BIN];
     uint32_t color[BIN * BIN];
     float plane[PLANES][BATCH];
-    uint32_t span[BATCH][BIN];        // left | right << 16 per bin row (0 = empty)
-    int16_t qx0[BATCH][BIN / 2];      // first quad x per quad row
-    uint16_t qpre[BATCH][BIN / 2 + 1];
+    uint32_t span[BATCH][BIN];          // left | right << 16 per bin row
+    int16_t qx0[BATCH][BIN / 2];        // first quad x per quad row of the triangle
+    uint16_t qpre[BATCH][BIN / 2 + 1];  // prefix of quads per quad row
+    int8_t qr0[BATCH];                  // first quad row of the triangle in the bin
+    int8_t nqr[BATCH];                  // quad rows of the triangle in the bin
     int triStart[BATCH + 1];
     int chunkList[RASTER_THREADS];
-    int triList[CHUNK];
+    int triList[BATCH + RASTER_THREADS];
     int claim[BIN_QUADS];
+    QuadEntry queue[RASTER_THREADS];
     int warpCount[RASTER_THREADS / 32];
+    int queueCount;
 };
 
 // Block-wide ordered compaction: returns this thread's slot among the
@@ -729,6 +851,8 @@ __device__ __forceinline__ int ordered_compact(bool flag, int *warpCount, int &t
     return flag ? before + __popc(b & ((1u << lane) - 1u)) : -1;
 }
 
+__device__ __forceinline__ uint32_t select3(int o, uint32_t a, uint32_t b, uint32_t c) { return o == 0 ? a : (o == 1 ? b : c); }
+
 __device__ __forceinline__ float vary(const float4 &a, const float4 &b, int k)
 {
     // varying k of a post-transform vertex: float4[2].yzw then float4[3].xyzw
@@ -744,67 +868,76 @@ __device__ __forceinline__ float vary(const float4 &a, const float4 &b, int k)
     }
 }
 
-// R1: setup of one batch triangle -- spans of the bin rows (reference DDA),
-// quad rows, plane equations (SetupRoutine.cpp:270-548).  Returns its quads.
-__device__ int setup_batch_triangle(const DrawParams &D, RasterShared &S, int ti, uint32_t tIdx, int bx0, int by0)
+// R1: one batch triangle -- its span rows inside the bin (from the setup
+// stage's span buffer, or the reference DDA when the buffer was full), its
+// quad rows, and its plane equations (SetupRoutine.cpp:270-548).  Returns the
+// number of quad slots it expands to.
+__device__ int setup_batch_triangle(const DrawParams &D, RasterShared &S, int ti, uint32_t t, int bx0, int by0)
 {
-    TriRec r = D.tris[tIdx];
-    int n = r.info & 31, dW = (r.info >> 5) & 1;
-    uint32_t iv[3];
-    if(D.indexType == SWGB_INDEX_TYPE_NONE) { iv[0] = 3 * tIdx; iv[1] = 3 * tIdx + 1; iv[2] = 3 * tIdx + 2; }
-    else { iv[0] = fetch_index(D, 3 * tIdx); iv[1] = fetch_index(D, 3 * tIdx + 1); iv[2] = fetch_index(D, 3 * tIdx + 2); }
-    float4 V0[3], V1[3], V2[3], V3[3];
-#pragma unroll
-    for(int k = 0; k < 3; k++)
+    const short4 box = D.triBox[t];
+    const TriInfo inf = D.triInfo[t];
+    const int n = inf.info & 31, dW = (inf.info >> 5) & 1;
+    const int rowLo = max((int)box.y, by0), rowHi = min((int)box.w, by0 + BIN);  // bin rows of the triangle
+    const int qrA = (rowLo - by0) >> 1, qrB = (rowHi - 1 - by0) >> 1;            // quad rows [qrA, qrB]
+    // rows outside [rowLo, rowHi) but inside the quad rows are empty
+    S.span[ti][2 * qrA] = 0u;
+    S.span[ti][2 * qrB + 1] = 0u;
+    if(inf.info & 128)
     {
-        const float4 *p = D.ptv + (size_t)iv[k] * 4;
-        V0[k] = p[0]; V1[k] = p[1]; V2[k] = p[2]; V3[k] = p[3];
-    }
-    int32_t X[MAX_POLY], Y[MAX_POLY];
-    if(r.info & 64)
-    {
-        for(int i = 0; i < n; i++)
-        {
-            int2 q = D.poly[(size_t)r.slot * MAX_POLY + i];
-            X[i] = q.x; Y[i] = q.y;
-        }
+        const uint32_t *sp = D.spans + inf.spanOff + (rowLo - box.y);
+        for(int y = rowLo; y < rowHi; y++) S.span[ti][y - by0] = __ldg(sp + (y - rowLo));
     }
     else
     {
-#pragma unroll
-        for(int k = 0; k < 3; k++) { X[k] = __float_as_int(V1[k].x); Y[k] = __float_as_int(V1[k].y); }
-    }
-    // spans of the bin rows inside [yMin, yMax); the last edge writing a row wins
-    const int rowLo = max((int)r.y0, by0), rowHi = min((int)r.y1, by0 + BIN);
-    for(int y = 0; y < BIN; y++) S.span[ti][y] = 0u;
-    for(int i = 0; i < n; i++)
-    {
-        int ia = i + 1 - dW, ib = i + dW;
-        ia = ia == n ? 0 : ia;
-        ib = ib == n ? 0 : ib;
-        EdgeDDA e;
-        if(!edge_setup(D, X[ia], Y[ia], X[ib], Y[ib], e)) continue;
-        int ys = max(e.yMin, rowLo), ye = min(e.yMax, rowHi);
-        if(ys >= ye) continue;
-        int32_t dd;
-        int32_t x = edge_x_at(e, ys, &dd);
-        for(int y = ys; y < ye; y++)
+        // span scratch was full at setup: walk the edges here (SetupRoutine::edge)
+        uint32_t iv0 = 0, iv1 = 0, iv2 = 0;
+        int32_t X[MAX_POLY], Y[MAX_POLY];
+        if(inf.info & 64)
         {
-            uint32_t xc = (uint32_t)clamp_x(D, x);
-            uint32_t s = S.span[ti][y - by0];
-            S.span[ti][y - by0] = e.right ? ((s & 0xFFFFu) | (xc << 16)) : ((s & 0xFFFF0000u) | xc);
-            x += e.Q;
-            dd += e.R;
-            int32_t of = (-dd) >> 31;
-            dd -= e.D & of;
-            x -= of;
+            for(int i = 0; i < n; i++)
+            {
+                int2 q = D.poly[(size_t)inf.slot * MAX_POLY + i];
+                X[i] = q.x; Y[i] = q.y;
+            }
+        }
+        else
+        {
+            if(D.indexType == SWGB_INDEX_TYPE_NONE) { iv0 = 3 * t; iv1 = 3 * t + 1; iv2 = 3 * t + 2; }
+            else { iv0 = fetch_index(D, 3 * t); iv1 = fetch_index(D, 3 * t + 1); iv2 = fetch_index(D, 3 * t + 2); }
+            float4 a = D.ptv[(size_t)iv0 * 4 + 1], b = D.ptv[(size_t)iv1 * 4 + 1], c = D.ptv[(size_t)iv2 * 4 + 1];
+            X[0] = __float_as_int(a.x); X[1] = __float_as_int(b.x); X[2] = __float_as_int(c.x);
+            Y[0] = __float_as_int(a.y); Y[1] = __float_as_int(b.y); Y[2] = __float_as_int(c.y);
+        }
+        for(int y = rowLo; y < rowHi; y++) S.span[ti][y - by0] = 0u;
+        for(int i = 0; i < n; i++)
+        {
+            int ia = i + 1 - dW, ib = i + dW;
+            ia = ia == n ? 0 : ia;
+            ib = ib == n ? 0 : ib;
+            EdgeDDA e;
+            if(!edge_setup(D, X[ia], Y[ia], X[ib], Y[ib], e)) continue;
+            int ys = max(e.yMin, rowLo), ye = min(e.yMax, rowHi);
+            if(ys >= ye) continue;
+            int32_t dd;
+            int32_t x = edge_x_at(e, ys, &dd);
+            uint16_t *h = reinterpret_cast<uint16_t *>(&S.span[ti][0]) + (e.right ? 1 : 0);
+            for(int y = ys; y < ye; y++)
+            {
+                h[2 * (y - by0)] = (uint16_t)clamp_x(D, x);
+                x += e.Q;
+                dd += e.R;
+                int32_t of = (-dd) >> 31;
+                dd -= e.D & of;
+                x -= of;
+            }
         }
     }
     // quad rows: x range of the row pair (QuadRasterizer.cpp:96-123), clipped to the bin
     int pre = 0;
-    for(int qr = 0; qr < BIN / 2; qr++)
+    for(int qr = qrA; qr <= qrB; qr++)
     {
-        S.qpre[ti][qr] = (uint16_t)pre;
+        const int k = qr - qrA;
+        S.qpre[ti][k] = (uint16_t)pre;
         uint32_t s0 = S.span[ti][2 * qr], s1 = S.span[ti][2 * qr + 1];
         int l0 = s0 & 0xFFFF, r0 = s0 >> 16, l1 = s1 & 0xFFFF, r1 = s1 >> 16;
         bool e0 = l0 >= r0, e1 = l1 >= r1;
@@ -817,29 +950,42 @@ __device__ int setup_batch_triangle(const DrawParams &D, RasterShared &S, int ti
             xb = min(xb, bx0 + BIN);
             cnt = xb > xa ? (xb - xa + 1) >> 1 : 0;
         }
-        S.qx0[ti][qr] = (int16_t)xa;
+        S.qx0[ti][k] = (int16_t)xa;
         pre += cnt;
     }
-    S.qpre[ti][BIN / 2] = (uint16_t)pre;
+    S.qpre[ti][qrB - qrA + 1] = (uint16_t)pre;
+    S.qr0[ti] = (int8_t)qrA;
+    S.nqr[ti] = (int8_t)(qrB - qrA + 1);
 
+    // plane equations from the post-transform vertices (L2 resident)
+    uint32_t i0, i1, i2;
+    if(D.indexType == SWGB_INDEX_TYPE_NONE) { i0 = 3 * t; i1 = 3 * t + 1; i2 = 3 * t + 2; }
+    else { i0 = fetch_index(D, 3 * t); i1 = fetch_index(D, 3 * t + 1); i2 = fetch_index(D, 3 * t + 2); }
+    const float4 c0 = D.ptv[(size_t)i0 * 4], c1 = D.ptv[(size_t)i1 * 4], c2 = D.ptv[(size_t)i2 * 4];
     // sort by minimum y, then maximum w (SetupRoutine.cpp:270-294)
-    int o0 = 0, o1 = 1, o2 = 2, t;
+    int o0 = 0, o1 = 1, o2 = 2, tt;
     {
-        float y0 = V0[0].y, y1 = V0[1].y, y2 = V0[2].y;
-        float ym = rmin(rmin(y0, y1), y2);
-        if(ym == y1) { t = o0; o0 = o1; o1 = o2; o2 = t; }
-        if(ym == y2) { t = o2; o2 = o1; o1 = o0; o0 = t; }
+        float ym = rmin(rmin(c0.y, c1.y), c2.y);
+        if(ym == c1.y) { tt = o0; o0 = o1; o1 = o2; o2 = tt; }
+        if(ym == c2.y) { tt = o2; o2 = o1; o1 = o0; o0 = tt; }
     }
+    const float cw0 = c0.w, cw1 = c1.w, cw2 = c2.w;
     {
-        float w0 = V0[o0].w, w1 = V0[o1].w, w2 = V0[o2].w;
+        float w0 = o0 == 0 ? cw0 : (o0 == 1 ? cw1 : cw2);
+        float w1 = o1 == 0 ? cw0 : (o1 == 1 ? cw1 : cw2);
+        float w2 = o2 == 0 ? cw0 : (o2 == 1 ? cw1 : cw2);
         float wm = rmax(rmax(w0, w1), w2);
-        if(wm == w1) { t = o0; o0 = o1; o1 = o2; o2 = t; }
-        if(wm == w2) { t = o2; o2 = o1; o1 = o0; o0 = t; }
+        if(wm == w1) { tt = o0; o0 = o1; o1 = o2; o2 = tt; }
+        if(wm == w2) { tt = o2; o2 = o1; o1 = o0; o0 = tt; }
     }
-    const float w1 = V0[o1].w, w2 = V0[o2].w;
-    const float rhw0 = V2[o0].x;
-    int32_t X0 = __float_as_int(V1[o0].x), X1 = __float_as_int(V1[o1].x), X2 = __float_as_int(V1[o2].x);
-    int32_t Y0 = __float_as_int(V1[o0].y), Y1 = __float_as_int(V1[o1].y), Y2 = __float_as_int(V1[o2].y);
+    const uint32_t j0 = select3(o0, i0, i1, i2), j1 = select3(o1, i0, i1, i2), j2 = select3(o2, i0, i1, i2);
+    const float w1 = o1 == 0 ? cw0 : (o1 == 1 ? cw1 : cw2);
+    const float w2 = o2 == 0 ? cw0 : (o2 == 1 ? cw1 : cw2);
+    const float4 P0 = D.ptv[(size_t)j0 * 4 + 1], P1 = D.ptv[(size_t)j1 * 4 + 1], P2 = D.ptv[(size_t)j2 * 4 + 1];
+    const float4 A0 = D.ptv[(size_t)j0 * 4 + 2], A1 = D.ptv[(size_t)j1 * 4 + 2], A2 = D.ptv[(size_t)j2 * 4 + 2];
+    const float rhw0 = A0.x;
+    int32_t X0 = __float_as_int(P0.x), X1 = __float_as_int(P1.x), X2 = __float_as_int(P2.x);
+    int32_t Y0 = __float_as_int(P0.y), Y1 = __float_as_int(P1.y), Y2 = __float_as_int(P2.y);
     const float inv = 1.0f / 256.0f;
     S.plane[0][ti] = (float)X0 * inv;
     S.plane[1][ti] = (float)Y0 * inv;
@@ -865,7 +1011,7 @@ __device__ int setup_batch_triangle(const DrawParams &D, RasterShared &S, int ti
     S.plane[7][ti] = (M0z + M1z) + M2z;
     if(D.depthTest)
     {
-        float z0 = V1[o0].w, z1 = V1[o1].w - z0, z2 = V1[o2].w - z0;
+        float z0 = P0.w, z1 = P1.w - z0, z2 = P2.w - z0;
         float fx1 = (float)X1 * inv, fy1 = (float)Y1 * inv;
         float fx2 = (float)X2 * inv, fy2 = (float)Y2 * inv;
         float Dz = D.depthRange / (fx1 * fy2 - fx2 * fy1);
@@ -873,19 +1019,40 @@ __device__ int setup_batch_triangle(const DrawParams &D, RasterShared &S, int ti
         S.plane[3][ti] = (fx1 * z2 - fx2 * z1) * Dz;
         S.plane[4][ti] = z0 * D.depthRange + D.depthNear;
     }
-    for(int k = 0; k < D.nv; k++)
+    float4 B0 = make_float4(0, 0, 0, 0), B1 = B0, B2 = B0;
+    if(D.nv > 3)
     {
-        float i0 = vary(V2[o0], V3[o0], k), i1 = vary(V2[o1], V3[o1], k), i2 = vary(V2[o2], V3[o2], k);
-        S.plane[8 + 3 * k + 0][ti] = (i0 * M0x + i1 * M1x) + i2 * M2x;
-        S.plane[8 + 3 * k + 1][ti] = (i0 * M0y + i1 * M1y) + i2 * M2y;
-        S.plane[8 + 3 * k + 2][ti] = (i0 * M0z + i1 * M1z) + i2 * M2z;
+        B0 = D.ptv[(size_t)j0 * 4 + 3]; B1 = D.ptv[(size_t)j1 * 4 + 3]; B2 = D.ptv[(size_t)j2 * 4 + 3];
+    }
+#pragma unroll
+    for(int k = 0; k < MAXV; k++)
+    {
+        if(k >= D.nv) break;
+        float v0 = vary(A0, B0, k), v1 = vary(A1, B1, k), v2 = vary(A2, B2, k);
+        S.plane[8 + 3 * k + 0][ti] = (v0 * M0x + v1 * M1x) + v2 * M2x;
+        S.plane[8 + 3 * k + 1][ti] = (v0 * M0y + v1 * M1y) + v2 * M2y;
+        S.plane[8 + 3 * k + 2][ti] = (v0 * M0z + v1 * M1z) + v2 * M2z;
     }
     return pre;
 }
 
+__device__ __forceinline__ void quad_depth(const DrawParams &D, const RasterShared &S, int ti, int qx, int y, float zq[4])
+{
+    const float x0p = S.plane[0][ti], y0p = S.plane[1][ti];
+    const float zA = S.plane[2][ti], zB = S.plane[3][ti], zC = S.plane[4][ti];
+#pragma unroll
+    for(int i = 0; i < 4; i++)
+    {
+        float xF = ((float)qx + (float)(i & 1)) - x0p;
+        float yF = ((float)y + (float)(i >> 1)) - y0p;
+        float z = mul_add(xF, zA, zC + yF * zB);
+        zq[i] = rmin(rmax(z, D.minDepthClamp), D.maxDepthClamp);  // clampDepth
+    }
+}
+
 // R2: interpolation + fixed fragment shader of one 2x2 quad
 // (PixelRoutine::quad :124-261, PixelProgram::executeShader/clampColor).
-__device__ __forceinline__ void shade_quad(const DrawParams &D, const RasterShared &S, int ti, int qx, int y, float zq[4], float col[4][4])
+__device__ __forceinline__ void shade_quad(const DrawParams &D, const RasterShared &S, int ti, int qx, int y, int laneMask, float col[4][4], uint32_t &lvMask)
 {
     const float x0p = S.plane[0][ti], y0p = S.plane[1][ti];
     float xF[4], yF[4];
@@ -894,16 +1061,6 @@ __device__ __forceinline__ void shade_quad(const DrawParams &D, const RasterShar
     {
         xF[i] = ((float)qx + (float)(i & 1)) - x0p;
         yF[i] = ((float)y + (float)(i >> 1)) - y0p;
-    }
-    if(D.depthTest)
-    {
-        const float zA = S.plane[2][ti], zB = S.plane[3][ti], zC = S.plane[4][ti];
-#pragma unroll
-        for(int i = 0; i < 4; i++)
-        {
-            float z = mul_add(xF[i], zA, zC + yF[i] * zB);
-            zq[i] = rmin(rmax(z, D.minDepthClamp), D.maxDepthClamp);  // clampDepth
-        }
     }
     float rhw[4];
     {
@@ -922,8 +1079,8 @@ __device__ __forceinline__ void shade_quad(const DrawParams &D, const RasterShar
     }
     if(D.fs == SWGB_FS_TEX_X_VCOLOR)
     {
-        float tex[4][4];
-        sample_texture_quad(D, vin[4], vin[5], tex);
+        float tex[4][4] = {};
+        sample_texture_quad(D, vin[4], vin[5], laneMask, tex, lvMask);
 #pragma unroll
         for(int i = 0; i < 4; i++)
 #pragma unroll
@@ -998,6 +1155,141 @@ __device__ __forceinline__ void rop_quad(const DrawParams &D, RasterShared &S, i
     }
 }
 
+// One batch of nb triangles (primitive order) against the staged bin: R1
+// setup, a scan of quad counts, then rounds of 256 quad slots: coverage and
+// early depth rejection (phase A) compact the live quads into a queue, which
+// is shaded densely and resolved per quad in primitive order (phase B).
+__device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared &S, int nb, int bx0, int by0,
+                                          unsigned long long &nQuads, unsigned long long &nTested,
+                                          unsigned long long &nPassed, uint32_t &lvMask)
+{
+    const int tid = threadIdx.x;
+    int myQuads = 0;
+    if(tid < nb) myQuads = setup_batch_triangle(D, S, tid, (uint32_t)S.triList[tid], bx0, by0);
+    {
+        int lane = tid & 31, warp = tid >> 5;
+        int v = myQuads;
+#pragma unroll
+        for(int o = 1; o < 32; o <<= 1)
+        {
+            int u = __shfl_up_sync(0xFFFFFFFFu, v, o);
+            if(lane >= o) v += u;
+        }
+        if(lane == 31) S.warpCount[warp] = v;
+        if(tid == 0) S.queueCount = 0;
+        __syncthreads();
+        int before = 0;
+        for(int w = 0; w < warp; w++) before += S.warpCount[w];
+        if(tid < nb) S.triStart[tid] = before + v - myQuads;
+        if(tid == RASTER_THREADS - 1) S.triStart[BATCH] = before + v;
+        __syncthreads();
+    }
+    const int totalQuads = S.triStart[BATCH];
+    // Depth only moves one way under LESS/LESS_OR_EQUAL (down) and GREATER/
+    // GREATER_OR_EQUAL (up) with clamped, never-NaN fragment depth, so a lane
+    // that fails against the bin's current depth fails at its ordered turn too.
+    const bool earlyZ = D.depthTest && (D.compareOp == SWGB_COMPARE_LESS || D.compareOp == SWGB_COMPARE_LESS_OR_EQUAL ||
+                                        D.compareOp == SWGB_COMPARE_GREATER || D.compareOp == SWGB_COMPARE_GREATER_OR_EQUAL);
+    for(int f0 = 0; f0 < totalQuads; f0 += RASTER_THREADS)
+    {
+        // ---- phase A: locate, cover, early depth test, enqueue ------------
+        const int f = f0 + tid;
+        bool live = false;
+        QuadEntry qe;
+        if(f < totalQuads)
+        {
+            int lo = 0, hi = nb - 1;
+            while(lo < hi)
+            {
+                int mid = (lo + hi + 1) >> 1;
+                if(S.triStart[mid] <= f) lo = mid; else hi = mid - 1;
+            }
+            const int ti = lo;
+            const int local = f - S.triStart[ti];
+            int k = 0;
+            const int nq = S.nqr[ti];
+            while(k < nq - 1 && (int)S.qpre[ti][k + 1] <= local) k++;
+            const int qr = S.qr0[ti] + k;
+            const int qx = S.qx0[ti][k] + 2 * (local - (int)S.qpre[ti][k]);
+            const int y = by0 + 2 * qr;
+            uint32_t s0 = S.span[ti][2 * qr], s1 = S.span[ti][2 * qr + 1];
+            int l0 = s0 & 0xFFFF, r0 = s0 >> 16, l1 = s1 & 0xFFFF, r1 = s1 >> 16;
+            // per-lane coverage: left <= x < right (QuadRasterizer.cpp:184-209)
+            int cMask = 0;
+            if(qx >= l0 && qx < r0) cMask |= 1;
+            if(qx + 1 >= l0 && qx + 1 < r0) cMask |= 2;
+            if(qx >= l1 && qx < r1) cMask |= 4;
+            if(qx + 1 >= l1 && qx + 1 < r1) cMask |= 8;
+            if(cMask)
+            {
+                nQuads++;
+                if(earlyZ)
+                {
+                    float zq[4];
+                    quad_depth(D, S, ti, qx, y, zq);
+                    const int lx = qx - bx0, ly = 2 * qr;
+                    int keep = 0;
+#pragma unroll
+                    for(int i = 0; i < 4; i++)
+                        if((cMask >> i & 1) && depth_pass(D.compareOp, S.depth[(ly + (i >> 1)) * BIN + lx + (i & 1)], zq[i]))
+                            keep |= 1 << i;
+                    nTested += __popc(cMask & ~keep);
+                    cMask = keep;
+                }
+                if(cMask)
+                {
+                    live = true;
+                    qe.f = f;
+                    qe.ti = (int16_t)ti;
+                    qe.qx = (int16_t)qx;
+                    qe.y = (int16_t)y;
+                    qe.mask = (int16_t)cMask;
+                }
+            }
+        }
+        {
+            unsigned b = __ballot_sync(0xFFFFFFFFu, live);
+            int lane = tid & 31;
+            int base = 0;
+            if(lane == 0 && b) base = atomicAdd(&S.queueCount, __popc(b));
+            base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            if(live) S.queue[base + __popc(b & ((1u << lane) - 1u))] = qe;
+        }
+        __syncthreads();
+        const int nLive = S.queueCount;
+        // ---- phase B: shade densely, resolve in primitive order ------------
+        int cMask = 0, lx = 0, ly = 0, fq = 0;
+        float zq[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        float col[4][4];
+        if(tid < nLive)
+        {
+            const QuadEntry e = S.queue[tid];
+            fq = e.f;
+            cMask = e.mask;
+            lx = e.qx - bx0;
+            ly = e.y - by0;
+            if(D.depthTest) quad_depth(D, S, e.ti, e.qx, e.y, zq);
+            shade_quad(D, S, e.ti, e.qx, e.y, cMask, col, lvMask);
+        }
+        __syncthreads();
+        if(tid == 0) S.queueCount = 0;
+        const int qIndex = (ly >> 1) * (BIN / 2) + (lx >> 1);
+        bool pending = cMask != 0;
+        for(;;)
+        {
+            if(pending) atomicMin(&S.claim[qIndex], fq);
+            __syncthreads();
+            if(pending && S.claim[qIndex] == fq)
+            {
+                rop_quad(D, S, lx, ly, cMask, zq, col, nTested, nPassed);
+                S.claim[qIndex] = 0x7FFFFFFF;
+                pending = false;
+            }
+            if(!__syncthreads_or(pending)) break;
+        }
+    }
+}
+
 __global__ void __launch_bounds__(RASTER_THREADS) k_raster(const __grid_constant__ DrawParams D)
 {
     extern __shared__ __align__(16) uint8_t smem_raw[];
@@ -1042,8 +1334,11 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_raster(const __grid_constant
     __syncthreads();
 
     unsigned long long nQuads = 0, nTested = 0, nPassed = 0;
+    uint32_t lvMask = 0;
 
-    // ---- chunks in primitive order ----------------------------------------
+    // ---- chunks in primitive order; triangles accumulate into full batches ----
+    constexpr int CHUNKS_PER_PASS = RASTER_THREADS / CHUNK;
+    int listCount = 0;  // block-uniform
     for(int cbase = 0; cbase < D.nchunks; cbase += RASTER_THREADS)
     {
         int c = cbase + tid;
@@ -1057,110 +1352,50 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_raster(const __grid_constant
         int slot = ordered_compact(hit, S.warpCount, nHit);
         if(hit) S.chunkList[slot] = c;
         __syncthreads();
-        for(int h = 0; h < nHit; h++)
+        for(int h = 0; h < nHit; h += CHUNKS_PER_PASS)
         {
-            const int chunk = S.chunkList[h];
-            const uint32_t tri = (uint32_t)chunk * CHUNK + tid;
+            const int hc = h + tid / CHUNK;
             bool th = false;
-            if(tri < D.count)
+            uint32_t tri = 0;
+            if(hc < nHit)
             {
-                TriRec r = D.tris[tri];
-                th = r.info != 0 && r.x0 < bx0 + BIN && r.x1 > bx0 && r.y0 < by0 + BIN && r.y1 > by0;
+                tri = (uint32_t)S.chunkList[hc] * CHUNK + (tid % CHUNK);
+                if(tri < D.count)
+                {
+                    short4 r = D.triBox[tri];
+                    th = r.x < r.z && r.x < bx0 + BIN && r.z > bx0 && r.y < by0 + BIN && r.w > by0;
+                }
             }
             int nTri;
             int ts = ordered_compact(th, S.warpCount, nTri);
-            if(th) S.triList[ts] = (int)tri;
+            if(th) S.triList[listCount + ts] = (int)tri;
+            listCount += nTri;
             __syncthreads();
-            for(int b0 = 0; b0 < nTri; b0 += BATCH)
+            while(listCount >= BATCH)
             {
-                const int nb = min(BATCH, nTri - b0);
-                int myQuads = 0;
-                if(tid < nb) myQuads = setup_batch_triangle(D, S, tid, (uint32_t)S.triList[b0 + tid], bx0, by0);
-                // exclusive scan of quad counts (primitive order)
-                {
-                    int lane = tid & 31, warp = tid >> 5;
-                    int v = myQuads;
-#pragma unroll
-                    for(int o = 1; o < 32; o <<= 1)
-                    {
-                        int u = __shfl_up_sync(0xFFFFFFFFu, v, o);
-                        if(lane >= o) v += u;
-                    }
-                    if(lane == 31) S.warpCount[warp] = v;
-                    __syncthreads();
-                    int before = 0;
-                    for(int w = 0; w < warp; w++) before += S.warpCount[w];
-                    if(tid < nb) S.triStart[tid] = before + v - myQuads;
-                    if(tid == RASTER_THREADS - 1) S.triStart[BATCH] = before + v;
-                    __syncthreads();
-                }
-                const int totalQuads = S.triStart[BATCH];
-                for(int f0 = 0; f0 < totalQuads; f0 += RASTER_THREADS)
-                {
-                    const int f = f0 + tid;
-                    int cMask = 0, lx = 0, ly = 0;
-                    float zq[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-                    float col[4][4];
-                    if(f < totalQuads)
-                    {
-                        int lo = 0, hi = nb - 1;
-                        while(lo < hi)
-                        {
-                            int mid = (lo + hi + 1) >> 1;
-                            if(S.triStart[mid] <= f) lo = mid; else hi = mid - 1;
-                        }
-                        const int ti = lo;
-                        const int local = f - S.triStart[ti];
-                        int qr = 0;
-                        while(qr < BIN / 2 - 1 && (int)S.qpre[ti][qr + 1] <= local) qr++;
-                        const int qx = S.qx0[ti][qr] + 2 * (local - (int)S.qpre[ti][qr]);
-                        const int y = by0 + 2 * qr;
-                        uint32_t s0 = S.span[ti][2 * qr], s1 = S.span[ti][2 * qr + 1];
-                        int l0 = s0 & 0xFFFF, r0 = s0 >> 16, l1 = s1 & 0xFFFF, r1 = s1 >> 16;
-                        // per-lane coverage: left <= x < right (QuadRasterizer.cpp:184-209)
-                        if(qx >= l0 && qx < r0) cMask |= 1;
-                        if(qx + 1 >= l0 && qx + 1 < r0) cMask |= 2;
-                        if(qx >= l1 && qx < r1) cMask |= 4;
-                        if(qx + 1 >= l1 && qx + 1 < r1) cMask |= 8;
-                        lx = qx - bx0;
-                        ly = 2 * qr;
-                        if(cMask)
-                        {
-                            nQuads++;
-                            shade_quad(D, S, ti, qx, y, zq, col);
-                        }
-                    }
-                    // ordered resolve: per quad, fragments apply in primitive order
-                    const int qIndex = (ly >> 1) * (BIN / 2) + (lx >> 1);
-                    bool pending = cMask != 0;
-                    for(;;)
-                    {
-                        if(pending) atomicMin(&S.claim[qIndex], f);
-                        __syncthreads();
-                        if(pending && S.claim[qIndex] == f)
-                        {
-                            rop_quad(D, S, lx, ly, cMask, zq, col, nTested, nPassed);
-                            S.claim[qIndex] = 0x7FFFFFFF;
-                            pending = false;
-                        }
-                        if(!__syncthreads_or(pending)) break;
-                    }
-                }
+                raster_batch(D, S, BATCH, bx0, by0, nQuads, nTested, nPassed, lvMask);
+                int rem = listCount - BATCH;
+                int v = tid < rem ? S.triList[BATCH + tid] : 0;
+                __syncthreads();
+                if(tid < rem) S.triList[tid] = v;
+                listCount = rem;
+                __syncthreads();
             }
-            __syncthreads();
         }
         __syncthreads();
     }
+    if(listCount > 0) raster_batch(D, S, listCount, bx0, by0, nQuads, nTested, nPassed, lvMask);
+    __syncthreads();
 
     // ---- write the bin back ------------------------------------------------
     for(int i = tid; i < BIN * BIN / 4; i += RASTER_THREADS)
     {
         int ly = i / (BIN / 4), lx = (i % (BIN / 4)) * 4;
         int px = bx0 + lx, py = by0 + ly;
-        if(py >= D.sy1 || px >= D.sx1 || px < D.sx0 || py < D.sy0) continue;
+        if(py >= D.sy1 || px >= D.sx1 || py < D.sy0) continue;
         uint8_t *drow = D.depth + (size_t)py * D.depthPitch;
         uint8_t *crow = D.color + (size_t)py * D.colorPitch;
-        if(D.vec16 && px + 4 <= D.sx1)
+        if(D.vec16 && px + 4 <= D.sx1 && px >= D.sx0)
         {
             if(D.depthWrite) *(float4 *)(drow + (size_t)px * 4) = *(const float4 *)&S.depth[ly * BIN + lx];
             *(uint4 *)(crow + (size_t)px * 4) = *(const uint4 *)&S.color[ly * BIN + lx];
@@ -1169,6 +1404,7 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_raster(const __grid_constant
         {
             for(int k = 0; k < 4 && px + k < D.sx1; k++)
             {
+                if(px + k < D.sx0) continue;
                 if(D.depthWrite) *(float *)(drow + (size_t)(px + k) * 4) = S.depth[ly * BIN + lx + k];
                 *(uint32_t *)(crow + (size_t)(px + k) * 4) = S.color[ly * BIN + lx + k];
             }
@@ -1181,12 +1417,14 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_raster(const __grid_constant
         nQuads += __shfl_xor_sync(0xFFFFFFFFu, nQuads, o);
         nTested += __shfl_xor_sync(0xFFFFFFFFu, nTested, o);
         nPassed += __shfl_xor_sync(0xFFFFFFFFu, nPassed, o);
+        lvMask |= __shfl_xor_sync(0xFFFFFFFFu, lvMask, o);
     }
-    if((tid & 31) == 0 && (nQuads | nTested | nPassed))
+    if((tid & 31) == 0 && (nQuads | nTested | nPassed | lvMask))
     {
         atomicAdd(&D.counters[4], nQuads);
         atomicAdd(&D.counters[5], nTested);
         atomicAdd(&D.counters[6], nPassed);
+        atomicOr(&D.counters[7], (unsigned long long)lvMask);
     }
 }
 
@@ -1202,8 +1440,14 @@ struct swgb_ctx {
     bool ownStream;
     float4 *ptv;
     size_t ptvCap;
-    TriRec *tris;
-    size_t trisCap;
+    short4 *triBox;
+    size_t triBoxCap;
+    TriInfo *triInfo;
+    size_t triInfoCap;
+    uint32_t *spans;
+    size_t spansCap;
+    unsigned long long *spanCount;
+    uint64_t spanRowsLimit;
     short4 *chunkBox;
     size_t chunkCap;
     int2 *poly;
@@ -1213,6 +1457,9 @@ struct swgb_ctx {
     int *error;
     uint64_t launches;
     bool rasterAttr;
+    bool timing;
+    std::vector<cudaEvent_t> *evFree;           // recycled events
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> *evPairs;
 };
 
 namespace {
@@ -1405,17 +1652,61 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
     return SWGB_OK;
 }
 
+cudaEvent_t take_event(swgb_ctx *ctx)
+{
+    cudaEvent_t e = nullptr;
+    if(!ctx->evFree->empty())
+    {
+        e = ctx->evFree->back();
+        ctx->evFree->pop_back();
+    }
+    else
+        cudaEventCreate(&e);
+    return e;
+}
+
+// Launch helper: records a CUDA event pair around the launch when timing is on.
+template<typename F>
+void timed_launch(swgb_ctx *ctx, int kind, F &&launch)
+{
+    cudaEvent_t a = nullptr, b = nullptr;
+    if(ctx->timing)
+    {
+        a = take_event(ctx);
+        b = take_event(ctx);
+        cudaEventRecord(a, ctx->stream);
+    }
+    launch();
+    ctx->launches++;
+    if(ctx->timing)
+    {
+        cudaEventRecord(b, ctx->stream);
+        ctx->evPairs->push_back({kind, {a, b}});
+    }
+}
+
 swgb_status enqueue(swgb_ctx *ctx, DrawParams &D)
 {
     if(D.count == 0) return SWGB_OK;  // Renderer.cpp:187
     swgb_status s;
     if((s = ensure(ctx->ptv, ctx->ptvCap, (size_t)D.vertexCount * 4, "ptv")) != SWGB_OK) return s;
-    if((s = ensure(ctx->tris, ctx->trisCap, (size_t)D.nchunks * CHUNK, "tris")) != SWGB_OK) return s;
-    if((s = ensure(ctx->chunkBox, ctx->chunkCap, (size_t)D.nchunks, "chunk boxes")) != SWGB_OK) return s;
+    const size_t triSlots = ((size_t)D.count + SETUP_THREADS - 1) / SETUP_THREADS * SETUP_THREADS;
+    if((s = ensure(ctx->triBox, ctx->triBoxCap, triSlots, "triangle boxes")) != SWGB_OK) return s;
+    if((s = ensure(ctx->triInfo, ctx->triInfoCap, triSlots, "triangle records")) != SWGB_OK) return s;
+    // span rows: 24 per triangle covers typical meshes; triangles beyond the
+    // capacity fall back to walking their edges in k_raster
+    size_t spanNeed = (size_t)D.count * 24 + 4096;
+    if(ctx->spanRowsLimit && spanNeed > ctx->spanRowsLimit) spanNeed = ctx->spanRowsLimit;
+    if((s = ensure(ctx->spans, ctx->spansCap, spanNeed, "span rows")) != SWGB_OK) return s;
+    if((s = ensure(ctx->chunkBox, ctx->chunkCap, triSlots / CHUNK, "chunk boxes")) != SWGB_OK) return s;
     size_t polyNeed = (size_t)D.count * MAX_POLY;
     if((s = ensure(ctx->poly, ctx->polyCap, polyNeed, "clip polygons")) != SWGB_OK) return s;
     D.ptv = ctx->ptv;
-    D.tris = ctx->tris;
+    D.triBox = ctx->triBox;
+    D.triInfo = ctx->triInfo;
+    D.spans = ctx->spans;
+    D.spanCount = ctx->spanCount;
+    D.spanCapacity = ctx->spanRowsLimit ? (ctx->spansCap < ctx->spanRowsLimit ? ctx->spansCap : ctx->spanRowsLimit) : ctx->spansCap;
     D.chunkBox = ctx->chunkBox;
     D.poly = ctx->poly;
     D.polyCount = ctx->polyCount;
@@ -1428,15 +1719,14 @@ swgb_status enqueue(swgb_ctx *ctx, DrawParams &D)
         ctx->rasterAttr = true;
     }
     const uint32_t nv = D.vertexCount;
-    k_vertex<<<(nv + 255) / 256, 256, 0, ctx->stream>>>(D, nv);
-    k_setup<<<D.nchunks, CHUNK, 0, ctx->stream>>>(D);
+    timed_launch(ctx, SWGB_KERNEL_VERTEX, [&] { k_vertex<<<(nv + 255) / 256, 256, 0, ctx->stream>>>(D, nv); });
+    const uint32_t setupBlocks = (uint32_t)((D.count + SETUP_THREADS - 1) / SETUP_THREADS);
+    timed_launch(ctx, SWGB_KERNEL_SETUP, [&] { k_setup<<<setupBlocks, SETUP_THREADS, 0, ctx->stream>>>(D); });
     if(D.binsX > 0 && D.binsY > 0)
     {
         dim3 grid(D.binsX, D.binsY);
-        k_raster<<<grid, RASTER_THREADS, sizeof(RasterShared), ctx->stream>>>(D);
-        ctx->launches += 1;
+        timed_launch(ctx, SWGB_KERNEL_RASTER, [&] { k_raster<<<grid, RASTER_THREADS, sizeof(RasterShared), ctx->stream>>>(D); });
     }
-    ctx->launches += 2;
     return cuda_check(cudaGetLastError(), "kernel launch");
 }
 
@@ -1460,6 +1750,8 @@ swgb_status swgb_ctx_create(int device, void *stream, swgb_ctx **out)
     swgb_ctx *c = new swgb_ctx();
     memset(c, 0, sizeof(*c));
     c->device = device;
+    c->evFree = new std::vector<cudaEvent_t>();
+    c->evPairs = new std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>>();
     if(stream)
         c->stream = (cudaStream_t)stream;
     else
@@ -1467,7 +1759,9 @@ swgb_status swgb_ctx_create(int device, void *stream, swgb_ctx **out)
         if((s = cuda_check(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream")) != SWGB_OK) { delete c; return s; }
         c->ownStream = true;
     }
+    if(const char *lim = getenv("SWGB_SPAN_ROWS")) c->spanRowsLimit = strtoull(lim, nullptr, 10);
     if((s = cuda_check(cudaMalloc((void **)&c->polyCount, sizeof(uint32_t)), "polyCount")) != SWGB_OK ||
+       (s = cuda_check(cudaMalloc((void **)&c->spanCount, sizeof(unsigned long long)), "spanCount")) != SWGB_OK ||
        (s = cuda_check(cudaMalloc((void **)&c->counters, 8 * sizeof(unsigned long long)), "counters")) != SWGB_OK ||
        (s = cuda_check(cudaMalloc((void **)&c->error, sizeof(int)), "error")) != SWGB_OK)
     {
@@ -1487,13 +1781,26 @@ swgb_status swgb_ctx_destroy(swgb_ctx *c)
     cudaSetDevice(c->device);
     if(c->stream) cudaStreamSynchronize(c->stream);
     cudaFree(c->ptv);
-    cudaFree(c->tris);
+    cudaFree(c->triBox);
+    cudaFree(c->triInfo);
+    cudaFree(c->spans);
+    cudaFree(c->spanCount);
     cudaFree(c->chunkBox);
     cudaFree(c->poly);
     cudaFree(c->polyCount);
     cudaFree(c->counters);
     cudaFree(c->error);
     if(c->ownStream && c->stream) cudaStreamDestroy(c->stream);
+    if(c->evPairs)
+        for(auto &p : *c->evPairs)
+        {
+            cudaEventDestroy(p.second.first);
+            cudaEventDestroy(p.second.second);
+        }
+    if(c->evFree)
+        for(auto e : *c->evFree) cudaEventDestroy(e);
+    delete c->evPairs;
+    delete c->evFree;
     delete c;
     return SWGB_OK;
 }
@@ -1563,7 +1870,7 @@ swgb_status swgb_get_counters(swgb_ctx *ctx, swgb_counters *out)
     out->quads = h[4];
     out->fragments_tested = h[5];
     out->fragments_passed = h[6];
-    out->reserved = 0;
+    out->texture_levels_mask = h[7];
     return SWGB_OK;
 }
 
@@ -1574,5 +1881,34 @@ swgb_status swgb_reset_counters(swgb_ctx *ctx)
 }
 
 uint64_t swgb_launch_count(swgb_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+swgb_status swgb_set_kernel_timing(swgb_ctx *ctx, int enable)
+{
+    if(!ctx) return SWGB_INVALID_ARG;
+    ctx->timing = enable != 0;
+    return SWGB_OK;
+}
+
+swgb_status swgb_get_kernel_times(swgb_ctx *ctx, double ms[SWGB_KERNEL_KINDS], uint32_t launches[SWGB_KERNEL_KINDS])
+{
+    if(!ctx || !ms || !launches) return SWGB_INVALID_ARG;
+    swgb_status s = cuda_check(cudaStreamSynchronize(ctx->stream), "stream sync");
+    if(s != SWGB_OK) return s;
+    for(int k = 0; k < SWGB_KERNEL_KINDS; k++) { ms[k] = 0.0; launches[k] = 0; }
+    for(auto &p : *ctx->evPairs)
+    {
+        float t = 0.0f;
+        cudaEventElapsedTime(&t, p.second.first, p.second.second);
+        if(p.first >= 0 && p.first < SWGB_KERNEL_KINDS)
+        {
+            ms[p.first] += t;
+            launches[p.first]++;
+        }
+        ctx->evFree->push_back(p.second.first);
+        ctx->evFree->push_back(p.second.second);
+    }
+    ctx->evPairs->clear();
+    return SWGB_OK;
+}
 
 }  // extern "C"

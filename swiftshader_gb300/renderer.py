@@ -26,7 +26,10 @@ class Renderer:
         ctx = C.c_void_p()
         handle = None
         if stream is not None:
-            handle = C.c_void_p(stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream))
+            raw = stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+            # handle 0 is the legacy default stream; NULL would ask the library
+            # for a private stream, so pass cudaStreamLegacy (1) instead.
+            handle = C.c_void_p(raw if raw else 1)
         check(self._L.swgb_ctx_create(int(device), handle, C.byref(ctx)), "swgb_ctx_create")
         self._ctx = ctx
 
@@ -53,8 +56,21 @@ class Renderer:
     def launch_count(self):
         return int(self._L.swgb_launch_count(self._ctx))
 
+    def set_kernel_timing(self, enable):
+        check(self._L.swgb_set_kernel_timing(self._ctx, 1 if enable else 0), "swgb_set_kernel_timing")
+
+    KERNEL_NAMES = ("vertex", "setup", "raster")
+
+    def kernel_times(self):
+        """{kernel: (total ms, launches)} since the last call (synchronises)."""
+        ms = (C.c_double * 8)()
+        n = (C.c_uint32 * 8)()
+        check(self._L.swgb_get_kernel_times(self._ctx, ms, n), "swgb_get_kernel_times")
+        return {name: (ms[i], int(n[i])) for i, name in enumerate(self.KERNEL_NAMES) if n[i]}
+
     def set_stream(self, stream):
-        check(self._L.swgb_ctx_set_stream(self._ctx, C.c_void_p(stream.cuda_stream)), "swgb_ctx_set_stream")
+        raw = stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+        check(self._L.swgb_ctx_set_stream(self._ctx, C.c_void_p(raw if raw else 1)), "swgb_ctx_set_stream")
 
     def close(self):
         if getattr(self, "_ctx", None):
