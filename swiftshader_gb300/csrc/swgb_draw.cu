@@ -39,10 +39,11 @@ using namespace swgb;
 namespace {
 
 constexpr int MAXV = 7;          // varying components carried per vertex
-constexpr int BIN = 32;          // bin side in pixels
-constexpr int BIN_QUADS = (BIN / 2) * (BIN / 2);
-constexpr int RASTER_THREADS = 256;
-constexpr int BATCH = 128;       // triangles staged per raster batch
+constexpr int BIN = 16;          // bin side in pixels; one warp owns one bin
+constexpr int RASTER_WARPS = 4;  // independent warps (bins) per raster block
+constexpr int RASTER_THREADS = 32 * RASTER_WARPS;
+constexpr int BATCH = 32;        // triangles staged per batch: one per lane
+constexpr int SUPER = 32;        // chunks per super-chunk box
 constexpr int SETUP_THREADS = 256;
 constexpr int CHUNK = 64;        // triangles per chunk box
 constexpr int MAX_POLY = 16;     // clipped polygon capacity (Polygon::B, src/Device/Polygon.hpp:45)
@@ -118,6 +119,9 @@ struct DrawParams {
     short4 *triBox;       // pixel box per triangle
     TriInfo *triInfo;
     short4 *chunkBox;     // union of the boxes of CHUNK consecutive triangles
+    int4 *superBox;       // union of SUPER consecutive chunk boxes (x0, y0, x1, y1)
+    int nsuper;
+    unsigned int *binQueue;  // next bin for the persistent raster warps
     uint32_t *spans;      // left | right << 16 per triangle row
     unsigned long long *spanCount;
     uint64_t spanCapacity;
@@ -159,7 +163,10 @@ __global__ void k_vertex(const __grid_constant__ DrawParams D, uint32_t nverts)
     {
         *D.polyCount = 0;
         *D.spanCount = 0;
+        *D.binQueue = 0;
     }
+    for(uint32_t j = i; j < (uint32_t)D.nsuper; j += gridDim.x * blockDim.x)
+        D.superBox[j] = make_int4(0x7FFFFFFF, 0x7FFFFFFF, (int)0x80000000, (int)0x80000000);
     if(i >= nverts) return;
     uint32_t index = (D.indexType == SWGB_INDEX_TYPE_NONE ? D.firstVertex + i : i) + (uint32_t)D.baseVertex;
     float p[4];
@@ -615,6 +622,14 @@ __global__ void __launch_bounds__(SETUP_THREADS) k_setup(const __grid_constant__
             b.x = min(b.x, c.x); b.y = min(b.y, c.y); b.z = max(b.z, c.z); b.w = max(b.w, c.w);
         }
         D.chunkBox[blockIdx.x * (SETUP_THREADS / CHUNK) + threadIdx.x] = b;
+        if(b.x < b.z)
+        {
+            int4 *sb = D.superBox + blockIdx.x / (SUPER * CHUNK / SETUP_THREADS);
+            atomicMin(&sb->x, (int)b.x);
+            atomicMin(&sb->y, (int)b.y);
+            atomicMax(&sb->z, (int)b.z);
+            atomicMax(&sb->w, (int)b.w);
+        }
     }
     if(threadIdx.x == 0)
     {
@@ -705,10 +720,12 @@ __device__ __forceinline__ void sample_quad_2d(const DrawParams &D, float u, flo
 
 // sampleTexture128 on the 16-bit path (SamplerCore.cpp:59-253) with the implicit
 // LOD of computeLod2D (:1376-1422); result scaled by 1 / 0xFF00.
-__device__ void sample_texture_quad(const DrawParams &D, const float u[4], const float v[4], int laneMask, float out[4][4], uint32_t &lvMask)
+// sampleTexture128 on the 16-bit path (SamplerCore.cpp:59-253) for lane 'lane'
+// of a quad: the implicit LOD of computeLod2D (:1376-1422) uses lanes 0, 1, 2;
+// the result is scaled by 1 / 0xFF00 (getComponentScale).
+__device__ __forceinline__ void sample_texture_lane(const DrawParams &D, const float u[4], const float v[4], int lane, float out[4],
+                                                    uint32_t &lvMask)
 {
-    // The LOD comes from all four lanes of the quad, covered or not; only the
-    // lanes in laneMask are filtered (the others are never written).
     float lod;
     if(D.minLod == D.maxLod)
         lod = D.minLod;
@@ -723,25 +740,30 @@ __device__ void sample_texture_quad(const DrawParams &D, const float u[4], const
         lod = rmax(lod, D.minLod);
         lod = rmin(lod, D.maxLod);
     }
-    const float scale = 1.0f / 65280.0f;
-    uint32_t utri = 0;
-    if(D.mipLinear) utri = (uint32_t)trunc_int(lod * 65536.0f) & 0xFFFFu;
+    const float ul = lane == 0 ? u[0] : (lane == 1 ? u[1] : (lane == 2 ? u[2] : u[3]));
+    const float vl = lane == 0 ? v[0] : (lane == 1 ? v[1] : (lane == 2 ? v[2] : v[3]));
+    uint32_t c[4], cc[4] = {0u, 0u, 0u, 0u};
+    const int levels = D.mipLinear ? 2 : 1;
 #pragma unroll 1
-    for(int lane = 0; lane < 4; lane++)
+    for(int second = 0; second < levels; second++)
     {
-        if(!(laneMask >> lane & 1)) continue;
-        uint32_t c[4];
-        sample_quad_2d(D, u[lane], v[lane], lod, 0, c, lvMask);
-        if(D.mipLinear)  // sampleFilter trilinear blend (:324-379)
+        uint32_t t[4];
+        sample_quad_2d(D, ul, vl, lod, second, t, lvMask);
+#pragma unroll
+        for(int k = 0; k < 4; k++)
         {
-            uint32_t cc[4];
-            sample_quad_2d(D, u[lane], v[lane], lod, 1, cc, lvMask);
-#pragma unroll
-            for(int k = 0; k < 4; k++) c[k] = (mulhi_u16(c[k], (~utri) & 0xFFFFu) + mulhi_u16(cc[k], utri)) & 0xFFFFu;
+            if(second) cc[k] = t[k]; else c[k] = t[k];
         }
-#pragma unroll
-        for(int k = 0; k < 4; k++) out[lane][k] = __uint2float_rn(c[k]) * scale;
     }
+    if(D.mipLinear)  // sampleFilter trilinear blend (:324-379)
+    {
+        const uint32_t utri = (uint32_t)trunc_int(lod * 65536.0f) & 0xFFFFu;
+#pragma unroll
+        for(int k = 0; k < 4; k++) c[k] = (mulhi_u16(c[k], (~utri) & 0xFFFFu) + mulhi_u16(cc[k], utri)) & 0xFFFFu;
+    }
+    const float scale = 1.0f / 65280.0f;
+#pragma unroll
+    for(int k = 0; k < 4; k++) out[k] = __uint2float_rn(c[k]) * scale;
 }
 
 // ------------------------------------------------------------------------
@@ -806,12 +828,8 @@ __device__ __forceinline__ bool depth_pass(uint32_t op, float zb, float z)
 // x0, y0, z(A,B,C), w(A,B,C), V[k](A,B,C).
 constexpr int PLANES = 8 + 3 * MAXV;
 
-struct QuadEntry {
-    int f;        // fragment sequence number within the batch (primitive order)
-    int16_t ti, qx, y;
-    int16_t mask;
-};
-
+// Shared memory of one warp: its bin's depth and colour, the staged batch,
+// and its ordered candidate list.
 struct RasterShared {
     float depth[BIN * BIN];
     uint32_t color[BIN * BIN];
@@ -821,35 +839,8 @@ struct RasterShared {
     uint16_t qpre[BATCH][BIN / 2 + 1];  // prefix of quads per quad row
     int8_t qr0[BATCH];                  // first quad row of the triangle in the bin
     int8_t nqr[BATCH];                  // quad rows of the triangle in the bin
-    int triStart[BATCH + 1];
-    int chunkList[RASTER_THREADS];
-    int triList[BATCH + RASTER_THREADS];
-    int claim[BIN_QUADS];
-    QuadEntry queue[RASTER_THREADS];
-    int warpCount[RASTER_THREADS / 32];
-    int queueCount;
+    int triList[2 * BATCH];
 };
-
-// Block-wide ordered compaction: returns this thread's slot among the
-// flagged threads (thread order) and the flagged total.
-__device__ __forceinline__ int ordered_compact(bool flag, int *warpCount, int &total)
-{
-    unsigned b = __ballot_sync(0xFFFFFFFFu, flag);
-    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if(lane == 0) warpCount[warp] = __popc(b);
-    __syncthreads();
-    int before = 0;
-    total = 0;
-#pragma unroll
-    for(int w = 0; w < RASTER_THREADS / 32; w++)
-    {
-        int c = warpCount[w];
-        if(w < warp) before += c;
-        total += c;
-    }
-    __syncthreads();
-    return flag ? before + __popc(b & ((1u << lane) - 1u)) : -1;
-}
 
 __device__ __forceinline__ uint32_t select3(int o, uint32_t a, uint32_t b, uint32_t c) { return o == 0 ? a : (o == 1 ? b : c); }
 
@@ -1050,172 +1041,160 @@ __device__ __forceinline__ void quad_depth(const DrawParams &D, const RasterShar
     }
 }
 
-// R2: interpolation + fixed fragment shader of one 2x2 quad
-// (PixelRoutine::quad :124-261, PixelProgram::executeShader/clampColor).
-__device__ __forceinline__ void shade_quad(const DrawParams &D, const RasterShared &S, int ti, int qx, int y, int laneMask, float col[4][4], uint32_t &lvMask)
+// Shades one covered pixel (lane i of the 2x2 quad at (qx, y)) of batch
+// triangle ti: interpolation (PixelRoutine::quad :124-261), the fixed fragment
+// shader with SamplerCore filtering (the LOD comes from lanes 0, 1 and 2 of the
+// quad, covered or not, as the reference's 4-wide SIMD computes it), and the
+// UNORM clamp (PixelProgram::clampColor).
+__device__ __forceinline__ void shade_pixel(const DrawParams &D, const RasterShared &S, int ti, int qx, int y, int i,
+                                            float col[4], uint32_t &lvMask)
 {
     const float x0p = S.plane[0][ti], y0p = S.plane[1][ti];
-    float xF[4], yF[4];
+    const float wA = S.plane[5][ti], wB = S.plane[6][ti], wC = S.plane[7][ti];
+    const float xFi = ((float)qx + (float)(i & 1)) - x0p;
+    const float yFi = ((float)y + (float)(i >> 1)) - y0p;
+    const float rhwI = 1.0f / mul_add(xFi, wA, wC + yFi * wB);
+    float c[4];
 #pragma unroll
-    for(int i = 0; i < 4; i++)
+    for(int k = 0; k < 4; k++)
     {
-        xF[i] = ((float)qx + (float)(i & 1)) - x0p;
-        yF[i] = ((float)y + (float)(i >> 1)) - y0p;
-    }
-    float rhw[4];
-    {
-        const float wA = S.plane[5][ti], wB = S.plane[6][ti], wC = S.plane[7][ti];
-#pragma unroll
-        for(int i = 0; i < 4; i++) rhw[i] = 1.0f / mul_add(xF[i], wA, wC + yF[i] * wB);
-    }
-    float vin[MAXV][4];
-#pragma unroll
-    for(int k = 0; k < MAXV; k++)
-    {
-        if(k >= D.nv) break;
         const float A = S.plane[8 + 3 * k][ti], B = S.plane[9 + 3 * k][ti], C = S.plane[10 + 3 * k][ti];
-#pragma unroll
-        for(int i = 0; i < 4; i++) vin[k][i] = mul_add(xF[i], A, C + yF[i] * B) * rhw[i];
+        c[k] = mul_add(xFi, A, C + yFi * B) * rhwI;
     }
     if(D.fs == SWGB_FS_TEX_X_VCOLOR)
     {
-        float tex[4][4] = {};
-        sample_texture_quad(D, vin[4], vin[5], laneMask, tex, lvMask);
+        const float uA = S.plane[20][ti], uB = S.plane[21][ti], uC = S.plane[22][ti];
+        const float vA = S.plane[23][ti], vB = S.plane[24][ti], vC = S.plane[25][ti];
+        float u[4], v[4];
 #pragma unroll
-        for(int i = 0; i < 4; i++)
+        for(int j = 0; j < 4; j++)
+        {
+            if(j == 3 && i != 3) break;  // lane 3 only feeds itself
+            const float xF = ((float)qx + (float)(j & 1)) - x0p;
+            const float yF = ((float)y + (float)(j >> 1)) - y0p;
+            const float r = j == i ? rhwI : 1.0f / mul_add(xF, wA, wC + yF * wB);
+            u[j] = mul_add(xF, uA, uC + yF * uB) * r;
+            v[j] = mul_add(xF, vA, vC + yF * vB) * r;
+        }
+        float t[4];
+        sample_texture_lane(D, u, v, i, t, lvMask);
 #pragma unroll
-            for(int k = 0; k < 4; k++) col[i][k] = tex[i][k] * vin[k][i];
+        for(int k = 0; k < 4; k++) c[k] = t[k] * c[k];
+    }
+#pragma unroll
+    for(int k = 0; k < 4; k++) col[k] = rmin(rmax(c[k], 0.0f), 1.0f);  // UNORM target
+}
+
+// Depth test/write, blend and RGBA8 write of one pixel of the staged bin
+// (PixelRoutine.cpp:494-574,660-685,1653-1961,1975-1993,2609-2650).
+__device__ __forceinline__ void rop_pixel(const DrawParams &D, RasterShared &S, int idx, float z, const float col[4],
+                                          unsigned long long &nTested, unsigned long long &nPassed)
+{
+    if(D.depthTest)
+    {
+        nTested++;
+        if(!depth_pass(D.compareOp, S.depth[idx], z)) return;
+        if(D.depthWrite) S.depth[idx] = z;
+    }
+    nPassed++;
+    float out[4];
+    const uint32_t old = S.color[idx];
+    if(D.blend)
+    {
+        float dst[4];
+#pragma unroll
+        for(int c = 0; c < 4; c++) dst[c] = (float)(((old >> (8 * c)) & 0xFFu) * 257u) * (1.0f / 0xFFFF);
+        float sf[4], df[4];
+#pragma unroll
+        for(int c = 0; c < 3; c++)
+        {
+            sf[c] = blend_factor(D.srcC, col, dst, c);
+            df[c] = blend_factor(D.dstC, col, dst, c);
+        }
+        sf[3] = blend_factor(D.srcA, col, dst, 3);
+        df[3] = blend_factor(D.dstA, col, dst, 3);
+#pragma unroll
+        for(int c = 0; c < 3; c++) out[c] = blend_op(D.opC, col[c], sf[c], dst[c], df[c]);
+        out[3] = blend_op(D.opA, col[3], sf[3], dst[3], df[3]);
     }
     else
     {
 #pragma unroll
-        for(int i = 0; i < 4; i++)
-#pragma unroll
-            for(int k = 0; k < 4; k++) col[i][k] = vin[k][i];
+        for(int c = 0; c < 4; c++) out[c] = col[c];
     }
+    uint32_t packed = old;
 #pragma unroll
-    for(int i = 0; i < 4; i++)
-#pragma unroll
-        for(int k = 0; k < 4; k++) col[i][k] = rmin(rmax(col[i][k], 0.0f), 1.0f);  // UNORM target
+    for(int c = 0; c < 4; c++)
+    {
+        float v = rmin(rmax(out[c], 0.0f), 1.0f);
+        int32_t r = round_int(v * 255.0f);
+        int32_t s16 = (int32_t)(int16_t)r;
+        uint32_t b = s16 < 0 ? 0u : (s16 > 255 ? 255u : (uint32_t)s16);  // PackUnsigned
+        if(D.writeMask & (1u << c)) packed = (packed & ~(0xFFu << (8 * c))) | (b << (8 * c));
+    }
+    S.color[idx] = packed;
 }
 
-// R3: depth test/write, blend and RGBA8 write of the covered lanes of one quad
-// into the staged bin (PixelRoutine.cpp:494-574,660-685,1653-1961,1975-1993,2609-2650).
-__device__ __forceinline__ void rop_quad(const DrawParams &D, RasterShared &S, int lx, int ly, int cMask, const float zq[4],
-                                         const float col[4][4], unsigned long long &nTested, unsigned long long &nPassed)
+__device__ __forceinline__ int warp_incl_scan(int v, int lane)
 {
 #pragma unroll
-    for(int i = 0; i < 4; i++)
+    for(int o = 1; o < 32; o <<= 1)
     {
-        if(!(cMask & (1 << i))) continue;
-        int idx = (ly + (i >> 1)) * BIN + lx + (i & 1);
-        if(D.depthTest)
-        {
-            nTested++;
-            if(!depth_pass(D.compareOp, S.depth[idx], zq[i])) continue;
-            if(D.depthWrite) S.depth[idx] = zq[i];
-        }
-        nPassed++;
-        float out[4];
-        uint32_t old = S.color[idx];
-        if(D.blend)
-        {
-            float dst[4];
-#pragma unroll
-            for(int c = 0; c < 4; c++) dst[c] = (float)(((old >> (8 * c)) & 0xFFu) * 257u) * (1.0f / 0xFFFF);
-            float sf[4], df[4];
-#pragma unroll
-            for(int c = 0; c < 3; c++)
-            {
-                sf[c] = blend_factor(D.srcC, col[i], dst, c);
-                df[c] = blend_factor(D.dstC, col[i], dst, c);
-            }
-            sf[3] = blend_factor(D.srcA, col[i], dst, 3);
-            df[3] = blend_factor(D.dstA, col[i], dst, 3);
-#pragma unroll
-            for(int c = 0; c < 3; c++) out[c] = blend_op(D.opC, col[i][c], sf[c], dst[c], df[c]);
-            out[3] = blend_op(D.opA, col[i][3], sf[3], dst[3], df[3]);
-        }
-        else
-        {
-#pragma unroll
-            for(int c = 0; c < 4; c++) out[c] = col[i][c];
-        }
-        uint32_t packed = old;
-#pragma unroll
-        for(int c = 0; c < 4; c++)
-        {
-            float v = rmin(rmax(out[c], 0.0f), 1.0f);
-            int32_t r = round_int(v * 255.0f);
-            int32_t s16 = (int32_t)(int16_t)r;
-            uint32_t b = s16 < 0 ? 0u : (s16 > 255 ? 255u : (uint32_t)s16);  // PackUnsigned
-            if(D.writeMask & (1u << c)) packed = (packed & ~(0xFFu << (8 * c))) | (b << (8 * c));
-        }
-        S.color[idx] = packed;
+        int u = __shfl_up_sync(0xFFFFFFFFu, v, o);
+        if(lane >= o) v += u;
     }
+    return v;
 }
 
-// One batch of nb triangles (primitive order) against the staged bin: R1
-// setup, a scan of quad counts, then rounds of 256 quad slots: coverage and
-// early depth rejection (phase A) compact the live quads into a queue, which
-// is shaded densely and resolved per quad in primitive order (phase B).
+// One batch of nb <= 32 triangles (primitive order) against the warp's staged
+// bin.  Lane j sets up triangle j; then the warp expands quad slots, masks
+// coverage, rejects early on depth, and shades the live pixels one per lane;
+// lanes hitting the same pixel resolve lowest lane (earliest triangle) first.
 __device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared &S, int nb, int bx0, int by0,
                                           unsigned long long &nQuads, unsigned long long &nTested,
                                           unsigned long long &nPassed, uint32_t &lvMask)
 {
-    const int tid = threadIdx.x;
-    int myQuads = 0;
-    if(tid < nb) myQuads = setup_batch_triangle(D, S, tid, (uint32_t)S.triList[tid], bx0, by0);
-    {
-        int lane = tid & 31, warp = tid >> 5;
-        int v = myQuads;
-#pragma unroll
-        for(int o = 1; o < 32; o <<= 1)
-        {
-            int u = __shfl_up_sync(0xFFFFFFFFu, v, o);
-            if(lane >= o) v += u;
-        }
-        if(lane == 31) S.warpCount[warp] = v;
-        if(tid == 0) S.queueCount = 0;
-        __syncthreads();
-        int before = 0;
-        for(int w = 0; w < warp; w++) before += S.warpCount[w];
-        if(tid < nb) S.triStart[tid] = before + v - myQuads;
-        if(tid == RASTER_THREADS - 1) S.triStart[BATCH] = before + v;
-        __syncthreads();
-    }
-    const int totalQuads = S.triStart[BATCH];
+    const int lane = threadIdx.x & 31;
+    int cnt = 0;
+    if(lane < nb) cnt = setup_batch_triangle(D, S, lane, (uint32_t)S.triList[lane], bx0, by0);
+    __syncwarp();
     // Depth only moves one way under LESS/LESS_OR_EQUAL (down) and GREATER/
     // GREATER_OR_EQUAL (up) with clamped, never-NaN fragment depth, so a lane
     // that fails against the bin's current depth fails at its ordered turn too.
     const bool earlyZ = D.depthTest && (D.compareOp == SWGB_COMPARE_LESS || D.compareOp == SWGB_COMPARE_LESS_OR_EQUAL ||
                                         D.compareOp == SWGB_COMPARE_GREATER || D.compareOp == SWGB_COMPARE_GREATER_OR_EQUAL);
-    for(int f0 = 0; f0 < totalQuads; f0 += RASTER_THREADS)
+    const int incl = warp_incl_scan(cnt, lane);
+    const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    for(int s0 = 0; s0 < total; s0 += 32)
     {
-        // ---- phase A: locate, cover, early depth test, enqueue ------------
-        const int f = f0 + tid;
-        bool live = false;
-        QuadEntry qe;
-        if(f < totalQuads)
+        // ---- quad slot -> (triangle, quad) -> coverage, early depth ---------
+        const int slot = s0 + lane;
+        int src;
         {
-            int lo = 0, hi = nb - 1;
-            while(lo < hi)
+            int lo = 0, hi = 31;  // smallest lane j with incl_j > slot
+#pragma unroll
+            for(int step = 0; step < 5; step++)
             {
-                int mid = (lo + hi + 1) >> 1;
-                if(S.triStart[mid] <= f) lo = mid; else hi = mid - 1;
+                int mid = (lo + hi) >> 1;
+                int v = __shfl_sync(0xFFFFFFFFu, incl, mid);
+                if(v > slot) hi = mid; else lo = mid + 1;
             }
-            const int ti = lo;
-            const int local = f - S.triStart[ti];
+            src = lo;
+        }
+        const int sIncl = __shfl_sync(0xFFFFFFFFu, incl, src);
+        const int sCnt = __shfl_sync(0xFFFFFFFFu, cnt, src);
+        int cMask = 0, qti = src, qx = 0, qrow = 0;
+        if(slot < total)
+        {
+            const int local = slot - (sIncl - sCnt);
             int k = 0;
-            const int nq = S.nqr[ti];
-            while(k < nq - 1 && (int)S.qpre[ti][k + 1] <= local) k++;
-            const int qr = S.qr0[ti] + k;
-            const int qx = S.qx0[ti][k] + 2 * (local - (int)S.qpre[ti][k]);
-            const int y = by0 + 2 * qr;
-            uint32_t s0 = S.span[ti][2 * qr], s1 = S.span[ti][2 * qr + 1];
-            int l0 = s0 & 0xFFFF, r0 = s0 >> 16, l1 = s1 & 0xFFFF, r1 = s1 >> 16;
+            const int nq = S.nqr[qti];
+            while(k < nq - 1 && (int)S.qpre[qti][k + 1] <= local) k++;
+            qrow = S.qr0[qti] + k;
+            qx = S.qx0[qti][k] + 2 * (local - (int)S.qpre[qti][k]);
+            const uint32_t sp0 = S.span[qti][2 * qrow], sp1 = S.span[qti][2 * qrow + 1];
+            const int l0 = sp0 & 0xFFFF, r0 = sp0 >> 16, l1 = sp1 & 0xFFFF, r1 = sp1 >> 16;
             // per-lane coverage: left <= x < right (QuadRasterizer.cpp:184-209)
-            int cMask = 0;
             if(qx >= l0 && qx < r0) cMask |= 1;
             if(qx + 1 >= l0 && qx + 1 < r0) cMask |= 2;
             if(qx >= l1 && qx < r1) cMask |= 4;
@@ -1226,8 +1205,8 @@ __device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared &S, 
                 if(earlyZ)
                 {
                     float zq[4];
-                    quad_depth(D, S, ti, qx, y, zq);
-                    const int lx = qx - bx0, ly = 2 * qr;
+                    quad_depth(D, S, qti, qx, by0 + 2 * qrow, zq);
+                    const int lx = qx - bx0, ly = 2 * qrow;
                     int keep = 0;
 #pragma unroll
                     for(int i = 0; i < 4; i++)
@@ -1236,73 +1215,110 @@ __device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared &S, 
                     nTested += __popc(cMask & ~keep);
                     cMask = keep;
                 }
-                if(cMask)
-                {
-                    live = true;
-                    qe.f = f;
-                    qe.ti = (int16_t)ti;
-                    qe.qx = (int16_t)qx;
-                    qe.y = (int16_t)y;
-                    qe.mask = (int16_t)cMask;
-                }
             }
         }
+        // ---- live pixels, one per lane --------------------------------------
+        const int np = __popc(cMask);
+        const int pIncl = warp_incl_scan(np, lane);
+        const int pTotal = __shfl_sync(0xFFFFFFFFu, pIncl, 31);
+        for(int p0 = 0; p0 < pTotal; p0 += 32)
         {
-            unsigned b = __ballot_sync(0xFFFFFFFFu, live);
-            int lane = tid & 31;
-            int base = 0;
-            if(lane == 0 && b) base = atomicAdd(&S.queueCount, __popc(b));
-            base = __shfl_sync(0xFFFFFFFFu, base, 0);
-            if(live) S.queue[base + __popc(b & ((1u << lane) - 1u))] = qe;
-        }
-        __syncthreads();
-        const int nLive = S.queueCount;
-        // ---- phase B: shade densely, resolve in primitive order ------------
-        int cMask = 0, lx = 0, ly = 0, fq = 0;
-        float zq[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        float col[4][4];
-        if(tid < nLive)
-        {
-            const QuadEntry e = S.queue[tid];
-            fq = e.f;
-            cMask = e.mask;
-            lx = e.qx - bx0;
-            ly = e.y - by0;
-            if(D.depthTest) quad_depth(D, S, e.ti, e.qx, e.y, zq);
-            shade_quad(D, S, e.ti, e.qx, e.y, cMask, col, lvMask);
-        }
-        __syncthreads();
-        if(tid == 0) S.queueCount = 0;
-        const int qIndex = (ly >> 1) * (BIN / 2) + (lx >> 1);
-        bool pending = cMask != 0;
-        for(;;)
-        {
-            if(pending) atomicMin(&S.claim[qIndex], fq);
-            __syncthreads();
-            if(pending && S.claim[qIndex] == fq)
+            const int pix = p0 + lane;
+            int lo = 0, hi = 31;
+#pragma unroll
+            for(int step = 0; step < 5; step++)
             {
-                rop_quad(D, S, lx, ly, cMask, zq, col, nTested, nPassed);
-                S.claim[qIndex] = 0x7FFFFFFF;
-                pending = false;
+                int mid = (lo + hi) >> 1;
+                int v = __shfl_sync(0xFFFFFFFFu, pIncl, mid);
+                if(v > pix) hi = mid; else lo = mid + 1;
             }
-            if(!__syncthreads_or(pending)) break;
+            const int q = lo;
+            const int qIncl = __shfl_sync(0xFFFFFFFFu, pIncl, q);
+            const int qN = __shfl_sync(0xFFFFFFFFu, np, q);
+            const int qMask = __shfl_sync(0xFFFFFFFFu, cMask, q);
+            const int qTi = __shfl_sync(0xFFFFFFFFu, qti, q);
+            const int qX = __shfl_sync(0xFFFFFFFFu, qx, q);
+            const int qRow = __shfl_sync(0xFFFFFFFFu, qrow, q);
+            const bool valid = pix < pTotal;
+            int pidx = -1 - lane;
+            float z = 0.0f, col[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            if(valid)
+            {
+                int nth = pix - (qIncl - qN);  // the nth set bit of the quad's mask
+                int i = 0;
+#pragma unroll
+                for(int b = 0; b < 4; b++)
+                {
+                    if(qMask >> b & 1)
+                    {
+                        if(nth == 0) i = b;
+                        nth--;
+                    }
+                }
+                const int y = by0 + 2 * qRow;
+                pidx = (2 * qRow + (i >> 1)) * BIN + (qX - bx0) + (i & 1);
+                if(D.depthTest)
+                {
+                    const float xF = ((float)qX + (float)(i & 1)) - S.plane[0][qTi];
+                    const float yF = ((float)y + (float)(i >> 1)) - S.plane[1][qTi];
+                    z = mul_add(xF, S.plane[2][qTi], S.plane[4][qTi] + yF * S.plane[3][qTi]);
+                    z = rmin(rmax(z, D.minDepthClamp), D.maxDepthClamp);  // clampDepth
+                }
+                shade_pixel(D, S, qTi, qX, y, i, col, lvMask);
+            }
+            // ordered resolve: among lanes on the same pixel, lowest lane first
+            unsigned pend = __ballot_sync(0xFFFFFFFFu, valid);
+            while(pend)
+            {
+                const bool mine = (pend >> lane) & 1;
+                const unsigned peers = __match_any_sync(0xFFFFFFFFu, mine ? pidx : -1 - lane);
+                if(mine && (__ffs(peers) - 1) == lane)
+                {
+                    rop_pixel(D, S, pidx, z, col, nTested, nPassed);
+                    pend &= ~(1u << lane);
+                }
+                __syncwarp();
+                pend = __ballot_sync(0xFFFFFFFFu, mine && ((pend >> lane) & 1));
+            }
         }
     }
+    __syncwarp();
+}
+
+__device__ __forceinline__ bool box_hits(short4 b, int bx0, int by0)
+{
+    return b.x < b.z && b.x < bx0 + BIN && b.z > bx0 && b.y < by0 + BIN && b.w > by0;
+}
+
+__device__ __forceinline__ bool box_hits(int4 b, int bx0, int by0)
+{
+    return b.x < b.z && b.x < bx0 + BIN && b.z > bx0 && b.y < by0 + BIN && b.w > by0;
 }
 
 __global__ void __launch_bounds__(RASTER_THREADS) k_raster(const __grid_constant__ DrawParams D)
 {
     extern __shared__ __align__(16) uint8_t smem_raw[];
-    RasterShared &S = *reinterpret_cast<RasterShared *>(smem_raw);
-    const int tid = threadIdx.x;
-    const int bx0 = D.binX0 + (int)blockIdx.x * BIN;
-    const int by0 = D.binY0 + (int)blockIdx.y * BIN;
-
-    // ---- stage the bin's depth and colour in shared memory (16-byte rows) ----
-    for(int i = tid; i < BIN * BIN / 4; i += RASTER_THREADS)
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    RasterShared &S = reinterpret_cast<RasterShared *>(smem_raw)[warp];
+    const int nbins = D.binsX * D.binsY;
+    unsigned long long nQuads = 0, nTested = 0, nPassed = 0;
+    uint32_t lvMask = 0;
+    // Persistent warps: each takes the next bin from the queue until it drains,
+    // so a slow bin never holds idle warps of its block.
+    for(;;)
     {
-        int ly = i / (BIN / 4), lx = (i % (BIN / 4)) * 4;
-        int px = bx0 + lx, py = by0 + ly;
+    int bin = 0;
+    if(lane == 0) bin = (int)atomicAdd(D.binQueue, 1u);
+    bin = __shfl_sync(0xFFFFFFFFu, bin, 0);
+    if(bin >= nbins) break;
+    const int bx0 = D.binX0 + (bin % D.binsX) * BIN;
+    const int by0 = D.binY0 + (bin / D.binsX) * BIN;
+
+    // ---- stage the bin's depth and colour (16-byte row segments) ---------------
+    for(int i = lane; i < BIN * BIN / 4; i += 32)
+    {
+        const int ly = i / (BIN / 4), lx = (i % (BIN / 4)) * 4;
+        const int px = bx0 + lx, py = by0 + ly;
         float4 dz = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
         uint4 cc = make_uint4(0, 0, 0, 0);
         if(py < D.sy1 && px < D.sx1)
@@ -1330,68 +1346,53 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_raster(const __grid_constant
         *(float4 *)&S.depth[ly * BIN + lx] = dz;
         *(uint4 *)&S.color[ly * BIN + lx] = cc;
     }
-    for(int i = tid; i < BIN_QUADS; i += RASTER_THREADS) S.claim[i] = 0x7FFFFFFF;
-    __syncthreads();
+    __syncwarp();
 
-    unsigned long long nQuads = 0, nTested = 0, nPassed = 0;
-    uint32_t lvMask = 0;
-
-    // ---- chunks in primitive order; triangles accumulate into full batches ----
-    constexpr int CHUNKS_PER_PASS = RASTER_THREADS / CHUNK;
-    int listCount = 0;  // block-uniform
-    for(int cbase = 0; cbase < D.nchunks; cbase += RASTER_THREADS)
+    // ---- candidates in primitive order: super-chunk, chunk, triangle boxes -----
+    int listCount = 0;  // warp-uniform
+    for(int sb = 0; sb < D.nsuper; sb += 32)
     {
-        int c = cbase + tid;
-        bool hit = false;
-        if(c < D.nchunks)
+        unsigned superHits = __ballot_sync(0xFFFFFFFFu, sb + lane < D.nsuper && box_hits(D.superBox[sb + lane], bx0, by0));
+        while(superHits)
         {
-            short4 b = D.chunkBox[c];
-            hit = b.x < b.z && b.x < bx0 + BIN && b.z > bx0 && b.y < by0 + BIN && b.w > by0;
-        }
-        int nHit;
-        int slot = ordered_compact(hit, S.warpCount, nHit);
-        if(hit) S.chunkList[slot] = c;
-        __syncthreads();
-        for(int h = 0; h < nHit; h += CHUNKS_PER_PASS)
-        {
-            const int hc = h + tid / CHUNK;
-            bool th = false;
-            uint32_t tri = 0;
-            if(hc < nHit)
+            const int sc = sb + __ffs(superHits) - 1;
+            superHits &= superHits - 1;
+            const int c = sc * SUPER + lane;
+            unsigned chunkHits = __ballot_sync(0xFFFFFFFFu, c < D.nchunks && box_hits(D.chunkBox[c], bx0, by0));
+            while(chunkHits)
             {
-                tri = (uint32_t)S.chunkList[hc] * CHUNK + (tid % CHUNK);
-                if(tri < D.count)
+                const int chunk = sc * SUPER + __ffs(chunkHits) - 1;
+                chunkHits &= chunkHits - 1;
+#pragma unroll
+                for(int half = 0; half < CHUNK / 32; half++)
                 {
-                    short4 r = D.triBox[tri];
-                    th = r.x < r.z && r.x < bx0 + BIN && r.z > bx0 && r.y < by0 + BIN && r.w > by0;
+                    const uint32_t tri = (uint32_t)chunk * CHUNK + half * 32 + lane;
+                    const bool th = tri < D.count && box_hits(D.triBox[tri], bx0, by0);
+                    const unsigned b = __ballot_sync(0xFFFFFFFFu, th);
+                    if(th) S.triList[listCount + __popc(b & ((1u << lane) - 1u))] = (int)tri;
+                    listCount += __popc(b);
+                    __syncwarp();
+                    if(listCount >= BATCH)
+                    {
+                        raster_batch(D, S, BATCH, bx0, by0, nQuads, nTested, nPassed, lvMask);
+                        const int rem = listCount - BATCH;
+                        const int v = lane < rem ? S.triList[BATCH + lane] : 0;
+                        __syncwarp();
+                        if(lane < rem) S.triList[lane] = v;
+                        listCount = rem;
+                        __syncwarp();
+                    }
                 }
             }
-            int nTri;
-            int ts = ordered_compact(th, S.warpCount, nTri);
-            if(th) S.triList[listCount + ts] = (int)tri;
-            listCount += nTri;
-            __syncthreads();
-            while(listCount >= BATCH)
-            {
-                raster_batch(D, S, BATCH, bx0, by0, nQuads, nTested, nPassed, lvMask);
-                int rem = listCount - BATCH;
-                int v = tid < rem ? S.triList[BATCH + tid] : 0;
-                __syncthreads();
-                if(tid < rem) S.triList[tid] = v;
-                listCount = rem;
-                __syncthreads();
-            }
         }
-        __syncthreads();
     }
     if(listCount > 0) raster_batch(D, S, listCount, bx0, by0, nQuads, nTested, nPassed, lvMask);
-    __syncthreads();
 
-    // ---- write the bin back ------------------------------------------------
-    for(int i = tid; i < BIN * BIN / 4; i += RASTER_THREADS)
+    // ---- write the bin back ----------------------------------------------------
+    for(int i = lane; i < BIN * BIN / 4; i += 32)
     {
-        int ly = i / (BIN / 4), lx = (i % (BIN / 4)) * 4;
-        int px = bx0 + lx, py = by0 + ly;
+        const int ly = i / (BIN / 4), lx = (i % (BIN / 4)) * 4;
+        const int px = bx0 + lx, py = by0 + ly;
         if(py >= D.sy1 || px >= D.sx1 || py < D.sy0) continue;
         uint8_t *drow = D.depth + (size_t)py * D.depthPitch;
         uint8_t *crow = D.color + (size_t)py * D.colorPitch;
@@ -1410,8 +1411,11 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_raster(const __grid_constant
             }
         }
     }
+    __syncwarp();
+    }
 
-    // ---- counters ----------------------------------------------------------
+    // ---- counters ----------------------------------------------------------------
+#pragma unroll
     for(int o = 16; o > 0; o >>= 1)
     {
         nQuads += __shfl_xor_sync(0xFFFFFFFFu, nQuads, o);
@@ -1419,7 +1423,7 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_raster(const __grid_constant
         nPassed += __shfl_xor_sync(0xFFFFFFFFu, nPassed, o);
         lvMask |= __shfl_xor_sync(0xFFFFFFFFu, lvMask, o);
     }
-    if((tid & 31) == 0 && (nQuads | nTested | nPassed | lvMask))
+    if(lane == 0 && (nQuads | nTested | nPassed | lvMask))
     {
         atomicAdd(&D.counters[4], nQuads);
         atomicAdd(&D.counters[5], nTested);
@@ -1450,9 +1454,13 @@ struct swgb_ctx {
     uint64_t spanRowsLimit;
     short4 *chunkBox;
     size_t chunkCap;
+    int4 *superBox;
+    size_t superCap;
     int2 *poly;
     size_t polyCap;
     uint32_t *polyCount;
+    unsigned int *binQueue;
+    int rasterBlocks;  // persistent raster grid: SMs x resident blocks per SM
     unsigned long long *counters;
     int *error;
     uint64_t launches;
@@ -1649,6 +1657,7 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
     D.binsX = (D.sx1 - D.binX0 + BIN - 1) / BIN;
     D.binsY = (D.sy1 - D.binY0 + BIN - 1) / BIN;
     D.nchunks = (int)((a->count + CHUNK - 1) / CHUNK);
+    D.nsuper = (D.nchunks + SUPER - 1) / SUPER;
     return SWGB_OK;
 }
 
@@ -1699,6 +1708,7 @@ swgb_status enqueue(swgb_ctx *ctx, DrawParams &D)
     if(ctx->spanRowsLimit && spanNeed > ctx->spanRowsLimit) spanNeed = ctx->spanRowsLimit;
     if((s = ensure(ctx->spans, ctx->spansCap, spanNeed, "span rows")) != SWGB_OK) return s;
     if((s = ensure(ctx->chunkBox, ctx->chunkCap, triSlots / CHUNK, "chunk boxes")) != SWGB_OK) return s;
+    if((s = ensure(ctx->superBox, ctx->superCap, (size_t)D.nsuper, "super-chunk boxes")) != SWGB_OK) return s;
     size_t polyNeed = (size_t)D.count * MAX_POLY;
     if((s = ensure(ctx->poly, ctx->polyCap, polyNeed, "clip polygons")) != SWGB_OK) return s;
     D.ptv = ctx->ptv;
@@ -1708,14 +1718,20 @@ swgb_status enqueue(swgb_ctx *ctx, DrawParams &D)
     D.spanCount = ctx->spanCount;
     D.spanCapacity = ctx->spanRowsLimit ? (ctx->spansCap < ctx->spanRowsLimit ? ctx->spansCap : ctx->spanRowsLimit) : ctx->spansCap;
     D.chunkBox = ctx->chunkBox;
+    D.superBox = ctx->superBox;
     D.poly = ctx->poly;
     D.polyCount = ctx->polyCount;
+    D.binQueue = ctx->binQueue;
     D.polyCapacity = (uint32_t)(ctx->polyCap / MAX_POLY);
     D.counters = ctx->counters;
     D.error = ctx->error;
     if(!ctx->rasterAttr)
     {
-        if((s = cuda_check(cudaFuncSetAttribute(k_raster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(RasterShared)), "raster smem attribute")) != SWGB_OK) return s;
+        if((s = cuda_check(cudaFuncSetAttribute(k_raster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(RASTER_WARPS * sizeof(RasterShared))), "raster smem attribute")) != SWGB_OK) return s;
+        int sms = 0, perSM = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_raster, RASTER_THREADS, RASTER_WARPS * sizeof(RasterShared));
+        ctx->rasterBlocks = (sms > 0 ? sms : 1) * (perSM > 0 ? perSM : 1);
         ctx->rasterAttr = true;
     }
     const uint32_t nv = D.vertexCount;
@@ -1724,8 +1740,9 @@ swgb_status enqueue(swgb_ctx *ctx, DrawParams &D)
     timed_launch(ctx, SWGB_KERNEL_SETUP, [&] { k_setup<<<setupBlocks, SETUP_THREADS, 0, ctx->stream>>>(D); });
     if(D.binsX > 0 && D.binsY > 0)
     {
-        dim3 grid(D.binsX, D.binsY);
-        timed_launch(ctx, SWGB_KERNEL_RASTER, [&] { k_raster<<<grid, RASTER_THREADS, sizeof(RasterShared), ctx->stream>>>(D); });
+        uint32_t blocks = (uint32_t)((D.binsX * D.binsY + RASTER_WARPS - 1) / RASTER_WARPS);
+        if(blocks > (uint32_t)ctx->rasterBlocks) blocks = (uint32_t)ctx->rasterBlocks;
+        timed_launch(ctx, SWGB_KERNEL_RASTER, [&] { k_raster<<<blocks, RASTER_THREADS, RASTER_WARPS * sizeof(RasterShared), ctx->stream>>>(D); });
     }
     return cuda_check(cudaGetLastError(), "kernel launch");
 }
@@ -1762,6 +1779,7 @@ swgb_status swgb_ctx_create(int device, void *stream, swgb_ctx **out)
     if(const char *lim = getenv("SWGB_SPAN_ROWS")) c->spanRowsLimit = strtoull(lim, nullptr, 10);
     if((s = cuda_check(cudaMalloc((void **)&c->polyCount, sizeof(uint32_t)), "polyCount")) != SWGB_OK ||
        (s = cuda_check(cudaMalloc((void **)&c->spanCount, sizeof(unsigned long long)), "spanCount")) != SWGB_OK ||
+       (s = cuda_check(cudaMalloc((void **)&c->binQueue, sizeof(unsigned int)), "binQueue")) != SWGB_OK ||
        (s = cuda_check(cudaMalloc((void **)&c->counters, 8 * sizeof(unsigned long long)), "counters")) != SWGB_OK ||
        (s = cuda_check(cudaMalloc((void **)&c->error, sizeof(int)), "error")) != SWGB_OK)
     {
@@ -1786,8 +1804,10 @@ swgb_status swgb_ctx_destroy(swgb_ctx *c)
     cudaFree(c->spans);
     cudaFree(c->spanCount);
     cudaFree(c->chunkBox);
+    cudaFree(c->superBox);
     cudaFree(c->poly);
     cudaFree(c->polyCount);
+    cudaFree(c->binQueue);
     cudaFree(c->counters);
     cudaFree(c->error);
     if(c->ownStream && c->stream) cudaStreamDestroy(c->stream);
