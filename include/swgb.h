@@ -255,6 +255,26 @@ swgb_status swgb_draw(swgb_ctx *ctx, const swgb_pipeline_state *state, const swg
  * launch fed by a device work queue. */
 swgb_status swgb_draw_batch(swgb_ctx *ctx, const swgb_pipeline_state *states, const swgb_draw_args *args, uint32_t n);
 
+/* Allocation-free draw.  No counterpart in the reference: it exists for
+ * callers of this library that cannot allocate device memory when they draw --
+ * code recording into a CUDA stream capture (cudaMalloc is not capturable), a
+ * host whose device memory belongs to another allocator, or a real-time loop
+ * that must not enter the allocator.  It runs the same kernels as swgb_draw on
+ * 'stream' (a cudaStream_t; NULL = the legacy default stream) on the current
+ * device, with all scratch taken from one fixed __device__ array of about
+ * 14 MiB that every GPU loading this library holds until the process exits.
+ * Limits: at most SWGB_NOALLOC_MAX_TRIANGLES triangles and
+ * SWGB_NOALLOC_MAX_VERTICES transformed vertices per call; larger draws return
+ * SWGB_INVALID_ARG.  The first call on a device resolves the array's device
+ * address, so make it before any stream capture begins.  Every call shares
+ * the one array: calls whose work overlaps on the GPU (different streams, or
+ * several host threads) race and corrupt each other; order them on one stream.
+ * Device-side errors (an index >= vertex_count) drop the triangle silently,
+ * as there is no context to report them through. */
+#define SWGB_NOALLOC_MAX_TRIANGLES 32768u
+#define SWGB_NOALLOC_MAX_VERTICES 98304u
+swgb_status swgb_draw_noalloc(const swgb_pipeline_state *state, const swgb_draw_args *args, void *stream);
+
 /* Waits for every draw enqueued so far (Renderer::synchronize). */
 swgb_status swgb_sync(swgb_ctx *ctx);
 

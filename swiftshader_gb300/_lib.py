@@ -13,7 +13,8 @@ _lib = None
 
 EXPORTS = ["swgb_abi_version", "swgb_last_error", "swgb_ctx_create", "swgb_ctx_destroy",
            "swgb_ctx_set_stream", "swgb_draw", "swgb_draw_batch", "swgb_sync", "swgb_get_counters",
-           "swgb_reset_counters", "swgb_launch_count", "swgb_set_kernel_timing", "swgb_get_kernel_times"]
+           "swgb_reset_counters", "swgb_launch_count", "swgb_set_kernel_timing", "swgb_get_kernel_times",
+           "swgb_draw_noalloc"]
 
 
 class SwgbError(RuntimeError):
@@ -55,6 +56,8 @@ def load(path=None):
     L.swgb_set_kernel_timing.restype = C.c_int
     L.swgb_get_kernel_times.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_uint32)]
     L.swgb_get_kernel_times.restype = C.c_int
+    L.swgb_draw_noalloc.argtypes = [C.POINTER(abi.PipelineState), C.POINTER(abi.DrawArgs), C.c_void_p]
+    L.swgb_draw_noalloc.restype = C.c_int
     if L.swgb_abi_version() != 1:
         raise OSError("libswgb ABI version mismatch")
     _lib = L

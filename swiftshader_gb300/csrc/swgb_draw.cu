@@ -28,6 +28,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1749,6 +1750,72 @@ swgb_status enqueue(swgb_ctx *ctx, DrawParams &D)
 
 }  // namespace
 
+// --------------------------------------------------------------------------
+// Allocation-free draws (swgb_draw_noalloc)
+//
+// Some callers cannot allocate device memory at draw time: a driver-style
+// caller running inside a CUDA stream capture (graph capture forbids
+// cudaMalloc), a caller whose memory pool is owned by another allocator, or a
+// real-time loop that must not touch the allocator.  For them the draw's
+// scratch lives in one file-scope __device__ array of fixed size, which every
+// GPU that loads this library holds until the process exits.
+// --------------------------------------------------------------------------
+
+constexpr size_t NA_ALIGN = 256;
+constexpr size_t na_up(size_t x) { return (x + NA_ALIGN - 1) / NA_ALIGN * NA_ALIGN; }
+constexpr uint32_t NA_TRIS = SWGB_NOALLOC_MAX_TRIANGLES;
+constexpr uint32_t NA_VERTS = SWGB_NOALLOC_MAX_VERTICES;
+constexpr uint32_t NA_SLOTS = (NA_TRIS + SETUP_THREADS - 1) / SETUP_THREADS * SETUP_THREADS;
+constexpr uint32_t NA_CHUNKS = NA_SLOTS / CHUNK;
+constexpr uint32_t NA_SUPER = (NA_CHUNKS + SUPER - 1) / SUPER;
+constexpr uint64_t NA_SPAN_ROWS = (uint64_t)NA_TRIS * 24;
+constexpr size_t NA_OFF_PTV = 0;
+constexpr size_t NA_OFF_BOX = na_up(NA_OFF_PTV + (size_t)NA_VERTS * 4 * sizeof(float4));
+constexpr size_t NA_OFF_INFO = na_up(NA_OFF_BOX + (size_t)NA_SLOTS * sizeof(short4));
+constexpr size_t NA_OFF_CHUNK = na_up(NA_OFF_INFO + (size_t)NA_SLOTS * sizeof(TriInfo));
+constexpr size_t NA_OFF_SUPER = na_up(NA_OFF_CHUNK + (size_t)NA_CHUNKS * sizeof(short4));
+constexpr size_t NA_OFF_SPANS = na_up(NA_OFF_SUPER + (size_t)NA_SUPER * sizeof(int4));
+constexpr size_t NA_OFF_POLY = na_up(NA_OFF_SPANS + (size_t)NA_SPAN_ROWS * sizeof(uint32_t));
+constexpr size_t NA_OFF_WORDS = na_up(NA_OFF_POLY + (size_t)NA_TRIS * MAX_POLY * sizeof(int2));
+// words: counters[8] (u64), spanCount (u64), polyCount (u32), binQueue (u32), error (i32)
+constexpr size_t NA_WORDS_BYTES = 8 * 8 + 8 + 4 + 4 + 4;
+constexpr size_t NA_BYTES = na_up(NA_OFF_WORDS + NA_WORDS_BYTES);
+static_assert(RASTER_WARPS * sizeof(RasterShared) <= 48 * 1024, "the allocation-free raster launch uses the default shared-memory limit");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
+
+struct NoAllocDevice {
+    bool ready;
+    unsigned char *base;  // device address of g_noalloc_scratch on this device
+    int rasterBlocks;
+};
+static NoAllocDevice g_noalloc_dev[64];
+static std::mutex g_noalloc_mu;
+
+// Once per device, with that device current: resolve the device address of
+// the scratch array (the host-side symbol is only a stand-in and must never
+// reach a kernel) and size the persistent raster grid.
+swgb_status noalloc_device(int dev, NoAllocDevice *&out)
+{
+    if(dev < 0 || dev >= 64) return set_error(SWGB_INVALID_ARG, "device index beyond 63");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    NoAllocDevice &d = g_noalloc_dev[dev];
+    if(!d.ready)
+    {
+        void *ptr = nullptr;
+        swgb_status s = cuda_check(cudaGetSymbolAddress(&ptr, g_noalloc_scratch), "cudaGetSymbolAddress(scratch)");
+        if(s != SWGB_OK) return s;
+        int sms = 0, perSM = 0;
+        if((s = cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count")) != SWGB_OK) return s;
+        if((s = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_raster, RASTER_THREADS, RASTER_WARPS * sizeof(RasterShared)), "raster occupancy")) != SWGB_OK) return s;
+        d.base = (unsigned char *)ptr;
+        d.rasterBlocks = (sms > 0 ? sms : 1) * (perSM > 0 ? perSM : 1);
+        d.ready = true;
+    }
+    out = &d;
+    return SWGB_OK;
+}
+
 extern "C" {
 
 int swgb_abi_version(void) { return SWGB_ABI_VERSION; }
@@ -1847,6 +1914,57 @@ swgb_status swgb_draw(swgb_ctx *ctx, const swgb_pipeline_state *st, const swgb_d
     if(s != SWGB_OK) return s;
     cudaSetDevice(ctx->device);
     return enqueue(ctx, D);
+}
+
+// The allocation-free variant of swgb_draw: the same validation, baking and
+// kernels, with every scratch buffer carved out of g_noalloc_scratch.  It calls
+// no cudaMalloc/cudaFree and no allocating library routine.
+swgb_status swgb_draw_noalloc(const swgb_pipeline_state *st, const swgb_draw_args *args, void *stream)
+{
+    if(!st || !args) return set_error(SWGB_INVALID_ARG, "null argument");
+    if(args->count == 0) return SWGB_OK;
+    if(args->count > SWGB_NOALLOC_MAX_TRIANGLES)
+        return set_error(SWGB_INVALID_ARG, "swgb_draw_noalloc: more than SWGB_NOALLOC_MAX_TRIANGLES (32768) triangles");
+    DrawParams D;
+    swgb_status s = bake(st, args, D);
+    if(s != SWGB_OK) return s;
+    if(D.vertexCount > SWGB_NOALLOC_MAX_VERTICES)
+        return set_error(SWGB_INVALID_ARG, "swgb_draw_noalloc: vertex_count above SWGB_NOALLOC_MAX_VERTICES (98304)");
+    int dev = 0;
+    if((s = cuda_check(cudaGetDevice(&dev), "cudaGetDevice")) != SWGB_OK) return s;
+    NoAllocDevice *nd = nullptr;
+    if((s = noalloc_device(dev, nd)) != SWGB_OK) return s;
+    unsigned char *b = nd->base;
+    D.ptv = (float4 *)(b + NA_OFF_PTV);
+    D.triBox = (short4 *)(b + NA_OFF_BOX);
+    D.triInfo = (TriInfo *)(b + NA_OFF_INFO);
+    D.chunkBox = (short4 *)(b + NA_OFF_CHUNK);
+    D.superBox = (int4 *)(b + NA_OFF_SUPER);
+    D.spans = (uint32_t *)(b + NA_OFF_SPANS);
+    D.spanCapacity = NA_SPAN_ROWS;
+    D.poly = (int2 *)(b + NA_OFF_POLY);
+    D.polyCapacity = NA_TRIS;
+    unsigned char *w = b + NA_OFF_WORDS;
+    D.counters = (unsigned long long *)w;
+    D.spanCount = (unsigned long long *)(w + 64);
+    D.polyCount = (uint32_t *)(w + 72);
+    D.binQueue = (unsigned int *)(w + 76);
+    D.error = (int *)(w + 80);
+    cudaStream_t st0 = (cudaStream_t)stream;
+    // The array keeps the previous call's contents: the counters and the error
+    // word are cleared here, the queue heads and super-chunk boxes by k_vertex.
+    if((s = cuda_check(cudaMemsetAsync(w, 0, NA_WORDS_BYTES, st0), "clear scratch words")) != SWGB_OK) return s;
+    const uint32_t nv = D.vertexCount;
+    k_vertex<<<(nv + 255) / 256, 256, 0, st0>>>(D, nv);
+    const uint32_t setupBlocks = (uint32_t)((D.count + SETUP_THREADS - 1) / SETUP_THREADS);
+    k_setup<<<setupBlocks, SETUP_THREADS, 0, st0>>>(D);
+    if(D.binsX > 0 && D.binsY > 0)
+    {
+        uint32_t blocks = (uint32_t)((D.binsX * D.binsY + RASTER_WARPS - 1) / RASTER_WARPS);
+        if(blocks > (uint32_t)nd->rasterBlocks) blocks = (uint32_t)nd->rasterBlocks;
+        k_raster<<<blocks, RASTER_THREADS, RASTER_WARPS * sizeof(RasterShared), st0>>>(D);
+    }
+    return cuda_check(cudaGetLastError(), "kernel launch");
 }
 
 swgb_status swgb_draw_batch(swgb_ctx *ctx, const swgb_pipeline_state *states, const swgb_draw_args *args, uint32_t n)

@@ -1,0 +1,61 @@
+"""swgb_draw_noalloc: the allocation-free draw, for callers that cannot
+allocate device memory while they draw (code recording a CUDA stream capture,
+hosts whose device memory belongs to another allocator, real-time loops).
+
+It must produce exactly the bits of swgb_draw, call after call, although every
+call reuses the same fixed scratch array.  This file is collected last so a
+failure here never hides the other tests' results."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from swiftshader_gb300 import abi, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _noalloc_render(L, scene):
+    import torch
+    from swiftshader_gb300 import DeviceScene
+    ds = DeviceScene(scene)
+    torch.cuda.synchronize()
+    st, a = ds.state(), ds.args()
+    status = L.swgb_draw_noalloc(C.byref(st), C.byref(a), None)
+    assert status == abi.OK, L.swgb_last_error()
+    torch.cuda.synchronize()
+    return ds.color.cpu().numpy(), ds.depth.cpu().numpy()
+
+
+def _ctx_render(scene):
+    from gpu_helpers import render_gpu
+    c, d, _ = render_gpu(scene)
+    return c, d
+
+
+def test_noalloc_matches_draw_twice(gpu_lib):
+    L = gpu_lib
+    first = scenes.scene_heightfield(quads_x=120, quads_y=60, width=320, height=180, tex_size=256)
+    second = scenes.scene_textured_small(n_tris=300, width=150, height=90)
+    for sc in (first, second):
+        c_ref, d_ref = _ctx_render(sc)
+        c, d = _noalloc_render(L, sc)
+        assert np.array_equal(c, c_ref)
+        assert np.array_equal(d.view(np.uint32), d_ref.view(np.uint32))
+    # and the first scene again, after the array holds the second's leftovers
+    c_ref, d_ref = _ctx_render(first)
+    c, d = _noalloc_render(L, first)
+    assert np.array_equal(c, c_ref)
+    assert np.array_equal(d.view(np.uint32), d_ref.view(np.uint32))
+
+
+def test_noalloc_rejects_oversized_draws(gpu_lib):
+    L = gpu_lib
+    sc = scenes.scene_small(n_tris=8, width=32, height=32)
+    st = abi.PipelineState()
+    a = abi.DrawArgs()
+    st = scenes.build_state(sc, 1 << 20, 1 << 20, 1 << 20)  # never dereferenced: rejected first
+    a = scenes.build_args(sc)
+    a.count = 32769
+    assert L.swgb_draw_noalloc(C.byref(st), C.byref(a), None) == abi.INVALID_ARG
+    assert b"32768" in L.swgb_last_error()
