@@ -102,6 +102,17 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(values, device=None):
+    """Element-wise maximum of per-rank timings across the process group
+    (the slowest rank defines a replicated step's time)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor(values, dtype=torch.float64, device=device)
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t.tolist()]
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -233,11 +244,7 @@ def run_ours(args):
     e2e_ms = sum(s.elapsed_time(e) for s, e in zip(e_starts, e_ends)) / args.steps
 
     # max over ranks
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms_per_step, e2e_ms], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_per_step, e2e_ms = float(t[0]), float(t[1])
+    ms_per_step, e2e_ms = max_over_ranks([ms_per_step, e2e_ms], dev)
 
     if rank != 0:
         if world > 1:

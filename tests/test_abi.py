@@ -1,0 +1,96 @@
+"""The C-ABI on the CPU: struct layouts of the ctypes mirror against the
+header (compiled with gcc), the exported symbols of libswgb.so, and host-side
+error handling that needs no device."""
+import ctypes as C
+import os
+import subprocess
+import sys
+
+import pytest
+
+from swiftshader_gb300 import abi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "swgb.h")
+
+STRUCTS = {
+    "swgb_vertex_attrib": abi.VertexAttrib,
+    "swgb_vertex_binding": abi.VertexBinding,
+    "swgb_texture_level": abi.TextureLevel,
+    "swgb_texture": abi.Texture,
+    "swgb_pipeline_state": abi.PipelineState,
+    "swgb_draw_args": abi.DrawArgs,
+    "swgb_counters": abi.Counters,
+}
+
+
+def header_layout(tmp_path):
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "%s"' % HEADER, "int main(void) {"]
+    for cname, py in STRUCTS.items():
+        lines.append('printf("%s %%zu\\n", sizeof(%s));' % (cname, cname))
+        for f, _ in py._fields_:
+            lines.append('printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (cname, f, cname, f))
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.check_call(["gcc", "-std=c11", "-Wall", "-Werror", "-o", str(exe), str(src)])
+    out = subprocess.check_output([str(exe)], text=True)
+    return dict((k, int(v)) for k, v in (ln.split() for ln in out.splitlines()))
+
+
+def test_ctypes_mirror_matches_header(tmp_path):
+    lay = header_layout(tmp_path)
+    for cname, py in STRUCTS.items():
+        assert lay[cname] == C.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert lay["%s.%s" % (cname, f)] == getattr(py, f).offset, (cname, f)
+
+
+def test_header_declares_every_export():
+    text = open(HEADER).read()
+    from swiftshader_gb300 import _lib
+    for name in _lib.EXPORTS:
+        assert name + "(" in text, name
+
+
+@pytest.fixture(scope="module")
+def built_lib():
+    from swiftshader_gb300 import build
+    path = build.build()
+    return path
+
+
+def test_library_loads_and_exports_all_symbols(built_lib):
+    """Loading needs no GPU; every symbol the header declares is exported."""
+    out = subprocess.check_output(["nm", "-D", "--defined-only", built_lib], text=True)
+    exported = {ln.split()[-1] for ln in out.splitlines() if " T " in ln}
+    from swiftshader_gb300 import _lib
+    for name in _lib.EXPORTS:
+        assert name in exported, name
+    L = _lib.load(built_lib)
+    assert L.swgb_abi_version() == 1
+
+
+def test_host_side_errors_without_device(built_lib):
+    """Argument validation happens on the host and returns a status (never
+    aborts); context creation without a GPU reports NO_DEVICE."""
+    import torch
+    from swiftshader_gb300 import _lib, scenes
+    L = _lib.load(built_lib)
+    ctx = C.c_void_p()
+    status = L.swgb_ctx_create(0, None, C.byref(ctx))
+    if torch.cuda.is_available():
+        assert status == abi.OK
+        L.swgb_ctx_destroy(ctx)
+    else:
+        assert status == abi.NO_DEVICE
+    assert L.swgb_draw(None, None, None) == abi.INVALID_ARG
+    assert L.swgb_sync(None) == abi.INVALID_ARG
+    # the allocation-free draw validates sizes before touching any device
+    sc = scenes.scene_small(n_tris=4, width=16, height=16)
+    st = scenes.build_state(sc, 1 << 20, 1 << 20, 1 << 20)
+    a = scenes.build_args(sc)
+    a.count = 40000
+    assert L.swgb_draw_noalloc(C.byref(st), C.byref(a), None) == abi.INVALID_ARG
+    assert b"32768" in L.swgb_last_error()
