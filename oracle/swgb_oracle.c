@@ -215,7 +215,8 @@ static swgb_status prepare(ODraw *d, const swgb_pipeline_state *st, const swgb_d
     if(st->color_format != SWGB_FORMAT_R8G8B8A8_UNORM && st->color_format != SWGB_FORMAT_R32G32B32A32_SFLOAT &&
        st->color_format != SWGB_FORMAT_R16G16B16A16_SFLOAT)
         return SWGB_UNSUPPORTED_STATE;
-    if(st->fragment_shader == SWGB_FS_TEX_X_VCOLOR && st->texture.format != SWGB_FORMAT_R8G8B8A8_UNORM)
+    if(st->fragment_shader == SWGB_FS_TEX_X_VCOLOR && st->texture.format != SWGB_FORMAT_R8G8B8A8_UNORM &&
+       st->texture.format != SWGB_FORMAT_R16G16B16A16_SFLOAT && st->texture.format != SWGB_FORMAT_R32G32B32A32_SFLOAT)
         return SWGB_UNSUPPORTED_STATE;
 
     /* Viewport (Renderer.cpp:300-331) */
@@ -796,6 +797,106 @@ static float lod_2d(const OSampler *s, const float u[4], const float v[4])
     return log2sqrt(lod);
 }
 
+/* halfToFloatBits (src/Pipeline/ShaderCore.cpp:627-645): texel conversion of
+ * R16G16B16A16_SFLOAT textures. */
+static float half_bits_to_float(uint16_t h)
+{
+    uint32_t sign16 = h & 0x8000u, man16 = h & 0x03FFu, exp16 = h & 0x7C00u;
+    uint32_t sign32 = sign16 << 16, man32 = man16 << 13, exp32 = (exp16 + 0x1C000u) << 13;
+    uint32_t norm32 = (man32 | exp32) | (exp16 == 0x7C00u ? 0x7F800000u : 0u);
+    uint32_t magic = 126u << 23;
+    uint32_t denorm32 = f2u(fsub(u2f(magic + man16), u2f(magic)));
+    return u2f(sign32 | (exp16 == 0 ? denorm32 : norm32));
+}
+
+/* Float4 Frac (LLVMReactor.cpp:3252-3275): x - floor(x), at most 0x3F7FFFFF. */
+static float frac4(float x)
+{
+    x = daz(x);
+    return fminr(fsub(x, floorf(x)), u2f(0x3F7FFFFF));
+}
+
+/* address() for normalized float coordinates (SamplerCore.cpp:2463-2638). */
+static void address_float(const OSampler *s, float coord, uint32_t mode, int dim, int32_t *x0, int32_t *x1, float *f)
+{
+    const float one = u2f(0x3F7FFFFF);
+    if(mode == SWGB_ADDRESS_CLAMP_TO_EDGE)
+        coord = fminr(fmaxr(coord, 0.0f), one);
+    else if(mode == SWGB_ADDRESS_MIRRORED_REPEAT)
+    {
+        coord = fmul(coord, 0.5f);
+        coord = fmul(2.0f, fabsf(fsub(coord, rintf(daz(coord)))));
+        coord = fminr(coord, one);
+    }
+    else
+        coord = frac4(coord);
+    coord = fmul(coord, (float)dim);
+    if(!s->linearFilter)
+    {
+        *x0 = trunc_int(coord);
+        *x1 = *x0 + 1;
+        *f = 0.0f;
+        return;
+    }
+    coord = fsub(coord, 0.5f);
+    float fl = floorf(daz(coord));
+    *x0 = trunc_int(fl);
+    *f = fsub(coord, fl);
+    *x1 = *x0 + 1;
+    if(mode == SWGB_ADDRESS_REPEAT)
+    {
+        if(*x0 < 0) *x0 = dim - 1;
+        if(!(*x1 < dim)) *x1 = 0;
+    }
+    else
+    {
+        if(*x0 < 0) *x0 = 0;
+        if(*x1 > dim - 1) *x1 = dim - 1;
+    }
+}
+
+static void texel_float(const swgb_texture *t, const swgb_texture_level *lv, int32_t index, float out[4])
+{
+    if(t->format == SWGB_FORMAT_R32G32B32A32_SFLOAT)
+        memcpy(out, (const uint8_t *)lv->buffer + (size_t)(uint32_t)index * 16, 16);
+    else
+    {
+        const uint16_t *p = (const uint16_t *)((const uint8_t *)lv->buffer + (size_t)(uint32_t)index * 8);
+        for(int c = 0; c < 4; c++) out[c] = half_bits_to_float(p[c]);
+    }
+}
+
+/* sampleFloat2D for one lane (SamplerCore.cpp:1155-1248). */
+static void sample_float_2d(const OSampler *s, float u, float v, float lod, int secondLOD, float out[4], uint32_t *lvMask)
+{
+    int ilod = s->mipLinear ? trunc_int(lod) : round_int(lod);
+    const swgb_texture_level *lv = level_at(s, ilod + secondLOD);
+    if(lvMask) *lvMask |= 1u << (uint32_t)(lv - s->t->levels);
+    int32_t x0, x1, y0, y1;
+    float fu, fv;
+    address_float(s, u, s->t->address_u, (int)lv->width, &x0, &x1, &fu);
+    address_float(s, v, s->t->address_v, (int)lv->height, &y0, &y1, &fv);
+    int32_t pitch = (int32_t)lv->pitch_texels;
+    y0 *= pitch;
+    if(!s->linearFilter)
+    {
+        texel_float(s->t, lv, x0 + y0, out);
+        return;
+    }
+    y1 *= pitch;
+    float c00[4], c10[4], c01[4], c11[4];
+    texel_float(s->t, lv, x0 + y0, c00);
+    texel_float(s->t, lv, x1 + y0, c10);
+    texel_float(s->t, lv, x0 + y1, c01);
+    texel_float(s->t, lv, x1 + y1, c11);
+    for(int c = 0; c < 4; c++)
+    {
+        float a = fadd(c00[c], fmul(fu, fsub(c10[c], c00[c])));
+        float b = fadd(c01[c], fmul(fu, fsub(c11[c], c01[c])));
+        out[c] = fadd(a, fmul(fv, fsub(b, a)));
+    }
+}
+
 /* sampleTexture128 for the 16-bit path (SamplerCore.cpp:59-253): returns
  * 4 lanes x RGBA, scaled by 1/getComponentScale() = 1/0xFF00. */
 static void sample_texture_quad(const OSampler *s, const float u[4], const float v[4], float out[4][4], uint32_t *lvMask)
@@ -809,6 +910,24 @@ static void sample_texture_quad(const OSampler *s, const float u[4], const float
         lod = fadd(lod, s->bias);
         lod = fmaxr(lod, s->minLod);
         lod = fminr(lod, s->maxLod);
+    }
+    if(s->t->format != SWGB_FORMAT_R8G8B8A8_UNORM)
+    {
+        /* sampleFloatFilter (SamplerCore.cpp:1061-1083) */
+        float fr = fsub(daz(lod), floorf(daz(lod))); /* scalar Frac: lod - floor(lod) */
+        for(int lane = 0; lane < 4; lane++)
+        {
+            float c[4];
+            sample_float_2d(s, u[lane], v[lane], lod, 0, c, lvMask);
+            if(s->mipLinear)
+            {
+                float cc[4];
+                sample_float_2d(s, u[lane], v[lane], lod, 1, cc, lvMask);
+                for(int k = 0; k < 4; k++) c[k] = fadd(fmul(fsub(cc[k], c[k]), fr), c[k]);
+            }
+            for(int k = 0; k < 4; k++) out[lane][k] = c[k];
+        }
+        return;
     }
     const float scale = 1.0f / 65280.0f;
     for(int lane = 0; lane < 4; lane++)
@@ -831,7 +950,6 @@ static void sample_texture_quad(const OSampler *s, const float u[4], const float
 
 swgb_status oracle_sample_quad(const swgb_texture *tex, const float u[4], const float v[4], float out[16])
 {
-    if(tex->format != SWGB_FORMAT_R8G8B8A8_UNORM) return SWGB_UNSUPPORTED_STATE;
     OSampler s;
     sampler_init(&s, tex);
     float o[4][4];
@@ -883,32 +1001,48 @@ static float blend_op(uint32_t op, float s, float sf, float dd, float df)
     }
 }
 
-/* Half conversions for R16G16B16A16_SFLOAT attachments
- * (halfToFloatBits / floatToHalfBits, src/Pipeline/ShaderCore.cpp:627-671). */
+/* R16G16B16A16_SFLOAT attachments: the blend reads with Reactor's
+ * Float(Half) (src/Reactor/Reactor.cpp:3787-3815; a half infinity/NaN reads as
+ * 65536 + ...), and writeColor stores Half(Float) (:3744-3770). */
 static float half_to_float(uint16_t h)
 {
-    uint32_t sign16 = h & 0x8000u, man16 = h & 0x03FFu, exp16 = h & 0x7C00u;
-    uint32_t sign32 = sign16 << 16, man32 = man16 << 13, exp32 = (exp16 + 0x1C000u) << 13;
-    uint32_t norm32 = (man32 | exp32) | (exp16 == 0x7C00u ? 0x7F800000u : 0u);
-    uint32_t magic = 126u << 23;
-    uint32_t denorm32 = f2u(fsub(u2f(magic + man16), u2f(magic)));
-    return u2f(sign32 | (exp16 == 0 ? denorm32 : norm32));
+    int32_t fp16i = h;
+    int32_t sgn = (fp16i >> 15) & 1, e = (fp16i >> 10) & 0x1F, m = fp16i & 0x3FF;
+    uint32_t fp32i = (uint32_t)sgn << 31;
+    if(e == 0)
+    {
+        if(m != 0)
+        {
+            while((m & 0x400) == 0)
+            {
+                m <<= 1;
+                e -= 1;
+            }
+            fp32i |= (uint32_t)(((e + (127 - 15) + 1) << 23) | ((m & ~0x400) << 13));
+        }
+    }
+    else
+        fp32i |= (uint32_t)(((e + (127 - 15)) << 23) | (m << 13));
+    return u2f(fp32i);
 }
 
 static uint16_t float_to_half(float f)
 {
-    uint32_t bits = f2u(f);
-    uint32_t sign = bits & 0x80000000u, ab = bits & 0x7FFFFFFFu;
-    int normal = ab > 0x38800000u;
-    uint32_t mantissa = (ab & 0x007FFFFFu) | 0x00800000u;
-    uint32_t e = 113u - (ab >> 23);
-    uint32_t denormal = e < 24u ? (mantissa >> e) : 0u;
-    uint32_t base = normal ? ab : denormal;
-    uint32_t bias = normal ? 0xC8000000u : 0u;
-    uint32_t rounded = base + bias + 0x00000FFFu + ((base >> 13) & 1u);
-    uint32_t fp16u = rounded >> 13;
-    if(ab > 0x47FFEFFFu) fp16u |= 0x7FFFu;
-    return (uint16_t)((sign >> 16) | (fp16u & 0xFFFFu));
+    uint32_t fp32i = f2u(f);
+    uint32_t ab = fp32i & 0x7FFFFFFFu;
+    uint16_t fp16i = (uint16_t)((fp32i & 0x80000000u) >> 16);
+    if(ab > 0x47FFEFFFu)
+        fp16i |= 0x7FFF;
+    else if(ab < 0x38800000u)
+    {
+        int32_t mantissa = (int32_t)((ab & 0x007FFFFFu) | 0x00800000u);
+        int32_t e = 113 - (int32_t)(ab >> 23);
+        uint32_t a2 = e < 24 ? (uint32_t)(mantissa >> e) : 0u;
+        fp16i |= (uint16_t)((a2 + 0x00000FFFu + ((a2 >> 13) & 1u)) >> 13);
+    }
+    else
+        fp16i |= (uint16_t)((ab + 0xC8000000u + 0x00000FFFu + ((ab >> 13) & 1u)) >> 13);
+    return fp16i;
 }
 
 static void read_color(const ODraw *d, int x, int y, float dst[4])

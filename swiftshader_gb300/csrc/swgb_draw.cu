@@ -100,6 +100,8 @@ struct DrawParams {
     uint32_t srcC, dstC, opC, srcA, dstA, opA;
     uint32_t writeMask;
     int fs;
+    int cf;       // colour attachment format, CF_*
+    int texFloat; // 0: R8G8B8A8_UNORM texture (16-bit path), 1: RGBA16F, 2: RGBA32F (fp32 path)
     uint8_t *color;
     uint32_t colorPitch;
     uint8_t *depth;
@@ -719,30 +721,26 @@ __device__ __forceinline__ void sample_quad_2d(const DrawParams &D, float u, flo
     }
 }
 
-// sampleTexture128 on the 16-bit path (SamplerCore.cpp:59-253) with the implicit
-// LOD of computeLod2D (:1376-1422); result scaled by 1 / 0xFF00.
+// Implicit LOD of computeLod2D (SamplerCore.cpp:1376-1422) from lanes 0, 1, 2
+// of the quad, plus mipLodBias and the [minLod, maxLod] clamp (:116-157).
+__device__ __forceinline__ float implicit_lod(const DrawParams &D, const float u[4], const float v[4])
+{
+    if(D.minLod == D.maxLod) return D.minLod;
+    float dudx = u[1] - u[0], dudy = u[2] - u[0];
+    float dvdx = v[1] - v[0], dvdy = v[2] - v[0];
+    float a = dudx * D.texW, b = dudy * D.texW, c = dvdx * D.texH, e = dvdy * D.texH;
+    a = a * a; b = b * b; c = c * c; e = e * e;
+    float lod = log2sqrt(rmax(a + c, b + e));
+    lod = lod + D.lodBias;
+    lod = rmax(lod, D.minLod);
+    return rmin(lod, D.maxLod);
+}
+
 // sampleTexture128 on the 16-bit path (SamplerCore.cpp:59-253) for lane 'lane'
-// of a quad: the implicit LOD of computeLod2D (:1376-1422) uses lanes 0, 1, 2;
-// the result is scaled by 1 / 0xFF00 (getComponentScale).
-__device__ __forceinline__ void sample_texture_lane(const DrawParams &D, const float u[4], const float v[4], int lane, float out[4],
+// of a quad; the result is scaled by 1 / 0xFF00 (getComponentScale).
+__device__ __forceinline__ void sample_texture_lane(const DrawParams &D, float lod, float ul, float vl, float out[4],
                                                     uint32_t &lvMask)
 {
-    float lod;
-    if(D.minLod == D.maxLod)
-        lod = D.minLod;
-    else
-    {
-        float dudx = u[1] - u[0], dudy = u[2] - u[0];
-        float dvdx = v[1] - v[0], dvdy = v[2] - v[0];
-        float a = dudx * D.texW, b = dudy * D.texW, c = dvdx * D.texH, e = dvdy * D.texH;
-        a = a * a; b = b * b; c = c * c; e = e * e;
-        lod = log2sqrt(rmax(a + c, b + e));
-        lod = lod + D.lodBias;
-        lod = rmax(lod, D.minLod);
-        lod = rmin(lod, D.maxLod);
-    }
-    const float ul = lane == 0 ? u[0] : (lane == 1 ? u[1] : (lane == 2 ? u[2] : u[3]));
-    const float vl = lane == 0 ? v[0] : (lane == 1 ? v[1] : (lane == 2 ? v[2] : v[3]));
     uint32_t c[4], cc[4] = {0u, 0u, 0u, 0u};
     const int levels = D.mipLinear ? 2 : 1;
 #pragma unroll 1
@@ -765,6 +763,100 @@ __device__ __forceinline__ void sample_texture_lane(const DrawParams &D, const f
     const float scale = 1.0f / 65280.0f;
 #pragma unroll
     for(int k = 0; k < 4; k++) out[k] = __uint2float_rn(c[k]) * scale;
+}
+
+// ---- fp32 filtering path for R16G16B16A16_SFLOAT / R32G32B32A32_SFLOAT ----------
+
+// address() for normalized float coordinates (SamplerCore.cpp:2463-2638).
+__device__ __forceinline__ void address_float(const DrawParams &D, float coord, uint32_t mode, int dim, int32_t &x0, int32_t &x1, float &f)
+{
+    const float one = __int_as_float(0x3F7FFFFF);
+    if(mode == SWGB_ADDRESS_CLAMP_TO_EDGE)
+        coord = rmin(rmax(coord, 0.0f), one);
+    else if(mode == SWGB_ADDRESS_MIRRORED_REPEAT)
+    {
+        coord = coord * 0.5f;
+        coord = 2.0f * fabsf(coord - rintf(coord));
+        coord = rmin(coord, one);
+    }
+    else
+        coord = rmin(coord - floorf(coord), one);  // Float4 Frac (LLVMReactor.cpp:3252-3275)
+    coord = coord * (float)dim;
+    if(!D.texLinear)
+    {
+        x0 = trunc_int(coord);
+        x1 = x0 + 1;
+        f = 0.0f;
+        return;
+    }
+    coord = coord - 0.5f;
+    const float fl = floorf(coord);
+    x0 = trunc_int(fl);
+    f = coord - fl;
+    x1 = x0 + 1;
+    if(mode == SWGB_ADDRESS_REPEAT)
+    {
+        if(x0 < 0) x0 = dim - 1;
+        if(!(x1 < dim)) x1 = 0;
+    }
+    else
+    {
+        x0 = max(x0, 0);
+        x1 = min(x1, dim - 1);
+    }
+}
+
+__device__ __forceinline__ float4 texel_float(const DrawParams &D, const TexLevel &lv, int32_t index)
+{
+    if(D.texFloat == 2) return __ldg((const float4 *)lv.buf + (uint32_t)index);
+    const uint2 h = __ldg((const uint2 *)lv.buf + (uint32_t)index);
+    return make_float4(half_bits_to_float(h.x & 0xFFFFu), half_bits_to_float(h.x >> 16),
+                       half_bits_to_float(h.y & 0xFFFFu), half_bits_to_float(h.y >> 16));
+}
+
+// sampleFloat2D for one lane (SamplerCore.cpp:1155-1248).
+__device__ __forceinline__ float4 sample_float_2d(const DrawParams &D, float u, float v, float lod, int second, uint32_t &lvMask)
+{
+    int ilod = D.mipLinear ? trunc_int(lod) : round_int(lod);
+    int li = ilod + second;
+    li = li < 0 ? 0 : (li > D.levelCount - 1 ? D.levelCount - 1 : li);
+    lvMask |= 1u << li;
+    const TexLevel &lv = D.lv[li];
+    int32_t x0, x1, y0, y1;
+    float fu, fv;
+    address_float(D, u, D.addrU, (int)lv.w, x0, x1, fu);
+    address_float(D, v, D.addrV, (int)lv.h, y0, y1, fv);
+    const int32_t pitch = (int32_t)lv.pitch;
+    y0 *= pitch;
+    if(!D.texLinear) return texel_float(D, lv, x0 + y0);
+    y1 *= pitch;
+    const float4 c00 = texel_float(D, lv, x0 + y0), c10 = texel_float(D, lv, x1 + y0);
+    const float4 c01 = texel_float(D, lv, x0 + y1), c11 = texel_float(D, lv, x1 + y1);
+    float4 a, b, o;
+    a.x = c00.x + fu * (c10.x - c00.x); a.y = c00.y + fu * (c10.y - c00.y);
+    a.z = c00.z + fu * (c10.z - c00.z); a.w = c00.w + fu * (c10.w - c00.w);
+    b.x = c01.x + fu * (c11.x - c01.x); b.y = c01.y + fu * (c11.y - c01.y);
+    b.z = c01.z + fu * (c11.z - c01.z); b.w = c01.w + fu * (c11.w - c01.w);
+    o.x = a.x + fv * (b.x - a.x); o.y = a.y + fv * (b.y - a.y);
+    o.z = a.z + fv * (b.z - a.z); o.w = a.w + fv * (b.w - a.w);
+    return o;
+}
+
+// sampleFloatFilter (SamplerCore.cpp:1061-1083): trilinear blend by the scalar
+// Frac of the LOD (x86 SSE4.1: lod - floor(lod)).
+__device__ __forceinline__ void sample_float_lane(const DrawParams &D, float lod, float ul, float vl, float out[4], uint32_t &lvMask)
+{
+    float4 c = sample_float_2d(D, ul, vl, lod, 0, lvMask);
+    if(D.mipLinear)
+    {
+        const float4 cc = sample_float_2d(D, ul, vl, lod, 1, lvMask);
+        const float fr = lod - floorf(lod);
+        c.x = (cc.x - c.x) * fr + c.x;
+        c.y = (cc.y - c.y) * fr + c.y;
+        c.z = (cc.z - c.z) * fr + c.z;
+        c.w = (cc.w - c.w) * fr + c.w;
+    }
+    out[0] = c.x; out[1] = c.y; out[2] = c.z; out[3] = c.w;
 }
 
 // ------------------------------------------------------------------------
@@ -827,13 +919,20 @@ __device__ __forceinline__ bool depth_pass(uint32_t op, float zb, float z)
 
 // Per-triangle plane-equation floats staged for a batch:
 // x0, y0, z(A,B,C), w(A,B,C), V[k](A,B,C).
-constexpr int PLANES = 8 + 3 * MAXV;
+constexpr int PLANE_V = 6;  // varying components with plane equations (colour + uv)
+constexpr int PLANES = 8 + 3 * PLANE_V;
+
+// 32-bit words per pixel of a colour attachment: R8G8B8A8_UNORM,
+// R16G16B16A16_SFLOAT, R32G32B32A32_SFLOAT.
+enum { CF_RGBA8 = 0, CF_RGBA16F = 1, CF_RGBA32F = 2 };
+__host__ __device__ constexpr int color_words(int cf) { return cf == CF_RGBA8 ? 1 : (cf == CF_RGBA16F ? 2 : 4); }
 
 // Shared memory of one warp: its bin's depth and colour, the staged batch,
 // and its ordered candidate list.
+template<int CF>
 struct RasterShared {
     float depth[BIN * BIN];
-    uint32_t color[BIN * BIN];
+    uint32_t color[BIN * BIN * color_words(CF)];
     float plane[PLANES][BATCH];
     uint32_t span[BATCH][BIN];          // left | right << 16 per bin row
     int16_t qx0[BATCH][BIN / 2];        // first quad x per quad row of the triangle
@@ -864,7 +963,8 @@ __device__ __forceinline__ float vary(const float4 &a, const float4 &b, int k)
 // stage's span buffer, or the reference DDA when the buffer was full), its
 // quad rows, and its plane equations (SetupRoutine.cpp:270-548).  Returns the
 // number of quad slots it expands to.
-__device__ int setup_batch_triangle(const DrawParams &D, RasterShared &S, int ti, uint32_t t, int bx0, int by0)
+template<class SH>
+__device__ int setup_batch_triangle(const DrawParams &D, SH &S, int ti, uint32_t t, int bx0, int by0)
 {
     const short4 box = D.triBox[t];
     const TriInfo inf = D.triInfo[t];
@@ -1017,7 +1117,7 @@ __device__ int setup_batch_triangle(const DrawParams &D, RasterShared &S, int ti
         B0 = D.ptv[(size_t)j0 * 4 + 3]; B1 = D.ptv[(size_t)j1 * 4 + 3]; B2 = D.ptv[(size_t)j2 * 4 + 3];
     }
 #pragma unroll
-    for(int k = 0; k < MAXV; k++)
+    for(int k = 0; k < PLANE_V; k++)
     {
         if(k >= D.nv) break;
         float v0 = vary(A0, B0, k), v1 = vary(A1, B1, k), v2 = vary(A2, B2, k);
@@ -1028,7 +1128,8 @@ __device__ int setup_batch_triangle(const DrawParams &D, RasterShared &S, int ti
     return pre;
 }
 
-__device__ __forceinline__ void quad_depth(const DrawParams &D, const RasterShared &S, int ti, int qx, int y, float zq[4])
+template<class SH>
+__device__ __forceinline__ void quad_depth(const DrawParams &D, const SH &S, int ti, int qx, int y, float zq[4])
 {
     const float x0p = S.plane[0][ti], y0p = S.plane[1][ti];
     const float zA = S.plane[2][ti], zB = S.plane[3][ti], zC = S.plane[4][ti];
@@ -1047,7 +1148,8 @@ __device__ __forceinline__ void quad_depth(const DrawParams &D, const RasterShar
 // shader with SamplerCore filtering (the LOD comes from lanes 0, 1 and 2 of the
 // quad, covered or not, as the reference's 4-wide SIMD computes it), and the
 // UNORM clamp (PixelProgram::clampColor).
-__device__ __forceinline__ void shade_pixel(const DrawParams &D, const RasterShared &S, int ti, int qx, int y, int i,
+template<int CF, class SH>
+__device__ __forceinline__ void shade_pixel(const DrawParams &D, const SH &S, int ti, int qx, int y, int i,
                                             float col[4], uint32_t &lvMask)
 {
     const float x0p = S.plane[0][ti], y0p = S.plane[1][ti];
@@ -1077,18 +1179,24 @@ __device__ __forceinline__ void shade_pixel(const DrawParams &D, const RasterSha
             u[j] = mul_add(xF, uA, uC + yF * uB) * r;
             v[j] = mul_add(xF, vA, vC + yF * vB) * r;
         }
+        const float lod = implicit_lod(D, u, v);
+        const float ul = i == 0 ? u[0] : (i == 1 ? u[1] : (i == 2 ? u[2] : u[3]));
+        const float vl = i == 0 ? v[0] : (i == 1 ? v[1] : (i == 2 ? v[2] : v[3]));
         float t[4];
-        sample_texture_lane(D, u, v, i, t, lvMask);
+        if(D.texFloat) sample_float_lane(D, lod, ul, vl, t, lvMask);
+        else sample_texture_lane(D, lod, ul, vl, t, lvMask);
 #pragma unroll
         for(int k = 0; k < 4; k++) c[k] = t[k] * c[k];
     }
 #pragma unroll
-    for(int k = 0; k < 4; k++) col[k] = rmin(rmax(c[k], 0.0f), 1.0f);  // UNORM target
+    for(int k = 0; k < 4; k++) col[k] = CF == CF_RGBA8 ? rmin(rmax(c[k], 0.0f), 1.0f) : c[k];  // clampColor: UNORM only
 }
 
-// Depth test/write, blend and RGBA8 write of one pixel of the staged bin
-// (PixelRoutine.cpp:494-574,660-685,1653-1961,1975-1993,2609-2650).
-__device__ __forceinline__ void rop_pixel(const DrawParams &D, RasterShared &S, int idx, float z, const float col[4],
+// Depth test/write, blend and colour write of one pixel of the staged bin
+// (PixelRoutine.cpp:494-574,660-685; alphaBlend :1653-1961; writeColor
+// :1975-1993,2429-2650).
+template<int CF>
+__device__ __forceinline__ void rop_pixel(const DrawParams &D, RasterShared<CF> &S, int idx, float z, const float col[4],
                                           unsigned long long &nTested, unsigned long long &nPassed)
 {
     if(D.depthTest)
@@ -1099,12 +1207,29 @@ __device__ __forceinline__ void rop_pixel(const DrawParams &D, RasterShared &S, 
     }
     nPassed++;
     float out[4];
-    const uint32_t old = S.color[idx];
     if(D.blend)
     {
         float dst[4];
+        if(CF == CF_RGBA8)
+        {
+            // readPixel widens b to b * 257, alphaBlend scales by 1 / 0xFFFF
+            const uint32_t old = S.color[idx];
 #pragma unroll
-        for(int c = 0; c < 4; c++) dst[c] = (float)(((old >> (8 * c)) & 0xFFu) * 257u) * (1.0f / 0xFFFF);
+            for(int c = 0; c < 4; c++) dst[c] = (float)(((old >> (8 * c)) & 0xFFu) * 257u) * (1.0f / 0xFFFF);
+        }
+        else if(CF == CF_RGBA16F)
+        {
+            const uint32_t w0 = S.color[2 * idx], w1 = S.color[2 * idx + 1];
+            dst[0] = reactor_half_to_float(w0 & 0xFFFFu);
+            dst[1] = reactor_half_to_float(w0 >> 16);
+            dst[2] = reactor_half_to_float(w1 & 0xFFFFu);
+            dst[3] = reactor_half_to_float(w1 >> 16);
+        }
+        else
+        {
+#pragma unroll
+            for(int c = 0; c < 4; c++) dst[c] = __uint_as_float(S.color[4 * idx + c]);
+        }
         float sf[4], df[4];
 #pragma unroll
         for(int c = 0; c < 3; c++)
@@ -1123,17 +1248,39 @@ __device__ __forceinline__ void rop_pixel(const DrawParams &D, RasterShared &S, 
 #pragma unroll
         for(int c = 0; c < 4; c++) out[c] = col[c];
     }
-    uint32_t packed = old;
-#pragma unroll
-    for(int c = 0; c < 4; c++)
+    if(CF == CF_RGBA8)
     {
-        float v = rmin(rmax(out[c], 0.0f), 1.0f);
-        int32_t r = round_int(v * 255.0f);
-        int32_t s16 = (int32_t)(int16_t)r;
-        uint32_t b = s16 < 0 ? 0u : (s16 > 255 ? 255u : (uint32_t)s16);  // PackUnsigned
-        if(D.writeMask & (1u << c)) packed = (packed & ~(0xFFu << (8 * c))) | (b << (8 * c));
+        uint32_t packed = S.color[idx];
+#pragma unroll
+        for(int c = 0; c < 4; c++)
+        {
+            float v = rmin(rmax(out[c], 0.0f), 1.0f);
+            int32_t r = round_int(v * 255.0f);
+            int32_t s16 = (int32_t)(int16_t)r;
+            uint32_t b = s16 < 0 ? 0u : (s16 > 255 ? 255u : (uint32_t)s16);  // PackUnsigned
+            if(D.writeMask & (1u << c)) packed = (packed & ~(0xFFu << (8 * c))) | (b << (8 * c));
+        }
+        S.color[idx] = packed;
     }
-    S.color[idx] = packed;
+    else if(CF == CF_RGBA16F)
+    {
+        uint32_t w[2] = {S.color[2 * idx], S.color[2 * idx + 1]};
+#pragma unroll
+        for(int c = 0; c < 4; c++)
+            if(D.writeMask & (1u << c))
+            {
+                const int sh = 16 * (c & 1);
+                w[c >> 1] = (w[c >> 1] & ~(0xFFFFu << sh)) | (reactor_float_to_half(out[c]) << sh);
+            }
+        S.color[2 * idx] = w[0];
+        S.color[2 * idx + 1] = w[1];
+    }
+    else
+    {
+#pragma unroll
+        for(int c = 0; c < 4; c++)
+            if(D.writeMask & (1u << c)) S.color[4 * idx + c] = __float_as_uint(out[c]);
+    }
 }
 
 __device__ __forceinline__ int warp_incl_scan(int v, int lane)
@@ -1151,7 +1298,8 @@ __device__ __forceinline__ int warp_incl_scan(int v, int lane)
 // bin.  Lane j sets up triangle j; then the warp expands quad slots, masks
 // coverage, rejects early on depth, and shades the live pixels one per lane;
 // lanes hitting the same pixel resolve lowest lane (earliest triangle) first.
-__device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared &S, int nb, int bx0, int by0,
+template<int CF>
+__device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared<CF> &S, int nb, int bx0, int by0,
                                           unsigned long long &nQuads, unsigned long long &nTested,
                                           unsigned long long &nPassed, uint32_t &lvMask)
 {
@@ -1265,7 +1413,7 @@ __device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared &S, 
                     z = mul_add(xF, S.plane[2][qTi], S.plane[4][qTi] + yF * S.plane[3][qTi]);
                     z = rmin(rmax(z, D.minDepthClamp), D.maxDepthClamp);  // clampDepth
                 }
-                shade_pixel(D, S, qTi, qX, y, i, col, lvMask);
+                shade_pixel<CF>(D, S, qTi, qX, y, i, col, lvMask);
             }
             // ordered resolve: among lanes on the same pixel, lowest lane first
             unsigned pend = __ballot_sync(0xFFFFFFFFu, valid);
@@ -1275,7 +1423,7 @@ __device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared &S, 
                 const unsigned peers = __match_any_sync(0xFFFFFFFFu, mine ? pidx : -1 - lane);
                 if(mine && (__ffs(peers) - 1) == lane)
                 {
-                    rop_pixel(D, S, pidx, z, col, nTested, nPassed);
+                    rop_pixel<CF>(D, S, pidx, z, col, nTested, nPassed);
                     pend &= ~(1u << lane);
                 }
                 __syncwarp();
@@ -1296,11 +1444,13 @@ __device__ __forceinline__ bool box_hits(int4 b, int bx0, int by0)
     return b.x < b.z && b.x < bx0 + BIN && b.z > bx0 && b.y < by0 + BIN && b.w > by0;
 }
 
+template<int CF>
 __global__ void __launch_bounds__(RASTER_THREADS) k_raster(const __grid_constant__ DrawParams D)
 {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    RasterShared &S = reinterpret_cast<RasterShared *>(smem_raw)[warp];
+    constexpr int CW = color_words(CF);
+    RasterShared<CF> &S = reinterpret_cast<RasterShared<CF> *>(smem_raw)[warp];
     const int nbins = D.binsX * D.binsY;
     unsigned long long nQuads = 0, nTested = 0, nPassed = 0;
     uint32_t lvMask = 0;
@@ -1321,31 +1471,39 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_raster(const __grid_constant
         const int ly = i / (BIN / 4), lx = (i % (BIN / 4)) * 4;
         const int px = bx0 + lx, py = by0 + ly;
         float4 dz = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
-        uint4 cc = make_uint4(0, 0, 0, 0);
-        if(py < D.sy1 && px < D.sx1)
+        if(D.depthTest && py < D.sy1 && px < D.sx1)
         {
             const uint8_t *drow = D.depth + (size_t)py * D.depthPitch;
-            const uint8_t *crow = D.color + (size_t)py * D.colorPitch;
             if(D.vec16 && px + 4 <= D.sx1)
-            {
-                if(D.depthTest) dz = *(const float4 *)(drow + (size_t)px * 4);
-                cc = *(const uint4 *)(crow + (size_t)px * 4);
-            }
+                dz = *(const float4 *)(drow + (size_t)px * 4);
             else
             {
                 float dv[4] = {1.0f, 1.0f, 1.0f, 1.0f};
-                uint32_t cv[4] = {0, 0, 0, 0};
-                for(int k = 0; k < 4 && px + k < D.sx1; k++)
-                {
-                    if(D.depthTest) dv[k] = *(const float *)(drow + (size_t)(px + k) * 4);
-                    cv[k] = *(const uint32_t *)(crow + (size_t)(px + k) * 4);
-                }
+                for(int k = 0; k < 4 && px + k < D.sx1; k++) dv[k] = *(const float *)(drow + (size_t)(px + k) * 4);
                 dz = make_float4(dv[0], dv[1], dv[2], dv[3]);
-                cc = make_uint4(cv[0], cv[1], cv[2], cv[3]);
             }
         }
         *(float4 *)&S.depth[ly * BIN + lx] = dz;
-        *(uint4 *)&S.color[ly * BIN + lx] = cc;
+    }
+    for(int i = lane; i < BIN * BIN * CW / 4; i += 32)
+    {
+        // 16-byte segment i of the bin's colour rows: 4 / CW pixels
+        const int ly = i / (BIN * CW / 4), lx = (i % (BIN * CW / 4)) * 4 / CW;
+        const int px = bx0 + lx, py = by0 + ly;
+        uint4 cc = make_uint4(0, 0, 0, 0);
+        if(py < D.sy1 && px < D.sx1)
+        {
+            const uint8_t *crow = D.color + (size_t)py * D.colorPitch + (size_t)px * 4 * CW;
+            if(D.vec16 && px + 4 / CW <= D.sx1)
+                cc = *(const uint4 *)crow;
+            else
+            {
+                uint32_t cv[4] = {0, 0, 0, 0};
+                for(int k = 0; k < 4 && px + k / CW < D.sx1; k++) cv[k] = *(const uint32_t *)(crow + 4 * k);
+                cc = make_uint4(cv[0], cv[1], cv[2], cv[3]);
+            }
+        }
+        *(uint4 *)&S.color[(ly * BIN + lx) * CW] = cc;
     }
     __syncwarp();
 
@@ -1392,25 +1550,28 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_raster(const __grid_constant
     // ---- write the bin back ----------------------------------------------------
     for(int i = lane; i < BIN * BIN / 4; i += 32)
     {
+        if(!D.depthWrite) break;
         const int ly = i / (BIN / 4), lx = (i % (BIN / 4)) * 4;
         const int px = bx0 + lx, py = by0 + ly;
         if(py >= D.sy1 || px >= D.sx1 || py < D.sy0) continue;
         uint8_t *drow = D.depth + (size_t)py * D.depthPitch;
-        uint8_t *crow = D.color + (size_t)py * D.colorPitch;
         if(D.vec16 && px + 4 <= D.sx1 && px >= D.sx0)
-        {
-            if(D.depthWrite) *(float4 *)(drow + (size_t)px * 4) = *(const float4 *)&S.depth[ly * BIN + lx];
-            *(uint4 *)(crow + (size_t)px * 4) = *(const uint4 *)&S.color[ly * BIN + lx];
-        }
+            *(float4 *)(drow + (size_t)px * 4) = *(const float4 *)&S.depth[ly * BIN + lx];
         else
-        {
             for(int k = 0; k < 4 && px + k < D.sx1; k++)
-            {
-                if(px + k < D.sx0) continue;
-                if(D.depthWrite) *(float *)(drow + (size_t)(px + k) * 4) = S.depth[ly * BIN + lx + k];
-                *(uint32_t *)(crow + (size_t)(px + k) * 4) = S.color[ly * BIN + lx + k];
-            }
-        }
+                if(px + k >= D.sx0) *(float *)(drow + (size_t)(px + k) * 4) = S.depth[ly * BIN + lx + k];
+    }
+    for(int i = lane; i < BIN * BIN * CW / 4; i += 32)
+    {
+        const int ly = i / (BIN * CW / 4), lx = (i % (BIN * CW / 4)) * 4 / CW;
+        const int px = bx0 + lx, py = by0 + ly;
+        if(py >= D.sy1 || px >= D.sx1 || py < D.sy0) continue;
+        uint8_t *crow = D.color + (size_t)py * D.colorPitch + (size_t)px * 4 * CW;
+        if(D.vec16 && px + 4 / CW <= D.sx1 && px >= D.sx0)
+            *(uint4 *)crow = *(const uint4 *)&S.color[(ly * BIN + lx) * CW];
+        else
+            for(int k = 0; k < 4 && px + k / CW < D.sx1; k++)
+                if(px + k / CW >= D.sx0) *(uint32_t *)(crow + 4 * k) = S.color[(ly * BIN + lx) * CW + k];
     }
     __syncwarp();
     }
@@ -1461,7 +1622,7 @@ struct swgb_ctx {
     size_t polyCap;
     uint32_t *polyCount;
     unsigned int *binQueue;
-    int rasterBlocks;  // persistent raster grid: SMs x resident blocks per SM
+    int rasterBlocks[3];  // persistent raster grid per colour format: SMs x resident blocks per SM
     unsigned long long *counters;
     int *error;
     uint64_t launches;
@@ -1542,7 +1703,9 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
     if(st->vertex_shader != SWGB_VS_MVP_PASSTHROUGH) return set_error(SWGB_UNSUPPORTED_STATE, "vertex_shader");
     if(st->fragment_shader != SWGB_FS_VCOLOR && st->fragment_shader != SWGB_FS_TEX_X_VCOLOR) return set_error(SWGB_UNSUPPORTED_STATE, "fragment_shader");
     if(st->depth_clamp_enable || st->depth_bias_constant != 0.0f || st->depth_bias_slope != 0.0f) return set_error(SWGB_UNSUPPORTED_STATE, "depth clamp / bias");
-    if(st->color_format != SWGB_FORMAT_R8G8B8A8_UNORM) return set_error(SWGB_UNSUPPORTED_STATE, "color_format");
+    if(st->color_format != SWGB_FORMAT_R8G8B8A8_UNORM && st->color_format != SWGB_FORMAT_R16G16B16A16_SFLOAT &&
+       st->color_format != SWGB_FORMAT_R32G32B32A32_SFLOAT)
+        return set_error(SWGB_UNSUPPORTED_STATE, "color_format");
     if(!st->color) return set_error(SWGB_INVALID_ARG, "color attachment is null");
     if(st->attrib_count < 1 || st->attrib_count > SWGB_MAX_ATTRIBS) return set_error(SWGB_INVALID_ARG, "attrib_count");
     if(st->color_blend_op > SWGB_BLEND_OP_MAX || st->alpha_blend_op > SWGB_BLEND_OP_MAX) return set_error(SWGB_UNSUPPORTED_STATE, "blend op");
@@ -1560,7 +1723,7 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
         D.vcomp[i] = at.format == SWGB_FORMAT_R32G32_SFLOAT ? 2 : 4;
         if(i > 0) D.nv += (int)D.vcomp[i];
     }
-    if(D.nv > MAXV) return set_error(SWGB_UNSUPPORTED_STATE, "too many varyings");
+    if(D.nv > PLANE_V) return set_error(SWGB_UNSUPPORTED_STATE, "too many varyings");
     if(D.nattr < 2 || D.vcomp[1] != 4) return set_error(SWGB_INVALID_ARG, "the fixed FS reads a vec4 colour at location 0");
     D.fs = (int)st->fragment_shader;
     if(D.fs == SWGB_FS_TEX_X_VCOLOR && (D.nattr < 3 || D.nv < 6)) return set_error(SWGB_INVALID_ARG, "textured FS needs a uv varying");
@@ -1614,6 +1777,7 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
     D.srcC = st->src_color_factor; D.dstC = st->dst_color_factor; D.opC = opC;
     D.srcA = st->src_alpha_factor; D.dstA = st->dst_alpha_factor; D.opA = opA;
     D.writeMask = st->color_write_mask & 0xFu;
+    D.cf = st->color_format == SWGB_FORMAT_R8G8B8A8_UNORM ? CF_RGBA8 : (st->color_format == SWGB_FORMAT_R16G16B16A16_SFLOAT ? CF_RGBA16F : CF_RGBA32F);
     D.color = (uint8_t *)st->color;
     D.colorPitch = st->color_pitch_bytes;
     D.depth = (uint8_t *)st->depth;
@@ -1624,7 +1788,10 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
     if(D.fs == SWGB_FS_TEX_X_VCOLOR)
     {
         const swgb_texture &t = st->texture;
-        if(t.format != SWGB_FORMAT_R8G8B8A8_UNORM) return set_error(SWGB_UNSUPPORTED_STATE, "texture format");
+        if(t.format == SWGB_FORMAT_R8G8B8A8_UNORM) D.texFloat = 0;
+        else if(t.format == SWGB_FORMAT_R16G16B16A16_SFLOAT) D.texFloat = 1;
+        else if(t.format == SWGB_FORMAT_R32G32B32A32_SFLOAT) D.texFloat = 2;
+        else return set_error(SWGB_UNSUPPORTED_STATE, "texture format");
         if(t.level_count < 1 || t.level_count > SWGB_MAX_MIP_LEVELS) return set_error(SWGB_INVALID_ARG, "texture level_count");
         if(t.mag_filter != t.min_filter) return set_error(SWGB_UNSUPPORTED_STATE, "mixed min/mag filters");
         if(t.address_u > SWGB_ADDRESS_CLAMP_TO_EDGE || t.address_v > SWGB_ADDRESS_CLAMP_TO_EDGE) return set_error(SWGB_UNSUPPORTED_STATE, "address mode");
@@ -1660,6 +1827,33 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
     D.nchunks = (int)((a->count + CHUNK - 1) / CHUNK);
     D.nsuper = (D.nchunks + SUPER - 1) / SUPER;
     return SWGB_OK;
+}
+
+template<int CF>
+constexpr size_t raster_smem() { return RASTER_WARPS * sizeof(RasterShared<CF>); }
+
+// Persistent raster grid of the colour format's kernel: SMs x resident blocks.
+template<int CF>
+swgb_status raster_grid(int device, bool setAttr, int &blocks)
+{
+    swgb_status s;
+    if(setAttr && (s = cuda_check(cudaFuncSetAttribute(k_raster<CF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)raster_smem<CF>()),
+                                  "raster smem attribute")) != SWGB_OK)
+        return s;
+    int sms = 0, perSM = 0;
+    if((s = cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "SM count")) != SWGB_OK) return s;
+    if((s = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_raster<CF>, RASTER_THREADS, raster_smem<CF>()),
+                       "raster occupancy")) != SWGB_OK)
+        return s;
+    blocks = (sms > 0 ? sms : 1) * (perSM > 0 ? perSM : 1);
+    return SWGB_OK;
+}
+
+void launch_raster(const DrawParams &D, uint32_t blocks, cudaStream_t st)
+{
+    if(D.cf == CF_RGBA8) k_raster<CF_RGBA8><<<blocks, RASTER_THREADS, raster_smem<CF_RGBA8>(), st>>>(D);
+    else if(D.cf == CF_RGBA16F) k_raster<CF_RGBA16F><<<blocks, RASTER_THREADS, raster_smem<CF_RGBA16F>(), st>>>(D);
+    else k_raster<CF_RGBA32F><<<blocks, RASTER_THREADS, raster_smem<CF_RGBA32F>(), st>>>(D);
 }
 
 cudaEvent_t take_event(swgb_ctx *ctx)
@@ -1728,11 +1922,9 @@ swgb_status enqueue(swgb_ctx *ctx, DrawParams &D)
     D.error = ctx->error;
     if(!ctx->rasterAttr)
     {
-        if((s = cuda_check(cudaFuncSetAttribute(k_raster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(RASTER_WARPS * sizeof(RasterShared))), "raster smem attribute")) != SWGB_OK) return s;
-        int sms = 0, perSM = 0;
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_raster, RASTER_THREADS, RASTER_WARPS * sizeof(RasterShared));
-        ctx->rasterBlocks = (sms > 0 ? sms : 1) * (perSM > 0 ? perSM : 1);
+        if((s = raster_grid<CF_RGBA8>(ctx->device, true, ctx->rasterBlocks[CF_RGBA8])) != SWGB_OK) return s;
+        if((s = raster_grid<CF_RGBA16F>(ctx->device, true, ctx->rasterBlocks[CF_RGBA16F])) != SWGB_OK) return s;
+        if((s = raster_grid<CF_RGBA32F>(ctx->device, true, ctx->rasterBlocks[CF_RGBA32F])) != SWGB_OK) return s;
         ctx->rasterAttr = true;
     }
     const uint32_t nv = D.vertexCount;
@@ -1742,8 +1934,8 @@ swgb_status enqueue(swgb_ctx *ctx, DrawParams &D)
     if(D.binsX > 0 && D.binsY > 0)
     {
         uint32_t blocks = (uint32_t)((D.binsX * D.binsY + RASTER_WARPS - 1) / RASTER_WARPS);
-        if(blocks > (uint32_t)ctx->rasterBlocks) blocks = (uint32_t)ctx->rasterBlocks;
-        timed_launch(ctx, SWGB_KERNEL_RASTER, [&] { k_raster<<<blocks, RASTER_THREADS, RASTER_WARPS * sizeof(RasterShared), ctx->stream>>>(D); });
+        if(blocks > (uint32_t)ctx->rasterBlocks[D.cf]) blocks = (uint32_t)ctx->rasterBlocks[D.cf];
+        timed_launch(ctx, SWGB_KERNEL_RASTER, [&] { launch_raster(D, blocks, ctx->stream); });
     }
     return cuda_check(cudaGetLastError(), "kernel launch");
 }
@@ -1780,14 +1972,15 @@ constexpr size_t NA_OFF_WORDS = na_up(NA_OFF_POLY + (size_t)NA_TRIS * MAX_POLY *
 // words: counters[8] (u64), spanCount (u64), polyCount (u32), binQueue (u32), error (i32)
 constexpr size_t NA_WORDS_BYTES = 8 * 8 + 8 + 4 + 4 + 4;
 constexpr size_t NA_BYTES = na_up(NA_OFF_WORDS + NA_WORDS_BYTES);
-static_assert(RASTER_WARPS * sizeof(RasterShared) <= 48 * 1024, "the allocation-free raster launch uses the default shared-memory limit");
+static_assert(raster_smem<CF_RGBA32F>() <= 48 * 1024 && raster_smem<CF_RGBA16F>() <= 48 * 1024 && raster_smem<CF_RGBA8>() <= 48 * 1024,
+              "the allocation-free raster launch uses the default shared-memory limit");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
 
 struct NoAllocDevice {
     bool ready;
     unsigned char *base;  // device address of g_noalloc_scratch on this device
-    int rasterBlocks;
+    int rasterBlocks[3];
 };
 static NoAllocDevice g_noalloc_dev[64];
 static std::mutex g_noalloc_mu;
@@ -1805,11 +1998,10 @@ swgb_status noalloc_device(int dev, NoAllocDevice *&out)
         void *ptr = nullptr;
         swgb_status s = cuda_check(cudaGetSymbolAddress(&ptr, g_noalloc_scratch), "cudaGetSymbolAddress(scratch)");
         if(s != SWGB_OK) return s;
-        int sms = 0, perSM = 0;
-        if((s = cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count")) != SWGB_OK) return s;
-        if((s = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_raster, RASTER_THREADS, RASTER_WARPS * sizeof(RasterShared)), "raster occupancy")) != SWGB_OK) return s;
+        if((s = raster_grid<CF_RGBA8>(dev, false, d.rasterBlocks[CF_RGBA8])) != SWGB_OK) return s;
+        if((s = raster_grid<CF_RGBA16F>(dev, false, d.rasterBlocks[CF_RGBA16F])) != SWGB_OK) return s;
+        if((s = raster_grid<CF_RGBA32F>(dev, false, d.rasterBlocks[CF_RGBA32F])) != SWGB_OK) return s;
         d.base = (unsigned char *)ptr;
-        d.rasterBlocks = (sms > 0 ? sms : 1) * (perSM > 0 ? perSM : 1);
         d.ready = true;
     }
     out = &d;
@@ -1961,8 +2153,8 @@ swgb_status swgb_draw_noalloc(const swgb_pipeline_state *st, const swgb_draw_arg
     if(D.binsX > 0 && D.binsY > 0)
     {
         uint32_t blocks = (uint32_t)((D.binsX * D.binsY + RASTER_WARPS - 1) / RASTER_WARPS);
-        if(blocks > (uint32_t)nd->rasterBlocks) blocks = (uint32_t)nd->rasterBlocks;
-        k_raster<<<blocks, RASTER_THREADS, RASTER_WARPS * sizeof(RasterShared), st0>>>(D);
+        if(blocks > (uint32_t)nd->rasterBlocks[D.cf]) blocks = (uint32_t)nd->rasterBlocks[D.cf];
+        launch_raster(D, blocks, st0);
     }
     return cuda_check(cudaGetLastError(), "kernel launch");
 }

@@ -61,8 +61,9 @@ __device__ __forceinline__ float log2sqrt(float lod)
     return lod;
 }
 
-// halfToFloatBits / floatToHalfBits (src/Pipeline/ShaderCore.cpp:627-671).
-__device__ __forceinline__ float half_to_float(uint32_t h)
+// halfToFloatBits (src/Pipeline/ShaderCore.cpp:627-645): texel conversion of
+// R16G16B16A16_SFLOAT textures.
+__device__ __forceinline__ float half_bits_to_float(uint32_t h)
 {
     uint32_t sign16 = h & 0x8000u, man16 = h & 0x03FFu, exp16 = h & 0x7C00u;
     uint32_t sign32 = sign16 << 16, man32 = man16 << 13, exp32 = (exp16 + 0x1C000u) << 13;
@@ -72,20 +73,48 @@ __device__ __forceinline__ float half_to_float(uint32_t h)
     return __uint_as_float(sign32 | (exp16 == 0 ? denorm32 : norm32));
 }
 
-__device__ __forceinline__ uint32_t float_to_half(float f)
+// Reactor's Float(Half) (src/Reactor/Reactor.cpp:3787-3815), used when the
+// blend reads an R16G16B16A16_SFLOAT attachment (a half inf/NaN reads as 65536+).
+__device__ __forceinline__ float reactor_half_to_float(uint32_t h)
 {
-    uint32_t bits = __float_as_uint(f);
-    uint32_t sign = bits & 0x80000000u, ab = bits & 0x7FFFFFFFu;
-    bool normal = ab > 0x38800000u;
-    uint32_t mantissa = (ab & 0x007FFFFFu) | 0x00800000u;
-    uint32_t e = 113u - (ab >> 23);
-    uint32_t denormal = e < 24u ? (mantissa >> e) : 0u;
-    uint32_t base = normal ? ab : denormal;
-    uint32_t bias = normal ? 0xC8000000u : 0u;
-    uint32_t rounded = base + bias + 0x00000FFFu + ((base >> 13) & 1u);
-    uint32_t fp16u = rounded >> 13;
-    if(ab > 0x47FFEFFFu) fp16u |= 0x7FFFu;
-    return ((sign >> 16) | fp16u) & 0xFFFFu;
+    int32_t e = (int32_t)((h >> 10) & 0x1Fu), m = (int32_t)(h & 0x3FFu);
+    uint32_t fp32i = ((h >> 15) & 1u) << 31;
+    if(e == 0)
+    {
+        if(m != 0)
+        {
+            while((m & 0x400) == 0)
+            {
+                m <<= 1;
+                e -= 1;
+            }
+            fp32i |= (uint32_t)(((e + (127 - 15) + 1) << 23) | ((m & ~0x400) << 13));
+        }
+    }
+    else
+        fp32i |= (uint32_t)(((e + (127 - 15)) << 23) | (m << 13));
+    return __uint_as_float(fp32i);
+}
+
+// Reactor's Half(Float) (src/Reactor/Reactor.cpp:3744-3770), used by
+// writeColor for R16G16B16A16_SFLOAT attachments.
+__device__ __forceinline__ uint32_t reactor_float_to_half(float f)
+{
+    uint32_t fp32i = __float_as_uint(f);
+    uint32_t ab = fp32i & 0x7FFFFFFFu;
+    uint32_t fp16i = (fp32i & 0x80000000u) >> 16;
+    if(ab > 0x47FFEFFFu)
+        fp16i |= 0x7FFFu;
+    else if(ab < 0x38800000u)
+    {
+        int32_t mantissa = (int32_t)((ab & 0x007FFFFFu) | 0x00800000u);
+        int32_t e = 113 - (int32_t)(ab >> 23);
+        uint32_t a2 = e < 24 ? (uint32_t)(mantissa >> e) : 0u;
+        fp16i |= ((a2 + 0x00000FFFu + ((a2 >> 13) & 1u)) >> 13) & 0xFFFFu;
+    }
+    else
+        fp16i |= ((ab + 0xC8000000u + 0x00000FFFu + ((ab >> 13) & 1u)) >> 13) & 0xFFFFu;
+    return fp16i & 0xFFFFu;
 }
 
 }  // namespace swgb

@@ -30,7 +30,8 @@ class Scene:
     tri_count: int = 0
     mvp: np.ndarray = None            # float32 [4, 4] row-major math matrix
     fragment_shader: int = abi.FS_VCOLOR
-    texture_levels: list = field(default_factory=list)  # uint8 [h, w, 4] per level
+    texture_levels: list = field(default_factory=list)  # [h, w, 4] per level (uint8 / float16 / float32)
+    texture_format: int = abi.FORMAT_R8G8B8A8_UNORM
     sampler: dict = field(default_factory=dict)
     blend: tuple = None               # (srcC, dstC, opC, srcA, dstA, opA) or None
     cull_mode: int = abi.CULL_NONE
@@ -180,6 +181,109 @@ def scene_textured_small(n_tris=200, width=128, height=96, tex_size=64, mip=True
     return s
 
 
+def uv_sphere(rng, seg_u, seg_v, radius=1.0, noise_sigma=0.0):
+    """Vertices and uint32 indices of a uv-sphere with seg_u x seg_v quads
+    (2 triangles each, the pole rows degenerate), optional radial Gaussian
+    displacement, uv = (u, v) in [0,1]^2, RGBA uniform in [0,1]."""
+    nu, nv = seg_u + 1, seg_v + 1
+    th = np.linspace(0.0, 2.0 * math.pi, nu)
+    ph = np.linspace(0.0, math.pi, nv)
+    TH, PH = np.meshgrid(th, ph)
+    r = radius * (1.0 + (rng.normal(0.0, noise_sigma, TH.shape) if noise_sigma > 0 else 0.0))
+    x = r * np.sin(PH) * np.cos(TH)
+    y = r * np.cos(PH)
+    z = r * np.sin(PH) * np.sin(TH)
+    v = np.zeros((nu * nv, VERTEX_FLOATS), np.float32)
+    v[:, 0], v[:, 1], v[:, 2], v[:, 3] = x.reshape(-1), y.reshape(-1), z.reshape(-1), 1.0
+    v[:, 4:8] = rng.uniform(0.0, 1.0, (nu * nv, 4))
+    U, V = np.meshgrid(np.linspace(0.0, 1.0, nu), np.linspace(0.0, 1.0, nv))
+    v[:, 8], v[:, 9] = U.reshape(-1), V.reshape(-1)
+    j, i = np.meshgrid(np.arange(seg_v, dtype=np.uint32), np.arange(seg_u, dtype=np.uint32), indexing="ij")
+    a = (j * nu + i).reshape(-1)
+    b, c = a + 1, a + nu
+    d = c + 1
+    idx = np.stack([a, c, b, b, c, d], axis=1).reshape(-1).astype(np.uint32)
+    return v, idx
+
+
+def look_at(eye, target=(0.0, 0.0, 0.0), up=(0.0, 1.0, 0.0)):
+    eye, target, up = (np.asarray(a, np.float64) for a in (eye, target, up))
+    f = target - eye
+    f /= np.linalg.norm(f)
+    if abs(np.dot(f, up)) > 0.99:
+        up = np.array([1.0, 0.0, 0.0])
+    sd = np.cross(f, up)
+    sd /= np.linalg.norm(sd)
+    u = np.cross(sd, f)
+    m = np.eye(4)
+    m[0, :3], m[1, :3], m[2, :3] = sd, u, -f
+    m[:3, 3] = -m[:3, :3] @ eye
+    return m
+
+
+def scene_sphere_fp32(seg=100, width=512, height=512, tex_size=1024, seed_index=3, texels=None):
+    """Adjoint workload, forward part: a seg x seg uv-sphere (~2*seg^2
+    triangles) under a fixed perspective MVP, RGBA32F texture uniform in [0,1]
+    sampled bilinearly with CLAMP (the fp32 SamplerCore path), FP32 vertex
+    colours, colour = texel * vertex colour, RGBA32F attachment, depth LESS."""
+    rng = _rng(seed_index)
+    v, idx = uv_sphere(rng, seg, seg)
+    tex = texels if texels is not None else rng.uniform(0.0, 1.0, (tex_size, tex_size, 4)).astype(np.float32)
+    mvp = perspective_vk(45.0, width / height, 0.1, 100.0) @ look_at((0.4, 0.6, 3.0))
+    return Scene(name="sphere%d_fp32_%dx%d" % (len(idx) // 3, width, height), width=width, height=height,
+                 vertices=v, indices=idx, tri_count=len(idx) // 3, mvp=mvp.astype(np.float32),
+                 fragment_shader=abi.FS_TEX_X_VCOLOR, texture_levels=[np.ascontiguousarray(tex)],
+                 texture_format=abi.FORMAT_R32G32B32A32_SFLOAT,
+                 sampler=dict(mag_filter=abi.FILTER_LINEAR, min_filter=abi.FILTER_LINEAR,
+                              mipmap_mode=abi.MIPMAP_MODE_NEAREST, address_u=abi.ADDRESS_CLAMP_TO_EDGE,
+                              address_v=abi.ADDRESS_CLAMP_TO_EDGE, mip_lod_bias=0.0, min_lod=0.0, max_lod=0.0),
+                 color_format=abi.FORMAT_R32G32B32A32_SFLOAT, clear_color=(0.0, 0.0, 0.0, 0.0))
+
+
+def float_mip_chain(level0, dtype):
+    """Box-filtered chain of a float image (averaged in float64, stored as dtype)."""
+    levels = [np.ascontiguousarray(level0.astype(dtype))]
+    cur = level0.astype(np.float64)
+    while cur.shape[0] > 1 or cur.shape[1] > 1:
+        h, w = cur.shape[:2]
+        if h > 1:
+            cur = 0.5 * (cur[0:h // 2 * 2:2] + cur[1:h // 2 * 2:2])
+        if w > 1:
+            cur = 0.5 * (cur[:, 0:w // 2 * 2:2] + cur[:, 1:w // 2 * 2:2])
+        levels.append(np.ascontiguousarray(cur.astype(dtype)))
+    return levels
+
+
+def scene_sphere_views(view, n_views=256, seg_u=250, seg_v=200, width=512, height=512, tex_size=2048,
+                       seed_index=4, mesh=None, levels=None):
+    """Batched-adjoint workload, one view: a ~100k-triangle sphere with radial
+    N(0, 0.02^2) displacement seen from camera 'view' of n_views placed
+    uniformly on a radius-3 sphere; RGBA16F mipmapped texture, trilinear;
+    premultiplied-alpha OVER (ONE, ONE_MINUS_SRC_ALPHA) into RGBA16F."""
+    rng = _rng(seed_index)
+    if mesh is None:
+        mesh = uv_sphere(rng, seg_u, seg_v, noise_sigma=0.02)
+    v, idx = mesh
+    if levels is None:
+        tex0 = rng.uniform(0.0, 1.0, (tex_size, tex_size, 4))
+        levels = float_mip_chain(tex0, np.float16)
+    crng = np.random.Generator(np.random.PCG64(SEED_BASE + 0x100 + seed_index))
+    dirs = crng.normal(0.0, 1.0, (n_views, 3))
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    eye = 3.0 * dirs[view]
+    mvp = perspective_vk(45.0, width / height, 0.1, 100.0) @ look_at(eye)
+    return Scene(name="spherenoise%d_view%d" % (len(idx) // 3, view), width=width, height=height, vertices=v,
+                 indices=idx, tri_count=len(idx) // 3, mvp=mvp.astype(np.float32),
+                 fragment_shader=abi.FS_TEX_X_VCOLOR, texture_levels=levels,
+                 texture_format=abi.FORMAT_R16G16B16A16_SFLOAT,
+                 sampler=dict(mag_filter=abi.FILTER_LINEAR, min_filter=abi.FILTER_LINEAR,
+                              mipmap_mode=abi.MIPMAP_MODE_LINEAR, address_u=abi.ADDRESS_REPEAT,
+                              address_v=abi.ADDRESS_CLAMP_TO_EDGE, mip_lod_bias=0.0, min_lod=0.0, max_lod=1000.0),
+                 blend=(abi.BLEND_ONE, abi.BLEND_ONE_MINUS_SRC_ALPHA, abi.BLEND_OP_ADD,
+                        abi.BLEND_ONE, abi.BLEND_ONE_MINUS_SRC_ALPHA, abi.BLEND_OP_ADD),
+                 color_format=abi.FORMAT_R16G16B16A16_SFLOAT, clear_color=(0.0, 0.0, 0.0, 0.0))
+
+
 def build_state(scene, color_ptr, depth_ptr, vertex_ptr, level_ptrs=None, color_pitch=None, depth_pitch=None):
     """PipelineState for a scene given buffer addresses (device pointers for
     the GB300 path, host pointers for the oracle)."""
@@ -223,7 +327,7 @@ def build_state(scene, color_ptr, depth_ptr, vertex_ptr, level_ptrs=None, color_
     st.framebuffer_width, st.framebuffer_height = scene.width, scene.height
     if scene.fragment_shader == abi.FS_TEX_X_VCOLOR:
         t = st.texture
-        t.format = abi.FORMAT_R8G8B8A8_UNORM
+        t.format = scene.texture_format
         t.level_count = len(scene.texture_levels)
         for i, lv in enumerate(scene.texture_levels):
             t.levels[i] = abi.TextureLevel(level_ptrs[i], lv.shape[1], lv.shape[0], lv.shape[1], 0)

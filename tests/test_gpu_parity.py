@@ -152,3 +152,53 @@ def test_span_scratch_fallback(gpu_lib, monkeypatch, rows):
     monkeypatch.setenv("SWGB_SPAN_ROWS", rows if rows != "0" else "1")
     check_scene(scenes.scene_textured_small(n_tris=150, width=96, height=72), gpu_lib)
     check_scene(scenes.scene_heightfield(quads_x=60, quads_y=30, width=160, height=96, tex_size=64), gpu_lib)
+
+
+def _float_variant(tex_fmt, color_fmt, blend, address, mip, seed=31):
+    """Random textured triangles with float textures / float attachments."""
+    s = scenes.scene_textured_small(n_tris=180, width=80, height=64, tex_size=32, mip=mip, address=address,
+                                    blend=False, seed_index=seed)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    dt = np.float16 if tex_fmt == abi.FORMAT_R16G16B16A16_SFLOAT else np.float32
+    if tex_fmt != abi.FORMAT_R8G8B8A8_UNORM:
+        base = rng.uniform(-0.25, 1.5, (32, 32, 4))
+        s.texture_levels = scenes.float_mip_chain(base, dt) if mip else [base.astype(dt)]
+        s.texture_format = tex_fmt
+    s.color_format = color_fmt
+    s.clear_color = (0.1, 0.2, 0.3, 0.4) if color_fmt != abi.FORMAT_R8G8B8A8_UNORM else (10, 20, 30, 40)
+    if blend:
+        s.blend = (abi.BLEND_ONE, abi.BLEND_ONE_MINUS_SRC_ALPHA, abi.BLEND_OP_ADD,
+                   abi.BLEND_ONE, abi.BLEND_ONE_MINUS_SRC_ALPHA, abi.BLEND_OP_ADD)
+    return s
+
+
+@pytest.mark.parametrize("tex_fmt,color_fmt,blend,address,mip", [
+    (abi.FORMAT_R32G32B32A32_SFLOAT, abi.FORMAT_R32G32B32A32_SFLOAT, False, abi.ADDRESS_CLAMP_TO_EDGE, False),
+    (abi.FORMAT_R32G32B32A32_SFLOAT, abi.FORMAT_R32G32B32A32_SFLOAT, True, abi.ADDRESS_REPEAT, True),
+    (abi.FORMAT_R16G16B16A16_SFLOAT, abi.FORMAT_R16G16B16A16_SFLOAT, True, abi.ADDRESS_REPEAT, True),
+    (abi.FORMAT_R16G16B16A16_SFLOAT, abi.FORMAT_R32G32B32A32_SFLOAT, False, abi.ADDRESS_MIRRORED_REPEAT, True),
+    (abi.FORMAT_R32G32B32A32_SFLOAT, abi.FORMAT_R8G8B8A8_UNORM, True, abi.ADDRESS_CLAMP_TO_EDGE, True),
+    (abi.FORMAT_R8G8B8A8_UNORM, abi.FORMAT_R16G16B16A16_SFLOAT, True, abi.ADDRESS_REPEAT, True),
+])
+def test_float_texture_and_attachment_formats(gpu_lib, tex_fmt, color_fmt, blend, address, mip):
+    """fp32 SamplerCore path (RGBA16F / RGBA32F textures) and float colour
+    attachments (Reactor's Half/Float conversions), bit for bit."""
+    check_scene(_float_variant(tex_fmt, color_fmt, blend, address, mip), gpu_lib)
+
+
+def test_sphere_fp32_full_size(gpu_lib):
+    """The adjoint workload's forward frame: 20k-triangle uv-sphere, 1024^2
+    RGBA32F texture bilinear CLAMP, RGBA32F attachment at 512^2."""
+    cnt = check_scene(scenes.scene_sphere_fp32(), gpu_lib)
+    assert cnt["triangles_visible"] > 10000
+
+
+def test_sphere_views_rgba16f_reduced(gpu_lib):
+    """The batched-adjoint workload's views (noisy sphere, RGBA16F mipmapped
+    trilinear, premultiplied OVER into RGBA16F) at reduced size, three views."""
+    rng = np.random.Generator(np.random.PCG64(4))
+    mesh = scenes.uv_sphere(rng, 60, 40, noise_sigma=0.02)
+    levels = scenes.float_mip_chain(rng.uniform(0.0, 1.0, (128, 128, 4)), np.float16)
+    for view in (0, 7, 200):
+        s = scenes.scene_sphere_views(view, width=96, height=96, mesh=mesh, levels=levels)
+        check_scene(s, gpu_lib)
