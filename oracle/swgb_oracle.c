@@ -142,14 +142,25 @@ typedef struct {
     int blend;               /* alpha blend active after simplification  */
     uint32_t srcC, dstC, opC, srcA, dstA, opA; /* simplified blend state */
     int rows;                /* span rows per primitive (fb height + 2)  */
+    int ms;                  /* samples: 1 or 4                          */
 } ODraw;
+
+/* 4x MSAA sample positions (src/Pipeline/Constants.hpp:26-52,
+ * src/Pipeline/Constants.cpp:293-294): VkSampleLocations4 relative to the
+ * pixel centre (SampleLocationsX/Y) and in sub-pixel fixed point (Xf/Yf). */
+static const float SLX[4] = { 0.375f - 0.5f, 0.875f - 0.5f, 0.125f - 0.5f, 0.625f - 0.5f };
+static const float SLY[4] = { 0.125f - 0.5f, 0.375f - 0.5f, 0.625f - 0.5f, 0.875f - 0.5f };
+static const int XF[4] = { -32, 96, -96, 32 };
+static const int YF[4] = { -96, -32, 32, 96 };
+#define Y_MIN_MS_OFFSET 159 /* 256 - toFixedPoint(0.375) - 1 */
+#define Y_MAX_MS_OFFSET 351 /* 256 + toFixedPoint(0.375) - 1 */
 
 typedef struct {
     int visible;
     int yMin, yMax;
     float x0, y0;
     OPlane z, w, V[MAXV];
-    uint16_t *left, *right; /* indexed [y + 1] */
+    uint16_t *left[4], *right[4]; /* per sample, indexed [y + 1] */
 } OPrim;
 
 /* ------------------------------------------------------------------------ */
@@ -209,7 +220,7 @@ static swgb_status prepare(ODraw *d, const swgb_pipeline_state *st, const swgb_d
     d->args = a;
     if(st->precision_profile != SWGB_PRECISION_CMAKE) return SWGB_UNSUPPORTED_STATE;
     if(st->topology != SWGB_TOPOLOGY_TRIANGLE_LIST) return SWGB_UNSUPPORTED_STATE;
-    if(st->sample_count != 1) return SWGB_UNSUPPORTED_STATE;
+    if(st->sample_count != 1 && st->sample_count != 4) return SWGB_UNSUPPORTED_STATE;
     if(st->depth_clamp_enable || st->depth_bias_constant != 0.0f || st->depth_bias_slope != 0.0f) return SWGB_UNSUPPORTED_STATE;
     if(st->attrib_count < 1 || st->attrib_count > SWGB_MAX_ATTRIBS) return SWGB_INVALID_ARG;
     if(st->color_format != SWGB_FORMAT_R8G8B8A8_UNORM && st->color_format != SWGB_FORMAT_R32G32B32A32_SFLOAT &&
@@ -277,6 +288,7 @@ static swgb_status prepare(ODraw *d, const swgb_pipeline_state *st, const swgb_d
     if(st->color_blend_op > SWGB_BLEND_OP_MAX || st->alpha_blend_op > SWGB_BLEND_OP_MAX) return SWGB_UNSUPPORTED_STATE;
 
     d->rows = (int)st->framebuffer_height + 2;
+    d->ms = (int)st->sample_count;
     return SWGB_OK;
 }
 
@@ -451,7 +463,7 @@ static inline int32_t clampi(int32_t x, int32_t lo, int32_t hi) { return x < lo 
 static inline int32_t shl(int32_t x, int s) { return (int32_t)((uint32_t)x << s); }
 
 /* SetupRoutine::edge (SetupRoutine.cpp:550-621) */
-static void setup_edge(const ODraw *d, OPrim *pr, int32_t Xa, int32_t Ya, int32_t Xb, int32_t Yb)
+static void setup_edge(const ODraw *d, OPrim *pr, int q, int32_t Xa, int32_t Ya, int32_t Xb, int32_t Yb)
 {
     if(Ya == Yb) return;
     int swap = Yb < Ya;
@@ -462,7 +474,7 @@ static void setup_edge(const ODraw *d, OPrim *pr, int32_t Xa, int32_t Ya, int32_
     int32_t yMin = y1 > d->sy0 ? y1 : d->sy0;
     int32_t yMax = y2 < d->sy1 ? y2 : d->sy1;
     if(!(yMin < yMax)) return;
-    uint16_t *edge = swap ? pr->right : pr->left;
+    uint16_t *edge = swap ? pr->right[q] : pr->left[q];
     int32_t DX12 = X2 - X1, DY12 = Y2 - Y1;
     int32_t FDX12 = shl(DX12, 8), FDY12 = shl(DY12, 8);
     int32_t X = DX12 * (shl(y1, 8) - Y1) + (X1 & 0xFF) * DY12;
@@ -538,26 +550,61 @@ static int setup_triangle(const ODraw *d, const OVertex *tv0, const OVertex *tv1
         yMin = Y[i] < yMin ? Y[i] : yMin;
         yMax = Y[i] > yMax ? Y[i] : yMax;
     }
-    yMin = (yMin + 0xFF) >> 8;
-    yMax = (yMax + 0xFF) >> 8;
+    if(d->ms > 1)
+    {
+        yMin = (yMin + Y_MIN_MS_OFFSET) >> 8;
+        yMax = (yMax + Y_MAX_MS_OFFSET) >> 8;
+    }
+    else
+    {
+        yMin = (yMin + 0xFF) >> 8;
+        yMax = (yMax + 0xFF) >> 8;
+    }
     yMin = yMin > d->sy0 ? yMin : d->sy0;
     yMax = yMax < d->sy1 ? yMax : d->sy1;
     if(yMin >= yMax) return 0;
 
-    /* Rasterize the outline (:201-240) */
-    X[n] = X[0];
-    Y[n] = Y[0];
-    for(int i = 0; i < n; i++)
-        setup_edge(d, pr, X[i + 1 - dW], Y[i + 1 - dW], X[i + dW], Y[i + dW]);
-
-    /* Trim empty rows and pad (:243-264) */
-    while(yMin < yMax && pr->left[yMin + 1] == pr->right[yMin + 1]) yMin++;
-    while(yMax > yMin && pr->left[yMax - 1 + 1] == pr->right[yMax - 1 + 1]) yMax--;
-    if(yMin == yMax) return 0;
-    pr->left[yMin - 1 + 1] = pr->left[yMin + 1];
-    pr->right[yMin - 1 + 1] = pr->left[yMin + 1];
-    pr->left[yMax + 1] = pr->left[yMax - 1 + 1];
-    pr->right[yMax + 1] = pr->left[yMax - 1 + 1];
+    /* Rasterize the outline of every sample (:188-240) */
+    for(int q = 0; q < d->ms; q++)
+    {
+        int32_t Xq[17], Yq[17];
+        for(int i = 0; i < n; i++)
+        {
+            Xq[i] = X[i];
+            Yq[i] = Y[i];
+            if(d->ms > 1)
+            {
+                /* the edge is tested against the sample point (:199-203) */
+                Xq[i] = Xq[i] - XF[q];
+                Yq[i] = Yq[i] - YF[q];
+            }
+        }
+        if(d->ms > 1)
+        {
+            int32_t x = clampi((X[0] + 0xFF) >> 8, d->sx0, d->sx1);
+            for(int32_t y = yMin - 1; y < yMax + 1; y++)
+            {
+                pr->left[q][y + 1] = (uint16_t)x;
+                pr->right[q][y + 1] = (uint16_t)x;
+            }
+        }
+        Xq[n] = Xq[0];
+        Yq[n] = Yq[0];
+        for(int i = 0; i < n; i++)
+            setup_edge(d, pr, q, Xq[i + 1 - dW], Yq[i + 1 - dW], Xq[i + dW], Yq[i + dW]);
+        if(d->ms == 1)
+        {
+            /* Trim empty rows and pad (:243-264) */
+            uint16_t *L = pr->left[0], *R = pr->right[0];
+            while(yMin < yMax && L[yMin + 1] == R[yMin + 1]) yMin++;
+            while(yMax > yMin && L[yMax - 1 + 1] == R[yMax - 1 + 1]) yMax--;
+            if(yMin == yMax) return 0;
+            L[yMin - 1 + 1] = L[yMin + 1];
+            R[yMin - 1 + 1] = L[yMin + 1];
+            L[yMax + 1] = L[yMax - 1 + 1];
+            R[yMax + 1] = L[yMax - 1 + 1];
+        }
+    }
     pr->yMin = yMin;
     pr->yMax = yMax;
 
@@ -1045,10 +1092,10 @@ static uint16_t float_to_half(float f)
     return fp16i;
 }
 
-static void read_color(const ODraw *d, int x, int y, float dst[4])
+static void read_color(const ODraw *d, int q, int x, int y, float dst[4])
 {
     const swgb_pipeline_state *st = d->st;
-    uint8_t *row = (uint8_t *)st->color + (size_t)y * st->color_pitch_bytes;
+    uint8_t *row = (uint8_t *)st->color + (size_t)q * st->color_slice_bytes + (size_t)y * st->color_pitch_bytes;
     if(st->color_format == SWGB_FORMAT_R8G8B8A8_UNORM)
     {
         /* readPixel (PixelRoutine.cpp:1111-1130) widens b to b*257; alphaBlend
@@ -1065,10 +1112,10 @@ static void read_color(const ODraw *d, int x, int y, float dst[4])
     }
 }
 
-static void write_color(const ODraw *d, int x, int y, const float col[4])
+static void write_color(const ODraw *d, int q, int x, int y, const float col[4])
 {
     const swgb_pipeline_state *st = d->st;
-    uint8_t *row = (uint8_t *)st->color + (size_t)y * st->color_pitch_bytes;
+    uint8_t *row = (uint8_t *)st->color + (size_t)q * st->color_slice_bytes + (size_t)y * st->color_pitch_bytes;
     uint32_t wm = st->color_write_mask;
     if(st->color_format == SWGB_FORMAT_R8G8B8A8_UNORM)
     {
@@ -1097,8 +1144,16 @@ static void write_color(const ODraw *d, int x, int y, const float col[4])
     }
 }
 
-/* One 2x2 quad of one primitive (PixelRoutine::quad, single-sample). */
-static void pixel_quad(const ODraw *d, const OSampler *smp, const OPrim *pr, int x, int y, int cMask, swgb_counters *cnt)
+static float *depth_at(const ODraw *d, int q, int x, int y)
+{
+    const swgb_pipeline_state *st = d->st;
+    return (float *)((uint8_t *)st->depth + (size_t)q * st->depth_slice_bytes + (size_t)y * st->depth_pitch_bytes + (size_t)x * 4);
+}
+
+/* One 2x2 quad of one primitive (PixelRoutine::quad :97-358); cMask[q] holds
+ * the lane coverage of sample q.  The shader runs once per quad at the pixel
+ * centres (no per-sample shading); depth and colour are per sample. */
+static void pixel_quad(const ODraw *d, const OSampler *smp, const OPrim *pr, int x, int y, const int cMask[4], swgb_counters *cnt)
 {
     const swgb_pipeline_state *st = d->st;
     float xF[4], yF[4];
@@ -1107,13 +1162,20 @@ static void pixel_quad(const ODraw *d, const OSampler *smp, const OPrim *pr, int
         xF[i] = fsub(fadd((float)x, (float)(i & 1)), pr->x0);
         yF[i] = fsub(fadd((float)y, (float)(i >> 1)), pr->y0);
     }
-    float z[4] = { 0, 0, 0, 0 };
+    float z[4][4] = { { 0 } };
     if(d->interpolateZ)
-        for(int i = 0; i < 4; i++)
-        {
-            float Dz = fadd(pr->z.C, fmul(yF[i], pr->z.B));
-            z[i] = ffma(xF[i], pr->z.A, Dz);
-        }
+        for(int q = 0; q < d->ms; q++)
+            for(int i = 0; i < 4; i++)
+            {
+                float yq = yF[i], xq = xF[i];
+                if(d->ms > 1)
+                {
+                    yq = fadd(yq, SLY[q]); /* QuadRasterizer.cpp:131-141 */
+                    xq = fsub(xq, SLX[q]); /* PixelRoutine.cpp:128-148 */
+                }
+                float Dz = fadd(pr->z.C, fmul(yq, pr->z.B));
+                z[q][i] = ffma(xq, pr->z.A, Dz);
+            }
     /* w, rhw (:196-199) and varyings (:231-261) */
     float rhw[4];
     for(int i = 0; i < 4; i++)
@@ -1148,66 +1210,66 @@ static void pixel_quad(const ODraw *d, const OSampler *smp, const OPrim *pr, int
         for(int i = 0; i < 4; i++)
             for(int k = 0; k < 4; k++) c[i][k] = fminr(fmaxr(c[i][k], 0.0f), 1.0f);
 
-    /* late depth test (:330-344), depth write (:715-739) */
-    int zMask = cMask;
-    if(d->depthTest)
+    for(int q = 0; q < d->ms; q++)
     {
-        zMask = 0;
+        /* late depth test (:330-344), depth write (:715-739) */
+        int zMask = cMask[q];
+        if(d->depthTest)
+        {
+            zMask = 0;
+            for(int i = 0; i < 4; i++)
+            {
+                if(!(cMask[q] & (1 << i))) continue;
+                float Z = z[q][i];
+                if(d->depthClamp) Z = fminr(fmaxr(Z, d->minDepthClamp), d->maxDepthClamp);
+                z[q][i] = Z;
+                float zb = *depth_at(d, q, x + (i & 1), y + (i >> 1));
+                int pass;
+                switch(st->depth_compare_op)
+                {
+                case SWGB_COMPARE_NEVER: pass = 0; break;
+                case SWGB_COMPARE_LESS: pass = !fle(zb, Z); break;
+                case SWGB_COMPARE_EQUAL: pass = feq(zb, Z); break;
+                case SWGB_COMPARE_LESS_OR_EQUAL: pass = !flt(zb, Z); break;
+                case SWGB_COMPARE_GREATER: pass = flt(zb, Z); break;
+                case SWGB_COMPARE_NOT_EQUAL: pass = !feq(zb, Z); break;
+                case SWGB_COMPARE_GREATER_OR_EQUAL: pass = fle(zb, Z); break;
+                default: pass = 1; break;
+                }
+                if(pass) zMask |= 1 << i;
+            }
+            if(cnt) cnt->fragments_tested += (uint64_t)__builtin_popcount((unsigned)cMask[q]);
+            if(d->depthWrite)
+                for(int i = 0; i < 4; i++)
+                    if(zMask & (1 << i)) *depth_at(d, q, x + (i & 1), y + (i >> 1)) = z[q][i];
+        }
+        if(cnt) cnt->fragments_passed += (uint64_t)__builtin_popcount((unsigned)zMask);
+
+        /* blendColor / alphaBlend / writeColor per sample plane (PixelProgram.cpp:261-284) */
         for(int i = 0; i < 4; i++)
         {
-            if(!(cMask & (1 << i))) continue;
+            if(!(zMask & (1 << i))) continue;
             int px = x + (i & 1), py = y + (i >> 1);
-            float Z = z[i];
-            if(d->depthClamp) Z = fminr(fmaxr(Z, d->minDepthClamp), d->maxDepthClamp);
-            z[i] = Z;
-            float zb = *(float *)((uint8_t *)st->depth + (size_t)py * st->depth_pitch_bytes + (size_t)px * 4);
-            int pass;
-            switch(st->depth_compare_op)
+            float out[4];
+            if(d->blend)
             {
-            case SWGB_COMPARE_NEVER: pass = 0; break;
-            case SWGB_COMPARE_LESS: pass = !fle(zb, Z); break;
-            case SWGB_COMPARE_EQUAL: pass = feq(zb, Z); break;
-            case SWGB_COMPARE_LESS_OR_EQUAL: pass = !flt(zb, Z); break;
-            case SWGB_COMPARE_GREATER: pass = flt(zb, Z); break;
-            case SWGB_COMPARE_NOT_EQUAL: pass = !feq(zb, Z); break;
-            case SWGB_COMPARE_GREATER_OR_EQUAL: pass = fle(zb, Z); break;
-            default: pass = 1; break;
+                float dst[4];
+                read_color(d, q, px, py, dst);
+                float sf[4], df[4];
+                for(int k = 0; k < 3; k++)
+                {
+                    sf[k] = blend_factor(d->srcC, c[i], dst, k);
+                    df[k] = blend_factor(d->dstC, c[i], dst, k);
+                }
+                sf[3] = blend_factor(d->srcA, c[i], dst, 3);
+                df[3] = blend_factor(d->dstA, c[i], dst, 3);
+                for(int k = 0; k < 3; k++) out[k] = blend_op(d->opC, c[i][k], sf[k], dst[k], df[k]);
+                out[3] = blend_op(d->opA, c[i][3], sf[3], dst[3], df[3]);
             }
-            if(pass) zMask |= 1 << i;
+            else
+                memcpy(out, c[i], sizeof(out));
+            write_color(d, q, px, py, out);
         }
-        if(cnt) cnt->fragments_tested += (uint64_t)__builtin_popcount((unsigned)cMask);
-        if(zMask == 0) return;
-        if(d->depthWrite)
-            for(int i = 0; i < 4; i++)
-                if(zMask & (1 << i))
-                    *(float *)((uint8_t *)st->depth + (size_t)(y + (i >> 1)) * st->depth_pitch_bytes + (size_t)(x + (i & 1)) * 4) = z[i];
-    }
-    if(cnt) cnt->fragments_passed += (uint64_t)__builtin_popcount((unsigned)zMask);
-
-    /* blendColor / alphaBlend / writeColor (PixelProgram.cpp:261-284) */
-    for(int i = 0; i < 4; i++)
-    {
-        if(!(zMask & (1 << i))) continue;
-        int px = x + (i & 1), py = y + (i >> 1);
-        float out[4];
-        if(d->blend)
-        {
-            float dst[4];
-            read_color(d, px, py, dst);
-            float sf[4], df[4];
-            for(int k = 0; k < 3; k++)
-            {
-                sf[k] = blend_factor(d->srcC, c[i], dst, k);
-                df[k] = blend_factor(d->dstC, c[i], dst, k);
-            }
-            sf[3] = blend_factor(d->srcA, c[i], dst, 3);
-            df[3] = blend_factor(d->dstA, c[i], dst, 3);
-            for(int k = 0; k < 3; k++) out[k] = blend_op(d->opC, c[i][k], sf[k], dst[k], df[k]);
-            out[3] = blend_op(d->opA, c[i][3], sf[3], dst[3], df[3]);
-        }
-        else
-            memcpy(out, c[i], sizeof(out));
-        write_color(d, px, py, out);
     }
 }
 
@@ -1222,19 +1284,30 @@ static void raster_cluster(const ODraw *d, const OSampler *smp, const OPrim *pr,
     yMin += cluster2;
     for(int y = yMin; y < yMax; y += 2 * clusterCount)
     {
-        int l0 = pr->left[y + 1], l1 = pr->left[y + 2];
-        int r0 = pr->right[y + 1], r1 = pr->right[y + 2];
-        int x0 = (l0 < l1 ? l0 : l1) & ~1;
-        int x1 = r0 > r1 ? r0 : r1;
-        int16_t xl[4] = { (int16_t)(l0 - 1), (int16_t)(l0 - 2), (int16_t)(l1 - 1), (int16_t)(l1 - 2) };
-        int16_t xr[4] = { (int16_t)(r0 - 0), (int16_t)(r0 - 1), (int16_t)(r1 - 0), (int16_t)(r1 - 1) };
+        int x0 = 0x7FFFFFFF, x1 = -0x7FFFFFFF;
+        int16_t xl[4][4], xr[4][4];
+        for(int q = 0; q < d->ms; q++)
+        {
+            int l0 = pr->left[q][y + 1], l1 = pr->left[q][y + 2];
+            int r0 = pr->right[q][y + 1], r1 = pr->right[q][y + 2];
+            int a = l0 < l1 ? l0 : l1, b = r0 > r1 ? r0 : r1;
+            x0 = a < x0 ? a : x0;
+            x1 = b > x1 ? b : x1;
+            xl[q][0] = (int16_t)(l0 - 1); xl[q][1] = (int16_t)(l0 - 2); xl[q][2] = (int16_t)(l1 - 1); xl[q][3] = (int16_t)(l1 - 2);
+            xr[q][0] = (int16_t)(r0 - 0); xr[q][1] = (int16_t)(r0 - 1); xr[q][2] = (int16_t)(r1 - 0); xr[q][3] = (int16_t)(r1 - 1);
+        }
+        x0 &= ~1;
         for(int x = x0; x < x1; x += 2)
         {
             int16_t xx = (int16_t)x;
-            int cMask = 0;
-            for(int i = 0; i < 4; i++)
-                if(xx > xl[i] && xr[i] > xx) cMask |= 1 << i;
-            if(cMask == 0) continue;
+            int cMask[4] = { 0, 0, 0, 0 }, any = 0;
+            for(int q = 0; q < d->ms; q++)
+            {
+                for(int i = 0; i < 4; i++)
+                    if(xx > xl[q][i] && xr[q][i] > xx) cMask[q] |= 1 << i;
+                any |= cMask[q];
+            }
+            if(any == 0) continue;
             if(cnt) cnt->quads++;
             pixel_quad(d, smp, pr, x, y, cMask, cnt);
         }
@@ -1277,8 +1350,11 @@ static void run_setup(OJob *j, int t)
         for(uint32_t i = start; i < end; i++)
         {
             OPrim *pr = &j->prims[i];
-            pr->left = j->spans + (size_t)i * 2 * d->rows;
-            pr->right = pr->left + d->rows;
+            for(int q = 0; q < 4; q++)
+            {
+                pr->left[q] = j->spans + ((size_t)i * 8 + 2 * q) * d->rows;
+                pr->right[q] = pr->left[q] + d->rows;
+            }
             int clipped = 0;
             int vis = process_triangle(d, j->first + i, pr, &j->local[t], &clipped);
             j->local[t].triangles_in++;
@@ -1355,7 +1431,7 @@ swgb_status oracle_draw(const swgb_pipeline_state *st, const swgb_draw_args *a, 
     j.nthreads = nthreads;
     pthread_mutex_init(&j.mu, NULL);
     j.prims = (OPrim *)calloc(group, sizeof(OPrim));
-    j.spans = (uint16_t *)malloc((size_t)group * 2 * d.rows * sizeof(uint16_t));
+    j.spans = (uint16_t *)malloc((size_t)group * 8 * d.rows * sizeof(uint16_t));
     if(!j.prims || !j.spans)
     {
         free(j.prims);
@@ -1410,10 +1486,13 @@ int oracle_setup(const swgb_pipeline_state *st, const swgb_draw_args *a, uint32_
     if(prepare(&d, st, a) != SWGB_OK) return -1;
     OPrim pr;
     memset(&pr, 0, sizeof(pr));
-    uint16_t *buf = (uint16_t *)calloc((size_t)2 * d.rows, sizeof(uint16_t));
+    uint16_t *buf = (uint16_t *)calloc((size_t)8 * d.rows, sizeof(uint16_t));
     if(!buf) return -1;
-    pr.left = buf;
-    pr.right = buf + d.rows;
+    for(int q = 0; q < 4; q++)
+    {
+        pr.left[q] = buf + (size_t)2 * q * d.rows;
+        pr.right[q] = pr.left[q] + d.rows;
+    }
     int clipped = 0;
     int vis = process_triangle(&d, tri, &pr, NULL, &clipped);
     out_i[0] = vis ? pr.yMin : 0;
@@ -1423,8 +1502,8 @@ int oracle_setup(const swgb_pipeline_state *st, const swgb_draw_args *a, uint32_
     if(vis && spans)
         for(int y = pr.yMin; y < pr.yMax && y - pr.yMin < max_rows; y++)
         {
-            spans[2 * (y - pr.yMin) + 0] = pr.left[y + 1];
-            spans[2 * (y - pr.yMin) + 1] = pr.right[y + 1];
+            spans[2 * (y - pr.yMin) + 0] = pr.left[0][y + 1];
+            spans[2 * (y - pr.yMin) + 1] = pr.right[0][y + 1];
         }
     if(vis && out_f)
     {

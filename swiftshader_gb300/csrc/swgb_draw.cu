@@ -54,6 +54,15 @@ enum { CLIP_RIGHT = 1 << 0, CLIP_TOP = 1 << 1, CLIP_FAR = 1 << 2, CLIP_LEFT = 1 
 
 enum { OP_ZERO_EXT = 1000, OP_SRC_EXT = 1001, OP_DST_EXT = 1002 };
 
+// 4x MSAA sample positions (src/Pipeline/Constants.hpp:26-52, Constants.cpp:293-294):
+// VkSampleLocations4 relative to the pixel centre, and in sub-pixel fixed point.
+__device__ constexpr float SLX[4] = {0.375f - 0.5f, 0.875f - 0.5f, 0.125f - 0.5f, 0.625f - 0.5f};
+__device__ constexpr float SLY[4] = {0.125f - 0.5f, 0.375f - 0.5f, 0.625f - 0.5f, 0.875f - 0.5f};
+__device__ constexpr int XF[4] = {-32, 96, -96, 32};
+__device__ constexpr int YF[4] = {-96, -32, 32, 96};
+constexpr int Y_MIN_MS_OFFSET = 159;  // 256 - toFixedPoint(0.375) - 1
+constexpr int Y_MAX_MS_OFFSET = 351;  // 256 + toFixedPoint(0.375) - 1
+
 enum { ERR_INDEX_RANGE = 1, ERR_POLY_OVERFLOW = 2 };
 
 struct TexLevel {
@@ -67,8 +76,8 @@ struct TexLevel {
 struct TriInfo {
     uint32_t info;     // bits 0-4: polygon vertex count, bit 5: winding d, bit 6: clipped, bit 7: spans stored
     uint32_t slot;     // clipped polygon slot
-    uint32_t spanOff;  // span-buffer index of row y0 (when stored)
-    uint32_t pad;
+    uint32_t spanOff;  // span-buffer index of row y0 of sample 0 (when stored)
+    uint32_t rows;     // rows per sample plane in the span buffer
 };
 
 // Everything a draw's kernels read, baked on the host from the pipeline state
@@ -100,6 +109,8 @@ struct DrawParams {
     uint32_t srcC, dstC, opC, srcA, dstA, opA;
     uint32_t writeMask;
     int fs;
+    int ms;       // samples per pixel: 1 or 4
+    uint64_t colorSlice, depthSlice;  // bytes between sample planes
     int cf;       // colour attachment format, CF_*
     int texFloat; // 0: R8G8B8A8_UNORM texture (16-bit path), 1: RGBA16F, 2: RGBA32F (fp32 path)
     uint8_t *color;
@@ -483,8 +494,16 @@ __global__ void __launch_bounds__(SETUP_THREADS) k_setup(const __grid_constant__
                         xMinS = min(xMinS, X[i]); xMaxS = max(xMaxS, X[i]);
                     }
                     // Vertical range (SetupRoutine.cpp:147-186)
-                    yMin = max((yMin + 0xFF) >> 8, D.sy0);
-                    yMax = min((yMax + 0xFF) >> 8, D.sy1);
+                    if(D.ms > 1)
+                    {
+                        yMin = max((yMin + Y_MIN_MS_OFFSET) >> 8, D.sy0);
+                        yMax = min((yMax + Y_MAX_MS_OFFSET) >> 8, D.sy1);
+                    }
+                    else
+                    {
+                        yMin = max((yMin + 0xFF) >> 8, D.sy0);
+                        yMax = min((yMax + 0xFF) >> 8, D.sy1);
+                    }
                     cand = yMin < yMax;
                 }
             }
@@ -494,8 +513,8 @@ __global__ void __launch_bounds__(SETUP_THREADS) k_setup(const __grid_constant__
     // ---- allocate span rows: block scan + one atomic per block ----------
     __shared__ uint32_t sWarp[SETUP_THREADS / 32];
     __shared__ unsigned long long sBase;
-    uint32_t rows = cand ? (uint32_t)(yMax - yMin) : 0u;
-    uint32_t incl = rows;
+    const uint32_t rows = cand ? (uint32_t)(yMax - yMin) : 0u;
+    uint32_t incl = rows * (uint32_t)D.ms;
 #pragma unroll
     for(int o = 1; o < 32; o <<= 1)
     {
@@ -516,11 +535,32 @@ __global__ void __launch_bounds__(SETUP_THREADS) k_setup(const __grid_constant__
         sBase = tot ? atomicAdd(D.spanCount, (unsigned long long)tot) : 0ull;
     }
     __syncthreads();
-    const uint64_t off = (uint64_t)sBase + sWarp[warp] + (incl - rows);
+    const uint64_t off = (uint64_t)sBase + sWarp[warp] + (incl - rows * (uint32_t)D.ms);
 
-    if(cand)
+    bool stored = false;
+    if(cand && D.ms > 1)
     {
-        bool stored = off + rows <= (uint64_t)D.spanCapacity;
+        // 4x MSAA: one outline per sample, the polygon shifted by -Xf/-Yf
+        // (SetupRoutine.cpp:188-240); rows no edge writes stay empty and
+        // nothing is trimmed.
+        stored = off + (uint64_t)rows * 4 <= (uint64_t)D.spanCapacity;
+        if(stored)
+        {
+            for(int q = 0; q < 4; q++)
+            {
+                uint32_t *sp = D.spans + off + (uint64_t)q * rows;
+                for(uint32_t r = 0; r < rows; r++) sp[r] = 0u;
+                int32_t Xq[MAX_POLY + 1], Yq[MAX_POLY + 1];
+                for(int i = 0; i < n; i++) { Xq[i] = X[i] - XF[q]; Yq[i] = Y[i] - YF[q]; }
+                write_spans(D, Xq, Yq, n, dW, yMin, sp);
+            }
+            inf.spanOff = (uint32_t)off;
+            inf.rows = rows;
+        }
+    }
+    else if(cand)
+    {
+        stored = off + rows <= (uint64_t)D.spanCapacity;
         if(stored)
         {
             uint32_t *sp = D.spans + off;
@@ -559,15 +599,19 @@ __global__ void __launch_bounds__(SETUP_THREADS) k_setup(const __grid_constant__
                 yMax--;
             }
         }
-        if(yMin < yMax)
+    }
+    if(cand && yMin < yMax)
+    {
         {
             // pixel box: covered x satisfy ceil(Xmin/256) <= left <= x < right <= ceil(Xmax/256)
-            int32_t bx0 = max(D.sx0, (xMinS + 0xFF) >> 8);
-            int32_t bx1 = max(bx0, min(D.sx1, (xMaxS + 0xFF) >> 8));
+            const int32_t pad = D.ms > 1 ? 96 : 0;  // farthest sample offset (Xf)
+            int32_t bx0 = max(D.sx0, (xMinS - pad + 0xFF) >> 8);
+            int32_t bx1 = max(bx0, min(D.sx1, (xMaxS + pad + 0xFF) >> 8));
             {
                 cntVis = 1;
                 box = make_short4((short)bx0, (short)yMin, (short)bx1, (short)yMax);
                 inf.info = (uint32_t)n | ((uint32_t)dW << 5) | ((uint32_t)cntClip << 6) | ((uint32_t)stored << 7);
+                if(!stored) inf.rows = 0;
                 if(cntClip)
                 {
                     uint32_t slot = atomicAdd(D.polyCount, 1u);
@@ -929,17 +973,18 @@ __host__ __device__ constexpr int color_words(int cf) { return cf == CF_RGBA8 ? 
 
 // Shared memory of one warp: its bin's depth and colour, the staged batch,
 // and its ordered candidate list.
-template<int CF>
+template<int CF, int MS>
 struct RasterShared {
-    float depth[BIN * BIN];
-    uint32_t color[BIN * BIN * color_words(CF)];
+    float depth[MS][BIN * BIN];
+    uint32_t color[MS][BIN * BIN * color_words(CF)];
     float plane[PLANES][BATCH];
-    uint32_t span[BATCH][BIN];          // left | right << 16 per bin row
+    uint32_t span[BATCH][MS][BIN];      // left | right << 16 per sample and bin row
     int16_t qx0[BATCH][BIN / 2];        // first quad x per quad row of the triangle
     uint16_t qpre[BATCH][BIN / 2 + 1];  // prefix of quads per quad row
     int8_t qr0[BATCH];                  // first quad row of the triangle in the bin
     int8_t nqr[BATCH];                  // quad rows of the triangle in the bin
     int triList[2 * BATCH];
+    static constexpr int kSamples = MS;
 };
 
 __device__ __forceinline__ uint32_t select3(int o, uint32_t a, uint32_t b, uint32_t c) { return o == 0 ? a : (o == 1 ? b : c); }
@@ -971,13 +1016,22 @@ __device__ int setup_batch_triangle(const DrawParams &D, SH &S, int ti, uint32_t
     const int n = inf.info & 31, dW = (inf.info >> 5) & 1;
     const int rowLo = max((int)box.y, by0), rowHi = min((int)box.w, by0 + BIN);  // bin rows of the triangle
     const int qrA = (rowLo - by0) >> 1, qrB = (rowHi - 1 - by0) >> 1;            // quad rows [qrA, qrB]
+    constexpr int MS = SH::kSamples;
     // rows outside [rowLo, rowHi) but inside the quad rows are empty
-    S.span[ti][2 * qrA] = 0u;
-    S.span[ti][2 * qrB + 1] = 0u;
+#pragma unroll
+    for(int q = 0; q < MS; q++)
+    {
+        S.span[ti][q][2 * qrA] = 0u;
+        S.span[ti][q][2 * qrB + 1] = 0u;
+    }
     if(inf.info & 128)
     {
-        const uint32_t *sp = D.spans + inf.spanOff + (rowLo - box.y);
-        for(int y = rowLo; y < rowHi; y++) S.span[ti][y - by0] = __ldg(sp + (y - rowLo));
+#pragma unroll
+        for(int q = 0; q < MS; q++)
+        {
+            const uint32_t *sp = D.spans + inf.spanOff + (size_t)q * inf.rows + (rowLo - box.y);
+            for(int y = rowLo; y < rowHi; y++) S.span[ti][q][y - by0] = __ldg(sp + (y - rowLo));
+        }
     }
     else
     {
@@ -1000,48 +1054,58 @@ __device__ int setup_batch_triangle(const DrawParams &D, SH &S, int ti, uint32_t
             X[0] = __float_as_int(a.x); X[1] = __float_as_int(b.x); X[2] = __float_as_int(c.x);
             Y[0] = __float_as_int(a.y); Y[1] = __float_as_int(b.y); Y[2] = __float_as_int(c.y);
         }
-        for(int y = rowLo; y < rowHi; y++) S.span[ti][y - by0] = 0u;
-        for(int i = 0; i < n; i++)
+        for(int q = 0; q < MS; q++)
         {
-            int ia = i + 1 - dW, ib = i + dW;
-            ia = ia == n ? 0 : ia;
-            ib = ib == n ? 0 : ib;
-            EdgeDDA e;
-            if(!edge_setup(D, X[ia], Y[ia], X[ib], Y[ib], e)) continue;
-            int ys = max(e.yMin, rowLo), ye = min(e.yMax, rowHi);
-            if(ys >= ye) continue;
-            int32_t dd;
-            int32_t x = edge_x_at(e, ys, &dd);
-            uint16_t *h = reinterpret_cast<uint16_t *>(&S.span[ti][0]) + (e.right ? 1 : 0);
-            for(int y = ys; y < ye; y++)
+            for(int y = rowLo; y < rowHi; y++) S.span[ti][q][y - by0] = 0u;
+            const int32_t dx = MS > 1 ? XF[q] : 0, dy = MS > 1 ? YF[q] : 0;
+            for(int i = 0; i < n; i++)
             {
-                h[2 * (y - by0)] = (uint16_t)clamp_x(D, x);
-                x += e.Q;
-                dd += e.R;
-                int32_t of = (-dd) >> 31;
-                dd -= e.D & of;
-                x -= of;
+                int ia = i + 1 - dW, ib = i + dW;
+                ia = ia == n ? 0 : ia;
+                ib = ib == n ? 0 : ib;
+                EdgeDDA e;
+                if(!edge_setup(D, X[ia] - dx, Y[ia] - dy, X[ib] - dx, Y[ib] - dy, e)) continue;
+                int ys = max(e.yMin, rowLo), ye = min(e.yMax, rowHi);
+                if(ys >= ye) continue;
+                int32_t dd;
+                int32_t x = edge_x_at(e, ys, &dd);
+                uint16_t *h = reinterpret_cast<uint16_t *>(&S.span[ti][q][0]) + (e.right ? 1 : 0);
+                for(int y = ys; y < ye; y++)
+                {
+                    h[2 * (y - by0)] = (uint16_t)clamp_x(D, x);
+                    x += e.Q;
+                    dd += e.R;
+                    int32_t of = (-dd) >> 31;
+                    dd -= e.D & of;
+                    x -= of;
+                }
             }
         }
     }
-    // quad rows: x range of the row pair (QuadRasterizer.cpp:96-123), clipped to the bin
+    // quad rows: x range of the row pair over all samples (QuadRasterizer.cpp:96-123), clipped to the bin
     int pre = 0;
     for(int qr = qrA; qr <= qrB; qr++)
     {
         const int k = qr - qrA;
         S.qpre[ti][k] = (uint16_t)pre;
-        uint32_t s0 = S.span[ti][2 * qr], s1 = S.span[ti][2 * qr + 1];
-        int l0 = s0 & 0xFFFF, r0 = s0 >> 16, l1 = s1 & 0xFFFF, r1 = s1 >> 16;
-        bool e0 = l0 >= r0, e1 = l1 >= r1;
-        int xa = 0, cnt = 0;
-        if(!(e0 && e1))
+        int xa = 0x7FFF, xb = -1;
+#pragma unroll
+        for(int q = 0; q < MS; q++)
         {
-            xa = e0 ? l1 : (e1 ? l0 : min(l0, l1));
-            int xb = e0 ? r1 : (e1 ? r0 : max(r0, r1));
+            uint32_t s0 = S.span[ti][q][2 * qr], s1 = S.span[ti][q][2 * qr + 1];
+            int l0 = s0 & 0xFFFF, r0 = s0 >> 16, l1 = s1 & 0xFFFF, r1 = s1 >> 16;
+            if(l0 < r0) { xa = min(xa, l0); xb = max(xb, r0); }
+            if(l1 < r1) { xa = min(xa, l1); xb = max(xb, r1); }
+        }
+        int cnt = 0;
+        if(xb >= 0)
+        {
             xa = max(xa & ~1, bx0);
             xb = min(xb, bx0 + BIN);
             cnt = xb > xa ? (xb - xa + 1) >> 1 : 0;
         }
+        else
+            xa = 0;
         S.qx0[ti][k] = (int16_t)xa;
         pre += cnt;
     }
@@ -1195,15 +1259,17 @@ __device__ __forceinline__ void shade_pixel(const DrawParams &D, const SH &S, in
 // Depth test/write, blend and colour write of one pixel of the staged bin
 // (PixelRoutine.cpp:494-574,660-685; alphaBlend :1653-1961; writeColor
 // :1975-1993,2429-2650).
-template<int CF>
-__device__ __forceinline__ void rop_pixel(const DrawParams &D, RasterShared<CF> &S, int idx, float z, const float col[4],
+template<int CF, int MS>
+__device__ __forceinline__ void rop_pixel(const DrawParams &D, RasterShared<CF, MS> &S, int q, int idx, float z, const float col[4],
                                           unsigned long long &nTested, unsigned long long &nPassed)
 {
+    float *depth = S.depth[q];
+    uint32_t *color = S.color[q];
     if(D.depthTest)
     {
         nTested++;
-        if(!depth_pass(D.compareOp, S.depth[idx], z)) return;
-        if(D.depthWrite) S.depth[idx] = z;
+        if(!depth_pass(D.compareOp, depth[idx], z)) return;
+        if(D.depthWrite) depth[idx] = z;
     }
     nPassed++;
     float out[4];
@@ -1213,13 +1279,13 @@ __device__ __forceinline__ void rop_pixel(const DrawParams &D, RasterShared<CF> 
         if(CF == CF_RGBA8)
         {
             // readPixel widens b to b * 257, alphaBlend scales by 1 / 0xFFFF
-            const uint32_t old = S.color[idx];
+            const uint32_t old = color[idx];
 #pragma unroll
             for(int c = 0; c < 4; c++) dst[c] = (float)(((old >> (8 * c)) & 0xFFu) * 257u) * (1.0f / 0xFFFF);
         }
         else if(CF == CF_RGBA16F)
         {
-            const uint32_t w0 = S.color[2 * idx], w1 = S.color[2 * idx + 1];
+            const uint32_t w0 = color[2 * idx], w1 = color[2 * idx + 1];
             dst[0] = reactor_half_to_float(w0 & 0xFFFFu);
             dst[1] = reactor_half_to_float(w0 >> 16);
             dst[2] = reactor_half_to_float(w1 & 0xFFFFu);
@@ -1228,7 +1294,7 @@ __device__ __forceinline__ void rop_pixel(const DrawParams &D, RasterShared<CF> 
         else
         {
 #pragma unroll
-            for(int c = 0; c < 4; c++) dst[c] = __uint_as_float(S.color[4 * idx + c]);
+            for(int c = 0; c < 4; c++) dst[c] = __uint_as_float(color[4 * idx + c]);
         }
         float sf[4], df[4];
 #pragma unroll
@@ -1250,7 +1316,7 @@ __device__ __forceinline__ void rop_pixel(const DrawParams &D, RasterShared<CF> 
     }
     if(CF == CF_RGBA8)
     {
-        uint32_t packed = S.color[idx];
+        uint32_t packed = color[idx];
 #pragma unroll
         for(int c = 0; c < 4; c++)
         {
@@ -1260,11 +1326,11 @@ __device__ __forceinline__ void rop_pixel(const DrawParams &D, RasterShared<CF> 
             uint32_t b = s16 < 0 ? 0u : (s16 > 255 ? 255u : (uint32_t)s16);  // PackUnsigned
             if(D.writeMask & (1u << c)) packed = (packed & ~(0xFFu << (8 * c))) | (b << (8 * c));
         }
-        S.color[idx] = packed;
+        color[idx] = packed;
     }
     else if(CF == CF_RGBA16F)
     {
-        uint32_t w[2] = {S.color[2 * idx], S.color[2 * idx + 1]};
+        uint32_t w[2] = {color[2 * idx], color[2 * idx + 1]};
 #pragma unroll
         for(int c = 0; c < 4; c++)
             if(D.writeMask & (1u << c))
@@ -1272,14 +1338,14 @@ __device__ __forceinline__ void rop_pixel(const DrawParams &D, RasterShared<CF> 
                 const int sh = 16 * (c & 1);
                 w[c >> 1] = (w[c >> 1] & ~(0xFFFFu << sh)) | (reactor_float_to_half(out[c]) << sh);
             }
-        S.color[2 * idx] = w[0];
-        S.color[2 * idx + 1] = w[1];
+        color[2 * idx] = w[0];
+        color[2 * idx + 1] = w[1];
     }
     else
     {
 #pragma unroll
         for(int c = 0; c < 4; c++)
-            if(D.writeMask & (1u << c)) S.color[4 * idx + c] = __float_as_uint(out[c]);
+            if(D.writeMask & (1u << c)) color[4 * idx + c] = __float_as_uint(out[c]);
     }
 }
 
@@ -1298,8 +1364,30 @@ __device__ __forceinline__ int warp_incl_scan(int v, int lane)
 // bin.  Lane j sets up triangle j; then the warp expands quad slots, masks
 // coverage, rejects early on depth, and shades the live pixels one per lane;
 // lanes hitting the same pixel resolve lowest lane (earliest triangle) first.
-template<int CF>
-__device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared<CF> &S, int nb, int bx0, int by0,
+// Depth of sample q (z per sample, QuadRasterizer.cpp:131-141 and
+// PixelRoutine.cpp:128-148) at lane i of the quad at (qx, y), clamped.
+template<int MS, class SH>
+__device__ __forceinline__ float sample_depth(const DrawParams &D, const SH &S, int ti, int qx, int y, int i, int q)
+{
+    float xF = ((float)qx + (float)(i & 1)) - S.plane[0][ti];
+    float yF = ((float)y + (float)(i >> 1)) - S.plane[1][ti];
+    if(MS > 1)
+    {
+        yF = yF + SLY[q];
+        xF = xF - SLX[q];
+    }
+    const float z = mul_add(xF, S.plane[2][ti], S.plane[4][ti] + yF * S.plane[3][ti]);
+    return rmin(rmax(z, D.minDepthClamp), D.maxDepthClamp);  // clampDepth
+}
+
+// One batch of nb <= 32 triangles (primitive order) against the warp's staged
+// bin.  Lane j sets up triangle j; then the warp expands quad slots, masks
+// coverage per sample, rejects early on depth, and shades the live pixels one
+// per lane (once per pixel, at its centre); lanes hitting the same pixel
+// resolve lowest lane (earliest triangle) first, all of the pixel's samples
+// at once.
+template<int CF, int MS>
+__device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared<CF, MS> &S, int nb, int bx0, int by0,
                                           unsigned long long &nQuads, unsigned long long &nTested,
                                           unsigned long long &nPassed, uint32_t &lvMask)
 {
@@ -1308,8 +1396,9 @@ __device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared<CF> 
     if(lane < nb) cnt = setup_batch_triangle(D, S, lane, (uint32_t)S.triList[lane], bx0, by0);
     __syncwarp();
     // Depth only moves one way under LESS/LESS_OR_EQUAL (down) and GREATER/
-    // GREATER_OR_EQUAL (up) with clamped, never-NaN fragment depth, so a lane
-    // that fails against the bin's current depth fails at its ordered turn too.
+    // GREATER_OR_EQUAL (up) with clamped, never-NaN fragment depth, so a
+    // sample that fails against the bin's current depth fails at its ordered
+    // turn too.
     const bool earlyZ = D.depthTest && (D.compareOp == SWGB_COMPARE_LESS || D.compareOp == SWGB_COMPARE_LESS_OR_EQUAL ||
                                         D.compareOp == SWGB_COMPARE_GREATER || D.compareOp == SWGB_COMPARE_GREATER_OR_EQUAL);
     const int incl = warp_incl_scan(cnt, lane);
@@ -1332,7 +1421,7 @@ __device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared<CF> 
         }
         const int sIncl = __shfl_sync(0xFFFFFFFFu, incl, src);
         const int sCnt = __shfl_sync(0xFFFFFFFFu, cnt, src);
-        int cMask = 0, qti = src, qx = 0, qrow = 0;
+        int cMask = 0, qti = src, qx = 0, qrow = 0;  // cMask bit 4q+i: sample q of lane i
         if(slot < total)
         {
             const int local = slot - (sIncl - sCnt);
@@ -1341,33 +1430,43 @@ __device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared<CF> 
             while(k < nq - 1 && (int)S.qpre[qti][k + 1] <= local) k++;
             qrow = S.qr0[qti] + k;
             qx = S.qx0[qti][k] + 2 * (local - (int)S.qpre[qti][k]);
-            const uint32_t sp0 = S.span[qti][2 * qrow], sp1 = S.span[qti][2 * qrow + 1];
-            const int l0 = sp0 & 0xFFFF, r0 = sp0 >> 16, l1 = sp1 & 0xFFFF, r1 = sp1 >> 16;
-            // per-lane coverage: left <= x < right (QuadRasterizer.cpp:184-209)
-            if(qx >= l0 && qx < r0) cMask |= 1;
-            if(qx + 1 >= l0 && qx + 1 < r0) cMask |= 2;
-            if(qx >= l1 && qx < r1) cMask |= 4;
-            if(qx + 1 >= l1 && qx + 1 < r1) cMask |= 8;
+#pragma unroll
+            for(int q = 0; q < MS; q++)
+            {
+                const uint32_t sp0 = S.span[qti][q][2 * qrow], sp1 = S.span[qti][q][2 * qrow + 1];
+                const int l0 = sp0 & 0xFFFF, r0 = sp0 >> 16, l1 = sp1 & 0xFFFF, r1 = sp1 >> 16;
+                // per-lane coverage: left <= x < right (QuadRasterizer.cpp:184-209)
+                int m = 0;
+                if(qx >= l0 && qx < r0) m |= 1;
+                if(qx + 1 >= l0 && qx + 1 < r0) m |= 2;
+                if(qx >= l1 && qx < r1) m |= 4;
+                if(qx + 1 >= l1 && qx + 1 < r1) m |= 8;
+                cMask |= m << (4 * q);
+            }
             if(cMask)
             {
                 nQuads++;
                 if(earlyZ)
                 {
-                    float zq[4];
-                    quad_depth(D, S, qti, qx, by0 + 2 * qrow, zq);
-                    const int lx = qx - bx0, ly = 2 * qrow;
+                    const int lx = qx - bx0, ly = 2 * qrow, y = by0 + 2 * qrow;
                     int keep = 0;
 #pragma unroll
-                    for(int i = 0; i < 4; i++)
-                        if((cMask >> i & 1) && depth_pass(D.compareOp, S.depth[(ly + (i >> 1)) * BIN + lx + (i & 1)], zq[i]))
-                            keep |= 1 << i;
+                    for(int q = 0; q < MS; q++)
+#pragma unroll
+                        for(int i = 0; i < 4; i++)
+                            if((cMask >> (4 * q + i) & 1) &&
+                               depth_pass(D.compareOp, S.depth[q][(ly + (i >> 1)) * BIN + lx + (i & 1)], sample_depth<MS>(D, S, qti, qx, y, i, q)))
+                                keep |= 1 << (4 * q + i);
                     nTested += __popc(cMask & ~keep);
                     cMask = keep;
                 }
             }
         }
-        // ---- live pixels, one per lane --------------------------------------
-        const int np = __popc(cMask);
+        // ---- live pixels (any live sample), one per lane ----------------------
+        int pixMask = 0;
+#pragma unroll
+        for(int q = 0; q < MS; q++) pixMask |= (cMask >> (4 * q)) & 0xF;
+        const int np = __popc(pixMask);
         const int pIncl = warp_incl_scan(np, lane);
         const int pTotal = __shfl_sync(0xFFFFFFFFu, pIncl, 31);
         for(int p0 = 0; p0 < pTotal; p0 += 32)
@@ -1381,39 +1480,31 @@ __device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared<CF> 
                 int v = __shfl_sync(0xFFFFFFFFu, pIncl, mid);
                 if(v > pix) hi = mid; else lo = mid + 1;
             }
-            const int q = lo;
-            const int qIncl = __shfl_sync(0xFFFFFFFFu, pIncl, q);
-            const int qN = __shfl_sync(0xFFFFFFFFu, np, q);
-            const int qMask = __shfl_sync(0xFFFFFFFFu, cMask, q);
-            const int qTi = __shfl_sync(0xFFFFFFFFu, qti, q);
-            const int qX = __shfl_sync(0xFFFFFFFFu, qx, q);
-            const int qRow = __shfl_sync(0xFFFFFFFFu, qrow, q);
+            const int qq = lo;
+            const int qIncl = __shfl_sync(0xFFFFFFFFu, pIncl, qq);
+            const int qN = __shfl_sync(0xFFFFFFFFu, np, qq);
+            const int qPix = __shfl_sync(0xFFFFFFFFu, pixMask, qq);
+            const int qMask = __shfl_sync(0xFFFFFFFFu, cMask, qq);
+            const int qTi = __shfl_sync(0xFFFFFFFFu, qti, qq);
+            const int qX = __shfl_sync(0xFFFFFFFFu, qx, qq);
+            const int qRow = __shfl_sync(0xFFFFFFFFu, qrow, qq);
             const bool valid = pix < pTotal;
-            int pidx = -1 - lane;
-            float z = 0.0f, col[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            int pidx = -1 - lane, i = 0;
+            float col[4] = {0.0f, 0.0f, 0.0f, 0.0f};
             if(valid)
             {
-                int nth = pix - (qIncl - qN);  // the nth set bit of the quad's mask
-                int i = 0;
+                int nth = pix - (qIncl - qN);  // the nth set bit of the quad's pixel mask
 #pragma unroll
                 for(int b = 0; b < 4; b++)
                 {
-                    if(qMask >> b & 1)
+                    if(qPix >> b & 1)
                     {
                         if(nth == 0) i = b;
                         nth--;
                     }
                 }
-                const int y = by0 + 2 * qRow;
                 pidx = (2 * qRow + (i >> 1)) * BIN + (qX - bx0) + (i & 1);
-                if(D.depthTest)
-                {
-                    const float xF = ((float)qX + (float)(i & 1)) - S.plane[0][qTi];
-                    const float yF = ((float)y + (float)(i >> 1)) - S.plane[1][qTi];
-                    z = mul_add(xF, S.plane[2][qTi], S.plane[4][qTi] + yF * S.plane[3][qTi]);
-                    z = rmin(rmax(z, D.minDepthClamp), D.maxDepthClamp);  // clampDepth
-                }
-                shade_pixel<CF>(D, S, qTi, qX, y, i, col, lvMask);
+                shade_pixel<CF>(D, S, qTi, qX, by0 + 2 * qRow, i, col, lvMask);
             }
             // ordered resolve: among lanes on the same pixel, lowest lane first
             unsigned pend = __ballot_sync(0xFFFFFFFFu, valid);
@@ -1423,7 +1514,13 @@ __device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared<CF> 
                 const unsigned peers = __match_any_sync(0xFFFFFFFFu, mine ? pidx : -1 - lane);
                 if(mine && (__ffs(peers) - 1) == lane)
                 {
-                    rop_pixel<CF>(D, S, pidx, z, col, nTested, nPassed);
+#pragma unroll
+                    for(int q = 0; q < MS; q++)
+                        if(qMask >> (4 * q + i) & 1)
+                        {
+                            const float z = D.depthTest ? sample_depth<MS>(D, S, qTi, qX, by0 + 2 * qRow, i, q) : 0.0f;
+                            rop_pixel<CF, MS>(D, S, q, pidx, z, col, nTested, nPassed);
+                        }
                     pend &= ~(1u << lane);
                 }
                 __syncwarp();
@@ -1444,13 +1541,13 @@ __device__ __forceinline__ bool box_hits(int4 b, int bx0, int by0)
     return b.x < b.z && b.x < bx0 + BIN && b.z > bx0 && b.y < by0 + BIN && b.w > by0;
 }
 
-template<int CF>
+template<int CF, int MS>
 __global__ void __launch_bounds__(RASTER_THREADS) k_raster(const __grid_constant__ DrawParams D)
 {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     constexpr int CW = color_words(CF);
-    RasterShared<CF> &S = reinterpret_cast<RasterShared<CF> *>(smem_raw)[warp];
+    RasterShared<CF, MS> &S = reinterpret_cast<RasterShared<CF, MS> *>(smem_raw)[warp];
     const int nbins = D.binsX * D.binsY;
     unsigned long long nQuads = 0, nTested = 0, nPassed = 0;
     uint32_t lvMask = 0;
@@ -1465,45 +1562,50 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_raster(const __grid_constant
     const int bx0 = D.binX0 + (bin % D.binsX) * BIN;
     const int by0 = D.binY0 + (bin / D.binsX) * BIN;
 
-    // ---- stage the bin's depth and colour (16-byte row segments) ---------------
-    for(int i = lane; i < BIN * BIN / 4; i += 32)
+    // ---- stage the bin's depth and colour, every sample plane (16-byte segments) ----
+    for(int q = 0; q < MS; q++)
     {
-        const int ly = i / (BIN / 4), lx = (i % (BIN / 4)) * 4;
-        const int px = bx0 + lx, py = by0 + ly;
-        float4 dz = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
-        if(D.depthTest && py < D.sy1 && px < D.sx1)
+        const uint8_t *dbase = D.depth + (size_t)q * D.depthSlice;
+        const uint8_t *cbase = D.color + (size_t)q * D.colorSlice;
+        for(int i = lane; i < BIN * BIN / 4; i += 32)
         {
-            const uint8_t *drow = D.depth + (size_t)py * D.depthPitch;
-            if(D.vec16 && px + 4 <= D.sx1)
-                dz = *(const float4 *)(drow + (size_t)px * 4);
-            else
+            const int ly = i / (BIN / 4), lx = (i % (BIN / 4)) * 4;
+            const int px = bx0 + lx, py = by0 + ly;
+            float4 dz = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+            if(D.depthTest && py < D.sy1 && px < D.sx1)
             {
-                float dv[4] = {1.0f, 1.0f, 1.0f, 1.0f};
-                for(int k = 0; k < 4 && px + k < D.sx1; k++) dv[k] = *(const float *)(drow + (size_t)(px + k) * 4);
-                dz = make_float4(dv[0], dv[1], dv[2], dv[3]);
+                const uint8_t *drow = dbase + (size_t)py * D.depthPitch;
+                if(D.vec16 && px + 4 <= D.sx1)
+                    dz = *(const float4 *)(drow + (size_t)px * 4);
+                else
+                {
+                    float dv[4] = {1.0f, 1.0f, 1.0f, 1.0f};
+                    for(int k = 0; k < 4 && px + k < D.sx1; k++) dv[k] = *(const float *)(drow + (size_t)(px + k) * 4);
+                    dz = make_float4(dv[0], dv[1], dv[2], dv[3]);
+                }
             }
+            *(float4 *)&S.depth[q][ly * BIN + lx] = dz;
         }
-        *(float4 *)&S.depth[ly * BIN + lx] = dz;
-    }
-    for(int i = lane; i < BIN * BIN * CW / 4; i += 32)
-    {
-        // 16-byte segment i of the bin's colour rows: 4 / CW pixels
-        const int ly = i / (BIN * CW / 4), lx = (i % (BIN * CW / 4)) * 4 / CW;
-        const int px = bx0 + lx, py = by0 + ly;
-        uint4 cc = make_uint4(0, 0, 0, 0);
-        if(py < D.sy1 && px < D.sx1)
+        for(int i = lane; i < BIN * BIN * CW / 4; i += 32)
         {
-            const uint8_t *crow = D.color + (size_t)py * D.colorPitch + (size_t)px * 4 * CW;
-            if(D.vec16 && px + 4 / CW <= D.sx1)
-                cc = *(const uint4 *)crow;
-            else
+            // 16-byte segment i of the bin's colour rows: 4 / CW pixels
+            const int ly = i / (BIN * CW / 4), lx = (i % (BIN * CW / 4)) * 4 / CW;
+            const int px = bx0 + lx, py = by0 + ly;
+            uint4 cc = make_uint4(0, 0, 0, 0);
+            if(py < D.sy1 && px < D.sx1)
             {
-                uint32_t cv[4] = {0, 0, 0, 0};
-                for(int k = 0; k < 4 && px + k / CW < D.sx1; k++) cv[k] = *(const uint32_t *)(crow + 4 * k);
-                cc = make_uint4(cv[0], cv[1], cv[2], cv[3]);
+                const uint8_t *crow = cbase + (size_t)py * D.colorPitch + (size_t)px * 4 * CW;
+                if(D.vec16 && px + 4 / CW <= D.sx1)
+                    cc = *(const uint4 *)crow;
+                else
+                {
+                    uint32_t cv[4] = {0, 0, 0, 0};
+                    for(int k = 0; k < 4 && px + k / CW < D.sx1; k++) cv[k] = *(const uint32_t *)(crow + 4 * k);
+                    cc = make_uint4(cv[0], cv[1], cv[2], cv[3]);
+                }
             }
+            *(uint4 *)&S.color[q][(ly * BIN + lx) * CW] = cc;
         }
-        *(uint4 *)&S.color[(ly * BIN + lx) * CW] = cc;
     }
     __syncwarp();
 
@@ -1533,7 +1635,7 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_raster(const __grid_constant
                     __syncwarp();
                     if(listCount >= BATCH)
                     {
-                        raster_batch(D, S, BATCH, bx0, by0, nQuads, nTested, nPassed, lvMask);
+                        raster_batch<CF, MS>(D, S, BATCH, bx0, by0, nQuads, nTested, nPassed, lvMask);
                         const int rem = listCount - BATCH;
                         const int v = lane < rem ? S.triList[BATCH + lane] : 0;
                         __syncwarp();
@@ -1545,33 +1647,38 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_raster(const __grid_constant
             }
         }
     }
-    if(listCount > 0) raster_batch(D, S, listCount, bx0, by0, nQuads, nTested, nPassed, lvMask);
+    if(listCount > 0) raster_batch<CF, MS>(D, S, listCount, bx0, by0, nQuads, nTested, nPassed, lvMask);
 
-    // ---- write the bin back ----------------------------------------------------
-    for(int i = lane; i < BIN * BIN / 4; i += 32)
+    // ---- write the bin back, every sample plane ----------------------------------
+    for(int q = 0; q < MS; q++)
     {
-        if(!D.depthWrite) break;
-        const int ly = i / (BIN / 4), lx = (i % (BIN / 4)) * 4;
-        const int px = bx0 + lx, py = by0 + ly;
-        if(py >= D.sy1 || px >= D.sx1 || py < D.sy0) continue;
-        uint8_t *drow = D.depth + (size_t)py * D.depthPitch;
-        if(D.vec16 && px + 4 <= D.sx1 && px >= D.sx0)
-            *(float4 *)(drow + (size_t)px * 4) = *(const float4 *)&S.depth[ly * BIN + lx];
-        else
-            for(int k = 0; k < 4 && px + k < D.sx1; k++)
-                if(px + k >= D.sx0) *(float *)(drow + (size_t)(px + k) * 4) = S.depth[ly * BIN + lx + k];
-    }
-    for(int i = lane; i < BIN * BIN * CW / 4; i += 32)
-    {
-        const int ly = i / (BIN * CW / 4), lx = (i % (BIN * CW / 4)) * 4 / CW;
-        const int px = bx0 + lx, py = by0 + ly;
-        if(py >= D.sy1 || px >= D.sx1 || py < D.sy0) continue;
-        uint8_t *crow = D.color + (size_t)py * D.colorPitch + (size_t)px * 4 * CW;
-        if(D.vec16 && px + 4 / CW <= D.sx1 && px >= D.sx0)
-            *(uint4 *)crow = *(const uint4 *)&S.color[(ly * BIN + lx) * CW];
-        else
-            for(int k = 0; k < 4 && px + k / CW < D.sx1; k++)
-                if(px + k / CW >= D.sx0) *(uint32_t *)(crow + 4 * k) = S.color[(ly * BIN + lx) * CW + k];
+        uint8_t *dbase = D.depth + (size_t)q * D.depthSlice;
+        uint8_t *cbase = D.color + (size_t)q * D.colorSlice;
+        for(int i = lane; i < BIN * BIN / 4; i += 32)
+        {
+            if(!D.depthWrite) break;
+            const int ly = i / (BIN / 4), lx = (i % (BIN / 4)) * 4;
+            const int px = bx0 + lx, py = by0 + ly;
+            if(py >= D.sy1 || px >= D.sx1 || py < D.sy0) continue;
+            uint8_t *drow = dbase + (size_t)py * D.depthPitch;
+            if(D.vec16 && px + 4 <= D.sx1 && px >= D.sx0)
+                *(float4 *)(drow + (size_t)px * 4) = *(const float4 *)&S.depth[q][ly * BIN + lx];
+            else
+                for(int k = 0; k < 4 && px + k < D.sx1; k++)
+                    if(px + k >= D.sx0) *(float *)(drow + (size_t)(px + k) * 4) = S.depth[q][ly * BIN + lx + k];
+        }
+        for(int i = lane; i < BIN * BIN * CW / 4; i += 32)
+        {
+            const int ly = i / (BIN * CW / 4), lx = (i % (BIN * CW / 4)) * 4 / CW;
+            const int px = bx0 + lx, py = by0 + ly;
+            if(py >= D.sy1 || px >= D.sx1 || py < D.sy0) continue;
+            uint8_t *crow = cbase + (size_t)py * D.colorPitch + (size_t)px * 4 * CW;
+            if(D.vec16 && px + 4 / CW <= D.sx1 && px >= D.sx0)
+                *(uint4 *)crow = *(const uint4 *)&S.color[q][(ly * BIN + lx) * CW];
+            else
+                for(int k = 0; k < 4 && px + k / CW < D.sx1; k++)
+                    if(px + k / CW >= D.sx0) *(uint32_t *)(crow + 4 * k) = S.color[q][(ly * BIN + lx) * CW + k];
+        }
     }
     __syncwarp();
     }
@@ -1622,7 +1729,7 @@ struct swgb_ctx {
     size_t polyCap;
     uint32_t *polyCount;
     unsigned int *binQueue;
-    int rasterBlocks[3];  // persistent raster grid per colour format: SMs x resident blocks per SM
+    int rasterBlocks[6];  // persistent raster grid per kernel variant: SMs x resident blocks per SM
     unsigned long long *counters;
     int *error;
     uint64_t launches;
@@ -1699,7 +1806,7 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
     memset(&D, 0, sizeof(D));
     if(st->precision_profile != SWGB_PRECISION_CMAKE) return set_error(SWGB_UNSUPPORTED_STATE, "only the CMake precision profile is implemented");
     if(st->topology != SWGB_TOPOLOGY_TRIANGLE_LIST) return set_error(SWGB_UNSUPPORTED_STATE, "topology");
-    if(st->sample_count != 1) return set_error(SWGB_UNSUPPORTED_STATE, "sample_count");
+    if(st->sample_count != 1 && st->sample_count != 4) return set_error(SWGB_UNSUPPORTED_STATE, "sample_count (1 or 4)");
     if(st->vertex_shader != SWGB_VS_MVP_PASSTHROUGH) return set_error(SWGB_UNSUPPORTED_STATE, "vertex_shader");
     if(st->fragment_shader != SWGB_FS_VCOLOR && st->fragment_shader != SWGB_FS_TEX_X_VCOLOR) return set_error(SWGB_UNSUPPORTED_STATE, "fragment_shader");
     if(st->depth_clamp_enable || st->depth_bias_constant != 0.0f || st->depth_bias_slope != 0.0f) return set_error(SWGB_UNSUPPORTED_STATE, "depth clamp / bias");
@@ -1777,6 +1884,9 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
     D.srcC = st->src_color_factor; D.dstC = st->dst_color_factor; D.opC = opC;
     D.srcA = st->src_alpha_factor; D.dstA = st->dst_alpha_factor; D.opA = opA;
     D.writeMask = st->color_write_mask & 0xFu;
+    D.ms = (int)st->sample_count;
+    D.colorSlice = st->color_slice_bytes;
+    D.depthSlice = st->depth_slice_bytes;
     D.cf = st->color_format == SWGB_FORMAT_R8G8B8A8_UNORM ? CF_RGBA8 : (st->color_format == SWGB_FORMAT_R16G16B16A16_SFLOAT ? CF_RGBA16F : CF_RGBA32F);
     D.color = (uint8_t *)st->color;
     D.colorPitch = st->color_pitch_bytes;
@@ -1829,31 +1939,52 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
     return SWGB_OK;
 }
 
-template<int CF>
-constexpr size_t raster_smem() { return RASTER_WARPS * sizeof(RasterShared<CF>); }
+template<int CF, int MS>
+constexpr size_t raster_smem() { return RASTER_WARPS * sizeof(RasterShared<CF, MS>); }
 
-// Persistent raster grid of the colour format's kernel: SMs x resident blocks.
-template<int CF>
+// Persistent raster grid of one kernel instantiation: SMs x resident blocks.
+template<int CF, int MS>
 swgb_status raster_grid(int device, bool setAttr, int &blocks)
 {
     swgb_status s;
-    if(setAttr && (s = cuda_check(cudaFuncSetAttribute(k_raster<CF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)raster_smem<CF>()),
+    if(setAttr && (s = cuda_check(cudaFuncSetAttribute(k_raster<CF, MS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)raster_smem<CF, MS>()),
                                   "raster smem attribute")) != SWGB_OK)
         return s;
     int sms = 0, perSM = 0;
     if((s = cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "SM count")) != SWGB_OK) return s;
-    if((s = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_raster<CF>, RASTER_THREADS, raster_smem<CF>()),
+    if((s = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_raster<CF, MS>, RASTER_THREADS, raster_smem<CF, MS>()),
                        "raster occupancy")) != SWGB_OK)
         return s;
     blocks = (sms > 0 ? sms : 1) * (perSM > 0 ? perSM : 1);
     return SWGB_OK;
 }
 
+// Raster kernel index: colour format x (1 or 4 samples).
+inline int raster_variant(const DrawParams &D) { return D.cf + (D.ms > 1 ? 3 : 0); }
+
+swgb_status raster_grids(int device, bool setAttr, int blocks[6])
+{
+    swgb_status s;
+    if((s = raster_grid<CF_RGBA8, 1>(device, setAttr, blocks[0])) != SWGB_OK) return s;
+    if((s = raster_grid<CF_RGBA16F, 1>(device, setAttr, blocks[1])) != SWGB_OK) return s;
+    if((s = raster_grid<CF_RGBA32F, 1>(device, setAttr, blocks[2])) != SWGB_OK) return s;
+    if(!setAttr) return SWGB_OK;  // the allocation-free path runs single-sample draws only
+    if((s = raster_grid<CF_RGBA8, 4>(device, setAttr, blocks[3])) != SWGB_OK) return s;
+    if((s = raster_grid<CF_RGBA16F, 4>(device, setAttr, blocks[4])) != SWGB_OK) return s;
+    return raster_grid<CF_RGBA32F, 4>(device, setAttr, blocks[5]);
+}
+
 void launch_raster(const DrawParams &D, uint32_t blocks, cudaStream_t st)
 {
-    if(D.cf == CF_RGBA8) k_raster<CF_RGBA8><<<blocks, RASTER_THREADS, raster_smem<CF_RGBA8>(), st>>>(D);
-    else if(D.cf == CF_RGBA16F) k_raster<CF_RGBA16F><<<blocks, RASTER_THREADS, raster_smem<CF_RGBA16F>(), st>>>(D);
-    else k_raster<CF_RGBA32F><<<blocks, RASTER_THREADS, raster_smem<CF_RGBA32F>(), st>>>(D);
+    switch(raster_variant(D))
+    {
+    case 0: k_raster<CF_RGBA8, 1><<<blocks, RASTER_THREADS, raster_smem<CF_RGBA8, 1>(), st>>>(D); break;
+    case 1: k_raster<CF_RGBA16F, 1><<<blocks, RASTER_THREADS, raster_smem<CF_RGBA16F, 1>(), st>>>(D); break;
+    case 2: k_raster<CF_RGBA32F, 1><<<blocks, RASTER_THREADS, raster_smem<CF_RGBA32F, 1>(), st>>>(D); break;
+    case 3: k_raster<CF_RGBA8, 4><<<blocks, RASTER_THREADS, raster_smem<CF_RGBA8, 4>(), st>>>(D); break;
+    case 4: k_raster<CF_RGBA16F, 4><<<blocks, RASTER_THREADS, raster_smem<CF_RGBA16F, 4>(), st>>>(D); break;
+    default: k_raster<CF_RGBA32F, 4><<<blocks, RASTER_THREADS, raster_smem<CF_RGBA32F, 4>(), st>>>(D); break;
+    }
 }
 
 cudaEvent_t take_event(swgb_ctx *ctx)
@@ -1922,9 +2053,7 @@ swgb_status enqueue(swgb_ctx *ctx, DrawParams &D)
     D.error = ctx->error;
     if(!ctx->rasterAttr)
     {
-        if((s = raster_grid<CF_RGBA8>(ctx->device, true, ctx->rasterBlocks[CF_RGBA8])) != SWGB_OK) return s;
-        if((s = raster_grid<CF_RGBA16F>(ctx->device, true, ctx->rasterBlocks[CF_RGBA16F])) != SWGB_OK) return s;
-        if((s = raster_grid<CF_RGBA32F>(ctx->device, true, ctx->rasterBlocks[CF_RGBA32F])) != SWGB_OK) return s;
+        if((s = raster_grids(ctx->device, true, ctx->rasterBlocks)) != SWGB_OK) return s;
         ctx->rasterAttr = true;
     }
     const uint32_t nv = D.vertexCount;
@@ -1934,7 +2063,7 @@ swgb_status enqueue(swgb_ctx *ctx, DrawParams &D)
     if(D.binsX > 0 && D.binsY > 0)
     {
         uint32_t blocks = (uint32_t)((D.binsX * D.binsY + RASTER_WARPS - 1) / RASTER_WARPS);
-        if(blocks > (uint32_t)ctx->rasterBlocks[D.cf]) blocks = (uint32_t)ctx->rasterBlocks[D.cf];
+        if(blocks > (uint32_t)ctx->rasterBlocks[raster_variant(D)]) blocks = (uint32_t)ctx->rasterBlocks[raster_variant(D)];
         timed_launch(ctx, SWGB_KERNEL_RASTER, [&] { launch_raster(D, blocks, ctx->stream); });
     }
     return cuda_check(cudaGetLastError(), "kernel launch");
@@ -1972,7 +2101,7 @@ constexpr size_t NA_OFF_WORDS = na_up(NA_OFF_POLY + (size_t)NA_TRIS * MAX_POLY *
 // words: counters[8] (u64), spanCount (u64), polyCount (u32), binQueue (u32), error (i32)
 constexpr size_t NA_WORDS_BYTES = 8 * 8 + 8 + 4 + 4 + 4;
 constexpr size_t NA_BYTES = na_up(NA_OFF_WORDS + NA_WORDS_BYTES);
-static_assert(raster_smem<CF_RGBA32F>() <= 48 * 1024 && raster_smem<CF_RGBA16F>() <= 48 * 1024 && raster_smem<CF_RGBA8>() <= 48 * 1024,
+static_assert(raster_smem<CF_RGBA32F, 1>() <= 48 * 1024 && raster_smem<CF_RGBA16F, 1>() <= 48 * 1024 && raster_smem<CF_RGBA8, 1>() <= 48 * 1024,
               "the allocation-free raster launch uses the default shared-memory limit");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
@@ -1980,7 +2109,7 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
 struct NoAllocDevice {
     bool ready;
     unsigned char *base;  // device address of g_noalloc_scratch on this device
-    int rasterBlocks[3];
+    int rasterBlocks[6];
 };
 static NoAllocDevice g_noalloc_dev[64];
 static std::mutex g_noalloc_mu;
@@ -1998,9 +2127,7 @@ swgb_status noalloc_device(int dev, NoAllocDevice *&out)
         void *ptr = nullptr;
         swgb_status s = cuda_check(cudaGetSymbolAddress(&ptr, g_noalloc_scratch), "cudaGetSymbolAddress(scratch)");
         if(s != SWGB_OK) return s;
-        if((s = raster_grid<CF_RGBA8>(dev, false, d.rasterBlocks[CF_RGBA8])) != SWGB_OK) return s;
-        if((s = raster_grid<CF_RGBA16F>(dev, false, d.rasterBlocks[CF_RGBA16F])) != SWGB_OK) return s;
-        if((s = raster_grid<CF_RGBA32F>(dev, false, d.rasterBlocks[CF_RGBA32F])) != SWGB_OK) return s;
+        if((s = raster_grids(dev, false, d.rasterBlocks)) != SWGB_OK) return s;
         d.base = (unsigned char *)ptr;
         d.ready = true;
     }
@@ -2120,6 +2247,7 @@ swgb_status swgb_draw_noalloc(const swgb_pipeline_state *st, const swgb_draw_arg
     DrawParams D;
     swgb_status s = bake(st, args, D);
     if(s != SWGB_OK) return s;
+    if(D.ms > 1) return set_error(SWGB_UNSUPPORTED_STATE, "swgb_draw_noalloc: multisampled attachments need swgb_draw");
     if(D.vertexCount > SWGB_NOALLOC_MAX_VERTICES)
         return set_error(SWGB_INVALID_ARG, "swgb_draw_noalloc: vertex_count above SWGB_NOALLOC_MAX_VERTICES (98304)");
     int dev = 0;
@@ -2153,7 +2281,7 @@ swgb_status swgb_draw_noalloc(const swgb_pipeline_state *st, const swgb_draw_arg
     if(D.binsX > 0 && D.binsY > 0)
     {
         uint32_t blocks = (uint32_t)((D.binsX * D.binsY + RASTER_WARPS - 1) / RASTER_WARPS);
-        if(blocks > (uint32_t)nd->rasterBlocks[D.cf]) blocks = (uint32_t)nd->rasterBlocks[D.cf];
+        if(blocks > (uint32_t)nd->rasterBlocks[D.cf]) blocks = (uint32_t)nd->rasterBlocks[D.cf];  // single-sample variants
         launch_raster(D, blocks, st0);
     }
     return cuda_check(cudaGetLastError(), "kernel launch");

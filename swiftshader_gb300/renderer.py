@@ -96,11 +96,11 @@ class DeviceScene:
         self.indices = None if scene.indices is None else torch.from_numpy(
             np.ascontiguousarray(scene.indices).view(np.int32)).to(self.device)
         self.levels = [torch.from_numpy(np.ascontiguousarray(l)).to(self.device) for l in scene.texture_levels]
-        h, w = scene.height, scene.width
         cdtype = {abi.FORMAT_R8G8B8A8_UNORM: torch.uint8, abi.FORMAT_R32G32B32A32_SFLOAT: torch.float32,
                   abi.FORMAT_R16G16B16A16_SFLOAT: torch.float16}[scene.color_format]
-        self.color = torch.empty((h, w, 4), dtype=cdtype, device=self.device)
-        self.depth = torch.empty((h, w), dtype=torch.float32, device=self.device)
+        cshape, dshape = scenes.attachment_shapes(scene)
+        self.color = torch.empty(cshape, dtype=cdtype, device=self.device)
+        self.depth = torch.empty(dshape, dtype=torch.float32, device=self.device)
         self.clear()
 
     def clear(self):

@@ -42,6 +42,7 @@ class Scene:
     color_format: int = abi.FORMAT_R8G8B8A8_UNORM
     viewport: tuple = None            # (x, y, w, h) default full framebuffer
     scissor: tuple = None             # (x, y, w, h)
+    samples: int = 1                  # 1 or 4 (4x MSAA: one plane per sample)
 
     @property
     def vertex_count(self):
@@ -315,7 +316,7 @@ def build_state(scene, color_ptr, depth_ptr, vertex_ptr, level_ptrs=None, color_
         (st.src_color_factor, st.dst_color_factor, st.color_blend_op,
          st.src_alpha_factor, st.dst_alpha_factor, st.alpha_blend_op) = scene.blend
     st.color_write_mask = 0xF
-    st.sample_count = 1
+    st.sample_count = scene.samples
     bpp = {abi.FORMAT_R8G8B8A8_UNORM: 4, abi.FORMAT_R16G16B16A16_SFLOAT: 8,
            abi.FORMAT_R32G32B32A32_SFLOAT: 16}[scene.color_format]
     st.color = color_ptr
@@ -354,14 +355,22 @@ def build_args(scene, index_ptr=None):
     return a
 
 
+def attachment_shapes(scene):
+    """Colour and depth array shapes: (h, w, 4) / (h, w), or with 4x MSAA one
+    plane per sample in front, (4, h, w, 4) / (4, h, w)."""
+    lead = (scene.samples,) if scene.samples > 1 else ()
+    return lead + (scene.height, scene.width, 4), lead + (scene.height, scene.width)
+
+
+def color_dtype(scene):
+    return {abi.FORMAT_R8G8B8A8_UNORM: np.uint8, abi.FORMAT_R32G32B32A32_SFLOAT: np.float32,
+            abi.FORMAT_R16G16B16A16_SFLOAT: np.float16}[scene.color_format]
+
+
 def clear_buffers(scene):
     """Host colour (uint8/float) and depth (float32) attachments, cleared."""
-    if scene.color_format == abi.FORMAT_R8G8B8A8_UNORM:
-        color = np.empty((scene.height, scene.width, 4), np.uint8)
-    elif scene.color_format == abi.FORMAT_R32G32B32A32_SFLOAT:
-        color = np.empty((scene.height, scene.width, 4), np.float32)
-    else:
-        color = np.empty((scene.height, scene.width, 4), np.float16)
+    cs, ds = attachment_shapes(scene)
+    color = np.empty(cs, color_dtype(scene))
     color[...] = np.asarray(scene.clear_color, color.dtype)
-    depth = np.full((scene.height, scene.width), scene.clear_depth, np.float32)
+    depth = np.full(ds, scene.clear_depth, np.float32)
     return color, depth

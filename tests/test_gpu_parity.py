@@ -202,3 +202,42 @@ def test_sphere_views_rgba16f_reduced(gpu_lib):
     for view in (0, 7, 200):
         s = scenes.scene_sphere_views(view, width=96, height=96, mesh=mesh, levels=levels)
         check_scene(s, gpu_lib)
+
+
+@pytest.mark.parametrize("color_fmt,blend,textured", [
+    (abi.FORMAT_R8G8B8A8_UNORM, False, False),
+    (abi.FORMAT_R8G8B8A8_UNORM, True, True),
+    (abi.FORMAT_R16G16B16A16_SFLOAT, True, True),
+    (abi.FORMAT_R32G32B32A32_SFLOAT, False, True),
+])
+def test_msaa4(gpu_lib, color_fmt, blend, textured):
+    """4x MSAA: per-sample spans, coverage, depth and colour planes; shading
+    once per pixel at its centre."""
+    if textured:
+        s = _float_variant(abi.FORMAT_R16G16B16A16_SFLOAT, color_fmt, blend, abi.ADDRESS_REPEAT, True, seed=41)
+    else:
+        s = scenes.scene_small(n_tris=300, width=72, height=56, seed_index=42)
+    s.samples = 4
+    cnt = check_scene(s, gpu_lib)
+    assert cnt["fragments_tested"] > 0
+
+
+def test_msaa4_clipped_and_scissored(gpu_lib):
+    s = scenes.scene_small(n_tris=300, width=96, height=80, seed_index=43)
+    rng = np.random.Generator(np.random.PCG64(43))
+    v = s.vertices
+    v[:, 0:2] = rng.uniform(-2.0, 2.0, (v.shape[0], 2))
+    v[:, 3] = rng.uniform(0.3, 1.5, v.shape[0])
+    s.scissor = (5, 7, 81, 60)
+    s.samples = 4
+    check_scene(s, gpu_lib)
+
+
+def test_sphere_views_msaa_reduced(gpu_lib):
+    """The batched-adjoint view at reduced size with its 4x MSAA attachment."""
+    rng = np.random.Generator(np.random.PCG64(4))
+    mesh = scenes.uv_sphere(rng, 60, 40, noise_sigma=0.02)
+    levels = scenes.float_mip_chain(rng.uniform(0.0, 1.0, (128, 128, 4)), np.float16)
+    s = scenes.scene_sphere_views(3, width=96, height=96, mesh=mesh, levels=levels)
+    s.samples = 4
+    check_scene(s, gpu_lib)
