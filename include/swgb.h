@@ -251,8 +251,14 @@ swgb_status swgb_ctx_set_stream(swgb_ctx *ctx, void *stream);
  * returns before its marl tasks finish). */
 swgb_status swgb_draw(swgb_ctx *ctx, const swgb_pipeline_state *state, const swgb_draw_args *args);
 
-/* N independent draws (own state, own attachments) enqueued as one persistent
- * launch fed by a device work queue. */
+/* N draws enqueued as batches: the draws' vertex blocks, triangle blocks and
+ * screen bins form one work space for one persistent launch of each kernel,
+ * replayed from a captured CUDA graph.  The result equals N sequential
+ * swgb_draw calls: draws are split into consecutive segments (one graph replay
+ * each) wherever a draw touches attachment bytes an earlier draw of the
+ * segment touches, or needs another raster variant (colour format or sample
+ * count).  Textures and vertex/index buffers must not alias attachments
+ * written in the same call. */
 swgb_status swgb_draw_batch(swgb_ctx *ctx, const swgb_pipeline_state *states, const swgb_draw_args *args, uint32_t n);
 
 /* Allocation-free draw.  No counterpart in the reference: it exists for
@@ -293,6 +299,7 @@ uint64_t swgb_launch_count(swgb_ctx *ctx);
 #define SWGB_KERNEL_VERTEX 0
 #define SWGB_KERNEL_SETUP 1
 #define SWGB_KERNEL_RASTER 2
+#define SWGB_KERNEL_BATCH 3 /* one graph replay of a batch segment (three kernels) */
 #define SWGB_KERNEL_KINDS 8
 swgb_status swgb_set_kernel_timing(swgb_ctx *ctx, int enable);
 swgb_status swgb_get_kernel_times(swgb_ctx *ctx, double ms[SWGB_KERNEL_KINDS], uint32_t launches[SWGB_KERNEL_KINDS]);

@@ -28,8 +28,11 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
+#include <map>
 #include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/swgb.h"
@@ -170,18 +173,8 @@ __device__ __forceinline__ void read_attrib(const DrawParams &D, int a, uint32_t
 // Post-transform vertex: float4[0] = clip position; float4[1] = (X bits, Y
 // bits, clipFlags bits, projected z); float4[2] = (rhw, v0, v1, v2);
 // float4[3] = (v3, v4, v5, v6).
-__global__ void k_vertex(const __grid_constant__ DrawParams D, uint32_t nverts)
+__device__ __forceinline__ void vertex_body(const DrawParams &D, uint32_t i)
 {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if(i == 0)
-    {
-        *D.polyCount = 0;
-        *D.spanCount = 0;
-        *D.binQueue = 0;
-    }
-    for(uint32_t j = i; j < (uint32_t)D.nsuper; j += gridDim.x * blockDim.x)
-        D.superBox[j] = make_int4(0x7FFFFFFF, 0x7FFFFFFF, (int)0x80000000, (int)0x80000000);
-    if(i >= nverts) return;
     uint32_t index = (D.indexType == SWGB_INDEX_TYPE_NONE ? D.firstVertex + i : i) + (uint32_t)D.baseVertex;
     float p[4];
     read_attrib(D, 0, index, p);
@@ -229,6 +222,20 @@ __global__ void k_vertex(const __grid_constant__ DrawParams D, uint32_t nverts)
     o[1] = make_float4(__int_as_float(X), __int_as_float(Y), __int_as_float(f), z * rhw);
     o[2] = make_float4(rhw, v[0], v[1], v[2]);
     o[3] = make_float4(v[3], v[4], v[5], v[6]);
+}
+
+__global__ void k_vertex(const __grid_constant__ DrawParams D, uint32_t nverts)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i == 0)
+    {
+        *D.polyCount = 0;
+        *D.spanCount = 0;
+        *D.binQueue = 0;
+    }
+    for(uint32_t j = i; j < (uint32_t)D.nsuper; j += gridDim.x * blockDim.x)
+        D.superBox[j] = make_int4(0x7FFFFFFF, 0x7FFFFFFF, (int)0x80000000, (int)0x80000000);
+    if(i < nverts) vertex_body(D, i);
 }
 
 // ------------------------------------------------------------------------
@@ -410,9 +417,10 @@ __device__ void write_spans(const DrawParams &D, const int32_t *X, const int32_t
     }
 }
 
-__global__ void __launch_bounds__(SETUP_THREADS) k_setup(const __grid_constant__ DrawParams D)
+// One 256-triangle block of a draw (block index 'blk' within the draw).
+__device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
 {
-    const uint32_t t = blockIdx.x * SETUP_THREADS + threadIdx.x;
+    const uint32_t t = blk * SETUP_THREADS + threadIdx.x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     short4 box = make_short4(0, 0, 0, 0);
     TriInfo inf = {0u, 0u, 0u, 0u};
@@ -668,10 +676,10 @@ __global__ void __launch_bounds__(SETUP_THREADS) k_setup(const __grid_constant__
             short4 c = sBox[w0 + w];
             b.x = min(b.x, c.x); b.y = min(b.y, c.y); b.z = max(b.z, c.z); b.w = max(b.w, c.w);
         }
-        D.chunkBox[blockIdx.x * (SETUP_THREADS / CHUNK) + threadIdx.x] = b;
+        D.chunkBox[blk * (SETUP_THREADS / CHUNK) + threadIdx.x] = b;
         if(b.x < b.z)
         {
-            int4 *sb = D.superBox + blockIdx.x / (SUPER * CHUNK / SETUP_THREADS);
+            int4 *sb = D.superBox + blk / (SUPER * CHUNK / SETUP_THREADS);
             atomicMin(&sb->x, (int)b.x);
             atomicMin(&sb->y, (int)b.y);
             atomicMax(&sb->z, (int)b.z);
@@ -688,6 +696,8 @@ __global__ void __launch_bounds__(SETUP_THREADS) k_setup(const __grid_constant__
         atomicAdd(&D.counters[3], (unsigned long long)d);
     }
 }
+
+__global__ void __launch_bounds__(SETUP_THREADS) k_setup(const __grid_constant__ DrawParams D) { setup_body(D, blockIdx.x); }
 
 // ------------------------------------------------------------------------
 // SamplerCore 16-bit path for R8G8B8A8_UNORM (src/Pipeline/SamplerCore.cpp)
@@ -1541,24 +1551,35 @@ __device__ __forceinline__ bool box_hits(int4 b, int bx0, int by0)
     return b.x < b.z && b.x < bx0 + BIN && b.z > bx0 && b.y < by0 + BIN && b.w > by0;
 }
 
-template<int CF, int MS>
-__global__ void __launch_bounds__(RASTER_THREADS) k_raster(const __grid_constant__ DrawParams D)
+__device__ __forceinline__ void flush_counters(unsigned long long *counters, unsigned long long nQuads, unsigned long long nTested,
+                                               unsigned long long nPassed, uint32_t lvMask)
 {
-    extern __shared__ __align__(16) uint8_t smem_raw[];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    constexpr int CW = color_words(CF);
-    RasterShared<CF, MS> &S = reinterpret_cast<RasterShared<CF, MS> *>(smem_raw)[warp];
-    const int nbins = D.binsX * D.binsY;
-    unsigned long long nQuads = 0, nTested = 0, nPassed = 0;
-    uint32_t lvMask = 0;
-    // Persistent warps: each takes the next bin from the queue until it drains,
-    // so a slow bin never holds idle warps of its block.
-    for(;;)
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for(int o = 16; o > 0; o >>= 1)
     {
-    int bin = 0;
-    if(lane == 0) bin = (int)atomicAdd(D.binQueue, 1u);
-    bin = __shfl_sync(0xFFFFFFFFu, bin, 0);
-    if(bin >= nbins) break;
+        nQuads += __shfl_xor_sync(0xFFFFFFFFu, nQuads, o);
+        nTested += __shfl_xor_sync(0xFFFFFFFFu, nTested, o);
+        nPassed += __shfl_xor_sync(0xFFFFFFFFu, nPassed, o);
+        lvMask |= __shfl_xor_sync(0xFFFFFFFFu, lvMask, o);
+    }
+    if(lane == 0 && (nQuads | nTested | nPassed | lvMask))
+    {
+        atomicAdd(&counters[4], nQuads);
+        atomicAdd(&counters[5], nTested);
+        atomicAdd(&counters[6], nPassed);
+        atomicOr(&counters[7], (unsigned long long)lvMask);
+    }
+}
+
+// One bin of a draw: stage its depth and colour, walk the candidates in
+// primitive order in batches, write the bin back.
+template<int CF, int MS>
+__device__ __forceinline__ void raster_bin(const DrawParams &D, RasterShared<CF, MS> &S, int bin, unsigned long long &nQuads,
+                                           unsigned long long &nTested, unsigned long long &nPassed, uint32_t &lvMask)
+{
+    const int lane = threadIdx.x & 31;
+    constexpr int CW = color_words(CF);
     const int bx0 = D.binX0 + (bin % D.binsX) * BIN;
     const int by0 = D.binY0 + (bin / D.binsX) * BIN;
 
@@ -1681,24 +1702,141 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_raster(const __grid_constant
         }
     }
     __syncwarp();
-    }
+}
 
-    // ---- counters ----------------------------------------------------------------
-#pragma unroll
-    for(int o = 16; o > 0; o >>= 1)
+template<int CF, int MS>
+__global__ void __launch_bounds__(RASTER_THREADS) k_raster(const __grid_constant__ DrawParams D)
+{
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    RasterShared<CF, MS> &S = reinterpret_cast<RasterShared<CF, MS> *>(smem_raw)[warp];
+    const int nbins = D.binsX * D.binsY;
+    unsigned long long nQuads = 0, nTested = 0, nPassed = 0;
+    uint32_t lvMask = 0;
+    // Persistent warps: each takes the next bin from the queue until it drains,
+    // so a slow bin never holds idle warps of its block.
+    for(;;)
     {
-        nQuads += __shfl_xor_sync(0xFFFFFFFFu, nQuads, o);
-        nTested += __shfl_xor_sync(0xFFFFFFFFu, nTested, o);
-        nPassed += __shfl_xor_sync(0xFFFFFFFFu, nPassed, o);
-        lvMask |= __shfl_xor_sync(0xFFFFFFFFu, lvMask, o);
+        int bin = 0;
+        if(lane == 0) bin = (int)atomicAdd(D.binQueue, 1u);
+        bin = __shfl_sync(0xFFFFFFFFu, bin, 0);
+        if(bin >= nbins) break;
+        raster_bin<CF, MS>(D, S, bin, nQuads, nTested, nPassed, lvMask);
     }
-    if(lane == 0 && (nQuads | nTested | nPassed | lvMask))
+    flush_counters(D.counters, nQuads, nTested, nPassed, lvMask);
+}
+
+// ------------------------------------------------------------------------
+// Batched draws: N independent draws in one launch of each kernel.  Work units
+// (vertex blocks, setup blocks, bins) of all draws form one index space; a
+// unit finds its draw by binary search over the per-draw prefix arrays.  The
+// grids are persistent (grid-stride / atomic queue), and all counts live in
+// device memory, so one captured graph serves any batch shape.
+// ------------------------------------------------------------------------
+
+struct BatchHeader {
+    uint32_t n;        // draws
+    uint32_t vblocks;  // vertex blocks (256 vertices each)
+    uint32_t sblocks;  // setup blocks (256 triangles each)
+    uint32_t bins;     // bins
+    uint32_t nsuper;   // super-chunk boxes of all draws
+    // byte offsets from the header of the draw records and of the three
+    // n + 1 prefix arrays; they depend on n, so they travel with the data and
+    // a captured graph serves any n
+    uint32_t offDraws, offV, offS, offB;
+    uint32_t pad[7];
+};
+
+struct BatchPtrs {
+    const BatchHeader *hdr;
+    int4 *superAll;
+    unsigned int *binQueue;
+    uint32_t *polyCount;
+    unsigned long long *spanCount;
+    unsigned long long *counters;
+};
+
+// The header and the arrays it locates.
+struct BatchView {
+    BatchHeader h;
+    const DrawParams *draws;
+    const uint32_t *vStart, *sStart, *bStart;
+    __device__ __forceinline__ explicit BatchView(const BatchHeader *p) : h(*p)
     {
-        atomicAdd(&D.counters[4], nQuads);
-        atomicAdd(&D.counters[5], nTested);
-        atomicAdd(&D.counters[6], nPassed);
-        atomicOr(&D.counters[7], (unsigned long long)lvMask);
+        const uint8_t *base = (const uint8_t *)p;
+        draws = (const DrawParams *)(base + h.offDraws);
+        vStart = (const uint32_t *)(base + h.offV);
+        sStart = (const uint32_t *)(base + h.offS);
+        bStart = (const uint32_t *)(base + h.offB);
     }
+};
+
+// Largest d < n with start[d] <= u (start is non-decreasing, start[0] = 0).
+__device__ __forceinline__ uint32_t find_draw(const uint32_t *start, uint32_t n, uint32_t u)
+{
+    uint32_t lo = 0, hi = n - 1;
+    while(lo < hi)
+    {
+        uint32_t mid = (lo + hi + 1) >> 1;
+        if(__ldg(start + mid) <= u) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(256) k_vertex_batch(const __grid_constant__ BatchPtrs B)
+{
+    const BatchView V(B.hdr);
+    const BatchHeader &h = V.h;
+    const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    if(gtid == 0)
+    {
+        *B.polyCount = 0;
+        *B.spanCount = 0;
+        *B.binQueue = 0;
+    }
+    for(uint32_t j = gtid; j < h.nsuper; j += gridDim.x * blockDim.x)
+        B.superAll[j] = make_int4(0x7FFFFFFF, 0x7FFFFFFF, (int)0x80000000, (int)0x80000000);
+    for(uint32_t u = blockIdx.x; u < h.vblocks; u += gridDim.x)
+    {
+        const uint32_t d = find_draw(V.vStart, h.n, u);
+        const DrawParams &D = V.draws[d];
+        const uint32_t i = (u - __ldg(V.vStart + d)) * 256 + threadIdx.x;
+        if(i < D.vertexCount) vertex_body(D, i);
+    }
+}
+
+__global__ void __launch_bounds__(SETUP_THREADS) k_setup_batch(const __grid_constant__ BatchPtrs B)
+{
+    const BatchView V(B.hdr);
+    const BatchHeader &h = V.h;
+    for(uint32_t u = blockIdx.x; u < h.sblocks; u += gridDim.x)
+    {
+        const uint32_t d = find_draw(V.sStart, h.n, u);
+        setup_body(V.draws[d], u - __ldg(V.sStart + d));
+        __syncthreads();  // the next unit reuses the block's shared memory
+    }
+}
+
+template<int CF, int MS>
+__global__ void __launch_bounds__(RASTER_THREADS) k_raster_batch(const __grid_constant__ BatchPtrs B)
+{
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    RasterShared<CF, MS> &S = reinterpret_cast<RasterShared<CF, MS> *>(smem_raw)[warp];
+    const BatchView V(B.hdr);
+    const BatchHeader &h = V.h;
+    unsigned long long nQuads = 0, nTested = 0, nPassed = 0;
+    uint32_t lvMask = 0;
+    for(;;)
+    {
+        uint32_t bin = 0;
+        if(lane == 0) bin = atomicAdd(B.binQueue, 1u);
+        bin = __shfl_sync(0xFFFFFFFFu, bin, 0);
+        if(bin >= h.bins) break;
+        const uint32_t d = find_draw(V.bStart, h.n, bin);
+        raster_bin<CF, MS>(V.draws[d], S, (int)(bin - __ldg(V.bStart + d)), nQuads, nTested, nPassed, lvMask);
+    }
+    flush_counters(B.counters, nQuads, nTested, nPassed, lvMask);
 }
 
 }  // namespace
@@ -1737,6 +1875,7 @@ struct swgb_ctx {
     bool timing;
     std::vector<cudaEvent_t> *evFree;           // recycled events
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> *evPairs;
+    struct BatchState *batch;                   // batched-draw scratch, descriptors and graphs
 };
 
 namespace {
@@ -2072,6 +2211,480 @@ swgb_status enqueue(swgb_ctx *ctx, DrawParams &D)
 }  // namespace
 
 // --------------------------------------------------------------------------
+// Batched draws (swgb_draw_batch)
+// --------------------------------------------------------------------------
+
+struct BatchState {
+    // scratch shared by the draws of one segment
+    float4 *ptv = nullptr; size_t ptvCap = 0;
+    short4 *triBox = nullptr; size_t triBoxCap = 0;
+    TriInfo *triInfo = nullptr; size_t triInfoCap = 0;
+    short4 *chunk = nullptr; size_t chunkCap = 0;
+    int4 *super = nullptr; size_t superCap = 0;
+    uint32_t *spans = nullptr; size_t spansCap = 0;
+    int2 *poly = nullptr; size_t polyCap = 0;
+    unsigned int *queue = nullptr;
+    // descriptors: device copy and pinned staging
+    unsigned char *desc = nullptr; size_t descCap = 0;
+    unsigned char *stage = nullptr; size_t stageCap = 0;
+    cudaEvent_t stageFree = nullptr;
+    bool stagePending = false;
+    // graph per raster variant, valid for one scratch/descriptor generation
+    cudaGraphExec_t graph[6] = {};
+    uint64_t graphGen[6] = {};
+    uint64_t gen = 1;
+    cudaStream_t captureStream = nullptr;
+    int vertexBlocks = 0, setupBlocks = 0;
+    int rasterBlocks[6] = {};  // persistent grid per raster variant
+};
+
+template<typename T>
+swgb_status ensure_gen(T *&ptr, size_t &cap, size_t need, BatchState &B, const char *what)
+{
+    if(need <= cap && ptr) return SWGB_OK;
+    size_t grow = need + need / 4 + 1024;
+    swgb_status s = ensure(ptr, cap, grow, what);
+    if(s == SWGB_OK) B.gen++;
+    return s;
+}
+
+// Attachment bytes a draw writes, as rectangles in a frame per row pitch:
+// address = origin + row * pitch + col, 0 <= col < pitch, origin the lowest
+// attachment address of the call.  Colour planes count whole bins within the
+// scissor (bins are written back whole); depth planes count when the depth
+// test is on.
+struct TouchRect {
+    uint32_t pitch;
+    int64_t row0, row1, col0, col1;
+};
+
+inline bool touch_overlap(const TouchRect &a, const TouchRect &b)
+{
+    return a.pitch == b.pitch && a.row0 < b.row1 && b.row0 < a.row1 && a.col0 < b.col1 && b.col0 < a.col1;
+}
+
+void plane_rects(uintptr_t base, uintptr_t origin, uint32_t pitch, int64_t x0b, int64_t x1b, int y0, int y1, std::vector<TouchRect> &out)
+{
+    if(x1b <= x0b || y1 <= y0 || pitch == 0) return;
+    const uintptr_t rel = base - origin;
+    int64_t r = (int64_t)(rel / pitch), c = (int64_t)(rel % pitch);
+    int64_t sc = c + x0b, ec = c + x1b;
+    const int64_t k = sc / pitch;
+    r += k;
+    sc -= k * pitch;
+    ec -= k * pitch;
+    if(ec - sc >= (int64_t)pitch)
+        out.push_back({pitch, r + y0, r + y1 + 1, 0, (int64_t)pitch});
+    else if(ec <= (int64_t)pitch)
+        out.push_back({pitch, r + y0, r + y1, sc, ec});
+    else
+    {
+        out.push_back({pitch, r + y0, r + y1, sc, (int64_t)pitch});
+        out.push_back({pitch, r + y0 + 1, r + y1 + 1, 0, ec - (int64_t)pitch});
+    }
+}
+
+void draw_writes(const DrawParams &D, uintptr_t origin, std::vector<TouchRect> &out)
+{
+    out.clear();
+    const int cbpp = 4 * color_words(D.cf);
+    // bins cover the scissor rounded out to BIN on the left; the write-back
+    // clips to the scissor, so the scissor is the written rectangle
+    for(int q = 0; q < D.ms; q++)
+    {
+        plane_rects((uintptr_t)D.color + (uintptr_t)q * D.colorSlice, origin, D.colorPitch, (int64_t)D.sx0 * cbpp,
+                    (int64_t)D.sx1 * cbpp, D.sy0, D.sy1, out);
+        if(D.depthTest)
+            plane_rects((uintptr_t)D.depth + (uintptr_t)q * D.depthSlice, origin, D.depthPitch, (int64_t)D.sx0 * 4,
+                        (int64_t)D.sx1 * 4, D.sy0, D.sy1, out);
+    }
+}
+
+// Byte extent [lo, hi) of a rectangle.
+inline std::pair<uintptr_t, uintptr_t> rect_extent(const TouchRect &r, uintptr_t origin)
+{
+    return {origin + (uintptr_t)(r.row0 * r.pitch + r.col0), origin + (uintptr_t)((r.row1 - 1) * r.pitch + r.col1)};
+}
+
+// Union of byte intervals, kept merged.
+struct IntervalSet {
+    std::map<uintptr_t, uintptr_t> iv;
+    bool overlaps(uintptr_t lo, uintptr_t hi) const
+    {
+        if(lo >= hi) return false;
+        auto it = iv.upper_bound(lo);
+        if(it != iv.begin() && std::prev(it)->second > lo) return true;
+        return it != iv.end() && it->first < hi;
+    }
+    void insert(uintptr_t lo, uintptr_t hi)
+    {
+        if(lo >= hi) return;
+        auto it = iv.upper_bound(lo);
+        if(it != iv.begin() && std::prev(it)->second >= lo)
+        {
+            --it;
+            lo = it->first;
+            hi = std::max(hi, it->second);
+            it = iv.erase(it);
+        }
+        while(it != iv.end() && it->first <= hi)
+        {
+            hi = std::max(hi, it->second);
+            it = iv.erase(it);
+        }
+        iv[lo] = hi;
+    }
+    void clear() { iv.clear(); }
+};
+
+// Bytes a draw reads besides its attachments: vertex bindings, index buffer,
+// texture levels.
+void draw_reads(const swgb_pipeline_state &st, const swgb_draw_args &a, const DrawParams &D,
+                std::vector<std::pair<uintptr_t, uintptr_t>> &out)
+{
+    out.clear();
+    // vertices [firstVertex, firstVertex + vertexCount) (non-indexed) or
+    // [baseVertex, baseVertex + vertexCount) (indexed), widened to both
+    const int64_t first = std::min<int64_t>(0, D.baseVertex);
+    const int64_t last = (int64_t)D.firstVertex + std::max<int64_t>(0, D.baseVertex) + D.vertexCount;
+    for(int i = 0; i < D.nattr; i++)
+    {
+        const intptr_t lo = (intptr_t)D.vbuf[i] + (intptr_t)(first * D.vstride[i]);
+        const intptr_t hi = (intptr_t)D.vbuf[i] + (intptr_t)(last * D.vstride[i]) + 16;
+        out.push_back({(uintptr_t)lo, (uintptr_t)hi});
+    }
+    if(a.index_type != SWGB_INDEX_TYPE_NONE && a.indices)
+    {
+        const uintptr_t lo = (uintptr_t)a.indices, isz = a.index_type == SWGB_INDEX_TYPE_UINT16 ? 2 : 4;
+        out.push_back({lo, lo + (uintptr_t)a.count * 3 * isz});
+    }
+    if(D.fs == SWGB_FS_TEX_X_VCOLOR)
+    {
+        const uintptr_t tb = st.texture.format == SWGB_FORMAT_R8G8B8A8_UNORM ? 4 : st.texture.format == SWGB_FORMAT_R16G16B16A16_SFLOAT ? 8 : 16;
+        for(uint32_t l = 0; l < st.texture.level_count && l < SWGB_MAX_MIP_LEVELS; l++)
+        {
+            const swgb_texture_level &lv = st.texture.levels[l];
+            const uintptr_t lo = (uintptr_t)lv.buffer;
+            out.push_back({lo, lo + (uintptr_t)lv.pitch_texels * lv.height * tb});
+        }
+    }
+}
+
+// Splits draws into consecutive segments that each run as one batch: same
+// raster variant, no two draws of a segment write overlapping attachment
+// bytes, and no draw reads bytes another draw of its segment writes.  Running
+// a segment's draws concurrently then gives the sequential result.
+void segment_batch(const std::vector<DrawParams> &D, const std::vector<uint32_t> &src, const swgb_pipeline_state *states,
+                   const swgb_draw_args *args, std::vector<std::pair<uint32_t, uint32_t>> &segs)
+{
+    uintptr_t origin = UINTPTR_MAX;
+    for(const DrawParams &d : D)
+    {
+        origin = std::min(origin, (uintptr_t)d.color);
+        if(d.depthTest) origin = std::min(origin, (uintptr_t)d.depth);
+    }
+    std::unordered_map<uint64_t, std::vector<TouchRect>> cells;  // write rects by (pitch, 64-row, 4 KiB-column) cell
+    std::map<uint32_t, IntervalSet> writesByPitch;
+    IntervalSet reads;
+    std::vector<TouchRect> w;
+    std::vector<std::pair<uintptr_t, uintptr_t>> r;
+    std::vector<uint64_t> keys;
+    auto cellKeys = [&keys](const TouchRect &t) {
+        keys.clear();
+        for(int64_t y = t.row0 >> 6; y <= (t.row1 - 1) >> 6; y++)
+            for(int64_t x = t.col0 >> 12; x <= (t.col1 - 1) >> 12; x++)
+                keys.push_back(((uint64_t)t.pitch << 40) ^ ((uint64_t)(y & 0xFFFFF) << 20) ^ (uint64_t)(x & 0xFFFFF));
+    };
+    uint32_t start = 0;
+    for(uint32_t i = 0; i < (uint32_t)D.size(); i++)
+    {
+        draw_writes(D[i], origin, w);
+        draw_reads(states[src[i]], args[src[i]], D[i], r);
+        bool conflict = i > start && raster_variant(D[i]) != raster_variant(D[start]);
+        for(size_t k = 0; k < w.size() && !conflict; k++)
+        {
+            const TouchRect &t = w[k];
+            cellKeys(t);
+            for(uint64_t key : keys)
+            {
+                auto it = cells.find(key);
+                if(it == cells.end()) continue;
+                for(const TouchRect &o : it->second)
+                    if(touch_overlap(t, o)) { conflict = true; break; }
+                if(conflict) break;
+            }
+            const auto ext = rect_extent(t, origin);
+            if(!conflict && reads.overlaps(ext.first, ext.second)) conflict = true;
+            for(auto &wp : writesByPitch)
+                if(!conflict && wp.first != t.pitch && wp.second.overlaps(ext.first, ext.second)) conflict = true;
+        }
+        for(size_t k = 0; k < r.size() && !conflict; k++)
+            for(auto &wp : writesByPitch)
+                if(wp.second.overlaps(r[k].first, r[k].second)) { conflict = true; break; }
+        if(conflict)
+        {
+            segs.push_back({start, i});
+            start = i;
+            cells.clear();
+            writesByPitch.clear();
+            reads.clear();
+        }
+        for(const TouchRect &t : w)
+        {
+            cellKeys(t);
+            for(uint64_t key : keys) cells[key].push_back(t);
+            const auto ext = rect_extent(t, origin);
+            writesByPitch[t.pitch].insert(ext.first, ext.second);
+        }
+        for(auto &e : r) reads.insert(e.first, e.second);
+    }
+    if(start < (uint32_t)D.size()) segs.push_back({start, (uint32_t)D.size()});
+}
+
+void launch_raster_batch(int variant, const BatchPtrs &P, uint32_t blocks, cudaStream_t st)
+{
+    switch(variant)
+    {
+    case 0: k_raster_batch<CF_RGBA8, 1><<<blocks, RASTER_THREADS, raster_smem<CF_RGBA8, 1>(), st>>>(P); break;
+    case 1: k_raster_batch<CF_RGBA16F, 1><<<blocks, RASTER_THREADS, raster_smem<CF_RGBA16F, 1>(), st>>>(P); break;
+    case 2: k_raster_batch<CF_RGBA32F, 1><<<blocks, RASTER_THREADS, raster_smem<CF_RGBA32F, 1>(), st>>>(P); break;
+    case 3: k_raster_batch<CF_RGBA8, 4><<<blocks, RASTER_THREADS, raster_smem<CF_RGBA8, 4>(), st>>>(P); break;
+    case 4: k_raster_batch<CF_RGBA16F, 4><<<blocks, RASTER_THREADS, raster_smem<CF_RGBA16F, 4>(), st>>>(P); break;
+    default: k_raster_batch<CF_RGBA32F, 4><<<blocks, RASTER_THREADS, raster_smem<CF_RGBA32F, 4>(), st>>>(P); break;
+    }
+}
+
+template<int CF, int MS>
+swgb_status batch_attr(int sms, int &blocks)
+{
+    swgb_status s = cuda_check(cudaFuncSetAttribute(k_raster_batch<CF, MS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)raster_smem<CF, MS>()),
+                               "batch raster smem attribute");
+    if(s != SWGB_OK) return s;
+    int perSM = 0;
+    if((s = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_raster_batch<CF, MS>, RASTER_THREADS, raster_smem<CF, MS>()),
+                       "batch raster occupancy")) != SWGB_OK)
+        return s;
+    blocks = sms * (perSM > 0 ? perSM : 1);
+    return SWGB_OK;
+}
+
+swgb_status batch_init(swgb_ctx *ctx)
+{
+    if(ctx->batch) return SWGB_OK;
+    BatchState *B = new BatchState();
+    swgb_status s;
+    int sms = 1, perSM = 1;
+    if((s = cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device), "SM count")) != SWGB_OK ||
+       (s = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_setup_batch, SETUP_THREADS, 0), "setup occupancy")) != SWGB_OK ||
+       (s = batch_attr<CF_RGBA8, 1>(sms, B->rasterBlocks[0])) != SWGB_OK || (s = batch_attr<CF_RGBA16F, 1>(sms, B->rasterBlocks[1])) != SWGB_OK ||
+       (s = batch_attr<CF_RGBA32F, 1>(sms, B->rasterBlocks[2])) != SWGB_OK || (s = batch_attr<CF_RGBA8, 4>(sms, B->rasterBlocks[3])) != SWGB_OK ||
+       (s = batch_attr<CF_RGBA16F, 4>(sms, B->rasterBlocks[4])) != SWGB_OK || (s = batch_attr<CF_RGBA32F, 4>(sms, B->rasterBlocks[5])) != SWGB_OK)
+    {
+        delete B;
+        return s;
+    }
+    B->setupBlocks = std::max(1, sms * std::max(1, perSM));
+    B->vertexBlocks = std::max(1, sms * 8);
+    if((s = cuda_check(cudaMalloc((void **)&B->queue, sizeof(unsigned int)), "batch queue")) != SWGB_OK ||
+       (s = cuda_check(cudaEventCreateWithFlags(&B->stageFree, cudaEventDisableTiming), "batch event")) != SWGB_OK ||
+       (s = cuda_check(cudaStreamCreateWithFlags(&B->captureStream, cudaStreamNonBlocking), "capture stream")) != SWGB_OK)
+    {
+        delete B;
+        return s;
+    }
+    ctx->batch = B;
+    return SWGB_OK;
+}
+
+void batch_free(BatchState *B)
+{
+    if(!B) return;
+    cudaFree(B->ptv); cudaFree(B->triBox); cudaFree(B->triInfo); cudaFree(B->chunk); cudaFree(B->super);
+    cudaFree(B->spans); cudaFree(B->poly); cudaFree(B->queue); cudaFree(B->desc);
+    if(B->stage) cudaFreeHost(B->stage);
+    if(B->stageFree) cudaEventDestroy(B->stageFree);
+    for(int v = 0; v < 6; v++)
+        if(B->graph[v]) cudaGraphExecDestroy(B->graph[v]);
+    if(B->captureStream) cudaStreamDestroy(B->captureStream);
+    delete B;
+}
+
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Enqueues one segment: descriptors (staged at stageOff), then the three
+// batched kernels, as a graph replay unless kernel timing is on.
+swgb_status enqueue_segment(swgb_ctx *ctx, std::vector<DrawParams> &draws, uint32_t first, uint32_t last, size_t &stageOff)
+{
+    BatchState &B = *ctx->batch;
+    const uint32_t n = last - first;
+    std::vector<uint32_t> vStart(n + 1), sStart(n + 1), bStart(n + 1);
+    uint64_t verts = 0, vblocks = 0, sblocks = 0, bins = 0, nsuper = 0;
+    for(uint32_t k = 0; k < n; k++)
+    {
+        const DrawParams &d = draws[first + k];
+        vStart[k] = (uint32_t)vblocks;
+        sStart[k] = (uint32_t)sblocks;
+        bStart[k] = (uint32_t)bins;
+        const uint32_t vc = d.count ? d.vertexCount : 0;
+        vblocks += (vc + 255) / 256;
+        verts += (uint64_t)((vc + 255) / 256) * 256;
+        sblocks += (d.count + SETUP_THREADS - 1) / SETUP_THREADS;
+        bins += d.count ? (uint64_t)d.binsX * d.binsY : 0;
+        nsuper += (uint64_t)d.nsuper;
+    }
+    vStart[n] = (uint32_t)vblocks;
+    sStart[n] = (uint32_t)sblocks;
+    bStart[n] = (uint32_t)bins;
+    if(vblocks > 0xFFFFFFFFull || sblocks > 0xFFFFFFFFull || bins > 0xFFFFFFFFull || (uint64_t)n * sizeof(DrawParams) > 0xF0000000ull)
+        return set_error(SWGB_UNSUPPORTED_STATE, "batch too large");
+    swgb_status s;
+    const uint64_t triSlots = sblocks * SETUP_THREADS;
+    if((s = ensure_gen(B.ptv, B.ptvCap, (size_t)verts * 4, B, "batch ptv")) != SWGB_OK) return s;
+    if((s = ensure_gen(B.triBox, B.triBoxCap, (size_t)triSlots, B, "batch boxes")) != SWGB_OK) return s;
+    if((s = ensure_gen(B.triInfo, B.triInfoCap, (size_t)triSlots, B, "batch records")) != SWGB_OK) return s;
+    if((s = ensure_gen(B.chunk, B.chunkCap, (size_t)triSlots / CHUNK, B, "batch chunks")) != SWGB_OK) return s;
+    if((s = ensure_gen(B.super, B.superCap, (size_t)nsuper + 1, B, "batch super boxes")) != SWGB_OK) return s;
+    uint64_t tris = 0;
+    for(uint32_t k = 0; k < n; k++) tris += draws[first + k].count;
+    if((s = ensure_gen(B.spans, B.spansCap, (size_t)(tris * 24 + 4096), B, "batch spans")) != SWGB_OK) return s;
+    if((s = ensure_gen(B.poly, B.polyCap, (size_t)(tris + 1) * MAX_POLY, B, "batch polygons")) != SWGB_OK) return s;
+    // per-draw scratch windows
+    uint64_t vOff = 0, sOff = 0, supOff = 0;
+    for(uint32_t k = 0; k < n; k++)
+    {
+        DrawParams &d = draws[first + k];
+        d.ptv = B.ptv + vOff * 4;
+        d.triBox = B.triBox + sOff;
+        d.triInfo = B.triInfo + sOff;
+        d.chunkBox = B.chunk + sOff / CHUNK;
+        d.superBox = B.super + supOff;
+        d.spans = B.spans;
+        d.spanCount = ctx->spanCount;
+        d.spanCapacity = ctx->spanRowsLimit ? std::min<uint64_t>(B.spansCap, ctx->spanRowsLimit) : B.spansCap;
+        d.poly = B.poly;
+        d.polyCount = ctx->polyCount;
+        d.polyCapacity = (uint32_t)std::min<size_t>(B.polyCap / MAX_POLY, 0xFFFFFFFFu);
+        d.counters = ctx->counters;
+        d.error = ctx->error;
+        d.binQueue = B.queue;
+        const uint32_t vc = d.count ? d.vertexCount : 0;
+        vOff += (uint64_t)((vc + 255) / 256) * 256;
+        sOff += (uint64_t)((d.count + SETUP_THREADS - 1) / SETUP_THREADS) * SETUP_THREADS;
+        supOff += (uint64_t)d.nsuper;
+    }
+    // descriptor image: header | draws | vStart | sStart | bStart
+    const size_t offDraws = align_up(sizeof(BatchHeader), 64);
+    const size_t offV = align_up(offDraws + (size_t)n * sizeof(DrawParams), 64);
+    const size_t offS = align_up(offV + (size_t)(n + 1) * 4, 64);
+    const size_t offB = align_up(offS + (size_t)(n + 1) * 4, 64);
+    const size_t bytes = align_up(offB + (size_t)(n + 1) * 4, 256);
+    if((s = ensure_gen(B.desc, B.descCap, bytes, B, "batch descriptors")) != SWGB_OK) return s;
+    unsigned char *img = B.stage + stageOff;
+    BatchHeader h = {};
+    h.n = n;
+    h.vblocks = (uint32_t)vblocks;
+    h.sblocks = (uint32_t)sblocks;
+    h.bins = (uint32_t)bins;
+    h.nsuper = (uint32_t)nsuper;
+    h.offDraws = (uint32_t)offDraws;
+    h.offV = (uint32_t)offV;
+    h.offS = (uint32_t)offS;
+    h.offB = (uint32_t)offB;
+    memcpy(img, &h, sizeof(h));
+    memcpy(img + offDraws, draws.data() + first, (size_t)n * sizeof(DrawParams));
+    memcpy(img + offV, vStart.data(), (size_t)(n + 1) * 4);
+    memcpy(img + offS, sStart.data(), (size_t)(n + 1) * 4);
+    memcpy(img + offB, bStart.data(), (size_t)(n + 1) * 4);
+    if((s = cuda_check(cudaMemcpyAsync(B.desc, img, bytes, cudaMemcpyHostToDevice, ctx->stream), "batch descriptors upload")) != SWGB_OK)
+        return s;
+    stageOff += bytes;
+
+    BatchPtrs P;
+    P.hdr = (const BatchHeader *)B.desc;
+    P.superAll = B.super;
+    P.binQueue = B.queue;
+    P.polyCount = ctx->polyCount;
+    P.spanCount = ctx->spanCount;
+    P.counters = ctx->counters;
+    const int variant = raster_variant(draws[first]);
+    const uint32_t rblocks = (uint32_t)B.rasterBlocks[variant];
+    if(ctx->timing)
+    {
+        timed_launch(ctx, SWGB_KERNEL_VERTEX, [&] { k_vertex_batch<<<B.vertexBlocks, 256, 0, ctx->stream>>>(P); });
+        timed_launch(ctx, SWGB_KERNEL_SETUP, [&] { k_setup_batch<<<B.setupBlocks, SETUP_THREADS, 0, ctx->stream>>>(P); });
+        timed_launch(ctx, SWGB_KERNEL_RASTER, [&] { launch_raster_batch(variant, P, rblocks, ctx->stream); });
+        return cuda_check(cudaGetLastError(), "batch launch");
+    }
+    // The graph's kernel parameters point at fixed scratch and descriptor
+    // addresses; it is captured again only when one of them moved.
+    if(!B.graph[variant] || B.graphGen[variant] != B.gen)
+    {
+        if(B.graph[variant]) cudaGraphExecDestroy(B.graph[variant]);
+        B.graph[variant] = nullptr;
+        cudaGraph_t g = nullptr;
+        if((s = cuda_check(cudaStreamBeginCapture(B.captureStream, cudaStreamCaptureModeThreadLocal), "begin capture")) != SWGB_OK) return s;
+        k_vertex_batch<<<B.vertexBlocks, 256, 0, B.captureStream>>>(P);
+        k_setup_batch<<<B.setupBlocks, SETUP_THREADS, 0, B.captureStream>>>(P);
+        launch_raster_batch(variant, P, rblocks, B.captureStream);
+        if((s = cuda_check(cudaStreamEndCapture(B.captureStream, &g), "end capture")) != SWGB_OK) return s;
+        s = cuda_check(cudaGraphInstantiate(&B.graph[variant], g, 0), "graph instantiate");
+        cudaGraphDestroy(g);
+        if(s != SWGB_OK) return s;
+        B.graphGen[variant] = B.gen;
+    }
+    timed_launch(ctx, SWGB_KERNEL_BATCH, [&] { cudaGraphLaunch(B.graph[variant], ctx->stream); });
+    ctx->launches += 2;  // the graph holds three kernel launches
+    return cuda_check(cudaGetLastError(), "graph launch");
+}
+
+swgb_status draw_batch(swgb_ctx *ctx, const swgb_pipeline_state *states, const swgb_draw_args *args, uint32_t n)
+{
+    std::vector<DrawParams> draws;
+    std::vector<uint32_t> src;
+    draws.reserve(n);
+    for(uint32_t i = 0; i < n; i++)
+    {
+        if(args[i].count == 0) continue;  // Renderer.cpp:187
+        DrawParams D;
+        swgb_status s = bake(&states[i], &args[i], D);
+        if(s != SWGB_OK) return s;
+        draws.push_back(D);
+        src.push_back(i);
+    }
+    if(draws.empty()) return SWGB_OK;
+    swgb_status s;
+    if((s = batch_init(ctx)) != SWGB_OK) return s;
+    BatchState &B = *ctx->batch;
+    std::vector<std::pair<uint32_t, uint32_t>> segs;
+    segment_batch(draws, src, states, args, segs);
+    // staging for every segment of this call; wait until the previous call's
+    // uploads have read theirs
+    size_t need = 0;
+    for(auto &sg : segs)
+        need += align_up(sizeof(BatchHeader), 64) + align_up((size_t)(sg.second - sg.first) * sizeof(DrawParams), 64) +
+                3 * align_up((size_t)(sg.second - sg.first + 1) * 4, 64) + 512;
+    if(B.stagePending)
+    {
+        if((s = cuda_check(cudaEventSynchronize(B.stageFree), "staging reuse")) != SWGB_OK) return s;
+        B.stagePending = false;
+    }
+    if(need > B.stageCap)
+    {
+        if(B.stage) cudaFreeHost(B.stage);
+        B.stage = nullptr;
+        B.stageCap = 0;
+        if((s = cuda_check(cudaMallocHost((void **)&B.stage, need + need / 4), "batch staging")) != SWGB_OK) return s;
+        B.stageCap = need + need / 4;
+    }
+    size_t stageOff = 0;
+    for(auto &sg : segs)
+        if((s = enqueue_segment(ctx, draws, sg.first, sg.second, stageOff)) != SWGB_OK) return s;
+    if((s = cuda_check(cudaEventRecord(B.stageFree, ctx->stream), "staging event")) != SWGB_OK) return s;
+    B.stagePending = true;
+    return SWGB_OK;
+}
+
+// --------------------------------------------------------------------------
 // Allocation-free draws (swgb_draw_noalloc)
 //
 // Some callers cannot allocate device memory at draw time: a driver-style
@@ -2207,6 +2820,7 @@ swgb_status swgb_ctx_destroy(swgb_ctx *c)
         for(auto e : *c->evFree) cudaEventDestroy(e);
     delete c->evPairs;
     delete c->evFree;
+    batch_free(c->batch);
     delete c;
     return SWGB_OK;
 }
@@ -2290,12 +2904,9 @@ swgb_status swgb_draw_noalloc(const swgb_pipeline_state *st, const swgb_draw_arg
 swgb_status swgb_draw_batch(swgb_ctx *ctx, const swgb_pipeline_state *states, const swgb_draw_args *args, uint32_t n)
 {
     if(!ctx || (!states && n) || (!args && n)) return set_error(SWGB_INVALID_ARG, "null argument");
-    for(uint32_t i = 0; i < n; i++)
-    {
-        swgb_status s = swgb_draw(ctx, &states[i], &args[i]);
-        if(s != SWGB_OK) return s;
-    }
-    return SWGB_OK;
+    if(n == 0) return SWGB_OK;
+    cudaSetDevice(ctx->device);
+    return draw_batch(ctx, states, args, n);
 }
 
 swgb_status swgb_sync(swgb_ctx *ctx)

@@ -37,9 +37,11 @@ class Renderer:
         check(self._L.swgb_draw(self._ctx, C.byref(state), C.byref(args)), "swgb_draw")
 
     def draw_batch(self, states, args):
+        """Enqueue draws as batches; `states`/`args` are sequences or prebuilt
+        ctypes arrays of PipelineState / DrawArgs."""
         n = len(states)
-        S = (abi.PipelineState * n)(*states)
-        A = (abi.DrawArgs * n)(*args)
+        S = states if isinstance(states, C.Array) else (abi.PipelineState * n)(*states)
+        A = args if isinstance(args, C.Array) else (abi.DrawArgs * n)(*args)
         check(self._L.swgb_draw_batch(self._ctx, S, A, n), "swgb_draw_batch")
 
     def synchronize(self):
@@ -59,7 +61,7 @@ class Renderer:
     def set_kernel_timing(self, enable):
         check(self._L.swgb_set_kernel_timing(self._ctx, 1 if enable else 0), "swgb_set_kernel_timing")
 
-    KERNEL_NAMES = ("vertex", "setup", "raster")
+    KERNEL_NAMES = ("vertex", "setup", "raster", "batch")
 
     def kernel_times(self):
         """{kernel: (total ms, launches)} since the last call (synchronises)."""
@@ -114,3 +116,56 @@ class DeviceScene:
 
     def args(self):
         return scenes.build_args(self.scene, None if self.indices is None else self.indices.data_ptr())
+
+
+class DeviceBatch:
+    """A BatchScene resident in device memory: one vertex array, one texture
+    array, atlas pages of colour (RGBA8) and depth (D32F), and the C-ABI
+    state/args arrays of every draw."""
+
+    def __init__(self, batch, device="cuda"):
+        import torch
+        self.batch = batch
+        self.device = torch.device(device)
+        P = batch.page_size
+        self.vertices = torch.from_numpy(np.ascontiguousarray(batch.vertices)).to(self.device)
+        self.textures = torch.from_numpy(np.ascontiguousarray(batch.textures)).to(self.device)
+        self.color = torch.empty((batch.pages, P, P, 4), dtype=torch.uint8, device=self.device)
+        self.depth = torch.empty((batch.pages, P, P), dtype=torch.float32, device=self.device)
+        self.clear()
+        n = batch.n
+        self.states = (abi.PipelineState * n)()
+        self.args = (abi.DrawArgs * n)()
+        cbase, dbase = self.color.data_ptr(), self.depth.data_ptr()
+        vbase, tbase = self.vertices.data_ptr(), self.textures.data_ptr()
+        tex_bytes = batch.textures[0].nbytes
+        for i in range(n):
+            sc = batch.draw_scene(i)
+            page, x, y = (int(v) for v in batch.place[i])
+            off = (page * P + y) * P + x
+            self.states[i] = scenes.build_state(sc, cbase + off * 4, dbase + off * 4,
+                                                vbase + int(batch.vstart[i]) * scenes.VERTEX_STRIDE,
+                                                [tbase + i * tex_bytes], color_pitch=P * 4, depth_pitch=P * 4)
+            self.args[i] = scenes.build_args(sc)
+
+    def clear(self):
+        self.color[...] = torch_tensor(self.batch.clear_color, self.color)
+        self.depth.fill_(self.batch.clear_depth)
+
+    def draw_batch(self, renderer):
+        renderer.draw_batch(self.states, self.args)
+
+    def draw_each(self, renderer):
+        for i in range(self.batch.n):
+            renderer.draw(self.states[i], self.args[i])
+
+    def view(self, i):
+        """Colour and depth of draw i's viewport (device tensor views)."""
+        page, x, y = (int(v) for v in self.batch.place[i])
+        s = int(self.batch.sides[i])
+        return self.color[page, y:y + s, x:x + s], self.depth[page, y:y + s, x:x + s]
+
+
+def torch_tensor(values, like):
+    import torch
+    return torch.tensor(values, dtype=like.dtype, device=like.device)

@@ -374,3 +374,79 @@ def clear_buffers(scene):
     color[...] = np.asarray(scene.clear_color, color.dtype)
     depth = np.full(ds, scene.clear_depth, np.float32)
     return color, depth
+
+
+def shelf_pack(sides, page_size):
+    """Shelf-pack squares into pages of page_size x page_size, tallest first.
+    Returns (page, x, y) per input square, in input order."""
+    sides = np.asarray(sides, np.int64)
+    order = np.argsort(-sides, kind="stable")
+    out = np.zeros((len(sides), 3), np.int64)
+    page, x, y, shelf_h = 0, 0, 0, 0
+    for i in order:
+        s = int(sides[i])
+        if s > page_size:
+            raise ValueError("viewport %d larger than the atlas page %d" % (s, page_size))
+        if x + s > page_size:
+            x, y, shelf_h = 0, y + shelf_h, 0
+        if y + s > page_size:
+            page, x, y, shelf_h = page + 1, 0, 0, 0
+        out[i] = (page, x, y)
+        x += s
+        shelf_h = max(shelf_h, s)
+    return out
+
+
+@dataclass
+class BatchScene:
+    """Independent draws into disjoint viewports of an atlas (one or more
+    square pages of RGBA8 + D32F).  Draw i renders vertices
+    [vstart[i], vstart[i] + 3 * tris[i]) with texture textures[i] into the
+    side[i] x side[i] square at (x, y) of page `page`."""
+    name: str
+    tris: np.ndarray          # int64 [n]
+    sides: np.ndarray         # int64 [n]
+    place: np.ndarray         # int64 [n, 3]: page, x, y
+    vertices: np.ndarray      # float32 [3 * sum(tris), 10]
+    vstart: np.ndarray        # int64 [n]
+    textures: np.ndarray      # uint8 [n, T, T, 4]
+    page_size: int
+    pages: int
+    sampler: dict = field(default_factory=dict)
+    clear_color: tuple = (0, 0, 0, 0)
+    clear_depth: float = 1.0
+
+    @property
+    def n(self):
+        return len(self.tris)
+
+    def draw_scene(self, i):
+        """Draw i as a stand-alone Scene (its own side x side framebuffer)."""
+        s = int(self.sides[i])
+        v0 = int(self.vstart[i])
+        return Scene(name="%s_draw%d" % (self.name, i), width=s, height=s,
+                     vertices=self.vertices[v0:v0 + 3 * int(self.tris[i])], tri_count=int(self.tris[i]),
+                     fragment_shader=abi.FS_TEX_X_VCOLOR, texture_levels=[self.textures[i]],
+                     sampler=dict(self.sampler), clear_color=self.clear_color, clear_depth=self.clear_depth)
+
+
+def scene_batch(n_draws=4096, tri_min=16, tri_max=65536, sides=(128, 256, 384, 512), page_size=16384,
+                tex_size=256, seed_index=2):
+    """Batched forward: n_draws independent draws, triangle counts
+    log-uniform in [tri_min, tri_max] (rounded), square viewports with side
+    uniform in `sides`, shelf-packed into page_size^2 RGBA8 + D32F atlas
+    pages; triangles uniform in clip space as in scene_small; each draw
+    samples its own tex_size^2 RGBA8 texture bilinearly (one level)."""
+    rng = _rng(seed_index)
+    tris = np.rint(np.exp(rng.uniform(math.log(tri_min), math.log(tri_max), n_draws))).astype(np.int64)
+    tris = np.clip(tris, tri_min, tri_max)
+    side = rng.choice(np.asarray(sides, np.int64), n_draws)
+    place = shelf_pack(side, page_size)
+    vertices = random_triangles(rng, int(tris.sum()), textured=True)
+    vstart = np.concatenate([[0], np.cumsum(3 * tris)[:-1]]).astype(np.int64)
+    textures = rng.integers(0, 256, (n_draws, tex_size, tex_size, 4), dtype=np.uint8)
+    sampler = dict(mag_filter=abi.FILTER_LINEAR, min_filter=abi.FILTER_LINEAR, mipmap_mode=abi.MIPMAP_MODE_NEAREST,
+                   address_u=abi.ADDRESS_REPEAT, address_v=abi.ADDRESS_REPEAT, mip_lod_bias=0.0, min_lod=0.0, max_lod=0.0)
+    return BatchScene(name="batch%d_tris%d-%d_page%d" % (n_draws, tri_min, tri_max, page_size), tris=tris, sides=side,
+                      place=place, vertices=vertices, vstart=vstart, textures=textures, page_size=page_size,
+                      pages=int(place[:, 0].max()) + 1, sampler=sampler)
