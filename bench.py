@@ -1,9 +1,15 @@
 """Benchmark of the GB300 draw path on the 1M-triangle textured 1080p frame.
 
-python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload heightfield|small]
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload heightfield|small|batch]
 
 One step = one frame: clear colour + depth, then one draw of the whole scene
-through the C-ABI (swgb_draw).  Inputs are resident in HBM for ``value``; the L2
+through the C-ABI (swgb_draw).  The default line also carries "batched": the
+4096-draw atlas workload with triangle counts log-uniform in [16, 1024] (a
+reduced-size sample of the batch workload, stated in its config), one
+swgb_draw_batch call per step against the same draws issued one swgb_draw
+each.  --workload batch measures the full 4096-draw atlas workload
+(log-uniform [16, 65536] triangles) as the headline line: one step = clear the
+atlas + one swgb_draw_batch of all draws.  Inputs are resident in HBM for ``value``; the L2
 (129 MB) is flushed by writing a 256 MiB buffer before every timed step,
 outside the step's CUDA events.  ``e2e`` is the same metric through the same
 public call with host buffers: every step copies the scene (vertices, indices,
@@ -35,11 +41,19 @@ WORKLOADS = {
                    "2048^2 RGBA8 12-level chain trilinear REPEAT, colour = texel * vertex colour, depth LESS, "
                    "blend SRC_ALPHA/ONE_MINUS_SRC_ALPHA",
     "small": "1000 independent Gouraud triangles, 256x256 RGBA8 + D32F, depth LESS, no blend, no texture",
+    "batch": "4096 independent draws, triangle counts log-uniform in [16, 65536], uniform clip-space triangles, "
+             "square viewports with side uniform in {128,256,384,512} shelf-packed into 16384^2 RGBA8 + D32F "
+             "atlas pages, each draw sampling its own 256^2 RGBA8 texture bilinearly, depth LESS, no blend",
 }
+
+BATCH_FULL = dict(n_draws=4096, tri_min=16, tri_max=65536)
+BATCH_REDUCED = dict(n_draws=4096, tri_min=16, tri_max=1024)
 
 
 def make_scene(name):
     from swiftshader_gb300 import scenes
+    if name == "batch":
+        return scenes.scene_batch(**BATCH_FULL)
     return scenes.scene_heightfield() if name == "heightfield" else scenes.scene_small()
 
 
@@ -243,6 +257,14 @@ def run_ours(args):
     barrier()
     e2e_ms = sum(s.elapsed_time(e) for s, e in zip(e_starts, e_ends)) / args.steps
 
+    # batched vs per-draw on the reduced-size atlas workload (free the frame first)
+    batched = None
+    if args.workload == "heightfield" and not args.no_batched:
+        del h_vert, h_idx, h_lv, h_color, h_depth
+        _, _, batched = measure_batch(r, stream, flush, BATCH_REDUCED, 3, 1, 2, dev)
+        batched["config"]["note"] = ("reduced-size sample of the batch workload (triangles log-uniform in "
+                                     "[16, 1024] instead of [16, 65536]); --workload batch runs the full one")
+
     # max over ranks
     ms_per_step, e2e_ms = max_over_ranks([ms_per_step, e2e_ms], dev)
 
@@ -296,12 +318,187 @@ def run_ours(args):
                 line["roofline"]["traffic"] = tj["bytes_per_launch"]
         except Exception:
             pass
+    if batched is not None:
+        line["batched"] = batched
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args, scene, bounded_s=args.cpu_seconds)
     print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def batch_raster_bytes(b, cnt):
+    """Algorithmic bytes of the batched raster kernel: F_t*4 + F_p*(4 + 4) +
+    every draw's texture once (no blending in this workload)."""
+    return cnt["fragments_tested"] * 4 + cnt["fragments_passed"] * 8 + int(b.textures.nbytes)
+
+
+def time_steps(stream, flush, steps, body):
+    import torch
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    torch.cuda.synchronize()
+    for i in range(steps):
+        flush.fill_(i & 0xFF)  # L2 flush, outside the step's events
+        starts[i].record(stream)
+        body()
+        ends[i].record(stream)
+    torch.cuda.synchronize()
+    return [s.elapsed_time(e) for s, e in zip(starts, ends)]
+
+
+def measure_batch(r, stream, flush, params, steps, warmup, per_draw_steps, dev):
+    """Batched vs per-draw on the atlas workload: one swgb_draw_batch call per
+    step against one swgb_draw per draw, same draws, same kernels' work."""
+    from swiftshader_gb300 import DeviceBatch, scenes
+    b = scenes.scene_batch(**params)
+    db = DeviceBatch(b, dev)
+
+    def batched():
+        db.clear()
+        db.draw_batch(r)
+
+    def per_draw():
+        db.clear()
+        db.draw_each(r)
+
+    for _ in range(warmup):
+        batched()
+    per_draw()
+    r.synchronize()
+    r.reset_counters()
+    l0 = r.launch_count()
+    tb = time_steps(stream, flush, steps, batched)
+    r.synchronize()
+    launches = r.launch_count() - l0
+    cnt = r.counters()
+    tp = time_steps(stream, flush, per_draw_steps, per_draw)
+    r.synchronize()
+    mb, mp = sum(tb) / len(tb), sum(tp) / len(tp)
+    per_step = {k: v // steps if k != "texture_levels_mask" else v for k, v in cnt.items()}
+    return b, db, {
+        "config": {"draws": b.n, "triangles_log_uniform": [params["tri_min"], params["tri_max"]],
+                   "triangles": int(b.tris.sum()), "viewport_sides": [128, 256, 384, 512],
+                   "atlas_pages": b.pages, "page": b.page_size, "texture": "256^2 RGBA8 per draw, bilinear"},
+        "batched_ms_per_step": round(mb, 3), "per_draw_ms_per_step": round(mp, 3),
+        "speedup_vs_per_draw": round(mp / mb, 2),
+        "draws_per_s": round(b.n / (mb * 1e-3), 1), "per_draw_draws_per_s": round(b.n / (mp * 1e-3), 1),
+        "gfrag_per_s": round(per_step["fragments_tested"] / (mb * 1e-3) / 1e9, 3),
+        "mtri_per_s": round(per_step["triangles_in"] / (mb * 1e-3) / 1e6, 2),
+        "gpu_launches_per_step": launches / steps, "steps": steps, "per_draw_steps": per_draw_steps,
+        "counters_per_step": per_step,
+    }
+
+
+def run_batch(args):
+    """--workload batch: the full 4096-draw atlas workload as the headline."""
+    import numpy as np
+    import torch
+    from swiftshader_gb300 import Renderer
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    r = Renderer(local, stream)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    if world > 1:
+        torch.distributed.barrier()
+    b, db, res = measure_batch(r, stream, flush, BATCH_FULL, args.steps, args.warmup, min(args.steps, 2), dev)
+    clk = clocks.stop()
+    # kernel-level timing: the batch as direct launches (timing disables the graph)
+    r.set_kernel_timing(True)
+    r.kernel_times()
+    db.clear()
+    db.draw_batch(r)
+    r.synchronize()
+    kt = r.kernel_times()
+    r.set_kernel_timing(False)
+    # end to end: vertices + textures host->device, atlas back, inside the timed region
+    pin = lambda arr: torch.from_numpy(np.ascontiguousarray(arr)).pin_memory()
+    h_vert, h_tex = pin(b.vertices), pin(b.textures)
+    h_color = torch.empty(db.color.shape, dtype=db.color.dtype).pin_memory()
+    h_depth = torch.empty(db.depth.shape, dtype=db.depth.dtype).pin_memory()
+    h2d = h_vert.numel() * 4 + h_tex.numel()
+    d2h = h_color.numel() + h_depth.numel() * 4
+
+    def e2e_step():
+        db.vertices.copy_(h_vert, non_blocking=True)
+        db.textures.copy_(h_tex, non_blocking=True)
+        db.clear()
+        db.draw_batch(r)
+        h_color.copy_(db.color, non_blocking=True)
+        h_depth.copy_(db.depth, non_blocking=True)
+
+    e2e_step()
+    e2e_steps = max(1, min(args.steps, 3))
+    te = time_steps(stream, flush, e2e_steps, e2e_step)
+    mb = res["batched_ms_per_step"]
+    me = sum(te) / len(te)
+    mb, me = max_over_ranks([mb, me], dev)
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+    rast_ms, rast_n = kt.get("raster", (0.0, 0))
+    rast_avg = rast_ms / max(1, rast_n)
+    rbytes = batch_raster_bytes(b, res["counters_per_step"])
+    peak, peak_kind = measured_peaks()
+    achieved = rbytes / (rast_avg * 1e-3) / 1e9 if rast_avg > 0 else 0.0
+    line = {
+        "metric": "draws/s", "value": round(world * b.n / (mb * 1e-3), 1), "unit": "draws/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(mb, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 + int32 fixed point (RGBA8 / D32F out)",
+        "data": "synthetic (seeded generator, swiftshader_gb300.scenes.scene_batch)",
+        "config": {"workload": WORKLOADS["batch"], "l2": "flushed before every timed step (256 MiB write)",
+                   "parallelism": "replicas only" if world > 1 else "single GPU"},
+        "batched": res,
+        "kernels": {k: {"avg_ms": v[0] / max(1, v[1]), "launches": v[1]} for k, v in kt.items()},
+        "roofline": {"kernel": "k_raster_batch", "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "algorithmic_bytes_per_launch": rbytes, "traffic": None},
+        "e2e": {"value": round(world * b.n / (me * 1e-3), 1), "unit": "draws/s", "ms_per_step": round(me, 3),
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(round(res["gpu_launches_per_step"] * args.steps)),
+        "clocks": clk,
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_batch(b, bounded_s=args.cpu_seconds)
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cpu_baseline_batch(b, bounded_s=12.0, threads=None):
+    """Oracle on a seeded random sample of the batch's draws, scaled to the
+    whole batch by fragment work (triangles x viewport area)."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    threads = threads or os.cpu_count() or 1
+    order = np.random.Generator(np.random.PCG64(7)).permutation(b.n)
+    cost = b.tris.astype(np.float64) * b.sides.astype(np.float64) ** 2
+    done, work, t0 = 0, 0.0, time.perf_counter()
+    for i in order:
+        oracle.render(b.draw_scene(int(i)), threads)
+        done += 1
+        work += cost[i]
+        if time.perf_counter() - t0 >= bounded_s:
+            break
+    dt = time.perf_counter() - t0
+    est = dt * cost.sum() / work
+    return {"value": round(b.n / est, 3), "unit": "draws/s", "cores": threads, "kind": "port",
+            "sample": "%d of %d draws (seeded random order), %.1f s, scaled to the batch by triangles x viewport "
+                      "area; %s" % (done, b.n, dt, platform.machine())}
 
 
 def cpu_baseline(args, scene, bounded_s=12.0, threads=None):
@@ -332,6 +529,8 @@ def run_reference(args):
     oracle.build()
     scene = make_scene(args.workload)
     threads = os.cpu_count() or 1
+    if args.workload == "batch":
+        return run_reference_batch(args, scene, world, threads)
     for _ in range(args.warmup):
         oracle.render(scene, threads)
     t = []
@@ -358,6 +557,29 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_reference_batch(args, b, world, threads):
+    """Reference arm of the batch workload: every step times the oracle on a
+    bounded sample of draws, scaled to the whole batch."""
+    per_step = max(2.0, min(10.0, 150.0 / max(1, args.steps + args.warmup)))
+    for _ in range(args.warmup):
+        cpu_baseline_batch(b, bounded_s=per_step, threads=threads)
+    vals = [cpu_baseline_batch(b, bounded_s=per_step, threads=threads) for _ in range(args.steps)]
+    value = statistics.mean(v["value"] for v in vals)
+    line = {
+        "impl": "reference",
+        "metric": "draws/s", "value": round(value, 3), "unit": "draws/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * b.n / value, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 + int32 fixed point (RGBA8 / D32F out)",
+        "data": "synthetic (seeded generator, swiftshader_gb300.scenes.scene_batch)",
+        "config": {"workload": WORKLOADS["batch"], "parallelism": "host threads"},
+        "cpu_baseline": {"value": round(value, 3), "unit": "draws/s", "cores": threads, "kind": "port",
+                         "sample": "per step: " + vals[-1]["sample"]},
+        "e2e": {"value": round(value, 3), "unit": "draws/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -367,9 +589,12 @@ def main():
     ap.add_argument("--workload", default="heightfield", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-vs-per-draw sample")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch":
+        run_batch(args)
     else:
         run_ours(args)
 
