@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-#define SWGB_ABI_VERSION 1
+#define SWGB_ABI_VERSION 2
 
 typedef enum swgb_status {
     SWGB_OK = 0,
@@ -233,6 +233,11 @@ typedef struct swgb_counters {
     uint64_t fragments_tested;   /* covered samples that reached the depth test       */
     uint64_t fragments_passed;   /* samples that passed and were written              */
     uint64_t texture_levels_mask; /* bit i set: mip level i was sampled (OR across draws) */
+    /* adjoint (swgb_draw_adjoint*) */
+    uint64_t adjoint_fragments;       /* (pixel, primitive) shading adjoints evaluated       */
+    uint64_t adjoint_depth_mismatch;  /* samples whose replayed depth differs from the saved depth */
+    uint64_t adjoint_list_overflow;   /* blended fragments dropped: more than 2048 on one pixel */
+    uint64_t reserved;
 } swgb_counters;
 
 typedef struct swgb_ctx swgb_ctx;
@@ -281,6 +286,55 @@ swgb_status swgb_draw_batch(swgb_ctx *ctx, const swgb_pipeline_state *states, co
 #define SWGB_NOALLOC_MAX_VERTICES 98304u
 swgb_status swgb_draw_noalloc(const swgb_pipeline_state *state, const swgb_draw_args *args, void *stream);
 
+/* Adjoint of a draw.  No counterpart in the reference (it has no backward
+ * pass).  Given dL/d(colour attachment) after the draw, it adds to the
+ * gradient buffers dL/d(texels), dL/d(vertex attributes) and dL/d(vertex
+ * positions), holding visibility fixed:
+ *   - visibility is recomputed by replaying the draw's coverage and depth
+ *     test from the attachment contents before the draw, which must be the
+ *     clear values below (the draw ran on freshly cleared attachments); the
+ *     saved depth attachment (state->depth, as the draw left it) is compared
+ *     against the replay sample by sample (adjoint_depth_mismatch counts
+ *     differences);
+ *   - the differentiated colour is the perspective-correct interpolation of
+ *     the triangle's vertex attributes at the pixel centre, the fixed
+ *     fragment shader, the fp32 texture filter with its level of detail held
+ *     constant, and the blend (none, or premultiplied OVER: ONE,
+ *     ONE_MINUS_SRC_ALPHA, ADD for colour and alpha), with attachment
+ *     rounding taken as the identity and sub-pixel snapping ignored;
+ *   - positions receive gradients through the barycentrics only (no edge or
+ *     visibility terms); depth gets none.
+ * Supported: float colour attachments (R16G16B16A16_SFLOAT,
+ * R32G32B32A32_SFLOAT), float textures or none, 1 or 4 samples.  Other
+ * states return SWGB_UNSUPPORTED_STATE.  Gradients accumulate with fp32
+ * atomics, so their low bits vary from run to run.  A blended pixel may hold
+ * any number of passing fragments up to 2048 (the excess is counted in
+ * adjoint_list_overflow).  The context keeps about 110 KiB of adjoint scratch
+ * per resident adjoint warp, allocated on the first adjoint call. */
+typedef struct swgb_adjoint_args {
+    const float *grad_color;         /* dL/dcolour: float RGBA per pixel and sample, device memory */
+    uint32_t grad_color_pitch_bytes; /* row pitch of grad_color                                     */
+    uint32_t reserved0;
+    uint64_t grad_color_slice_bytes; /* bytes between sample planes of grad_color                   */
+    float clear_color[4];            /* attachment contents before the draw                         */
+    float clear_depth;
+    uint32_t reserved1;
+    /* outputs (added to): per mip level, float RGBA per texel with the
+     * level's pitch_texels; per vertex binding, a buffer with that binding's
+     * stride whose float fields at each attribute's offset receive the
+     * attribute's gradient (attribute 0: object-space position) */
+    float *grad_texels[SWGB_MAX_MIP_LEVELS];
+    void *grad_vertices[SWGB_MAX_ATTRIBS];
+} swgb_adjoint_args;
+swgb_status swgb_draw_adjoint(swgb_ctx *ctx, const swgb_pipeline_state *state, const swgb_draw_args *args,
+                              const swgb_adjoint_args *adj);
+
+/* Adjoints of n independent draws (e.g. views of one scene) as one launch of
+ * each kernel: gradients of all draws accumulate into their buffers (which
+ * may be shared between draws). */
+swgb_status swgb_draw_adjoint_batch(swgb_ctx *ctx, const swgb_pipeline_state *states, const swgb_draw_args *args,
+                                    const swgb_adjoint_args *adjs, uint32_t n);
+
 /* Waits for every draw enqueued so far (Renderer::synchronize). */
 swgb_status swgb_sync(swgb_ctx *ctx);
 
@@ -300,6 +354,7 @@ uint64_t swgb_launch_count(swgb_ctx *ctx);
 #define SWGB_KERNEL_SETUP 1
 #define SWGB_KERNEL_RASTER 2
 #define SWGB_KERNEL_BATCH 3 /* one graph replay of a batch segment (three kernels) */
+#define SWGB_KERNEL_ADJOINT 4
 #define SWGB_KERNEL_KINDS 8
 swgb_status swgb_set_kernel_timing(swgb_ctx *ctx, int enable);
 swgb_status swgb_get_kernel_times(swgb_ctx *ctx, double ms[SWGB_KERNEL_KINDS], uint32_t launches[SWGB_KERNEL_KINDS]);

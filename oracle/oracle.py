@@ -43,6 +43,9 @@ def lib():
         L.oracle_draw.argtypes = [C.POINTER(abi.PipelineState), C.POINTER(abi.DrawArgs), C.c_int,
                                   C.POINTER(abi.Counters)]
         L.oracle_draw.restype = C.c_int
+        L.oracle_draw_visibility.argtypes = [C.POINTER(abi.PipelineState), C.POINTER(abi.DrawArgs), C.c_int,
+                                             C.POINTER(abi.Counters), C.c_void_p, C.c_void_p, C.c_int]
+        L.oracle_draw_visibility.restype = C.c_int
         L.oracle_round_int.argtypes = [C.c_float]
         L.oracle_round_int.restype = C.c_int32
         L.oracle_round_int_clamped.argtypes = [C.c_float]
@@ -100,3 +103,22 @@ def render(scene, nthreads=1, color=None, depth=None):
         raise RuntimeError("oracle_draw failed: %s" % abi.STATUS_NAMES.get(s, s))
     del keep
     return color, depth, cnt.as_dict()
+
+
+def render_visibility(scene, nthreads=1, cap=8):
+    """render() that also returns the fixed visibility: vis [S, H, W, cap]
+    primitive ids passing the depth test per sample in primitive order, and
+    vis_len [S, H, W] (counts every entry, even past cap)."""
+    from swiftshader_gb300 import abi, scenes
+    color, depth = scenes.clear_buffers(scene)
+    st, args, keep = host_state(scene, color, depth)
+    S = scene.samples
+    vis = np.zeros((S, scene.height, scene.width, cap), np.uint32)
+    vis_len = np.zeros((S, scene.height, scene.width), np.uint32)
+    cnt = abi.Counters()
+    s = lib().oracle_draw_visibility(C.byref(st), C.byref(args), nthreads, C.byref(cnt), vis.ctypes.data,
+                                     vis_len.ctypes.data, cap)
+    if s != 0:
+        raise RuntimeError("oracle_draw_visibility failed: %s" % abi.STATUS_NAMES.get(s, s))
+    del keep
+    return color, depth, cnt.as_dict(), vis, vis_len

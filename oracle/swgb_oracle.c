@@ -143,6 +143,11 @@ typedef struct {
     uint32_t srcC, dstC, opC, srcA, dstA, opA; /* simplified blend state */
     int rows;                /* span rows per primitive (fb height + 2)  */
     int ms;                  /* samples: 1 or 4                          */
+    /* optional visibility record: per sample and pixel, the primitives whose
+     * fragment passed the depth test, in primitive order (up to visCap) */
+    uint32_t *vis;
+    uint32_t *visLen;        /* entries appended (may exceed visCap)      */
+    int visCap;
 } ODraw;
 
 /* 4x MSAA sample positions (src/Pipeline/Constants.hpp:26-52,
@@ -157,6 +162,7 @@ static const int YF[4] = { -96, -32, 32, 96 };
 
 typedef struct {
     int visible;
+    uint32_t id;     /* primitive index within the draw */
     int yMin, yMax;
     float x0, y0;
     OPlane z, w, V[MAXV];
@@ -1244,6 +1250,14 @@ static void pixel_quad(const ODraw *d, const OSampler *smp, const OPrim *pr, int
                     if(zMask & (1 << i)) *depth_at(d, q, x + (i & 1), y + (i >> 1)) = z[q][i];
         }
         if(cnt) cnt->fragments_passed += (uint64_t)__builtin_popcount((unsigned)zMask);
+        if(d->vis)
+            for(int i = 0; i < 4; i++)
+            {
+                if(!(zMask & (1 << i))) continue;
+                size_t pix = ((size_t)q * st->framebuffer_height + (size_t)(y + (i >> 1))) * st->framebuffer_width + (size_t)(x + (i & 1));
+                uint32_t n = d->visLen[pix]++;
+                if(n < (uint32_t)d->visCap) d->vis[pix * (size_t)d->visCap + n] = pr->id;
+            }
 
         /* blendColor / alphaBlend / writeColor per sample plane (PixelProgram.cpp:261-284) */
         for(int i = 0; i < 4; i++)
@@ -1356,6 +1370,7 @@ static void run_setup(OJob *j, int t)
                 pr->right[q] = pr->left[q] + d->rows;
             }
             int clipped = 0;
+            pr->id = j->first + i;
             int vis = process_triangle(d, j->first + i, pr, &j->local[t], &clipped);
             j->local[t].triangles_in++;
             if(clipped) j->local[t].triangles_clipped++;
@@ -1409,13 +1424,17 @@ static void run_phase(OJob *j, int phase)
     for(int t = 0; t < n; t++) pthread_join(th[t], NULL);
 }
 
-swgb_status oracle_draw(const swgb_pipeline_state *st, const swgb_draw_args *a, int nthreads, swgb_counters *cnt)
+static swgb_status draw_impl(const swgb_pipeline_state *st, const swgb_draw_args *a, int nthreads, swgb_counters *cnt,
+                             uint32_t *vis, uint32_t *visLen, int visCap)
 {
     if(!st || !a) return SWGB_INVALID_ARG;
     if(a->count == 0) return SWGB_OK; /* Renderer.cpp:187 */
     ODraw d;
     swgb_status s = prepare(&d, st, a);
     if(s != SWGB_OK) return s;
+    d.vis = visCap > 0 ? vis : NULL;
+    d.visLen = visLen;
+    d.visCap = visCap;
     if(!st->color) return SWGB_INVALID_ARG;
     OSampler smp;
     memset(&smp, 0, sizeof(smp));
@@ -1461,6 +1480,18 @@ swgb_status oracle_draw(const swgb_pipeline_state *st, const swgb_draw_args *a, 
     free(j.prims);
     free(j.spans);
     return SWGB_OK;
+}
+
+swgb_status oracle_draw(const swgb_pipeline_state *st, const swgb_draw_args *a, int nthreads, swgb_counters *cnt)
+{
+    return draw_impl(st, a, nthreads, cnt, NULL, NULL, 0);
+}
+
+swgb_status oracle_draw_visibility(const swgb_pipeline_state *st, const swgb_draw_args *a, int nthreads, swgb_counters *cnt,
+                                   uint32_t *vis, uint32_t *visLen, int visCap)
+{
+    if(!vis || !visLen || visCap < 1) return SWGB_INVALID_ARG;
+    return draw_impl(st, a, nthreads, cnt, vis, visLen, visCap);
 }
 
 /* ------------------------------------------------------------------------ */

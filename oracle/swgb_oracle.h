@@ -26,6 +26,15 @@ extern "C" {
  * Counters are accumulated into *cnt when it is non-null. */
 swgb_status oracle_draw(const swgb_pipeline_state *state, const swgb_draw_args *args, int nthreads, swgb_counters *cnt);
 
+/* oracle_draw that also records visibility: for every sample plane q and
+ * pixel (x, y), the primitives whose fragment passed the depth test, in
+ * primitive order.  vis[((q * H + y) * W + x) * visCap + k] holds entry k,
+ * visLen[(q * H + y) * W + x] counts every entry (entries past visCap are
+ * counted but not stored).  visLen must be zeroed by the caller.  The
+ * adjoint's FP64 reference gradient takes its fixed visibility from here. */
+swgb_status oracle_draw_visibility(const swgb_pipeline_state *state, const swgb_draw_args *args, int nthreads, swgb_counters *cnt,
+                                   uint32_t *vis, uint32_t *visLen, int visCap);
+
 /* Primitive-level probes, exported so the reference's Reactor known-answer
  * vectors (tests/ReactorUnitTests/ReactorUnitTests.cpp) can pin them. */
 int32_t oracle_round_int(float x);         /* RoundInt: cvtss2si, half-even, INT_MIN on overflow */

@@ -114,7 +114,19 @@ class Counters(C.Structure):
     _fields_ = [("triangles_in", C.c_uint64), ("triangles_rejected", C.c_uint64),
                 ("triangles_clipped", C.c_uint64), ("triangles_visible", C.c_uint64),
                 ("quads", C.c_uint64), ("fragments_tested", C.c_uint64),
-                ("fragments_passed", C.c_uint64), ("texture_levels_mask", C.c_uint64)]
+                ("fragments_passed", C.c_uint64), ("texture_levels_mask", C.c_uint64),
+                ("adjoint_fragments", C.c_uint64), ("adjoint_depth_mismatch", C.c_uint64),
+                ("adjoint_list_overflow", C.c_uint64), ("reserved", C.c_uint64)]
 
     def as_dict(self):
-        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+        return {k: int(getattr(self, k)) for k, _ in self._fields_ if k != "reserved"}
+
+
+ADJOINT_MAX_FRAGMENTS_PER_PIXEL = 2048
+
+
+class AdjointArgs(C.Structure):
+    _fields_ = [("grad_color", C.c_void_p), ("grad_color_pitch_bytes", C.c_uint32), ("reserved0", C.c_uint32),
+                ("grad_color_slice_bytes", C.c_uint64), ("clear_color", C.c_float * 4), ("clear_depth", C.c_float),
+                ("reserved1", C.c_uint32), ("grad_texels", C.c_void_p * MAX_MIP_LEVELS),
+                ("grad_vertices", C.c_void_p * MAX_ATTRIBS)]

@@ -68,6 +68,9 @@ constexpr int Y_MAX_MS_OFFSET = 351;  // 256 + toFixedPoint(0.375) - 1
 
 enum { ERR_INDEX_RANGE = 1, ERR_POLY_OVERFLOW = 2 };
 
+// Device counter words of a context: 0-7 as swgb_counters, then the adjoint's.
+enum { CNT_ADJ_FRAGMENTS = 8, CNT_ADJ_MISMATCH = 9, CNT_ADJ_OVERFLOW = 10, CTX_COUNTERS = 12 };
+
 struct TexLevel {
     const uint8_t *buf;
     uint32_t w, h, pitch;
@@ -1572,6 +1575,54 @@ __device__ __forceinline__ void flush_counters(unsigned long long *counters, uns
     }
 }
 
+// Walks the candidates of the bin at (bx0, by0) in primitive order --
+// super-chunk, chunk, then triangle boxes, compacted with ballots into
+// S.triList -- and hands them to batch(nb) BATCH at a time (nb < BATCH for the
+// last call).
+template<class SH, class F>
+__device__ __forceinline__ void walk_bin(const DrawParams &D, SH &S, int bx0, int by0, F &&batch)
+{
+    const int lane = threadIdx.x & 31;
+    int listCount = 0;  // warp-uniform
+    for(int sb = 0; sb < D.nsuper; sb += 32)
+    {
+        unsigned superHits = __ballot_sync(0xFFFFFFFFu, sb + lane < D.nsuper && box_hits(D.superBox[sb + lane], bx0, by0));
+        while(superHits)
+        {
+            const int sc = sb + __ffs(superHits) - 1;
+            superHits &= superHits - 1;
+            const int c = sc * SUPER + lane;
+            unsigned chunkHits = __ballot_sync(0xFFFFFFFFu, c < D.nchunks && box_hits(D.chunkBox[c], bx0, by0));
+            while(chunkHits)
+            {
+                const int chunk = sc * SUPER + __ffs(chunkHits) - 1;
+                chunkHits &= chunkHits - 1;
+#pragma unroll
+                for(int half = 0; half < CHUNK / 32; half++)
+                {
+                    const uint32_t tri = (uint32_t)chunk * CHUNK + half * 32 + lane;
+                    const bool th = tri < D.count && box_hits(D.triBox[tri], bx0, by0);
+                    const unsigned b = __ballot_sync(0xFFFFFFFFu, th);
+                    if(th) S.triList[listCount + __popc(b & ((1u << lane) - 1u))] = (int)tri;
+                    listCount += __popc(b);
+                    __syncwarp();
+                    if(listCount >= BATCH)
+                    {
+                        batch(BATCH);
+                        const int rem = listCount - BATCH;
+                        const int v = lane < rem ? S.triList[BATCH + lane] : 0;
+                        __syncwarp();
+                        if(lane < rem) S.triList[lane] = v;
+                        listCount = rem;
+                        __syncwarp();
+                    }
+                }
+            }
+        }
+    }
+    if(listCount > 0) batch(listCount);
+}
+
 // One bin of a draw: stage its depth and colour, walk the candidates in
 // primitive order in batches, write the bin back.
 template<int CF, int MS>
@@ -1630,45 +1681,8 @@ __device__ __forceinline__ void raster_bin(const DrawParams &D, RasterShared<CF,
     }
     __syncwarp();
 
-    // ---- candidates in primitive order: super-chunk, chunk, triangle boxes -----
-    int listCount = 0;  // warp-uniform
-    for(int sb = 0; sb < D.nsuper; sb += 32)
-    {
-        unsigned superHits = __ballot_sync(0xFFFFFFFFu, sb + lane < D.nsuper && box_hits(D.superBox[sb + lane], bx0, by0));
-        while(superHits)
-        {
-            const int sc = sb + __ffs(superHits) - 1;
-            superHits &= superHits - 1;
-            const int c = sc * SUPER + lane;
-            unsigned chunkHits = __ballot_sync(0xFFFFFFFFu, c < D.nchunks && box_hits(D.chunkBox[c], bx0, by0));
-            while(chunkHits)
-            {
-                const int chunk = sc * SUPER + __ffs(chunkHits) - 1;
-                chunkHits &= chunkHits - 1;
-#pragma unroll
-                for(int half = 0; half < CHUNK / 32; half++)
-                {
-                    const uint32_t tri = (uint32_t)chunk * CHUNK + half * 32 + lane;
-                    const bool th = tri < D.count && box_hits(D.triBox[tri], bx0, by0);
-                    const unsigned b = __ballot_sync(0xFFFFFFFFu, th);
-                    if(th) S.triList[listCount + __popc(b & ((1u << lane) - 1u))] = (int)tri;
-                    listCount += __popc(b);
-                    __syncwarp();
-                    if(listCount >= BATCH)
-                    {
-                        raster_batch<CF, MS>(D, S, BATCH, bx0, by0, nQuads, nTested, nPassed, lvMask);
-                        const int rem = listCount - BATCH;
-                        const int v = lane < rem ? S.triList[BATCH + lane] : 0;
-                        __syncwarp();
-                        if(lane < rem) S.triList[lane] = v;
-                        listCount = rem;
-                        __syncwarp();
-                    }
-                }
-            }
-        }
-    }
-    if(listCount > 0) raster_batch<CF, MS>(D, S, listCount, bx0, by0, nQuads, nTested, nPassed, lvMask);
+    // ---- candidates in primitive order, in batches of BATCH ----------------------
+    walk_bin(D, S, bx0, by0, [&](int nb) { raster_batch<CF, MS>(D, S, nb, bx0, by0, nQuads, nTested, nPassed, lvMask); });
 
     // ---- write the bin back, every sample plane ----------------------------------
     for(int q = 0; q < MS; q++)
@@ -1744,7 +1758,8 @@ struct BatchHeader {
     // n + 1 prefix arrays; they depend on n, so they travel with the data and
     // a captured graph serves any n
     uint32_t offDraws, offV, offS, offB;
-    uint32_t pad[7];
+    uint32_t offAdj;  // per-draw AdjParams (adjoint batches only)
+    uint32_t pad[6];
 };
 
 struct BatchPtrs {
@@ -1839,6 +1854,8 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_raster_batch(const __grid_co
     flush_counters(B.counters, nQuads, nTested, nPassed, lvMask);
 }
 
+#include "swgb_adjoint.cuh"
+
 }  // namespace
 
 // ==========================================================================
@@ -1876,6 +1893,9 @@ struct swgb_ctx {
     std::vector<cudaEvent_t> *evFree;           // recycled events
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> *evPairs;
     struct BatchState *batch;                   // batched-draw scratch, descriptors and graphs
+    bool adjAttr;
+    int adjBlocks[2];      // persistent adjoint grid: 1 and 4 samples
+    uint8_t *adjScratch;   // one region per adjoint warp of the larger grid
 };
 
 namespace {
@@ -2159,9 +2179,9 @@ void timed_launch(swgb_ctx *ctx, int kind, F &&launch)
     }
 }
 
-swgb_status enqueue(swgb_ctx *ctx, DrawParams &D)
+// Grows the context's scratch for draw D and points D at it.
+swgb_status prepare_scratch(swgb_ctx *ctx, DrawParams &D)
 {
-    if(D.count == 0) return SWGB_OK;  // Renderer.cpp:187
     swgb_status s;
     if((s = ensure(ctx->ptv, ctx->ptvCap, (size_t)D.vertexCount * 4, "ptv")) != SWGB_OK) return s;
     const size_t triSlots = ((size_t)D.count + SETUP_THREADS - 1) / SETUP_THREADS * SETUP_THREADS;
@@ -2195,6 +2215,14 @@ swgb_status enqueue(swgb_ctx *ctx, DrawParams &D)
         if((s = raster_grids(ctx->device, true, ctx->rasterBlocks)) != SWGB_OK) return s;
         ctx->rasterAttr = true;
     }
+    return SWGB_OK;
+}
+
+swgb_status enqueue(swgb_ctx *ctx, DrawParams &D)
+{
+    if(D.count == 0) return SWGB_OK;  // Renderer.cpp:187
+    swgb_status s;
+    if((s = prepare_scratch(ctx, D)) != SWGB_OK) return s;
     const uint32_t nv = D.vertexCount;
     timed_launch(ctx, SWGB_KERNEL_VERTEX, [&] { k_vertex<<<(nv + 255) / 256, 256, 0, ctx->stream>>>(D, nv); });
     const uint32_t setupBlocks = (uint32_t)((D.count + SETUP_THREADS - 1) / SETUP_THREADS);
@@ -2230,8 +2258,8 @@ struct BatchState {
     cudaEvent_t stageFree = nullptr;
     bool stagePending = false;
     // graph per raster variant, valid for one scratch/descriptor generation
-    cudaGraphExec_t graph[6] = {};
-    uint64_t graphGen[6] = {};
+    cudaGraphExec_t graph[8] = {};  // raster variants 0-5, adjoint 1 / 4 samples
+    uint64_t graphGen[8] = {};
     uint64_t gen = 1;
     cudaStream_t captureStream = nullptr;
     int vertexBlocks = 0, setupBlocks = 0;
@@ -2503,7 +2531,7 @@ void batch_free(BatchState *B)
     cudaFree(B->spans); cudaFree(B->poly); cudaFree(B->queue); cudaFree(B->desc);
     if(B->stage) cudaFreeHost(B->stage);
     if(B->stageFree) cudaEventDestroy(B->stageFree);
-    for(int v = 0; v < 6; v++)
+    for(int v = 0; v < 8; v++)
         if(B->graph[v]) cudaGraphExecDestroy(B->graph[v]);
     if(B->captureStream) cudaStreamDestroy(B->captureStream);
     delete B;
@@ -2511,9 +2539,35 @@ void batch_free(BatchState *B)
 
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
-// Enqueues one segment: descriptors (staged at stageOff), then the three
-// batched kernels, as a graph replay unless kernel timing is on.
-swgb_status enqueue_segment(swgb_ctx *ctx, std::vector<DrawParams> &draws, uint32_t first, uint32_t last, size_t &stageOff)
+// Descriptor image of a segment of n draws: header | draws | vStart | sStart
+// | bStart | (adjoint batches) AdjParams.  Returns its size in bytes.
+struct DescLayout {
+    size_t offDraws, offV, offS, offB, offAdj, bytes;
+};
+
+DescLayout desc_layout(uint32_t n, bool adjoint)
+{
+    DescLayout L;
+    L.offDraws = align_up(sizeof(BatchHeader), 64);
+    L.offV = align_up(L.offDraws + (size_t)n * sizeof(DrawParams), 64);
+    L.offS = align_up(L.offV + (size_t)(n + 1) * 4, 64);
+    L.offB = align_up(L.offS + (size_t)(n + 1) * 4, 64);
+    L.offAdj = align_up(L.offB + (size_t)(n + 1) * 4, 64);
+    L.bytes = align_up(L.offAdj + (adjoint ? (size_t)n * sizeof(AdjParams) : 0), 256);
+    return L;
+}
+
+void launch_adjoint_batch(int ms4, const BatchPtrs &P, uint32_t blocks, cudaStream_t st, uint8_t *scratch)
+{
+    if(ms4) k_adjoint_batch<4><<<blocks, ADJ_THREADS, ADJ_WARPS * sizeof(AdjShared<4>), st>>>(P, scratch);
+    else k_adjoint_batch<1><<<blocks, ADJ_THREADS, ADJ_WARPS * sizeof(AdjShared<1>), st>>>(P, scratch);
+}
+
+// Enqueues one segment: descriptors (staged at stageOff), then the batched
+// vertex and setup kernels and the raster kernel (or, with adj, the adjoint
+// kernel), as a graph replay unless kernel timing is on.
+swgb_status enqueue_segment(swgb_ctx *ctx, std::vector<DrawParams> &draws, uint32_t first, uint32_t last, size_t &stageOff,
+                            const AdjParams *adj = nullptr)
 {
     BatchState &B = *ctx->batch;
     const uint32_t n = last - first;
@@ -2572,12 +2626,8 @@ swgb_status enqueue_segment(swgb_ctx *ctx, std::vector<DrawParams> &draws, uint3
         sOff += (uint64_t)((d.count + SETUP_THREADS - 1) / SETUP_THREADS) * SETUP_THREADS;
         supOff += (uint64_t)d.nsuper;
     }
-    // descriptor image: header | draws | vStart | sStart | bStart
-    const size_t offDraws = align_up(sizeof(BatchHeader), 64);
-    const size_t offV = align_up(offDraws + (size_t)n * sizeof(DrawParams), 64);
-    const size_t offS = align_up(offV + (size_t)(n + 1) * 4, 64);
-    const size_t offB = align_up(offS + (size_t)(n + 1) * 4, 64);
-    const size_t bytes = align_up(offB + (size_t)(n + 1) * 4, 256);
+    const DescLayout L = desc_layout(n, adj != nullptr);
+    const size_t bytes = L.bytes;
     if((s = ensure_gen(B.desc, B.descCap, bytes, B, "batch descriptors")) != SWGB_OK) return s;
     unsigned char *img = B.stage + stageOff;
     BatchHeader h = {};
@@ -2586,15 +2636,17 @@ swgb_status enqueue_segment(swgb_ctx *ctx, std::vector<DrawParams> &draws, uint3
     h.sblocks = (uint32_t)sblocks;
     h.bins = (uint32_t)bins;
     h.nsuper = (uint32_t)nsuper;
-    h.offDraws = (uint32_t)offDraws;
-    h.offV = (uint32_t)offV;
-    h.offS = (uint32_t)offS;
-    h.offB = (uint32_t)offB;
+    h.offDraws = (uint32_t)L.offDraws;
+    h.offV = (uint32_t)L.offV;
+    h.offS = (uint32_t)L.offS;
+    h.offB = (uint32_t)L.offB;
+    h.offAdj = (uint32_t)L.offAdj;
     memcpy(img, &h, sizeof(h));
-    memcpy(img + offDraws, draws.data() + first, (size_t)n * sizeof(DrawParams));
-    memcpy(img + offV, vStart.data(), (size_t)(n + 1) * 4);
-    memcpy(img + offS, sStart.data(), (size_t)(n + 1) * 4);
-    memcpy(img + offB, bStart.data(), (size_t)(n + 1) * 4);
+    memcpy(img + L.offDraws, draws.data() + first, (size_t)n * sizeof(DrawParams));
+    memcpy(img + L.offV, vStart.data(), (size_t)(n + 1) * 4);
+    memcpy(img + L.offS, sStart.data(), (size_t)(n + 1) * 4);
+    memcpy(img + L.offB, bStart.data(), (size_t)(n + 1) * 4);
+    if(adj) memcpy(img + L.offAdj, adj + first, (size_t)n * sizeof(AdjParams));
     if((s = cuda_check(cudaMemcpyAsync(B.desc, img, bytes, cudaMemcpyHostToDevice, ctx->stream), "batch descriptors upload")) != SWGB_OK)
         return s;
     stageOff += bytes;
@@ -2606,13 +2658,18 @@ swgb_status enqueue_segment(swgb_ctx *ctx, std::vector<DrawParams> &draws, uint3
     P.polyCount = ctx->polyCount;
     P.spanCount = ctx->spanCount;
     P.counters = ctx->counters;
-    const int variant = raster_variant(draws[first]);
-    const uint32_t rblocks = (uint32_t)B.rasterBlocks[variant];
+    // graph slot: raster variants 0-5, adjoint 6 (1 sample) and 7 (4 samples)
+    const int variant = adj ? 6 + (draws[first].ms > 1 ? 1 : 0) : raster_variant(draws[first]);
+    const uint32_t rblocks = (uint32_t)(adj ? ctx->adjBlocks[variant - 6] : B.rasterBlocks[variant]);
+    auto third = [&](cudaStream_t st) {
+        if(adj) launch_adjoint_batch(variant - 6, P, rblocks, st, ctx->adjScratch);
+        else launch_raster_batch(variant, P, rblocks, st);
+    };
     if(ctx->timing)
     {
         timed_launch(ctx, SWGB_KERNEL_VERTEX, [&] { k_vertex_batch<<<B.vertexBlocks, 256, 0, ctx->stream>>>(P); });
         timed_launch(ctx, SWGB_KERNEL_SETUP, [&] { k_setup_batch<<<B.setupBlocks, SETUP_THREADS, 0, ctx->stream>>>(P); });
-        timed_launch(ctx, SWGB_KERNEL_RASTER, [&] { launch_raster_batch(variant, P, rblocks, ctx->stream); });
+        timed_launch(ctx, adj ? SWGB_KERNEL_ADJOINT : SWGB_KERNEL_RASTER, [&] { third(ctx->stream); });
         return cuda_check(cudaGetLastError(), "batch launch");
     }
     // The graph's kernel parameters point at fixed scratch and descriptor
@@ -2625,7 +2682,7 @@ swgb_status enqueue_segment(swgb_ctx *ctx, std::vector<DrawParams> &draws, uint3
         if((s = cuda_check(cudaStreamBeginCapture(B.captureStream, cudaStreamCaptureModeThreadLocal), "begin capture")) != SWGB_OK) return s;
         k_vertex_batch<<<B.vertexBlocks, 256, 0, B.captureStream>>>(P);
         k_setup_batch<<<B.setupBlocks, SETUP_THREADS, 0, B.captureStream>>>(P);
-        launch_raster_batch(variant, P, rblocks, B.captureStream);
+        third(B.captureStream);
         if((s = cuda_check(cudaStreamEndCapture(B.captureStream, &g), "end capture")) != SWGB_OK) return s;
         s = cuda_check(cudaGraphInstantiate(&B.graph[variant], g, 0), "graph instantiate");
         cudaGraphDestroy(g);
@@ -2635,6 +2692,36 @@ swgb_status enqueue_segment(swgb_ctx *ctx, std::vector<DrawParams> &draws, uint3
     timed_launch(ctx, SWGB_KERNEL_BATCH, [&] { cudaGraphLaunch(B.graph[variant], ctx->stream); });
     ctx->launches += 2;  // the graph holds three kernel launches
     return cuda_check(cudaGetLastError(), "graph launch");
+}
+
+// Stages the descriptors of every segment of one call (after the previous
+// call's uploads have read theirs) and enqueues the segments in order.
+swgb_status run_segments(swgb_ctx *ctx, std::vector<DrawParams> &draws, const std::vector<std::pair<uint32_t, uint32_t>> &segs,
+                         const AdjParams *adj)
+{
+    swgb_status s;
+    BatchState &B = *ctx->batch;
+    size_t need = 0;
+    for(auto &sg : segs) need += desc_layout(sg.second - sg.first, adj != nullptr).bytes;
+    if(B.stagePending)
+    {
+        if((s = cuda_check(cudaEventSynchronize(B.stageFree), "staging reuse")) != SWGB_OK) return s;
+        B.stagePending = false;
+    }
+    if(need > B.stageCap)
+    {
+        if(B.stage) cudaFreeHost(B.stage);
+        B.stage = nullptr;
+        B.stageCap = 0;
+        if((s = cuda_check(cudaMallocHost((void **)&B.stage, need + need / 4), "batch staging")) != SWGB_OK) return s;
+        B.stageCap = need + need / 4;
+    }
+    size_t stageOff = 0;
+    for(auto &sg : segs)
+        if((s = enqueue_segment(ctx, draws, sg.first, sg.second, stageOff, adj)) != SWGB_OK) return s;
+    if((s = cuda_check(cudaEventRecord(B.stageFree, ctx->stream), "staging event")) != SWGB_OK) return s;
+    B.stagePending = true;
+    return SWGB_OK;
 }
 
 swgb_status draw_batch(swgb_ctx *ctx, const swgb_pipeline_state *states, const swgb_draw_args *args, uint32_t n)
@@ -2654,34 +2741,154 @@ swgb_status draw_batch(swgb_ctx *ctx, const swgb_pipeline_state *states, const s
     if(draws.empty()) return SWGB_OK;
     swgb_status s;
     if((s = batch_init(ctx)) != SWGB_OK) return s;
-    BatchState &B = *ctx->batch;
     std::vector<std::pair<uint32_t, uint32_t>> segs;
     segment_batch(draws, src, states, args, segs);
-    // staging for every segment of this call; wait until the previous call's
-    // uploads have read theirs
-    size_t need = 0;
-    for(auto &sg : segs)
-        need += align_up(sizeof(BatchHeader), 64) + align_up((size_t)(sg.second - sg.first) * sizeof(DrawParams), 64) +
-                3 * align_up((size_t)(sg.second - sg.first + 1) * 4, 64) + 512;
-    if(B.stagePending)
+    return run_segments(ctx, draws, segs, nullptr);
+}
+
+// --------------------------------------------------------------------------
+// Adjoint draws (swgb_draw_adjoint, swgb_draw_adjoint_batch)
+// --------------------------------------------------------------------------
+
+inline bool aligned(const void *p, size_t a) { return ((uintptr_t)p % a) == 0; }
+
+// Validates the adjoint's scope and bakes its parameters.
+swgb_status bake_adjoint(const swgb_pipeline_state *st, const swgb_draw_args *a, const swgb_adjoint_args *g, const DrawParams &D,
+                         AdjParams &A)
+{
+    if(!g) return set_error(SWGB_INVALID_ARG, "null adjoint arguments");
+    if(D.cf == CF_RGBA8) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint needs a float colour attachment");
+    if(D.fs == SWGB_FS_TEX_X_VCOLOR && !D.texFloat) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint needs a float texture");
+    if(D.writeMask != 0xFu) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint needs color_write_mask 0xF");
+    if(a->count > ADJ_TRI_MASK) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint: too many triangles");
+    int over = 0;
+    if(st->blend_enable)
     {
-        if((s = cuda_check(cudaEventSynchronize(B.stageFree), "staging reuse")) != SWGB_OK) return s;
-        B.stagePending = false;
+        over = st->src_color_factor == SWGB_BLEND_ONE && st->dst_color_factor == SWGB_BLEND_ONE_MINUS_SRC_ALPHA &&
+               st->color_blend_op == SWGB_BLEND_OP_ADD && st->src_alpha_factor == SWGB_BLEND_ONE &&
+               st->dst_alpha_factor == SWGB_BLEND_ONE_MINUS_SRC_ALPHA && st->alpha_blend_op == SWGB_BLEND_OP_ADD;
+        if(!over) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint blends: none or premultiplied OVER only");
     }
-    if(need > B.stageCap)
+    if(!g->grad_color || !aligned(g->grad_color, 16) || g->grad_color_pitch_bytes % 16 || g->grad_color_slice_bytes % 16 ||
+       g->grad_color_pitch_bytes < 16u * st->framebuffer_width ||
+       (D.ms > 1 && g->grad_color_slice_bytes < (uint64_t)g->grad_color_pitch_bytes * st->framebuffer_height))
+        return set_error(SWGB_INVALID_ARG, "grad_color: null, not 16-byte aligned, or pitch/slice too small");
+    memset(&A, 0, sizeof(A));
+    A.gradColor = (const uint8_t *)g->grad_color;
+    A.gradPitch = g->grad_color_pitch_bytes;
+    A.gradSlice = g->grad_color_slice_bytes;
+    for(int c = 0; c < 4; c++) A.clear[c] = g->clear_color[c];
+    A.clearDepth = g->clear_depth;
+    A.blendOver = over;
+    if(D.fs == SWGB_FS_TEX_X_VCOLOR)
+        for(int l = 0; l < D.levelCount; l++)
+        {
+            if(g->grad_texels[l] && !aligned(g->grad_texels[l], 16))
+                return set_error(SWGB_INVALID_ARG, "grad_texels: not 16-byte aligned");
+            A.gradTex[l] = g->grad_texels[l];
+        }
+    for(uint32_t i = 0; i < st->attrib_count && i < SWGB_MAX_ATTRIBS; i++)
     {
-        if(B.stage) cudaFreeHost(B.stage);
-        B.stage = nullptr;
-        B.stageCap = 0;
-        if((s = cuda_check(cudaMallocHost((void **)&B.stage, need + need / 4), "batch staging")) != SWGB_OK) return s;
-        B.stageCap = need + need / 4;
+        const swgb_vertex_attrib &at = st->attribs[i];
+        uint8_t *base = (uint8_t *)g->grad_vertices[at.binding];
+        if(!base) continue;
+        if(!aligned(base, 4) || at.offset % 4 || st->bindings[at.binding].stride % 4)
+            return set_error(SWGB_INVALID_ARG, "grad_vertices: not 4-byte aligned");
+        A.gradAttr[i] = base + at.offset;
+        A.gradStride[i] = st->bindings[at.binding].stride;
     }
-    size_t stageOff = 0;
-    for(auto &sg : segs)
-        if((s = enqueue_segment(ctx, draws, sg.first, sg.second, stageOff)) != SWGB_OK) return s;
-    if((s = cuda_check(cudaEventRecord(B.stageFree, ctx->stream), "staging event")) != SWGB_OK) return s;
-    B.stagePending = true;
     return SWGB_OK;
+}
+
+template<int MS>
+swgb_status adjoint_grid(int device, int &blocks)
+{
+    constexpr size_t smem = ADJ_WARPS * sizeof(AdjShared<MS>);
+    swgb_status s;
+    if((s = cuda_check(cudaFuncSetAttribute(k_adjoint<MS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "adjoint smem")) != SWGB_OK ||
+       (s = cuda_check(cudaFuncSetAttribute(k_adjoint_batch<MS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "adjoint smem")) != SWGB_OK)
+        return s;
+    int sms = 0, perSM = 0, perSM1 = 0;
+    if((s = cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "SM count")) != SWGB_OK) return s;
+    if((s = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_adjoint_batch<MS>, ADJ_THREADS, smem), "adjoint occupancy")) != SWGB_OK ||
+       (s = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM1, k_adjoint<MS>, ADJ_THREADS, smem), "adjoint occupancy")) != SWGB_OK)
+        return s;
+    perSM = std::min(perSM, perSM1);
+    blocks = (sms > 0 ? sms : 1) * (perSM > 0 ? perSM : 1);
+    return SWGB_OK;
+}
+
+swgb_status adjoint_init(swgb_ctx *ctx)
+{
+    if(ctx->adjAttr) return SWGB_OK;
+    swgb_status s;
+    if((s = adjoint_grid<1>(ctx->device, ctx->adjBlocks[0])) != SWGB_OK || (s = adjoint_grid<4>(ctx->device, ctx->adjBlocks[1])) != SWGB_OK)
+        return s;
+    const size_t warps = (size_t)std::max(ctx->adjBlocks[0], ctx->adjBlocks[1]) * ADJ_WARPS;
+    if((s = cuda_check(cudaMalloc((void **)&ctx->adjScratch, warps * ADJ_REGION_BYTES), "adjoint scratch")) != SWGB_OK) return s;
+    ctx->adjAttr = true;
+    return SWGB_OK;
+}
+
+swgb_status draw_adjoint(swgb_ctx *ctx, const swgb_pipeline_state *st, const swgb_draw_args *a, const swgb_adjoint_args *g)
+{
+    DrawParams D;
+    swgb_status s = bake(st, a, D);
+    if(s != SWGB_OK) return s;
+    AdjParams A;
+    if((s = bake_adjoint(st, a, g, D, A)) != SWGB_OK) return s;
+    if(D.count == 0) return SWGB_OK;
+    if((s = adjoint_init(ctx)) != SWGB_OK) return s;
+    if((s = prepare_scratch(ctx, D)) != SWGB_OK) return s;
+    const uint32_t nv = D.vertexCount;
+    timed_launch(ctx, SWGB_KERNEL_VERTEX, [&] { k_vertex<<<(nv + 255) / 256, 256, 0, ctx->stream>>>(D, nv); });
+    const uint32_t setupBlocks = (uint32_t)((D.count + SETUP_THREADS - 1) / SETUP_THREADS);
+    timed_launch(ctx, SWGB_KERNEL_SETUP, [&] { k_setup<<<setupBlocks, SETUP_THREADS, 0, ctx->stream>>>(D); });
+    if(D.binsX > 0 && D.binsY > 0)
+    {
+        const int v = D.ms > 1 ? 1 : 0;
+        uint32_t blocks = (uint32_t)((D.binsX * D.binsY + ADJ_WARPS - 1) / ADJ_WARPS);
+        if(blocks > (uint32_t)ctx->adjBlocks[v]) blocks = (uint32_t)ctx->adjBlocks[v];
+        timed_launch(ctx, SWGB_KERNEL_ADJOINT, [&] {
+            if(v) k_adjoint<4><<<blocks, ADJ_THREADS, ADJ_WARPS * sizeof(AdjShared<4>), ctx->stream>>>(D, A, ctx->adjScratch);
+            else k_adjoint<1><<<blocks, ADJ_THREADS, ADJ_WARPS * sizeof(AdjShared<1>), ctx->stream>>>(D, A, ctx->adjScratch);
+        });
+    }
+    return cuda_check(cudaGetLastError(), "adjoint launch");
+}
+
+swgb_status draw_adjoint_batch(swgb_ctx *ctx, const swgb_pipeline_state *states, const swgb_draw_args *args,
+                               const swgb_adjoint_args *adjs, uint32_t n)
+{
+    std::vector<DrawParams> draws;
+    std::vector<AdjParams> adj;
+    draws.reserve(n);
+    adj.reserve(n);
+    for(uint32_t i = 0; i < n; i++)
+    {
+        DrawParams D;
+        swgb_status s = bake(&states[i], &args[i], D);
+        if(s != SWGB_OK) return s;
+        AdjParams A;
+        if((s = bake_adjoint(&states[i], &args[i], &adjs[i], D, A)) != SWGB_OK) return s;
+        if(args[i].count == 0) continue;
+        draws.push_back(D);
+        adj.push_back(A);
+    }
+    if(draws.empty()) return SWGB_OK;
+    swgb_status s;
+    if((s = batch_init(ctx)) != SWGB_OK || (s = adjoint_init(ctx)) != SWGB_OK) return s;
+    // adjoints only read attachments and add to gradients, so draws never
+    // conflict; segments split by sample count only
+    std::vector<std::pair<uint32_t, uint32_t>> segs;
+    uint32_t start = 0;
+    for(uint32_t i = 1; i <= (uint32_t)draws.size(); i++)
+        if(i == (uint32_t)draws.size() || (draws[i].ms > 1) != (draws[start].ms > 1))
+        {
+            segs.push_back({start, i});
+            start = i;
+        }
+    return run_segments(ctx, draws, segs, adj.data());
 }
 
 // --------------------------------------------------------------------------
@@ -2779,13 +2986,13 @@ swgb_status swgb_ctx_create(int device, void *stream, swgb_ctx **out)
     if((s = cuda_check(cudaMalloc((void **)&c->polyCount, sizeof(uint32_t)), "polyCount")) != SWGB_OK ||
        (s = cuda_check(cudaMalloc((void **)&c->spanCount, sizeof(unsigned long long)), "spanCount")) != SWGB_OK ||
        (s = cuda_check(cudaMalloc((void **)&c->binQueue, sizeof(unsigned int)), "binQueue")) != SWGB_OK ||
-       (s = cuda_check(cudaMalloc((void **)&c->counters, 8 * sizeof(unsigned long long)), "counters")) != SWGB_OK ||
+       (s = cuda_check(cudaMalloc((void **)&c->counters, CTX_COUNTERS * sizeof(unsigned long long)), "counters")) != SWGB_OK ||
        (s = cuda_check(cudaMalloc((void **)&c->error, sizeof(int)), "error")) != SWGB_OK)
     {
         swgb_ctx_destroy(c);
         return s;
     }
-    cudaMemset(c->counters, 0, 8 * sizeof(unsigned long long));
+    cudaMemset(c->counters, 0, CTX_COUNTERS * sizeof(unsigned long long));
     cudaMemset(c->error, 0, sizeof(int));
     cudaMemset(c->polyCount, 0, sizeof(uint32_t));
     *out = c;
@@ -2821,6 +3028,7 @@ swgb_status swgb_ctx_destroy(swgb_ctx *c)
     delete c->evPairs;
     delete c->evFree;
     batch_free(c->batch);
+    cudaFree(c->adjScratch);
     delete c;
     return SWGB_OK;
 }
@@ -2909,6 +3117,22 @@ swgb_status swgb_draw_batch(swgb_ctx *ctx, const swgb_pipeline_state *states, co
     return draw_batch(ctx, states, args, n);
 }
 
+swgb_status swgb_draw_adjoint(swgb_ctx *ctx, const swgb_pipeline_state *state, const swgb_draw_args *args, const swgb_adjoint_args *adj)
+{
+    if(!ctx || !state || !args || !adj) return set_error(SWGB_INVALID_ARG, "null argument");
+    cudaSetDevice(ctx->device);
+    return draw_adjoint(ctx, state, args, adj);
+}
+
+swgb_status swgb_draw_adjoint_batch(swgb_ctx *ctx, const swgb_pipeline_state *states, const swgb_draw_args *args,
+                                    const swgb_adjoint_args *adjs, uint32_t n)
+{
+    if(!ctx || (n && (!states || !args || !adjs))) return set_error(SWGB_INVALID_ARG, "null argument");
+    if(n == 0) return SWGB_OK;
+    cudaSetDevice(ctx->device);
+    return draw_adjoint_batch(ctx, states, args, adjs, n);
+}
+
 swgb_status swgb_sync(swgb_ctx *ctx)
 {
     if(!ctx) return SWGB_INVALID_ARG;
@@ -2930,7 +3154,7 @@ swgb_status swgb_get_counters(swgb_ctx *ctx, swgb_counters *out)
     if(!ctx || !out) return SWGB_INVALID_ARG;
     swgb_status s = cuda_check(cudaStreamSynchronize(ctx->stream), "stream sync");
     if(s != SWGB_OK) return s;
-    unsigned long long h[8];
+    unsigned long long h[CTX_COUNTERS];
     if((s = cuda_check(cudaMemcpy(h, ctx->counters, sizeof(h), cudaMemcpyDeviceToHost), "counters")) != SWGB_OK) return s;
     out->triangles_in = h[0];
     out->triangles_rejected = h[1];
@@ -2940,13 +3164,17 @@ swgb_status swgb_get_counters(swgb_ctx *ctx, swgb_counters *out)
     out->fragments_tested = h[5];
     out->fragments_passed = h[6];
     out->texture_levels_mask = h[7];
+    out->adjoint_fragments = h[CNT_ADJ_FRAGMENTS];
+    out->adjoint_depth_mismatch = h[CNT_ADJ_MISMATCH];
+    out->adjoint_list_overflow = h[CNT_ADJ_OVERFLOW];
+    out->reserved = 0;
     return SWGB_OK;
 }
 
 swgb_status swgb_reset_counters(swgb_ctx *ctx)
 {
     if(!ctx) return SWGB_INVALID_ARG;
-    return cuda_check(cudaMemsetAsync(ctx->counters, 0, 8 * sizeof(unsigned long long), ctx->stream), "counters reset");
+    return cuda_check(cudaMemsetAsync(ctx->counters, 0, CTX_COUNTERS * sizeof(unsigned long long), ctx->stream), "counters reset");
 }
 
 uint64_t swgb_launch_count(swgb_ctx *ctx) { return ctx ? ctx->launches : 0; }

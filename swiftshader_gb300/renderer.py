@@ -44,6 +44,17 @@ class Renderer:
         A = args if isinstance(args, C.Array) else (abi.DrawArgs * n)(*args)
         check(self._L.swgb_draw_batch(self._ctx, S, A, n), "swgb_draw_batch")
 
+    def draw_adjoint(self, state, args, adj):
+        """Adjoint of one draw (swgb_draw_adjoint); adj is an abi.AdjointArgs."""
+        check(self._L.swgb_draw_adjoint(self._ctx, C.byref(state), C.byref(args), C.byref(adj)), "swgb_draw_adjoint")
+
+    def draw_adjoint_batch(self, states, args, adjs):
+        n = len(states)
+        S = states if isinstance(states, C.Array) else (abi.PipelineState * n)(*states)
+        A = args if isinstance(args, C.Array) else (abi.DrawArgs * n)(*args)
+        G = adjs if isinstance(adjs, C.Array) else (abi.AdjointArgs * n)(*adjs)
+        check(self._L.swgb_draw_adjoint_batch(self._ctx, S, A, G, n), "swgb_draw_adjoint_batch")
+
     def synchronize(self):
         check(self._L.swgb_sync(self._ctx), "swgb_sync")
 
@@ -61,7 +72,7 @@ class Renderer:
     def set_kernel_timing(self, enable):
         check(self._L.swgb_set_kernel_timing(self._ctx, 1 if enable else 0), "swgb_set_kernel_timing")
 
-    KERNEL_NAMES = ("vertex", "setup", "raster", "batch")
+    KERNEL_NAMES = ("vertex", "setup", "raster", "batch", "adjoint")
 
     def kernel_times(self):
         """{kernel: (total ms, launches)} since the last call (synchronises)."""

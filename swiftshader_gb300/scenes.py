@@ -185,12 +185,21 @@ def scene_textured_small(n_tris=200, width=128, height=96, tex_size=64, mip=True
 def uv_sphere(rng, seg_u, seg_v, radius=1.0, noise_sigma=0.0):
     """Vertices and uint32 indices of a uv-sphere with seg_u x seg_v quads
     (2 triangles each, the pole rows degenerate), optional radial Gaussian
-    displacement, uv = (u, v) in [0,1]^2, RGBA uniform in [0,1]."""
+    displacement per point of the sphere, uv = (u, v) in [0,1]^2, RGBA
+    uniform in [0,1]."""
     nu, nv = seg_u + 1, seg_v + 1
     th = np.linspace(0.0, 2.0 * math.pi, nu)
     ph = np.linspace(0.0, math.pi, nv)
     TH, PH = np.meshgrid(th, ph)
-    r = radius * (1.0 + (rng.normal(0.0, noise_sigma, TH.shape) if noise_sigma > 0 else 0.0))
+    noise = 0.0
+    if noise_sigma > 0:
+        # one displacement per point of the sphere: the seam column repeats
+        # column 0 and each pole row is one point, so the mesh stays closed
+        noise = rng.normal(0.0, noise_sigma, TH.shape)
+        noise[:, -1] = noise[:, 0]
+        noise[0, :] = noise[0, 0]
+        noise[-1, :] = noise[-1, 0]
+    r = radius * (1.0 + noise)
     x = r * np.sin(PH) * np.cos(TH)
     y = r * np.cos(PH)
     z = r * np.sin(PH) * np.sin(TH)

@@ -21,6 +21,7 @@ STRUCTS = {
     "swgb_pipeline_state": abi.PipelineState,
     "swgb_draw_args": abi.DrawArgs,
     "swgb_counters": abi.Counters,
+    "swgb_adjoint_args": abi.AdjointArgs,
 }
 
 
@@ -69,7 +70,7 @@ def test_library_loads_and_exports_all_symbols(built_lib):
     for name in _lib.EXPORTS:
         assert name in exported, name
     L = _lib.load(built_lib)
-    assert L.swgb_abi_version() == 1
+    assert L.swgb_abi_version() == 2
 
 
 def test_host_side_errors_without_device(built_lib):
