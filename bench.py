@@ -3,18 +3,25 @@
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload heightfield|small|batch]
 
 One step = one frame: clear colour + depth, then one draw of the whole scene
-through the C-ABI (swgb_draw).  The default line also carries "batched": the
-4096-draw atlas workload with triangle counts log-uniform in [16, 1024] (a
-reduced-size sample of the batch workload, stated in its config), one
-swgb_draw_batch call per step against the same draws issued one swgb_draw
-each.  --workload batch measures the full 4096-draw atlas workload
-(log-uniform [16, 65536] triangles) as the headline line: one step = clear the
-atlas + one swgb_draw_batch of all draws.  Inputs are resident in HBM for ``value``; the L2
-(129 MB) is flushed by writing a 256 MiB buffer before every timed step,
+through the C-ABI (swgb_draw).  Inputs are resident in HBM for ``value``; the
+L2 (129 MB) is flushed by writing a 256 MiB buffer before every timed step,
 outside the step's CUDA events.  ``e2e`` is the same metric through the same
 public call with host buffers: every step copies the scene (vertices, indices,
 texture chain) host->device from pinned memory and reads the colour + depth
 attachments back, inside the timed region.
+
+The default line also carries
+  * "batched": the 4096-draw atlas workload with triangle counts log-uniform
+    in [16, 1024] (a reduced-size sample of the batch workload, stated in its
+    config), one swgb_draw_batch call per step against the same draws issued
+    one swgb_draw each;
+  * "adjoint": forward and adjoint times (and their ratio) of the two adjoint
+    workloads at full size -- the 20k-triangle sphere at 512^2 RGBA32F and 256
+    views of the 100k-triangle noisy sphere at 512^2 4x MSAA -- through the
+    calls the autograd function makes.
+--workload batch measures the full 4096-draw atlas workload (log-uniform
+[16, 65536] triangles) as the headline line: one step = clear the atlas + one
+swgb_draw_batch of all draws.
 
 Multi-GPU (torchrun, N > 1): the frame does not shard, so every rank renders
 its own replica ("replicas only"); value = all ranks' fragments / max time.
@@ -265,6 +272,11 @@ def run_ours(args):
         batched["config"]["note"] = ("reduced-size sample of the batch workload (triangles log-uniform in "
                                      "[16, 1024] instead of [16, 65536]); --workload batch runs the full one")
 
+    adjoint_lines = None
+    if args.workload == "heightfield" and not args.no_adjoint:
+        adjoint_lines = {"sphere": measure_adjoint(r, stream, flush, dev, "sphere"),
+                         "views": measure_adjoint(r, stream, flush, dev, "views", steps=2, warmup=1)}
+
     # max over ranks
     ms_per_step, e2e_ms = max_over_ranks([ms_per_step, e2e_ms], dev)
 
@@ -320,6 +332,8 @@ def run_ours(args):
             pass
     if batched is not None:
         line["batched"] = batched
+    if adjoint_lines is not None:
+        line["adjoint"] = adjoint_lines
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args, scene, bounded_s=args.cpu_seconds)
     print(json.dumps(line), flush=True)
@@ -389,6 +403,53 @@ def measure_batch(r, stream, flush, params, steps, warmup, per_draw_steps, dev):
         "gpu_launches_per_step": launches / steps, "steps": steps, "per_draw_steps": per_draw_steps,
         "counters_per_step": per_step,
     }
+
+
+def measure_adjoint(r, stream, flush, dev, workload, steps=3, warmup=2):
+    """Forward and adjoint times of one adjoint workload, through the same
+    DrawSet calls the autograd function makes (no torch autograd overhead):
+    forward = clear + draw(s); adjoint = zero gradients + adjoint draw(s) for
+    a fixed dL/dcolour."""
+    import numpy as np
+    import torch
+    from swiftshader_gb300 import abi, adjoint, scenes
+    if workload == "sphere":
+        scene_list = [scenes.scene_sphere_fp32()]
+        desc = ("20k-triangle uv-sphere (100x100 segments), 512^2 RGBA32F, 1024^2 RGBA32F texture bilinear "
+                "CLAMP, colour = texel x vertex colour, depth LESS; L2 loss gradient")
+    else:
+        rng = np.random.Generator(np.random.PCG64(0x53570004))
+        mesh = scenes.uv_sphere(rng, 250, 200, noise_sigma=0.02)
+        levels = scenes.float_mip_chain(rng.uniform(0.0, 1.0, (2048, 2048, 4)), np.float16)
+        scene_list = [scenes.scene_sphere_views(v, mesh=mesh, levels=levels) for v in range(256)]
+        for sc in scene_list:
+            sc.samples = 4
+        desc = ("256 views of a 100k-triangle uv-sphere with radial N(0, 0.02^2) noise, cameras on a radius-3 "
+                "sphere, 512^2 4x MSAA RGBA16F, 2048^2 RGBA16F mip chain trilinear, premultiplied OVER, depth "
+                "LESS; all views as one batch forward and one batch adjoint")
+    sc0 = scene_list[0]
+    verts = torch.from_numpy(np.ascontiguousarray(sc0.vertices, np.float32)).to(dev)
+    tdt = torch.float16 if sc0.texture_format == abi.FORMAT_R16G16B16A16_SFLOAT else torch.float32
+    tex = [torch.from_numpy(np.ascontiguousarray(l)).to(dev).to(tdt) for l in sc0.texture_levels]
+    ds = adjoint.DrawSet(scene_list, verts, tex)
+    ds.forward(r)
+    torch.cuda.synchronize()
+    g = (2.0 * (ds.colors() - 0.25)).contiguous()  # dL/dcolour of an L2 loss against a grey target
+    for _ in range(warmup):
+        ds.forward(r)
+        ds.adjoint(r, g)
+    r.synchronize()
+    r.reset_counters()
+    tf = time_steps(stream, flush, steps, lambda: ds.forward(r))
+    ta = time_steps(stream, flush, steps, lambda: ds.adjoint(r, g))
+    r.synchronize()
+    cnt = r.counters()
+    mf, ma = sum(tf) / len(tf), sum(ta) / len(ta)
+    return {"config": {"workload": desc, "views": len(scene_list), "triangles_per_view": sc0.tri_count},
+            "forward_ms": round(mf, 3), "adjoint_ms": round(ma, 3), "adjoint_over_forward": round(ma / mf, 3),
+            "adjoint_fragments_per_step": cnt["adjoint_fragments"] // steps,
+            "adjoint_depth_mismatch": cnt["adjoint_depth_mismatch"], "adjoint_list_overflow": cnt["adjoint_list_overflow"],
+            "steps": steps}
 
 
 def run_batch(args):
@@ -590,6 +651,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-vs-per-draw sample")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint / forward timings")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

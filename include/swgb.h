@@ -266,6 +266,13 @@ swgb_status swgb_draw(swgb_ctx *ctx, const swgb_pipeline_state *state, const swg
  * written in the same call. */
 swgb_status swgb_draw_batch(swgb_ctx *ctx, const swgb_pipeline_state *states, const swgb_draw_args *args, uint32_t n);
 
+/* The segments swgb_draw_batch would split these draws into, computed on the
+ * host without a device: *segment_count segments; when segment_first is not
+ * NULL it receives the index (into states/args) of each segment's first draw
+ * (room for n entries).  Draws with count 0 belong to no segment. */
+swgb_status swgb_plan_batch(const swgb_pipeline_state *states, const swgb_draw_args *args, uint32_t n, uint32_t *segment_first,
+                            uint32_t *segment_count);
+
 /* Allocation-free draw.  No counterpart in the reference: it exists for
  * callers of this library that cannot allocate device memory when they draw --
  * code recording into a CUDA stream capture (cudaMalloc is not capturable), a

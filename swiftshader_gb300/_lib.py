@@ -14,7 +14,7 @@ _lib = None
 EXPORTS = ["swgb_abi_version", "swgb_last_error", "swgb_ctx_create", "swgb_ctx_destroy",
            "swgb_ctx_set_stream", "swgb_draw", "swgb_draw_batch", "swgb_sync", "swgb_get_counters",
            "swgb_reset_counters", "swgb_launch_count", "swgb_set_kernel_timing", "swgb_get_kernel_times",
-           "swgb_draw_noalloc", "swgb_draw_adjoint", "swgb_draw_adjoint_batch"]
+           "swgb_draw_noalloc", "swgb_draw_adjoint", "swgb_draw_adjoint_batch", "swgb_plan_batch"]
 
 
 class SwgbError(RuntimeError):
@@ -64,6 +64,9 @@ def load(path=None):
     L.swgb_draw_adjoint_batch.argtypes = [C.c_void_p, C.POINTER(abi.PipelineState), C.POINTER(abi.DrawArgs),
                                           C.POINTER(abi.AdjointArgs), C.c_uint32]
     L.swgb_draw_adjoint_batch.restype = C.c_int
+    L.swgb_plan_batch.argtypes = [C.POINTER(abi.PipelineState), C.POINTER(abi.DrawArgs), C.c_uint32,
+                                  C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+    L.swgb_plan_batch.restype = C.c_int
     if L.swgb_abi_version() != 2:
         raise OSError("libswgb ABI version mismatch")
     _lib = L

@@ -77,6 +77,50 @@ def _check_inputs(vertices, levels):
             raise ValueError("texture levels: float32 CUDA tensors [h, w, 4]")
 
 
+class DrawSet:
+    """Draws of one mesh and texture into one attachment pair per scene (one
+    scene per view), set up once for repeated forward and adjoint calls:
+    ``forward`` clears the attachments and enqueues the draws (one
+    swgb_draw_batch call for several views); ``adjoint`` zeroes the gradient
+    buffers and enqueues swgb_draw_adjoint(_batch) for dL/dcolour
+    ``grad_color`` (float32, [V, (4,) H, W, 4])."""
+
+    def __init__(self, scene_list, vertices, tex_levels):
+        self.vertices = vertices
+        self.tex = tex_levels
+        cache = {}
+        self.views = [_View(s, vertices, tex_levels, cache) for s in scene_list]
+        self.grad_vertices = torch.zeros_like(vertices)
+        self.grad_levels = [torch.zeros(l.shape, dtype=torch.float32, device=l.device) for l in tex_levels]
+
+    def clear(self):
+        for v in self.views:
+            v.color[...] = torch.tensor(v.scene.clear_color, dtype=v.color.dtype, device=v.color.device)
+            v.depth.fill_(v.scene.clear_depth)
+
+    def forward(self, renderer):
+        self.clear()
+        if len(self.views) == 1:
+            renderer.draw(self.views[0].state, self.views[0].args)
+        else:
+            renderer.draw_batch([v.state for v in self.views], [v.args for v in self.views])
+
+    def colors(self):
+        return torch.stack([v.color.float() for v in self.views])
+
+    def adjoint(self, renderer, grad_color):
+        g = grad_color.detach().float().contiguous()
+        self._grad = g  # kept alive until the enqueued adjoint has read it
+        self.grad_vertices.zero_()
+        for l in self.grad_levels:
+            l.zero_()
+        adj = [v.adjoint_args(g[i], self.grad_vertices, self.grad_levels) for i, v in enumerate(self.views)]
+        if len(self.views) == 1:
+            renderer.draw_adjoint(self.views[0].state, self.views[0].args, adj[0])
+        else:
+            renderer.draw_adjoint_batch([v.state for v in self.views], [v.args for v in self.views], adj)
+
+
 class _DrawViews(torch.autograd.Function):
     @staticmethod
     def forward(ctx, renderer, scene_list, vertices, *levels):
@@ -84,31 +128,17 @@ class _DrawViews(torch.autograd.Function):
         renderer.set_stream(torch.cuda.current_stream(vertices.device))  # order with torch's work
         verts = vertices.detach().contiguous()
         tex = [l.detach().to(_texture_dtype(scene_list[0])).contiguous() for l in levels]
-        cache = {}
-        views = [_View(s, verts, tex, cache) for s in scene_list]
-        if len(views) == 1:
-            renderer.draw(views[0].state, views[0].args)
-        else:
-            renderer.draw_batch([v.state for v in views], [v.args for v in views])
-        out = torch.stack([v.color.float() for v in views])
-        ctx.renderer, ctx.views, ctx.keep = renderer, views, (verts, tex)
-        ctx.level_shapes = [l.shape for l in levels]
-        return out
+        ds = DrawSet(scene_list, verts, tex)
+        ds.forward(renderer)
+        ctx.renderer, ctx.drawset = renderer, ds
+        return ds.colors()
 
     @staticmethod
     def backward(ctx, grad_out):
-        views, r = ctx.views, ctx.renderer
-        verts, tex = ctx.keep
-        g = grad_out.detach().float().contiguous()
-        gv = torch.zeros_like(verts)
-        gl = [torch.zeros(s, dtype=torch.float32, device=verts.device) for s in ctx.level_shapes]
-        adj = [v.adjoint_args(g[i], gv, gl) for i, v in enumerate(views)]
-        r.set_stream(torch.cuda.current_stream(verts.device))
-        if len(views) == 1:
-            r.draw_adjoint(views[0].state, views[0].args, adj[0])
-        else:
-            r.draw_adjoint_batch([v.state for v in views], [v.args for v in views], adj)
-        return (None, None, gv) + tuple(gl)
+        ds, r = ctx.drawset, ctx.renderer
+        r.set_stream(torch.cuda.current_stream(ds.vertices.device))
+        ds.adjoint(r, grad_out)
+        return (None, None, ds.grad_vertices) + tuple(ds.grad_levels)
 
 
 def render(renderer, scene, vertices, levels=()):

@@ -2301,7 +2301,7 @@ void plane_rects(uintptr_t base, uintptr_t origin, uint32_t pitch, int64_t x0b, 
     r += k;
     sc -= k * pitch;
     ec -= k * pitch;
-    if(ec - sc >= (int64_t)pitch)
+    if(ec - sc > (int64_t)pitch)  // rows longer than the pitch overlap each other: whole rows
         out.push_back({pitch, r + y0, r + y1 + 1, 0, (int64_t)pitch});
     else if(ec <= (int64_t)pitch)
         out.push_back({pitch, r + y0, r + y1, sc, ec});
@@ -3115,6 +3115,29 @@ swgb_status swgb_draw_batch(swgb_ctx *ctx, const swgb_pipeline_state *states, co
     if(n == 0) return SWGB_OK;
     cudaSetDevice(ctx->device);
     return draw_batch(ctx, states, args, n);
+}
+
+swgb_status swgb_plan_batch(const swgb_pipeline_state *states, const swgb_draw_args *args, uint32_t n, uint32_t *segment_first,
+                            uint32_t *segment_count)
+{
+    if((n && (!states || !args)) || !segment_count) return set_error(SWGB_INVALID_ARG, "null argument");
+    std::vector<DrawParams> draws;
+    std::vector<uint32_t> src;
+    for(uint32_t i = 0; i < n; i++)
+    {
+        if(args[i].count == 0) continue;
+        DrawParams D;
+        swgb_status s = bake(&states[i], &args[i], D);
+        if(s != SWGB_OK) return s;
+        draws.push_back(D);
+        src.push_back(i);
+    }
+    std::vector<std::pair<uint32_t, uint32_t>> segs;
+    if(!draws.empty()) segment_batch(draws, src, states, args, segs);
+    if(segment_first)
+        for(size_t k = 0; k < segs.size(); k++) segment_first[k] = src[segs[k].first];
+    *segment_count = (uint32_t)segs.size();
+    return SWGB_OK;
 }
 
 swgb_status swgb_draw_adjoint(swgb_ctx *ctx, const swgb_pipeline_state *state, const swgb_draw_args *args, const swgb_adjoint_args *adj)
