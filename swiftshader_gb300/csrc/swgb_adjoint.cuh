@@ -28,7 +28,7 @@ constexpr uint32_t ADJ_NO_WRITER = 0xFFFFFFFFu;
 // Blended fragments a warp holds at once (its region of the adjoint
 // scratch); a bin with more is processed in pixel chunks.
 constexpr int ADJ_ENTRIES = 2048;
-constexpr size_t ADJ_REGION_BYTES = (size_t)ADJ_ENTRIES * (4 + 4 + 16 + 16 + 16);
+constexpr size_t ADJ_REGION_BYTES = (size_t)ADJ_ENTRIES * (4 + 4 + 4 + 4 + 16 + 16 + 16);
 
 // Per-draw adjoint parameters, baked on the host from swgb_adjoint_args.
 struct AdjParams {
@@ -41,6 +41,8 @@ struct AdjParams {
     float *gradTex[SWGB_MAX_MIP_LEVELS];   // float RGBA per texel, level pitch
     uint8_t *gradAttr[SWGB_MAX_ATTRIBS];   // binding gradient buffer + attribute offset
     uint32_t gradStride[SWGB_MAX_ATTRIBS];
+    // clip-space ray of pixel centre (px, py): (rx0 + px rxs, ry0 + py rys, 1)
+    double rx0, rxs, ry0, rys;
 };
 
 // A warp's region of the adjoint scratch: one blended fragment per entry,
@@ -48,6 +50,8 @@ struct AdjParams {
 struct AdjRegion {
     uint32_t *tri;   // triangle | sample mask << 28
     uint32_t *pix;   // pixel index in the bin
+    uint32_t *ltri;  // the same, in arrival order (the replay's log)
+    uint32_t *lpix;
     float4 *sc;      // shaded colour
     float4 *ds;      // dL/d(shaded colour)
     float4 *before;  // colour of the sample before the fragment (one sample at a time)
@@ -55,7 +59,9 @@ struct AdjRegion {
     {
         tri = (uint32_t *)base;
         pix = tri + ADJ_ENTRIES;
-        sc = (float4 *)(pix + ADJ_ENTRIES);
+        ltri = pix + ADJ_ENTRIES;
+        lpix = ltri + ADJ_ENTRIES;
+        sc = (float4 *)(lpix + ADJ_ENTRIES);
         ds = sc + ADJ_ENTRIES;
         before = ds + ADJ_ENTRIES;
     }
@@ -75,11 +81,30 @@ struct AdjShared {
     uint32_t off[BIN * BIN + 1];     // blended: first entry of each pixel (prefix of cnt)
     uint16_t cnt[BIN * BIN];         // blended: fragments per pixel
     uint16_t fill[BIN * BIN];        // blended: fragments recorded per pixel
+    uint32_t logCount;               // blended: fragments appended to the region's log
     static constexpr int kSamples = MS;
 };
 
+// A bin's pixels may be split between four warps (quarters of 8x8 pixels,
+// sub = 0..3; sub = -1: the whole bin).  Pixel j of a part, in row order:
+__device__ __forceinline__ bool in_sub(int idx, int sub)
+{
+    return sub < 0 || ((idx & (BIN - 1)) >> 3) + 2 * ((idx / BIN) >> 3) == sub;
+}
+
+__device__ __forceinline__ int sub_pixel(int j, int sub)
+{
+    if(sub < 0) return j;
+    return ((sub >> 1) * 8 + (j >> 3)) * BIN + (sub & 1) * 8 + (j & 7);
+}
+
+__device__ __forceinline__ int sub_pixels(int sub) { return sub < 0 ? BIN * BIN : BIN * BIN / 4; }
+
 // What a replay does with each passing (pixel, triangle, samples).
-enum { REPLAY_WRITERS = 0, REPLAY_COUNT = 1, REPLAY_RECORD = 2 };
+// REPLAY_LOG counts like REPLAY_COUNT and also appends every fragment to the
+// region's log (arrival order keeps each pixel's primitive order) while it
+// fits; REPLAY_RECORD is the fallback that records chunks of pixels.
+enum { REPLAY_WRITERS = 0, REPLAY_COUNT = 1, REPLAY_RECORD = 2, REPLAY_LOG = 3 };
 
 // Replay of one batch of nb <= 32 triangles: coverage per sample (the
 // forward's spans), depth test against the replayed depth in primitive
@@ -87,9 +112,9 @@ enum { REPLAY_WRITERS = 0, REPLAY_COUNT = 1, REPLAY_RECORD = 2 };
 // resolve lowest lane (earliest triangle) first, so per-pixel state needs no
 // atomics.  REPLAY_RECORD stores the fragments of pixels [p0, p1) at
 // S.off[idx] - S.off[p0] + (running count) of the region.
-template<int MS, int MODE>
-__device__ __noinline__ void adjoint_replay(const DrawParams &D, AdjShared<MS> &S, AdjRegion R, int nb, int bx0, int by0,
-                                            int p0, int p1, unsigned long long &nOverflow)
+template<int MS>
+__device__ __noinline__ void adjoint_replay(const DrawParams &D, AdjShared<MS> &S, AdjRegion R, int MODE, int nb, int bx0,
+                                            int by0, int p0, int p1, int sub, unsigned long long &nOverflow)
 {
     const int lane = threadIdx.x & 31;
     int cnt = 0;
@@ -187,8 +212,21 @@ __device__ __noinline__ void adjoint_replay(const DrawParams &D, AdjShared<MS> &
                         for(int q = 0; q < MS; q++)
                             if(m >> q & 1) S.writer[q][idx] = tri;
                     }
-                    else if(MODE == REPLAY_COUNT)
+                    else if(!in_sub(idx, sub))
+                        continue;
+                    else if(MODE == REPLAY_COUNT || MODE == REPLAY_LOG)
+                    {
                         S.cnt[idx] = (uint16_t)min((int)S.cnt[idx] + 1, 0xFFFF);
+                        if(MODE == REPLAY_LOG)
+                        {
+                            const uint32_t pos = atomicAdd(&S.logCount, 1u);
+                            if(pos < (uint32_t)ADJ_ENTRIES)
+                            {
+                                R.ltri[pos] = tri | (m << 28);
+                                R.lpix[pos] = (uint32_t)idx;
+                            }
+                        }
+                    }
                     else if(idx >= p0 && idx < p1)
                     {
                         const uint32_t pos = S.off[idx] - base + S.fill[idx];
@@ -224,10 +262,11 @@ __device__ __noinline__ void adjoint_replay(const DrawParams &D, AdjShared<MS> &
 struct AdjTri {
     uint32_t slot[3];
     double3 q[3];
+    double2 proj[3];  // (x / w, y / w); 0 when w = 0
     float var[3][MAXV];
 };
 
-__device__ __forceinline__ void adj_load_tri(const DrawParams &D, uint32_t t, AdjTri &T)
+__device__ __noinline__ void adj_load_tri(const DrawParams &D, uint32_t t, AdjTri &T)
 {
     if(D.indexType == SWGB_INDEX_TYPE_NONE)
     {
@@ -240,17 +279,12 @@ __device__ __forceinline__ void adj_load_tri(const DrawParams &D, uint32_t t, Ad
 #pragma unroll
     for(int i = 0; i < 3; i++)
     {
-        // clip (x, y, w) = MVP p in fp64 from the vertex buffer: the forward's
-        // fp32 clip coordinates would move the position gradient by ~1e-4
-        const uint32_t index = (D.indexType == SWGB_INDEX_TYPE_NONE ? D.firstVertex + T.slot[i] : T.slot[i]) + (uint32_t)D.baseVertex;
-        float p[4];
-        read_attrib(D, 0, index, p);
-        double c[4];
-#pragma unroll
-        for(int row = 0; row < 4; row++)
-            c[row] = (double)D.mvp[row] * p[0] + (double)D.mvp[4 + row] * p[1] + (double)D.mvp[8 + row] * p[2] +
-                     (double)D.mvp[12 + row] * p[3];
-        T.q[i] = make_double3(c[0], c[1], c[3]);
+        // clip (x, y, w) = MVP p and its projection, fp64, from the vertex
+        // stage: the forward's fp32 clip coordinates would move the position
+        // gradient by ~1e-4
+        const double *c = D.ptv64 + (size_t)T.slot[i] * 6;
+        T.q[i] = make_double3(c[0], c[1], c[2]);
+        T.proj[i] = make_double2(c[3], c[4]);
         const float4 a = D.ptv[(size_t)T.slot[i] * 4 + 2], b = D.ptv[(size_t)T.slot[i] * 4 + 3];
         T.var[i][0] = a.y; T.var[i][1] = a.z; T.var[i][2] = a.w;
         T.var[i][3] = b.x; T.var[i][4] = b.y; T.var[i][5] = b.z; T.var[i][6] = b.w;
@@ -267,10 +301,11 @@ __device__ __forceinline__ double dot3(double3 a, double3 b) { return a.x * b.x 
 __device__ __forceinline__ double3 sub3(double3 a, double3 b) { return make_double3(a.x - b.x, a.y - b.y, a.z - b.z); }
 
 // Clip-space ray of the centre of pixel (px, py): the sample point of pixel
-// px is X = 256 px in the fixed-point frame X = X0xF + x_ndc * WxF.
-__device__ __forceinline__ double3 pixel_ray(const DrawParams &D, int px, int py)
+// px is X = 256 px in the fixed-point frame X = X0xF + x_ndc * WxF, so
+// x_ndc = px * 256 / WxF - X0xF / WxF (the two constants baked in AdjParams).
+__device__ __forceinline__ double3 pixel_ray(const AdjParams &A, int px, int py)
 {
-    return make_double3((256.0 * px - (double)D.X0xF) / (double)D.WxF, (256.0 * py - (double)D.Y0xF) / (double)D.HxF, 1.0);
+    return make_double3(fma((double)px, A.rxs, A.rx0), fma((double)py, A.rys, A.ry0), 1.0);
 }
 
 // address_float in fp64 with its slope: x0, x1, the filter fraction f and
@@ -340,8 +375,8 @@ __device__ __forceinline__ void grad_texel(float *g, int32_t index, float w, con
 // The filter at (u, v) with the level of detail fixed: the filtered texel,
 // its derivatives by u and v, and (when gt != nullptr) the texel gradients
 // gt * filter weight accumulated into the level gradients.
-__device__ void adj_filter(const DrawParams &D, const AdjParams &A, double u, double v, float lod, const float *gt, float4 &tex,
-                           float4 &dtdu, float4 &dtdv)
+__device__ __noinline__ void adj_filter(const DrawParams &D, const AdjParams &A, double u, double v, float lod, const float *gt,
+                                        float4 &tex, float4 &dtdu, float4 &dtdv)
 {
     tex = dtdu = dtdv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const int levels = D.mipLinear ? 2 : 1;
@@ -397,18 +432,14 @@ struct AdjInterp {
     bool ok;
 };
 
-__device__ __forceinline__ void adj_interp(const DrawParams &D, const AdjTri &T, int px, int py, AdjInterp &I)
+__device__ __noinline__ void adj_interp(const DrawParams &D, const AdjParams &A, const AdjTri &T, int px, int py, AdjInterp &I)
 {
     I.K[0] = cross3(T.q[1], sub3(T.q[2], T.q[1]));
     I.K[1] = cross3(T.q[2], sub3(T.q[0], T.q[2]));
     I.K[2] = cross3(T.q[0], sub3(T.q[1], T.q[0]));
-    I.r = pixel_ray(D, px, py);
+    I.r = pixel_ray(A, px, py);
 #pragma unroll
-    for(int j = 0; j < 3; j++)
-    {
-        const double w = T.q[j].z;
-        I.d[j] = w != 0.0 ? make_double3(I.r.x - T.q[j].x / w, I.r.y - T.q[j].y / w, 0.0) : I.r;
-    }
+    for(int j = 0; j < 3; j++) I.d[j] = make_double3(I.r.x - T.proj[j].x, I.r.y - T.proj[j].y, T.q[j].z != 0.0 ? 0.0 : 1.0);
     double uu[3];
 #pragma unroll
     for(int i = 0; i < 3; i++) uu[i] = dot3(I.d[(i + 1) % 3], I.K[i]);
@@ -419,25 +450,32 @@ __device__ __forceinline__ void adj_interp(const DrawParams &D, const AdjTri &T,
     for(int i = 0; i < 3; i++) I.b[i] = uu[i] * I.invU;
 #pragma unroll
     for(int k = 0; k < MAXV; k++) I.val[k] = I.b[0] * T.var[0][k] + I.b[1] * T.var[1][k] + I.b[2] * T.var[2][k];
-    I.lod = 0.0f;
-    if(D.fs == SWGB_FS_TEX_X_VCOLOR && I.ok)
+    I.lod = D.minLod;
+    if(D.fs == SWGB_FS_TEX_X_VCOLOR && I.ok && D.minLod != D.maxLod)
     {
-        // level of detail from lanes 0, 1, 2 of the pixel's quad, as the forward
+        // level of detail from lanes 0, 1, 2 of the pixel's quad, as the
+        // forward, in fp32 (it is held constant; only its value is used)
         const int qx = px & ~1, qy = py & ~1;
+        const float3 K[3] = {make_float3((float)I.K[0].x, (float)I.K[0].y, (float)I.K[0].z),
+                             make_float3((float)I.K[1].x, (float)I.K[1].y, (float)I.K[1].z),
+                             make_float3((float)I.K[2].x, (float)I.K[2].y, (float)I.K[2].z)};
         float lu[4], lv[4];
 #pragma unroll
         for(int j = 0; j < 3; j++)
         {
-            const double3 r = pixel_ray(D, qx + (j & 1), qy + (j >> 1));
-            double w[3], s = 0.0;
+            // w_i = d_k . K_i with d_k the lane's offset from vertex k's projection
+            const double3 rd = pixel_ray(A, qx + (j & 1), qy + (j >> 1));
+            float w[3];
 #pragma unroll
             for(int i = 0; i < 3; i++)
             {
-                w[i] = dot3(r, I.K[i]);
-                s += w[i];
+                const int k = (i + 1) % 3;
+                const float dx = (float)(rd.x - T.proj[k].x), dy = (float)(rd.y - T.proj[k].y);
+                w[i] = dx * K[i].x + dy * K[i].y + (T.q[k].z != 0.0 ? 0.0f : K[i].z);
             }
-            lu[j] = (float)((w[0] * T.var[0][4] + w[1] * T.var[1][4] + w[2] * T.var[2][4]) / s);
-            lv[j] = (float)((w[0] * T.var[0][5] + w[1] * T.var[1][5] + w[2] * T.var[2][5]) / s);
+            const float is = 1.0f / (w[0] + w[1] + w[2]);
+            lu[j] = (w[0] * T.var[0][4] + w[1] * T.var[1][4] + w[2] * T.var[2][4]) * is;
+            lv[j] = (w[0] * T.var[0][5] + w[1] * T.var[1][5] + w[2] * T.var[2][5]) * is;
         }
         lu[3] = lu[0];
         lv[3] = lv[0];
@@ -446,10 +484,10 @@ __device__ __forceinline__ void adj_interp(const DrawParams &D, const AdjTri &T,
 }
 
 // Forward colour of triangle T at pixel (px, py) under the model.
-__device__ __forceinline__ float4 adj_shade(const DrawParams &D, const AdjParams &A, const AdjTri &T, int px, int py)
+__device__ __noinline__ float4 adj_shade(const DrawParams &D, const AdjParams &A, const AdjTri &T, int px, int py)
 {
     AdjInterp I;
-    adj_interp(D, T, px, py, I);
+    adj_interp(D, A, T, px, py, I);
     float4 c = make_float4((float)I.val[0], (float)I.val[1], (float)I.val[2], (float)I.val[3]);
     if(D.fs == SWGB_FS_TEX_X_VCOLOR && I.ok)
     {
@@ -469,10 +507,10 @@ __device__ __forceinline__ void grad_attr(const AdjParams &A, int a, uint32_t in
 // gS: texel gradients, then dL/d(varyings) and dL/d(barycentrics), then
 // dL/d(clip x, y, w) of the three vertices through b_i = u_i / U, and
 // dL/d(position) = MVP^T dL/d(clip).
-__device__ void adj_shade_grad(const DrawParams &D, const AdjParams &A, const AdjTri &T, int px, int py, float4 gS4)
+__device__ __noinline__ void adj_shade_grad(const DrawParams &D, const AdjParams &A, const AdjTri &T, int px, int py, float4 gS4)
 {
     AdjInterp I;
-    adj_interp(D, T, px, py, I);
+    adj_interp(D, A, T, px, py, I);
     if(!I.ok) return;
     const float gS[4] = {gS4.x, gS4.y, gS4.z, gS4.w};
     // dL/d(varying k) of the pixel; varyings 0-3 colour, 4-5 texture coordinates
@@ -515,8 +553,9 @@ __device__ void adj_shade_grad(const DrawParams &D, const AdjParams &A, const Ad
     {
         const uint32_t index = (D.indexType == SWGB_INDEX_TYPE_NONE ? D.firstVertex + T.slot[i] : T.slot[i]) + (uint32_t)D.baseVertex;
         // position: clip = MVP p (column-major), so dL/dp_c = sum_r MVP[r][c] dL/dclip_r; z gets none
+        const float gx = (float)gq[i].x, gy = (float)gq[i].y, gw = (float)gq[i].z;
         for(int c = 0; c < (int)D.vcomp[0]; c++)
-            grad_attr(A, 0, index, c, (float)(D.mvp[4 * c] * gq[i].x + D.mvp[4 * c + 1] * gq[i].y + D.mvp[4 * c + 3] * gq[i].z));
+            grad_attr(A, 0, index, c, D.mvp[4 * c] * gx + D.mvp[4 * c + 1] * gy + D.mvp[4 * c + 3] * gw);
         int k = 0;
         for(int a = 1; a < D.nattr; a++)
             for(int c = 0; c < (int)D.vcomp[a] && k < MAXV; c++, k++)
@@ -530,35 +569,63 @@ __device__ __forceinline__ float4 grad_color_at(const AdjParams &A, int q, int p
 }
 
 // Not blended: each sample's colour is its last writer's shaded colour, so a
-// writer of several samples takes the sum of their gradients.
+// writer of several samples takes the sum of their gradients.  The (pixel,
+// writer, samples) entries are gathered into the region first, then shaded
+// with lanes over entries (a pixel has up to MS of them).
 template<int MS>
-__device__ void adjoint_pixels_writers(const DrawParams &D, const AdjParams &A, AdjShared<MS> &S, int bx0, int by0,
-                                       unsigned long long &nFrag)
+__device__ void adjoint_pixels_writers(const DrawParams &D, const AdjParams &A, AdjShared<MS> &S, AdjRegion R, int bx0, int by0,
+                                       int sub, unsigned long long &nFrag)
 {
     const int lane = threadIdx.x & 31;
-    for(int idx = lane; idx < BIN * BIN; idx += 32)
+    int nE = 0;  // warp-uniform
+    for(int j0 = 0; j0 < sub_pixels(sub); j0 += 32)
     {
-        const int px = bx0 + (idx % BIN), py = by0 + idx / BIN;
-#pragma unroll 1
+        const int idx = sub_pixel(j0 + lane, sub);
+        uint32_t ent[MS];
+        int ne = 0;
+#pragma unroll
         for(int q = 0; q < MS; q++)
         {
             const uint32_t w = S.writer[q][idx];
-            if(w == ADJ_NO_WRITER) continue;
-            bool first = true;
+            bool first = w != ADJ_NO_WRITER;
+#pragma unroll
             for(int p = 0; p < q; p++) first = first && S.writer[p][idx] != w;
             if(!first) continue;
-            float4 g = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            uint32_t m = 0;
+#pragma unroll
             for(int p = q; p < MS; p++)
-                if(S.writer[p][idx] == w)
-                {
-                    const float4 G = grad_color_at(A, p, px, py);
-                    g = make_float4(g.x + G.x, g.y + G.y, g.z + G.z, g.w + G.w);
-                }
-            AdjTri T;
-            adj_load_tri(D, w, T);
-            adj_shade_grad(D, A, T, px, py, g);
-            nFrag++;
+                if(S.writer[p][idx] == w) m |= 1u << p;
+            ent[ne++] = w | (m << 28);
         }
+        const int incl = warp_incl_scan(ne, lane);
+        const int base = nE + incl - ne;
+#pragma unroll
+        for(int k = 0; k < MS; k++)
+            if(k < ne)
+            {
+                R.tri[base + k] = ent[k];
+                R.pix[base + k] = (uint32_t)idx;
+            }
+        nE += __shfl_sync(0xFFFFFFFFu, incl, 31);
+    }
+    __syncwarp();
+    for(int e = lane; e < nE; e += 32)
+    {
+        const uint32_t v = R.tri[e];
+        const int idx = (int)R.pix[e];
+        const int px = bx0 + (idx % BIN), py = by0 + idx / BIN;
+        float4 g = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+#pragma unroll
+        for(int q = 0; q < MS; q++)
+            if(v >> (28 + q) & 1)
+            {
+                const float4 G = grad_color_at(A, q, px, py);
+                g = make_float4(g.x + G.x, g.y + G.y, g.z + G.z, g.w + G.w);
+            }
+        AdjTri T;
+        adj_load_tri(D, v & ADJ_TRI_MASK, T);
+        adj_shade_grad(D, A, T, px, py, g);
+        nFrag++;
     }
     __syncwarp();
 }
@@ -648,7 +715,7 @@ struct AdjCount {
 // the saved depth, then the pixels.
 template<int MS>
 __device__ __forceinline__ void adjoint_bin(const DrawParams &D, const AdjParams &A, AdjShared<MS> &S, AdjRegion R, int bin,
-                                            AdjCount &n)
+                                            int sub, AdjCount &n)
 {
     const int lane = threadIdx.x & 31;
     const int bx0 = D.binX0 + (bin % D.binsX) * BIN;
@@ -661,14 +728,16 @@ __device__ __forceinline__ void adjoint_bin(const DrawParams &D, const AdjParams
         for(int q = 0; q < MS; q++) S.writer[q][i] = ADJ_NO_WRITER;
         S.cnt[i] = 0;
     }
+    if(lane == 0) S.logCount = 0;
     __syncwarp();
     if(over)
-        walk_bin(D, S, bx0, by0, [&](int nb) { adjoint_replay<MS, REPLAY_COUNT>(D, S, R, nb, bx0, by0, 0, 0, n.overflow); });
+        walk_bin(D, S, bx0, by0, [&](int nb) { adjoint_replay<MS>(D, S, R, REPLAY_LOG, nb, bx0, by0, 0, 0, sub, n.overflow); });
     else
-        walk_bin(D, S, bx0, by0, [&](int nb) { adjoint_replay<MS, REPLAY_WRITERS>(D, S, R, nb, bx0, by0, 0, 0, n.overflow); });
+        walk_bin(D, S, bx0, by0, [&](int nb) { adjoint_replay<MS>(D, S, R, REPLAY_WRITERS, nb, bx0, by0, 0, 0, sub, n.overflow); });
     // the replay must end where the draw ended
-    for(int idx = lane; idx < BIN * BIN; idx += 32)
+    for(int j = lane; j < sub_pixels(sub); j += 32)
     {
+        const int idx = sub_pixel(j, sub);
         const int px = bx0 + (idx % BIN), py = by0 + idx / BIN;
         if(!D.depthTest || !D.depthWrite || px < D.sx0 || px >= D.sx1 || py < D.sy0 || py >= D.sy1) continue;
 #pragma unroll
@@ -680,7 +749,7 @@ __device__ __forceinline__ void adjoint_bin(const DrawParams &D, const AdjParams
     }
     if(!over)
     {
-        adjoint_pixels_writers<MS>(D, A, S, bx0, by0, n.frag);
+        adjoint_pixels_writers<MS>(D, A, S, R, bx0, by0, sub, n.frag);
         return;
     }
     // fragments per pixel -> first entry per pixel (8 pixels per lane)
@@ -706,7 +775,31 @@ __device__ __forceinline__ void adjoint_bin(const DrawParams &D, const AdjParams
     }
     __syncwarp();
     if(S.off[BIN * BIN] == 0) return;
-    // pixel chunks whose fragments fit the region; replay once per chunk
+    if(S.logCount <= (uint32_t)ADJ_ENTRIES)
+    {
+        // the log holds every fragment: stable scatter into pixel order (lanes
+        // on one pixel take consecutive slots in lane order)
+        for(int e0 = 0; e0 < (int)S.logCount; e0 += 32)
+        {
+            const int e = e0 + lane;
+            const bool valid = e < (int)S.logCount;
+            const uint32_t pix = valid ? R.lpix[e] : 0x10000u + lane;
+            const unsigned peers = __match_any_sync(0xFFFFFFFFu, pix);
+            if(valid)
+            {
+                const uint32_t pos = S.off[pix] + S.fill[pix] + __popc(peers & ((1u << lane) - 1u));
+                R.tri[pos] = R.ltri[e];
+                R.pix[pos] = pix;
+            }
+            __syncwarp();
+            if(valid && (peers >> lane) == 1u) S.fill[pix] += (uint16_t)__popc(peers);
+            __syncwarp();
+        }
+        adjoint_pixels_blended<MS>(D, A, S, R, bx0, by0, 0, BIN * BIN, n.frag);
+        return;
+    }
+    // more fragments than the region holds: pixel chunks that fit it, one
+    // replay each
     int p0 = 0;
     while(p0 < BIN * BIN)
     {
@@ -715,7 +808,7 @@ __device__ __forceinline__ void adjoint_bin(const DrawParams &D, const AdjParams
         if(S.off[p1] > S.off[p0])
         {
             adj_reset(A, S);
-            walk_bin(D, S, bx0, by0, [&](int nb) { adjoint_replay<MS, REPLAY_RECORD>(D, S, R, nb, bx0, by0, p0, p1, n.overflow); });
+            walk_bin(D, S, bx0, by0, [&](int nb) { adjoint_replay<MS>(D, S, R, REPLAY_RECORD, nb, bx0, by0, p0, p1, sub, n.overflow); });
             adjoint_pixels_blended<MS>(D, A, S, R, bx0, by0, p0, p1, n.frag);
         }
         p0 = p1;
@@ -741,23 +834,25 @@ __device__ __forceinline__ uint8_t *adj_region_base(uint8_t *scratch)
     return scratch + (size_t)(blockIdx.x * ADJ_WARPS + (threadIdx.x >> 5)) * ADJ_REGION_BYTES;
 }
 
+// Work item k of a draw: bin k / split, part k % split (split 1: whole bins,
+// split 4: quarters, for frames with fewer bins than resident warps).
 template<int MS>
 __global__ void __launch_bounds__(ADJ_THREADS) k_adjoint(const __grid_constant__ DrawParams D, const __grid_constant__ AdjParams A,
-                                                         uint8_t *scratch)
+                                                         uint8_t *scratch, int split)
 {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     AdjShared<MS> &S = reinterpret_cast<AdjShared<MS> *>(smem_raw)[threadIdx.x >> 5];
     const AdjRegion R(adj_region_base(scratch));
     const int lane = threadIdx.x & 31;
-    const int nbins = D.binsX * D.binsY;
+    const int items = D.binsX * D.binsY * split;
     AdjCount n;
     for(;;)
     {
-        int bin = 0;
-        if(lane == 0) bin = (int)atomicAdd(D.binQueue, 1u);
-        bin = __shfl_sync(0xFFFFFFFFu, bin, 0);
-        if(bin >= nbins) break;
-        adjoint_bin<MS>(D, A, S, R, bin, n);
+        int item = 0;
+        if(lane == 0) item = (int)atomicAdd(D.binQueue, 1u);
+        item = __shfl_sync(0xFFFFFFFFu, item, 0);
+        if(item >= items) break;
+        adjoint_bin<MS>(D, A, S, R, item / split, split > 1 ? item % split : -1, n);
     }
     flush_adjoint_counters(D.counters, n);
 }
@@ -773,15 +868,17 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adjoint_batch(const __grid_cons
     const int lane = threadIdx.x & 31;
     const BatchView V(B.hdr);
     const AdjParams *adj = (const AdjParams *)((const uint8_t *)B.hdr + V.h.offAdj);
+    const uint32_t split = V.h.split ? V.h.split : 1;
     AdjCount n;
     for(;;)
     {
-        uint32_t bin = 0;
-        if(lane == 0) bin = atomicAdd(B.binQueue, 1u);
-        bin = __shfl_sync(0xFFFFFFFFu, bin, 0);
-        if(bin >= V.h.bins) break;
+        uint32_t item = 0;
+        if(lane == 0) item = atomicAdd(B.binQueue, 1u);
+        item = __shfl_sync(0xFFFFFFFFu, item, 0);
+        if(item >= V.h.bins * split) break;
+        const uint32_t bin = item / split;
         const uint32_t d = find_draw(V.bStart, V.h.n, bin);
-        adjoint_bin<MS>(V.draws[d], adj[d], S, R, (int)(bin - __ldg(V.bStart + d)), n);
+        adjoint_bin<MS>(V.draws[d], adj[d], S, R, (int)(bin - __ldg(V.bStart + d)), split > 1 ? (int)(item % split) : -1, n);
     }
     flush_adjoint_counters(B.counters, n);
 }

@@ -136,6 +136,7 @@ struct DrawParams {
     int nchunks;
     // scratch
     float4 *ptv;          // 4 x float4 per vertex
+    double *ptv64;        // adjoint runs only: clip x, y, w and x/w, y/w in fp64 (6 doubles per vertex), else null
     short4 *triBox;       // pixel box per triangle
     TriInfo *triInfo;
     short4 *chunkBox;     // union of the boxes of CHUNK consecutive triangles
@@ -225,6 +226,22 @@ __device__ __forceinline__ void vertex_body(const DrawParams &D, uint32_t i)
     o[1] = make_float4(__int_as_float(X), __int_as_float(Y), __int_as_float(f), z * rhw);
     o[2] = make_float4(rhw, v[0], v[1], v[2]);
     o[3] = make_float4(v[3], v[4], v[5], v[6]);
+    if(D.ptv64)
+    {
+        // the adjoint's clip coordinates: MVP p in fp64, and the projection
+        double c[4];
+#pragma unroll
+        for(int row = 0; row < 4; row++)
+            c[row] = (double)D.mvp[row] * p[0] + (double)D.mvp[4 + row] * p[1] + (double)D.mvp[8 + row] * p[2] +
+                     (double)D.mvp[12 + row] * p[3];
+        double *o64 = D.ptv64 + (size_t)i * 6;
+        o64[0] = c[0];
+        o64[1] = c[1];
+        o64[2] = c[3];
+        o64[3] = c[3] != 0.0 ? c[0] / c[3] : 0.0;
+        o64[4] = c[3] != 0.0 ? c[1] / c[3] : 0.0;
+        o64[5] = 0.0;
+    }
 }
 
 __global__ void k_vertex(const __grid_constant__ DrawParams D, uint32_t nverts)
@@ -1759,7 +1776,8 @@ struct BatchHeader {
     // a captured graph serves any n
     uint32_t offDraws, offV, offS, offB;
     uint32_t offAdj;  // per-draw AdjParams (adjoint batches only)
-    uint32_t pad[6];
+    uint32_t split;   // adjoint batches: warps per bin (1 or 4)
+    uint32_t pad[5];
 };
 
 struct BatchPtrs {
@@ -1896,6 +1914,8 @@ struct swgb_ctx {
     bool adjAttr;
     int adjBlocks[2];      // persistent adjoint grid: 1 and 4 samples
     uint8_t *adjScratch;   // one region per adjoint warp of the larger grid
+    double *ptv64;         // adjoint: fp64 clip coordinates per vertex
+    size_t ptv64Cap;
 };
 
 namespace {
@@ -2245,6 +2265,7 @@ swgb_status enqueue(swgb_ctx *ctx, DrawParams &D)
 struct BatchState {
     // scratch shared by the draws of one segment
     float4 *ptv = nullptr; size_t ptvCap = 0;
+    double *ptv64 = nullptr; size_t ptv64Cap = 0;  // adjoint segments only
     short4 *triBox = nullptr; size_t triBoxCap = 0;
     TriInfo *triInfo = nullptr; size_t triInfoCap = 0;
     short4 *chunk = nullptr; size_t chunkCap = 0;
@@ -2527,7 +2548,7 @@ swgb_status batch_init(swgb_ctx *ctx)
 void batch_free(BatchState *B)
 {
     if(!B) return;
-    cudaFree(B->ptv); cudaFree(B->triBox); cudaFree(B->triInfo); cudaFree(B->chunk); cudaFree(B->super);
+    cudaFree(B->ptv); cudaFree(B->ptv64); cudaFree(B->triBox); cudaFree(B->triInfo); cudaFree(B->chunk); cudaFree(B->super);
     cudaFree(B->spans); cudaFree(B->poly); cudaFree(B->queue); cudaFree(B->desc);
     if(B->stage) cudaFreeHost(B->stage);
     if(B->stageFree) cudaEventDestroy(B->stageFree);
@@ -2594,6 +2615,7 @@ swgb_status enqueue_segment(swgb_ctx *ctx, std::vector<DrawParams> &draws, uint3
     swgb_status s;
     const uint64_t triSlots = sblocks * SETUP_THREADS;
     if((s = ensure_gen(B.ptv, B.ptvCap, (size_t)verts * 4, B, "batch ptv")) != SWGB_OK) return s;
+    if(adj && (s = ensure_gen(B.ptv64, B.ptv64Cap, (size_t)verts * 6, B, "batch fp64 clip coordinates")) != SWGB_OK) return s;
     if((s = ensure_gen(B.triBox, B.triBoxCap, (size_t)triSlots, B, "batch boxes")) != SWGB_OK) return s;
     if((s = ensure_gen(B.triInfo, B.triInfoCap, (size_t)triSlots, B, "batch records")) != SWGB_OK) return s;
     if((s = ensure_gen(B.chunk, B.chunkCap, (size_t)triSlots / CHUNK, B, "batch chunks")) != SWGB_OK) return s;
@@ -2608,6 +2630,7 @@ swgb_status enqueue_segment(swgb_ctx *ctx, std::vector<DrawParams> &draws, uint3
     {
         DrawParams &d = draws[first + k];
         d.ptv = B.ptv + vOff * 4;
+        d.ptv64 = adj ? B.ptv64 + vOff * 6 : nullptr;
         d.triBox = B.triBox + sOff;
         d.triInfo = B.triInfo + sOff;
         d.chunkBox = B.chunk + sOff / CHUNK;
@@ -2641,6 +2664,8 @@ swgb_status enqueue_segment(swgb_ctx *ctx, std::vector<DrawParams> &draws, uint3
     h.offS = (uint32_t)L.offS;
     h.offB = (uint32_t)L.offB;
     h.offAdj = (uint32_t)L.offAdj;
+    // adjoint over few bins: four warps per bin (quarters)
+    h.split = adj && bins < 2ull * (uint64_t)ctx->adjBlocks[draws[first].ms > 1 ? 1 : 0] * ADJ_WARPS ? 4 : 1;
     memcpy(img, &h, sizeof(h));
     memcpy(img + L.offDraws, draws.data() + first, (size_t)n * sizeof(DrawParams));
     memcpy(img + L.offV, vStart.data(), (size_t)(n + 1) * 4);
@@ -2776,6 +2801,10 @@ swgb_status bake_adjoint(const swgb_pipeline_state *st, const swgb_draw_args *a,
     memset(&A, 0, sizeof(A));
     A.gradColor = (const uint8_t *)g->grad_color;
     A.gradPitch = g->grad_color_pitch_bytes;
+    A.rxs = 256.0 / (double)D.WxF;
+    A.rx0 = -(double)D.X0xF / (double)D.WxF;
+    A.rys = 256.0 / (double)D.HxF;
+    A.ry0 = -(double)D.Y0xF / (double)D.HxF;
     A.gradSlice = g->grad_color_slice_bytes;
     for(int c = 0; c < 4; c++) A.clear[c] = g->clear_color[c];
     A.clearDepth = g->clear_depth;
@@ -2840,6 +2869,8 @@ swgb_status draw_adjoint(swgb_ctx *ctx, const swgb_pipeline_state *st, const swg
     if(D.count == 0) return SWGB_OK;
     if((s = adjoint_init(ctx)) != SWGB_OK) return s;
     if((s = prepare_scratch(ctx, D)) != SWGB_OK) return s;
+    if((s = ensure(ctx->ptv64, ctx->ptv64Cap, (size_t)D.vertexCount * 6, "fp64 clip coordinates")) != SWGB_OK) return s;
+    D.ptv64 = ctx->ptv64;
     const uint32_t nv = D.vertexCount;
     timed_launch(ctx, SWGB_KERNEL_VERTEX, [&] { k_vertex<<<(nv + 255) / 256, 256, 0, ctx->stream>>>(D, nv); });
     const uint32_t setupBlocks = (uint32_t)((D.count + SETUP_THREADS - 1) / SETUP_THREADS);
@@ -2847,11 +2878,13 @@ swgb_status draw_adjoint(swgb_ctx *ctx, const swgb_pipeline_state *st, const swg
     if(D.binsX > 0 && D.binsY > 0)
     {
         const int v = D.ms > 1 ? 1 : 0;
-        uint32_t blocks = (uint32_t)((D.binsX * D.binsY + ADJ_WARPS - 1) / ADJ_WARPS);
+        const uint32_t bins = (uint32_t)(D.binsX * D.binsY);
+        const int split = bins < 2u * (uint32_t)ctx->adjBlocks[v] * ADJ_WARPS ? 4 : 1;  // few bins: quarter them
+        uint32_t blocks = (bins * split + ADJ_WARPS - 1) / ADJ_WARPS;
         if(blocks > (uint32_t)ctx->adjBlocks[v]) blocks = (uint32_t)ctx->adjBlocks[v];
         timed_launch(ctx, SWGB_KERNEL_ADJOINT, [&] {
-            if(v) k_adjoint<4><<<blocks, ADJ_THREADS, ADJ_WARPS * sizeof(AdjShared<4>), ctx->stream>>>(D, A, ctx->adjScratch);
-            else k_adjoint<1><<<blocks, ADJ_THREADS, ADJ_WARPS * sizeof(AdjShared<1>), ctx->stream>>>(D, A, ctx->adjScratch);
+            if(v) k_adjoint<4><<<blocks, ADJ_THREADS, ADJ_WARPS * sizeof(AdjShared<4>), ctx->stream>>>(D, A, ctx->adjScratch, split);
+            else k_adjoint<1><<<blocks, ADJ_THREADS, ADJ_WARPS * sizeof(AdjShared<1>), ctx->stream>>>(D, A, ctx->adjScratch, split);
         });
     }
     return cuda_check(cudaGetLastError(), "adjoint launch");
@@ -3029,6 +3062,7 @@ swgb_status swgb_ctx_destroy(swgb_ctx *c)
     delete c->evFree;
     batch_free(c->batch);
     cudaFree(c->adjScratch);
+    cudaFree(c->ptv64);
     delete c;
     return SWGB_OK;
 }
