@@ -429,6 +429,18 @@ class BatchScene:
     def n(self):
         return len(self.tris)
 
+    def subset(self, idx):
+        """The draws idx (ascending) of this batch, keeping their atlas places."""
+        idx = np.asarray(idx, np.int64)
+        tris = self.tris[idx]
+        verts = np.concatenate([self.vertices[self.vstart[i]:self.vstart[i] + 3 * self.tris[i]] for i in idx]) \
+            if len(idx) else self.vertices[:0]
+        vstart = np.concatenate([[0], np.cumsum(3 * tris)[:-1]]).astype(np.int64) if len(idx) else tris
+        return BatchScene(name="%s_part%d" % (self.name, len(idx)), tris=tris, sides=self.sides[idx], place=self.place[idx],
+                          vertices=verts, vstart=vstart, textures=self.textures[idx], page_size=self.page_size,
+                          pages=self.pages, sampler=dict(self.sampler), clear_color=self.clear_color,
+                          clear_depth=self.clear_depth)
+
     def draw_scene(self, i):
         """Draw i as a stand-alone Scene (its own side x side framebuffer)."""
         s = int(self.sides[i])
@@ -439,6 +451,19 @@ class BatchScene:
                      sampler=dict(self.sampler), clear_color=self.clear_color, clear_depth=self.clear_depth)
 
 
+def _batch_sizes(rng, n_draws, tri_min, tri_max, sides):
+    tris = np.rint(np.exp(rng.uniform(math.log(tri_min), math.log(tri_max), n_draws))).astype(np.int64)
+    tris = np.clip(tris, tri_min, tri_max)
+    side = rng.choice(np.asarray(sides, np.int64), n_draws)
+    return tris, side
+
+
+def batch_draw_sizes(n_draws=4096, tri_min=16, tri_max=65536, sides=(128, 256, 384, 512), seed_index=2):
+    """Triangle counts and viewport sides of scene_batch's draws (same seed,
+    no vertex data)."""
+    return _batch_sizes(_rng(seed_index), n_draws, tri_min, tri_max, sides)
+
+
 def scene_batch(n_draws=4096, tri_min=16, tri_max=65536, sides=(128, 256, 384, 512), page_size=16384,
                 tex_size=256, seed_index=2):
     """Batched forward: n_draws independent draws, triangle counts
@@ -447,9 +472,7 @@ def scene_batch(n_draws=4096, tri_min=16, tri_max=65536, sides=(128, 256, 384, 5
     pages; triangles uniform in clip space as in scene_small; each draw
     samples its own tex_size^2 RGBA8 texture bilinearly (one level)."""
     rng = _rng(seed_index)
-    tris = np.rint(np.exp(rng.uniform(math.log(tri_min), math.log(tri_max), n_draws))).astype(np.int64)
-    tris = np.clip(tris, tri_min, tri_max)
-    side = rng.choice(np.asarray(sides, np.int64), n_draws)
+    tris, side = _batch_sizes(rng, n_draws, tri_min, tri_max, sides)
     place = shelf_pack(side, page_size)
     vertices = random_triangles(rng, int(tris.sum()), textured=True)
     vstart = np.concatenate([[0], np.cumsum(3 * tris)[:-1]]).astype(np.int64)
