@@ -48,6 +48,8 @@ WORKLOADS = {
                    "2048^2 RGBA8 12-level chain trilinear REPEAT, colour = texel * vertex colour, depth LESS, "
                    "blend SRC_ALPHA/ONE_MINUS_SRC_ALPHA",
     "small": "1000 independent Gouraud triangles, 256x256 RGBA8 + D32F, depth LESS, no blend, no texture",
+    "sphere": "adjoint: 20k-triangle uv-sphere, 512^2 RGBA32F, 1024^2 RGBA32F texture (forward + adjoint)",
+    "views": "adjoint: views of a 100k-triangle noisy sphere, 512^2 4x MSAA RGBA16F, OVER (forward + adjoint)",
     "batch": "4096 independent draws, triangle counts log-uniform in [16, 65536], uniform clip-space triangles, "
              "square viewports with side uniform in {128,256,384,512} shelf-packed into 16384^2 RGBA8 + D32F "
              "atlas pages, each draw sampling its own 256^2 RGBA8 texture bilinearly, depth LESS, no blend",
@@ -382,7 +384,8 @@ def measure_batch(r, stream, flush, params, steps, warmup, per_draw_steps, dev, 
 
     for _ in range(warmup):
         batched()
-    per_draw()
+    if per_draw_steps:
+        per_draw()
     r.synchronize()
     r.reset_counters()
     l0 = r.launch_count()
@@ -390,7 +393,7 @@ def measure_batch(r, stream, flush, params, steps, warmup, per_draw_steps, dev, 
     r.synchronize()
     launches = r.launch_count() - l0
     cnt = r.counters()
-    tp = time_steps(stream, flush, per_draw_steps, per_draw)
+    tp = time_steps(stream, flush, per_draw_steps, per_draw) if per_draw_steps else [float("nan")]
     r.synchronize()
     mb, mp = sum(tb) / len(tb), sum(tp) / len(tp)
     per_step = {k: v // steps if k != "texture_levels_mask" else v for k, v in cnt.items()}
@@ -398,9 +401,9 @@ def measure_batch(r, stream, flush, params, steps, warmup, per_draw_steps, dev, 
         "config": {"draws": b.n, "triangles_log_uniform": [params["tri_min"], params["tri_max"]],
                    "triangles": int(b.tris.sum()), "viewport_sides": [128, 256, 384, 512],
                    "atlas_pages": b.pages, "page": b.page_size, "texture": "256^2 RGBA8 per draw, bilinear"},
-        "batched_ms_per_step": round(mb, 3), "per_draw_ms_per_step": round(mp, 3),
-        "speedup_vs_per_draw": round(mp / mb, 2),
-        "draws_per_s": round(b.n / (mb * 1e-3), 1), "per_draw_draws_per_s": round(b.n / (mp * 1e-3), 1),
+        "batched_ms_per_step": round(mb, 3), "per_draw_ms_per_step": round(mp, 3) if per_draw_steps else None,
+        "speedup_vs_per_draw": round(mp / mb, 2) if per_draw_steps else None,
+        "draws_per_s": round(b.n / (mb * 1e-3), 1), "per_draw_draws_per_s": round(b.n / (mp * 1e-3), 1) if per_draw_steps else None,
         "gfrag_per_s": round(per_step["fragments_tested"] / (mb * 1e-3) / 1e9, 3),
         "mtri_per_s": round(per_step["triangles_in"] / (mb * 1e-3) / 1e6, 2),
         "gpu_launches_per_step": launches / steps, "steps": steps, "per_draw_steps": per_draw_steps,
@@ -408,7 +411,7 @@ def measure_batch(r, stream, flush, params, steps, warmup, per_draw_steps, dev, 
     }
 
 
-def measure_adjoint(r, stream, flush, dev, workload, steps=3, warmup=2):
+def measure_adjoint(r, stream, flush, dev, workload, steps=3, warmup=2, views=256):
     """Forward and adjoint times of one adjoint workload, through the same
     DrawSet calls the autograd function makes (no torch autograd overhead):
     forward = clear + draw(s); adjoint = zero gradients + adjoint draw(s) for
@@ -424,12 +427,12 @@ def measure_adjoint(r, stream, flush, dev, workload, steps=3, warmup=2):
         rng = np.random.Generator(np.random.PCG64(0x53570004))
         mesh = scenes.uv_sphere(rng, 250, 200, noise_sigma=0.02)
         levels = scenes.float_mip_chain(rng.uniform(0.0, 1.0, (2048, 2048, 4)), np.float16)
-        scene_list = [scenes.scene_sphere_views(v, mesh=mesh, levels=levels) for v in range(256)]
+        scene_list = [scenes.scene_sphere_views(v, mesh=mesh, levels=levels) for v in range(views)]
         for sc in scene_list:
             sc.samples = 4
-        desc = ("256 views of a 100k-triangle uv-sphere with radial N(0, 0.02^2) noise, cameras on a radius-3 "
+        desc = ("%d views of a 100k-triangle uv-sphere with radial N(0, 0.02^2) noise, cameras on a radius-3 "
                 "sphere, 512^2 4x MSAA RGBA16F, 2048^2 RGBA16F mip chain trilinear, premultiplied OVER, depth "
-                "LESS; all views as one batch forward and one batch adjoint")
+                "LESS; all views as one batch forward and one batch adjoint" % views)
     sc0 = scene_list[0]
     verts = torch.from_numpy(np.ascontiguousarray(sc0.vertices, np.float32)).to(dev)
     tdt = torch.float16 if sc0.texture_format == abi.FORMAT_R16G16B16A16_SFLOAT else torch.float32
@@ -455,6 +458,34 @@ def measure_adjoint(r, stream, flush, dev, workload, steps=3, warmup=2):
             "steps": steps}
 
 
+def run_adjoint(args):
+    """--workload sphere|views: forward and adjoint of one adjoint workload
+    as the headline line (metric: adjoint ms per step; the forward beside)."""
+    import torch
+    from swiftshader_gb300 import Renderer
+    world, rank, local = dist_env()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    r = Renderer(local, stream)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    res = measure_adjoint(r, stream, flush, dev, args.workload, steps=args.steps, warmup=args.warmup, views=args.views)
+    clk = clocks.stop()
+    if rank != 0:
+        return
+    line = {
+        "metric": "adjoint ms/step", "value": res["adjoint_ms"], "unit": "ms", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": res["adjoint_ms"], "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (fp64 geometry in the adjoint)", "data": "synthetic (seeded generator)",
+        "config": res["config"], "adjoint": res, "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_batch(args):
     """--workload batch: the full 4096-draw atlas workload as the headline."""
     import numpy as np
@@ -476,7 +507,9 @@ def run_batch(args):
     time.sleep(0.3)
     if world > 1:
         torch.distributed.barrier()
-    b, db, res = measure_batch(r, stream, flush, BATCH_FULL, args.steps, args.warmup, min(args.steps, 2), dev, world, rank)
+    params = dict(BATCH_FULL, n_draws=args.batch_draws, tri_max=args.batch_tri_max)
+    b, db, res = measure_batch(r, stream, flush, params, args.steps, args.warmup,
+                               0 if args.no_per_draw else min(args.steps, 2), dev, world, rank)
     clk = clocks.stop()
     # kernel-level timing: the batch as direct launches (timing disables the graph)
     r.set_kernel_timing(True)
@@ -517,13 +550,16 @@ def run_batch(args):
     rbytes = batch_raster_bytes(b, res["counters_per_step"])
     peak, peak_kind = measured_peaks()
     achieved = rbytes / (rast_avg * 1e-3) / 1e9 if rast_avg > 0 else 0.0
-    total = BATCH_FULL["n_draws"]
+    total = params["n_draws"]
     line = {
         "metric": "draws/s", "value": round(total / (mb * 1e-3), 1), "unit": "draws/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(mb, 3), "higher_is_better": True,
         "scaling": "strong", "vs_baseline": None, "dtype": "f32 + int32 fixed point (RGBA8 / D32F out)",
         "data": "synthetic (seeded generator, swiftshader_gb300.scenes.scene_batch)",
-        "config": {"workload": WORKLOADS["batch"], "l2": "flushed before every timed step (256 MiB write)",
+        "config": {"workload": WORKLOADS["batch"] if params == BATCH_FULL else
+                   "%d independent draws, triangle counts log-uniform in [%d, %d], otherwise as the 4096-draw atlas "
+                   "workload" % (params["n_draws"], params["tri_min"], params["tri_max"]),
+                   "l2": "flushed before every timed step (256 MiB write)",
                    "parallelism": ("draws split over ranks, longest-processing-time-first on triangles x viewport "
                                    "area; no collective") if world > 1 else "single GPU"},
         "batched": res,
@@ -589,6 +625,9 @@ def cpu_baseline(args, scene, bounded_s=12.0, threads=None):
 def run_reference(args):
     world, rank, local = dist_env()
     if rank != 0:
+        return
+    if args.workload in ("sphere", "views"):
+        print(json.dumps({"impl": "reference", "unavailable": "the reference draw path has no backward pass"}), flush=True)
         return
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
@@ -657,11 +696,17 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-vs-per-draw sample")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint / forward timings")
+    ap.add_argument("--batch-draws", type=int, default=BATCH_FULL["n_draws"], help="--workload batch: draws")
+    ap.add_argument("--batch-tri-max", type=int, default=BATCH_FULL["tri_max"], help="--workload batch: largest draw")
+    ap.add_argument("--no-per-draw", action="store_true", help="--workload batch: skip the per-draw comparison")
+    ap.add_argument("--views", type=int, default=256, help="--workload views: views")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batch":
         run_batch(args)
+    elif args.workload in ("sphere", "views"):
+        run_adjoint(args)
     else:
         run_ours(args)
 
