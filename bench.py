@@ -169,7 +169,7 @@ def algorithmic_bytes(scene, cnt):
 
 def run_ours(args):
     import torch
-    from swiftshader_gb300 import DeviceScene, Renderer
+    from swiftshader_gb300 import DeviceScene, Renderer, scenes
     world, rank, local = dist_env()
     if world > 1:
         import torch.distributed as dist
@@ -233,11 +233,11 @@ def run_ours(args):
     pin = lambda arr: torch.from_numpy(arr).pin_memory()
     import numpy as np
     h_vert = pin(np.ascontiguousarray(scene.vertices))
-    h_idx = None if scene.indices is None else pin(np.ascontiguousarray(scene.indices).view(np.int32))
+    h_idx = None if scene.indices is None else pin(scenes.index_bytes(scene))
     h_lv = [pin(np.ascontiguousarray(l)) for l in scene.texture_levels]
     h_color = torch.empty(ds.color.shape, dtype=ds.color.dtype).pin_memory()
     h_depth = torch.empty(ds.depth.shape, dtype=ds.depth.dtype).pin_memory()
-    h2d = h_vert.numel() * 4 + (0 if h_idx is None else h_idx.numel() * 4) + sum(l.numel() for l in h_lv)
+    h2d = h_vert.numel() * 4 + (0 if h_idx is None else h_idx.numel()) + sum(l.numel() for l in h_lv)
     d2h = h_color.numel() * h_color.element_size() + h_depth.numel() * 4
 
     def e2e_step():

@@ -61,9 +61,12 @@ typedef enum swgb_status {
 #define SWGB_FORMAT_D32_SFLOAT 126
 /* VkPrimitiveTopology */
 #define SWGB_TOPOLOGY_TRIANGLE_LIST 3
+#define SWGB_TOPOLOGY_TRIANGLE_STRIP 4
+#define SWGB_TOPOLOGY_TRIANGLE_FAN 5
 /* VkIndexType (0xFFFFFFFF = non-indexed draw) */
 #define SWGB_INDEX_TYPE_UINT16 0
 #define SWGB_INDEX_TYPE_UINT32 1
+#define SWGB_INDEX_TYPE_UINT8 1000265000u /* VK_INDEX_TYPE_UINT8_EXT */
 #define SWGB_INDEX_TYPE_NONE 0xFFFFFFFFu
 /* VkCullModeFlagBits */
 #define SWGB_CULL_NONE 0
@@ -163,7 +166,10 @@ typedef struct swgb_texture {
 } swgb_texture;
 
 typedef struct swgb_pipeline_state {
-    /* vertex input interface (vk::VertexInputInterfaceState) */
+    /* vertex input interface (vk::VertexInputInterfaceState): triangle list,
+     * strip or fan, provoking vertex first (Renderer.cpp setBatchIndices);
+     * primitive restart is resolved by the caller into separate draws, as
+     * vk::IndexBuffer does before Renderer::draw */
     uint32_t topology;
     uint32_t attrib_count;
     swgb_vertex_attrib attribs[SWGB_MAX_ATTRIBS];
@@ -211,7 +217,7 @@ typedef struct swgb_draw_args {
     uint32_t count;        /* number of triangles (Renderer::draw 'count')              */
     int32_t base_vertex;   /* added to every vertex index ('baseVertex')                */
     uint32_t first_vertex; /* non-indexed draws: index of the first vertex              */
-    uint32_t index_type;   /* SWGB_INDEX_TYPE_UINT16/UINT32, or SWGB_INDEX_TYPE_NONE    */
+    uint32_t index_type;   /* SWGB_INDEX_TYPE_UINT8/16/32, or SWGB_INDEX_TYPE_NONE      */
     const void *indices;   /* device pointer to the first index of the draw             */
     uint32_t vertex_count; /* indexed draws: vertices addressable after base_vertex;
                               every index must be < vertex_count                       */

@@ -36,6 +36,24 @@ def log2sqrt_f32(x):
     return (bits - np.float32(1065353216.0)) * np.float32(2.0 ** -25)
 
 
+def triangle_vertices(scene):
+    """Vertex-buffer index of each corner of each triangle [T, 3]: list,
+    strip or fan positions (setBatchIndices, first vertex provoking,
+    src/Device/Renderer.cpp:97-134), through the index buffer when indexed,
+    plus first_vertex (non-indexed) and base_vertex."""
+    from swiftshader_gb300 import abi
+    t = np.arange(scene.tri_count, dtype=np.int64)
+    if scene.topology == abi.TOPOLOGY_TRIANGLE_STRIP:
+        pos = np.stack([t, t + 1 + (t & 1), t + 2 - (t & 1)], axis=1)
+    elif scene.topology == abi.TOPOLOGY_TRIANGLE_FAN:
+        pos = np.stack([t + 1, t + 2, np.zeros_like(t)], axis=1)
+    else:
+        pos = 3 * t[:, None] + np.arange(3)
+    if scene.indices is None:
+        return pos + scene.first_vertex + scene.base_vertex
+    return np.asarray(scene.indices, np.int64)[pos] + scene.base_vertex
+
+
 class Model:
     """The differentiable draw of one scene with fixed visibility."""
 
@@ -46,9 +64,7 @@ class Model:
         self.abi = abi
         self.S, self.H, self.W = vis_len.shape
         self.mvp = np.asarray(scene.mvp if scene.mvp is not None else np.eye(4), np.float64)
-        n = scene.tri_count
-        self.tri_vertices = (np.arange(3 * n).reshape(n, 3) if scene.indices is None
-                             else np.asarray(scene.indices, np.int64).reshape(n, 3))
+        self.tri_vertices = triangle_vertices(scene)
         vx, vy, vw, vh = scene.viewport or (0, 0, scene.width, scene.height)
         self.rx_of = lambda px: (np.asarray(px, np.float64) + 0.5 - vx - 0.5 * vw) / (0.5 * vw)
         self.ry_of = lambda py: (np.asarray(py, np.float64) + 0.5 - vy - 0.5 * vh) / (0.5 * vh)

@@ -85,7 +85,7 @@ def host_state(scene, color, depth):
     verts = np.ascontiguousarray(scene.vertices, np.float32)
     levels = [np.ascontiguousarray(l) for l in scene.texture_levels]
     st = scenes.build_state(scene, _ptr(color), _ptr(depth), _ptr(verts), [_ptr(l) for l in levels])
-    idx = None if scene.indices is None else np.ascontiguousarray(scene.indices, np.uint32)
+    idx = None if scene.indices is None else np.ascontiguousarray(scene.indices)
     args = scenes.build_args(scene, _ptr(idx))
     keep = (verts, levels, idx)
     return st, args, keep

@@ -225,7 +225,9 @@ static swgb_status prepare(ODraw *d, const swgb_pipeline_state *st, const swgb_d
     d->st = st;
     d->args = a;
     if(st->precision_profile != SWGB_PRECISION_CMAKE) return SWGB_UNSUPPORTED_STATE;
-    if(st->topology != SWGB_TOPOLOGY_TRIANGLE_LIST) return SWGB_UNSUPPORTED_STATE;
+    if(st->topology != SWGB_TOPOLOGY_TRIANGLE_LIST && st->topology != SWGB_TOPOLOGY_TRIANGLE_STRIP &&
+       st->topology != SWGB_TOPOLOGY_TRIANGLE_FAN)
+        return SWGB_UNSUPPORTED_STATE;
     if(st->sample_count != 1 && st->sample_count != 4) return SWGB_UNSUPPORTED_STATE;
     if(st->depth_clamp_enable || st->depth_bias_constant != 0.0f || st->depth_bias_slope != 0.0f) return SWGB_UNSUPPORTED_STATE;
     if(st->attrib_count < 1 || st->attrib_count > SWGB_MAX_ATTRIBS) return SWGB_INVALID_ARG;
@@ -310,6 +312,8 @@ static uint32_t vertex_index(const ODraw *d, uint32_t k)
         idx = a->first_vertex + k;
     else if(a->index_type == SWGB_INDEX_TYPE_UINT16)
         idx = ((const uint16_t *)a->indices)[k];
+    else if(a->index_type == SWGB_INDEX_TYPE_UINT8)
+        idx = ((const uint8_t *)a->indices)[k];
     else
         idx = ((const uint32_t *)a->indices)[k];
     return idx + (uint32_t)a->base_vertex; /* readStream: (index + baseVertex) * stride, UInt arithmetic */
@@ -692,12 +696,38 @@ static int setup_triangle(const ODraw *d, const OVertex *tv0, const OVertex *tv1
 
 /* setupSolidTriangles for one triangle (src/Device/Renderer.cpp:733-776).
  * Returns visibility; counters updated. */
+/* Index-buffer positions of triangle tri: setBatchIndices with the first
+ * vertex provoking (src/Device/Renderer.cpp:97-134). */
+static void triangle_positions(uint32_t topology, uint32_t tri, uint32_t k[3])
+{
+    switch(topology)
+    {
+    case SWGB_TOPOLOGY_TRIANGLE_STRIP: /* :110-121 */
+        k[0] = tri;
+        k[1] = tri + (tri & 1) + 1;
+        k[2] = tri + (~tri & 1) + 1;
+        break;
+    case SWGB_TOPOLOGY_TRIANGLE_FAN: /* :122-133 */
+        k[0] = tri + 1;
+        k[1] = tri + 2;
+        k[2] = 0;
+        break;
+    default: /* TRIANGLE_LIST :97-109 */
+        k[0] = 3 * tri;
+        k[1] = 3 * tri + 1;
+        k[2] = 3 * tri + 2;
+        break;
+    }
+}
+
 static int process_triangle(const ODraw *d, uint32_t tri, OPrim *pr, swgb_counters *cnt, int *clipped_out)
 {
     OVertex v0, v1, v2;
-    vertex_shade(d, vertex_index(d, 3 * tri + 0), &v0);
-    vertex_shade(d, vertex_index(d, 3 * tri + 1), &v1);
-    vertex_shade(d, vertex_index(d, 3 * tri + 2), &v2);
+    uint32_t k[3];
+    triangle_positions(d->st->topology, tri, k);
+    vertex_shade(d, vertex_index(d, k[0]), &v0);
+    vertex_shade(d, vertex_index(d, k[1]), &v1);
+    vertex_shade(d, vertex_index(d, k[2]), &v2);
     OPolygon poly;
     poly.P[0][0] = &v0.pos; poly.P[0][1] = &v1.pos; poly.P[0][2] = &v2.pos;
     poly.n = 3; poly.i = 0; poly.b = 0;

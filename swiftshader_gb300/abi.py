@@ -25,8 +25,11 @@ FORMAT_R32G32_SFLOAT = 103
 FORMAT_R32G32B32A32_SFLOAT = 109
 FORMAT_D32_SFLOAT = 126
 TOPOLOGY_TRIANGLE_LIST = 3
+TOPOLOGY_TRIANGLE_STRIP = 4
+TOPOLOGY_TRIANGLE_FAN = 5
 INDEX_TYPE_UINT16 = 0
 INDEX_TYPE_UINT32 = 1
+INDEX_TYPE_UINT8 = 1000265000
 INDEX_TYPE_NONE = 0xFFFFFFFF
 CULL_NONE, CULL_FRONT, CULL_BACK, CULL_FRONT_AND_BACK = 0, 1, 2, 3
 FRONT_FACE_CCW, FRONT_FACE_CW = 0, 1

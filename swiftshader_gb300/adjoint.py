@@ -49,7 +49,7 @@ class _View:
         if scene.indices is not None:
             key = id(scene.indices)
             if key not in index_cache:  # views of one mesh share its index buffer
-                index_cache[key] = torch.from_numpy(np.ascontiguousarray(scene.indices).view(np.int32)).to(dev)
+                index_cache[key] = torch.from_numpy(scenes.index_bytes(scene)).to(dev)
             self.indices = index_cache[key]
         self.args = scenes.build_args(scene, None if self.indices is None else self.indices.data_ptr())
 

@@ -268,14 +268,7 @@ struct AdjTri {
 
 __device__ __noinline__ void adj_load_tri(const DrawParams &D, uint32_t t, AdjTri &T)
 {
-    if(D.indexType == SWGB_INDEX_TYPE_NONE)
-    {
-        T.slot[0] = 3 * t; T.slot[1] = 3 * t + 1; T.slot[2] = 3 * t + 2;
-    }
-    else
-    {
-        T.slot[0] = fetch_index(D, 3 * t); T.slot[1] = fetch_index(D, 3 * t + 1); T.slot[2] = fetch_index(D, 3 * t + 2);
-    }
+    tri_slots(D, t, T.slot[0], T.slot[1], T.slot[2]);
 #pragma unroll
     for(int i = 0; i < 3; i++)
     {

@@ -99,6 +99,7 @@ struct DrawParams {
     float mvp[16];
     const void *indices;
     uint32_t indexType;
+    uint32_t topology;     // SWGB_TOPOLOGY_TRIANGLE_LIST / STRIP / FAN
     uint32_t firstVertex;
     int32_t baseVertex;
     uint32_t vertexCount;  // post-transform vertices
@@ -266,7 +267,38 @@ __device__ __forceinline__ uint32_t fetch_index(const DrawParams &D, uint32_t k)
 {
     if(D.indexType == SWGB_INDEX_TYPE_NONE) return k;
     if(D.indexType == SWGB_INDEX_TYPE_UINT16) return __ldg((const uint16_t *)D.indices + k);
+    if(D.indexType == SWGB_INDEX_TYPE_UINT8) return __ldg((const uint8_t *)D.indices + k);
     return __ldg((const uint32_t *)D.indices + k);
+}
+
+// Post-transform vertex slots of triangle t: the index-buffer positions of
+// setBatchIndices with the first vertex provoking (Renderer.cpp:97-134) --
+// list (3t, 3t+1, 3t+2); strip (t, t+1+odd, t+2-odd), odd = t & 1; fan
+// (t+1, t+2, 0) -- through the index buffer of an indexed draw.
+__device__ __forceinline__ void tri_slots(const DrawParams &D, uint32_t t, uint32_t &i0, uint32_t &i1, uint32_t &i2)
+{
+    uint32_t k0, k1, k2;
+    if(D.topology == SWGB_TOPOLOGY_TRIANGLE_STRIP)
+    {
+        k0 = t;
+        k1 = t + 1 + (t & 1);
+        k2 = t + 2 - (t & 1);
+    }
+    else if(D.topology == SWGB_TOPOLOGY_TRIANGLE_FAN)
+    {
+        k0 = t + 1;
+        k1 = t + 2;
+        k2 = 0;
+    }
+    else
+    {
+        k0 = 3 * t;
+        k1 = 3 * t + 1;
+        k2 = 3 * t + 2;
+    }
+    i0 = fetch_index(D, k0);
+    i1 = fetch_index(D, k1);
+    i2 = fetch_index(D, k2);
 }
 
 struct CVert { float x, y, z, w; };
@@ -454,18 +486,11 @@ __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
         cntIn = 1;
         uint32_t i0, i1, i2;
         bool ok = true;
-        if(D.indexType != SWGB_INDEX_TYPE_NONE)
+        tri_slots(D, t, i0, i1, i2);
+        if(D.indexType != SWGB_INDEX_TYPE_NONE && (i0 >= D.vertexCount || i1 >= D.vertexCount || i2 >= D.vertexCount))
         {
-            i0 = fetch_index(D, 3 * t + 0); i1 = fetch_index(D, 3 * t + 1); i2 = fetch_index(D, 3 * t + 2);
-            if(i0 >= D.vertexCount || i1 >= D.vertexCount || i2 >= D.vertexCount)
-            {
-                atomicOr(D.error, ERR_INDEX_RANGE);
-                ok = false;
-            }
-        }
-        else
-        {
-            i0 = 3 * t + 0; i1 = 3 * t + 1; i2 = 3 * t + 2;
+            atomicOr(D.error, ERR_INDEX_RANGE);
+            ok = false;
         }
         if(ok)
         {
@@ -1078,8 +1103,7 @@ __device__ int setup_batch_triangle(const DrawParams &D, SH &S, int ti, uint32_t
         }
         else
         {
-            if(D.indexType == SWGB_INDEX_TYPE_NONE) { iv0 = 3 * t; iv1 = 3 * t + 1; iv2 = 3 * t + 2; }
-            else { iv0 = fetch_index(D, 3 * t); iv1 = fetch_index(D, 3 * t + 1); iv2 = fetch_index(D, 3 * t + 2); }
+            tri_slots(D, t, iv0, iv1, iv2);
             float4 a = D.ptv[(size_t)iv0 * 4 + 1], b = D.ptv[(size_t)iv1 * 4 + 1], c = D.ptv[(size_t)iv2 * 4 + 1];
             X[0] = __float_as_int(a.x); X[1] = __float_as_int(b.x); X[2] = __float_as_int(c.x);
             Y[0] = __float_as_int(a.y); Y[1] = __float_as_int(b.y); Y[2] = __float_as_int(c.y);
@@ -1145,8 +1169,7 @@ __device__ int setup_batch_triangle(const DrawParams &D, SH &S, int ti, uint32_t
 
     // plane equations from the post-transform vertices (L2 resident)
     uint32_t i0, i1, i2;
-    if(D.indexType == SWGB_INDEX_TYPE_NONE) { i0 = 3 * t; i1 = 3 * t + 1; i2 = 3 * t + 2; }
-    else { i0 = fetch_index(D, 3 * t); i1 = fetch_index(D, 3 * t + 1); i2 = fetch_index(D, 3 * t + 2); }
+    tri_slots(D, t, i0, i1, i2);
     const float4 c0 = D.ptv[(size_t)i0 * 4], c1 = D.ptv[(size_t)i1 * 4], c2 = D.ptv[(size_t)i2 * 4];
     // sort by minimum y, then maximum w (SetupRoutine.cpp:270-294)
     int o0 = 0, o1 = 1, o2 = 2, tt;
@@ -1984,7 +2007,9 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
 {
     memset(&D, 0, sizeof(D));
     if(st->precision_profile != SWGB_PRECISION_CMAKE) return set_error(SWGB_UNSUPPORTED_STATE, "only the CMake precision profile is implemented");
-    if(st->topology != SWGB_TOPOLOGY_TRIANGLE_LIST) return set_error(SWGB_UNSUPPORTED_STATE, "topology");
+    if(st->topology != SWGB_TOPOLOGY_TRIANGLE_LIST && st->topology != SWGB_TOPOLOGY_TRIANGLE_STRIP &&
+       st->topology != SWGB_TOPOLOGY_TRIANGLE_FAN)
+        return set_error(SWGB_UNSUPPORTED_STATE, "topology (triangle list, strip or fan)");
     if(st->sample_count != 1 && st->sample_count != 4) return set_error(SWGB_UNSUPPORTED_STATE, "sample_count (1 or 4)");
     if(st->vertex_shader != SWGB_VS_MVP_PASSTHROUGH) return set_error(SWGB_UNSUPPORTED_STATE, "vertex_shader");
     if(st->fragment_shader != SWGB_FS_VCOLOR && st->fragment_shader != SWGB_FS_TEX_X_VCOLOR) return set_error(SWGB_UNSUPPORTED_STATE, "fragment_shader");
@@ -2020,11 +2045,13 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
     D.indices = a->indices;
     D.firstVertex = a->first_vertex;
     D.baseVertex = a->base_vertex;
+    D.topology = st->topology;
     if(a->index_type == SWGB_INDEX_TYPE_NONE)
-        D.vertexCount = 3u * a->count;
+        D.vertexCount = st->topology == SWGB_TOPOLOGY_TRIANGLE_LIST ? 3u * a->count : a->count + 2u;
     else
     {
-        if(a->index_type != SWGB_INDEX_TYPE_UINT16 && a->index_type != SWGB_INDEX_TYPE_UINT32) return set_error(SWGB_INVALID_ARG, "index_type");
+        if(a->index_type != SWGB_INDEX_TYPE_UINT16 && a->index_type != SWGB_INDEX_TYPE_UINT32 && a->index_type != SWGB_INDEX_TYPE_UINT8)
+            return set_error(SWGB_INVALID_ARG, "index_type");
         if(!a->indices) return set_error(SWGB_INVALID_ARG, "indices");
         if(a->vertex_count == 0) return set_error(SWGB_INVALID_ARG, "indexed draws need vertex_count");
         D.vertexCount = a->vertex_count;
@@ -2404,8 +2431,10 @@ void draw_reads(const swgb_pipeline_state &st, const swgb_draw_args &a, const Dr
     }
     if(a.index_type != SWGB_INDEX_TYPE_NONE && a.indices)
     {
-        const uintptr_t lo = (uintptr_t)a.indices, isz = a.index_type == SWGB_INDEX_TYPE_UINT16 ? 2 : 4;
-        out.push_back({lo, lo + (uintptr_t)a.count * 3 * isz});
+        const uintptr_t lo = (uintptr_t)a.indices;
+        const uintptr_t isz = a.index_type == SWGB_INDEX_TYPE_UINT16 ? 2 : (a.index_type == SWGB_INDEX_TYPE_UINT8 ? 1 : 4);
+        const uintptr_t n = D.topology == SWGB_TOPOLOGY_TRIANGLE_LIST ? (uintptr_t)a.count * 3 : (uintptr_t)a.count + 2;
+        out.push_back({lo, lo + n * isz});
     }
     if(D.fs == SWGB_FS_TEX_X_VCOLOR)
     {

@@ -106,8 +106,7 @@ class DeviceScene:
         self.scene = scene
         self.device = torch.device(device)
         self.vertices = torch.from_numpy(np.ascontiguousarray(scene.vertices)).to(self.device)
-        self.indices = None if scene.indices is None else torch.from_numpy(
-            np.ascontiguousarray(scene.indices).view(np.int32)).to(self.device)
+        self.indices = None if scene.indices is None else torch.from_numpy(scenes.index_bytes(scene)).to(self.device)
         self.levels = [torch.from_numpy(np.ascontiguousarray(l)).to(self.device) for l in scene.texture_levels]
         cdtype = {abi.FORMAT_R8G8B8A8_UNORM: torch.uint8, abi.FORMAT_R32G32B32A32_SFLOAT: torch.float32,
                   abi.FORMAT_R16G16B16A16_SFLOAT: torch.float16}[scene.color_format]

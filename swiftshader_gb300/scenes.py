@@ -26,7 +26,7 @@ class Scene:
     width: int
     height: int
     vertices: np.ndarray              # float32 [N, 10]
-    indices: np.ndarray = None        # uint32 [3T] or None (non-indexed)
+    indices: np.ndarray = None        # uint8/uint16/uint32 index buffer or None (non-indexed)
     tri_count: int = 0
     mvp: np.ndarray = None            # float32 [4, 4] row-major math matrix
     fragment_shader: int = abi.FS_VCOLOR
@@ -43,6 +43,9 @@ class Scene:
     viewport: tuple = None            # (x, y, w, h) default full framebuffer
     scissor: tuple = None             # (x, y, w, h)
     samples: int = 1                  # 1 or 4 (4x MSAA: one plane per sample)
+    topology: int = abi.TOPOLOGY_TRIANGLE_LIST
+    first_vertex: int = 0
+    base_vertex: int = 0
 
     @property
     def vertex_count(self):
@@ -298,7 +301,7 @@ def build_state(scene, color_ptr, depth_ptr, vertex_ptr, level_ptrs=None, color_
     """PipelineState for a scene given buffer addresses (device pointers for
     the GB300 path, host pointers for the oracle)."""
     st = abi.PipelineState()
-    st.topology = abi.TOPOLOGY_TRIANGLE_LIST
+    st.topology = scene.topology
     st.attrib_count = 3
     st.attribs[0] = abi.VertexAttrib(abi.FORMAT_R32G32B32A32_SFLOAT, 0, 0, 0)
     st.attribs[1] = abi.VertexAttrib(abi.FORMAT_R32G32B32A32_SFLOAT, 0, 16, 0)
@@ -347,21 +350,51 @@ def build_state(scene, color_ptr, depth_ptr, vertex_ptr, level_ptrs=None, color_
     return st
 
 
+INDEX_TYPES = {np.dtype(np.uint8): abi.INDEX_TYPE_UINT8, np.dtype(np.uint16): abi.INDEX_TYPE_UINT16,
+               np.dtype(np.uint32): abi.INDEX_TYPE_UINT32}
+
+
 def build_args(scene, index_ptr=None):
     a = abi.DrawArgs()
     a.count = scene.tri_count
-    a.base_vertex = 0
-    a.first_vertex = 0
+    a.base_vertex = scene.base_vertex
+    a.first_vertex = scene.first_vertex
     if scene.indices is None:
         a.index_type = abi.INDEX_TYPE_NONE
         a.indices = None
     else:
-        a.index_type = abi.INDEX_TYPE_UINT32
+        a.index_type = INDEX_TYPES[np.asarray(scene.indices).dtype]
         a.indices = index_ptr
     a.vertex_count = scene.vertex_count
     a.render_area_x, a.render_area_y = 0, 0
     a.render_area_width, a.render_area_height = scene.width, scene.height
     return a
+
+
+def index_bytes(scene):
+    """The scene's index buffer as raw bytes (uint8 array), any index type."""
+    return np.ascontiguousarray(scene.indices).view(np.uint8)
+
+
+def strip_fan_scene(topology, n_tris=300, width=96, height=80, indexed=None, seed_index=50):
+    """Random clip-space triangles (as scene_small) assembled as a triangle
+    strip or fan over n_tris + 2 vertices; indexed with a shuffled index
+    buffer of the given dtype (uint8 / uint16 / uint32) or non-indexed."""
+    rng = _rng(seed_index)
+    nv = n_tris + 2
+    v = random_triangles(rng, (nv + 2) // 3)[:nv]
+    if topology == abi.TOPOLOGY_TRIANGLE_FAN:
+        v[0, 0:3] = (0.0, 0.0, 0.5)  # fan centre inside the frame
+    indices = None
+    if indexed is not None:
+        perm = rng.permutation(nv)
+        verts = np.empty_like(v)
+        verts[perm] = v
+        v = verts
+        indices = perm.astype(indexed)
+    return Scene(name="topo%d_%d_%s" % (topology, n_tris, "none" if indexed is None else np.dtype(indexed).name),
+                 width=width, height=height, vertices=v, indices=indices, tri_count=n_tris, topology=topology,
+                 cull_mode=abi.CULL_BACK)
 
 
 def attachment_shapes(scene):

@@ -248,3 +248,21 @@ def test_unsupported_states_are_rejected(gpu_lib):
     with pytest.raises(SwgbError) as e:
         r.draw_adjoint(ds.state(), ds.args(), a)
     assert e.value.status == abi.UNSUPPORTED_STATE
+
+
+def test_adjoint_of_indexed_strip(gpu_lib):
+    """Triangle-strip assembly (uint16 indices) in the adjoint: vertex
+    colour and position gradients against the FP64 reference."""
+    import torch
+    from swiftshader_gb300 import Renderer, adjoint
+    sc = scenes.strip_fan_scene(abi.TOPOLOGY_TRIANGLE_STRIP, n_tris=120, indexed=np.uint16)
+    sc.color_format = abi.FORMAT_R32G32B32A32_SFLOAT
+    sc.cull_mode = abi.CULL_NONE
+    r = Renderer(0)
+    verts, _ = device_inputs(sc)
+    color = adjoint.render(r, sc, verts)
+    target = torch.full_like(color, 0.3)
+    ((color - target) ** 2).sum().backward()
+    G = (2.0 * (color - target)).detach().cpu().numpy()
+    gref, _ = reference(sc, G)
+    compare(gref, verts.grad, [])

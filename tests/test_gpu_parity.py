@@ -241,3 +241,22 @@ def test_sphere_views_msaa_reduced(gpu_lib):
     s = scenes.scene_sphere_views(3, width=96, height=96, mesh=mesh, levels=levels)
     s.samples = 4
     check_scene(s, gpu_lib)
+
+
+@pytest.mark.parametrize("topology", [abi.TOPOLOGY_TRIANGLE_STRIP, abi.TOPOLOGY_TRIANGLE_FAN])
+@pytest.mark.parametrize("index_dtype", [None, np.uint8, np.uint16, np.uint32])
+def test_strips_and_fans(gpu_lib, topology, index_dtype):
+    """Triangle strips and fans (setBatchIndices, first vertex provoking) with
+    every index type, back faces culled."""
+    check_scene(scenes.strip_fan_scene(topology, n_tris=240, indexed=index_dtype), gpu_lib)
+
+
+def test_strip_with_first_and_base_vertex(gpu_lib):
+    sc = scenes.strip_fan_scene(abi.TOPOLOGY_TRIANGLE_STRIP, n_tris=150, indexed=np.uint16)
+    sc.vertices = np.concatenate([np.zeros((5, scenes.VERTEX_FLOATS), np.float32), sc.vertices])
+    sc.base_vertex = 5
+    check_scene(sc, gpu_lib)
+    nd = scenes.strip_fan_scene(abi.TOPOLOGY_TRIANGLE_FAN, n_tris=150)
+    nd.vertices = np.concatenate([np.zeros((9, scenes.VERTEX_FLOATS), np.float32), nd.vertices])
+    nd.first_vertex = 9
+    check_scene(nd, gpu_lib)
