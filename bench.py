@@ -190,6 +190,12 @@ def run_ours(args):
             import torch.distributed as dist
             dist.barrier()
 
+    # raster configuration chosen by the library's autotuner on this frame
+    tune = None
+    if not args.no_autotune:
+        ds.clear()
+        tune = autotune_summary(*r.autotune([st], [a], batched=False))
+
     # warm-up
     for _ in range(args.warmup):
         ds.clear()
@@ -270,7 +276,7 @@ def run_ours(args):
     batched = None
     if args.workload == "heightfield" and not args.no_batched:
         del h_vert, h_idx, h_lv, h_color, h_depth
-        _, _, batched = measure_batch(r, stream, flush, BATCH_REDUCED, 3, 1, 2, dev)
+        _, _, batched = measure_batch(r, stream, flush, BATCH_REDUCED, 3, 1, 2, dev, tune=not args.no_autotune)
         batched["config"]["note"] = ("reduced-size sample of the batch workload (triangles log-uniform in "
                                      "[16, 1024] instead of [16, 65536]); --workload batch runs the full one")
 
@@ -322,6 +328,7 @@ def run_ours(args):
                 "ms_per_step": round(e2e_ms, 4), "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
         "clocks": clk,
+        "raster_config": tune,
     }
     traffic = os.path.join(ROOT, "profiles", "raster_traffic.json")
     if os.path.exists(traffic):
@@ -364,15 +371,25 @@ def time_steps(stream, flush, steps, body):
     return [s.elapsed_time(e) for s, e in zip(starts, ends)]
 
 
-def measure_batch(r, stream, flush, params, steps, warmup, per_draw_steps, dev, world=1, rank=0):
+def autotune_summary(best, table):
+    return {"best": best, "candidates_ms": {"%s hiz%d" % (c["bin"], c["hiz"]): round(ms, 3) for c, ms in table},
+            "how": "swgb_autotune: one warm-up and one CUDA-event-timed run per candidate, attachments restored between"}
+
+
+def measure_batch(r, stream, flush, params, steps, warmup, per_draw_steps, dev, world=1, rank=0, tune=True):
     """Batched vs per-draw on the atlas workload: one swgb_draw_batch call per
-    step against one swgb_draw per draw, same draws, same kernels' work.  On
+    step against one swgb_draw per draw, same draws, same kernels' work (the
+    raster configuration the autotuner picks for the batch serves both).  On
     N ranks each rank draws its longest-processing-time-first share."""
     from swiftshader_gb300 import DeviceBatch, scenes, shard
     b = scenes.scene_batch(**params)
     if world > 1:
         b = b.subset(shard.lpt_partition(shard.draw_costs(b.tris, b.sides), world)[rank])
     db = DeviceBatch(b, dev)
+    tuned = None
+    if tune:
+        db.clear()
+        tuned = autotune_summary(*r.autotune(db.states, db.args, batched=True))
 
     def batched():
         db.clear()
@@ -407,7 +424,7 @@ def measure_batch(r, stream, flush, params, steps, warmup, per_draw_steps, dev, 
         "gfrag_per_s": round(per_step["fragments_tested"] / (mb * 1e-3) / 1e9, 3),
         "mtri_per_s": round(per_step["triangles_in"] / (mb * 1e-3) / 1e6, 2),
         "gpu_launches_per_step": launches / steps, "steps": steps, "per_draw_steps": per_draw_steps,
-        "counters_per_step": per_step,
+        "counters_per_step": per_step, "raster_config": tuned,
     }
 
 
@@ -509,7 +526,7 @@ def run_batch(args):
         torch.distributed.barrier()
     params = dict(BATCH_FULL, n_draws=args.batch_draws, tri_max=args.batch_tri_max)
     b, db, res = measure_batch(r, stream, flush, params, args.steps, args.warmup,
-                               0 if args.no_per_draw else min(args.steps, 2), dev, world, rank)
+                               0 if args.no_per_draw else min(args.steps, 2), dev, world, rank, tune=not args.no_autotune)
     clk = clocks.stop()
     # kernel-level timing: the batch as direct launches (timing disables the graph)
     r.set_kernel_timing(True)
@@ -696,6 +713,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-vs-per-draw sample")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint / forward timings")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default raster configuration (16x16 bins, hiz on)")
     ap.add_argument("--batch-draws", type=int, default=BATCH_FULL["n_draws"], help="--workload batch: draws")
     ap.add_argument("--batch-tri-max", type=int, default=BATCH_FULL["tri_max"], help="--workload batch: largest draw")
     ap.add_argument("--no-per-draw", action="store_true", help="--workload batch: skip the per-draw comparison")

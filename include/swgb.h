@@ -195,7 +195,7 @@ typedef struct swgb_pipeline_state {
     uint32_t src_color_factor, dst_color_factor, color_blend_op;
     uint32_t src_alpha_factor, dst_alpha_factor, alpha_blend_op;
     uint32_t color_write_mask; /* VkColorComponentFlags, 0xF = RGBA        */
-    uint32_t sample_count;     /* 1 (4 = MSAA, not yet implemented)        */
+    uint32_t sample_count;     /* 1, or 4 (4x MSAA, standard sample locations) */
     /* attachments (vk::Attachments -> DrawData colorBuffer/depthBuffer) */
     void *color;
     uint32_t color_pitch_bytes;
@@ -347,6 +347,42 @@ swgb_status swgb_draw_adjoint(swgb_ctx *ctx, const swgb_pipeline_state *state, c
  * may be shared between draws). */
 swgb_status swgb_draw_adjoint_batch(swgb_ctx *ctx, const swgb_pipeline_state *states, const swgb_draw_args *args,
                                     const swgb_adjoint_args *adjs, uint32_t n);
+
+/* Raster configuration of a context.  No counterpart in the reference, whose
+ * work split is fixed (128-primitive batches, 16 row-interleaved clusters,
+ * src/Device/Renderer.cpp:551-662, src/Device/Config.hpp).  It chooses how
+ * swgb_draw and swgb_draw_batch tile the framebuffer; every configuration
+ * gives the same attachments and counters bit for bit.
+ *   bin_width x bin_height: the screen bin one raster warp owns, one of
+ *     16x16 (default), 32x16, 32x32.  Four-sample draws always use 16x16.
+ *   hiz: 1 (default) rejects a triangle's fragments in a bin without
+ *     expanding them when the bin's depth bound proves every one fails a
+ *     LESS / LESS_OR_EQUAL / GREATER / GREATER_OR_EQUAL test; 0 expands them. */
+typedef struct swgb_raster_config {
+    uint32_t bin_width;
+    uint32_t bin_height;
+    uint32_t hiz;
+    uint32_t reserved;
+} swgb_raster_config;
+swgb_status swgb_ctx_set_raster_config(swgb_ctx *ctx, const swgb_raster_config *config);
+swgb_status swgb_ctx_get_raster_config(swgb_ctx *ctx, swgb_raster_config *config);
+
+/* Autotuner of the raster configuration.  No counterpart in the reference.
+ * It runs the n draws (one swgb_draw_batch when batched != 0, else one
+ * swgb_draw each) under every candidate configuration -- each supported bin
+ * shape, with hiz on and off -- one untimed warm-up run and one run timed
+ * with CUDA events on the context's stream per candidate, and sets the
+ * context's configuration to the fastest.  The attachment bytes the draws
+ * can touch are copied to a temporary device buffer first and restored
+ * before every run, so on return the attachments hold the draws' result
+ * exactly once (as one swgb_draw_batch / n swgb_draw calls would leave them).
+ * The temporary buffer is as large as those attachment bytes; it is freed
+ * before returning.  ms[] (room for SWGB_AUTOTUNE_CANDIDATES entries, may be
+ * NULL) receives each candidate's time and candidates[] (may be NULL) the
+ * candidates, in the same order.  Synchronises the context's stream. */
+#define SWGB_AUTOTUNE_CANDIDATES 6
+swgb_status swgb_autotune(swgb_ctx *ctx, const swgb_pipeline_state *states, const swgb_draw_args *args, uint32_t n,
+                          int batched, swgb_raster_config *best, swgb_raster_config *candidates, double *ms);
 
 /* Waits for every draw enqueued so far (Renderer::synchronize). */
 swgb_status swgb_sync(swgb_ctx *ctx);

@@ -14,7 +14,8 @@ _lib = None
 EXPORTS = ["swgb_abi_version", "swgb_last_error", "swgb_ctx_create", "swgb_ctx_destroy",
            "swgb_ctx_set_stream", "swgb_draw", "swgb_draw_batch", "swgb_sync", "swgb_get_counters",
            "swgb_reset_counters", "swgb_launch_count", "swgb_set_kernel_timing", "swgb_get_kernel_times",
-           "swgb_draw_noalloc", "swgb_draw_adjoint", "swgb_draw_adjoint_batch", "swgb_plan_batch"]
+           "swgb_draw_noalloc", "swgb_draw_adjoint", "swgb_draw_adjoint_batch", "swgb_plan_batch",
+           "swgb_ctx_set_raster_config", "swgb_ctx_get_raster_config", "swgb_autotune"]
 
 
 class SwgbError(RuntimeError):
@@ -67,6 +68,13 @@ def load(path=None):
     L.swgb_plan_batch.argtypes = [C.POINTER(abi.PipelineState), C.POINTER(abi.DrawArgs), C.c_uint32,
                                   C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
     L.swgb_plan_batch.restype = C.c_int
+    L.swgb_ctx_set_raster_config.argtypes = [C.c_void_p, C.POINTER(abi.RasterConfig)]
+    L.swgb_ctx_set_raster_config.restype = C.c_int
+    L.swgb_ctx_get_raster_config.argtypes = [C.c_void_p, C.POINTER(abi.RasterConfig)]
+    L.swgb_ctx_get_raster_config.restype = C.c_int
+    L.swgb_autotune.argtypes = [C.c_void_p, C.POINTER(abi.PipelineState), C.POINTER(abi.DrawArgs), C.c_uint32, C.c_int,
+                                C.POINTER(abi.RasterConfig), C.POINTER(abi.RasterConfig), C.POINTER(C.c_double)]
+    L.swgb_autotune.restype = C.c_int
     if L.swgb_abi_version() != 2:
         raise OSError("libswgb ABI version mismatch")
     _lib = L

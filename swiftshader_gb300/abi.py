@@ -133,3 +133,15 @@ class AdjointArgs(C.Structure):
                 ("grad_color_slice_bytes", C.c_uint64), ("clear_color", C.c_float * 4), ("clear_depth", C.c_float),
                 ("reserved1", C.c_uint32), ("grad_texels", C.c_void_p * MAX_MIP_LEVELS),
                 ("grad_vertices", C.c_void_p * MAX_ATTRIBS)]
+
+
+class RasterConfig(C.Structure):
+    """swgb_raster_config: the bin one raster warp owns and depth rejection."""
+    _fields_ = [("bin_width", C.c_uint32), ("bin_height", C.c_uint32), ("hiz", C.c_uint32), ("reserved", C.c_uint32)]
+
+    def as_dict(self):
+        return {"bin": "%dx%d" % (self.bin_width, self.bin_height), "hiz": int(self.hiz)}
+
+
+BIN_SHAPES = ((16, 16), (32, 16), (32, 32))
+AUTOTUNE_CANDIDATES = 6

@@ -1,6 +1,10 @@
 """Builds libswgb.so in-tree with nvcc for sm_103a.
 
-The library is compiled with -ftz=true -prec-div=true -prec-sqrt=true
+Four translation units are compiled in parallel and linked into one library:
+swgb_draw.cu (vertex, setup and adjoint kernels, host side, C-ABI) and
+swgb_raster.cu once per colour format (the raster kernel variants).
+
+Every unit is compiled with -ftz=true -prec-div=true -prec-sqrt=true
 -fmad=false: subnormals flush like the reference's FTZ/DAZ worker threads,
 divisions are IEEE-rounded, and only the explicit fused multiply-adds of the
 kernels (the reference's MulAdd) are fused.
@@ -13,12 +17,16 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libswgb.so")
-SOURCES = [os.path.join(CSRC, "swgb_draw.cu")]
-DEPS = SOURCES + [os.path.join(CSRC, "swgb_numeric.cuh"), os.path.join(ROOT, "include", "swgb.h")]
+# (source, extra defines, object name)
+UNITS = [("swgb_draw.cu", [], "swgb_draw.o")] + [
+    ("swgb_raster.cu", ["-DSWGB_RASTER_CF=%d" % cf], "swgb_raster_cf%d.o" % cf) for cf in range(3)]
+SOURCES = [os.path.join(CSRC, u) for u in ("swgb_draw.cu", "swgb_raster.cu")]
+DEPS = SOURCES + [os.path.join(CSRC, h) for h in ("swgb_kernels.cuh", "swgb_numeric.cuh", "swgb_adjoint.cuh", "swgb.map")] + \
+    [os.path.join(ROOT, "include", "swgb.h")]
 
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo", "-O3", "-std=c++17",
               "-ftz=true", "-prec-div=true", "-prec-sqrt=true", "-fmad=false",
-              "-Xcompiler", "-fPIC", "-shared", "-diag-suppress", "177"]
+              "-Xcompiler", "-fPIC", "-diag-suppress", "177"]
 
 
 def nvcc():
@@ -36,15 +44,33 @@ def up_to_date():
 
 
 def build(force=False, verbose=False):
-    """Compiles the extension if a source is newer than the library."""
+    """Compiles the library if a source is newer than it (units in parallel)."""
     os.makedirs(BUILD, exist_ok=True)
     if not force and up_to_date():
         return LIB
-    tmp = LIB + ".tmp%d" % os.getpid()
-    cmd = [nvcc()] + NVCC_FLAGS + ["-o", tmp] + SOURCES
+    tag = ".tmp%d" % os.getpid()
+    procs, objs = [], []
+    for src, defs, obj in UNITS:
+        o = os.path.join(BUILD, obj[:-2] + tag + ".o")
+        cmd = [nvcc()] + NVCC_FLAGS + defs + ["-c", "-o", o, os.path.join(CSRC, src)]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        procs.append((subprocess.Popen(cmd), cmd))
+        objs.append(o)
+    failed = [cmd for p, cmd in procs if p.wait() != 0]
+    if failed:
+        for o in objs:
+            if os.path.exists(o):
+                os.remove(o)
+        raise subprocess.CalledProcessError(1, failed[0])
+    tmp = LIB[:-3] + tag + ".so"
+    cmd = [nvcc(), "-gencode", "arch=compute_103a,code=sm_103a", "-shared",
+           "-Xlinker", "--version-script=" + os.path.join(CSRC, "swgb.map"), "-o", tmp] + objs
     if verbose:
-        print(" ".join(cmd))
+        print(" ".join(cmd), flush=True)
     subprocess.check_call(cmd)
+    for o in objs:
+        os.remove(o)
     os.replace(tmp, LIB)
     return LIB
 

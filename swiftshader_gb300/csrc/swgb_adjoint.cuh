@@ -83,6 +83,7 @@ struct AdjShared {
     uint16_t fill[BIN * BIN];        // blended: fragments recorded per pixel
     uint32_t logCount;               // blended: fragments appended to the region's log
     static constexpr int kSamples = MS;
+    static constexpr int kBW = BIN, kBH = BIN;
 };
 
 // A bin's pixels may be split between four warps (quarters of 8x8 pixels,

@@ -58,6 +58,27 @@ class Renderer:
     def synchronize(self):
         check(self._L.swgb_sync(self._ctx), "swgb_sync")
 
+    def set_raster_config(self, bin_width=16, bin_height=16, hiz=True):
+        cfg = abi.RasterConfig(bin_width, bin_height, 1 if hiz else 0, 0)
+        check(self._L.swgb_ctx_set_raster_config(self._ctx, C.byref(cfg)), "swgb_ctx_set_raster_config")
+
+    def raster_config(self):
+        cfg = abi.RasterConfig()
+        check(self._L.swgb_ctx_get_raster_config(self._ctx, C.byref(cfg)), "swgb_ctx_get_raster_config")
+        return cfg.as_dict()
+
+    def autotune(self, states, args, batched=True):
+        """Runs the draws under every raster configuration (swgb_autotune),
+        keeps the fastest on this renderer and returns (best, [(config, ms)])."""
+        n = len(states)
+        S = states if isinstance(states, C.Array) else (abi.PipelineState * n)(*states)
+        A = args if isinstance(args, C.Array) else (abi.DrawArgs * n)(*args)
+        best = abi.RasterConfig()
+        cands = (abi.RasterConfig * abi.AUTOTUNE_CANDIDATES)()
+        ms = (C.c_double * abi.AUTOTUNE_CANDIDATES)()
+        check(self._L.swgb_autotune(self._ctx, S, A, n, 1 if batched else 0, C.byref(best), cands, ms), "swgb_autotune")
+        return best.as_dict(), [(c.as_dict(), float(t)) for c, t in zip(cands, ms)]
+
     def counters(self):
         c = abi.Counters()
         check(self._L.swgb_get_counters(self._ctx, C.byref(c)), "swgb_get_counters")

@@ -22,6 +22,7 @@ STRUCTS = {
     "swgb_draw_args": abi.DrawArgs,
     "swgb_counters": abi.Counters,
     "swgb_adjoint_args": abi.AdjointArgs,
+    "swgb_raster_config": abi.RasterConfig,
 }
 
 
@@ -95,3 +96,15 @@ def test_host_side_errors_without_device(built_lib):
     a.count = 40000
     assert L.swgb_draw_noalloc(C.byref(st), C.byref(a), None) == abi.INVALID_ARG
     assert b"32768" in L.swgb_last_error()
+    # raster configuration: validated on the host
+    assert L.swgb_ctx_set_raster_config(None, None) == abi.INVALID_ARG
+    assert L.swgb_autotune(None, None, None, 0, 1, None, None, None) == abi.INVALID_ARG
+
+
+def test_header_lists_the_bin_shapes():
+    """The shapes the header documents are the ones the Python mirror offers."""
+    text = open(HEADER).read()
+    for w, h in abi.BIN_SHAPES:
+        assert "%dx%d" % (w, h) in text
+    assert "#define SWGB_AUTOTUNE_CANDIDATES %d" % abi.AUTOTUNE_CANDIDATES in text
+    assert abi.AUTOTUNE_CANDIDATES == 2 * len(abi.BIN_SHAPES)
