@@ -404,6 +404,7 @@ uint64_t swgb_launch_count(swgb_ctx *ctx);
 #define SWGB_KERNEL_RASTER 2
 #define SWGB_KERNEL_BATCH 3 /* one graph replay of a batch segment (three kernels) */
 #define SWGB_KERNEL_ADJOINT 4
+#define SWGB_KERNEL_BIN_ORDER 5 /* longest-first bin order of a single draw */
 #define SWGB_KERNEL_KINDS 8
 swgb_status swgb_set_kernel_timing(swgb_ctx *ctx, int enable);
 swgb_status swgb_get_kernel_times(swgb_ctx *ctx, double ms[SWGB_KERNEL_KINDS], uint32_t launches[SWGB_KERNEL_KINDS]);

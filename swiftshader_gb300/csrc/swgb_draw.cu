@@ -70,6 +70,11 @@ struct swgb_ctx {
     size_t polyCap;
     uint32_t *polyCount;
     unsigned int *binQueue;
+    int *binDiff;          // longest-first bin order of single draws: difference array and order
+    size_t binDiffCap;
+    uint32_t *binOrder;
+    size_t binOrderCap;
+    bool binOrderAttr;
     int rasterBlocks[NRASTER];  // persistent raster grid per kernel variant: SMs x resident blocks per SM
     swgb_raster_config rasterConfig;  // bin shape and depth rejection of single-sample draws
     unsigned long long *counters;
@@ -247,6 +252,8 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
     D.blend = st->blend_enable && (opC != OP_SRC_EXT || opA != OP_SRC_EXT) && st->color_write_mask != 0;
     D.srcC = st->src_color_factor; D.dstC = st->dst_color_factor; D.opC = opC;
     D.srcA = st->src_alpha_factor; D.dstA = st->dst_alpha_factor; D.opA = opA;
+    D.blendAlpha = D.srcC == SWGB_BLEND_SRC_ALPHA && D.dstC == SWGB_BLEND_ONE_MINUS_SRC_ALPHA && D.opC == SWGB_BLEND_OP_ADD &&
+                   D.srcA == SWGB_BLEND_SRC_ALPHA && D.dstA == SWGB_BLEND_ONE_MINUS_SRC_ALPHA && D.opA == SWGB_BLEND_OP_ADD;
     D.writeMask = st->color_write_mask & 0xFu;
     D.ms = (int)st->sample_count;
     D.colorSlice = st->color_slice_bytes;
@@ -379,8 +386,11 @@ void timed_launch(swgb_ctx *ctx, int kind, F &&launch)
     }
 }
 
-// Grows the context's scratch for draw D and points D at it.
-swgb_status prepare_scratch(swgb_ctx *ctx, DrawParams &D)
+constexpr size_t BIN_ORDER_SMEM = 200 * 1024;  // bin grids up to 51200 cells are ordered
+
+// Grows the context's scratch for draw D and points D at it; with order, also
+// the scratch of the longest-first bin order when it applies.
+swgb_status prepare_scratch(swgb_ctx *ctx, DrawParams &D, bool order = true)
 {
     swgb_status s;
     if((s = ensure(ctx->ptv, ctx->ptvCap, (size_t)D.vertexCount * 4, "ptv")) != SWGB_OK) return s;
@@ -415,6 +425,26 @@ swgb_status prepare_scratch(swgb_ctx *ctx, DrawParams &D)
         if((s = raster_grids(ctx->device, true, ctx->rasterBlocks)) != SWGB_OK) return s;
         ctx->rasterAttr = true;
     }
+    // Longest-first bin order when the bins outnumber the resident raster
+    // warps (with fewer, every bin starts at once) and the bin grid's counts
+    // fit k_bin_order's shared memory.
+    const size_t nbins = (size_t)D.binsX * D.binsY, cells = (size_t)(D.binsX + 1) * (D.binsY + 1);
+    D.binDiff = nullptr;
+    D.binOrder = nullptr;
+    if(order && nbins > (size_t)ctx->rasterBlocks[raster_variant(D)] * RASTER_WARPS && cells * sizeof(int) <= BIN_ORDER_SMEM)
+    {
+        if(!ctx->binOrderAttr)
+        {
+            if((s = cuda_check(cudaFuncSetAttribute(k_bin_order, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BIN_ORDER_SMEM),
+                               "bin order smem attribute")) != SWGB_OK)
+                return s;
+            ctx->binOrderAttr = true;
+        }
+        if((s = ensure(ctx->binDiff, ctx->binDiffCap, cells, "bin counts")) != SWGB_OK) return s;
+        if((s = ensure(ctx->binOrder, ctx->binOrderCap, nbins, "bin order")) != SWGB_OK) return s;
+        D.binDiff = ctx->binDiff;
+        D.binOrder = ctx->binOrder;
+    }
     return SWGB_OK;
 }
 
@@ -435,6 +465,11 @@ swgb_status enqueue(swgb_ctx *ctx, DrawParams &D)
     timed_launch(ctx, SWGB_KERNEL_VERTEX, [&] { k_vertex<<<(nv + 255) / 256, 256, 0, ctx->stream>>>(D, nv); });
     const uint32_t setupBlocks = (uint32_t)((D.count + SETUP_THREADS - 1) / SETUP_THREADS);
     timed_launch(ctx, SWGB_KERNEL_SETUP, [&] { k_setup<<<setupBlocks, SETUP_THREADS, 0, ctx->stream>>>(D); });
+    if(D.binOrder)
+    {
+        const size_t smem = (size_t)(D.binsX + 1) * (D.binsY + 1) * sizeof(int);
+        timed_launch(ctx, SWGB_KERNEL_BIN_ORDER, [&] { k_bin_order<<<1, BIN_ORDER_THREADS, smem, ctx->stream>>>(D); });
+    }
     if(D.binsX > 0 && D.binsY > 0)
     {
         uint32_t blocks = (uint32_t)((D.binsX * D.binsY + RASTER_WARPS - 1) / RASTER_WARPS);
@@ -940,6 +975,13 @@ swgb_status draw_batch(swgb_ctx *ctx, const swgb_pipeline_state *states, const s
     if((s = batch_init(ctx)) != SWGB_OK) return s;
     std::vector<std::pair<uint32_t, uint32_t>> segs;
     segment_batch(draws, src, states, args, segs);
+    // Longest first inside a segment: its draws touch disjoint attachment
+    // bytes, so their order changes no result, and the persistent raster warps
+    // take the bins of the costliest draws (triangles x bins) first.
+    for(const auto &sg : segs)
+        std::stable_sort(draws.begin() + sg.first, draws.begin() + sg.second, [](const DrawParams &a, const DrawParams &b) {
+            return (uint64_t)a.count * (uint64_t)(a.binsX * a.binsY) > (uint64_t)b.count * (uint64_t)(b.binsX * b.binsY);
+        });
     return run_segments(ctx, draws, segs, nullptr);
 }
 
@@ -1040,7 +1082,7 @@ swgb_status draw_adjoint(swgb_ctx *ctx, const swgb_pipeline_state *st, const swg
     if((s = bake_adjoint(st, a, g, D, A)) != SWGB_OK) return s;
     if(D.count == 0) return SWGB_OK;
     if((s = adjoint_init(ctx)) != SWGB_OK) return s;
-    if((s = prepare_scratch(ctx, D)) != SWGB_OK) return s;
+    if((s = prepare_scratch(ctx, D, false)) != SWGB_OK) return s;
     if((s = ensure(ctx->ptv64, ctx->ptv64Cap, (size_t)D.vertexCount * 6, "fp64 clip coordinates")) != SWGB_OK) return s;
     D.ptv64 = ctx->ptv64;
     const uint32_t nv = D.vertexCount;
@@ -1212,6 +1254,8 @@ swgb_status swgb_ctx_destroy(swgb_ctx *c)
     cudaSetDevice(c->device);
     if(c->stream) cudaStreamSynchronize(c->stream);
     cudaFree(c->ptv);
+    cudaFree(c->binDiff);
+    cudaFree(c->binOrder);
     cudaFree(c->triBox);
     cudaFree(c->triInfo);
     cudaFree(c->spans);

@@ -105,6 +105,7 @@ struct DrawParams {
     float minDepthClamp, maxDepthClamp;
     int blend;
     uint32_t srcC, dstC, opC, srcA, dstA, opA;
+    int blendAlpha;  // SRC_ALPHA / ONE_MINUS_SRC_ALPHA / ADD on colour and alpha
     uint32_t writeMask;
     int fs;
     int ms;       // samples per pixel: 1 or 4
@@ -136,6 +137,8 @@ struct DrawParams {
     int4 *superBox;       // union of SUPER consecutive chunk boxes (x0, y0, x1, y1)
     int nsuper;
     unsigned int *binQueue;  // next bin for the persistent raster warps
+    int *binDiff;         // single draws: 2D difference array of triangle boxes over the bin grid, (binsY+1) x (binsX+1), or null
+    uint32_t *binOrder;   // single draws: bins longest first (k_bin_order), or null for raster order
     uint32_t *spans;      // left | right << 16 per triangle row
     unsigned long long *spanCount;
     uint64_t spanCapacity;
@@ -249,6 +252,8 @@ __global__ void k_vertex(const __grid_constant__ DrawParams D, uint32_t nverts)
     }
     for(uint32_t j = i; j < (uint32_t)D.nsuper; j += gridDim.x * blockDim.x)
         D.superBox[j] = make_int4(0x7FFFFFFF, 0x7FFFFFFF, (int)0x80000000, (int)0x80000000);
+    if(D.binDiff)
+        for(uint32_t j = i; j < (uint32_t)((D.binsX + 1) * (D.binsY + 1)); j += gridDim.x * blockDim.x) D.binDiff[j] = 0;
     if(i < nverts) vertex_body(D, i);
 }
 
@@ -681,6 +686,18 @@ __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
     }
     D.triBox[t] = box;  // capacity is a whole number of setup blocks
     D.triInfo[t] = inf;
+    if(D.binDiff && box.x < box.z && box.y < box.w)
+    {
+        // triangles per bin, for the raster's longest-first bin order: the
+        // box's bin rectangle into a 2D difference array (k_bin_order integrates)
+        const int W = D.binsX + 1;
+        const int xa = (box.x - D.binX0) / D.binW, xb = (box.z - 1 - D.binX0) / D.binW + 1;
+        const int ya = (box.y - D.binY0) / D.binH, yb = (box.w - 1 - D.binY0) / D.binH + 1;
+        atomicAdd(&D.binDiff[ya * W + xa], 1);
+        atomicAdd(&D.binDiff[ya * W + xb], -1);
+        atomicAdd(&D.binDiff[yb * W + xa], -1);
+        atomicAdd(&D.binDiff[yb * W + xb], 1);
+    }
 
     // ---- chunk boxes (64 triangles = 2 warps) and counters ------------------
     const bool has = cntVis != 0;
@@ -739,6 +756,54 @@ __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
 
 #ifndef SWGB_RASTER_TU
 __global__ void __launch_bounds__(SETUP_THREADS) k_setup(const __grid_constant__ DrawParams D) { setup_body(D, blockIdx.x); }
+
+// Longest-first order of a draw's bins for the persistent raster warps (the
+// heaviest bins start first, so none starts last and holds the frame's tail):
+// the setup stage's difference array integrated in shared memory into
+// triangles per bin, then bins bucketed by the bit length of their count,
+// heaviest bucket first.  One block; the order inside a bucket is arbitrary,
+// as the bins are independent.
+constexpr int BIN_ORDER_THREADS = 1024;
+__device__ __forceinline__ int bin_order_key(int c) { return c > 0 ? 32 - __clz(c) : 0; }
+
+__global__ void __launch_bounds__(BIN_ORDER_THREADS) k_bin_order(const __grid_constant__ DrawParams D)
+{
+    extern __shared__ int cnt[];  // (binsY + 1) x (binsX + 1)
+    __shared__ uint32_t hist[33], base[33];
+    const int W = D.binsX + 1, H = D.binsY + 1, nb = D.binsX * D.binsY, tid = threadIdx.x;
+    for(int i = tid; i < W * H; i += blockDim.x) cnt[i] = D.binDiff[i];
+    if(tid < 33) hist[tid] = 0;
+    __syncthreads();
+    for(int r = tid; r < H; r += blockDim.x)
+    {
+        int acc = 0;
+        for(int x = 0; x < W; x++) cnt[r * W + x] = (acc += cnt[r * W + x]);
+    }
+    __syncthreads();
+    for(int c = tid; c < W; c += blockDim.x)
+    {
+        int acc = 0;
+        for(int y = 0; y < H; y++) cnt[y * W + c] = (acc += cnt[y * W + c]);
+    }
+    __syncthreads();
+    for(int b = tid; b < nb; b += blockDim.x) atomicAdd(&hist[bin_order_key(cnt[(b / D.binsX) * W + b % D.binsX])], 1u);
+    __syncthreads();
+    if(tid == 0)
+    {
+        uint32_t acc = 0;
+        for(int k = 32; k >= 0; k--)
+        {
+            base[k] = acc;
+            acc += hist[k];
+        }
+    }
+    __syncthreads();
+    for(int b = tid; b < nb; b += blockDim.x)
+    {
+        const uint32_t pos = atomicAdd(&base[bin_order_key(cnt[(b / D.binsX) * W + b % D.binsX])], 1u);
+        D.binOrder[pos] = (uint32_t)b;
+    }
+}
 
 #endif  // SWGB_RASTER_TU
 
@@ -941,7 +1006,9 @@ __device__ __forceinline__ float4 sample_float_2d(const DrawParams &D, float u, 
 
 // sampleFloatFilter (SamplerCore.cpp:1061-1083): trilinear blend by the scalar
 // Frac of the LOD (x86 SSE4.1: lod - floor(lod)).
-__device__ __forceinline__ void sample_float_lane(const DrawParams &D, float lod, float ul, float vl, float out[4], uint32_t &lvMask)
+// Out of line: the raster kernels carry both filtering paths, and the fp32 one
+// inlined would crowd the UNORM8 path's code in the loop.
+static __device__ __noinline__ void sample_float_lane(const DrawParams &D, float lod, float ul, float vl, float out[4], uint32_t &lvMask)
 {
     float4 c = sample_float_2d(D, ul, vl, lod, 0, lvMask);
     if(D.mipLinear)
@@ -993,6 +1060,24 @@ __device__ __forceinline__ float blend_op(uint32_t op, float s, float sf, float 
     case OP_ZERO_EXT: return 0.0f;
     default: return s;
     }
+}
+
+// alphaBlend with any factors and ops (PixelRoutine.cpp:1653-1961).  Out of
+// line, like every rarely taken path of the raster loop.
+static __device__ __noinline__ void blend_generic(const DrawParams &D, const float col[4], const float dst[4], float out[4])
+{
+    float sf[4], df[4];
+#pragma unroll
+    for(int c = 0; c < 3; c++)
+    {
+        sf[c] = blend_factor(D.srcC, col, dst, c);
+        df[c] = blend_factor(D.dstC, col, dst, c);
+    }
+    sf[3] = blend_factor(D.srcA, col, dst, 3);
+    df[3] = blend_factor(D.dstA, col, dst, 3);
+#pragma unroll
+    for(int c = 0; c < 3; c++) out[c] = blend_op(D.opC, col[c], sf[c], dst[c], df[c]);
+    out[3] = blend_op(D.opA, col[3], sf[3], dst[3], df[3]);
 }
 
 __device__ __forceinline__ bool depth_pass(uint32_t op, float zb, float z)
@@ -1059,6 +1144,61 @@ __device__ __forceinline__ float vary(const float4 &a, const float4 &b, int k)
     }
 }
 
+// The span rows of triangle t inside bin rows [rowLo, rowHi) by the reference's
+// edge DDA, for triangles whose rows did not fit the setup stage's span
+// scratch (SetupRoutine::edge, src/Pipeline/SetupRoutine.cpp:550-621).  Out of
+// line: it is rare, and inlined it would crowd the raster loop's code.
+template<class SH>
+__device__ __noinline__ void walk_spans_in_bin(const DrawParams &D, SH &S, int ti, uint32_t t, const TriInfo inf, int by0, int rowLo, int rowHi)
+{
+    constexpr int MS = SH::kSamples;
+    const int n = inf.info & 31, dW = (inf.info >> 5) & 1;
+    uint32_t iv0 = 0, iv1 = 0, iv2 = 0;
+    int32_t X[MAX_POLY], Y[MAX_POLY];
+    if(inf.info & 64)
+    {
+        for(int i = 0; i < n; i++)
+        {
+            int2 q = D.poly[(size_t)inf.slot * MAX_POLY + i];
+            X[i] = q.x; Y[i] = q.y;
+        }
+    }
+    else
+    {
+        tri_slots(D, t, iv0, iv1, iv2);
+        float4 a = D.ptv[(size_t)iv0 * 4 + 1], b = D.ptv[(size_t)iv1 * 4 + 1], c = D.ptv[(size_t)iv2 * 4 + 1];
+        X[0] = __float_as_int(a.x); X[1] = __float_as_int(b.x); X[2] = __float_as_int(c.x);
+        Y[0] = __float_as_int(a.y); Y[1] = __float_as_int(b.y); Y[2] = __float_as_int(c.y);
+    }
+    for(int q = 0; q < MS; q++)
+    {
+        for(int y = rowLo; y < rowHi; y++) S.span[ti][q][y - by0] = 0u;
+        const int32_t dx = MS > 1 ? XF[q] : 0, dy = MS > 1 ? YF[q] : 0;
+        for(int i = 0; i < n; i++)
+        {
+            int ia = i + 1 - dW, ib = i + dW;
+            ia = ia == n ? 0 : ia;
+            ib = ib == n ? 0 : ib;
+            EdgeDDA e;
+            if(!edge_setup(D, X[ia] - dx, Y[ia] - dy, X[ib] - dx, Y[ib] - dy, e)) continue;
+            int ys = max(e.yMin, rowLo), ye = min(e.yMax, rowHi);
+            if(ys >= ye) continue;
+            int32_t dd;
+            int32_t x = edge_x_at(e, ys, &dd);
+            uint16_t *h = reinterpret_cast<uint16_t *>(&S.span[ti][q][0]) + (e.right ? 1 : 0);
+            for(int y = ys; y < ye; y++)
+            {
+                h[2 * (y - by0)] = (uint16_t)clamp_x(D, x);
+                x += e.Q;
+                dd += e.R;
+                int32_t of = (-dd) >> 31;
+                dd -= e.D & of;
+                x -= of;
+            }
+        }
+    }
+}
+
 // R1: one batch triangle -- its span rows inside the bin (from the setup
 // stage's span buffer, or the reference DDA when the buffer was full), its
 // quad rows, and its plane equations (SetupRoutine.cpp:270-548).  Returns the
@@ -1092,50 +1232,7 @@ __device__ int setup_batch_triangle(const DrawParams &D, SH &S, int ti, uint32_t
     else
     {
         // span scratch was full at setup: walk the edges here (SetupRoutine::edge)
-        uint32_t iv0 = 0, iv1 = 0, iv2 = 0;
-        int32_t X[MAX_POLY], Y[MAX_POLY];
-        if(inf.info & 64)
-        {
-            for(int i = 0; i < n; i++)
-            {
-                int2 q = D.poly[(size_t)inf.slot * MAX_POLY + i];
-                X[i] = q.x; Y[i] = q.y;
-            }
-        }
-        else
-        {
-            tri_slots(D, t, iv0, iv1, iv2);
-            float4 a = D.ptv[(size_t)iv0 * 4 + 1], b = D.ptv[(size_t)iv1 * 4 + 1], c = D.ptv[(size_t)iv2 * 4 + 1];
-            X[0] = __float_as_int(a.x); X[1] = __float_as_int(b.x); X[2] = __float_as_int(c.x);
-            Y[0] = __float_as_int(a.y); Y[1] = __float_as_int(b.y); Y[2] = __float_as_int(c.y);
-        }
-        for(int q = 0; q < MS; q++)
-        {
-            for(int y = rowLo; y < rowHi; y++) S.span[ti][q][y - by0] = 0u;
-            const int32_t dx = MS > 1 ? XF[q] : 0, dy = MS > 1 ? YF[q] : 0;
-            for(int i = 0; i < n; i++)
-            {
-                int ia = i + 1 - dW, ib = i + dW;
-                ia = ia == n ? 0 : ia;
-                ib = ib == n ? 0 : ib;
-                EdgeDDA e;
-                if(!edge_setup(D, X[ia] - dx, Y[ia] - dy, X[ib] - dx, Y[ib] - dy, e)) continue;
-                int ys = max(e.yMin, rowLo), ye = min(e.yMax, rowHi);
-                if(ys >= ye) continue;
-                int32_t dd;
-                int32_t x = edge_x_at(e, ys, &dd);
-                uint16_t *h = reinterpret_cast<uint16_t *>(&S.span[ti][q][0]) + (e.right ? 1 : 0);
-                for(int y = ys; y < ye; y++)
-                {
-                    h[2 * (y - by0)] = (uint16_t)clamp_x(D, x);
-                    x += e.Q;
-                    dd += e.R;
-                    int32_t of = (-dd) >> 31;
-                    dd -= e.D & of;
-                    x -= of;
-                }
-            }
-        }
+        walk_spans_in_bin(D, S, ti, t, inf, by0, rowLo, rowHi);
     }
     // quad rows: x range of the row pair over all samples (QuadRasterizer.cpp:96-123), clipped to the bin
     int pre = 0;
@@ -1350,18 +1447,16 @@ __device__ __forceinline__ void rop_pixel(const DrawParams &D, SH &S, int q, int
 #pragma unroll
             for(int c = 0; c < 4; c++) dst[c] = __uint_as_float(color[4 * idx + c]);
         }
-        float sf[4], df[4];
-#pragma unroll
-        for(int c = 0; c < 3; c++)
+        if(D.blendAlpha)
         {
-            sf[c] = blend_factor(D.srcC, col, dst, c);
-            df[c] = blend_factor(D.dstC, col, dst, c);
-        }
-        sf[3] = blend_factor(D.srcA, col, dst, 3);
-        df[3] = blend_factor(D.dstA, col, dst, 3);
+            // SRC_ALPHA, ONE_MINUS_SRC_ALPHA, ADD on colour and alpha: the
+            // general path's arithmetic, inline
+            const float a = col[3], oma = 1.0f - col[3];
 #pragma unroll
-        for(int c = 0; c < 3; c++) out[c] = blend_op(D.opC, col[c], sf[c], dst[c], df[c]);
-        out[3] = blend_op(D.opA, col[3], sf[3], dst[3], df[3]);
+            for(int c = 0; c < 4; c++) out[c] = col[c] * a + dst[c] * oma;
+        }
+        else
+            blend_generic(D, col, dst, out);
     }
     else
     {
@@ -1917,6 +2012,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, (raster_min_blocks<CF, MS, BW,
         if(lane == 0) bin = (int)atomicAdd(D.binQueue, 1u);
         bin = __shfl_sync(0xFFFFFFFFu, bin, 0);
         if(bin >= nbins) break;
+        if(D.binOrder) bin = (int)__ldg(D.binOrder + bin);
         raster_bin<CF, MS, BW, BH, HIZ>(D, S, bin, nQuads, nTested, nPassed, lvMask);
     }
     flush_counters(D.counters, nQuads, nTested, nPassed, lvMask);

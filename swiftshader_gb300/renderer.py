@@ -93,7 +93,7 @@ class Renderer:
     def set_kernel_timing(self, enable):
         check(self._L.swgb_set_kernel_timing(self._ctx, 1 if enable else 0), "swgb_set_kernel_timing")
 
-    KERNEL_NAMES = ("vertex", "setup", "raster", "batch", "adjoint")
+    KERNEL_NAMES = ("vertex", "setup", "raster", "batch", "adjoint", "bin_order")
 
     def kernel_times(self):
         """{kernel: (total ms, launches)} since the last call (synchronises)."""

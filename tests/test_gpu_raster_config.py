@@ -130,3 +130,16 @@ def test_autotune_leaves_one_run(gpu_lib, batched):
     assert_bit_exact(db.depth.cpu().numpy(), d1, "depth")
     assert_bit_exact(db.color.cpu().numpy(), c1, "color")
     assert r.counters() == k1
+
+
+@pytest.mark.parametrize("cfg", [(16, 16, True), (16, 16, False), (32, 16, True)], ids=lambda c: "%dx%d-hiz%d" % c)
+def test_longest_first_bin_order(gpu_lib, cfg):
+    """Frames with more bins than resident raster warps take the longest-first
+    bin order (per-bin triangle counts from the setup stage): small triangles
+    clustered unevenly over a 1920x1088 frame, empty bins included."""
+    s = scenes.scene_small(n_tris=20000, width=1920, height=1088, seed_index=71)
+    rng = np.random.Generator(np.random.PCG64(71))
+    v = s.vertices
+    centers = rng.uniform(-1.0, 1.0, (20000, 2)) ** 3  # denser towards the middle
+    v[:, 0:2] = (np.repeat(centers, 3, axis=0) + rng.uniform(-0.03, 0.03, (60000, 2))).astype(np.float32)
+    check_config(s, cfg)
