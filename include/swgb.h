@@ -286,7 +286,7 @@ swgb_status swgb_plan_batch(const swgb_pipeline_state *states, const swgb_draw_a
  * that must not enter the allocator.  It runs the same kernels as swgb_draw on
  * 'stream' (a cudaStream_t; NULL = the legacy default stream) on the current
  * device, with all scratch taken from one fixed __device__ array of about
- * 14 MiB that every GPU loading this library holds until the process exits.
+ * 17.3 MiB that every GPU loading this library holds until the process exits.
  * Limits: at most SWGB_NOALLOC_MAX_TRIANGLES triangles and
  * SWGB_NOALLOC_MAX_VERTICES transformed vertices per call; larger draws return
  * SWGB_INVALID_ARG.  The first call on a device resolves the array's device

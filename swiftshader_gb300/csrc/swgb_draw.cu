@@ -58,6 +58,8 @@ struct swgb_ctx {
     size_t triBoxCap;
     TriInfo *triInfo;
     size_t triInfoCap;
+    float4 *planes;
+    size_t planesCap;
     uint32_t *spans;
     size_t spansCap;
     unsigned long long *spanCount;
@@ -197,6 +199,7 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
         if(i > 0) D.nv += (int)D.vcomp[i];
     }
     if(D.nv > PLANE_V) return set_error(SWGB_UNSUPPORTED_STATE, "too many varyings");
+    D.planeVec4 = (8 + 3 * D.nv + 3) / 4;
     if(D.nattr < 2 || D.vcomp[1] != 4) return set_error(SWGB_INVALID_ARG, "the fixed FS reads a vec4 colour at location 0");
     D.fs = (int)st->fragment_shader;
     if(D.fs == SWGB_FS_TEX_X_VCOLOR && (D.nattr < 3 || D.nv < 6)) return set_error(SWGB_INVALID_ARG, "textured FS needs a uv varying");
@@ -397,6 +400,7 @@ swgb_status prepare_scratch(swgb_ctx *ctx, DrawParams &D, bool order = true)
     const size_t triSlots = ((size_t)D.count + SETUP_THREADS - 1) / SETUP_THREADS * SETUP_THREADS;
     if((s = ensure(ctx->triBox, ctx->triBoxCap, triSlots, "triangle boxes")) != SWGB_OK) return s;
     if((s = ensure(ctx->triInfo, ctx->triInfoCap, triSlots, "triangle records")) != SWGB_OK) return s;
+    if((s = ensure(ctx->planes, ctx->planesCap, triSlots * (PLANES_STORED / 4), "plane equations")) != SWGB_OK) return s;
     // span rows: 24 per triangle covers typical meshes; triangles beyond the
     // capacity fall back to walking their edges in k_raster
     size_t spanNeed = (size_t)D.count * 24 + 4096;
@@ -409,6 +413,7 @@ swgb_status prepare_scratch(swgb_ctx *ctx, DrawParams &D, bool order = true)
     D.ptv = ctx->ptv;
     D.triBox = ctx->triBox;
     D.triInfo = ctx->triInfo;
+    D.planes = ctx->planes;
     D.spans = ctx->spans;
     D.spanCount = ctx->spanCount;
     D.spanCapacity = ctx->spanRowsLimit ? (ctx->spansCap < ctx->spanRowsLimit ? ctx->spansCap : ctx->spanRowsLimit) : ctx->spansCap;
@@ -491,6 +496,7 @@ struct BatchState {
     double *ptv64 = nullptr; size_t ptv64Cap = 0;  // adjoint segments only
     short4 *triBox = nullptr; size_t triBoxCap = 0;
     TriInfo *triInfo = nullptr; size_t triInfoCap = 0;
+    float4 *planes = nullptr; size_t planesCap = 0;
     short4 *chunk = nullptr; size_t chunkCap = 0;
     int4 *super = nullptr; size_t superCap = 0;
     uint32_t *spans = nullptr; size_t spansCap = 0;
@@ -754,7 +760,7 @@ swgb_status batch_init(swgb_ctx *ctx)
 void batch_free(BatchState *B)
 {
     if(!B) return;
-    cudaFree(B->ptv); cudaFree(B->ptv64); cudaFree(B->triBox); cudaFree(B->triInfo); cudaFree(B->chunk); cudaFree(B->super);
+    cudaFree(B->ptv); cudaFree(B->ptv64); cudaFree(B->triBox); cudaFree(B->triInfo); cudaFree(B->planes); cudaFree(B->chunk); cudaFree(B->super);
     cudaFree(B->spans); cudaFree(B->poly); cudaFree(B->queue); cudaFree(B->desc);
     if(B->stage) cudaFreeHost(B->stage);
     if(B->stageFree) cudaEventDestroy(B->stageFree);
@@ -824,6 +830,7 @@ swgb_status enqueue_segment(swgb_ctx *ctx, std::vector<DrawParams> &draws, uint3
     if(adj && (s = ensure_gen(B.ptv64, B.ptv64Cap, (size_t)verts * 6, B, "batch fp64 clip coordinates")) != SWGB_OK) return s;
     if((s = ensure_gen(B.triBox, B.triBoxCap, (size_t)triSlots, B, "batch boxes")) != SWGB_OK) return s;
     if((s = ensure_gen(B.triInfo, B.triInfoCap, (size_t)triSlots, B, "batch records")) != SWGB_OK) return s;
+    if((s = ensure_gen(B.planes, B.planesCap, (size_t)triSlots * (PLANES_STORED / 4), B, "batch plane equations")) != SWGB_OK) return s;
     if((s = ensure_gen(B.chunk, B.chunkCap, (size_t)triSlots / CHUNK, B, "batch chunks")) != SWGB_OK) return s;
     if((s = ensure_gen(B.super, B.superCap, (size_t)nsuper + 1, B, "batch super boxes")) != SWGB_OK) return s;
     uint64_t tris = 0;
@@ -839,6 +846,7 @@ swgb_status enqueue_segment(swgb_ctx *ctx, std::vector<DrawParams> &draws, uint3
         d.ptv64 = adj ? B.ptv64 + vOff * 6 : nullptr;
         d.triBox = B.triBox + sOff;
         d.triInfo = B.triInfo + sOff;
+        d.planes = B.planes + (size_t)sOff * (PLANES_STORED / 4);
         d.chunkBox = B.chunk + sOff / CHUNK;
         d.superBox = B.super + supOff;
         d.spans = B.spans;
@@ -1160,7 +1168,8 @@ constexpr uint64_t NA_SPAN_ROWS = (uint64_t)NA_TRIS * 24;
 constexpr size_t NA_OFF_PTV = 0;
 constexpr size_t NA_OFF_BOX = na_up(NA_OFF_PTV + (size_t)NA_VERTS * 4 * sizeof(float4));
 constexpr size_t NA_OFF_INFO = na_up(NA_OFF_BOX + (size_t)NA_SLOTS * sizeof(short4));
-constexpr size_t NA_OFF_CHUNK = na_up(NA_OFF_INFO + (size_t)NA_SLOTS * sizeof(TriInfo));
+constexpr size_t NA_OFF_PLANES = na_up(NA_OFF_INFO + (size_t)NA_SLOTS * sizeof(TriInfo));
+constexpr size_t NA_OFF_CHUNK = na_up(NA_OFF_PLANES + (size_t)NA_SLOTS * PLANES_STORED * sizeof(float));
 constexpr size_t NA_OFF_SUPER = na_up(NA_OFF_CHUNK + (size_t)NA_CHUNKS * sizeof(short4));
 constexpr size_t NA_OFF_SPANS = na_up(NA_OFF_SUPER + (size_t)NA_SUPER * sizeof(int4));
 constexpr size_t NA_OFF_POLY = na_up(NA_OFF_SPANS + (size_t)NA_SPAN_ROWS * sizeof(uint32_t));
@@ -1258,6 +1267,7 @@ swgb_status swgb_ctx_destroy(swgb_ctx *c)
     cudaFree(c->binOrder);
     cudaFree(c->triBox);
     cudaFree(c->triInfo);
+    cudaFree(c->planes);
     cudaFree(c->spans);
     cudaFree(c->spanCount);
     cudaFree(c->chunkBox);
@@ -1333,6 +1343,7 @@ swgb_status swgb_draw_noalloc(const swgb_pipeline_state *st, const swgb_draw_arg
     D.ptv = (float4 *)(b + NA_OFF_PTV);
     D.triBox = (short4 *)(b + NA_OFF_BOX);
     D.triInfo = (TriInfo *)(b + NA_OFF_INFO);
+    D.planes = (float4 *)(b + NA_OFF_PLANES);
     D.chunkBox = (short4 *)(b + NA_OFF_CHUNK);
     D.superBox = (int4 *)(b + NA_OFF_SUPER);
     D.spans = (uint32_t *)(b + NA_OFF_SPANS);

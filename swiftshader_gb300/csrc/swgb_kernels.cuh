@@ -133,6 +133,8 @@ struct DrawParams {
     double *ptv64;        // adjoint runs only: clip x, y, w and x/w, y/w in fp64 (6 doubles per vertex), else null
     short4 *triBox;       // pixel box per triangle
     TriInfo *triInfo;
+    float4 *planes;       // plane equations per triangle (PLANES_STORED floats), written by setup
+    int planeVec4;        // float4s of them in use: (8 + 3 * varyings + 3) / 4
     short4 *chunkBox;     // union of the boxes of CHUNK consecutive triangles
     int4 *superBox;       // union of SUPER consecutive chunk boxes (x0, y0, x1, y1)
     int nsuper;
@@ -470,6 +472,112 @@ static __device__ void write_spans(const DrawParams &D, const int32_t *X, const 
 }
 
 // One 256-triangle block of a draw (block index 'blk' within the draw).
+constexpr int PLANE_V = 6;  // varying components with plane equations (colour + uv)
+constexpr int PLANES = 8 + 3 * PLANE_V;
+constexpr int PLANES_STORED = 28;  // PLANES rounded up to whole float4s
+
+__device__ __forceinline__ uint32_t select3(int o, uint32_t a, uint32_t b, uint32_t c) { return o == 0 ? a : (o == 1 ? b : c); }
+
+__device__ __forceinline__ float vary(const float4 &a, const float4 &b, int k)
+{
+    // varying k of a post-transform vertex: float4[2].yzw then float4[3].xyzw
+    switch(k)
+    {
+    case 0: return a.y;
+    case 1: return a.z;
+    case 2: return a.w;
+    case 3: return b.x;
+    case 4: return b.y;
+    case 5: return b.z;
+    default: return b.w;
+    }
+}
+
+// Plane equations of triangle t from its post-transform vertices
+// (SetupRoutine.cpp:270-548): x0, y0 of the rotated first vertex, z (A, B, C),
+// w (A, B, C) and each varying (A, B, C), PLANES floats, unused ones zero.
+// The setup stage evaluates them once per triangle; the raster stage loads them
+// for every bin the triangle touches.
+__device__ __forceinline__ void triangle_planes(const DrawParams &D, uint32_t t, float p[PLANES_STORED])
+{
+#pragma unroll
+    for(int k = 0; k < PLANES_STORED; k++) p[k] = 0.0f;
+    uint32_t i0, i1, i2;
+    tri_slots(D, t, i0, i1, i2);
+    const float4 c0 = D.ptv[(size_t)i0 * 4], c1 = D.ptv[(size_t)i1 * 4], c2 = D.ptv[(size_t)i2 * 4];
+    // sort by minimum y, then maximum w (SetupRoutine.cpp:270-294)
+    int o0 = 0, o1 = 1, o2 = 2, tt;
+    {
+        float ym = rmin(rmin(c0.y, c1.y), c2.y);
+        if(ym == c1.y) { tt = o0; o0 = o1; o1 = o2; o2 = tt; }
+        if(ym == c2.y) { tt = o2; o2 = o1; o1 = o0; o0 = tt; }
+    }
+    const float cw0 = c0.w, cw1 = c1.w, cw2 = c2.w;
+    {
+        float w0 = o0 == 0 ? cw0 : (o0 == 1 ? cw1 : cw2);
+        float w1 = o1 == 0 ? cw0 : (o1 == 1 ? cw1 : cw2);
+        float w2 = o2 == 0 ? cw0 : (o2 == 1 ? cw1 : cw2);
+        float wm = rmax(rmax(w0, w1), w2);
+        if(wm == w1) { tt = o0; o0 = o1; o1 = o2; o2 = tt; }
+        if(wm == w2) { tt = o2; o2 = o1; o1 = o0; o0 = tt; }
+    }
+    const uint32_t j0 = select3(o0, i0, i1, i2), j1 = select3(o1, i0, i1, i2), j2 = select3(o2, i0, i1, i2);
+    const float w1 = o1 == 0 ? cw0 : (o1 == 1 ? cw1 : cw2);
+    const float w2 = o2 == 0 ? cw0 : (o2 == 1 ? cw1 : cw2);
+    const float4 P0 = D.ptv[(size_t)j0 * 4 + 1], P1 = D.ptv[(size_t)j1 * 4 + 1], P2 = D.ptv[(size_t)j2 * 4 + 1];
+    const float4 A0 = D.ptv[(size_t)j0 * 4 + 2], A1 = D.ptv[(size_t)j1 * 4 + 2], A2 = D.ptv[(size_t)j2 * 4 + 2];
+    const float rhw0 = A0.x;
+    int32_t X0 = __float_as_int(P0.x), X1 = __float_as_int(P1.x), X2 = __float_as_int(P2.x);
+    int32_t Y0 = __float_as_int(P0.y), Y1 = __float_as_int(P1.y), Y2 = __float_as_int(P2.y);
+    const float inv = 1.0f / 256.0f;
+    p[0] = (float)X0 * inv;
+    p[1] = (float)Y0 * inv;
+    X1 -= X0; Y1 -= Y0; X2 -= X0; Y2 -= Y0;
+    float x1 = (w1 * inv) * (float)X1, y1 = (w1 * inv) * (float)Y1;
+    float x2 = (w2 * inv) * (float)X2, y2 = (w2 * inv) * (float)Y2;
+    float a = x1 * y2 - x2 * y1;
+    float M0x = 0.0f, M0y = 0.0f, M1x = 0.0f, M1y = 0.0f, M2x = 0.0f, M2y = 0.0f;
+    const float M0z = rhw0, M1z = 0.0f, M2z = 0.0f;
+    if(a != 0.0f)
+    {
+        float A = 1.0f / a;
+        float Dd = A * rhw0;
+        M0x = (y1 * w2 - y2 * w1) * Dd;
+        M0y = (x2 * w1 - x1 * w2) * Dd;
+        M1x = y2 * A;
+        M1y = (-x2) * A;
+        M2x = (-y1) * A;
+        M2y = x1 * A;
+    }
+    p[5] = (M0x + M1x) + M2x;
+    p[6] = (M0y + M1y) + M2y;
+    p[7] = (M0z + M1z) + M2z;
+    if(D.depthTest)
+    {
+        float z0 = P0.w, z1 = P1.w - z0, z2 = P2.w - z0;
+        float fx1 = (float)X1 * inv, fy1 = (float)Y1 * inv;
+        float fx2 = (float)X2 * inv, fy2 = (float)Y2 * inv;
+        float Dz = D.depthRange / (fx1 * fy2 - fx2 * fy1);
+        p[2] = (fy2 * z1 - fy1 * z2) * Dz;
+        p[3] = (fx1 * z2 - fx2 * z1) * Dz;
+        p[4] = z0 * D.depthRange + D.depthNear;
+    }
+    float4 B0 = make_float4(0, 0, 0, 0), B1 = B0, B2 = B0;
+    if(D.nv > 3)
+    {
+        B0 = D.ptv[(size_t)j0 * 4 + 3]; B1 = D.ptv[(size_t)j1 * 4 + 3]; B2 = D.ptv[(size_t)j2 * 4 + 3];
+    }
+#pragma unroll
+    for(int k = 0; k < PLANE_V; k++)
+    {
+        if(k >= D.nv) break;
+        float v0 = vary(A0, B0, k), v1 = vary(A1, B1, k), v2 = vary(A2, B2, k);
+        p[8 + 3 * k + 0] = (v0 * M0x + v1 * M1x) + v2 * M2x;
+        p[8 + 3 * k + 1] = (v0 * M0y + v1 * M1y) + v2 * M2y;
+        p[8 + 3 * k + 2] = (v0 * M0z + v1 * M1z) + v2 * M2z;
+    }
+}
+
 __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
 {
     const uint32_t t = blk * SETUP_THREADS + threadIdx.x;
@@ -686,6 +794,15 @@ __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
     }
     D.triBox[t] = box;  // capacity is a whole number of setup blocks
     D.triInfo[t] = inf;
+    if(cntVis)
+    {
+        float pl[PLANES_STORED];
+        triangle_planes(D, t, pl);
+        float4 *dst = D.planes + (size_t)t * (PLANES_STORED / 4);
+#pragma unroll
+        for(int k = 0; k < PLANES_STORED / 4; k++)
+            if(k < D.planeVec4) dst[k] = make_float4(pl[4 * k], pl[4 * k + 1], pl[4 * k + 2], pl[4 * k + 3]);
+    }
     if(D.binDiff && box.x < box.z && box.y < box.w)
     {
         // triangles per bin, for the raster's longest-first bin order: the
@@ -1101,8 +1218,7 @@ __device__ __forceinline__ bool depth_pass(uint32_t op, float zb, float z)
 
 // Per-triangle plane-equation floats staged for a batch:
 // x0, y0, z(A,B,C), w(A,B,C), V[k](A,B,C).
-constexpr int PLANE_V = 6;  // varying components with plane equations (colour + uv)
-constexpr int PLANES = 8 + 3 * PLANE_V;
+
 
 // 32-bit words per pixel of a colour attachment: R8G8B8A8_UNORM,
 // R16G16B16A16_SFLOAT, R32G32B32A32_SFLOAT.
@@ -1127,22 +1243,6 @@ struct RasterShared {
     static constexpr int kBW = BW, kBH = BH;
 };
 
-__device__ __forceinline__ uint32_t select3(int o, uint32_t a, uint32_t b, uint32_t c) { return o == 0 ? a : (o == 1 ? b : c); }
-
-__device__ __forceinline__ float vary(const float4 &a, const float4 &b, int k)
-{
-    // varying k of a post-transform vertex: float4[2].yzw then float4[3].xyzw
-    switch(k)
-    {
-    case 0: return a.y;
-    case 1: return a.z;
-    case 2: return a.w;
-    case 3: return b.x;
-    case 4: return b.y;
-    case 5: return b.z;
-    default: return b.w;
-    }
-}
 
 // The span rows of triangle t inside bin rows [rowLo, rowHi) by the reference's
 // edge DDA, for triangles whose rows did not fit the setup stage's span
@@ -1265,80 +1365,16 @@ __device__ int setup_batch_triangle(const DrawParams &D, SH &S, int ti, uint32_t
     S.qr0[ti] = (int8_t)qrA;
     S.nqr[ti] = (int8_t)(qrB - qrA + 1);
 
-    // plane equations from the post-transform vertices (L2 resident)
-    uint32_t i0, i1, i2;
-    tri_slots(D, t, i0, i1, i2);
-    const float4 c0 = D.ptv[(size_t)i0 * 4], c1 = D.ptv[(size_t)i1 * 4], c2 = D.ptv[(size_t)i2 * 4];
-    // sort by minimum y, then maximum w (SetupRoutine.cpp:270-294)
-    int o0 = 0, o1 = 1, o2 = 2, tt;
-    {
-        float ym = rmin(rmin(c0.y, c1.y), c2.y);
-        if(ym == c1.y) { tt = o0; o0 = o1; o1 = o2; o2 = tt; }
-        if(ym == c2.y) { tt = o2; o2 = o1; o1 = o0; o0 = tt; }
-    }
-    const float cw0 = c0.w, cw1 = c1.w, cw2 = c2.w;
-    {
-        float w0 = o0 == 0 ? cw0 : (o0 == 1 ? cw1 : cw2);
-        float w1 = o1 == 0 ? cw0 : (o1 == 1 ? cw1 : cw2);
-        float w2 = o2 == 0 ? cw0 : (o2 == 1 ? cw1 : cw2);
-        float wm = rmax(rmax(w0, w1), w2);
-        if(wm == w1) { tt = o0; o0 = o1; o1 = o2; o2 = tt; }
-        if(wm == w2) { tt = o2; o2 = o1; o1 = o0; o0 = tt; }
-    }
-    const uint32_t j0 = select3(o0, i0, i1, i2), j1 = select3(o1, i0, i1, i2), j2 = select3(o2, i0, i1, i2);
-    const float w1 = o1 == 0 ? cw0 : (o1 == 1 ? cw1 : cw2);
-    const float w2 = o2 == 0 ? cw0 : (o2 == 1 ? cw1 : cw2);
-    const float4 P0 = D.ptv[(size_t)j0 * 4 + 1], P1 = D.ptv[(size_t)j1 * 4 + 1], P2 = D.ptv[(size_t)j2 * 4 + 1];
-    const float4 A0 = D.ptv[(size_t)j0 * 4 + 2], A1 = D.ptv[(size_t)j1 * 4 + 2], A2 = D.ptv[(size_t)j2 * 4 + 2];
-    const float rhw0 = A0.x;
-    int32_t X0 = __float_as_int(P0.x), X1 = __float_as_int(P1.x), X2 = __float_as_int(P2.x);
-    int32_t Y0 = __float_as_int(P0.y), Y1 = __float_as_int(P1.y), Y2 = __float_as_int(P2.y);
-    const float inv = 1.0f / 256.0f;
-    S.plane[0][ti] = (float)X0 * inv;
-    S.plane[1][ti] = (float)Y0 * inv;
-    X1 -= X0; Y1 -= Y0; X2 -= X0; Y2 -= Y0;
-    float x1 = (w1 * inv) * (float)X1, y1 = (w1 * inv) * (float)Y1;
-    float x2 = (w2 * inv) * (float)X2, y2 = (w2 * inv) * (float)Y2;
-    float a = x1 * y2 - x2 * y1;
-    float M0x = 0.0f, M0y = 0.0f, M1x = 0.0f, M1y = 0.0f, M2x = 0.0f, M2y = 0.0f;
-    const float M0z = rhw0, M1z = 0.0f, M2z = 0.0f;
-    if(a != 0.0f)
-    {
-        float A = 1.0f / a;
-        float Dd = A * rhw0;
-        M0x = (y1 * w2 - y2 * w1) * Dd;
-        M0y = (x2 * w1 - x1 * w2) * Dd;
-        M1x = y2 * A;
-        M1y = (-x2) * A;
-        M2x = (-y1) * A;
-        M2y = x1 * A;
-    }
-    S.plane[5][ti] = (M0x + M1x) + M2x;
-    S.plane[6][ti] = (M0y + M1y) + M2y;
-    S.plane[7][ti] = (M0z + M1z) + M2z;
-    if(D.depthTest)
-    {
-        float z0 = P0.w, z1 = P1.w - z0, z2 = P2.w - z0;
-        float fx1 = (float)X1 * inv, fy1 = (float)Y1 * inv;
-        float fx2 = (float)X2 * inv, fy2 = (float)Y2 * inv;
-        float Dz = D.depthRange / (fx1 * fy2 - fx2 * fy1);
-        S.plane[2][ti] = (fy2 * z1 - fy1 * z2) * Dz;
-        S.plane[3][ti] = (fx1 * z2 - fx2 * z1) * Dz;
-        S.plane[4][ti] = z0 * D.depthRange + D.depthNear;
-    }
-    float4 B0 = make_float4(0, 0, 0, 0), B1 = B0, B2 = B0;
-    if(D.nv > 3)
-    {
-        B0 = D.ptv[(size_t)j0 * 4 + 3]; B1 = D.ptv[(size_t)j1 * 4 + 3]; B2 = D.ptv[(size_t)j2 * 4 + 3];
-    }
+    // plane equations, evaluated once per triangle by the setup stage
+    const float4 *pl = D.planes + (size_t)t * (PLANES_STORED / 4);
 #pragma unroll
-    for(int k = 0; k < PLANE_V; k++)
+    for(int k = 0; k < PLANES_STORED / 4; k++)
     {
-        if(k >= D.nv) break;
-        float v0 = vary(A0, B0, k), v1 = vary(A1, B1, k), v2 = vary(A2, B2, k);
-        S.plane[8 + 3 * k + 0][ti] = (v0 * M0x + v1 * M1x) + v2 * M2x;
-        S.plane[8 + 3 * k + 1][ti] = (v0 * M0y + v1 * M1y) + v2 * M2y;
-        S.plane[8 + 3 * k + 2][ti] = (v0 * M0z + v1 * M1z) + v2 * M2z;
+        const float4 v = __ldg(pl + k);  // past planeVec4: unused planes, never read
+        if(4 * k + 0 < PLANES) S.plane[4 * k + 0][ti] = v.x;
+        if(4 * k + 1 < PLANES) S.plane[4 * k + 1][ti] = v.y;
+        if(4 * k + 2 < PLANES) S.plane[4 * k + 2][ti] = v.z;
+        if(4 * k + 3 < PLANES) S.plane[4 * k + 3][ti] = v.w;
     }
     return pre;
 }
