@@ -378,9 +378,11 @@ def autotune_summary(best, table):
 
 def measure_batch(r, stream, flush, params, steps, warmup, per_draw_steps, dev, world=1, rank=0, tune=True):
     """Batched vs per-draw on the atlas workload: one swgb_draw_batch call per
-    step against one swgb_draw per draw, same draws, same kernels' work (the
-    raster configuration the autotuner picks for the batch serves both).  On
-    N ranks each rank draws its longest-processing-time-first share."""
+    step against one swgb_draw per draw, same draws, same kernels' work.  The
+    batched arm runs the raster configuration the autotuner picks for the
+    batch; the per-draw arm runs the faster of that one and the default (16x16
+    bins, depth rejection on), each timed.  On N ranks each rank draws its
+    longest-processing-time-first share."""
     from swiftshader_gb300 import DeviceBatch, scenes, shard
     b = scenes.scene_batch(**params)
     if world > 1:
@@ -390,6 +392,7 @@ def measure_batch(r, stream, flush, params, steps, warmup, per_draw_steps, dev, 
     if tune:
         db.clear()
         tuned = autotune_summary(*r.autotune(db.states, db.args, batched=True))
+    best = r.raster_config()
 
     def batched():
         db.clear()
@@ -401,8 +404,6 @@ def measure_batch(r, stream, flush, params, steps, warmup, per_draw_steps, dev, 
 
     for _ in range(warmup):
         batched()
-    if per_draw_steps:
-        per_draw()
     r.synchronize()
     r.reset_counters()
     l0 = r.launch_count()
@@ -410,15 +411,28 @@ def measure_batch(r, stream, flush, params, steps, warmup, per_draw_steps, dev, 
     r.synchronize()
     launches = r.launch_count() - l0
     cnt = r.counters()
-    tp = time_steps(stream, flush, per_draw_steps, per_draw) if per_draw_steps else [float("nan")]
+    per_draw_ms = {}
+    if per_draw_steps:
+        shapes = [best] + ([{"bin": "16x16", "hiz": 1}] if best != {"bin": "16x16", "hiz": 1} else [])
+        for c in shapes:
+            w, h = (int(x) for x in c["bin"].split("x"))
+            r.set_raster_config(w, h, bool(c["hiz"]))
+            per_draw()
+            r.synchronize()
+            tp = time_steps(stream, flush, per_draw_steps, per_draw)
+            per_draw_ms["%s hiz%d" % (c["bin"], c["hiz"])] = round(sum(tp) / len(tp), 3)
+        w, h = (int(x) for x in best["bin"].split("x"))
+        r.set_raster_config(w, h, bool(best["hiz"]))
     r.synchronize()
-    mb, mp = sum(tb) / len(tb), sum(tp) / len(tp)
+    mb = sum(tb) / len(tb)
+    mp = min(per_draw_ms.values()) if per_draw_ms else float("nan")
     per_step = {k: v // steps if k != "texture_levels_mask" else v for k, v in cnt.items()}
     return b, db, {
         "config": {"draws": b.n, "triangles_log_uniform": [params["tri_min"], params["tri_max"]],
                    "triangles": int(b.tris.sum()), "viewport_sides": [128, 256, 384, 512],
                    "atlas_pages": b.pages, "page": b.page_size, "texture": "256^2 RGBA8 per draw, bilinear"},
         "batched_ms_per_step": round(mb, 3), "per_draw_ms_per_step": round(mp, 3) if per_draw_steps else None,
+        "per_draw_ms_by_config": per_draw_ms or None,
         "speedup_vs_per_draw": round(mp / mb, 2) if per_draw_steps else None,
         "draws_per_s": round(b.n / (mb * 1e-3), 1), "per_draw_draws_per_s": round(b.n / (mp * 1e-3), 1) if per_draw_steps else None,
         "gfrag_per_s": round(per_step["fragments_tested"] / (mb * 1e-3) / 1e9, 3),
@@ -526,7 +540,7 @@ def run_batch(args):
         torch.distributed.barrier()
     params = dict(BATCH_FULL, n_draws=args.batch_draws, tri_max=args.batch_tri_max)
     b, db, res = measure_batch(r, stream, flush, params, args.steps, args.warmup,
-                               0 if args.no_per_draw else min(args.steps, 2), dev, world, rank, tune=not args.no_autotune)
+                               0 if args.no_per_draw else 1, dev, world, rank, tune=not args.no_autotune)
     clk = clocks.stop()
     # kernel-level timing: the batch as direct launches (timing disables the graph)
     r.set_kernel_timing(True)
