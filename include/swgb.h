@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-#define SWGB_ABI_VERSION 2
+#define SWGB_ABI_VERSION 3
 
 typedef enum swgb_status {
     SWGB_OK = 0,
@@ -209,7 +209,10 @@ typedef struct swgb_pipeline_state {
     /* the fragment shader's combined image sampler (FS_TEX_X_VCOLOR) */
     swgb_texture texture;
     uint32_t precision_profile;
-    uint32_t reserved2;
+    /* VkProvokingVertexModeEXT (VK_EXT_provoking_vertex): 0 = FIRST_VERTEX,
+     * 1 = LAST_VERTEX; the order setBatchIndices gives each triangle's
+     * vertices (src/Device/Renderer.cpp:49-145) */
+    uint32_t provoking_vertex;
 } swgb_pipeline_state;
 
 /* The per-draw arguments of sw::Renderer::draw. */
@@ -224,7 +227,15 @@ typedef struct swgb_draw_args {
     int32_t instance_id, layer;
     int32_t render_area_x, render_area_y;
     uint32_t render_area_width, render_area_height;
-    uint32_t reserved;
+    /* Primitive restart (VkPipelineInputAssemblyStateCreateInfo::
+     * primitiveRestartEnable) of an indexed draw: when nonzero, the draw reads
+     * this many indices, and every index equal to the all-ones value of the
+     * index type ends a sub-draw, as vk::IndexBuffer::getIndexBuffers splits
+     * the index buffer before Renderer::draw (src/Device/Context.cpp:49-91,
+     * 249-289); count is then ignored.  The split runs on the device.  Only
+     * swgb_draw takes it; swgb_draw_batch and swgb_draw_noalloc return
+     * SWGB_UNSUPPORTED_STATE.  0: no restart, count triangles. */
+    uint32_t restart_index_count;
 } swgb_draw_args;
 
 /* Device-side counters of one draw (the reference keeps occlusion counts per

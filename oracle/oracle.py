@@ -24,7 +24,8 @@ _lib = None
 def build(force=False):
     os.makedirs(BUILD, exist_ok=True)
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(
-            os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "swgb_oracle.h"))):
+            os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "swgb_oracle.h")),
+            os.path.getmtime(os.path.join(os.path.dirname(HERE), "include", "swgb.h"))):
         return LIB
     tmp = LIB + ".tmp%d" % os.getpid()
     subprocess.check_call(["gcc"] + CFLAGS + ["-o", tmp, SRC, "-lm", "-lpthread"])

@@ -696,26 +696,26 @@ static int setup_triangle(const ODraw *d, const OVertex *tv0, const OVertex *tv1
 
 /* setupSolidTriangles for one triangle (src/Device/Renderer.cpp:733-776).
  * Returns visibility; counters updated. */
-/* Index-buffer positions of triangle tri: setBatchIndices with the first
- * vertex provoking (src/Device/Renderer.cpp:97-134). */
-static void triangle_positions(uint32_t topology, uint32_t tri, uint32_t k[3])
+/* Index-buffer positions of triangle tri: setBatchIndices
+ * (src/Device/Renderer.cpp:49-145), provokeFirst = provoking vertex FIRST. */
+static void triangle_positions(uint32_t topology, int provokeFirst, uint32_t tri, uint32_t k[3])
 {
     switch(topology)
     {
     case SWGB_TOPOLOGY_TRIANGLE_STRIP: /* :110-121 */
-        k[0] = tri;
-        k[1] = tri + (tri & 1) + 1;
-        k[2] = tri + (~tri & 1) + 1;
+        k[0] = tri + (provokeFirst ? 0 : 2);
+        k[1] = tri + (tri & 1) + (provokeFirst ? 1 : 0);
+        k[2] = tri + (~tri & 1) + (provokeFirst ? 1 : 0);
         break;
-    case SWGB_TOPOLOGY_TRIANGLE_FAN: /* :122-133 */
-        k[0] = tri + 1;
-        k[1] = tri + 2;
-        k[2] = 0;
+    case SWGB_TOPOLOGY_TRIANGLE_FAN: /* :122-133: index = tri + 1 */
+        k[provokeFirst ? 0 : 2] = tri + 1;
+        k[provokeFirst ? 1 : 0] = tri + 2;
+        k[provokeFirst ? 2 : 1] = 0;
         break;
     default: /* TRIANGLE_LIST :97-109 */
-        k[0] = 3 * tri;
-        k[1] = 3 * tri + 1;
-        k[2] = 3 * tri + 2;
+        k[0] = 3 * tri + (provokeFirst ? 0 : 2);
+        k[1] = 3 * tri + (provokeFirst ? 1 : 0);
+        k[2] = 3 * tri + (provokeFirst ? 2 : 1);
         break;
     }
 }
@@ -724,7 +724,7 @@ static int process_triangle(const ODraw *d, uint32_t tri, OPrim *pr, swgb_counte
 {
     OVertex v0, v1, v2;
     uint32_t k[3];
-    triangle_positions(d->st->topology, tri, k);
+    triangle_positions(d->st->topology, d->st->provoking_vertex == 0, tri, k);
     vertex_shade(d, vertex_index(d, k[0]), &v0);
     vertex_shade(d, vertex_index(d, k[1]), &v1);
     vertex_shade(d, vertex_index(d, k[2]), &v2);
@@ -1455,9 +1455,58 @@ static void run_phase(OJob *j, int phase)
 }
 
 static swgb_status draw_impl(const swgb_pipeline_state *st, const swgb_draw_args *a, int nthreads, swgb_counters *cnt,
+                             uint32_t *vis, uint32_t *visLen, int visCap);
+
+/* ComputePrimitiveCount for the triangle topologies (src/Device/Context.cpp:26-46). */
+static uint32_t primitive_count(uint32_t topology, uint32_t vertexCount)
+{
+    if(topology == SWGB_TOPOLOGY_TRIANGLE_LIST) return vertexCount / 3;
+    return (vertexCount > 2 ? vertexCount : 2) - 2;
+}
+
+/* Primitive restart: vk::IndexBuffer::getIndexBuffers with
+ * ProcessPrimitiveRestart (src/Device/Context.cpp:49-91,249-289) splits the
+ * index stream at every all-ones index into sub-draws (primitive count, first
+ * index); each is drawn in turn, as its own Renderer::draw. */
+static swgb_status draw_restart(const swgb_pipeline_state *st, const swgb_draw_args *a, int nthreads, swgb_counters *cnt)
+{
+    const uint32_t bytes = a->index_type == SWGB_INDEX_TYPE_UINT8 ? 1u : (a->index_type == SWGB_INDEX_TYPE_UINT16 ? 2u : 4u);
+    const uint32_t restart = bytes == 1 ? 0xFFu : (bytes == 2 ? 0xFFFFu : 0xFFFFFFFFu);
+    uint32_t start = 0, vertexCount = 0;
+    for(uint32_t i = 0; i <= a->restart_index_count; i++)
+    {
+        uint32_t v = restart;
+        if(i < a->restart_index_count)
+            v = bytes == 1 ? ((const uint8_t *)a->indices)[i] : (bytes == 2 ? ((const uint16_t *)a->indices)[i] : ((const uint32_t *)a->indices)[i]);
+        if(v == restart)
+        {
+            const uint32_t prims = vertexCount ? primitive_count(st->topology, vertexCount) : 0;
+            if(prims > 0)
+            {
+                swgb_draw_args sub = *a;
+                sub.restart_index_count = 0;
+                sub.count = prims;
+                sub.indices = (const uint8_t *)a->indices + (size_t)start * bytes;
+                swgb_status s = draw_impl(st, &sub, nthreads, cnt, NULL, NULL, 0);
+                if(s != SWGB_OK) return s;
+            }
+            vertexCount = 0;
+        }
+        else
+        {
+            if(vertexCount == 0) start = i;
+            vertexCount++;
+        }
+    }
+    return SWGB_OK;
+}
+
+static swgb_status draw_impl(const swgb_pipeline_state *st, const swgb_draw_args *a, int nthreads, swgb_counters *cnt,
                              uint32_t *vis, uint32_t *visLen, int visCap)
 {
     if(!st || !a) return SWGB_INVALID_ARG;
+    if(a->restart_index_count && a->index_type != SWGB_INDEX_TYPE_NONE)
+        return visCap > 0 ? SWGB_UNSUPPORTED_STATE : draw_restart(st, a, nthreads, cnt);
     if(a->count == 0) return SWGB_OK; /* Renderer.cpp:187 */
     ODraw d;
     swgb_status s = prepare(&d, st, a);

@@ -98,7 +98,7 @@ class PipelineState(C.Structure):
         ("depth_slice_bytes", C.c_uint64),
         ("framebuffer_width", C.c_uint32), ("framebuffer_height", C.c_uint32),
         ("texture", Texture),
-        ("precision_profile", C.c_uint32), ("reserved2", C.c_uint32),
+        ("precision_profile", C.c_uint32), ("provoking_vertex", C.c_uint32),
     ]
 
 
@@ -109,7 +109,7 @@ class DrawArgs(C.Structure):
         ("instance_id", C.c_int32), ("layer", C.c_int32),
         ("render_area_x", C.c_int32), ("render_area_y", C.c_int32),
         ("render_area_width", C.c_uint32), ("render_area_height", C.c_uint32),
-        ("reserved", C.c_uint32),
+        ("restart_index_count", C.c_uint32),
     ]
 
 

@@ -72,6 +72,8 @@ struct swgb_ctx {
     size_t polyCap;
     uint32_t *polyCount;
     unsigned int *binQueue;
+    uint32_t *restart;     // primitive restart: per-position segment starts, then per-block carries
+    size_t restartCap;
     int *binDiff;          // longest-first bin order of single draws: difference array and order
     size_t binDiffCap;
     uint32_t *binOrder;
@@ -205,6 +207,8 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
     if(D.fs == SWGB_FS_TEX_X_VCOLOR && (D.nattr < 3 || D.nv < 6)) return set_error(SWGB_INVALID_ARG, "textured FS needs a uv varying");
     memcpy(D.mvp, st->mvp, sizeof(D.mvp));
 
+    if(st->provoking_vertex > 1) return set_error(SWGB_INVALID_ARG, "provoking_vertex (0 first, 1 last)");
+    D.provokingLast = st->provoking_vertex == 1;
     D.count = a->count;
     D.indexType = a->index_type;
     D.indices = a->indices;
@@ -220,6 +224,13 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
         if(!a->indices) return set_error(SWGB_INVALID_ARG, "indices");
         if(a->vertex_count == 0) return set_error(SWGB_INVALID_ARG, "indexed draws need vertex_count");
         D.vertexCount = a->vertex_count;
+        if(a->restart_index_count)
+        {
+            // triangle slots are index positions; k_restart_* find the sub-draws
+            D.restart = 1;
+            D.count = a->restart_index_count;
+            D.restartValue = a->index_type == SWGB_INDEX_TYPE_UINT8 ? 0xFFu : (a->index_type == SWGB_INDEX_TYPE_UINT16 ? 0xFFFFu : 0xFFFFFFFFu);
+        }
     }
 
     // Viewport and scissor (Renderer.cpp:300-345)
@@ -305,7 +316,7 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
         D.addrV = t.address_v;
     }
     set_bins(D, BIN, BIN);
-    D.nchunks = (int)((a->count + CHUNK - 1) / CHUNK);
+    D.nchunks = (int)((D.count + CHUNK - 1) / CHUNK);
     D.nsuper = (D.nchunks + SUPER - 1) / SUPER;
     return SWGB_OK;
 }
@@ -434,6 +445,13 @@ swgb_status prepare_scratch(swgb_ctx *ctx, DrawParams &D, bool order = true)
     // warps (with fewer, every bin starts at once) and the bin grid's counts
     // fit k_bin_order's shared memory.
     const size_t nbins = (size_t)D.binsX * D.binsY, cells = (size_t)(D.binsX + 1) * (D.binsY + 1);
+    if(D.restart)
+    {
+        const size_t nb = ((size_t)D.count + RESTART_BLOCK - 1) / RESTART_BLOCK;
+        if((s = ensure(ctx->restart, ctx->restartCap, (size_t)D.count + 2 * nb, "restart segments")) != SWGB_OK) return s;
+        D.restartLocal = ctx->restart;
+        D.restartCarry = ctx->restart + D.count + nb;
+    }
     D.binDiff = nullptr;
     D.binOrder = nullptr;
     if(order && nbins > (size_t)ctx->rasterBlocks[raster_variant(D)] * RASTER_WARPS && cells * sizeof(int) <= BIN_ORDER_SMEM)
@@ -467,6 +485,14 @@ swgb_status enqueue(swgb_ctx *ctx, DrawParams &D)
     swgb_status s;
     if((s = prepare_scratch(ctx, D)) != SWGB_OK) return s;
     const uint32_t nv = D.vertexCount;
+    if(D.restart)
+    {
+        // primitive restart: segment start of every index position (k_setup reads them)
+        const uint32_t nb = (D.count + RESTART_BLOCK - 1) / RESTART_BLOCK;
+        uint32_t *blockLast = ctx->restart + D.count;
+        timed_launch(ctx, SWGB_KERNEL_SETUP, [&] { k_restart_blocks<<<nb, RESTART_BLOCK, 0, ctx->stream>>>(D, ctx->restart, blockLast); });
+        timed_launch(ctx, SWGB_KERNEL_SETUP, [&] { k_restart_carry<<<1, 1024, 0, ctx->stream>>>(blockLast, ctx->restart + D.count + nb, nb); });
+    }
     timed_launch(ctx, SWGB_KERNEL_VERTEX, [&] { k_vertex<<<(nv + 255) / 256, 256, 0, ctx->stream>>>(D, nv); });
     const uint32_t setupBlocks = (uint32_t)((D.count + SETUP_THREADS - 1) / SETUP_THREADS);
     timed_launch(ctx, SWGB_KERNEL_SETUP, [&] { k_setup<<<setupBlocks, SETUP_THREADS, 0, ctx->stream>>>(D); });
@@ -970,10 +996,11 @@ swgb_status draw_batch(swgb_ctx *ctx, const swgb_pipeline_state *states, const s
     draws.reserve(n);
     for(uint32_t i = 0; i < n; i++)
     {
-        if(args[i].count == 0) continue;  // Renderer.cpp:187
+        if(args[i].count == 0 && !args[i].restart_index_count) continue;  // Renderer.cpp:187
         DrawParams D;
         swgb_status s = bake(&states[i], &args[i], D);
         if(s != SWGB_OK) return s;
+        if(D.restart) return set_error(SWGB_UNSUPPORTED_STATE, "swgb_draw_batch: primitive restart needs swgb_draw");
         apply_config(ctx, D);
         draws.push_back(D);
         src.push_back(i);
@@ -1005,6 +1032,7 @@ swgb_status bake_adjoint(const swgb_pipeline_state *st, const swgb_draw_args *a,
 {
     if(!g) return set_error(SWGB_INVALID_ARG, "null adjoint arguments");
     if(D.cf == CF_RGBA8) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint needs a float colour attachment");
+    if(D.restart) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint: primitive restart is not supported");
     if(D.fs == SWGB_FS_TEX_X_VCOLOR && !D.texFloat) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint needs a float texture");
     if(D.writeMask != 0xFu) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint needs color_write_mask 0xF");
     if(a->count > ADJ_TRI_MASK) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint: too many triangles");
@@ -1264,6 +1292,7 @@ swgb_status swgb_ctx_destroy(swgb_ctx *c)
     if(c->stream) cudaStreamSynchronize(c->stream);
     cudaFree(c->ptv);
     cudaFree(c->binDiff);
+    cudaFree(c->restart);
     cudaFree(c->binOrder);
     cudaFree(c->triBox);
     cudaFree(c->triInfo);
@@ -1311,10 +1340,10 @@ swgb_status swgb_ctx_set_stream(swgb_ctx *c, void *stream)
 swgb_status swgb_draw(swgb_ctx *ctx, const swgb_pipeline_state *st, const swgb_draw_args *args)
 {
     if(!ctx || !st || !args) return set_error(SWGB_INVALID_ARG, "null argument");
-    if(args->count == 0) return SWGB_OK;
     DrawParams D;
     swgb_status s = bake(st, args, D);
     if(s != SWGB_OK) return s;
+    if(D.count == 0) return SWGB_OK;
     apply_config(ctx, D);
     cudaSetDevice(ctx->device);
     return enqueue(ctx, D);
@@ -1326,6 +1355,8 @@ swgb_status swgb_draw(swgb_ctx *ctx, const swgb_pipeline_state *st, const swgb_d
 swgb_status swgb_draw_noalloc(const swgb_pipeline_state *st, const swgb_draw_args *args, void *stream)
 {
     if(!st || !args) return set_error(SWGB_INVALID_ARG, "null argument");
+    if(args->restart_index_count && args->index_type != SWGB_INDEX_TYPE_NONE)
+        return set_error(SWGB_UNSUPPORTED_STATE, "swgb_draw_noalloc: primitive restart needs swgb_draw");
     if(args->count == 0) return SWGB_OK;
     if(args->count > SWGB_NOALLOC_MAX_TRIANGLES)
         return set_error(SWGB_INVALID_ARG, "swgb_draw_noalloc: more than SWGB_NOALLOC_MAX_TRIANGLES (32768) triangles");
@@ -1410,10 +1441,11 @@ swgb_status swgb_autotune(swgb_ctx *ctx, const swgb_pipeline_state *states, cons
     std::vector<std::pair<uintptr_t, uintptr_t>> iv;
     for(uint32_t i = 0; i < n; i++)
     {
-        if(args[i].count == 0) continue;
         DrawParams D;
         swgb_status s = bake(&states[i], &args[i], D);
         if(s != SWGB_OK) return s;
+        if(D.count == 0) continue;
+        if(batched && D.restart) return set_error(SWGB_UNSUPPORTED_STATE, "swgb_draw_batch: primitive restart needs swgb_draw");
         const swgb_pipeline_state &st = states[i];
         const uint32_t h = st.framebuffer_height;
         const size_t cRow = (size_t)st.framebuffer_width * 4 * color_words(D.cf);
@@ -1465,10 +1497,10 @@ swgb_status swgb_autotune(swgb_ctx *ctx, const swgb_pipeline_state *states, cons
         if(batched) return n ? draw_batch(ctx, states, args, n) : SWGB_OK;
         for(uint32_t i = 0; i < n; i++)
         {
-            if(args[i].count == 0) continue;
             DrawParams D;
             swgb_status t = bake(&states[i], &args[i], D);
             if(t != SWGB_OK) return t;
+            if(D.count == 0) continue;
             apply_config(ctx, D);
             if((t = enqueue(ctx, D)) != SWGB_OK) return t;
         }
@@ -1544,10 +1576,11 @@ swgb_status swgb_plan_batch(const swgb_pipeline_state *states, const swgb_draw_a
     std::vector<uint32_t> src;
     for(uint32_t i = 0; i < n; i++)
     {
-        if(args[i].count == 0) continue;
+        if(args[i].count == 0 && !args[i].restart_index_count) continue;
         DrawParams D;
         swgb_status s = bake(&states[i], &args[i], D);
         if(s != SWGB_OK) return s;
+        if(D.restart) return set_error(SWGB_UNSUPPORTED_STATE, "swgb_draw_batch: primitive restart needs swgb_draw");
         draws.push_back(D);
         src.push_back(i);
     }

@@ -90,6 +90,11 @@ struct DrawParams {
     const void *indices;
     uint32_t indexType;
     uint32_t topology;     // SWGB_TOPOLOGY_TRIANGLE_LIST / STRIP / FAN
+    int provokingLast;     // VK_PROVOKING_VERTEX_MODE_LAST_VERTEX_EXT
+    int restart;           // primitive restart: triangle slots are index positions
+    uint32_t restartValue; // all ones of the index type
+    const uint32_t *restartLocal;  // per index position: block-local segment start (k_restart_blocks)
+    const uint32_t *restartCarry;  // per block of RESTART_BLOCK positions: segment start carried in
     uint32_t firstVertex;
     int32_t baseVertex;
     uint32_t vertexCount;  // post-transform vertices
@@ -273,35 +278,158 @@ __device__ __forceinline__ uint32_t fetch_index(const DrawParams &D, uint32_t k)
     return __ldg((const uint32_t *)D.indices + k);
 }
 
-// Post-transform vertex slots of triangle t: the index-buffer positions of
-// setBatchIndices with the first vertex provoking (Renderer.cpp:97-134) --
-// list (3t, 3t+1, 3t+2); strip (t, t+1+odd, t+2-odd), odd = t & 1; fan
-// (t+1, t+2, 0) -- through the index buffer of an indexed draw.
-__device__ __forceinline__ void tri_slots(const DrawParams &D, uint32_t t, uint32_t &i0, uint32_t &i1, uint32_t &i2)
+// Index-buffer positions of triangle t of a (sub-)draw whose indices start at
+// position base: setBatchIndices (Renderer.cpp:49-145).  Provoking vertex
+// first: list (3t, 3t+1, 3t+2), strip (t, t+1+odd, t+2-odd), odd = t & 1, fan
+// (t+1, t+2, 0); last: list (3t+2, 3t, 3t+1), strip (t+2, t+odd, t+1-odd), fan
+// (t+2, 0, t+1).
+__device__ __forceinline__ void tri_positions(const DrawParams &D, uint32_t base, uint32_t t, uint32_t &k0, uint32_t &k1, uint32_t &k2)
 {
-    uint32_t k0, k1, k2;
+    const uint32_t odd = t & 1;
     if(D.topology == SWGB_TOPOLOGY_TRIANGLE_STRIP)
     {
-        k0 = t;
-        k1 = t + 1 + (t & 1);
-        k2 = t + 2 - (t & 1);
+        if(D.provokingLast) { k0 = t + 2; k1 = t + odd; k2 = t + 1 - odd; }
+        else { k0 = t; k1 = t + 1 + odd; k2 = t + 2 - odd; }
     }
     else if(D.topology == SWGB_TOPOLOGY_TRIANGLE_FAN)
     {
-        k0 = t + 1;
-        k1 = t + 2;
-        k2 = 0;
+        if(D.provokingLast) { k0 = t + 2; k1 = 0; k2 = t + 1; }
+        else { k0 = t + 1; k1 = t + 2; k2 = 0; }
     }
     else
     {
-        k0 = 3 * t;
-        k1 = 3 * t + 1;
-        k2 = 3 * t + 2;
+        if(D.provokingLast) { k0 = 3 * t + 2; k1 = 3 * t; k2 = 3 * t + 1; }
+        else { k0 = 3 * t; k1 = 3 * t + 1; k2 = 3 * t + 2; }
     }
+    k0 += base;
+    k1 += base;
+    k2 += base;
+}
+
+// Primitive restart: slot p (an index position) is a triangle when it is not
+// a restart index and completes one inside its segment -- the sub-draws
+// vk::IndexBuffer::getIndexBuffers splits off (src/Device/Context.cpp:49-91),
+// each drawn from its first index.  base = the segment's first position, t =
+// the triangle's number inside it.
+constexpr int RESTART_BLOCK = 1024;
+__device__ __forceinline__ bool restart_slot(const DrawParams &D, uint32_t p, uint32_t &base, uint32_t &t)
+{
+    if(fetch_index(D, p) == D.restartValue) return false;
+    base = max(__ldg(D.restartLocal + p), __ldg(D.restartCarry + p / RESTART_BLOCK));
+    const uint32_t d = p - base;
+    if(D.topology == SWGB_TOPOLOGY_TRIANGLE_LIST)
+    {
+        if(d % 3 != 2) return false;
+        t = d / 3;
+    }
+    else
+    {
+        if(d < 2) return false;
+        t = d - 2;
+    }
+    return true;
+}
+
+// Triangle slot t of the draw is a triangle (always, without primitive restart).
+__device__ __forceinline__ bool tri_valid(const DrawParams &D, uint32_t t)
+{
+    uint32_t base, local;
+    return !D.restart || restart_slot(D, t, base, local);
+}
+
+// Post-transform vertex slots of triangle slot t (valid, see tri_valid),
+// through the index buffer of an indexed draw.
+__device__ __forceinline__ void tri_slots(const DrawParams &D, uint32_t t, uint32_t &i0, uint32_t &i1, uint32_t &i2)
+{
+    uint32_t base = 0, local = t, k0, k1, k2;
+    if(D.restart) restart_slot(D, t, base, local);
+    tri_positions(D, base, local, k0, k1, k2);
     i0 = fetch_index(D, k0);
     i1 = fetch_index(D, k1);
     i2 = fetch_index(D, k2);
 }
+
+#ifndef SWGB_RASTER_TU
+// Primitive restart, first pass: per block of RESTART_BLOCK index positions,
+// the segment start of every position as far as the block sees it (one past
+// the block's last restart index at or before it, else 0), and the block's
+// last such value for the carry pass.
+__global__ void __launch_bounds__(RESTART_BLOCK) k_restart_blocks(const __grid_constant__ DrawParams D, uint32_t *local, uint32_t *blockLast)
+{
+    __shared__ uint32_t warpMax[RESTART_BLOCK / 32];
+    const uint32_t p = blockIdx.x * RESTART_BLOCK + threadIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t v = (p < D.count && fetch_index(D, p) == D.restartValue) ? p + 1 : 0u;
+#pragma unroll
+    for(int o = 1; o < 32; o <<= 1)
+    {
+        const uint32_t u = __shfl_up_sync(0xFFFFFFFFu, v, o);
+        if(lane >= o) v = max(v, u);
+    }
+    if(lane == 31) warpMax[warp] = v;
+    __syncthreads();
+    if(warp == 0)
+    {
+        uint32_t w = warpMax[lane];
+#pragma unroll
+        for(int o = 1; o < 32; o <<= 1)
+        {
+            const uint32_t u = __shfl_up_sync(0xFFFFFFFFu, w, o);
+            if(lane >= o) w = max(w, u);
+        }
+        warpMax[lane] = w;  // inclusive prefix max over the block's warps
+    }
+    __syncthreads();
+    if(warp > 0) v = max(v, warpMax[warp - 1]);
+    if(p < D.count) local[p] = v;
+    if(threadIdx.x == RESTART_BLOCK - 1) blockLast[blockIdx.x] = v;
+}
+
+// Primitive restart, carry pass (one block): carry[b] = the largest segment
+// start of the blocks before b, so a position's segment start is
+// max(local[p], carry[p / RESTART_BLOCK]).
+__global__ void __launch_bounds__(1024) k_restart_carry(const uint32_t *blockLast, uint32_t *carry, uint32_t nblocks)
+{
+    __shared__ uint32_t chunkMax;
+    uint32_t run = 0;
+    for(uint32_t c0 = 0; c0 < nblocks; c0 += blockDim.x)
+    {
+        const uint32_t b = c0 + threadIdx.x;
+        uint32_t v = b < nblocks ? blockLast[b] : 0u;
+        // exclusive prefix max inside the chunk, by warps then across warps
+        __shared__ uint32_t wm[32];
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        uint32_t incl = v;
+#pragma unroll
+        for(int o = 1; o < 32; o <<= 1)
+        {
+            const uint32_t u = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if(lane >= o) incl = max(incl, u);
+        }
+        if(lane == 31) wm[warp] = incl;
+        __syncthreads();
+        if(warp == 0)
+        {
+            uint32_t w = wm[lane];
+#pragma unroll
+            for(int o = 1; o < 32; o <<= 1)
+            {
+                const uint32_t u = __shfl_up_sync(0xFFFFFFFFu, w, o);
+                if(lane >= o) w = max(w, u);
+            }
+            wm[lane] = w;
+        }
+        __syncthreads();
+        const uint32_t before = max(run, warp > 0 ? wm[warp - 1] : 0u);
+        const uint32_t excl = max(before, __shfl_up_sync(0xFFFFFFFFu, incl, 1) * (lane > 0));
+        if(b < nblocks) carry[b] = lane > 0 ? excl : before;
+        if(threadIdx.x == blockDim.x - 1) chunkMax = max(before, incl);
+        __syncthreads();
+        run = chunkMax;
+        __syncthreads();
+    }
+}
+#endif  // SWGB_RASTER_TU
 
 struct CVert { float x, y, z, w; };
 
@@ -589,7 +717,7 @@ __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
     int n = 3, dW = 1;
     int32_t X[MAX_POLY + 1], Y[MAX_POLY + 1];
     int32_t yMin = 0, yMax = 0, xMinS = 0, xMaxS = 0;
-    if(t < D.count)
+    if(t < D.count && tri_valid(D, t))
     {
         cntIn = 1;
         uint32_t i0, i1, i2;

@@ -46,6 +46,8 @@ class Scene:
     topology: int = abi.TOPOLOGY_TRIANGLE_LIST
     first_vertex: int = 0
     base_vertex: int = 0
+    provoking_vertex: int = 0         # 0 = FIRST_VERTEX, 1 = LAST_VERTEX (VK_EXT_provoking_vertex)
+    restart_index_count: int = 0      # > 0: primitive restart over this many indices (tri_count ignored)
 
     @property
     def vertex_count(self):
@@ -302,6 +304,7 @@ def build_state(scene, color_ptr, depth_ptr, vertex_ptr, level_ptrs=None, color_
     the GB300 path, host pointers for the oracle)."""
     st = abi.PipelineState()
     st.topology = scene.topology
+    st.provoking_vertex = scene.provoking_vertex
     st.attrib_count = 3
     st.attribs[0] = abi.VertexAttrib(abi.FORMAT_R32G32B32A32_SFLOAT, 0, 0, 0)
     st.attribs[1] = abi.VertexAttrib(abi.FORMAT_R32G32B32A32_SFLOAT, 0, 16, 0)
@@ -366,6 +369,7 @@ def build_args(scene, index_ptr=None):
         a.index_type = INDEX_TYPES[np.asarray(scene.indices).dtype]
         a.indices = index_ptr
     a.vertex_count = scene.vertex_count
+    a.restart_index_count = scene.restart_index_count
     a.render_area_x, a.render_area_y = 0, 0
     a.render_area_width, a.render_area_height = scene.width, scene.height
     return a
@@ -395,6 +399,29 @@ def strip_fan_scene(topology, n_tris=300, width=96, height=80, indexed=None, see
     return Scene(name="topo%d_%d_%s" % (topology, n_tris, "none" if indexed is None else np.dtype(indexed).name),
                  width=width, height=height, vertices=v, indices=indices, tri_count=n_tris, topology=topology,
                  cull_mode=abi.CULL_BACK)
+
+
+def restart_scene(topology, n_indices=600, width=96, height=80, dtype=np.uint16, restart_every=(1, 40), seed_index=51):
+    """Primitive restart: an index stream of n_indices entries over random
+    clip-space vertices (as scene_small), cut by all-ones restart indices at
+    random gaps in [restart_every] -- including back-to-back restarts, a leading
+    one and segments too short to hold a triangle; back faces culled."""
+    rng = _rng(seed_index)
+    nv = min(n_indices, int(np.iinfo(dtype).max))  # all-ones stays free for restart
+    v = random_triangles(rng, (nv + 2) // 3)[:nv]
+    if topology == abi.TOPOLOGY_TRIANGLE_FAN:
+        v[:, 0:2] *= 0.6
+    idx = rng.integers(0, nv, n_indices).astype(np.int64)
+    restart = np.iinfo(dtype).max
+    pos = 0
+    while pos < n_indices:
+        idx[pos] = restart
+        pos += int(rng.integers(restart_every[0], restart_every[1] + 1))
+    idx[-3:] = restart if n_indices > 8 else idx[-3:]
+    idx[0] = restart
+    return Scene(name="restart%d_%d_%s" % (topology, n_indices, np.dtype(dtype).name), width=width, height=height,
+                 vertices=v, indices=idx.astype(dtype), tri_count=0, topology=topology, cull_mode=abi.CULL_BACK,
+                 restart_index_count=n_indices)
 
 
 def attachment_shapes(scene):

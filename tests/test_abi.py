@@ -71,7 +71,7 @@ def test_library_loads_and_exports_all_symbols(built_lib):
     for name in _lib.EXPORTS:
         assert name in exported, name
     L = _lib.load(built_lib)
-    assert L.swgb_abi_version() == 2
+    assert L.swgb_abi_version() == 3
 
 
 def test_host_side_errors_without_device(built_lib):
@@ -96,6 +96,19 @@ def test_host_side_errors_without_device(built_lib):
     a.count = 40000
     assert L.swgb_draw_noalloc(C.byref(st), C.byref(a), None) == abi.INVALID_ARG
     assert b"32768" in L.swgb_last_error()
+    # primitive restart runs only through swgb_draw: the batched and
+    # allocation-free paths refuse it on the host
+    rs = scenes.restart_scene(abi.TOPOLOGY_TRIANGLE_STRIP, n_indices=64)
+    rst = scenes.build_state(rs, 1 << 20, 1 << 20, 1 << 20)
+    ra = scenes.build_args(rs, 1 << 20)
+    assert L.swgb_draw_noalloc(C.byref(rst), C.byref(ra), None) == abi.UNSUPPORTED_STATE
+    segs = C.c_uint32()
+    assert L.swgb_plan_batch(C.byref(rst), C.byref(ra), 1, None, C.byref(segs)) == abi.UNSUPPORTED_STATE
+    ra.restart_index_count = 0
+    ra.count = 4
+    rst.provoking_vertex = 2
+    assert L.swgb_draw_noalloc(C.byref(rst), C.byref(ra), None) == abi.INVALID_ARG
+    assert b"provoking" in L.swgb_last_error()
     # raster configuration: validated on the host
     assert L.swgb_ctx_set_raster_config(None, None) == abi.INVALID_ARG
     assert L.swgb_autotune(None, None, None, 0, 1, None, None, None) == abi.INVALID_ARG

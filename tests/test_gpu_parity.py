@@ -260,3 +260,41 @@ def test_strip_with_first_and_base_vertex(gpu_lib):
     nd.vertices = np.concatenate([np.zeros((9, scenes.VERTEX_FLOATS), np.float32), nd.vertices])
     nd.first_vertex = 9
     check_scene(nd, gpu_lib)
+
+
+@pytest.mark.parametrize("topology", [abi.TOPOLOGY_TRIANGLE_LIST, abi.TOPOLOGY_TRIANGLE_STRIP, abi.TOPOLOGY_TRIANGLE_FAN])
+@pytest.mark.parametrize("indexed", [None, np.uint16])
+def test_provoking_vertex_last(gpu_lib, topology, indexed):
+    """VK_EXT_provoking_vertex LAST: setBatchIndices' rotated vertex order
+    (the setup's tie-breaks and clipping see it), textured and blended."""
+    if topology == abi.TOPOLOGY_TRIANGLE_LIST:
+        s = scenes.scene_textured_small(n_tris=200, width=96, height=72, seed_index=61)
+        if indexed is not None:
+            s.indices = np.arange(s.vertex_count, dtype=indexed)[::-1].copy()
+            s.vertices = s.vertices[::-1].copy()
+    else:
+        s = scenes.strip_fan_scene(topology, n_tris=240, indexed=indexed, seed_index=62)
+    s.provoking_vertex = 1
+    check_scene(s, gpu_lib)
+
+
+@pytest.mark.parametrize("topology", [abi.TOPOLOGY_TRIANGLE_LIST, abi.TOPOLOGY_TRIANGLE_STRIP, abi.TOPOLOGY_TRIANGLE_FAN])
+@pytest.mark.parametrize("dtype", [np.uint8, np.uint16, np.uint32])
+def test_primitive_restart(gpu_lib, topology, dtype):
+    """Primitive restart split on the device into the sub-draws
+    vk::IndexBuffer::getIndexBuffers makes (leading, back-to-back and trailing
+    restarts, segments too short for a triangle), both provoking modes."""
+    for last in (0, 1):
+        s = scenes.restart_scene(topology, n_indices=200 if dtype == np.uint8 else 700, dtype=dtype, seed_index=63 + last)
+        s.provoking_vertex = last
+        cnt = check_scene(s, gpu_lib)
+        assert cnt["triangles_in"] > 0
+
+
+def test_primitive_restart_many_blocks(gpu_lib):
+    """1.5M indices: the segment scan crosses 1465 blocks of 1024 positions and
+    the carry pass's chunk loop."""
+    s = scenes.restart_scene(abi.TOPOLOGY_TRIANGLE_STRIP, n_indices=1_500_000, width=128, height=96, dtype=np.uint32,
+                             restart_every=(50, 3000), seed_index=65)
+    cnt = check_scene(s, gpu_lib)
+    assert cnt["triangles_in"] > 1_000_000

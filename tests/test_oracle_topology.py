@@ -52,3 +52,56 @@ def test_first_and_base_vertex(oracle_mod):
     shifted.first_vertex = 7
     got = oracle_mod.render(shifted)
     assert np.array_equal(got[0], ref[0]) and got[2] == ref[2]
+
+
+def split_restart(indices, topology, restart):
+    """vk::IndexBuffer's ProcessPrimitiveRestart restated in numpy: the
+    (first index, primitive count) of every sub-draw."""
+    out, start, n = [], 0, 0
+    for i, v in enumerate(list(indices) + [restart]):
+        if v == restart:
+            prims = (n // 3) if topology == abi.TOPOLOGY_TRIANGLE_LIST else max(n, 2) - 2
+            if n and prims:
+                out.append((start, prims))
+            n = 0
+        else:
+            if n == 0:
+                start = i
+            n += 1
+    return out
+
+
+@pytest.mark.parametrize("topology", [abi.TOPOLOGY_TRIANGLE_LIST, abi.TOPOLOGY_TRIANGLE_STRIP, abi.TOPOLOGY_TRIANGLE_FAN])
+@pytest.mark.parametrize("last", [0, 1])
+def test_primitive_restart_equals_sub_draws(oracle_mod, topology, last):
+    """A restart draw renders as its sub-draws drawn one after another, each
+    from its own first index (the reference's Renderer::draw per sub-draw)."""
+    sc = scenes.restart_scene(topology, n_indices=500, dtype=np.uint16, seed_index=66)
+    sc.provoking_vertex = last
+    got = oracle_mod.render(sc)
+    color, depth = scenes.clear_buffers(sc)
+    total = {}
+    for start, prims in split_restart(sc.indices, topology, 0xFFFF):
+        sub = scenes.restart_scene(topology, n_indices=500, dtype=np.uint16, seed_index=66)
+        sub.provoking_vertex = last
+        sub.restart_index_count = 0
+        sub.indices = sc.indices[start:].copy()
+        sub.tri_count = prims
+        _, _, cnt = oracle_mod.render(sub, color=color, depth=depth)
+        for k, v in cnt.items():
+            total[k] = (total.get(k, 0) | v) if k == "texture_levels_mask" else total.get(k, 0) + v
+    assert np.array_equal(got[0], color) and np.array_equal(got[1], depth)
+    assert got[2] == total and total["triangles_in"] > 50
+
+
+def test_provoking_vertex_last_rotates_vertices(oracle_mod):
+    """LAST draws each triangle from its rotated vertex list: the same as a
+    FIRST draw of a list whose triangles were rotated by hand."""
+    sc = scenes.scene_small(n_tris=150, width=64, height=48, seed_index=67)
+    sc.provoking_vertex = 1
+    got = oracle_mod.render(sc)
+    rot = scenes.scene_small(n_tris=150, width=64, height=48, seed_index=67)
+    v = rot.vertices.reshape(150, 3, -1)
+    rot.vertices = np.ascontiguousarray(v[:, [2, 0, 1], :].reshape(450, -1))
+    ref = oracle_mod.render(rot)
+    assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1]) and got[2] == ref[2]
