@@ -55,9 +55,13 @@ typedef enum swgb_status {
 /* VkFormat */
 #define SWGB_FORMAT_UNDEFINED 0
 #define SWGB_FORMAT_R8G8B8A8_UNORM 37
+#define SWGB_FORMAT_R8G8B8A8_SRGB 43
+#define SWGB_FORMAT_B8G8R8A8_UNORM 44
+#define SWGB_FORMAT_B8G8R8A8_SRGB 50
 #define SWGB_FORMAT_R16G16B16A16_SFLOAT 97
 #define SWGB_FORMAT_R32G32_SFLOAT 103
 #define SWGB_FORMAT_R32G32B32A32_SFLOAT 109
+#define SWGB_FORMAT_D16_UNORM 124
 #define SWGB_FORMAT_D32_SFLOAT 126
 /* VkPrimitiveTopology */
 #define SWGB_TOPOLOGY_TRIANGLE_LIST 3
@@ -157,7 +161,7 @@ typedef struct swgb_texture_level {
  * level_count are ignored (the descriptor replicates the last level,
  * src/Vulkan/VkDescriptorSetLayout.cpp:468-470). */
 typedef struct swgb_texture {
-    uint32_t format;      /* R8G8B8A8_UNORM, R16G16B16A16_SFLOAT or R32G32B32A32_SFLOAT */
+    uint32_t format;      /* R8G8B8A8_UNORM / _SRGB, B8G8R8A8_UNORM / _SRGB, R16G16B16A16_SFLOAT or R32G32B32A32_SFLOAT */
     uint32_t level_count;
     swgb_texture_level levels[SWGB_MAX_MIP_LEVELS];
     uint32_t mag_filter, min_filter, mipmap_mode;
@@ -190,7 +194,7 @@ typedef struct swgb_pipeline_state {
     /* fragment (vk::FragmentState) */
     uint32_t depth_test_enable, depth_write_enable, depth_compare_op;
     /* fragment output interface (vk::FragmentOutputInterfaceState) */
-    uint32_t color_format;
+    uint32_t color_format;  /* R8G8B8A8_UNORM, B8G8R8A8_UNORM, R16G16B16A16_SFLOAT or R32G32B32A32_SFLOAT */
     uint32_t blend_enable;
     uint32_t src_color_factor, dst_color_factor, color_blend_op;
     uint32_t src_alpha_factor, dst_alpha_factor, alpha_blend_op;
@@ -203,7 +207,7 @@ typedef struct swgb_pipeline_state {
     uint64_t color_slice_bytes;
     void *depth;
     uint32_t depth_pitch_bytes;
-    uint32_t reserved1;
+    uint32_t depth_format;  /* D32_SFLOAT (or 0, the same) or D16_UNORM */
     uint64_t depth_slice_bytes;
     uint32_t framebuffer_width, framebuffer_height;
     /* the fragment shader's combined image sampler (FS_TEX_X_VCOLOR) */
@@ -365,7 +369,8 @@ swgb_status swgb_draw_adjoint_batch(swgb_ctx *ctx, const swgb_pipeline_state *st
  * swgb_draw and swgb_draw_batch tile the framebuffer; every configuration
  * gives the same attachments and counters bit for bit.
  *   bin_width x bin_height: the screen bin one raster warp owns, one of
- *     16x16 (default), 32x16, 32x32.  Four-sample draws always use 16x16.
+ *     16x16 (default), 32x16, 32x32.  Four-sample draws and draws with a
+ *     D16_UNORM depth attachment always use 16x16.
  *   hiz: 1 (default) rejects a triangle's fragments in a bin without
  *     expanding them when the bin's depth bound proves every one fails a
  *     LESS / LESS_OR_EQUAL / GREATER / GREATER_OR_EQUAL test; 0 expands them. */

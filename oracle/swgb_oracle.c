@@ -213,7 +213,30 @@ static uint32_t simplify_op(uint32_t op, uint32_t sf, uint32_t df)
     return op;
 }
 
-static int is_unorm(uint32_t fmt) { return fmt == SWGB_FORMAT_R8G8B8A8_UNORM; }
+static int is_unorm(uint32_t fmt) { return fmt == SWGB_FORMAT_R8G8B8A8_UNORM || fmt == SWGB_FORMAT_B8G8R8A8_UNORM; }
+static int is_tex8(uint32_t fmt)
+{
+    return fmt == SWGB_FORMAT_R8G8B8A8_UNORM || fmt == SWGB_FORMAT_B8G8R8A8_UNORM || fmt == SWGB_FORMAT_R8G8B8A8_SRGB ||
+           fmt == SWGB_FORMAT_B8G8R8A8_SRGB;
+}
+/* byte of component c (R, G, B, A) in a B8G8R8A8 pixel or texel: R and B swap */
+static int bgra_byte(int c) { return c == 0 ? 2 : (c == 2 ? 0 : c); }
+static int d16(const swgb_pipeline_state *st) { return st->depth_format == SWGB_FORMAT_D16_UNORM; }
+
+/* sRGBtoLinearFF_FF00 (src/Pipeline/Constants.cpp:273-276), from
+ * sw::sRGBtoLinear (src/System/Math.hpp:326-336): 8-bit sRGB to 16-bit linear,
+ * 0xFF00 = 1.0. */
+static uint16_t srgb_lut[256];
+static pthread_once_t srgb_once = PTHREAD_ONCE_INIT;
+static void srgb_init(void)
+{
+    for(int i = 0; i < 256; i++)
+    {
+        const float c = (float)i / 0xFF;
+        const float lin = c <= 0.04045f ? c / 12.92f : powf((c + 0.055f) / 1.055f, 2.4f);
+        srgb_lut[i] = (uint16_t)(lin * 0xFF00 + 0.5f);
+    }
+}
 
 /* ------------------------------------------------------------------------ */
 /* Validation + DrawData                                                     */
@@ -231,12 +254,15 @@ static swgb_status prepare(ODraw *d, const swgb_pipeline_state *st, const swgb_d
     if(st->sample_count != 1 && st->sample_count != 4) return SWGB_UNSUPPORTED_STATE;
     if(st->depth_clamp_enable || st->depth_bias_constant != 0.0f || st->depth_bias_slope != 0.0f) return SWGB_UNSUPPORTED_STATE;
     if(st->attrib_count < 1 || st->attrib_count > SWGB_MAX_ATTRIBS) return SWGB_INVALID_ARG;
-    if(st->color_format != SWGB_FORMAT_R8G8B8A8_UNORM && st->color_format != SWGB_FORMAT_R32G32B32A32_SFLOAT &&
+    if(!is_unorm(st->color_format) && st->color_format != SWGB_FORMAT_R32G32B32A32_SFLOAT &&
        st->color_format != SWGB_FORMAT_R16G16B16A16_SFLOAT)
         return SWGB_UNSUPPORTED_STATE;
-    if(st->fragment_shader == SWGB_FS_TEX_X_VCOLOR && st->texture.format != SWGB_FORMAT_R8G8B8A8_UNORM &&
+    if(st->fragment_shader == SWGB_FS_TEX_X_VCOLOR && !is_tex8(st->texture.format) &&
        st->texture.format != SWGB_FORMAT_R16G16B16A16_SFLOAT && st->texture.format != SWGB_FORMAT_R32G32B32A32_SFLOAT)
         return SWGB_UNSUPPORTED_STATE;
+    if(st->depth_format != SWGB_FORMAT_UNDEFINED && st->depth_format != SWGB_FORMAT_D32_SFLOAT && st->depth_format != SWGB_FORMAT_D16_UNORM)
+        return SWGB_UNSUPPORTED_STATE;
+    pthread_once(&srgb_once, srgb_init);
 
     /* Viewport (Renderer.cpp:300-331) */
     float W = 0.5f * st->viewport_width;
@@ -811,15 +837,23 @@ static uint16_t offset_sample(uint16_t uvw, uint16_t half, int wrap, int count)
     return count < 0 ? subsat_u16(uvw, half) : addsat_u16(uvw, half);
 }
 
-/* computeIndices + sampleTexel for RGBA8 (SamplerCore.cpp:1593-1643,1747-1788):
- * texel component c is returned as c << 8. */
-static void texel_rgba8(const swgb_texture_level *lv, uint16_t u, uint16_t v, uint16_t out[4])
+/* computeIndices + sampleTexel for 8-bit RGBA textures (SamplerCore.cpp:
+ * 1593-1643,1747-1788): texel component c is returned as c << 8; B8G8R8A8
+ * texels swap R and B; the R, G, B of sRGB textures are replaced by their
+ * sRGBtoLinearFF_FF00 entry (:1966-1978,2670-2680). */
+static void texel_rgba8(const swgb_texture *t, const swgb_texture_level *lv, uint16_t u, uint16_t v, uint16_t out[4])
 {
     uint16_t xi = mulhi_u16(u, (uint16_t)lv->width);
     uint16_t yi = mulhi_u16(v, (uint16_t)lv->height);
     int32_t index = (int32_t)(int16_t)xi * 1 + (int32_t)(int16_t)yi * (int32_t)(int16_t)lv->pitch_texels; /* pmaddwd */
     const uint8_t *p = (const uint8_t *)lv->buffer + (size_t)(uint32_t)index * 4;
-    for(int c = 0; c < 4; c++) out[c] = (uint16_t)(p[c] << 8);
+    const int bgra = t->format == SWGB_FORMAT_B8G8R8A8_UNORM || t->format == SWGB_FORMAT_B8G8R8A8_SRGB;
+    const int srgb = t->format == SWGB_FORMAT_R8G8B8A8_SRGB || t->format == SWGB_FORMAT_B8G8R8A8_SRGB;
+    for(int c = 0; c < 4; c++)
+    {
+        const uint8_t b = p[bgra ? bgra_byte(c) : c];
+        out[c] = (srgb && c < 3) ? srgb_lut[b] : (uint16_t)(b << 8);
+    }
 }
 
 /* sampleQuad2D for one lane (SamplerCore.cpp:668-909) */
@@ -832,7 +866,7 @@ static void sample_quad_2d(const OSampler *s, float u, float v, float lod, int s
     uint16_t vvvv = address16(v, s->t->address_v);
     if(!s->linearFilter)
     {
-        texel_rgba8(lv, uuuu, vvvv, out);
+        texel_rgba8(s->t, lv, uuuu, vvvv, out);
         return;
     }
     /* WriteTextureLevelInfo: uHalf = 0x8000 / width (VkDescriptorSetLayout.cpp:316-321) */
@@ -845,10 +879,10 @@ static void sample_quad_2d(const OSampler *s, float u, float v, float lod, int s
     uint16_t u1 = offset_sample(uuuu, uHalf, wrapU, +1);
     uint16_t v1 = offset_sample(vvvv, vHalf, wrapV, +1);
     uint16_t c00[4], c10[4], c01[4], c11[4];
-    texel_rgba8(lv, u0, v0, c00);
-    texel_rgba8(lv, u1, v0, c10);
-    texel_rgba8(lv, u0, v1, c01);
-    texel_rgba8(lv, u1, v1, c11);
+    texel_rgba8(s->t, lv, u0, v0, c00);
+    texel_rgba8(s->t, lv, u1, v0, c10);
+    texel_rgba8(s->t, lv, u0, v1, c01);
+    texel_rgba8(s->t, lv, u1, v1, c11);
     /* bilinearInterpolate, 8-bit unsigned components (:516-575) */
     uint16_t f0u = (uint16_t)(u0 * (uint16_t)lv->width);
     uint16_t f0v = (uint16_t)(v0 * (uint16_t)lv->height);
@@ -994,7 +1028,7 @@ static void sample_texture_quad(const OSampler *s, const float u[4], const float
         lod = fmaxr(lod, s->minLod);
         lod = fminr(lod, s->maxLod);
     }
-    if(s->t->format != SWGB_FORMAT_R8G8B8A8_UNORM)
+    if(!is_tex8(s->t->format))
     {
         /* sampleFloatFilter (SamplerCore.cpp:1061-1083) */
         float fr = fsub(daz(lod), floorf(daz(lod))); /* scalar Frac: lod - floor(lod) */
@@ -1132,12 +1166,13 @@ static void read_color(const ODraw *d, int q, int x, int y, float dst[4])
 {
     const swgb_pipeline_state *st = d->st;
     uint8_t *row = (uint8_t *)st->color + (size_t)q * st->color_slice_bytes + (size_t)y * st->color_pitch_bytes;
-    if(st->color_format == SWGB_FORMAT_R8G8B8A8_UNORM)
+    if(is_unorm(st->color_format))
     {
-        /* readPixel (PixelRoutine.cpp:1111-1130) widens b to b*257; alphaBlend
-         * scales by 1/0xFFFF (:1812-1828). */
+        /* readPixel (PixelRoutine.cpp:1091-1130) widens b to b*257; alphaBlend
+         * scales by 1/0xFFFF (:1812-1828); B8G8R8A8 swaps R and B. */
         const uint8_t *p = row + (size_t)x * 4;
-        for(int c = 0; c < 4; c++) dst[c] = fmul((float)(p[c] * 257), 1.0f / 0xFFFF);
+        const int bgra = st->color_format == SWGB_FORMAT_B8G8R8A8_UNORM;
+        for(int c = 0; c < 4; c++) dst[c] = fmul((float)(p[bgra ? bgra_byte(c) : c] * 257), 1.0f / 0xFFFF);
     }
     else if(st->color_format == SWGB_FORMAT_R32G32B32A32_SFLOAT)
         memcpy(dst, row + (size_t)x * 16, 16);
@@ -1153,17 +1188,19 @@ static void write_color(const ODraw *d, int q, int x, int y, const float col[4])
     const swgb_pipeline_state *st = d->st;
     uint8_t *row = (uint8_t *)st->color + (size_t)q * st->color_slice_bytes + (size_t)y * st->color_pitch_bytes;
     uint32_t wm = st->color_write_mask;
-    if(st->color_format == SWGB_FORMAT_R8G8B8A8_UNORM)
+    if(is_unorm(st->color_format))
     {
-        /* writeColor (PixelRoutine.cpp:1975-1993,2609-2650) */
+        /* writeColor (PixelRoutine.cpp:1975-1993,2603-2650); B8G8R8A8 swaps
+         * R and B, and their write-mask bits with them (:2138-2143) */
         uint8_t *p = row + (size_t)x * 4;
+        const int bgra = st->color_format == SWGB_FORMAT_B8G8R8A8_UNORM;
         for(int c = 0; c < 4; c++)
         {
             float v = fminr(fmaxr(col[c], 0.0f), 1.0f);
             int32_t r = round_int(fmul(v, 255.0f));
             int16_t s16 = (int16_t)r;
             uint8_t b = s16 < 0 ? 0 : (s16 > 255 ? 255 : (uint8_t)s16); /* PackUnsigned */
-            if(wm & (1u << c)) p[c] = b;
+            if(wm & (1u << c)) p[bgra ? bgra_byte(c) : c] = b;
         }
     }
     else if(st->color_format == SWGB_FORMAT_R32G32B32A32_SFLOAT)
@@ -1180,10 +1217,33 @@ static void write_color(const ODraw *d, int q, int x, int y, const float col[4])
     }
 }
 
-static float *depth_at(const ODraw *d, int q, int x, int y)
+static void *depth_at(const ODraw *d, int q, int x, int y)
 {
     const swgb_pipeline_state *st = d->st;
-    return (float *)((uint8_t *)st->depth + (size_t)q * st->depth_slice_bytes + (size_t)y * st->depth_pitch_bytes + (size_t)x * 4);
+    return (uint8_t *)st->depth + (size_t)q * st->depth_slice_bytes + (size_t)y * st->depth_pitch_bytes + (size_t)x * (d16(st) ? 2 : 4);
+}
+
+/* Stored depth as the test compares it: D32_SFLOAT as is, D16_UNORM as the
+ * float of its integer (readDepth16, PixelRoutine.cpp:465-481). */
+static float read_depth(const ODraw *d, int q, int x, int y)
+{
+    if(d16(d->st)) return (float)*(const uint16_t *)depth_at(d, q, x, y);
+    return *(const float *)depth_at(d, q, x, y);
+}
+
+/* The fragment depth the test uses: Z for D32_SFLOAT, for D16_UNORM
+ * Min(Max(Round(Z * 0xFFFF), 0), 0xFFFF) (PixelRoutine.cpp:506-510); writeDepth16
+ * stores the same integer (:687-713). */
+static float depth_value(const ODraw *d, float Z)
+{
+    if(!d16(d->st)) return Z;
+    return fminr(fmaxr(nearbyintf(fmul(Z, 65535.0f)), 0.0f), 65535.0f);
+}
+
+static void write_depth(const ODraw *d, int q, int x, int y, float Z)
+{
+    if(d16(d->st)) *(uint16_t *)depth_at(d, q, x, y) = (uint16_t)Z;
+    else *(float *)depth_at(d, q, x, y) = Z;
 }
 
 /* One 2x2 quad of one primitive (PixelRoutine::quad :97-358); cMask[q] holds
@@ -1258,8 +1318,9 @@ static void pixel_quad(const ODraw *d, const OSampler *smp, const OPrim *pr, int
                 if(!(cMask[q] & (1 << i))) continue;
                 float Z = z[q][i];
                 if(d->depthClamp) Z = fminr(fmaxr(Z, d->minDepthClamp), d->maxDepthClamp);
+                Z = depth_value(d, Z);
                 z[q][i] = Z;
-                float zb = *depth_at(d, q, x + (i & 1), y + (i >> 1));
+                float zb = read_depth(d, q, x + (i & 1), y + (i >> 1));
                 int pass;
                 switch(st->depth_compare_op)
                 {
@@ -1277,7 +1338,7 @@ static void pixel_quad(const ODraw *d, const OSampler *smp, const OPrim *pr, int
             if(cnt) cnt->fragments_tested += (uint64_t)__builtin_popcount((unsigned)cMask[q]);
             if(d->depthWrite)
                 for(int i = 0; i < 4; i++)
-                    if(zMask & (1 << i)) *depth_at(d, q, x + (i & 1), y + (i >> 1)) = z[q][i];
+                    if(zMask & (1 << i)) write_depth(d, q, x + (i & 1), y + (i >> 1), z[q][i]);
         }
         if(cnt) cnt->fragments_passed += (uint64_t)__builtin_popcount((unsigned)zMask);
         if(d->vis)

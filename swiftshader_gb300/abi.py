@@ -20,6 +20,10 @@ STATUS_NAMES = {0: "OK", 1: "UNSUPPORTED_STATE", 2: "INVALID_ARG", 3: "OOM",
 
 # VkFormat subset
 FORMAT_R8G8B8A8_UNORM = 37
+FORMAT_R8G8B8A8_SRGB = 43
+FORMAT_B8G8R8A8_UNORM = 44
+FORMAT_B8G8R8A8_SRGB = 50
+FORMAT_D16_UNORM = 124
 FORMAT_R16G16B16A16_SFLOAT = 97
 FORMAT_R32G32_SFLOAT = 103
 FORMAT_R32G32B32A32_SFLOAT = 109
@@ -94,7 +98,7 @@ class PipelineState(C.Structure):
         ("color_write_mask", C.c_uint32), ("sample_count", C.c_uint32),
         ("color", C.c_void_p), ("color_pitch_bytes", C.c_uint32), ("reserved0", C.c_uint32),
         ("color_slice_bytes", C.c_uint64),
-        ("depth", C.c_void_p), ("depth_pitch_bytes", C.c_uint32), ("reserved1", C.c_uint32),
+        ("depth", C.c_void_p), ("depth_pitch_bytes", C.c_uint32), ("depth_format", C.c_uint32),
         ("depth_slice_bytes", C.c_uint64),
         ("framebuffer_width", C.c_uint32), ("framebuffer_height", C.c_uint32),
         ("texture", Texture),

@@ -1,6 +1,6 @@
 """Builds libswgb.so in-tree with nvcc for sm_103a.
 
-Four translation units are compiled in parallel and linked into one library:
+Five translation units are compiled in parallel and linked into one library:
 swgb_draw.cu (vertex, setup and adjoint kernels, host side, C-ABI) and
 swgb_raster.cu once per colour format (the raster kernel variants).
 
@@ -19,14 +19,14 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libswgb.so")
 # (source, extra defines, object name)
 UNITS = [("swgb_draw.cu", [], "swgb_draw.o")] + [
-    ("swgb_raster.cu", ["-DSWGB_RASTER_CF=%d" % cf], "swgb_raster_cf%d.o" % cf) for cf in range(3)]
+    ("swgb_raster.cu", ["-DSWGB_RASTER_CF=%d" % cf], "swgb_raster_cf%d.o" % cf) for cf in range(4)]
 SOURCES = [os.path.join(CSRC, u) for u in ("swgb_draw.cu", "swgb_raster.cu")]
 DEPS = SOURCES + [os.path.join(CSRC, h) for h in ("swgb_kernels.cuh", "swgb_numeric.cuh", "swgb_adjoint.cuh", "swgb.map")] + \
     [os.path.join(ROOT, "include", "swgb.h")]
 
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo", "-O3", "-std=c++17",
               "-ftz=true", "-prec-div=true", "-prec-sqrt=true", "-fmad=false",
-              "-Xcompiler", "-fPIC", "-diag-suppress", "177"]
+              "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-diag-suppress", "177"]
 
 
 def nvcc():

@@ -84,6 +84,7 @@ struct AdjShared {
     uint32_t logCount;               // blended: fragments appended to the region's log
     static constexpr int kSamples = MS;
     static constexpr int kBW = BIN, kBH = BIN;
+    static constexpr bool kD16 = false;  // the adjoint takes D32_SFLOAT depth only
 };
 
 // A bin's pixels may be split between four warps (quarters of 8x8 pixels,

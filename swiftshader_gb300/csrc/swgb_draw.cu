@@ -28,6 +28,7 @@
 //               src/Pipeline/PixelProgram.cpp:138-364,
 //               src/Pipeline/SamplerCore.cpp).
 #include <cuda_runtime.h>
+#include <math.h>
 #include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -72,6 +73,7 @@ struct swgb_ctx {
     size_t polyCap;
     uint32_t *polyCount;
     unsigned int *binQueue;
+    uint16_t *srgbLut;     // sRGBtoLinearFF_FF00 on the device (256 entries)
     uint32_t *restart;     // primitive restart: per-position segment starts, then per-block carries
     size_t restartCap;
     int *binDiff;          // longest-first bin order of single draws: difference array and order
@@ -169,6 +171,20 @@ void set_bins(DrawParams &D, int bw, int bh)
     D.binsY = (D.sy1 - D.binY0 + bh - 1) / bh;
 }
 
+// sRGBtoLinearFF_FF00, the table the reference's sampler decodes 8-bit sRGB
+// texels with (src/Pipeline/Constants.cpp:273-276, sw::sRGBtoLinear
+// src/System/Math.hpp:326-336): linear value with 0xFF00 = 1.0, computed on
+// the host at start-up as the reference does.
+void srgb_table(uint16_t out[256])
+{
+    for(int i = 0; i < 256; i++)
+    {
+        const float c = (float)i / 0xFF;
+        const float lin = c <= 0.04045f ? c / 12.92f : powf((c + 0.055f) / 1.055f, 2.4f);
+        out[i] = (uint16_t)(lin * 0xFF00 + 0.5f);
+    }
+}
+
 swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawParams &D)
 {
     memset(&D, 0, sizeof(D));
@@ -180,9 +196,11 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
     if(st->vertex_shader != SWGB_VS_MVP_PASSTHROUGH) return set_error(SWGB_UNSUPPORTED_STATE, "vertex_shader");
     if(st->fragment_shader != SWGB_FS_VCOLOR && st->fragment_shader != SWGB_FS_TEX_X_VCOLOR) return set_error(SWGB_UNSUPPORTED_STATE, "fragment_shader");
     if(st->depth_clamp_enable || st->depth_bias_constant != 0.0f || st->depth_bias_slope != 0.0f) return set_error(SWGB_UNSUPPORTED_STATE, "depth clamp / bias");
-    if(st->color_format != SWGB_FORMAT_R8G8B8A8_UNORM && st->color_format != SWGB_FORMAT_R16G16B16A16_SFLOAT &&
-       st->color_format != SWGB_FORMAT_R32G32B32A32_SFLOAT)
+    if(st->color_format != SWGB_FORMAT_R8G8B8A8_UNORM && st->color_format != SWGB_FORMAT_B8G8R8A8_UNORM &&
+       st->color_format != SWGB_FORMAT_R16G16B16A16_SFLOAT && st->color_format != SWGB_FORMAT_R32G32B32A32_SFLOAT)
         return set_error(SWGB_UNSUPPORTED_STATE, "color_format");
+    if(st->depth_format != SWGB_FORMAT_UNDEFINED && st->depth_format != SWGB_FORMAT_D32_SFLOAT && st->depth_format != SWGB_FORMAT_D16_UNORM)
+        return set_error(SWGB_UNSUPPORTED_STATE, "depth_format");
     if(!st->color) return set_error(SWGB_INVALID_ARG, "color attachment is null");
     if(st->attrib_count < 1 || st->attrib_count > SWGB_MAX_ATTRIBS) return set_error(SWGB_INVALID_ARG, "attrib_count");
     if(st->color_blend_op > SWGB_BLEND_OP_MAX || st->alpha_blend_op > SWGB_BLEND_OP_MAX) return set_error(SWGB_UNSUPPORTED_STATE, "blend op");
@@ -272,18 +290,29 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
     D.ms = (int)st->sample_count;
     D.colorSlice = st->color_slice_bytes;
     D.depthSlice = st->depth_slice_bytes;
-    D.cf = st->color_format == SWGB_FORMAT_R8G8B8A8_UNORM ? CF_RGBA8 : (st->color_format == SWGB_FORMAT_R16G16B16A16_SFLOAT ? CF_RGBA16F : CF_RGBA32F);
+    D.cf = st->color_format == SWGB_FORMAT_R8G8B8A8_UNORM ? CF_RGBA8
+           : st->color_format == SWGB_FORMAT_B8G8R8A8_UNORM ? CF_BGRA8
+           : (st->color_format == SWGB_FORMAT_R16G16B16A16_SFLOAT ? CF_RGBA16F : CF_RGBA32F);
+    D.depth16 = st->depth_format == SWGB_FORMAT_D16_UNORM;
     D.color = (uint8_t *)st->color;
     D.colorPitch = st->color_pitch_bytes;
     D.depth = (uint8_t *)st->depth;
     D.depthPitch = st->depth_pitch_bytes;
+    // 16-byte colour rows and 4-pixel depth groups (16 bytes D32F, 8 bytes D16)
+    const uint32_t dAlign = D.depth16 ? 8u : 16u;
     D.vec16 = ((uintptr_t)D.color % 16 == 0) && (D.colorPitch % 16 == 0) &&
-              (!D.depthTest || (((uintptr_t)D.depth % 16 == 0) && (D.depthPitch % 16 == 0)));
+              (!D.depthTest || (((uintptr_t)D.depth % dAlign == 0) && (D.depthPitch % dAlign == 0)));
 
     if(D.fs == SWGB_FS_TEX_X_VCOLOR)
     {
         const swgb_texture &t = st->texture;
-        if(t.format == SWGB_FORMAT_R8G8B8A8_UNORM) D.texFloat = 0;
+        if(t.format == SWGB_FORMAT_R8G8B8A8_UNORM || t.format == SWGB_FORMAT_B8G8R8A8_UNORM || t.format == SWGB_FORMAT_R8G8B8A8_SRGB ||
+           t.format == SWGB_FORMAT_B8G8R8A8_SRGB)
+        {
+            D.texFloat = 0;
+            D.texBGRA = t.format == SWGB_FORMAT_B8G8R8A8_UNORM || t.format == SWGB_FORMAT_B8G8R8A8_SRGB;
+            D.texSRGB = t.format == SWGB_FORMAT_R8G8B8A8_SRGB || t.format == SWGB_FORMAT_B8G8R8A8_SRGB;
+        }
         else if(t.format == SWGB_FORMAT_R16G16B16A16_SFLOAT) D.texFloat = 1;
         else if(t.format == SWGB_FORMAT_R32G32B32A32_SFLOAT) D.texFloat = 2;
         else return set_error(SWGB_UNSUPPORTED_STATE, "texture format");
@@ -330,13 +359,14 @@ const RasterKernel &raster_kernel(int v)
         fill_raster_table<CF_RGBA8>(t.data());
         fill_raster_table<CF_RGBA16F>(t.data());
         fill_raster_table<CF_RGBA32F>(t.data());
+        fill_raster_table<CF_BGRA8>(t.data());
         return t;
     }();
     return table[v];
 }
 
 // Raster kernel index of a draw: its bin shape, colour format and samples.
-inline int raster_variant(const DrawParams &D) { return raster_index(shape_index(D.binW, D.binH), D.hiz != 0, D.ms, D.cf); }
+inline int raster_variant(const DrawParams &D) { return raster_index(shape_index(D.binW, D.binH), D.hiz != 0, D.ms, D.cf, D.depth16 != 0); }
 
 // Persistent raster grid of one kernel variant: SMs x resident blocks.
 swgb_status raster_grid(int device, int v, bool batch, bool setAttr, int &blocks)
@@ -355,13 +385,18 @@ swgb_status raster_grid(int device, int v, bool batch, bool setAttr, int &blocks
     return SWGB_OK;
 }
 
-// Grids of every variant; without setAttr only the single-sample 16x16
-// variants (the allocation-free path's, whose shared memory needs no opt-in).
+// Grids of every variant; without setAttr only of the variants whose shared
+// memory needs no opt-in (the allocation-free path's single-sample 16x16
+// ones), 0 for the others.
 swgb_status raster_grids(int device, bool setAttr, int blocks[NRASTER])
 {
     swgb_status s;
-    for(int v = 0; v < (setAttr ? NRASTER : 6); v++)
+    for(int v = 0; v < NRASTER; v++)
+    {
+        blocks[v] = 0;
+        if(!setAttr && raster_kernel(v).smem > 48 * 1024) continue;
         if((s = raster_grid(device, v, false, setAttr, blocks[v])) != SWGB_OK) return s;
+    }
     return SWGB_OK;
 }
 
@@ -436,6 +471,7 @@ swgb_status prepare_scratch(swgb_ctx *ctx, DrawParams &D, bool order = true)
     D.polyCapacity = (uint32_t)(ctx->polyCap / MAX_POLY);
     D.counters = ctx->counters;
     D.error = ctx->error;
+    D.srgbLut = ctx->srgbLut;
     if(!ctx->rasterAttr)
     {
         if((s = raster_grids(ctx->device, true, ctx->rasterBlocks)) != SWGB_OK) return s;
@@ -475,7 +511,7 @@ swgb_status prepare_scratch(swgb_ctx *ctx, DrawParams &D, bool order = true)
 // draws keep 16x16 bins).
 void apply_config(const swgb_ctx *ctx, DrawParams &D)
 {
-    if(D.ms == 1) set_bins(D, (int)ctx->rasterConfig.bin_width, (int)ctx->rasterConfig.bin_height);
+    if(D.ms == 1 && !D.depth16) set_bins(D, (int)ctx->rasterConfig.bin_width, (int)ctx->rasterConfig.bin_height);
     D.hiz = (int)ctx->rasterConfig.hiz;
 }
 
@@ -599,8 +635,8 @@ void draw_writes(const DrawParams &D, uintptr_t origin, std::vector<TouchRect> &
         plane_rects((uintptr_t)D.color + (uintptr_t)q * D.colorSlice, origin, D.colorPitch, (int64_t)D.sx0 * cbpp,
                     (int64_t)D.sx1 * cbpp, D.sy0, D.sy1, out);
         if(D.depthTest)
-            plane_rects((uintptr_t)D.depth + (uintptr_t)q * D.depthSlice, origin, D.depthPitch, (int64_t)D.sx0 * 4,
-                        (int64_t)D.sx1 * 4, D.sy0, D.sy1, out);
+            plane_rects((uintptr_t)D.depth + (uintptr_t)q * D.depthSlice, origin, D.depthPitch, (int64_t)D.sx0 * (D.depth16 ? 2 : 4),
+                        (int64_t)D.sx1 * (D.depth16 ? 2 : 4), D.sy0, D.sy1, out);
     }
 }
 
@@ -666,7 +702,7 @@ void draw_reads(const swgb_pipeline_state &st, const swgb_draw_args &a, const Dr
     }
     if(D.fs == SWGB_FS_TEX_X_VCOLOR)
     {
-        const uintptr_t tb = st.texture.format == SWGB_FORMAT_R8G8B8A8_UNORM ? 4 : st.texture.format == SWGB_FORMAT_R16G16B16A16_SFLOAT ? 8 : 16;
+        const uintptr_t tb = D.texFloat == 0 ? 4 : D.texFloat == 1 ? 8 : 16;
         for(uint32_t l = 0; l < st.texture.level_count && l < SWGB_MAX_MIP_LEVELS; l++)
         {
             const swgb_texture_level &lv = st.texture.levels[l];
@@ -882,6 +918,7 @@ swgb_status enqueue_segment(swgb_ctx *ctx, std::vector<DrawParams> &draws, uint3
         d.polyCount = ctx->polyCount;
         d.polyCapacity = (uint32_t)std::min<size_t>(B.polyCap / MAX_POLY, 0xFFFFFFFFu);
         d.counters = ctx->counters;
+        d.srgbLut = ctx->srgbLut;
         d.error = ctx->error;
         d.binQueue = B.queue;
         const uint32_t vc = d.count ? d.vertexCount : 0;
@@ -1031,8 +1068,9 @@ swgb_status bake_adjoint(const swgb_pipeline_state *st, const swgb_draw_args *a,
                          AdjParams &A)
 {
     if(!g) return set_error(SWGB_INVALID_ARG, "null adjoint arguments");
-    if(D.cf == CF_RGBA8) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint needs a float colour attachment");
+    if(cf_unorm8(D.cf)) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint needs a float colour attachment");
     if(D.restart) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint: primitive restart is not supported");
+    if(D.depth16) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint needs a D32_SFLOAT depth attachment");
     if(D.fs == SWGB_FS_TEX_X_VCOLOR && !D.texFloat) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint needs a float texture");
     if(D.writeMask != 0xFu) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint needs color_write_mask 0xF");
     if(a->count > ADJ_TRI_MASK) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint: too many triangles");
@@ -1278,6 +1316,14 @@ swgb_status swgb_ctx_create(int device, void *stream, swgb_ctx **out)
         swgb_ctx_destroy(c);
         return s;
     }
+    uint16_t lut[256];
+    srgb_table(lut);
+    if((s = cuda_check(cudaMalloc((void **)&c->srgbLut, sizeof(lut)), "sRGB table")) != SWGB_OK ||
+       (s = cuda_check(cudaMemcpy(c->srgbLut, lut, sizeof(lut), cudaMemcpyHostToDevice), "sRGB table")) != SWGB_OK)
+    {
+        swgb_ctx_destroy(c);
+        return s;
+    }
     cudaMemset(c->counters, 0, CTX_COUNTERS * sizeof(unsigned long long));
     cudaMemset(c->error, 0, sizeof(int));
     cudaMemset(c->polyCount, 0, sizeof(uint32_t));
@@ -1293,6 +1339,7 @@ swgb_status swgb_ctx_destroy(swgb_ctx *c)
     cudaFree(c->ptv);
     cudaFree(c->binDiff);
     cudaFree(c->restart);
+    cudaFree(c->srgbLut);
     cudaFree(c->binOrder);
     cudaFree(c->triBox);
     cudaFree(c->triInfo);
@@ -1364,6 +1411,7 @@ swgb_status swgb_draw_noalloc(const swgb_pipeline_state *st, const swgb_draw_arg
     swgb_status s = bake(st, args, D);
     if(s != SWGB_OK) return s;
     if(D.ms > 1) return set_error(SWGB_UNSUPPORTED_STATE, "swgb_draw_noalloc: multisampled attachments need swgb_draw");
+    if(D.texSRGB) return set_error(SWGB_UNSUPPORTED_STATE, "swgb_draw_noalloc: sRGB textures need swgb_draw");
     if(D.vertexCount > SWGB_NOALLOC_MAX_VERTICES)
         return set_error(SWGB_INVALID_ARG, "swgb_draw_noalloc: vertex_count above SWGB_NOALLOC_MAX_VERTICES (98304)");
     int dev = 0;
@@ -1456,7 +1504,7 @@ swgb_status swgb_autotune(swgb_ctx *ctx, const swgb_pipeline_state *states, cons
             if(st.depth)
             {
                 const uintptr_t d = (uintptr_t)st.depth + (uintptr_t)q * D.depthSlice;
-                iv.push_back({d, d + (uintptr_t)(h - 1) * st.depth_pitch_bytes + (size_t)st.framebuffer_width * 4});
+                iv.push_back({d, d + (uintptr_t)(h - 1) * st.depth_pitch_bytes + (size_t)st.framebuffer_width * (D.depth16 ? 2 : 4)});
             }
         }
     }

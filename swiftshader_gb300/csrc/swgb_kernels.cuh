@@ -34,7 +34,7 @@ constexpr int MAX_POLY = 16;     // clipped polygon capacity (Polygon::B, src/De
 constexpr int NSHAPES = 3;
 constexpr int SHAPE_W[NSHAPES] = {16, 32, 32};
 constexpr int SHAPE_H[NSHAPES] = {16, 16, 32};
-constexpr int NRASTER = NSHAPES * 6 + 6;  // (shape, hiz, format) single-sample, then (hiz, format) four-sample
+constexpr int NRASTER = NSHAPES * 2 * 4 + 2 * 4 + 4 * 4;  // see raster_index
 inline int shape_index(int w, int h)
 {
     for(int i = 0; i < NSHAPES; i++)
@@ -116,6 +116,10 @@ struct DrawParams {
     int ms;       // samples per pixel: 1 or 4
     uint64_t colorSlice, depthSlice;  // bytes between sample planes
     int cf;       // colour attachment format, CF_*
+    int depth16;   // D16_UNORM depth attachment (else D32_SFLOAT)
+    int texBGRA;   // 8-bit texture stored B8G8R8A8
+    int texSRGB;   // 8-bit texture with sRGB-encoded R, G, B (decoded through srgbLut)
+    const uint16_t *srgbLut;  // sRGBtoLinearFF_FF00: 8-bit sRGB -> 16-bit linear (0xFF00 = 1.0)
     int texFloat; // 0: R8G8B8A8_UNORM texture (16-bit path), 1: RGBA16F, 2: RGBA32F (fp32 path)
     uint8_t *color;
     uint32_t colorPitch;
@@ -1082,6 +1086,47 @@ __device__ __forceinline__ uint32_t offset_sample(uint32_t uvw, uint32_t half, b
 }
 
 // computeIndices + 8-bit unpack (SamplerCore.cpp:1593-1643,1747-1788): returns the texel as 4 bytes.
+// The components of an 8-bit texel as the 16-bit path holds them
+// (SamplerCore.cpp:1747-1788): byte << 8 in R, G, B, A order (B8G8R8A8 texels,
+// R and B swapped in memory, are put in that order first with texel_order);
+// the R, G, B of an sRGB texture become their sRGBtoLinearFF_FF00 entry
+// (:1966-1978,2670-2680).
+__device__ __forceinline__ uint32_t texel_order(const DrawParams &D)
+{
+    return D.texBGRA ? 0x3012u : 0x3210u;  // __byte_perm selector
+}
+
+__device__ __forceinline__ void texel_components(const DrawParams &D, uint32_t t, uint32_t out[4])
+{
+#pragma unroll
+    for(int c = 0; c < 4; c++) out[c] = ((t >> (8 * c)) & 0xFFu) << 8;
+    if(D.texSRGB)
+#pragma unroll
+        for(int c = 0; c < 3; c++) out[c] = __ldg(D.srgbLut + (out[c] >> 8));
+}
+
+// bilinearInterpolate of sRGB texels (SamplerCore.cpp:516-575 after the
+// table decode).  Out of line: the raster loop carries it for sRGB textures
+// only.
+static __device__ __noinline__ void bilinear_srgb(const DrawParams &D, uint32_t t00, uint32_t t10, uint32_t t01, uint32_t t11,
+                                                  uint32_t f0u0v, uint32_t f1u0v, uint32_t f0u1v, uint32_t f1u1v, uint32_t out[4])
+{
+    uint32_t c00[4], c10[4], c01[4], c11[4];
+    texel_components(D, t00, c00);
+    texel_components(D, t10, c10);
+    texel_components(D, t01, c01);
+    texel_components(D, t11, c11);
+#pragma unroll
+    for(int c = 0; c < 4; c++)
+    {
+        uint32_t a = mulhi_u16(c00[c], f1u1v);
+        uint32_t b = mulhi_u16(c10[c], f0u1v);
+        uint32_t e = mulhi_u16(c01[c], f1u0v);
+        uint32_t g = mulhi_u16(c11[c], f0u0v);
+        out[c] = (((a + b) & 0xFFFFu) + ((e + g) & 0xFFFFu)) & 0xFFFFu;
+    }
+}
+
 __device__ __forceinline__ uint32_t texel_rgba8(const TexLevel &lv, uint32_t u, uint32_t v)
 {
     uint32_t xi = mulhi_u16(u, lv.w);
@@ -1102,9 +1147,7 @@ __device__ __forceinline__ void sample_quad_2d(const DrawParams &D, float u, flo
     uint32_t vv = address16(v, D.addrV);
     if(!D.texLinear)
     {
-        uint32_t t = texel_rgba8(lv, uu, vv);
-#pragma unroll
-        for(int c = 0; c < 4; c++) out[c] = ((t >> (8 * c)) & 0xFFu) << 8;
+        texel_components(D, __byte_perm(texel_rgba8(lv, uu, vv), 0u, texel_order(D)), out);
         return;
     }
     bool wu = D.addrU == SWGB_ADDRESS_REPEAT, wv = D.addrV == SWGB_ADDRESS_REPEAT;
@@ -1112,11 +1155,23 @@ __device__ __forceinline__ void sample_quad_2d(const DrawParams &D, float u, flo
     uint32_t u1 = offset_sample(uu, lv.uHalf, wu, +1), v1 = offset_sample(vv, lv.vHalf, wv, +1);
     uint32_t t00 = texel_rgba8(lv, u0, v0), t10 = texel_rgba8(lv, u1, v0);
     uint32_t t01 = texel_rgba8(lv, u0, v1), t11 = texel_rgba8(lv, u1, v1);
+    {
+        const uint32_t sel = texel_order(D);
+        t00 = __byte_perm(t00, 0u, sel);
+        t10 = __byte_perm(t10, 0u, sel);
+        t01 = __byte_perm(t01, 0u, sel);
+        t11 = __byte_perm(t11, 0u, sel);
+    }
     // bilinearInterpolate, unsigned 8-bit components (:516-575)
     uint32_t f0u = (u0 * lv.w) & 0xFFFFu, f0v = (v0 * lv.h) & 0xFFFFu;
     uint32_t f1u = (~f0u) & 0xFFFFu, f1v = (~f0v) & 0xFFFFu;
     uint32_t f0u0v = mulhi_u16(f0u, f0v), f1u0v = mulhi_u16(f1u, f0v);
     uint32_t f0u1v = mulhi_u16(f0u, f1v), f1u1v = mulhi_u16(f1u, f1v);
+    if(D.texSRGB)
+    {
+        bilinear_srgb(D, t00, t10, t01, t11, f0u0v, f1u0v, f0u1v, f1u1v, out);
+        return;
+    }
 #pragma unroll
     for(int c = 0; c < 4; c++)
     {
@@ -1325,6 +1380,17 @@ static __device__ __noinline__ void blend_generic(const DrawParams &D, const flo
     out[3] = blend_op(D.opA, col[3], sf[3], dst[3], df[3]);
 }
 
+// The depth a fragment tests and writes: z itself for D32_SFLOAT; for
+// D16_UNORM Min(Max(Round(z * 0xFFFF), 0), 0xFFFF), compared against the
+// stored 16-bit value as a float and written back as that integer
+// (PixelRoutine.cpp:506-510,687-713).  Monotonic in z.
+template<bool D16>
+__device__ __forceinline__ float depth_value(float z)
+{
+    if(!D16) return z;
+    return fminf(fmaxf(rintf(z * 65535.0f), 0.0f), 65535.0f);
+}
+
 __device__ __forceinline__ bool depth_pass(uint32_t op, float zb, float z)
 {
     switch(op)
@@ -1350,13 +1416,16 @@ __device__ __forceinline__ bool depth_pass(uint32_t op, float zb, float z)
 
 // 32-bit words per pixel of a colour attachment: R8G8B8A8_UNORM,
 // R16G16B16A16_SFLOAT, R32G32B32A32_SFLOAT.
-enum { CF_RGBA8 = 0, CF_RGBA16F = 1, CF_RGBA32F = 2 };
-__host__ __device__ constexpr int color_words(int cf) { return cf == CF_RGBA8 ? 1 : (cf == CF_RGBA16F ? 2 : 4); }
+// R8G8B8A8_UNORM, R16G16B16A16_SFLOAT, R32G32B32A32_SFLOAT, B8G8R8A8_UNORM.
+enum { CF_RGBA8 = 0, CF_RGBA16F = 1, CF_RGBA32F = 2, CF_BGRA8 = 3, NCF = 4 };
+__host__ __device__ constexpr bool cf_unorm8(int cf) { return cf == CF_RGBA8 || cf == CF_BGRA8; }
+__host__ __device__ constexpr int color_words(int cf) { return cf_unorm8(cf) ? 1 : (cf == CF_RGBA16F ? 2 : 4); }
 
 // Shared memory of one warp: its bin's depth and colour, the staged batch,
 // and its ordered candidate list.
-// BW x BH is the bin's shape in pixels (powers of two, BH even).
-template<int CF, int MS, int BW = BIN, int BH = BIN>
+// BW x BH is the bin's shape in pixels (powers of two, BH even); D16: the
+// depth attachment is D16_UNORM (the staged depth holds its integers).
+template<int CF, int MS, int BW = BIN, int BH = BIN, bool D16 = false>
 struct RasterShared {
     float depth[MS][BW * BH];
     uint32_t color[MS][BW * BH * color_words(CF)];
@@ -1369,6 +1438,7 @@ struct RasterShared {
     int triList[2 * BATCH];
     static constexpr int kSamples = MS;
     static constexpr int kBW = BW, kBH = BH;
+    static constexpr bool kD16 = D16;
 };
 
 
@@ -1507,21 +1577,6 @@ __device__ int setup_batch_triangle(const DrawParams &D, SH &S, int ti, uint32_t
     return pre;
 }
 
-template<class SH>
-__device__ __forceinline__ void quad_depth(const DrawParams &D, const SH &S, int ti, int qx, int y, float zq[4])
-{
-    const float x0p = S.plane[0][ti], y0p = S.plane[1][ti];
-    const float zA = S.plane[2][ti], zB = S.plane[3][ti], zC = S.plane[4][ti];
-#pragma unroll
-    for(int i = 0; i < 4; i++)
-    {
-        float xF = ((float)qx + (float)(i & 1)) - x0p;
-        float yF = ((float)y + (float)(i >> 1)) - y0p;
-        float z = mul_add(xF, zA, zC + yF * zB);
-        zq[i] = rmin(rmax(z, D.minDepthClamp), D.maxDepthClamp);  // clampDepth
-    }
-}
-
 // Shades one covered pixel (lane i of the 2x2 quad at (qx, y)) of batch
 // triangle ti: interpolation (PixelRoutine::quad :124-261), the fixed fragment
 // shader with SamplerCore filtering (the LOD comes from lanes 0, 1 and 2 of the
@@ -1568,7 +1623,7 @@ __device__ __forceinline__ void shade_pixel(const DrawParams &D, const SH &S, in
         for(int k = 0; k < 4; k++) c[k] = t[k] * c[k];
     }
 #pragma unroll
-    for(int k = 0; k < 4; k++) col[k] = CF == CF_RGBA8 ? rmin(rmax(c[k], 0.0f), 1.0f) : c[k];  // clampColor: UNORM only
+    for(int k = 0; k < 4; k++) col[k] = cf_unorm8(CF) ? rmin(rmax(c[k], 0.0f), 1.0f) : c[k];  // clampColor: UNORM only
 }
 
 // Depth test/write, blend and colour write of one pixel of the staged bin
@@ -1591,10 +1646,11 @@ __device__ __forceinline__ void rop_pixel(const DrawParams &D, SH &S, int q, int
     if(D.blend)
     {
         float dst[4];
-        if(CF == CF_RGBA8)
+        if(cf_unorm8(CF))
         {
-            // readPixel widens b to b * 257, alphaBlend scales by 1 / 0xFFFF
-            const uint32_t old = color[idx];
+            // readPixel widens b to b * 257, alphaBlend scales by 1 / 0xFFFF;
+            // B8G8R8A8 holds R in byte 2 and B in byte 0 (PixelRoutine.cpp:1091-1108)
+            const uint32_t old = CF == CF_BGRA8 ? __byte_perm(color[idx], 0u, 0x3012u) : color[idx];
 #pragma unroll
             for(int c = 0; c < 4; c++) dst[c] = (float)(((old >> (8 * c)) & 0xFFu) * 257u) * (1.0f / 0xFFFF);
         }
@@ -1627,9 +1683,11 @@ __device__ __forceinline__ void rop_pixel(const DrawParams &D, SH &S, int q, int
 #pragma unroll
         for(int c = 0; c < 4; c++) out[c] = col[c];
     }
-    if(CF == CF_RGBA8)
+    if(cf_unorm8(CF))
     {
-        uint32_t packed = color[idx];
+        // packed in R, G, B, A byte order; B8G8R8A8 swaps R and B back on the
+        // way out, and its write-mask bits with them (:2138-2143)
+        uint32_t packed = CF == CF_BGRA8 ? __byte_perm(color[idx], 0u, 0x3012u) : color[idx];
 #pragma unroll
         for(int c = 0; c < 4; c++)
         {
@@ -1639,7 +1697,7 @@ __device__ __forceinline__ void rop_pixel(const DrawParams &D, SH &S, int q, int
             uint32_t b = s16 < 0 ? 0u : (s16 > 255 ? 255u : (uint32_t)s16);  // PackUnsigned
             if(D.writeMask & (1u << c)) packed = (packed & ~(0xFFu << (8 * c))) | (b << (8 * c));
         }
-        color[idx] = packed;
+        color[idx] = CF == CF_BGRA8 ? __byte_perm(packed, 0u, 0x3012u) : packed;
     }
     else if(CF == CF_RGBA16F)
     {
@@ -1690,7 +1748,7 @@ __device__ __forceinline__ float sample_depth(const DrawParams &D, const SH &S, 
         xF = xF - SLX[q];
     }
     const float z = mul_add(xF, S.plane[2][ti], S.plane[4][ti] + yF * S.plane[3][ti]);
-    return rmin(rmax(z, D.minDepthClamp), D.maxDepthClamp);  // clampDepth
+    return depth_value<SH::kD16>(rmin(rmax(z, D.minDepthClamp), D.maxDepthClamp));  // clampDepth
 }
 
 // Hierarchical depth rejection of whole triangle-bin pairs.  Under LESS /
@@ -1747,13 +1805,13 @@ __device__ __forceinline__ bool hiz_rejects(const DrawParams &D, const SH &S, in
         const float xF = zA >= 0.0f ? xFa : xFb, yF = zB >= 0.0f ? yFa : yFb;
         float zlo = ((zC + yF * zB) + xF * zA) - margin;
         if(!(zlo >= D.minDepthClamp)) zlo = D.minDepthClamp;  // also NaN
-        zlo = fminf(zlo, D.maxDepthClamp);
+        zlo = depth_value<SH::kD16>(fminf(zlo, D.maxDepthClamp));
         return op == SWGB_COMPARE_LESS ? zb <= zlo : zb < zlo;
     }
     const float xF = zA >= 0.0f ? xFb : xFa, yF = zB >= 0.0f ? yFb : yFa;
     float zhi = ((zC + yF * zB) + xF * zA) + margin;
     if(!(zhi <= D.maxDepthClamp)) zhi = D.maxDepthClamp;
-    zhi = fmaxf(zhi, D.minDepthClamp);
+    zhi = depth_value<SH::kD16>(fmaxf(zhi, D.minDepthClamp));
     return op == SWGB_COMPARE_GREATER ? zb >= zhi : zb > zhi;
 }
 
@@ -1815,8 +1873,8 @@ __device__ __noinline__ int hiz_pass(const DrawParams &D, const SH &S, int cnt, 
 // per lane (once per pixel, at its centre); lanes hitting the same pixel
 // resolve lowest lane (earliest triangle) first, all of the pixel's samples
 // at once.
-template<int CF, int MS, int BW, int BH, bool HIZ>
-__device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared<CF, MS, BW, BH> &S, int nb, int bx0, int by0, uint32_t inMask,
+template<int CF, int MS, int BW, int BH, bool HIZ, bool D16>
+__device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared<CF, MS, BW, BH, D16> &S, int nb, int bx0, int by0, uint32_t inMask,
                                           unsigned long long &nQuads, unsigned long long &nTested,
                                           unsigned long long &nPassed, uint32_t &lvMask)
 {
@@ -2045,8 +2103,8 @@ __device__ __forceinline__ void walk_bin(const DrawParams &D, SH &S, int bx0, in
 
 // One bin of a draw: stage its depth and colour, walk the candidates in
 // primitive order in batches, write the bin back.
-template<int CF, int MS, int BW, int BH, bool HIZ>
-__device__ __forceinline__ void raster_bin(const DrawParams &D, RasterShared<CF, MS, BW, BH> &S, int bin, unsigned long long &nQuads,
+template<int CF, int MS, int BW, int BH, bool HIZ, bool D16>
+__device__ __forceinline__ void raster_bin(const DrawParams &D, RasterShared<CF, MS, BW, BH, D16> &S, int bin, unsigned long long &nQuads,
                                            unsigned long long &nTested, unsigned long long &nPassed, uint32_t &lvMask)
 {
     const int lane = threadIdx.x & 31;
@@ -2067,7 +2125,26 @@ __device__ __forceinline__ void raster_bin(const DrawParams &D, RasterShared<CF,
             if(D.depthTest && py < D.sy1 && px < D.sx1)
             {
                 const uint8_t *drow = dbase + (size_t)py * D.depthPitch;
-                if(D.vec16 && px + 4 <= D.sx1)
+                if(D16)
+                {
+                    // D16_UNORM: the stored integers as floats (readDepth16)
+                    uint32_t w0 = 0, w1 = 0;
+                    if(D.vec16 && px + 4 <= D.sx1)
+                    {
+                        const uint2 v = *(const uint2 *)(drow + (size_t)px * 2);
+                        w0 = v.x;
+                        w1 = v.y;
+                    }
+                    else
+                    {
+                        uint32_t h[4] = {0, 0, 0, 0};
+                        for(int k = 0; k < 4 && px + k < D.sx1; k++) h[k] = *(const uint16_t *)(drow + (size_t)(px + k) * 2);
+                        w0 = h[0] | h[1] << 16;
+                        w1 = h[2] | h[3] << 16;
+                    }
+                    dz = make_float4((float)(w0 & 0xFFFFu), (float)(w0 >> 16), (float)(w1 & 0xFFFFu), (float)(w1 >> 16));
+                }
+                else if(D.vec16 && px + 4 <= D.sx1)
                     dz = *(const float4 *)(drow + (size_t)px * 4);
                 else
                 {
@@ -2113,7 +2190,7 @@ __device__ __forceinline__ void raster_bin(const DrawParams &D, RasterShared<CF,
         }
 
     // ---- candidates in primitive order, in batches of BATCH ----------------------
-    walk_bin(D, S, bx0, by0, [&](int nb) { raster_batch<CF, MS, BW, BH, HIZ>(D, S, nb, bx0, by0, inMask, nQuads, nTested, nPassed, lvMask); });
+    walk_bin(D, S, bx0, by0, [&](int nb) { raster_batch<CF, MS, BW, BH, HIZ, D16>(D, S, nb, bx0, by0, inMask, nQuads, nTested, nPassed, lvMask); });
 
     // ---- write the bin back, every sample plane ----------------------------------
     for(int q = 0; q < MS; q++)
@@ -2127,7 +2204,18 @@ __device__ __forceinline__ void raster_bin(const DrawParams &D, RasterShared<CF,
             const int px = bx0 + lx, py = by0 + ly;
             if(py >= D.sy1 || px >= D.sx1 || py < D.sy0) continue;
             uint8_t *drow = dbase + (size_t)py * D.depthPitch;
-            if(D.vec16 && px + 4 <= D.sx1 && px >= D.sx0)
+            if(D16)
+            {
+                // D16_UNORM: the staged values are integers 0..65535
+                const float4 v = *(const float4 *)&S.depth[q][ly * BW + lx];
+                const uint32_t h[4] = {(uint32_t)v.x, (uint32_t)v.y, (uint32_t)v.z, (uint32_t)v.w};
+                if(D.vec16 && px + 4 <= D.sx1 && px >= D.sx0)
+                    *(uint2 *)(drow + (size_t)px * 2) = make_uint2(h[0] | h[1] << 16, h[2] | h[3] << 16);
+                else
+                    for(int k = 0; k < 4 && px + k < D.sx1; k++)
+                        if(px + k >= D.sx0) *(uint16_t *)(drow + (size_t)(px + k) * 2) = (uint16_t)h[k];
+            }
+            else if(D.vec16 && px + 4 <= D.sx1 && px >= D.sx0)
                 *(float4 *)(drow + (size_t)px * 4) = *(const float4 *)&S.depth[q][ly * BW + lx];
             else
                 for(int k = 0; k < 4 && px + k < D.sx1; k++)
@@ -2152,19 +2240,19 @@ __device__ __forceinline__ void raster_bin(const DrawParams &D, RasterShared<CF,
 // Shared memory of a raster block and the blocks one SM holds with it (the
 // register budget follows from that: 65536 / (blocks x threads)).
 template<int CF, int MS, int BW, int BH>
-constexpr size_t raster_smem() { return RASTER_WARPS * sizeof(RasterShared<CF, MS, BW, BH>); }
+constexpr size_t raster_smem() { return RASTER_WARPS * sizeof(RasterShared<CF, MS, BW, BH, false>); }  // D16 changes no size
 template<int CF, int MS, int BW, int BH>
 constexpr int raster_min_blocks()
 {
     return (int)std::min<size_t>(8, std::max<size_t>(1, (size_t)(228 * 1024) / (raster_smem<CF, MS, BW, BH>() + 1024)));
 }
 
-template<int CF, int MS, int BW, int BH, bool HIZ>
+template<int CF, int MS, int BW, int BH, bool HIZ, bool D16>
 __global__ void __launch_bounds__(RASTER_THREADS, (raster_min_blocks<CF, MS, BW, BH>())) k_raster(const __grid_constant__ DrawParams D)
 {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    RasterShared<CF, MS, BW, BH> &S = reinterpret_cast<RasterShared<CF, MS, BW, BH> *>(smem_raw)[warp];
+    RasterShared<CF, MS, BW, BH, D16> &S = reinterpret_cast<RasterShared<CF, MS, BW, BH, D16> *>(smem_raw)[warp];
     const int nbins = D.binsX * D.binsY;
     unsigned long long nQuads = 0, nTested = 0, nPassed = 0;
     uint32_t lvMask = 0;
@@ -2177,7 +2265,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, (raster_min_blocks<CF, MS, BW,
         bin = __shfl_sync(0xFFFFFFFFu, bin, 0);
         if(bin >= nbins) break;
         if(D.binOrder) bin = (int)__ldg(D.binOrder + bin);
-        raster_bin<CF, MS, BW, BH, HIZ>(D, S, bin, nQuads, nTested, nPassed, lvMask);
+        raster_bin<CF, MS, BW, BH, HIZ, D16>(D, S, bin, nQuads, nTested, nPassed, lvMask);
     }
     flush_counters(D.counters, nQuads, nTested, nPassed, lvMask);
 }
@@ -2278,12 +2366,12 @@ __global__ void __launch_bounds__(SETUP_THREADS) k_setup_batch(const __grid_cons
 
 #endif  // SWGB_RASTER_TU
 
-template<int CF, int MS, int BW, int BH, bool HIZ>
+template<int CF, int MS, int BW, int BH, bool HIZ, bool D16>
 __global__ void __launch_bounds__(RASTER_THREADS, (raster_min_blocks<CF, MS, BW, BH>())) k_raster_batch(const __grid_constant__ BatchPtrs B)
 {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    RasterShared<CF, MS, BW, BH> &S = reinterpret_cast<RasterShared<CF, MS, BW, BH> *>(smem_raw)[warp];
+    RasterShared<CF, MS, BW, BH, D16> &S = reinterpret_cast<RasterShared<CF, MS, BW, BH, D16> *>(smem_raw)[warp];
     const BatchView V(B.hdr);
     const BatchHeader &h = V.h;
     unsigned long long nQuads = 0, nTested = 0, nPassed = 0;
@@ -2295,7 +2383,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, (raster_min_blocks<CF, MS, BW,
         bin = __shfl_sync(0xFFFFFFFFu, bin, 0);
         if(bin >= h.bins) break;
         const uint32_t d = find_draw(V.bStart, h.n, bin);
-        raster_bin<CF, MS, BW, BH, HIZ>(V.draws[d], S, (int)(bin - __ldg(V.bStart + d)), nQuads, nTested, nPassed, lvMask);
+        raster_bin<CF, MS, BW, BH, HIZ, D16>(V.draws[d], S, (int)(bin - __ldg(V.bStart + d)), nQuads, nTested, nPassed, lvMask);
     }
     flush_counters(B.counters, nQuads, nTested, nPassed, lvMask);
 }
@@ -2318,10 +2406,13 @@ struct RasterKernel {
     void (*launchBatch)(const BatchPtrs &, uint32_t, cudaStream_t);
 };
 
-// Table index of a variant: single-sample (shape, hiz) then four-sample hiz.
-__host__ __device__ constexpr int raster_index(int shape, bool hiz, int ms, int cf)
+// Table index of a variant: single-sample D32F draws by (shape, hiz, format);
+// four-sample D32F draws (16x16) by (hiz, format); D16_UNORM draws (16x16) by
+// (samples, hiz, format).
+__host__ __device__ constexpr int raster_index(int shape, bool hiz, int ms, int cf, bool d16)
 {
-    return ms > 1 ? NSHAPES * 6 + (hiz ? 0 : 3) + cf : (shape * 2 + (hiz ? 0 : 1)) * 3 + cf;
+    return d16 ? NSHAPES * 2 * NCF + 2 * NCF + ((ms > 1 ? 2 : 0) + (hiz ? 0 : 1)) * NCF + cf
+               : (ms > 1 ? NSHAPES * 2 * NCF + (hiz ? 0 : 1) * NCF + cf : (shape * 2 + (hiz ? 0 : 1)) * NCF + cf);
 }
 
 template<int CF>
@@ -2329,6 +2420,7 @@ void fill_raster_table(RasterKernel *table);
 template<> void fill_raster_table<CF_RGBA8>(RasterKernel *table);
 template<> void fill_raster_table<CF_RGBA16F>(RasterKernel *table);
 template<> void fill_raster_table<CF_RGBA32F>(RasterKernel *table);
+template<> void fill_raster_table<CF_BGRA8>(RasterKernel *table);
 
 }  // namespace swgbk
 

@@ -47,6 +47,8 @@ class Scene:
     first_vertex: int = 0
     base_vertex: int = 0
     provoking_vertex: int = 0         # 0 = FIRST_VERTEX, 1 = LAST_VERTEX (VK_EXT_provoking_vertex)
+    depth_format: int = abi.FORMAT_D32_SFLOAT  # or FORMAT_D16_UNORM
+    color_write_mask: int = 0xF       # VkColorComponentFlags
     restart_index_count: int = 0      # > 0: primitive restart over this many indices (tri_count ignored)
 
     @property
@@ -330,15 +332,16 @@ def build_state(scene, color_ptr, depth_ptr, vertex_ptr, level_ptrs=None, color_
         st.blend_enable = 1
         (st.src_color_factor, st.dst_color_factor, st.color_blend_op,
          st.src_alpha_factor, st.dst_alpha_factor, st.alpha_blend_op) = scene.blend
-    st.color_write_mask = 0xF
+    st.color_write_mask = scene.color_write_mask
     st.sample_count = scene.samples
-    bpp = {abi.FORMAT_R8G8B8A8_UNORM: 4, abi.FORMAT_R16G16B16A16_SFLOAT: 8,
+    bpp = {abi.FORMAT_R8G8B8A8_UNORM: 4, abi.FORMAT_B8G8R8A8_UNORM: 4, abi.FORMAT_R16G16B16A16_SFLOAT: 8,
            abi.FORMAT_R32G32B32A32_SFLOAT: 16}[scene.color_format]
     st.color = color_ptr
     st.color_pitch_bytes = color_pitch or scene.width * bpp
     st.color_slice_bytes = st.color_pitch_bytes * scene.height
     st.depth = depth_ptr
-    st.depth_pitch_bytes = depth_pitch or scene.width * 4
+    st.depth_format = scene.depth_format
+    st.depth_pitch_bytes = depth_pitch or scene.width * (2 if scene.depth_format == abi.FORMAT_D16_UNORM else 4)
     st.depth_slice_bytes = st.depth_pitch_bytes * scene.height
     st.framebuffer_width, st.framebuffer_height = scene.width, scene.height
     if scene.fragment_shader == abi.FS_TEX_X_VCOLOR:
@@ -432,16 +435,28 @@ def attachment_shapes(scene):
 
 
 def color_dtype(scene):
-    return {abi.FORMAT_R8G8B8A8_UNORM: np.uint8, abi.FORMAT_R32G32B32A32_SFLOAT: np.float32,
+    return {abi.FORMAT_R8G8B8A8_UNORM: np.uint8, abi.FORMAT_B8G8R8A8_UNORM: np.uint8, abi.FORMAT_R32G32B32A32_SFLOAT: np.float32,
             abi.FORMAT_R16G16B16A16_SFLOAT: np.float16}[scene.color_format]
 
 
+def depth_dtype(scene):
+    return np.uint16 if scene.depth_format == abi.FORMAT_D16_UNORM else np.float32
+
+
+def depth_clear_value(scene):
+    """The stored clear depth: the float, or for D16_UNORM its 16-bit unorm
+    (round to nearest, as a depth clear converts it)."""
+    if scene.depth_format == abi.FORMAT_D16_UNORM:
+        return np.uint16(int(np.rint(np.float32(scene.clear_depth) * np.float32(65535.0))))
+    return np.float32(scene.clear_depth)
+
+
 def clear_buffers(scene):
-    """Host colour (uint8/float) and depth (float32) attachments, cleared."""
+    """Host colour (uint8/float) and depth (float32 / uint16) attachments, cleared."""
     cs, ds = attachment_shapes(scene)
     color = np.empty(cs, color_dtype(scene))
     color[...] = np.asarray(scene.clear_color, color.dtype)
-    depth = np.full(ds, scene.clear_depth, np.float32)
+    depth = np.full(ds, depth_clear_value(scene), depth_dtype(scene))
     return color, depth
 
 

@@ -15,7 +15,7 @@ def render_gpu(scene, renderer=None, repeat=1):
     r.synchronize()
     cnt = r.counters()
     color = ds.color.cpu().numpy()
-    depth = ds.depth.cpu().numpy()
+    depth = ds.depth_numpy()
     return color, depth, cnt
 
 

@@ -298,3 +298,47 @@ def test_primitive_restart_many_blocks(gpu_lib):
                              restart_every=(50, 3000), seed_index=65)
     cnt = check_scene(s, gpu_lib)
     assert cnt["triangles_in"] > 1_000_000
+
+
+@pytest.mark.parametrize("tex_fmt", [abi.FORMAT_B8G8R8A8_UNORM, abi.FORMAT_R8G8B8A8_SRGB, abi.FORMAT_B8G8R8A8_SRGB])
+@pytest.mark.parametrize("mip,address", [(True, abi.ADDRESS_REPEAT), (False, abi.ADDRESS_CLAMP_TO_EDGE)])
+def test_texture_formats_8bit(gpu_lib, tex_fmt, mip, address):
+    """B8G8R8A8 and sRGB 8-bit textures on the 16-bit filtering path (sRGB
+    texels decoded through sRGBtoLinearFF_FF00 before filtering)."""
+    s = scenes.scene_textured_small(mip=mip, address=address, blend=True, seed_index=71)
+    s.texture_format = tex_fmt
+    check_scene(s, gpu_lib)
+
+
+@pytest.mark.parametrize("write_mask", [0xF, 0b0101, 0b1010])
+def test_bgra_attachment(gpu_lib, write_mask):
+    """B8G8R8A8_UNORM colour attachment: R and B bytes swapped on read (blend)
+    and write, write-mask bits with them."""
+    s = scenes.scene_textured_small(n_tris=150, width=80, height=64, blend=True, seed_index=72)
+    s.color_format = abi.FORMAT_B8G8R8A8_UNORM
+    s.clear_color = (200, 100, 50, 25)
+    s.color_write_mask = write_mask
+    check_scene(s, gpu_lib)
+
+
+def test_d16_depth(gpu_lib):
+    """D16_UNORM depth: fragments quantized to Round(z * 0xFFFF) and compared
+    against the stored integers, every compare op; 4x MSAA; dense overlap."""
+    for op in range(8):
+        s = scenes.scene_small(n_tris=120, width=64, height=48, seed_index=25)
+        s.depth_format = abi.FORMAT_D16_UNORM
+        s.depth_compare = op
+        s.clear_depth = 0.5
+        check_scene(s, gpu_lib)
+    s = scenes.scene_small(n_tris=2000, width=96, height=96, seed_index=14)
+    s.depth_format = abi.FORMAT_D16_UNORM
+    check_scene(s, gpu_lib)
+    s = scenes.scene_small(n_tris=300, width=72, height=56, seed_index=42)
+    s.depth_format = abi.FORMAT_D16_UNORM
+    s.samples = 4
+    check_scene(s, gpu_lib)
+    s = scenes.scene_heightfield(quads_x=160, quads_y=80, width=320, height=180, tex_size=256)
+    s.depth_format = abi.FORMAT_D16_UNORM
+    s.color_format = abi.FORMAT_B8G8R8A8_UNORM
+    s.texture_format = abi.FORMAT_B8G8R8A8_SRGB
+    check_scene(s, gpu_lib)

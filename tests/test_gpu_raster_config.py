@@ -143,3 +143,15 @@ def test_longest_first_bin_order(gpu_lib, cfg):
     centers = rng.uniform(-1.0, 1.0, (20000, 2)) ** 3  # denser towards the middle
     v[:, 0:2] = (np.repeat(centers, 3, axis=0) + rng.uniform(-0.03, 0.03, (60000, 2))).astype(np.float32)
     check_config(s, cfg)
+
+
+@pytest.mark.parametrize("cfg", [(16, 16, True), (32, 32, True)], ids=lambda c: "%dx%d" % c[:2])
+def test_depth_bound_d16(gpu_lib, cfg):
+    """The depth bound on a D16_UNORM attachment (quantized like the fragments)."""
+    for op in (abi.COMPARE_LESS, abi.COMPARE_LESS_OR_EQUAL, abi.COMPARE_GREATER, abi.COMPARE_GREATER_OR_EQUAL):
+        s = layered_scene(op, 0.5)
+        s.depth_format = abi.FORMAT_D16_UNORM
+        check_config(s, cfg)
+    s = scenes.scene_small(n_tris=2000, width=96, height=96, seed_index=14)
+    s.depth_format = abi.FORMAT_D16_UNORM
+    check_config(s, cfg)

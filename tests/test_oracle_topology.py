@@ -105,3 +105,42 @@ def test_provoking_vertex_last_rotates_vertices(oracle_mod):
     rot.vertices = np.ascontiguousarray(v[:, [2, 0, 1], :].reshape(450, -1))
     ref = oracle_mod.render(rot)
     assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1]) and got[2] == ref[2]
+
+
+def test_bgra_attachment_and_texture_are_swizzles(oracle_mod):
+    """B8G8R8A8 attachments and textures hold R and B swapped: a BGRA draw of a
+    BGRA copy of the texture equals the RGBA draw with R and B bytes swapped,
+    write-mask bits included."""
+    base = scenes.scene_textured_small(n_tris=120, width=64, height=48, tex_size=32, seed_index=68)
+    base.clear_color = (10, 20, 30, 40)
+    base.color_write_mask = 0b1011  # R, G, A
+    ref = oracle_mod.render(base)
+    sw = scenes.scene_textured_small(n_tris=120, width=64, height=48, tex_size=32, seed_index=68)
+    sw.clear_color = (30, 20, 10, 40)
+    sw.color_write_mask = 0b1011
+    sw.color_format = abi.FORMAT_B8G8R8A8_UNORM
+    sw.texture_format = abi.FORMAT_B8G8R8A8_UNORM
+    sw.texture_levels = [np.ascontiguousarray(lv[..., [2, 1, 0, 3]]) for lv in sw.texture_levels]
+    got = oracle_mod.render(sw)
+    assert np.array_equal(got[0][..., [2, 1, 0, 3]], ref[0]) and np.array_equal(got[1], ref[1]) and got[2] == ref[2]
+
+
+def test_srgb_table_and_d16_quantization(oracle_mod):
+    """sRGB textures decode through sRGBtoLinearFF_FF00 (0 -> 0, 255 -> 0xFF00,
+    monotonic); a D16_UNORM draw stores every depth a D32F draw of the same
+    scene stores, rounded to 16 bits, where the two keep the same fragments."""
+    s = scenes.scene_textured_small(n_tris=60, width=48, height=40, tex_size=16, mip=False, blend=False, seed_index=69)
+    s.texture_levels = [np.full_like(s.texture_levels[0], 255)]
+    s.texture_format = abi.FORMAT_R8G8B8A8_SRGB
+    a = oracle_mod.render(s)
+    s.texture_format = abi.FORMAT_R8G8B8A8_UNORM
+    b = oracle_mod.render(s)
+    assert np.array_equal(a[0], b[0])  # sRGB 255 decodes to exactly 1.0, like UNORM 255
+    d32 = scenes.scene_small(n_tris=1, width=64, height=64, seed_index=70)
+    d16 = scenes.scene_small(n_tris=1, width=64, height=64, seed_index=70)
+    d16.depth_format = abi.FORMAT_D16_UNORM
+    z32 = oracle_mod.render(d32)[1]
+    z16 = oracle_mod.render(d16)[1]
+    covered = z32 < 1.0
+    assert covered.any()
+    assert np.array_equal(z16[covered], np.rint(z32[covered].astype(np.float64) * 65535.0).astype(np.uint16))
