@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-#define SWGB_ABI_VERSION 3
+#define SWGB_ABI_VERSION 4
 
 typedef enum swgb_status {
     SWGB_OK = 0,
@@ -190,7 +190,9 @@ typedef struct swgb_pipeline_state {
     uint32_t cull_mode, front_face;
     uint32_t depth_clip_enable;  /* VK_EXT_depth_clip_enable; default true   */
     uint32_t depth_clamp_enable; /* must be 0                                 */
-    float depth_bias_constant, depth_bias_slope, depth_bias_clamp; /* must be 0 */
+    /* depth bias (VkPipelineRasterizationStateCreateInfo depthBias*, all 0 when
+     * depthBiasEnable is false): constant factor, slope factor, clamp (0 = none) */
+    float depth_bias_constant, depth_bias_slope, depth_bias_clamp;
     /* fragment (vk::FragmentState) */
     uint32_t depth_test_enable, depth_write_enable, depth_compare_op;
     /* fragment output interface (vk::FragmentOutputInterfaceState) */
@@ -217,6 +219,11 @@ typedef struct swgb_pipeline_state {
      * 1 = LAST_VERTEX; the order setBatchIndices gives each triangle's
      * vertices (src/Device/Renderer.cpp:49-145) */
     uint32_t provoking_vertex;
+    /* depth bounds test (VkPipelineDepthStencilStateCreateInfo): the stored
+     * depth of a sample must lie in [min_depth_bounds, max_depth_bounds] */
+    uint32_t depth_bounds_test_enable;
+    float min_depth_bounds, max_depth_bounds;
+    uint32_t reserved3;
 } swgb_pipeline_state;
 
 /* The per-draw arguments of sw::Renderer::draw. */

@@ -166,6 +166,7 @@ typedef struct {
     int yMin, yMax;
     float x0, y0;
     OPlane z, w, V[MAXV];
+    float zBias;     /* Primitive::zBias */
     uint16_t *left[4], *right[4]; /* per sample, indexed [y + 1] */
 } OPrim;
 
@@ -252,7 +253,7 @@ static swgb_status prepare(ODraw *d, const swgb_pipeline_state *st, const swgb_d
        st->topology != SWGB_TOPOLOGY_TRIANGLE_FAN)
         return SWGB_UNSUPPORTED_STATE;
     if(st->sample_count != 1 && st->sample_count != 4) return SWGB_UNSUPPORTED_STATE;
-    if(st->depth_clamp_enable || st->depth_bias_constant != 0.0f || st->depth_bias_slope != 0.0f) return SWGB_UNSUPPORTED_STATE;
+    if(st->depth_clamp_enable) return SWGB_UNSUPPORTED_STATE;
     if(st->attrib_count < 1 || st->attrib_count > SWGB_MAX_ATTRIBS) return SWGB_INVALID_ARG;
     if(!is_unorm(st->color_format) && st->color_format != SWGB_FORMAT_R32G32B32A32_SFLOAT &&
        st->color_format != SWGB_FORMAT_R16G16B16A16_SFLOAT)
@@ -708,6 +709,39 @@ static int setup_triangle(const ODraw *d, const OVertex *tv0, const OVertex *tv1
         pr->z.A = fmul(fsub(fmul(fy2, z1), fmul(fy1, z2)), D);
         pr->z.B = fmul(fsub(fmul(fx1, z2), fmul(fx2, z1)), D);
         pr->z.C = fadd(fmul(z0, d->depthRange), d->depthNear);
+        /* depth bias (:417-476) */
+        const swgb_pipeline_state *st = d->st;
+        pr->zBias = 0.0f;
+        if(st->depth_bias_constant != 0.0f || st->depth_bias_slope != 0.0f)
+        {
+            float bias = 0.0f;
+            if(st->depth_bias_constant != 0.0f)
+            {
+                float r; /* minimum resolvable difference */
+                if(d16(st)) r = 1.01f / 0xFFFF; /* Renderer.cpp:426-430 */
+                else
+                {
+                    /* 2^(e-23), e the largest exponent of Z0, Z1, Z2; Z1 and Z2
+                     * are formed from the differences z1, z2 as the reference does */
+                    float Z0 = pr->z.C;
+                    float Z1 = fadd(fmul(z1, d->depthRange), d->depthNear);
+                    float Z2 = fadd(fmul(z2, d->depthRange), d->depthNear);
+                    int32_t e0 = (int32_t)(f2u(Z0) & 0x7F800000u), e1 = (int32_t)(f2u(Z1) & 0x7F800000u), e2 = (int32_t)(f2u(Z2) & 0x7F800000u);
+                    int32_t e = e0 > e1 ? e0 : e1;
+                    e = e > e2 ? e : e2;
+                    r = fmul(u2f((uint32_t)e), 1.0f / (1 << 23));
+                }
+                bias = fmul(r, st->depth_bias_constant);
+            }
+            if(st->depth_bias_slope != 0.0f)
+            {
+                float m = fmaxr(fabsf(pr->z.A), fabsf(pr->z.B));
+                bias = fadd(bias, fmul(m, st->depth_bias_slope));
+            }
+            float clamp = st->depth_bias_clamp == st->depth_bias_clamp ? st->depth_bias_clamp : 0.0f; /* Context.cpp:650-661 */
+            if(clamp != 0.0f) bias = clamp > 0.0f ? fminr(bias, clamp) : fmaxr(bias, clamp);
+            pr->zBias = bias;
+        }
     }
     /* setupGradient, smooth (perspective) varyings (:478-548) */
     for(int k = 0; k < d->nv; k++)
@@ -1240,6 +1274,14 @@ static float depth_value(const ODraw *d, float Z)
     return fminr(fmaxr(nearbyintf(fmul(Z, 65535.0f)), 0.0f), 65535.0f);
 }
 
+/* depthBoundsTest16 / 32F (PixelRoutine.cpp:576-609): the stored value, D16
+ * scaled by 1/0xFFFF, within [minDepthBounds, maxDepthBounds]. */
+static int bounds_pass(const ODraw *d, float stored)
+{
+    const float z = d16(d->st) ? fmul(stored, 1.0f / 0xFFFF) : stored;
+    return fle(d->st->min_depth_bounds, z) && fle(z, d->st->max_depth_bounds);
+}
+
 static void write_depth(const ODraw *d, int q, int x, int y, float Z)
 {
     if(d16(d->st)) *(uint16_t *)depth_at(d, q, x, y) = (uint16_t)Z;
@@ -1271,6 +1313,8 @@ static void pixel_quad(const ODraw *d, const OSampler *smp, const OPrim *pr, int
                 }
                 float Dz = fadd(pr->z.C, fmul(yq, pr->z.B));
                 z[q][i] = ffma(xq, pr->z.A, Dz);
+                if(d->st->depth_bias_constant != 0.0f || d->st->depth_bias_slope != 0.0f)
+                    z[q][i] = fadd(z[q][i], pr->zBias); /* PixelRoutine.cpp:141-144 */
             }
     /* w, rhw (:196-199) and varyings (:231-261) */
     float rhw[4];
@@ -1333,12 +1377,20 @@ static void pixel_quad(const ODraw *d, const OSampler *smp, const OPrim *pr, int
                 case SWGB_COMPARE_GREATER_OR_EQUAL: pass = fle(zb, Z); break;
                 default: pass = 1; break;
                 }
+                /* depthBoundsTest after the depth test, on the stored value (:576-640) */
+                if(pass && st->depth_bounds_test_enable && !bounds_pass(d, zb)) pass = 0;
                 if(pass) zMask |= 1 << i;
             }
             if(cnt) cnt->fragments_tested += (uint64_t)__builtin_popcount((unsigned)cMask[q]);
             if(d->depthWrite)
                 for(int i = 0; i < 4; i++)
                     if(zMask & (1 << i)) write_depth(d, q, x + (i & 1), y + (i >> 1), z[q][i]);
+        }
+        else if(st->depth_bounds_test_enable && st->depth)
+        {
+            /* no depth test: the bounds test masks the coverage (:626-629) */
+            for(int i = 0; i < 4; i++)
+                if((zMask & (1 << i)) && !bounds_pass(d, read_depth(d, q, x + (i & 1), y + (i >> 1)))) zMask &= ~(1 << i);
         }
         if(cnt) cnt->fragments_passed += (uint64_t)__builtin_popcount((unsigned)zMask);
         if(d->vis)

@@ -103,6 +103,8 @@ class PipelineState(C.Structure):
         ("framebuffer_width", C.c_uint32), ("framebuffer_height", C.c_uint32),
         ("texture", Texture),
         ("precision_profile", C.c_uint32), ("provoking_vertex", C.c_uint32),
+        ("depth_bounds_test_enable", C.c_uint32), ("min_depth_bounds", C.c_float), ("max_depth_bounds", C.c_float),
+        ("reserved3", C.c_uint32),
     ]
 
 

@@ -195,7 +195,7 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
     if(st->sample_count != 1 && st->sample_count != 4) return set_error(SWGB_UNSUPPORTED_STATE, "sample_count (1 or 4)");
     if(st->vertex_shader != SWGB_VS_MVP_PASSTHROUGH) return set_error(SWGB_UNSUPPORTED_STATE, "vertex_shader");
     if(st->fragment_shader != SWGB_FS_VCOLOR && st->fragment_shader != SWGB_FS_TEX_X_VCOLOR) return set_error(SWGB_UNSUPPORTED_STATE, "fragment_shader");
-    if(st->depth_clamp_enable || st->depth_bias_constant != 0.0f || st->depth_bias_slope != 0.0f) return set_error(SWGB_UNSUPPORTED_STATE, "depth clamp / bias");
+    if(st->depth_clamp_enable) return set_error(SWGB_UNSUPPORTED_STATE, "depth clamp");
     if(st->color_format != SWGB_FORMAT_R8G8B8A8_UNORM && st->color_format != SWGB_FORMAT_B8G8R8A8_UNORM &&
        st->color_format != SWGB_FORMAT_R16G16B16A16_SFLOAT && st->color_format != SWGB_FORMAT_R32G32B32A32_SFLOAT)
         return set_error(SWGB_UNSUPPORTED_STATE, "color_format");
@@ -219,7 +219,7 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
         if(i > 0) D.nv += (int)D.vcomp[i];
     }
     if(D.nv > PLANE_V) return set_error(SWGB_UNSUPPORTED_STATE, "too many varyings");
-    D.planeVec4 = (8 + 3 * D.nv + 3) / 4;
+    D.planeVec4 = (8 + 3 * D.nv + 3) / 4;  // grown to the zBias plane below when the draw has depth bias
     if(D.nattr < 2 || D.vcomp[1] != 4) return set_error(SWGB_INVALID_ARG, "the fixed FS reads a vec4 colour at location 0");
     D.fs = (int)st->fragment_shader;
     if(D.fs == SWGB_FS_TEX_X_VCOLOR && (D.nattr < 3 || D.nv < 6)) return set_error(SWGB_INVALID_ARG, "textured FS needs a uv varying");
@@ -275,6 +275,15 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
 
     D.depthTest = st->depth && st->depth_test_enable;
     D.depthWrite = D.depthTest && st->depth_write_enable;
+    // depth bias: a NaN clamp counts as 0 (Context.cpp:650-661)
+    D.biasConstant = st->depth_bias_constant;
+    D.biasSlope = st->depth_bias_slope;
+    D.biasClamp = st->depth_bias_clamp == st->depth_bias_clamp ? st->depth_bias_clamp : 0.0f;
+    D.depthBias = D.depthTest && (D.biasConstant != 0.0f || D.biasSlope != 0.0f);
+    D.depthBounds = st->depth && st->depth_bounds_test_enable;
+    D.minBounds = st->min_depth_bounds;
+    D.maxBounds = st->max_depth_bounds;
+    if(D.depthBias) D.planeVec4 = PLANES_STORED / 4;
     D.compareOp = st->depth_compare_op;
     D.hiz = 1;
     D.minDepthClamp = 0.0f;  // no VK_EXT_depth_range_unrestricted: clamp to [0,1] (PixelProcessor.cpp:106-128)
@@ -301,7 +310,7 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
     // 16-byte colour rows and 4-pixel depth groups (16 bytes D32F, 8 bytes D16)
     const uint32_t dAlign = D.depth16 ? 8u : 16u;
     D.vec16 = ((uintptr_t)D.color % 16 == 0) && (D.colorPitch % 16 == 0) &&
-              (!D.depthTest || (((uintptr_t)D.depth % dAlign == 0) && (D.depthPitch % dAlign == 0)));
+              (!(D.depthTest || D.depthBounds) || (((uintptr_t)D.depth % dAlign == 0) && (D.depthPitch % dAlign == 0)));
 
     if(D.fs == SWGB_FS_TEX_X_VCOLOR)
     {
@@ -634,7 +643,7 @@ void draw_writes(const DrawParams &D, uintptr_t origin, std::vector<TouchRect> &
     {
         plane_rects((uintptr_t)D.color + (uintptr_t)q * D.colorSlice, origin, D.colorPitch, (int64_t)D.sx0 * cbpp,
                     (int64_t)D.sx1 * cbpp, D.sy0, D.sy1, out);
-        if(D.depthTest)
+        if(D.depthTest || D.depthBounds)  // written, or read by the bounds test: either orders the draw
             plane_rects((uintptr_t)D.depth + (uintptr_t)q * D.depthSlice, origin, D.depthPitch, (int64_t)D.sx0 * (D.depth16 ? 2 : 4),
                         (int64_t)D.sx1 * (D.depth16 ? 2 : 4), D.sy0, D.sy1, out);
     }
@@ -1071,6 +1080,7 @@ swgb_status bake_adjoint(const swgb_pipeline_state *st, const swgb_draw_args *a,
     if(cf_unorm8(D.cf)) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint needs a float colour attachment");
     if(D.restart) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint: primitive restart is not supported");
     if(D.depth16) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint needs a D32_SFLOAT depth attachment");
+    if(D.depthBounds) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint: depth bounds test is not supported");
     if(D.fs == SWGB_FS_TEX_X_VCOLOR && !D.texFloat) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint needs a float texture");
     if(D.writeMask != 0xFu) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint needs color_write_mask 0xF");
     if(a->count > ADJ_TRI_MASK) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint: too many triangles");

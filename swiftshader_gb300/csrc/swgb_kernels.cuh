@@ -107,6 +107,10 @@ struct DrawParams {
     // pixel state
     int depthTest, depthWrite, compareOp;
     int hiz;      // reject triangle-bin pairs against the bin's depth bound
+    float biasConstant, biasSlope, biasClamp;  // depth bias (0: none)
+    int depthBias;     // biasConstant or biasSlope nonzero: fragments add the triangle's zBias
+    int depthBounds;   // depth bounds test against [minBounds, maxBounds]
+    float minBounds, maxBounds;
     float minDepthClamp, maxDepthClamp;
     int blend;
     uint32_t srcC, dstC, opC, srcA, dstA, opA;
@@ -605,7 +609,8 @@ static __device__ void write_spans(const DrawParams &D, const int32_t *X, const 
 
 // One 256-triangle block of a draw (block index 'blk' within the draw).
 constexpr int PLANE_V = 6;  // varying components with plane equations (colour + uv)
-constexpr int PLANES = 8 + 3 * PLANE_V;
+constexpr int PLANE_ZBIAS = 8 + 3 * PLANE_V;  // the triangle's depth bias (Primitive::zBias)
+constexpr int PLANES = PLANE_ZBIAS + 1;
 constexpr int PLANES_STORED = 28;  // PLANES rounded up to whole float4s
 
 __device__ __forceinline__ uint32_t select3(int o, uint32_t a, uint32_t b, uint32_t c) { return o == 0 ? a : (o == 1 ? b : c); }
@@ -693,6 +698,29 @@ __device__ __forceinline__ void triangle_planes(const DrawParams &D, uint32_t t,
         p[2] = (fy2 * z1 - fy1 * z2) * Dz;
         p[3] = (fx1 * z2 - fx2 * z1) * Dz;
         p[4] = z0 * D.depthRange + D.depthNear;
+        // depth bias (SetupRoutine.cpp:417-476)
+        if(D.biasConstant != 0.0f || D.biasSlope != 0.0f)
+        {
+            float bias = 0.0f;
+            if(D.biasConstant != 0.0f)
+            {
+                float r;  // minimum resolvable difference
+                if(D.depth16) r = 1.01f / 0xFFFF;
+                else
+                {
+                    // 2^(e - 23), e the largest exponent of the depths; the
+                    // reference forms Z1, Z2 from the vertex differences
+                    const float Z0 = p[4], Z1 = z1 * D.depthRange + D.depthNear, Z2 = z2 * D.depthRange + D.depthNear;
+                    const int e = max(max(__float_as_int(Z0) & 0x7F800000, __float_as_int(Z1) & 0x7F800000),
+                                      __float_as_int(Z2) & 0x7F800000);
+                    r = __int_as_float(e) * (1.0f / (1 << 23));
+                }
+                bias = r * D.biasConstant;
+            }
+            if(D.biasSlope != 0.0f) bias += rmax(fabsf(p[2]), fabsf(p[3])) * D.biasSlope;
+            if(D.biasClamp != 0.0f) bias = D.biasClamp > 0.0f ? rmin(bias, D.biasClamp) : rmax(bias, D.biasClamp);
+            p[PLANE_ZBIAS] = bias;
+        }
     }
     float4 B0 = make_float4(0, 0, 0, 0), B1 = B0, B2 = B0;
     if(D.nv > 3)
@@ -1391,6 +1419,17 @@ __device__ __forceinline__ float depth_value(float z)
     return fminf(fmaxf(rintf(z * 65535.0f), 0.0f), 65535.0f);
 }
 
+// Depth bounds test of the stored depth (depthBoundsTest16/32F,
+// PixelRoutine.cpp:576-640): minDepthBounds <= z <= maxDepthBounds, D16_UNORM
+// values scaled by 1 / 0xFFFF; applied after the depth test, on the value the
+// sample found.
+template<bool D16>
+__device__ __forceinline__ bool bounds_pass(const DrawParams &D, float stored)
+{
+    const float z = D16 ? stored * (1.0f / 0xFFFF) : stored;
+    return D.minBounds <= z && z <= D.maxBounds;
+}
+
 __device__ __forceinline__ bool depth_pass(uint32_t op, float zb, float z)
 {
     switch(op)
@@ -1638,9 +1677,13 @@ __device__ __forceinline__ void rop_pixel(const DrawParams &D, SH &S, int q, int
     if(D.depthTest)
     {
         nTested++;
-        if(!depth_pass(D.compareOp, depth[idx], z)) return;
+        const float stored = depth[idx];
+        if(!depth_pass(D.compareOp, stored, z)) return;
+        if(D.depthBounds && !bounds_pass<SH::kD16>(D, stored)) return;
         if(D.depthWrite) depth[idx] = z;
     }
+    else if(D.depthBounds && !bounds_pass<SH::kD16>(D, depth[idx]))
+        return;
     nPassed++;
     float out[4];
     if(D.blend)
@@ -1747,7 +1790,8 @@ __device__ __forceinline__ float sample_depth(const DrawParams &D, const SH &S, 
         yF = yF + SLY[q];
         xF = xF - SLX[q];
     }
-    const float z = mul_add(xF, S.plane[2][ti], S.plane[4][ti] + yF * S.plane[3][ti]);
+    float z = mul_add(xF, S.plane[2][ti], S.plane[4][ti] + yF * S.plane[3][ti]);
+    if(D.depthBias) z = z + S.plane[PLANE_ZBIAS][ti];  // PixelRoutine.cpp:141-144
     return depth_value<SH::kD16>(rmin(rmax(z, D.minDepthClamp), D.maxDepthClamp));  // clampDepth
 }
 
@@ -1797,19 +1841,20 @@ __device__ __forceinline__ bool hiz_rejects(const DrawParams &D, const SH &S, in
     const float zA = S.plane[2][ti], zB = S.plane[3][ti], zC = S.plane[4][ti];
     const float xFa = ((float)max((int)box.x, bx0) - 0.5f) - x0p, xFb = ((float)min((int)box.z, bx0 + SH::kBW) - 0.5f) - x0p;
     const float yFa = ((float)max((int)box.y, by0) - 0.5f) - y0p, yFb = ((float)min((int)box.w, by0 + SH::kBH) - 0.5f) - y0p;
-    const float T = fabsf(zC) + fmaxf(fabsf(yFa), fabsf(yFb)) * fabsf(zB) + fmaxf(fabsf(xFa), fabsf(xFb)) * fabsf(zA);
+    const float bias = D.depthBias ? S.plane[PLANE_ZBIAS][ti] : 0.0f;
+    const float T = fabsf(zC) + fmaxf(fabsf(yFa), fabsf(yFb)) * fabsf(zB) + fmaxf(fabsf(xFa), fabsf(xFb)) * fabsf(zA) + fabsf(bias);
     const float margin = T * (1.0f / 1048576.0f) + 1e-30f;
     const uint32_t op = D.compareOp;
     if(op == SWGB_COMPARE_LESS || op == SWGB_COMPARE_LESS_OR_EQUAL)
     {
         const float xF = zA >= 0.0f ? xFa : xFb, yF = zB >= 0.0f ? yFa : yFb;
-        float zlo = ((zC + yF * zB) + xF * zA) - margin;
+        float zlo = (((zC + yF * zB) + xF * zA) + bias) - margin;
         if(!(zlo >= D.minDepthClamp)) zlo = D.minDepthClamp;  // also NaN
         zlo = depth_value<SH::kD16>(fminf(zlo, D.maxDepthClamp));
         return op == SWGB_COMPARE_LESS ? zb <= zlo : zb < zlo;
     }
     const float xF = zA >= 0.0f ? xFb : xFa, yF = zB >= 0.0f ? yFb : yFa;
-    float zhi = ((zC + yF * zB) + xF * zA) + margin;
+    float zhi = (((zC + yF * zB) + xF * zA) + bias) + margin;
     if(!(zhi <= D.maxDepthClamp)) zhi = D.maxDepthClamp;
     zhi = depth_value<SH::kD16>(fmaxf(zhi, D.minDepthClamp));
     return op == SWGB_COMPARE_GREATER ? zb >= zhi : zb > zhi;
@@ -2122,7 +2167,7 @@ __device__ __forceinline__ void raster_bin(const DrawParams &D, RasterShared<CF,
             const int ly = i / (BW / 4), lx = (i % (BW / 4)) * 4;
             const int px = bx0 + lx, py = by0 + ly;
             float4 dz = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
-            if(D.depthTest && py < D.sy1 && px < D.sx1)
+            if((D.depthTest || D.depthBounds) && py < D.sy1 && px < D.sx1)
             {
                 const uint8_t *drow = dbase + (size_t)py * D.depthPitch;
                 if(D16)

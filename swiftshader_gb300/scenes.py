@@ -49,6 +49,9 @@ class Scene:
     provoking_vertex: int = 0         # 0 = FIRST_VERTEX, 1 = LAST_VERTEX (VK_EXT_provoking_vertex)
     depth_format: int = abi.FORMAT_D32_SFLOAT  # or FORMAT_D16_UNORM
     color_write_mask: int = 0xF       # VkColorComponentFlags
+    depth_bias: tuple = (0.0, 0.0, 0.0)     # (constant, slope, clamp)
+    depth_bounds: tuple = None        # (min, max) enables the depth bounds test
+    depth_test: bool = True
     restart_index_count: int = 0      # > 0: primitive restart over this many indices (tri_count ignored)
 
     @property
@@ -324,8 +327,12 @@ def build_state(scene, color_ptr, depth_ptr, vertex_ptr, level_ptrs=None, color_
     st.cull_mode = scene.cull_mode
     st.front_face = scene.front_face
     st.depth_clip_enable = 1
-    st.depth_test_enable = 1
+    st.depth_test_enable = 1 if scene.depth_test else 0
     st.depth_write_enable = 1
+    st.depth_bias_constant, st.depth_bias_slope, st.depth_bias_clamp = (float(x) for x in scene.depth_bias)
+    if scene.depth_bounds is not None:
+        st.depth_bounds_test_enable = 1
+        st.min_depth_bounds, st.max_depth_bounds = (float(x) for x in scene.depth_bounds)
     st.depth_compare_op = scene.depth_compare
     st.color_format = scene.color_format
     if scene.blend is not None:

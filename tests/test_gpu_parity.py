@@ -342,3 +342,35 @@ def test_d16_depth(gpu_lib):
     s.color_format = abi.FORMAT_B8G8R8A8_UNORM
     s.texture_format = abi.FORMAT_B8G8R8A8_SRGB
     check_scene(s, gpu_lib)
+
+
+@pytest.mark.parametrize("bias", [(3.0, 0.0, 0.0), (0.0, 1.5, 0.0), (-200.0, -2.0, -0.001), (1e5, 4.0, 0.002)])
+@pytest.mark.parametrize("d16", [False, True])
+def test_depth_bias(gpu_lib, bias, d16):
+    """Depth bias: constant (minimum resolvable difference per polygon for
+    D32F, 1.01/0xFFFF for D16), slope, and clamp, over dense overlap where the
+    bias decides the order; GREATER as well as LESS."""
+    for op in (abi.COMPARE_LESS, abi.COMPARE_GREATER_OR_EQUAL):
+        s = scenes.scene_small(n_tris=800, width=96, height=80, seed_index=74)
+        s.depth_bias = bias
+        s.depth_compare = op
+        s.clear_depth = 1.0 if op == abi.COMPARE_LESS else 0.0
+        if d16:
+            s.depth_format = abi.FORMAT_D16_UNORM
+        check_scene(s, gpu_lib)
+
+
+@pytest.mark.parametrize("bounds", [(0.0, 1.0), (0.3, 0.7), (0.5, 0.5), (0.9, 0.2)])
+@pytest.mark.parametrize("depth_test", [True, False])
+def test_depth_bounds(gpu_lib, bounds, depth_test):
+    """Depth bounds test on the stored depth after the depth test (or masking
+    the coverage without one), D32F and D16, with 4x MSAA."""
+    for d16, samples in ((False, 1), (True, 1), (False, 4)):
+        s = scenes.scene_small(n_tris=600, width=72, height=64, seed_index=75)
+        s.depth_bounds = bounds
+        s.depth_test = depth_test
+        s.clear_depth = 0.6
+        s.samples = samples
+        if d16:
+            s.depth_format = abi.FORMAT_D16_UNORM
+        check_scene(s, gpu_lib)

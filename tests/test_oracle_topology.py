@@ -144,3 +144,19 @@ def test_srgb_table_and_d16_quantization(oracle_mod):
     covered = z32 < 1.0
     assert covered.any()
     assert np.array_equal(z16[covered], np.rint(z32[covered].astype(np.float64) * 65535.0).astype(np.uint16))
+
+
+def test_depth_bias_constant_known_answer(oracle_mod):
+    """A constant-depth triangle at z = 0.5 with constant bias 2^20: r =
+    2^(e - 23) with e the exponent of 0.5, so every covered depth becomes
+    0.5 + 2^20 * 2^-24 = 0.5625 (SetupRoutine.cpp:417-476); a clamp of 0.03
+    limits it to 0.53."""
+    s = scenes.scene_small(n_tris=1, width=32, height=32, seed_index=73)
+    s.vertices[:, 0:2] = np.array([[-0.9, -0.9], [0.9, -0.9], [0.0, 0.9]], np.float32)
+    s.vertices[:, 2] = 0.5
+    s.depth_bias = (float(2 ** 20), 0.0, 0.0)
+    d = oracle_mod.render(s)[1]
+    assert (d[d < 1.0] == np.float32(0.5625)).all() and (d < 1.0).sum() > 100
+    s.depth_bias = (float(2 ** 20), 0.0, 0.03)
+    d = oracle_mod.render(s)[1]
+    assert (d[d < 1.0] == np.float32(0.5) + np.float32(0.03)).all()
