@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-#define SWGB_ABI_VERSION 4
+#define SWGB_ABI_VERSION 5
 
 typedef enum swgb_status {
     SWGB_OK = 0,
@@ -89,6 +89,15 @@ typedef enum swgb_status {
 #define SWGB_COMPARE_NOT_EQUAL 5
 #define SWGB_COMPARE_GREATER_OR_EQUAL 6
 #define SWGB_COMPARE_ALWAYS 7
+/* VkStencilOp */
+#define SWGB_STENCIL_OP_KEEP 0
+#define SWGB_STENCIL_OP_ZERO 1
+#define SWGB_STENCIL_OP_REPLACE 2
+#define SWGB_STENCIL_OP_INCREMENT_AND_CLAMP 3
+#define SWGB_STENCIL_OP_DECREMENT_AND_CLAMP 4
+#define SWGB_STENCIL_OP_INVERT 5
+#define SWGB_STENCIL_OP_INCREMENT_AND_WRAP 6
+#define SWGB_STENCIL_OP_DECREMENT_AND_WRAP 7
 /* VkBlendFactor */
 #define SWGB_BLEND_ZERO 0
 #define SWGB_BLEND_ONE 1
@@ -169,6 +178,13 @@ typedef struct swgb_texture {
     float mip_lod_bias, min_lod, max_lod;
 } swgb_texture;
 
+/* VkStencilOpState */
+typedef struct swgb_stencil_op_state {
+    uint32_t fail_op, pass_op, depth_fail_op, compare_op; /* VkStencilOp x3, VkCompareOp */
+    uint32_t compare_mask, write_mask, reference;
+    uint32_t reserved;
+} swgb_stencil_op_state;
+
 typedef struct swgb_pipeline_state {
     /* vertex input interface (vk::VertexInputInterfaceState): triangle list,
      * strip or fan, provoking vertex first (Renderer.cpp setBatchIndices);
@@ -196,7 +212,7 @@ typedef struct swgb_pipeline_state {
     /* fragment (vk::FragmentState) */
     uint32_t depth_test_enable, depth_write_enable, depth_compare_op;
     /* fragment output interface (vk::FragmentOutputInterfaceState) */
-    uint32_t color_format;  /* R8G8B8A8_UNORM, B8G8R8A8_UNORM, R16G16B16A16_SFLOAT or R32G32B32A32_SFLOAT */
+    uint32_t color_format;  /* R8G8B8A8_UNORM / _SRGB, B8G8R8A8_UNORM / _SRGB, R16G16B16A16_SFLOAT or R32G32B32A32_SFLOAT */
     uint32_t blend_enable;
     uint32_t src_color_factor, dst_color_factor, color_blend_op;
     uint32_t src_alpha_factor, dst_alpha_factor, alpha_blend_op;
@@ -223,7 +239,15 @@ typedef struct swgb_pipeline_state {
      * depth of a sample must lie in [min_depth_bounds, max_depth_bounds] */
     uint32_t depth_bounds_test_enable;
     float min_depth_bounds, max_depth_bounds;
+    /* stencil test (VkPipelineDepthStencilStateCreateInfo) on an S8_UINT
+     * attachment: pitch and sample-plane slice in bytes; 'front' applies to
+     * front-facing triangles, 'back' to back-facing ones */
+    uint32_t stencil_test_enable;
+    void *stencil;
+    uint32_t stencil_pitch_bytes;
     uint32_t reserved3;
+    uint64_t stencil_slice_bytes;
+    swgb_stencil_op_state front, back;
 } swgb_pipeline_state;
 
 /* The per-draw arguments of sw::Renderer::draw. */

@@ -63,6 +63,11 @@ def lib():
         L.oracle_log2sqrt.restype = C.c_float
         L.oracle_ftz.argtypes = [C.c_float]
         L.oracle_ftz.restype = C.c_float
+        for f in (L.oracle_linear_to_srgb, L.oracle_srgb_to_linear):
+            f.argtypes = [C.c_float]
+            f.restype = C.c_float
+        L.oracle_transcendental_n.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_size_t]
+        L.oracle_transcendental_n.restype = None
         L.oracle_vertex.argtypes = [C.POINTER(abi.PipelineState), C.POINTER(abi.DrawArgs), C.c_uint32,
                                     C.POINTER(C.c_float), C.POINTER(C.c_int32)]
         L.oracle_vertex.restype = C.c_int
@@ -76,34 +81,59 @@ def lib():
     return _lib
 
 
+TRANSCENDENTAL = {"log2_mediump": 0, "exp2_mediump": 1, "linear_to_srgb": 2, "srgb_to_linear": 3}
+
+
+def transcendental(name, x):
+    """Element-wise Log2 / Exp2 (mediump) or the sRGB transfer functions of the
+    oracle over a float32 array."""
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    out = np.empty_like(x)
+    lib().oracle_transcendental_n(TRANSCENDENTAL[name], x.ctypes.data, out.ctypes.data, x.size)
+    return out
+
+
 def _ptr(a):
     return a.ctypes.data if a is not None else None
 
 
-def host_state(scene, color, depth):
+def host_state(scene, color, depth, stencil=None):
     """PipelineState + DrawArgs whose pointers address host numpy arrays."""
     from swiftshader_gb300 import scenes
     verts = np.ascontiguousarray(scene.vertices, np.float32)
     levels = [np.ascontiguousarray(l) for l in scene.texture_levels]
-    st = scenes.build_state(scene, _ptr(color), _ptr(depth), _ptr(verts), [_ptr(l) for l in levels])
+    st = scenes.build_state(scene, _ptr(color), _ptr(depth), _ptr(verts), [_ptr(l) for l in levels],
+                            stencil_ptr=None if stencil is None else _ptr(stencil))
     idx = None if scene.indices is None else np.ascontiguousarray(scene.indices)
     args = scenes.build_args(scene, _ptr(idx))
     keep = (verts, levels, idx)
     return st, args, keep
 
 
-def render(scene, nthreads=1, color=None, depth=None):
-    """Runs one draw of 'scene' on the CPU oracle; returns (color, depth, counters dict)."""
+def render(scene, nthreads=1, color=None, depth=None, stencil=None):
+    """Runs one draw of 'scene' on the CPU oracle; returns (color, depth, counters dict).
+    A scene with a stencil state draws into 'stencil' (a fresh cleared one when
+    None; render_stencil returns it)."""
     from swiftshader_gb300 import abi, scenes
     if color is None or depth is None:
         color, depth = scenes.clear_buffers(scene)
-    st, args, keep = host_state(scene, color, depth)
+    if stencil is None:
+        stencil = scenes.stencil_buffer(scene)
+    st, args, keep = host_state(scene, color, depth, stencil)
     cnt = abi.Counters()
     s = lib().oracle_draw(C.byref(st), C.byref(args), nthreads, C.byref(cnt))
     if s != 0:
         raise RuntimeError("oracle_draw failed: %s" % abi.STATUS_NAMES.get(s, s))
     del keep
     return color, depth, cnt.as_dict()
+
+
+def render_stencil(scene, nthreads=1):
+    """render() of a scene with a stencil state; returns (color, depth, stencil, counters)."""
+    from swiftshader_gb300 import scenes
+    stencil = scenes.stencil_buffer(scene)
+    color, depth, cnt = render(scene, nthreads, stencil=stencil)
+    return color, depth, stencil, cnt
 
 
 def render_visibility(scene, nthreads=1, cap=8):

@@ -167,6 +167,7 @@ typedef struct {
     float x0, y0;
     OPlane z, w, V[MAXV];
     float zBias;     /* Primitive::zBias */
+    int front;       /* front-facing: clockwiseMask (SetupRoutine.cpp:104-114) */
     uint16_t *left[4], *right[4]; /* per sample, indexed [y + 1] */
 } OPrim;
 
@@ -214,7 +215,14 @@ static uint32_t simplify_op(uint32_t op, uint32_t sf, uint32_t df)
     return op;
 }
 
-static int is_unorm(uint32_t fmt) { return fmt == SWGB_FORMAT_R8G8B8A8_UNORM || fmt == SWGB_FORMAT_B8G8R8A8_UNORM; }
+/* 8-bit colour attachments: UNORM, or sRGB-encoded UNORM */
+static int is_unorm(uint32_t fmt)
+{
+    return fmt == SWGB_FORMAT_R8G8B8A8_UNORM || fmt == SWGB_FORMAT_B8G8R8A8_UNORM || fmt == SWGB_FORMAT_R8G8B8A8_SRGB ||
+           fmt == SWGB_FORMAT_B8G8R8A8_SRGB;
+}
+static int is_bgra(uint32_t fmt) { return fmt == SWGB_FORMAT_B8G8R8A8_UNORM || fmt == SWGB_FORMAT_B8G8R8A8_SRGB; }
+static int is_srgb(uint32_t fmt) { return fmt == SWGB_FORMAT_R8G8B8A8_SRGB || fmt == SWGB_FORMAT_B8G8R8A8_SRGB; }
 static int is_tex8(uint32_t fmt)
 {
     return fmt == SWGB_FORMAT_R8G8B8A8_UNORM || fmt == SWGB_FORMAT_B8G8R8A8_UNORM || fmt == SWGB_FORMAT_R8G8B8A8_SRGB ||
@@ -237,6 +245,53 @@ static void srgb_init(void)
         const float lin = c <= 0.04045f ? c / 12.92f : powf((c + 0.055f) / 1.055f, 2.4f);
         srgb_lut[i] = (uint16_t)(lin * 0xFF00 + 0.5f);
     }
+}
+
+/* Log2 / Exp2 at relaxed (mediump) precision and Pow<Mediump> = Exp2(Log2(x) * y)
+ * (src/Pipeline/ShaderCore.cpp:336-386,406-470,472-477; SWIFTSHADER_LEGACY_PRECISION
+ * is false in the CMake build): a bit-pattern log2 with a quadratic mantissa
+ * correction; floor/fraction split with a quadratic correction scaled into
+ * the exponent field. */
+static float log2_mediump(float x)
+{
+    const int32_t im = (int32_t)f2u(x);
+    float y = ffma((float)im, 1.0f / (1 << 23), -127.0f);
+    if(im == 0x7F800000) y = u2f(f2u(y) | 0x7F800000u);
+    const float m = (float)(im & 0x007FFFFF);
+    const float f = ffma(ffma(2.8017103e-22f, m, -8.373131e-15f), m, 5.0615534e-8f);
+    return ffma(f, m, y);
+}
+static float exp2_mediump(float x)
+{
+    float x0 = fminr(x, 128.0f);
+    x0 = fmaxr(x0, u2f(0xC2FDFFFFu));
+    const float f = fsub(x0, floorf(daz(x0)));
+    const float r = ffma(ffma(7.8145574e-2f, f, 2.2617357e-1f), f, -3.0444314e-1f);
+    const float y = ffma(r, f, x0);
+    return u2f((uint32_t)trunc_int(ffma((float)(1 << 23), y, (float)(127 << 23))));
+}
+static float pow_mediump(float x, float y) { return exp2_mediump(fmul(log2_mediump(x), y)); }
+/* linearToSRGB / sRGBtoLinear of colour attachments (ShaderCore.cpp:914-930) */
+static float linear_to_srgb(float c)
+{
+    const float lc = fmul(c, 12.92f);
+    const float ec = ffma(1.055f, pow_mediump(c, 1.0f / 2.4f), -0.055f);
+    return flt(c, 0.0031308f) ? lc : ec;
+}
+static float srgb_to_linear(float c)
+{
+    const float lc = fmul(c, 1.0f / 12.92f);
+    const float ec = pow_mediump(ffma(c, 1.0f / 1.055f, 0.055f / 1.055f), 2.4f);
+    return flt(c, 0.04045f) ? lc : ec;
+}
+float oracle_linear_to_srgb(float c) { return linear_to_srgb(c); }
+float oracle_srgb_to_linear(float c) { return srgb_to_linear(c); }
+/* element-wise over arrays, for the known-answer and error-bound tests:
+ * fn 0 Log2 mediump, 1 Exp2 mediump, 2 linearToSRGB, 3 sRGBtoLinear */
+void oracle_transcendental_n(int fn, const float *in, float *out, size_t n)
+{
+    for(size_t i = 0; i < n; i++)
+        out[i] = fn == 0 ? log2_mediump(in[i]) : fn == 1 ? exp2_mediump(in[i]) : fn == 2 ? linear_to_srgb(in[i]) : srgb_to_linear(in[i]);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -564,6 +619,7 @@ static int setup_triangle(const ODraw *d, const OVertex *tv0, const OVertex *tv1
         if((st->cull_mode & SWGB_CULL_FRONT) && frontFacing) return 0;
         if((st->cull_mode & SWGB_CULL_BACK) && !frontFacing) return 0;
         dW = fgt(A, 0.0f) ? 1 : 0;
+        pr->front = frontFacing;
     }
 
     int n = poly->n;
@@ -1203,10 +1259,13 @@ static void read_color(const ODraw *d, int q, int x, int y, float dst[4])
     if(is_unorm(st->color_format))
     {
         /* readPixel (PixelRoutine.cpp:1091-1130) widens b to b*257; alphaBlend
-         * scales by 1/0xFFFF (:1812-1828); B8G8R8A8 swaps R and B. */
+         * scales by 1/0xFFFF and decodes sRGB R, G, B (:1812-1828); B8G8R8A8
+         * swaps R and B. */
         const uint8_t *p = row + (size_t)x * 4;
-        const int bgra = st->color_format == SWGB_FORMAT_B8G8R8A8_UNORM;
+        const int bgra = is_bgra(st->color_format);
         for(int c = 0; c < 4; c++) dst[c] = fmul((float)(p[bgra ? bgra_byte(c) : c] * 257), 1.0f / 0xFFFF);
+        if(is_srgb(st->color_format))
+            for(int c = 0; c < 3; c++) dst[c] = srgb_to_linear(dst[c]);
     }
     else if(st->color_format == SWGB_FORMAT_R32G32B32A32_SFLOAT)
         memcpy(dst, row + (size_t)x * 16, 16);
@@ -1224,13 +1283,14 @@ static void write_color(const ODraw *d, int q, int x, int y, const float col[4])
     uint32_t wm = st->color_write_mask;
     if(is_unorm(st->color_format))
     {
-        /* writeColor (PixelRoutine.cpp:1975-1993,2603-2650); B8G8R8A8 swaps
-         * R and B, and their write-mask bits with them (:2138-2143) */
+        /* writeColor (PixelRoutine.cpp:1963-1993,2603-2650): sRGB encodes R, G,
+         * B first; B8G8R8A8 swaps R and B, and their write-mask bits with
+         * them (:2138-2143) */
         uint8_t *p = row + (size_t)x * 4;
-        const int bgra = st->color_format == SWGB_FORMAT_B8G8R8A8_UNORM;
+        const int bgra = is_bgra(st->color_format), srgb = is_srgb(st->color_format);
         for(int c = 0; c < 4; c++)
         {
-            float v = fminr(fmaxr(col[c], 0.0f), 1.0f);
+            float v = fminr(fmaxr((srgb && c < 3) ? linear_to_srgb(col[c]) : col[c], 0.0f), 1.0f);
             int32_t r = round_int(fmul(v, 255.0f));
             int16_t s16 = (int16_t)r;
             uint8_t b = s16 < 0 ? 0 : (s16 > 255 ? 255 : (uint8_t)s16); /* PackUnsigned */
@@ -1280,6 +1340,45 @@ static int bounds_pass(const ODraw *d, float stored)
 {
     const float z = d16(d->st) ? fmul(stored, 1.0f / 0xFFFF) : stored;
     return fle(d->st->min_depth_bounds, z) && fle(z, d->st->max_depth_bounds);
+}
+
+static uint8_t *stencil_at(const ODraw *d, int q, int x, int y)
+{
+    const swgb_pipeline_state *st = d->st;
+    return (uint8_t *)st->stencil + (size_t)q * st->stencil_slice_bytes + (size_t)y * st->stencil_pitch_bytes + (size_t)x;
+}
+
+/* stencilTest (:360-449): (reference & compareMask) op (stored & compareMask) */
+static int stencil_pass(const swgb_stencil_op_state *s, uint32_t stored)
+{
+    const uint32_t m = s->compare_mask & 0xFFu, r = s->reference & m, v = stored & m;
+    switch(s->compare_op)
+    {
+    case SWGB_COMPARE_NEVER: return 0;
+    case SWGB_COMPARE_LESS: return r < v;
+    case SWGB_COMPARE_EQUAL: return r == v;
+    case SWGB_COMPARE_LESS_OR_EQUAL: return r <= v;
+    case SWGB_COMPARE_GREATER: return r > v;
+    case SWGB_COMPARE_NOT_EQUAL: return r != v;
+    case SWGB_COMPARE_GREATER_OR_EQUAL: return r >= v;
+    default: return 1;
+    }
+}
+
+/* stencilOperation (:862-895), 8-bit with saturation / wrap */
+static uint32_t stencil_op(const swgb_stencil_op_state *s, uint32_t op, uint32_t v)
+{
+    switch(op)
+    {
+    case SWGB_STENCIL_OP_ZERO: return 0;
+    case SWGB_STENCIL_OP_REPLACE: return s->reference & 0xFFu;
+    case SWGB_STENCIL_OP_INCREMENT_AND_CLAMP: return v < 255 ? v + 1 : 255;
+    case SWGB_STENCIL_OP_DECREMENT_AND_CLAMP: return v > 0 ? v - 1 : 0;
+    case SWGB_STENCIL_OP_INVERT: return (~v) & 0xFFu;
+    case SWGB_STENCIL_OP_INCREMENT_AND_WRAP: return (v + 1) & 0xFFu;
+    case SWGB_STENCIL_OP_DECREMENT_AND_WRAP: return (v - 1) & 0xFFu;
+    default: return v;
+    }
 }
 
 static void write_depth(const ODraw *d, int q, int x, int y, float Z)
@@ -1352,6 +1451,19 @@ static void pixel_quad(const ODraw *d, const OSampler *smp, const OPrim *pr, int
 
     for(int q = 0; q < d->ms; q++)
     {
+        /* stencilTest (:360-449): sMask */
+        const int stencilOn = st->stencil && st->stencil_test_enable;
+        const swgb_stencil_op_state *so = pr->front ? &st->front : &st->back;
+        int sMask = cMask[q];
+        uint8_t sv[4] = { 0, 0, 0, 0 };
+        if(stencilOn)
+            for(int i = 0; i < 4; i++)
+            {
+                if(!(cMask[q] & (1 << i))) continue;
+                sv[i] = *stencil_at(d, q, x + (i & 1), y + (i >> 1));
+                if(!stencil_pass(so, sv[i])) sMask &= ~(1 << i);
+            }
+        int covered = cMask[q];
         /* late depth test (:330-344), depth write (:715-739) */
         int zMask = cMask[q];
         if(d->depthTest)
@@ -1381,6 +1493,7 @@ static void pixel_quad(const ODraw *d, const OSampler *smp, const OPrim *pr, int
                 if(pass && st->depth_bounds_test_enable && !bounds_pass(d, zb)) pass = 0;
                 if(pass) zMask |= 1 << i;
             }
+            if(stencilOn) zMask &= sMask; /* depthTest ends with zMask &= sMask (:571-574) */
             if(cnt) cnt->fragments_tested += (uint64_t)__builtin_popcount((unsigned)cMask[q]);
             if(d->depthWrite)
                 for(int i = 0; i < 4; i++)
@@ -1390,7 +1503,22 @@ static void pixel_quad(const ODraw *d, const OSampler *smp, const OPrim *pr, int
         {
             /* no depth test: the bounds test masks the coverage (:626-629) */
             for(int i = 0; i < 4; i++)
-                if((zMask & (1 << i)) && !bounds_pass(d, read_depth(d, q, x + (i & 1), y + (i >> 1)))) zMask &= ~(1 << i);
+                if((covered & (1 << i)) && !bounds_pass(d, read_depth(d, q, x + (i & 1), y + (i >> 1)))) covered &= ~(1 << i);
+            zMask = covered;
+        }
+        if(stencilOn)
+        {
+            /* writeStencil (:754-860): failOp where the stencil test failed,
+             * depthFailOp where the depth test did, passOp else; write mask */
+            for(int i = 0; i < 4; i++)
+            {
+                if(!(covered & (1 << i))) continue;
+                uint32_t op = !(sMask & (1 << i)) ? so->fail_op : ((d->depthTest && !(zMask & (1 << i))) ? so->depth_fail_op : so->pass_op);
+                uint32_t wm = so->write_mask & 0xFFu;
+                uint32_t nv = stencil_op(so, op, sv[i]);
+                *stencil_at(d, q, x + (i & 1), y + (i >> 1)) = (uint8_t)((nv & wm) | (sv[i] & ~wm));
+            }
+            zMask &= sMask; /* writeColor: xMask &= sMask (:2156-2159) */
         }
         if(cnt) cnt->fragments_passed += (uint64_t)__builtin_popcount((unsigned)zMask);
         if(d->vis)

@@ -75,7 +75,7 @@ def load(path=None):
     L.swgb_autotune.argtypes = [C.c_void_p, C.POINTER(abi.PipelineState), C.POINTER(abi.DrawArgs), C.c_uint32, C.c_int,
                                 C.POINTER(abi.RasterConfig), C.POINTER(abi.RasterConfig), C.POINTER(C.c_double)]
     L.swgb_autotune.restype = C.c_int
-    if L.swgb_abi_version() != 4:
+    if L.swgb_abi_version() != 5:
         raise OSError("libswgb ABI version mismatch")
     _lib = L
     return L

@@ -77,6 +77,15 @@ class Texture(C.Structure):
                 ("mip_lod_bias", C.c_float), ("min_lod", C.c_float), ("max_lod", C.c_float)]
 
 
+class StencilOpState(C.Structure):
+    _fields_ = [("fail_op", C.c_uint32), ("pass_op", C.c_uint32), ("depth_fail_op", C.c_uint32), ("compare_op", C.c_uint32),
+                ("compare_mask", C.c_uint32), ("write_mask", C.c_uint32), ("reference", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+STENCIL_OP_KEEP, STENCIL_OP_ZERO, STENCIL_OP_REPLACE, STENCIL_OP_INCREMENT_AND_CLAMP = 0, 1, 2, 3
+STENCIL_OP_DECREMENT_AND_CLAMP, STENCIL_OP_INVERT, STENCIL_OP_INCREMENT_AND_WRAP, STENCIL_OP_DECREMENT_AND_WRAP = 4, 5, 6, 7
+
+
 class PipelineState(C.Structure):
     _fields_ = [
         ("topology", C.c_uint32), ("attrib_count", C.c_uint32),
@@ -104,7 +113,9 @@ class PipelineState(C.Structure):
         ("texture", Texture),
         ("precision_profile", C.c_uint32), ("provoking_vertex", C.c_uint32),
         ("depth_bounds_test_enable", C.c_uint32), ("min_depth_bounds", C.c_float), ("max_depth_bounds", C.c_float),
-        ("reserved3", C.c_uint32),
+        ("stencil_test_enable", C.c_uint32), ("stencil", C.c_void_p), ("stencil_pitch_bytes", C.c_uint32),
+        ("reserved3", C.c_uint32), ("stencil_slice_bytes", C.c_uint64),
+        ("front", StencilOpState), ("back", StencilOpState),
     ]
 
 

@@ -68,7 +68,7 @@ struct AdjRegion {
 };
 
 template<int MS>
-struct AdjShared {
+struct __align__(16) AdjShared {  // 16: the warps' copies sit back to back
     float depth[MS][BIN * BIN];  // replayed depth
     float plane[PLANES][BATCH];
     uint32_t span[BATCH][MS][BIN];
@@ -76,6 +76,7 @@ struct AdjShared {
     uint16_t qpre[BATCH][BIN / 2 + 1];
     int8_t qr0[BATCH];
     int8_t nqr[BATCH];
+    int8_t front[BATCH];  // facing (unused: the adjoint takes no stencil)
     int triList[2 * BATCH];
     uint32_t writer[MS][BIN * BIN];  // not blended: last fragment written per sample
     uint32_t off[BIN * BIN + 1];     // blended: first entry of each pixel (prefix of cnt)
@@ -84,7 +85,7 @@ struct AdjShared {
     uint32_t logCount;               // blended: fragments appended to the region's log
     static constexpr int kSamples = MS;
     static constexpr int kBW = BIN, kBH = BIN;
-    static constexpr bool kD16 = false;  // the adjoint takes D32_SFLOAT depth only
+    static constexpr bool kFull = false;  // the adjoint takes D32_SFLOAT depth, no bias, bounds or stencil
 };
 
 // A bin's pixels may be split between four warps (quarters of 8x8 pixels,

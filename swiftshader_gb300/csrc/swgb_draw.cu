@@ -197,6 +197,7 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
     if(st->fragment_shader != SWGB_FS_VCOLOR && st->fragment_shader != SWGB_FS_TEX_X_VCOLOR) return set_error(SWGB_UNSUPPORTED_STATE, "fragment_shader");
     if(st->depth_clamp_enable) return set_error(SWGB_UNSUPPORTED_STATE, "depth clamp");
     if(st->color_format != SWGB_FORMAT_R8G8B8A8_UNORM && st->color_format != SWGB_FORMAT_B8G8R8A8_UNORM &&
+       st->color_format != SWGB_FORMAT_R8G8B8A8_SRGB && st->color_format != SWGB_FORMAT_B8G8R8A8_SRGB &&
        st->color_format != SWGB_FORMAT_R16G16B16A16_SFLOAT && st->color_format != SWGB_FORMAT_R32G32B32A32_SFLOAT)
         return set_error(SWGB_UNSUPPORTED_STATE, "color_format");
     if(st->depth_format != SWGB_FORMAT_UNDEFINED && st->depth_format != SWGB_FORMAT_D32_SFLOAT && st->depth_format != SWGB_FORMAT_D16_UNORM)
@@ -283,6 +284,34 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
     D.depthBounds = st->depth && st->depth_bounds_test_enable;
     D.minBounds = st->min_depth_bounds;
     D.maxBounds = st->max_depth_bounds;
+    // stencil (FragmentState::stencilActive and the stencil op states)
+    D.stencilTest = st->stencil && st->stencil_test_enable;
+    D.earlyDepthOK = 1;
+    if(D.stencilTest)
+    {
+        const swgb_stencil_op_state *ss[2] = {&st->front, &st->back};
+        for(int f = 0; f < 2; f++)
+        {
+            if(ss[f]->fail_op > SWGB_STENCIL_OP_DECREMENT_AND_WRAP || ss[f]->pass_op > SWGB_STENCIL_OP_DECREMENT_AND_WRAP ||
+               ss[f]->depth_fail_op > SWGB_STENCIL_OP_DECREMENT_AND_WRAP || ss[f]->compare_op > SWGB_COMPARE_ALWAYS)
+                return set_error(SWGB_INVALID_ARG, "stencil op state");
+            D.sFailOp[f] = ss[f]->fail_op;
+            D.sPassOp[f] = ss[f]->pass_op;
+            D.sDepthFailOp[f] = ss[f]->depth_fail_op;
+            D.sCompareOp[f] = ss[f]->compare_op;
+            D.sCompareMask[f] = ss[f]->compare_mask & 0xFFu;
+            D.sWriteMask[f] = ss[f]->write_mask & 0xFFu;
+            D.sReference[f] = ss[f]->reference & 0xFFu;
+            const bool ops = D.sFailOp[f] != SWGB_STENCIL_OP_KEEP || D.sPassOp[f] != SWGB_STENCIL_OP_KEEP ||
+                             D.sDepthFailOp[f] != SWGB_STENCIL_OP_KEEP;
+            if(ops && D.sWriteMask[f]) D.stencilWrite = 1;
+            // a depth-failing fragment must still update the stencil: no early rejection
+            if(D.sWriteMask[f] && (D.sFailOp[f] != SWGB_STENCIL_OP_KEEP || D.sDepthFailOp[f] != SWGB_STENCIL_OP_KEEP)) D.earlyDepthOK = 0;
+        }
+        D.stencil = (uint8_t *)st->stencil;
+        D.stencilPitch = st->stencil_pitch_bytes;
+        D.stencilSlice = st->stencil_slice_bytes;
+    }
     if(D.depthBias) D.planeVec4 = PLANES_STORED / 4;
     D.compareOp = st->depth_compare_op;
     D.hiz = 1;
@@ -299,9 +328,11 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
     D.ms = (int)st->sample_count;
     D.colorSlice = st->color_slice_bytes;
     D.depthSlice = st->depth_slice_bytes;
-    D.cf = st->color_format == SWGB_FORMAT_R8G8B8A8_UNORM ? CF_RGBA8
-           : st->color_format == SWGB_FORMAT_B8G8R8A8_UNORM ? CF_BGRA8
+    D.cf = (st->color_format == SWGB_FORMAT_R8G8B8A8_UNORM || st->color_format == SWGB_FORMAT_R8G8B8A8_SRGB) ? CF_RGBA8
+           : (st->color_format == SWGB_FORMAT_B8G8R8A8_UNORM || st->color_format == SWGB_FORMAT_B8G8R8A8_SRGB) ? CF_BGRA8
            : (st->color_format == SWGB_FORMAT_R16G16B16A16_SFLOAT ? CF_RGBA16F : CF_RGBA32F);
+    // sRGB-encoded 8-bit attachment: blend reads decode, writes encode R, G, B
+    D.colorSRGB = st->color_format == SWGB_FORMAT_R8G8B8A8_SRGB || st->color_format == SWGB_FORMAT_B8G8R8A8_SRGB;
     D.depth16 = st->depth_format == SWGB_FORMAT_D16_UNORM;
     D.color = (uint8_t *)st->color;
     D.colorPitch = st->color_pitch_bytes;
@@ -375,7 +406,14 @@ const RasterKernel &raster_kernel(int v)
 }
 
 // Raster kernel index of a draw: its bin shape, colour format and samples.
-inline int raster_variant(const DrawParams &D) { return raster_index(shape_index(D.binW, D.binH), D.hiz != 0, D.ms, D.cf, D.depth16 != 0); }
+// Draws with D16_UNORM depth, depth bias, the depth bounds test, the stencil
+// test or an sRGB colour attachment run the kernels that carry the full
+// per-sample pipeline.
+inline bool full_pipeline(const DrawParams &D)
+{
+    return D.depth16 || D.depthBias || D.depthBounds || D.stencilTest || D.colorSRGB;
+}
+inline int raster_variant(const DrawParams &D) { return raster_index(shape_index(D.binW, D.binH), D.hiz != 0, D.ms, D.cf, full_pipeline(D)); }
 
 // Persistent raster grid of one kernel variant: SMs x resident blocks.
 swgb_status raster_grid(int device, int v, bool batch, bool setAttr, int &blocks)
@@ -520,7 +558,7 @@ swgb_status prepare_scratch(swgb_ctx *ctx, DrawParams &D, bool order = true)
 // draws keep 16x16 bins).
 void apply_config(const swgb_ctx *ctx, DrawParams &D)
 {
-    if(D.ms == 1 && !D.depth16) set_bins(D, (int)ctx->rasterConfig.bin_width, (int)ctx->rasterConfig.bin_height);
+    if(D.ms == 1 && !full_pipeline(D)) set_bins(D, (int)ctx->rasterConfig.bin_width, (int)ctx->rasterConfig.bin_height);
     D.hiz = (int)ctx->rasterConfig.hiz;
 }
 
@@ -643,6 +681,9 @@ void draw_writes(const DrawParams &D, uintptr_t origin, std::vector<TouchRect> &
     {
         plane_rects((uintptr_t)D.color + (uintptr_t)q * D.colorSlice, origin, D.colorPitch, (int64_t)D.sx0 * cbpp,
                     (int64_t)D.sx1 * cbpp, D.sy0, D.sy1, out);
+        if(D.stencilTest)  // read by the test, maybe written: either orders the draw
+            plane_rects((uintptr_t)D.stencil + (uintptr_t)q * D.stencilSlice, origin, D.stencilPitch, (int64_t)D.sx0, (int64_t)D.sx1,
+                        D.sy0, D.sy1, out);
         if(D.depthTest || D.depthBounds)  // written, or read by the bounds test: either orders the draw
             plane_rects((uintptr_t)D.depth + (uintptr_t)q * D.depthSlice, origin, D.depthPitch, (int64_t)D.sx0 * (D.depth16 ? 2 : 4),
                         (int64_t)D.sx1 * (D.depth16 ? 2 : 4), D.sy0, D.sy1, out);
@@ -1081,6 +1122,7 @@ swgb_status bake_adjoint(const swgb_pipeline_state *st, const swgb_draw_args *a,
     if(D.restart) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint: primitive restart is not supported");
     if(D.depth16) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint needs a D32_SFLOAT depth attachment");
     if(D.depthBounds) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint: depth bounds test is not supported");
+    if(D.stencilTest) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint: stencil test is not supported");
     if(D.fs == SWGB_FS_TEX_X_VCOLOR && !D.texFloat) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint needs a float texture");
     if(D.writeMask != 0xFu) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint needs color_write_mask 0xF");
     if(a->count > ADJ_TRI_MASK) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint: too many triangles");
@@ -1253,9 +1295,6 @@ constexpr size_t NA_OFF_WORDS = na_up(NA_OFF_POLY + (size_t)NA_TRIS * MAX_POLY *
 // words: counters[8] (u64), spanCount (u64), polyCount (u32), binQueue (u32), error (i32)
 constexpr size_t NA_WORDS_BYTES = 8 * 8 + 8 + 4 + 4 + 4;
 constexpr size_t NA_BYTES = na_up(NA_OFF_WORDS + NA_WORDS_BYTES);
-static_assert(raster_smem<CF_RGBA32F, 1, 16, 16>() <= 48 * 1024 && raster_smem<CF_RGBA16F, 1, 16, 16>() <= 48 * 1024 &&
-                  raster_smem<CF_RGBA8, 1, 16, 16>() <= 48 * 1024,
-              "the allocation-free raster launch uses the default shared-memory limit");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
 
@@ -1280,7 +1319,9 @@ swgb_status noalloc_device(int dev, NoAllocDevice *&out)
         void *ptr = nullptr;
         swgb_status s = cuda_check(cudaGetSymbolAddress(&ptr, g_noalloc_scratch), "cudaGetSymbolAddress(scratch)");
         if(s != SWGB_OK) return s;
-        if((s = raster_grids(dev, false, d.rasterBlocks)) != SWGB_OK) return s;
+        // set-up, once per device: the raster kernels' shared-memory opt-in
+        // (a function attribute, no allocation) and their grids
+        if((s = raster_grids(dev, true, d.rasterBlocks)) != SWGB_OK) return s;
         d.base = (unsigned char *)ptr;
         d.ready = true;
     }
@@ -1511,6 +1552,11 @@ swgb_status swgb_autotune(swgb_ctx *ctx, const swgb_pipeline_state *states, cons
         {
             const uintptr_t c = (uintptr_t)st.color + (uintptr_t)q * D.colorSlice;
             iv.push_back({c, c + (uintptr_t)(h - 1) * st.color_pitch_bytes + cRow});
+            if(D.stencilTest)
+            {
+                const uintptr_t sb = (uintptr_t)st.stencil + (uintptr_t)q * D.stencilSlice;
+                iv.push_back({sb, sb + (uintptr_t)(h - 1) * st.stencil_pitch_bytes + st.framebuffer_width});
+            }
             if(st.depth)
             {
                 const uintptr_t d = (uintptr_t)st.depth + (uintptr_t)q * D.depthSlice;

@@ -70,7 +70,7 @@ struct TexLevel {
 // Per-triangle record written by k_setup next to its pixel box (a short4
 // x0, y0, x1, y1 with y0/y1 the trimmed [yMin, yMax); x0 >= x1 = no primitive).
 struct TriInfo {
-    uint32_t info;     // bits 0-4: polygon vertex count, bit 5: winding d, bit 6: clipped, bit 7: spans stored
+    uint32_t info;     // bits 0-4: polygon vertex count, bit 5: winding d, bit 6: clipped, bit 7: spans stored, bit 8: front-facing
     uint32_t slot;     // clipped polygon slot
     uint32_t spanOff;  // span-buffer index of row y0 of sample 0 (when stored)
     uint32_t rows;     // rows per sample plane in the span buffer
@@ -111,6 +111,15 @@ struct DrawParams {
     int depthBias;     // biasConstant or biasSlope nonzero: fragments add the triangle's zBias
     int depthBounds;   // depth bounds test against [minBounds, maxBounds]
     float minBounds, maxBounds;
+    // stencil (S8_UINT attachment): [0] front-facing, [1] back-facing state
+    uint8_t *stencil;
+    uint32_t stencilPitch;
+    uint64_t stencilSlice;
+    int stencilTest;        // stencil test active
+    int stencilWrite;       // some op can change a stored value
+    uint32_t sFailOp[2], sPassOp[2], sDepthFailOp[2], sCompareOp[2];
+    uint32_t sCompareMask[2], sWriteMask[2], sReference[2];
+    int earlyDepthOK;       // depth-failing fragments leave no trace (no stencil op on them): early / hierarchical rejection allowed
     float minDepthClamp, maxDepthClamp;
     int blend;
     uint32_t srcC, dstC, opC, srcA, dstA, opA;
@@ -121,6 +130,7 @@ struct DrawParams {
     uint64_t colorSlice, depthSlice;  // bytes between sample planes
     int cf;       // colour attachment format, CF_*
     int depth16;   // D16_UNORM depth attachment (else D32_SFLOAT)
+    int colorSRGB; // R8G8B8A8_SRGB / B8G8R8A8_SRGB colour attachment
     int texBGRA;   // 8-bit texture stored B8G8R8A8
     int texSRGB;   // 8-bit texture with sRGB-encoded R, G, B (decoded through srgbLut)
     const uint16_t *srgbLut;  // sRGBtoLinearFF_FF00: 8-bit sRGB -> 16-bit linear (0xFF00 = 1.0)
@@ -746,7 +756,7 @@ __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
     TriInfo inf = {0u, 0u, 0u, 0u};
     int cntIn = 0, cntClip = 0, cntVis = 0;
     bool cand = false;
-    int n = 3, dW = 1;
+    int n = 3, dW = 1, frontBit = 0;
     int32_t X[MAX_POLY + 1], Y[MAX_POLY + 1];
     int32_t yMin = 0, yMax = 0, xMinS = 0, xMaxS = 0;
     if(t < D.count && tri_valid(D, t))
@@ -791,6 +801,7 @@ __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
                     int32_t w0w1w2 = __float_as_int(c0.w) ^ __float_as_int(c1.w) ^ __float_as_int(c2.w);
                     if(w0w1w2 < 0) A = -A;
                     bool front = D.frontFace == SWGB_FRONT_FACE_COUNTER_CLOCKWISE ? (A >= 0.0f) : (A <= 0.0f);
+                    frontBit = front ? 1 : 0;
                     if((D.cullMode & SWGB_CULL_FRONT) && front) keep = false;
                     if((D.cullMode & SWGB_CULL_BACK) && !front) keep = false;
                     dW = A > 0.0f ? 1 : 0;
@@ -931,7 +942,7 @@ __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
             {
                 cntVis = 1;
                 box = make_short4((short)bx0, (short)yMin, (short)bx1, (short)yMax);
-                inf.info = (uint32_t)n | ((uint32_t)dW << 5) | ((uint32_t)cntClip << 6) | ((uint32_t)stored << 7);
+                inf.info = (uint32_t)n | ((uint32_t)dW << 5) | ((uint32_t)cntClip << 6) | ((uint32_t)stored << 7) | ((uint32_t)frontBit << 8);
                 if(!stored) inf.rows = 0;
                 if(cntClip)
                 {
@@ -1408,14 +1419,28 @@ static __device__ __noinline__ void blend_generic(const DrawParams &D, const flo
     out[3] = blend_op(D.opA, col[3], sf[3], dst[3], df[3]);
 }
 
+// sRGB colour attachments: decode of the blend's destination read, encode
+// before the write (ShaderCore.cpp:914-930).  Out of line: full-pipeline
+// kernels only.
+static __device__ __noinline__ void srgb_decode3(float v[4])
+{
+#pragma unroll
+    for(int c = 0; c < 3; c++) v[c] = srgb_to_linear(v[c]);
+}
+static __device__ __noinline__ void srgb_encode3(float v[4])
+{
+#pragma unroll
+    for(int c = 0; c < 3; c++) v[c] = linear_to_srgb(v[c]);
+}
+
 // The depth a fragment tests and writes: z itself for D32_SFLOAT; for
 // D16_UNORM Min(Max(Round(z * 0xFFFF), 0), 0xFFFF), compared against the
 // stored 16-bit value as a float and written back as that integer
 // (PixelRoutine.cpp:506-510,687-713).  Monotonic in z.
-template<bool D16>
-__device__ __forceinline__ float depth_value(float z)
+template<bool FULL>
+__device__ __forceinline__ float depth_value(const DrawParams &D, float z)
 {
-    if(!D16) return z;
+    if(!FULL || !D.depth16) return z;
     return fminf(fmaxf(rintf(z * 65535.0f), 0.0f), 65535.0f);
 }
 
@@ -1423,11 +1448,62 @@ __device__ __forceinline__ float depth_value(float z)
 // PixelRoutine.cpp:576-640): minDepthBounds <= z <= maxDepthBounds, D16_UNORM
 // values scaled by 1 / 0xFFFF; applied after the depth test, on the value the
 // sample found.
-template<bool D16>
 __device__ __forceinline__ bool bounds_pass(const DrawParams &D, float stored)
 {
-    const float z = D16 ? stored * (1.0f / 0xFFFF) : stored;
+    const float z = D.depth16 ? stored * (1.0f / 0xFFFF) : stored;
     return D.minBounds <= z && z <= D.maxBounds;
+}
+
+// Stencil test of face f (PixelRoutine.cpp:360-449): (reference & compareMask)
+// op (stored & compareMask), unsigned.
+__device__ __forceinline__ bool stencil_pass(const DrawParams &D, int f, uint32_t stored)
+{
+    const uint32_t m = D.sCompareMask[f] & 0xFFu;
+    const uint32_t r = D.sReference[f] & m, v = stored & m;
+    switch(D.sCompareOp[f])
+    {
+    case SWGB_COMPARE_NEVER: return false;
+    case SWGB_COMPARE_LESS: return r < v;
+    case SWGB_COMPARE_EQUAL: return r == v;
+    case SWGB_COMPARE_LESS_OR_EQUAL: return r <= v;
+    case SWGB_COMPARE_GREATER: return r > v;
+    case SWGB_COMPARE_NOT_EQUAL: return r != v;
+    case SWGB_COMPARE_GREATER_OR_EQUAL: return r >= v;
+    default: return true;
+    }
+}
+
+// A stencil operation on a stored byte (PixelRoutine.cpp:862-895).
+__device__ __forceinline__ uint32_t stencil_op(const DrawParams &D, int f, uint32_t op, uint32_t v)
+{
+    switch(op)
+    {
+    case SWGB_STENCIL_OP_ZERO: return 0u;
+    case SWGB_STENCIL_OP_REPLACE: return D.sReference[f] & 0xFFu;
+    case SWGB_STENCIL_OP_INCREMENT_AND_CLAMP: return v < 255u ? v + 1u : 255u;
+    case SWGB_STENCIL_OP_DECREMENT_AND_CLAMP: return v > 0u ? v - 1u : 0u;
+    case SWGB_STENCIL_OP_INVERT: return (~v) & 0xFFu;
+    case SWGB_STENCIL_OP_INCREMENT_AND_WRAP: return (v + 1u) & 0xFFu;
+    case SWGB_STENCIL_OP_DECREMENT_AND_WRAP: return (v - 1u) & 0xFFu;
+    default: return v;  // KEEP
+    }
+}
+
+// Stencil test, then the write-back of the sample's new stored value: failOp
+// where the stencil test failed, depthFailOp where the depth (and bounds) test
+// failed, passOp else, through the write mask (writeStencil :754-860).  Out of
+// line: only draws with a stencil attachment take it.
+static __device__ __noinline__ bool stencil_resolve(const DrawParams &D, uint8_t *sv, int f, bool depthPass)
+{
+    const uint32_t v = *sv;
+    const bool sp = stencil_pass(D, f, v);
+    if(D.stencilWrite)
+    {
+        const uint32_t op = !sp ? D.sFailOp[f] : (!depthPass ? D.sDepthFailOp[f] : D.sPassOp[f]);
+        const uint32_t wm = D.sWriteMask[f] & 0xFFu;
+        *sv = (uint8_t)((stencil_op(D, f, op, v) & wm) | (v & ~wm));
+    }
+    return sp;
 }
 
 __device__ __forceinline__ bool depth_pass(uint32_t op, float zb, float z)
@@ -1462,10 +1538,12 @@ __host__ __device__ constexpr int color_words(int cf) { return cf_unorm8(cf) ? 1
 
 // Shared memory of one warp: its bin's depth and colour, the staged batch,
 // and its ordered candidate list.
-// BW x BH is the bin's shape in pixels (powers of two, BH even); D16: the
-// depth attachment is D16_UNORM (the staged depth holds its integers).
-template<int CF, int MS, int BW = BIN, int BH = BIN, bool D16 = false>
-struct RasterShared {
+// BW x BH is the bin's shape in pixels (powers of two, BH even).  FULL: the
+// kernel carries the whole per-sample pipeline -- D16_UNORM depth (the staged
+// depth then holds its integers), depth bias, the depth bounds test and the
+// stencil test; without it those paths are compiled out.
+template<int CF, int MS, int BW = BIN, int BH = BIN, bool FULL = false>
+struct __align__(16) RasterShared {  // 16: the warps' copies sit back to back and take float4 / uint4 accesses
     float depth[MS][BW * BH];
     uint32_t color[MS][BW * BH * color_words(CF)];
     float plane[PLANES][BATCH];
@@ -1475,9 +1553,11 @@ struct RasterShared {
     int8_t qr0[BATCH];                 // first quad row of the triangle in the bin
     int8_t nqr[BATCH];                 // quad rows of the triangle in the bin
     int triList[2 * BATCH];
+    int8_t front[BATCH];               // the triangle faces front (stencil state [0]) or back ([1])
+    uint8_t stencil[FULL ? MS : 1][FULL ? BW * BH : 4];  // the bin's stencil values (stencil test active)
     static constexpr int kSamples = MS;
     static constexpr int kBW = BW, kBH = BH;
-    static constexpr bool kD16 = D16;
+    static constexpr bool kFull = FULL;
 };
 
 
@@ -1546,6 +1626,7 @@ __device__ int setup_batch_triangle(const DrawParams &D, SH &S, int ti, uint32_t
     const short4 box = D.triBox[t];
     const TriInfo inf = D.triInfo[t];
     const int n = inf.info & 31, dW = (inf.info >> 5) & 1;
+    S.front[ti] = (int8_t)((inf.info >> 8) & 1);
     constexpr int BW = SH::kBW, BH = SH::kBH;
     const int rowLo = max((int)box.y, by0), rowHi = min((int)box.w, by0 + BH);  // bin rows of the triangle
     const int qrA = (rowLo - by0) >> 1, qrB = (rowHi - 1 - by0) >> 1;            // quad rows [qrA, qrB]
@@ -1669,21 +1750,40 @@ __device__ __forceinline__ void shade_pixel(const DrawParams &D, const SH &S, in
 // (PixelRoutine.cpp:494-574,660-685; alphaBlend :1653-1961; writeColor
 // :1975-1993,2429-2650).
 template<int CF, class SH>
-__device__ __forceinline__ void rop_pixel(const DrawParams &D, SH &S, int q, int idx, float z, const float col[4],
+__device__ __forceinline__ void rop_pixel(const DrawParams &D, SH &S, int ti, int q, int idx, float z, const float col[4],
                                           unsigned long long &nTested, unsigned long long &nPassed)
 {
     float *depth = S.depth[q];
     uint32_t *color = S.color[q];
-    if(D.depthTest)
+    if(!SH::kFull)
     {
-        nTested++;
-        const float stored = depth[idx];
-        if(!depth_pass(D.compareOp, stored, z)) return;
-        if(D.depthBounds && !bounds_pass<SH::kD16>(D, stored)) return;
+        if(D.depthTest)
+        {
+            nTested++;
+            if(!depth_pass(D.compareOp, depth[idx], z)) return;
+            if(D.depthWrite) depth[idx] = z;
+        }
+    }
+    else
+    {
+        // masks as PixelRoutine::quad forms them (:97-124,330-358,530-575):
+        // the depth and bounds tests give zMask (with a depth test) or trim
+        // the coverage (without one); the stencil op then sees failOp /
+        // depthFailOp / passOp; depth and colour are written where every
+        // test passed
+        bool zPass = true;
+        if(D.depthTest)
+        {
+            nTested++;
+            const float stored = depth[idx];
+            zPass = depth_pass(D.compareOp, stored, z) && (!D.depthBounds || bounds_pass(D, stored));
+        }
+        else if(D.depthBounds && !bounds_pass(D, depth[idx]))
+            return;  // outside the coverage: no stencil op either
+        if(D.stencilTest && !stencil_resolve(D, &S.stencil[q][idx], S.front[ti] ? 0 : 1, zPass)) return;
+        if(!zPass) return;
         if(D.depthWrite) depth[idx] = z;
     }
-    else if(D.depthBounds && !bounds_pass<SH::kD16>(D, depth[idx]))
-        return;
     nPassed++;
     float out[4];
     if(D.blend)
@@ -1696,6 +1796,7 @@ __device__ __forceinline__ void rop_pixel(const DrawParams &D, SH &S, int q, int
             const uint32_t old = CF == CF_BGRA8 ? __byte_perm(color[idx], 0u, 0x3012u) : color[idx];
 #pragma unroll
             for(int c = 0; c < 4; c++) dst[c] = (float)(((old >> (8 * c)) & 0xFFu) * 257u) * (1.0f / 0xFFFF);
+            if(SH::kFull && D.colorSRGB) srgb_decode3(dst);  // sRGBtoLinear on R, G, B (:1822-1827)
         }
         else if(CF == CF_RGBA16F)
         {
@@ -1729,7 +1830,9 @@ __device__ __forceinline__ void rop_pixel(const DrawParams &D, SH &S, int q, int
     if(cf_unorm8(CF))
     {
         // packed in R, G, B, A byte order; B8G8R8A8 swaps R and B back on the
-        // way out, and its write-mask bits with them (:2138-2143)
+        // way out, and its write-mask bits with them (:2138-2143); sRGB
+        // attachments encode R, G, B before the clamp (:1965-1970)
+        if(SH::kFull && D.colorSRGB) srgb_encode3(out);
         uint32_t packed = CF == CF_BGRA8 ? __byte_perm(color[idx], 0u, 0x3012u) : color[idx];
 #pragma unroll
         for(int c = 0; c < 4; c++)
@@ -1791,8 +1894,8 @@ __device__ __forceinline__ float sample_depth(const DrawParams &D, const SH &S, 
         xF = xF - SLX[q];
     }
     float z = mul_add(xF, S.plane[2][ti], S.plane[4][ti] + yF * S.plane[3][ti]);
-    if(D.depthBias) z = z + S.plane[PLANE_ZBIAS][ti];  // PixelRoutine.cpp:141-144
-    return depth_value<SH::kD16>(rmin(rmax(z, D.minDepthClamp), D.maxDepthClamp));  // clampDepth
+    if(SH::kFull && D.depthBias) z = z + S.plane[PLANE_ZBIAS][ti];  // PixelRoutine.cpp:141-144
+    return depth_value<SH::kFull>(D, rmin(rmax(z, D.minDepthClamp), D.maxDepthClamp));  // clampDepth
 }
 
 // Hierarchical depth rejection of whole triangle-bin pairs.  Under LESS /
@@ -1841,7 +1944,7 @@ __device__ __forceinline__ bool hiz_rejects(const DrawParams &D, const SH &S, in
     const float zA = S.plane[2][ti], zB = S.plane[3][ti], zC = S.plane[4][ti];
     const float xFa = ((float)max((int)box.x, bx0) - 0.5f) - x0p, xFb = ((float)min((int)box.z, bx0 + SH::kBW) - 0.5f) - x0p;
     const float yFa = ((float)max((int)box.y, by0) - 0.5f) - y0p, yFb = ((float)min((int)box.w, by0 + SH::kBH) - 0.5f) - y0p;
-    const float bias = D.depthBias ? S.plane[PLANE_ZBIAS][ti] : 0.0f;
+    const float bias = (SH::kFull && D.depthBias) ? S.plane[PLANE_ZBIAS][ti] : 0.0f;
     const float T = fabsf(zC) + fmaxf(fabsf(yFa), fabsf(yFb)) * fabsf(zB) + fmaxf(fabsf(xFa), fabsf(xFb)) * fabsf(zA) + fabsf(bias);
     const float margin = T * (1.0f / 1048576.0f) + 1e-30f;
     const uint32_t op = D.compareOp;
@@ -1850,13 +1953,13 @@ __device__ __forceinline__ bool hiz_rejects(const DrawParams &D, const SH &S, in
         const float xF = zA >= 0.0f ? xFa : xFb, yF = zB >= 0.0f ? yFa : yFb;
         float zlo = (((zC + yF * zB) + xF * zA) + bias) - margin;
         if(!(zlo >= D.minDepthClamp)) zlo = D.minDepthClamp;  // also NaN
-        zlo = depth_value<SH::kD16>(fminf(zlo, D.maxDepthClamp));
+        zlo = depth_value<SH::kFull>(D, fminf(zlo, D.maxDepthClamp));
         return op == SWGB_COMPARE_LESS ? zb <= zlo : zb < zlo;
     }
     const float xF = zA >= 0.0f ? xFb : xFa, yF = zB >= 0.0f ? yFb : yFa;
     float zhi = (((zC + yF * zB) + xF * zA) + bias) + margin;
     if(!(zhi <= D.maxDepthClamp)) zhi = D.maxDepthClamp;
-    zhi = depth_value<SH::kD16>(fmaxf(zhi, D.minDepthClamp));
+    zhi = depth_value<SH::kFull>(D, fmaxf(zhi, D.minDepthClamp));
     return op == SWGB_COMPARE_GREATER ? zb >= zhi : zb > zhi;
 }
 
@@ -1918,8 +2021,8 @@ __device__ __noinline__ int hiz_pass(const DrawParams &D, const SH &S, int cnt, 
 // per lane (once per pixel, at its centre); lanes hitting the same pixel
 // resolve lowest lane (earliest triangle) first, all of the pixel's samples
 // at once.
-template<int CF, int MS, int BW, int BH, bool HIZ, bool D16>
-__device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared<CF, MS, BW, BH, D16> &S, int nb, int bx0, int by0, uint32_t inMask,
+template<int CF, int MS, int BW, int BH, bool HIZ, bool FULL>
+__device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared<CF, MS, BW, BH, FULL> &S, int nb, int bx0, int by0, uint32_t inMask,
                                           unsigned long long &nQuads, unsigned long long &nTested,
                                           unsigned long long &nPassed, uint32_t &lvMask)
 {
@@ -1932,7 +2035,8 @@ __device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared<CF, 
     // sample that fails against the bin's current depth fails at its ordered
     // turn too.
     const bool lessType = D.compareOp == SWGB_COMPARE_LESS || D.compareOp == SWGB_COMPARE_LESS_OR_EQUAL;
-    const bool earlyZ = D.depthTest && (lessType || D.compareOp == SWGB_COMPARE_GREATER || D.compareOp == SWGB_COMPARE_GREATER_OR_EQUAL);
+    const bool earlyZ = D.depthTest && (!FULL || D.earlyDepthOK) &&
+                        (lessType || D.compareOp == SWGB_COMPARE_GREATER || D.compareOp == SWGB_COMPARE_GREATER_OR_EQUAL);
     if(HIZ && earlyZ) cnt = hiz_pass<MS>(D, S, cnt, bx0, by0, inMask, lessType, nQuads, nTested);
     const int incl = warp_incl_scan(cnt, lane);
     const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
@@ -2052,7 +2156,7 @@ __device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared<CF, 
                         if(qMask >> (4 * q + i) & 1)
                         {
                             const float z = D.depthTest ? sample_depth<MS>(D, S, qTi, qX, by0 + 2 * qRow, i, q) : 0.0f;
-                            rop_pixel<CF>(D, S, q, pidx, z, col, nTested, nPassed);
+                            rop_pixel<CF>(D, S, qTi, q, pidx, z, col, nTested, nPassed);
                         }
                     pend &= ~(1u << lane);
                 }
@@ -2148,8 +2252,8 @@ __device__ __forceinline__ void walk_bin(const DrawParams &D, SH &S, int bx0, in
 
 // One bin of a draw: stage its depth and colour, walk the candidates in
 // primitive order in batches, write the bin back.
-template<int CF, int MS, int BW, int BH, bool HIZ, bool D16>
-__device__ __forceinline__ void raster_bin(const DrawParams &D, RasterShared<CF, MS, BW, BH, D16> &S, int bin, unsigned long long &nQuads,
+template<int CF, int MS, int BW, int BH, bool HIZ, bool FULL>
+__device__ __forceinline__ void raster_bin(const DrawParams &D, RasterShared<CF, MS, BW, BH, FULL> &S, int bin, unsigned long long &nQuads,
                                            unsigned long long &nTested, unsigned long long &nPassed, uint32_t &lvMask)
 {
     const int lane = threadIdx.x & 31;
@@ -2167,10 +2271,10 @@ __device__ __forceinline__ void raster_bin(const DrawParams &D, RasterShared<CF,
             const int ly = i / (BW / 4), lx = (i % (BW / 4)) * 4;
             const int px = bx0 + lx, py = by0 + ly;
             float4 dz = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
-            if((D.depthTest || D.depthBounds) && py < D.sy1 && px < D.sx1)
+            if((D.depthTest || (FULL && D.depthBounds)) && py < D.sy1 && px < D.sx1)
             {
                 const uint8_t *drow = dbase + (size_t)py * D.depthPitch;
-                if(D16)
+                if(FULL && D.depth16)
                 {
                     // D16_UNORM: the stored integers as floats (readDepth16)
                     uint32_t w0 = 0, w1 = 0;
@@ -2221,6 +2325,17 @@ __device__ __forceinline__ void raster_bin(const DrawParams &D, RasterShared<CF,
             *(uint4 *)&S.color[q][(ly * BW + lx) * CW] = cc;
         }
     }
+    if(FULL && D.stencilTest)
+        for(int q = 0; q < MS; q++)
+        {
+            // the bin's stencil bytes (1 per pixel and sample plane)
+            const uint8_t *sbase = D.stencil + (size_t)q * D.stencilSlice;
+            for(int i = lane; i < BW * BH; i += 32)
+            {
+                const int px = bx0 + i % BW, py = by0 + i / BW;
+                S.stencil[q][i] = (py < D.sy1 && px < D.sx1) ? sbase[(size_t)py * D.stencilPitch + px] : (uint8_t)0;
+            }
+        }
     __syncwarp();
 
     // bit k: pixel lane + 32k of the bin lies inside the scissor (the depth bound's domain)
@@ -2235,9 +2350,19 @@ __device__ __forceinline__ void raster_bin(const DrawParams &D, RasterShared<CF,
         }
 
     // ---- candidates in primitive order, in batches of BATCH ----------------------
-    walk_bin(D, S, bx0, by0, [&](int nb) { raster_batch<CF, MS, BW, BH, HIZ, D16>(D, S, nb, bx0, by0, inMask, nQuads, nTested, nPassed, lvMask); });
+    walk_bin(D, S, bx0, by0, [&](int nb) { raster_batch<CF, MS, BW, BH, HIZ, FULL>(D, S, nb, bx0, by0, inMask, nQuads, nTested, nPassed, lvMask); });
 
     // ---- write the bin back, every sample plane ----------------------------------
+    if(FULL && D.stencilWrite)
+        for(int q = 0; q < MS; q++)
+        {
+            uint8_t *sbase = D.stencil + (size_t)q * D.stencilSlice;
+            for(int i = lane; i < BW * BH; i += 32)
+            {
+                const int px = bx0 + i % BW, py = by0 + i / BW;
+                if(py >= D.sy0 && py < D.sy1 && px >= D.sx0 && px < D.sx1) sbase[(size_t)py * D.stencilPitch + px] = S.stencil[q][i];
+            }
+        }
     for(int q = 0; q < MS; q++)
     {
         uint8_t *dbase = D.depth + (size_t)q * D.depthSlice;
@@ -2249,7 +2374,7 @@ __device__ __forceinline__ void raster_bin(const DrawParams &D, RasterShared<CF,
             const int px = bx0 + lx, py = by0 + ly;
             if(py >= D.sy1 || px >= D.sx1 || py < D.sy0) continue;
             uint8_t *drow = dbase + (size_t)py * D.depthPitch;
-            if(D16)
+            if(FULL && D.depth16)
             {
                 // D16_UNORM: the staged values are integers 0..65535
                 const float4 v = *(const float4 *)&S.depth[q][ly * BW + lx];
@@ -2284,20 +2409,24 @@ __device__ __forceinline__ void raster_bin(const DrawParams &D, RasterShared<CF,
 
 // Shared memory of a raster block and the blocks one SM holds with it (the
 // register budget follows from that: 65536 / (blocks x threads)).
-template<int CF, int MS, int BW, int BH>
-constexpr size_t raster_smem() { return RASTER_WARPS * sizeof(RasterShared<CF, MS, BW, BH, false>); }  // D16 changes no size
-template<int CF, int MS, int BW, int BH>
+template<int CF, int MS, int BW, int BH, bool FULL>
+constexpr size_t raster_smem()
+{
+    static_assert(sizeof(RasterShared<CF, MS, BW, BH, FULL>) % 16 == 0, "each warp's shared block starts 16-byte aligned");
+    return RASTER_WARPS * sizeof(RasterShared<CF, MS, BW, BH, FULL>);
+}
+template<int CF, int MS, int BW, int BH, bool FULL>
 constexpr int raster_min_blocks()
 {
-    return (int)std::min<size_t>(8, std::max<size_t>(1, (size_t)(228 * 1024) / (raster_smem<CF, MS, BW, BH>() + 1024)));
+    return (int)std::min<size_t>(8, std::max<size_t>(1, (size_t)(228 * 1024) / (raster_smem<CF, MS, BW, BH, FULL>() + 1024)));
 }
 
-template<int CF, int MS, int BW, int BH, bool HIZ, bool D16>
-__global__ void __launch_bounds__(RASTER_THREADS, (raster_min_blocks<CF, MS, BW, BH>())) k_raster(const __grid_constant__ DrawParams D)
+template<int CF, int MS, int BW, int BH, bool HIZ, bool FULL>
+__global__ void __launch_bounds__(RASTER_THREADS, (raster_min_blocks<CF, MS, BW, BH, FULL>())) k_raster(const __grid_constant__ DrawParams D)
 {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    RasterShared<CF, MS, BW, BH, D16> &S = reinterpret_cast<RasterShared<CF, MS, BW, BH, D16> *>(smem_raw)[warp];
+    RasterShared<CF, MS, BW, BH, FULL> &S = reinterpret_cast<RasterShared<CF, MS, BW, BH, FULL> *>(smem_raw)[warp];
     const int nbins = D.binsX * D.binsY;
     unsigned long long nQuads = 0, nTested = 0, nPassed = 0;
     uint32_t lvMask = 0;
@@ -2310,7 +2439,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, (raster_min_blocks<CF, MS, BW,
         bin = __shfl_sync(0xFFFFFFFFu, bin, 0);
         if(bin >= nbins) break;
         if(D.binOrder) bin = (int)__ldg(D.binOrder + bin);
-        raster_bin<CF, MS, BW, BH, HIZ, D16>(D, S, bin, nQuads, nTested, nPassed, lvMask);
+        raster_bin<CF, MS, BW, BH, HIZ, FULL>(D, S, bin, nQuads, nTested, nPassed, lvMask);
     }
     flush_counters(D.counters, nQuads, nTested, nPassed, lvMask);
 }
@@ -2411,12 +2540,12 @@ __global__ void __launch_bounds__(SETUP_THREADS) k_setup_batch(const __grid_cons
 
 #endif  // SWGB_RASTER_TU
 
-template<int CF, int MS, int BW, int BH, bool HIZ, bool D16>
-__global__ void __launch_bounds__(RASTER_THREADS, (raster_min_blocks<CF, MS, BW, BH>())) k_raster_batch(const __grid_constant__ BatchPtrs B)
+template<int CF, int MS, int BW, int BH, bool HIZ, bool FULL>
+__global__ void __launch_bounds__(RASTER_THREADS, (raster_min_blocks<CF, MS, BW, BH, FULL>())) k_raster_batch(const __grid_constant__ BatchPtrs B)
 {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    RasterShared<CF, MS, BW, BH, D16> &S = reinterpret_cast<RasterShared<CF, MS, BW, BH, D16> *>(smem_raw)[warp];
+    RasterShared<CF, MS, BW, BH, FULL> &S = reinterpret_cast<RasterShared<CF, MS, BW, BH, FULL> *>(smem_raw)[warp];
     const BatchView V(B.hdr);
     const BatchHeader &h = V.h;
     unsigned long long nQuads = 0, nTested = 0, nPassed = 0;
@@ -2428,7 +2557,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, (raster_min_blocks<CF, MS, BW,
         bin = __shfl_sync(0xFFFFFFFFu, bin, 0);
         if(bin >= h.bins) break;
         const uint32_t d = find_draw(V.bStart, h.n, bin);
-        raster_bin<CF, MS, BW, BH, HIZ, D16>(V.draws[d], S, (int)(bin - __ldg(V.bStart + d)), nQuads, nTested, nPassed, lvMask);
+        raster_bin<CF, MS, BW, BH, HIZ, FULL>(V.draws[d], S, (int)(bin - __ldg(V.bStart + d)), nQuads, nTested, nPassed, lvMask);
     }
     flush_counters(B.counters, nQuads, nTested, nPassed, lvMask);
 }
@@ -2451,12 +2580,12 @@ struct RasterKernel {
     void (*launchBatch)(const BatchPtrs &, uint32_t, cudaStream_t);
 };
 
-// Table index of a variant: single-sample D32F draws by (shape, hiz, format);
-// four-sample D32F draws (16x16) by (hiz, format); D16_UNORM draws (16x16) by
-// (samples, hiz, format).
-__host__ __device__ constexpr int raster_index(int shape, bool hiz, int ms, int cf, bool d16)
+// Table index of a variant: single-sample draws by (shape, hiz, format);
+// four-sample draws (16x16) by (hiz, format); draws needing the full
+// per-sample pipeline (16x16) by (samples, hiz, format).
+__host__ __device__ constexpr int raster_index(int shape, bool hiz, int ms, int cf, bool full)
 {
-    return d16 ? NSHAPES * 2 * NCF + 2 * NCF + ((ms > 1 ? 2 : 0) + (hiz ? 0 : 1)) * NCF + cf
+    return full ? NSHAPES * 2 * NCF + 2 * NCF + ((ms > 1 ? 2 : 0) + (hiz ? 0 : 1)) * NCF + cf
                : (ms > 1 ? NSHAPES * 2 * NCF + (hiz ? 0 : 1) * NCF + cf : (shape * 2 + (hiz ? 0 : 1)) * NCF + cf);
 }
 

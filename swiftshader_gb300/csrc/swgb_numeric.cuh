@@ -117,4 +117,47 @@ __device__ __forceinline__ uint32_t reactor_float_to_half(float f)
     return fp16i & 0xFFFFu;
 }
 
+// Log2 and Exp2 at relaxed (mediump) precision, the forms Pow<Mediump> uses
+// (src/Pipeline/ShaderCore.cpp:336-386,406-470,472-477; the CMake build's
+// SWIFTSHADER_LEGACY_PRECISION is false).  Log2: the float's bits read as an
+// integer give a piecewise-linear log2; a quadratic in the unnormalised
+// mantissa corrects it.  Exp2: the clamped input split into floor and
+// fraction, a quadratic correction, and the sum scaled into the exponent
+// field (Malossi et al., "Fast Exponential Computation on SIMD
+// Architectures").
+__device__ __forceinline__ float log2_mediump(float x)
+{
+    const int32_t im = __float_as_int(x);
+    float y = mul_add(__int2float_rn(im), 1.0f / (1 << 23), -127.0f);
+    if(im == 0x7F800000) y = __int_as_float(__float_as_int(y) | 0x7F800000);  // log2(inf) = inf
+    const float m = __int2float_rn(im & 0x007FFFFF);
+    const float f = mul_add(mul_add(2.8017103e-22f, m, -8.373131e-15f), m, 5.0615534e-8f);
+    return mul_add(f, m, y);
+}
+__device__ __forceinline__ float exp2_mediump(float x)
+{
+    float x0 = rmin(x, 128.0f);
+    x0 = rmax(x0, __int_as_float((int32_t)0xC2FDFFFF));  // -126.999992
+    const float f = x0 - floorf(x0);
+    const float r = mul_add(mul_add(7.8145574e-2f, f, 2.2617357e-1f), f, -3.0444314e-1f);
+    const float y = mul_add(r, f, x0);
+    return __int_as_float(trunc_int(mul_add((float)(1 << 23), y, (float)(127 << 23))));
+}
+__device__ __forceinline__ float pow_mediump(float x, float y) { return exp2_mediump(log2_mediump(x) * y); }
+
+// sRGB transfer functions of colour attachments (ShaderCore.cpp:914-930):
+// linear below the knee, else the mediump power.
+__device__ __forceinline__ float linear_to_srgb(float c)
+{
+    const float lc = c * 12.92f;
+    const float ec = mul_add(1.055f, pow_mediump(c, 1.0f / 2.4f), -0.055f);
+    return c < 0.0031308f ? lc : ec;
+}
+__device__ __forceinline__ float srgb_to_linear(float c)
+{
+    const float lc = c * (1.0f / 12.92f);
+    const float ec = pow_mediump(mul_add(c, 1.0f / 1.055f, 0.055f / 1.055f), 2.4f);
+    return c < 0.04045f ? lc : ec;
+}
+
 }  // namespace swgb

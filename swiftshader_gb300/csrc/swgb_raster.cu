@@ -2,7 +2,8 @@
 // (SWGB_RASTER_CF = 0 R8G8B8A8_UNORM, 1 R16G16B16A16_SFLOAT,
 // 2 R32G32B32A32_SFLOAT, 3 B8G8R8A8_UNORM): every bin shape, with and without
 // hierarchical depth rejection, single-sample and (16x16 bins) four-sample,
-// for D32_SFLOAT depth; 16x16 bins for D16_UNORM depth.  The build compiles
+// for the common pixel pipeline; 16x16 bins for the full one (D16_UNORM
+// depth, depth bias, depth bounds, stencil).  The build compiles
 // this file once per format, in parallel, and links the objects into libswgb.
 #define SWGB_RASTER_TU 1
 #include "swgb_kernels.cuh"
@@ -15,24 +16,24 @@ namespace swgbk {
 
 namespace {
 
-template<int CF, int MS, int BW, int BH, bool HIZ, bool D16>
+template<int CF, int MS, int BW, int BH, bool HIZ, bool FULL>
 void launch_raster_t(const DrawParams &D, uint32_t blocks, cudaStream_t st)
 {
-    k_raster<CF, MS, BW, BH, HIZ, D16><<<blocks, RASTER_THREADS, raster_smem<CF, MS, BW, BH>(), st>>>(D);
+    k_raster<CF, MS, BW, BH, HIZ, FULL><<<blocks, RASTER_THREADS, raster_smem<CF, MS, BW, BH, FULL>(), st>>>(D);
 }
 
-template<int CF, int MS, int BW, int BH, bool HIZ, bool D16>
+template<int CF, int MS, int BW, int BH, bool HIZ, bool FULL>
 void launch_raster_batch_t(const BatchPtrs &P, uint32_t blocks, cudaStream_t st)
 {
-    k_raster_batch<CF, MS, BW, BH, HIZ, D16><<<blocks, RASTER_THREADS, raster_smem<CF, MS, BW, BH>(), st>>>(P);
+    k_raster_batch<CF, MS, BW, BH, HIZ, FULL><<<blocks, RASTER_THREADS, raster_smem<CF, MS, BW, BH, FULL>(), st>>>(P);
 }
 
-template<int CF, int MS, int BW, int BH, bool HIZ, bool D16 = false>
+template<int CF, int MS, int BW, int BH, bool HIZ, bool FULL = false>
 void put(RasterKernel *table)
 {
-    table[raster_index(shape_index(BW, BH), HIZ, MS, CF, D16)] = {
-        (const void *)k_raster<CF, MS, BW, BH, HIZ, D16>, (const void *)k_raster_batch<CF, MS, BW, BH, HIZ, D16>,
-        raster_smem<CF, MS, BW, BH>(), launch_raster_t<CF, MS, BW, BH, HIZ, D16>, launch_raster_batch_t<CF, MS, BW, BH, HIZ, D16>};
+    table[raster_index(shape_index(BW, BH), HIZ, MS, CF, FULL)] = {
+        (const void *)k_raster<CF, MS, BW, BH, HIZ, FULL>, (const void *)k_raster_batch<CF, MS, BW, BH, HIZ, FULL>,
+        raster_smem<CF, MS, BW, BH, FULL>(), launch_raster_t<CF, MS, BW, BH, HIZ, FULL>, launch_raster_batch_t<CF, MS, BW, BH, HIZ, FULL>};
 }
 
 }  // namespace
@@ -53,7 +54,7 @@ void fill_raster_table<SWGB_RASTER_CF>(RasterKernel *table)
     put<CF, 1, 16, 16, false, true>(table);
     put<CF, 4, 16, 16, true, true>(table);
     put<CF, 4, 16, 16, false, true>(table);
-    static_assert(NSHAPES == 3 && NRASTER == NSHAPES * 2 * NCF + 2 * NCF + 4 * NCF, "one entry per shape, hiz, samples and depth format");
+    static_assert(NSHAPES == 3 && NRASTER == NSHAPES * 2 * NCF + 2 * NCF + 4 * NCF, "one entry per shape, hiz, samples and pixel pipeline");
 }
 
 }  // namespace swgbk

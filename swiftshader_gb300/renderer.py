@@ -130,12 +130,14 @@ class DeviceScene:
         self.indices = None if scene.indices is None else torch.from_numpy(scenes.index_bytes(scene)).to(self.device)
         self.levels = [torch.from_numpy(np.ascontiguousarray(l)).to(self.device) for l in scene.texture_levels]
         cdtype = {abi.FORMAT_R8G8B8A8_UNORM: torch.uint8, abi.FORMAT_B8G8R8A8_UNORM: torch.uint8,
+                  abi.FORMAT_R8G8B8A8_SRGB: torch.uint8, abi.FORMAT_B8G8R8A8_SRGB: torch.uint8,
                   abi.FORMAT_R32G32B32A32_SFLOAT: torch.float32, abi.FORMAT_R16G16B16A16_SFLOAT: torch.float16}[scene.color_format]
         cshape, dshape = scenes.attachment_shapes(scene)
         self.color = torch.empty(cshape, dtype=cdtype, device=self.device)
         # D16_UNORM attachments live in int16 tensors (the same bits; torch has no uint16 arithmetic)
         self.d16 = scene.depth_format == abi.FORMAT_D16_UNORM
         self.depth = torch.empty(dshape, dtype=torch.int16 if self.d16 else torch.float32, device=self.device)
+        self.stencil = None if scene.stencil is None else torch.empty(dshape, dtype=torch.uint8, device=self.device)
         self.clear()
 
     def clear(self):
@@ -145,6 +147,8 @@ class DeviceScene:
             self.depth.fill_(int(np.array(scenes.depth_clear_value(self.scene)).view(np.int16)))
         else:
             self.depth.fill_(self.scene.clear_depth)
+        if self.stencil is not None:
+            self.stencil.fill_(int(self.scene.stencil.get("clear", 0)))
 
     def depth_numpy(self):
         """The depth attachment on the host: float32, or uint16 for D16_UNORM."""
@@ -153,7 +157,8 @@ class DeviceScene:
 
     def state(self):
         return scenes.build_state(self.scene, self.color.data_ptr(), self.depth.data_ptr(), self.vertices.data_ptr(),
-                                  [l.data_ptr() for l in self.levels])
+                                  [l.data_ptr() for l in self.levels],
+                                  stencil_ptr=None if self.stencil is None else self.stencil.data_ptr())
 
     def args(self):
         return scenes.build_args(self.scene, None if self.indices is None else self.indices.data_ptr())

@@ -52,6 +52,9 @@ class Scene:
     depth_bias: tuple = (0.0, 0.0, 0.0)     # (constant, slope, clamp)
     depth_bounds: tuple = None        # (min, max) enables the depth bounds test
     depth_test: bool = True
+    # stencil: {"front": (fail, pass, depth_fail, compare, compare_mask, write_mask, reference),
+    #           "back": (...), "clear": value} on an S8_UINT attachment, or None
+    stencil: dict = None
     restart_index_count: int = 0      # > 0: primitive restart over this many indices (tri_count ignored)
 
     @property
@@ -304,7 +307,7 @@ def scene_sphere_views(view, n_views=256, seg_u=250, seg_v=200, width=512, heigh
                  color_format=abi.FORMAT_R16G16B16A16_SFLOAT, clear_color=(0.0, 0.0, 0.0, 0.0))
 
 
-def build_state(scene, color_ptr, depth_ptr, vertex_ptr, level_ptrs=None, color_pitch=None, depth_pitch=None):
+def build_state(scene, color_ptr, depth_ptr, vertex_ptr, level_ptrs=None, color_pitch=None, depth_pitch=None, stencil_ptr=None):
     """PipelineState for a scene given buffer addresses (device pointers for
     the GB300 path, host pointers for the oracle)."""
     st = abi.PipelineState()
@@ -333,6 +336,14 @@ def build_state(scene, color_ptr, depth_ptr, vertex_ptr, level_ptrs=None, color_
     if scene.depth_bounds is not None:
         st.depth_bounds_test_enable = 1
         st.min_depth_bounds, st.max_depth_bounds = (float(x) for x in scene.depth_bounds)
+    if scene.stencil is not None:
+        st.stencil_test_enable = 1
+        st.stencil = stencil_ptr
+        st.stencil_pitch_bytes = scene.width
+        st.stencil_slice_bytes = scene.width * scene.height
+        for face in ("front", "back"):
+            v = scene.stencil[face]
+            setattr(st, face, abi.StencilOpState(*(int(x) for x in v), 0))
     st.depth_compare_op = scene.depth_compare
     st.color_format = scene.color_format
     if scene.blend is not None:
@@ -341,7 +352,8 @@ def build_state(scene, color_ptr, depth_ptr, vertex_ptr, level_ptrs=None, color_
          st.src_alpha_factor, st.dst_alpha_factor, st.alpha_blend_op) = scene.blend
     st.color_write_mask = scene.color_write_mask
     st.sample_count = scene.samples
-    bpp = {abi.FORMAT_R8G8B8A8_UNORM: 4, abi.FORMAT_B8G8R8A8_UNORM: 4, abi.FORMAT_R16G16B16A16_SFLOAT: 8,
+    bpp = {abi.FORMAT_R8G8B8A8_UNORM: 4, abi.FORMAT_B8G8R8A8_UNORM: 4, abi.FORMAT_R8G8B8A8_SRGB: 4,
+           abi.FORMAT_B8G8R8A8_SRGB: 4, abi.FORMAT_R16G16B16A16_SFLOAT: 8,
            abi.FORMAT_R32G32B32A32_SFLOAT: 16}[scene.color_format]
     st.color = color_ptr
     st.color_pitch_bytes = color_pitch or scene.width * bpp
@@ -442,7 +454,8 @@ def attachment_shapes(scene):
 
 
 def color_dtype(scene):
-    return {abi.FORMAT_R8G8B8A8_UNORM: np.uint8, abi.FORMAT_B8G8R8A8_UNORM: np.uint8, abi.FORMAT_R32G32B32A32_SFLOAT: np.float32,
+    return {abi.FORMAT_R8G8B8A8_UNORM: np.uint8, abi.FORMAT_B8G8R8A8_UNORM: np.uint8, abi.FORMAT_R8G8B8A8_SRGB: np.uint8,
+            abi.FORMAT_B8G8R8A8_SRGB: np.uint8, abi.FORMAT_R32G32B32A32_SFLOAT: np.float32,
             abi.FORMAT_R16G16B16A16_SFLOAT: np.float16}[scene.color_format]
 
 
@@ -456,6 +469,14 @@ def depth_clear_value(scene):
     if scene.depth_format == abi.FORMAT_D16_UNORM:
         return np.uint16(int(np.rint(np.float32(scene.clear_depth) * np.float32(65535.0))))
     return np.float32(scene.clear_depth)
+
+
+def stencil_buffer(scene):
+    """The scene's S8_UINT stencil attachment on the host, cleared (None without stencil)."""
+    if scene.stencil is None:
+        return None
+    _, ds = attachment_shapes(scene)
+    return np.full(ds, scene.stencil.get("clear", 0), np.uint8)
 
 
 def clear_buffers(scene):

@@ -23,6 +23,7 @@ STRUCTS = {
     "swgb_counters": abi.Counters,
     "swgb_adjoint_args": abi.AdjointArgs,
     "swgb_raster_config": abi.RasterConfig,
+    "swgb_stencil_op_state": abi.StencilOpState,
 }
 
 
@@ -71,7 +72,7 @@ def test_library_loads_and_exports_all_symbols(built_lib):
     for name in _lib.EXPORTS:
         assert name in exported, name
     L = _lib.load(built_lib)
-    assert L.swgb_abi_version() == 4
+    assert L.swgb_abi_version() == 5
 
 
 def test_host_side_errors_without_device(built_lib):

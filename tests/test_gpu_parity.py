@@ -321,6 +321,26 @@ def test_bgra_attachment(gpu_lib, write_mask):
     check_scene(s, gpu_lib)
 
 
+@pytest.mark.parametrize("color_fmt", [abi.FORMAT_R8G8B8A8_SRGB, abi.FORMAT_B8G8R8A8_SRGB])
+@pytest.mark.parametrize("blend,write_mask", [(True, 0xF), (False, 0xF), (True, 0b1011)])
+def test_srgb_attachment(gpu_lib, color_fmt, blend, write_mask):
+    """sRGB colour attachments: the blend decodes the destination's R, G, B with
+    sRGBtoLinear and the write encodes with linearToSRGB, both through
+    Pow<Mediump> (Reactor's relaxed Log2/Exp2 polynomials); 4x MSAA too."""
+    s = scenes.scene_textured_small(n_tris=400, width=96, height=72, blend=blend, seed_index=76)
+    s.color_format = color_fmt
+    s.clear_color = (3, 60, 181, 77)
+    s.color_write_mask = write_mask
+    check_scene(s, gpu_lib)
+    # additive blend: sums above 1 reach the encode before its clamp
+    s = scenes.scene_small(n_tris=200, width=64, height=48, seed_index=77)
+    s.color_format = color_fmt
+    s.samples = 4
+    if blend:
+        s.blend = (abi.BLEND_ONE, abi.BLEND_ONE, abi.BLEND_OP_ADD, abi.BLEND_ONE, abi.BLEND_ONE, abi.BLEND_OP_ADD)
+    check_scene(s, gpu_lib)
+
+
 def test_d16_depth(gpu_lib):
     """D16_UNORM depth: fragments quantized to Round(z * 0xFFFF) and compared
     against the stored integers, every compare op; 4x MSAA; dense overlap."""
@@ -374,3 +394,56 @@ def test_depth_bounds(gpu_lib, bounds, depth_test):
         if d16:
             s.depth_format = abi.FORMAT_D16_UNORM
         check_scene(s, gpu_lib)
+
+
+def check_stencil_scene(scene):
+    import torch
+    import oracle
+    from swiftshader_gb300 import DeviceScene, Renderer
+    r = Renderer(0)
+    ds = DeviceScene(scene)
+    torch.cuda.synchronize()
+    r.reset_counters()
+    r.draw(ds.state(), ds.args())
+    r.synchronize()
+    c_ref, d_ref, s_ref, cnt_ref = oracle.render_stencil(scene, 4)
+    assert_bit_exact(ds.stencil.cpu().numpy(), s_ref, "stencil")
+    assert_bit_exact(ds.depth_numpy(), d_ref, "depth")
+    assert_bit_exact(ds.color.cpu().numpy(), c_ref, "color")
+    assert_counters(r.counters(), cnt_ref)
+    return cnt_ref
+
+
+K, Z, R, IC, DC, INV, IW, DW = range(8)
+STENCIL_CASES = [
+    # front: (fail, pass, depth_fail, compare, compare_mask, write_mask, ref), back likewise, clear
+    ((K, IW, K, abi.COMPARE_ALWAYS, 0xFF, 0xFF, 0), (K, DW, K, abi.COMPARE_ALWAYS, 0xFF, 0xFF, 0), 7),
+    ((INV, R, IC, abi.COMPARE_LESS, 0x0F, 0xF0, 5), (DC, Z, INV, abi.COMPARE_GREATER_OR_EQUAL, 0xFF, 0x3F, 9), 6),
+    ((R, K, K, abi.COMPARE_EQUAL, 0xFF, 0xFF, 4), (R, K, K, abi.COMPARE_NOT_EQUAL, 0xFF, 0xFF, 4), 4),
+    ((K, IC, K, abi.COMPARE_LESS_OR_EQUAL, 0xFF, 0x00, 200), (K, DC, K, abi.COMPARE_GREATER, 0xFF, 0xFF, 3), 250),
+    ((K, K, K, abi.COMPARE_NEVER, 0xFF, 0xFF, 0), (K, K, K, abi.COMPARE_ALWAYS, 0xFF, 0xFF, 0), 0),
+]
+
+
+@pytest.mark.parametrize("case", range(len(STENCIL_CASES)))
+@pytest.mark.parametrize("depth_test,samples", [(True, 1), (False, 1), (True, 4)])
+def test_stencil(gpu_lib, case, depth_test, samples):
+    """Stencil test and ops (front / back by facing, compare and write masks,
+    every op and compare), with and without a depth test, 4x MSAA; cases whose
+    ops act on failing fragments run without early depth rejection."""
+    front, back, clear = STENCIL_CASES[case]
+    s = scenes.scene_small(n_tris=700, width=88, height=72, seed_index=77 + case)
+    s.stencil = {"front": front, "back": back, "clear": clear}
+    s.depth_test = depth_test
+    s.samples = samples
+    cnt = check_stencil_scene(s)
+    assert cnt["fragments_tested"] > 0 or not depth_test
+
+
+def test_stencil_with_bounds_and_d16(gpu_lib):
+    s = scenes.scene_small(n_tris=700, width=88, height=72, seed_index=83)
+    s.stencil = {"front": STENCIL_CASES[1][0], "back": STENCIL_CASES[1][1], "clear": 6}
+    s.depth_bounds = (0.2, 0.8)
+    s.clear_depth = 0.7
+    s.depth_format = abi.FORMAT_D16_UNORM
+    check_stencil_scene(s)

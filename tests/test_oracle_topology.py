@@ -160,3 +160,15 @@ def test_depth_bias_constant_known_answer(oracle_mod):
     s.depth_bias = (float(2 ** 20), 0.0, 0.03)
     d = oracle_mod.render(s)[1]
     assert (d[d < 1.0] == np.float32(0.5) + np.float32(0.03)).all()
+
+
+def test_stencil_counts_fragments(oracle_mod):
+    """Stencil INCREMENT_AND_WRAP on pass with compare ALWAYS and depth ALWAYS:
+    the stencil attachment ends holding, per pixel, how many fragments
+    passed; their sum is the fragments_passed counter."""
+    s = scenes.scene_small(n_tris=300, width=64, height=48, seed_index=76)
+    s.depth_compare = abi.COMPARE_ALWAYS
+    op = (abi.STENCIL_OP_KEEP, abi.STENCIL_OP_INCREMENT_AND_WRAP, abi.STENCIL_OP_KEEP, abi.COMPARE_ALWAYS, 0xFF, 0xFF, 0)
+    s.stencil = {"front": op, "back": op, "clear": 0}
+    _, _, st, cnt = oracle_mod.render_stencil(s)
+    assert int(st.astype(np.int64).sum()) == cnt["fragments_passed"] > 1000
