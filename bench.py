@@ -18,7 +18,12 @@ The default line also carries
   * "adjoint": forward and adjoint times (and their ratio) of the two adjoint
     workloads at full size -- the 20k-triangle sphere at 512^2 RGBA32F and 256
     views of the 100k-triangle noisy sphere at 512^2 4x MSAA -- through the
-    calls the autograd function makes.
+    calls the autograd function makes;
+  * "blitter": the Blitter steps either side of a draw on images larger than
+    L2 -- 4x MSAA resolves (byte-averaging RGBA8 and averaging RGBA16F),
+    a 13-level LINEAR mip chain of an 8192^2 RGBA8 texture, clears of 4x MSAA
+    colour and depth -- each as achieved GB/s of its algorithmic bytes and the
+    fraction of the measured HBM peak.
 --workload batch measures the full 4096-draw atlas workload (log-uniform
 [16, 65536] triangles) as the headline line: one step = clear the atlas + one
 swgb_draw_batch of all draws.
@@ -280,6 +285,10 @@ def run_ours(args):
         batched["config"]["note"] = ("reduced-size sample of the batch workload (triangles log-uniform in "
                                      "[16, 1024] instead of [16, 65536]); --workload batch runs the full one")
 
+    blitter = None
+    if args.workload == "heightfield" and not args.no_blitter:
+        blitter = measure_blitter(r, stream, flush, dev)
+
     adjoint_lines = None
     if args.workload == "heightfield" and not args.no_adjoint:
         adjoint_lines = {"sphere": measure_adjoint(r, stream, flush, dev, "sphere"),
@@ -343,12 +352,70 @@ def run_ours(args):
         line["batched"] = batched
     if adjoint_lines is not None:
         line["adjoint"] = adjoint_lines
+    if blitter is not None:
+        line["blitter"] = blitter
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args, scene, bounded_s=args.cpu_seconds)
     print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def measure_blitter(r, stream, flush, dev, steps=5, warmup=3):
+    """GB/s of swgb_resolve / swgb_blit (mip chain) / swgb_clear on images
+    larger than L2; algorithmic bytes = every byte read once + every byte
+    written once."""
+    import torch
+    from swiftshader_gb300 import abi
+    from swiftshader_gb300.renderer import image_view
+    peak, peak_kind = measured_peaks()
+    out = {}
+
+    def run(name, body, nbytes, note):
+        for _ in range(warmup):
+            body()
+        torch.cuda.synchronize()
+        ms = statistics.median(time_steps(stream, flush, steps, body))
+        gbs = nbytes / (ms * 1e-3) / 1e9
+        out[name] = {"ms": round(ms, 4), "bytes": int(nbytes), "achieved_gbs": round(gbs, 1),
+                     "frac": round(gbs / peak, 4), "what": note}
+
+    g = torch.Generator(device=dev).manual_seed(9)
+    n = 4096
+    ms4 = torch.randint(0, 256, (4, n, n, 4), dtype=torch.uint8, device=dev, generator=g)
+    one = torch.empty((n, n, 4), dtype=torch.uint8, device=dev)
+    src, dst = image_view(ms4, abi.FORMAT_R8G8B8A8_UNORM, 4), image_view(one, abi.FORMAT_R8G8B8A8_UNORM)
+    run("resolve_rgba8", lambda: r.resolve(src, dst), 5 * one.numel(),
+        "4x MSAA 4096^2 R8G8B8A8_UNORM -> 1x (byte-averaging path)")
+    clr = (0.25, 0.5, 0.75, 1.0)
+    run("clear_rgba8_4x", lambda: r.clear_image(src, clr), ms4.numel(), "clear of 4x MSAA 4096^2 R8G8B8A8_UNORM")
+    del ms4, one
+    m = 2048
+    h4 = torch.randn((4, m, m, 4), device=dev, generator=g).to(torch.float16).view(torch.int16)
+    h1 = torch.empty((m, m, 4), dtype=torch.int16, device=dev)
+    hs, hd = image_view(h4, abi.FORMAT_R16G16B16A16_SFLOAT, 4), image_view(h1, abi.FORMAT_R16G16B16A16_SFLOAT)
+    run("resolve_rgba16f", lambda: r.resolve(hs, hd), 5 * h1.numel() * 2,
+        "4x MSAA 2048^2 R16G16B16A16_SFLOAT -> 1x (averaging blit)")
+    del h4, h1
+    d4 = torch.empty((4, n, n), dtype=torch.float32, device=dev)
+    di = image_view(d4, abi.FORMAT_D32_SFLOAT, 4)
+    run("clear_d32f_4x", lambda: r.clear_image(di, 1.0), d4.numel() * 4, "clear of 4x MSAA 4096^2 D32_SFLOAT")
+    del d4
+    levels, size = [], 8192
+    while True:
+        levels.append(torch.empty((size, size, 4), dtype=torch.uint8, device=dev))
+        if size == 1:
+            break
+        size //= 2
+    levels[0].copy_(torch.randint(0, 256, levels[0].shape, dtype=torch.uint8, device=dev, generator=g))
+    views = [image_view(t, abi.FORMAT_R8G8B8A8_UNORM) for t in levels]
+    mip_bytes = sum(t.numel() for t in levels[:-1]) + sum(t.numel() for t in levels[1:])
+    run("mip_chain_rgba8", lambda: r.generate_mipmaps(views), mip_bytes,
+        "8192^2 R8G8B8A8_UNORM -> 13 levels, one LINEAR swgb_blit per level")
+    del levels, views
+    out["peak"] = {"value": peak, "kind": peak_kind, "unit": "GB/s"}
+    return out
 
 
 def batch_raster_bytes(b, cnt):
@@ -727,6 +794,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-vs-per-draw sample")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint / forward timings")
+    ap.add_argument("--no-blitter", action="store_true", help="skip the clear / resolve / mip-chain timings")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default raster configuration (16x16 bins, hiz on)")
     ap.add_argument("--batch-draws", type=int, default=BATCH_FULL["n_draws"], help="--workload batch: draws")
     ap.add_argument("--batch-tri-max", type=int, default=BATCH_FULL["tri_max"], help="--workload batch: largest draw")

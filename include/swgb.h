@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-#define SWGB_ABI_VERSION 5
+#define SWGB_ABI_VERSION 6
 
 typedef enum swgb_status {
     SWGB_OK = 0,
@@ -63,6 +63,7 @@ typedef enum swgb_status {
 #define SWGB_FORMAT_R32G32B32A32_SFLOAT 109
 #define SWGB_FORMAT_D16_UNORM 124
 #define SWGB_FORMAT_D32_SFLOAT 126
+#define SWGB_FORMAT_S8_UINT 127
 /* VkPrimitiveTopology */
 #define SWGB_TOPOLOGY_TRIANGLE_LIST 3
 #define SWGB_TOPOLOGY_TRIANGLE_STRIP 4
@@ -431,6 +432,67 @@ swgb_status swgb_ctx_get_raster_config(swgb_ctx *ctx, swgb_raster_config *config
 swgb_status swgb_autotune(swgb_ctx *ctx, const swgb_pipeline_state *states, const swgb_draw_args *args, uint32_t n,
                           int batched, swgb_raster_config *best, swgb_raster_config *candidates, double *ms);
 
+/* --- The Blitter steps either side of a draw: clears, multisample resolves
+ * and scaled blits (mip generation is one LINEAR blit per level), for the
+ * attachment and texture formats of the draw path (sw::Blitter,
+ * src/Device/Blitter.hpp:144-147, src/Device/Blitter.cpp).  Enqueued on the
+ * context's stream like draws; images are device memory. ------------------- */
+
+/* One level and layer of an image (a vk::Image subresource): the first sample
+ * plane, its VkFormat, extent, sample count, row pitch (rowPitchBytes) and
+ * sample-plane pitch (slicePitchBytes).  data and pitch_bytes must be
+ * multiples of the texel size. */
+typedef struct swgb_image {
+    void *data;
+    uint32_t format;
+    uint32_t width;
+    uint32_t height;
+    uint32_t samples; /* 1 or 4 */
+    uint64_t pitch_bytes;
+    uint64_t slice_bytes;
+} swgb_image;
+
+/* VkRect2D */
+typedef struct swgb_rect {
+    int32_t x, y;
+    uint32_t width, height;
+} swgb_rect;
+
+/* Blitter::clear (Blitter.cpp:55-168; fastClear :170-300): fills `area` (NULL:
+ * the whole image) of every sample plane of dst.  value is given in
+ * value_format: R32G32B32A32_SFLOAT (VkClearColorValue.float32[4]) for colour
+ * images, D32_SFLOAT (VkClearDepthStencilValue.depth) for D32_SFLOAT and
+ * D16_UNORM images, S8_UINT (VkClearDepthStencilValue.stencil, a uint32) for
+ * S8_UINT stencil planes.  Normalized formats clamp the value to [0, 1]. */
+swgb_status swgb_clear(swgb_ctx *ctx, const void *value, uint32_t value_format, const swgb_image *dst, const swgb_rect *area);
+
+/* VkImageResolve (2D, one layer) */
+typedef struct swgb_resolve_region {
+    int32_t src_x, src_y;
+    int32_t dst_x, dst_y;
+    uint32_t width, height;
+} swgb_resolve_region;
+
+/* Blitter::resolve (Blitter.cpp:2035-2205): averages the 4 samples of src into
+ * the single-sample dst of the same colour format; region NULL = the whole
+ * image.  A whole-image resolve of R8G8B8A8_UNORM / B8G8R8A8_UNORM takes the
+ * reference's byte-averaging fast path, everything else its float blit. */
+swgb_status swgb_resolve(swgb_ctx *ctx, const swgb_image *src, const swgb_image *dst, const swgb_resolve_region *region);
+
+/* VkImageBlit (2D, one layer): two corners {x0, y0, x1, y1} per image; dst
+ * corners in reverse order mirror the copy. */
+typedef struct swgb_blit_region {
+    int32_t src[4];
+    int32_t dst[4];
+} swgb_blit_region;
+
+/* Blitter::blit (Blitter.cpp:1497-1657,1659-1790,1820-1950): scaled copy of a
+ * single-sample colour image box to another, filter SWGB_FILTER_NEAREST or
+ * SWGB_FILTER_LINEAR, with the reference's sRGB conversions when the two
+ * formats differ in encoding or the copy filters.  The dst box must lie in
+ * dst; a src box reaching outside src clamps to its edge. */
+swgb_status swgb_blit(swgb_ctx *ctx, const swgb_image *src, const swgb_image *dst, const swgb_blit_region *region, uint32_t filter);
+
 /* Waits for every draw enqueued so far (Renderer::synchronize). */
 swgb_status swgb_sync(swgb_ctx *ctx);
 
@@ -452,6 +514,7 @@ uint64_t swgb_launch_count(swgb_ctx *ctx);
 #define SWGB_KERNEL_BATCH 3 /* one graph replay of a batch segment (three kernels) */
 #define SWGB_KERNEL_ADJOINT 4
 #define SWGB_KERNEL_BIN_ORDER 5 /* longest-first bin order of a single draw */
+#define SWGB_KERNEL_BLIT 6      /* swgb_clear / swgb_resolve / swgb_blit */
 #define SWGB_KERNEL_KINDS 8
 swgb_status swgb_set_kernel_timing(swgb_ctx *ctx, int enable);
 swgb_status swgb_get_kernel_times(swgb_ctx *ctx, double ms[SWGB_KERNEL_KINDS], uint32_t launches[SWGB_KERNEL_KINDS]);

@@ -15,6 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libswgb_oracle.so")
 SRC = os.path.join(HERE, "swgb_oracle.c")
+SRC_BLIT = os.path.join(HERE, "swgb_oracle_blit.c")
 CFLAGS = ["-O2", "-fPIC", "-shared", "-std=c11", "-fwrapv", "-ffp-contract=off", "-fno-fast-math",
           "-Wall", "-Wextra"]
 
@@ -24,11 +25,11 @@ _lib = None
 def build(force=False):
     os.makedirs(BUILD, exist_ok=True)
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(
-            os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "swgb_oracle.h")),
+            os.path.getmtime(SRC), os.path.getmtime(SRC_BLIT), os.path.getmtime(os.path.join(HERE, "swgb_oracle.h")),
             os.path.getmtime(os.path.join(os.path.dirname(HERE), "include", "swgb.h"))):
         return LIB
     tmp = LIB + ".tmp%d" % os.getpid()
-    subprocess.check_call(["gcc"] + CFLAGS + ["-o", tmp, SRC, "-lm", "-lpthread"])
+    subprocess.check_call(["gcc"] + CFLAGS + ["-o", tmp, SRC, SRC_BLIT, "-lm", "-lpthread"])
     os.replace(tmp, LIB)
     return LIB
 
@@ -68,6 +69,12 @@ def lib():
             f.restype = C.c_float
         L.oracle_transcendental_n.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_size_t]
         L.oracle_transcendental_n.restype = None
+        L.oracle_clear.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(abi.Image), C.POINTER(abi.Rect)]
+        L.oracle_clear.restype = C.c_int
+        L.oracle_resolve.argtypes = [C.POINTER(abi.Image), C.POINTER(abi.Image), C.POINTER(abi.ResolveRegion)]
+        L.oracle_resolve.restype = C.c_int
+        L.oracle_blit.argtypes = [C.POINTER(abi.Image), C.POINTER(abi.Image), C.POINTER(abi.BlitRegion), C.c_uint32]
+        L.oracle_blit.restype = C.c_int
         L.oracle_vertex.argtypes = [C.POINTER(abi.PipelineState), C.POINTER(abi.DrawArgs), C.c_uint32,
                                     C.POINTER(C.c_float), C.POINTER(C.c_int32)]
         L.oracle_vertex.restype = C.c_int
@@ -91,6 +98,47 @@ def transcendental(name, x):
     out = np.empty_like(x)
     lib().oracle_transcendental_n(TRANSCENDENTAL[name], x.ctypes.data, out.ctypes.data, x.size)
     return out
+
+
+def image(arr, format, samples=1):
+    """abi.Image over a C-contiguous numpy array [H, W, ...] or
+    [samples, H, W, ...] (host memory, for the oracle's Blitter)."""
+    from swiftshader_gb300 import abi
+    assert arr.flags["C_CONTIGUOUS"]
+    h, w = (arr.shape[1], arr.shape[2]) if samples > 1 else (arr.shape[0], arr.shape[1])
+    bpp = abi.TEXEL_BYTES[format]
+    return abi.Image(arr.ctypes.data, format, w, h, samples, w * bpp, w * bpp * h)
+
+
+def clear(arr, format, value, samples=1, area=None):
+    """Blitter::clear of a host image in place (value as Renderer.clear_area takes it)."""
+    from swiftshader_gb300 import abi
+    img = image(arr, format, samples)
+    if format == abi.FORMAT_S8_UINT:
+        v, vf = (C.c_uint32 * 4)(int(value), 0, 0, 0), abi.FORMAT_S8_UINT
+    elif format in (abi.FORMAT_D32_SFLOAT, abi.FORMAT_D16_UNORM):
+        v, vf = (C.c_float * 4)(float(value), 0, 0, 0), abi.FORMAT_D32_SFLOAT
+    else:
+        v, vf = (C.c_float * 4)(*[float(x) for x in value]), abi.FORMAT_R32G32B32A32_SFLOAT
+    r = C.byref(abi.Rect(*area)) if area is not None else None
+    st = lib().oracle_clear(v, vf, C.byref(img), r)
+    assert st == 0, st
+
+
+def resolve(src, dst, format, region=None):
+    """Blitter::resolve of a host [4, H, W, C] image into [H', W', C]."""
+    from swiftshader_gb300 import abi
+    r = C.byref(abi.ResolveRegion(*region)) if region is not None else None
+    st = lib().oracle_resolve(C.byref(image(src, format, 4)), C.byref(image(dst, format)), r)
+    assert st == 0, st
+
+
+def blit(src, src_format, dst, dst_format, src_box, dst_box, filter):
+    """Blitter::blit between host images."""
+    from swiftshader_gb300 import abi
+    reg = abi.BlitRegion((C.c_int32 * 4)(*src_box), (C.c_int32 * 4)(*dst_box))
+    st = lib().oracle_blit(C.byref(image(src, src_format)), C.byref(image(dst, dst_format)), C.byref(reg), int(filter))
+    assert st == 0, st
 
 
 def _ptr(a):

@@ -15,7 +15,8 @@ EXPORTS = ["swgb_abi_version", "swgb_last_error", "swgb_ctx_create", "swgb_ctx_d
            "swgb_ctx_set_stream", "swgb_draw", "swgb_draw_batch", "swgb_sync", "swgb_get_counters",
            "swgb_reset_counters", "swgb_launch_count", "swgb_set_kernel_timing", "swgb_get_kernel_times",
            "swgb_draw_noalloc", "swgb_draw_adjoint", "swgb_draw_adjoint_batch", "swgb_plan_batch",
-           "swgb_ctx_set_raster_config", "swgb_ctx_get_raster_config", "swgb_autotune"]
+           "swgb_ctx_set_raster_config", "swgb_ctx_get_raster_config", "swgb_autotune", "swgb_clear",
+           "swgb_resolve", "swgb_blit"]
 
 
 class SwgbError(RuntimeError):
@@ -75,7 +76,13 @@ def load(path=None):
     L.swgb_autotune.argtypes = [C.c_void_p, C.POINTER(abi.PipelineState), C.POINTER(abi.DrawArgs), C.c_uint32, C.c_int,
                                 C.POINTER(abi.RasterConfig), C.POINTER(abi.RasterConfig), C.POINTER(C.c_double)]
     L.swgb_autotune.restype = C.c_int
-    if L.swgb_abi_version() != 5:
+    L.swgb_clear.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(abi.Image), C.POINTER(abi.Rect)]
+    L.swgb_clear.restype = C.c_int
+    L.swgb_resolve.argtypes = [C.c_void_p, C.POINTER(abi.Image), C.POINTER(abi.Image), C.POINTER(abi.ResolveRegion)]
+    L.swgb_resolve.restype = C.c_int
+    L.swgb_blit.argtypes = [C.c_void_p, C.POINTER(abi.Image), C.POINTER(abi.Image), C.POINTER(abi.BlitRegion), C.c_uint32]
+    L.swgb_blit.restype = C.c_int
+    if L.swgb_abi_version() != 6:
         raise OSError("libswgb ABI version mismatch")
     _lib = L
     return L

@@ -28,6 +28,7 @@ FORMAT_R16G16B16A16_SFLOAT = 97
 FORMAT_R32G32_SFLOAT = 103
 FORMAT_R32G32B32A32_SFLOAT = 109
 FORMAT_D32_SFLOAT = 126
+FORMAT_S8_UINT = 127
 TOPOLOGY_TRIANGLE_LIST = 3
 TOPOLOGY_TRIANGLE_STRIP = 4
 TOPOLOGY_TRIANGLE_FAN = 5
@@ -162,3 +163,31 @@ class RasterConfig(C.Structure):
 
 BIN_SHAPES = ((16, 16), (32, 16), (32, 32))
 AUTOTUNE_CANDIDATES = 6
+
+
+class Image(C.Structure):
+    """swgb_image: one level and layer of an image in device memory."""
+    _fields_ = [("data", C.c_void_p), ("format", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("samples", C.c_uint32), ("pitch_bytes", C.c_uint64), ("slice_bytes", C.c_uint64)]
+
+
+class Rect(C.Structure):
+    """swgb_rect (VkRect2D)."""
+    _fields_ = [("x", C.c_int32), ("y", C.c_int32), ("width", C.c_uint32), ("height", C.c_uint32)]
+
+
+class ResolveRegion(C.Structure):
+    """swgb_resolve_region (VkImageResolve, 2D)."""
+    _fields_ = [("src_x", C.c_int32), ("src_y", C.c_int32), ("dst_x", C.c_int32), ("dst_y", C.c_int32),
+                ("width", C.c_uint32), ("height", C.c_uint32)]
+
+
+class BlitRegion(C.Structure):
+    """swgb_blit_region (VkImageBlit, 2D): {x0, y0, x1, y1} per image."""
+    _fields_ = [("src", C.c_int32 * 4), ("dst", C.c_int32 * 4)]
+
+
+# bytes per texel of the formats the Blitter entry points take
+TEXEL_BYTES = {FORMAT_R8G8B8A8_UNORM: 4, FORMAT_R8G8B8A8_SRGB: 4, FORMAT_B8G8R8A8_UNORM: 4, FORMAT_B8G8R8A8_SRGB: 4,
+               FORMAT_R16G16B16A16_SFLOAT: 8, FORMAT_R32G32B32A32_SFLOAT: 16, FORMAT_D32_SFLOAT: 4,
+               FORMAT_D16_UNORM: 2, FORMAT_S8_UINT: 1}

@@ -1,13 +1,14 @@
 """Builds libswgb.so in-tree with nvcc for sm_103a.
 
-Five translation units are compiled in parallel and linked into one library:
-swgb_draw.cu (vertex, setup and adjoint kernels, host side, C-ABI) and
-swgb_raster.cu once per colour format (the raster kernel variants).
+Six translation units are compiled in parallel and linked into one library:
+swgb_draw.cu (vertex, setup and adjoint kernels, host side, C-ABI),
+swgb_blit.cu (clears, resolves, blits) and swgb_raster.cu once per colour
+format (the raster kernel variants).
 
-Every unit is compiled with -ftz=true -prec-div=true -prec-sqrt=true
--fmad=false: subnormals flush like the reference's FTZ/DAZ worker threads,
-divisions are IEEE-rounded, and only the explicit fused multiply-adds of the
-kernels (the reference's MulAdd) are fused.
+Every unit is compiled with -prec-div=true -prec-sqrt=true -fmad=false
+(divisions IEEE-rounded, only the explicit fused multiply-adds of the kernels
+-- the reference's MulAdd -- fused) and, except swgb_blit.cu, -ftz=true:
+subnormals flush like the reference's FTZ/DAZ worker threads.
 """
 import os
 import subprocess
@@ -18,14 +19,17 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libswgb.so")
 # (source, extra defines, object name)
-UNITS = [("swgb_draw.cu", [], "swgb_draw.o")] + [
-    ("swgb_raster.cu", ["-DSWGB_RASTER_CF=%d" % cf], "swgb_raster_cf%d.o" % cf) for cf in range(4)]
-SOURCES = [os.path.join(CSRC, u) for u in ("swgb_draw.cu", "swgb_raster.cu")]
-DEPS = SOURCES + [os.path.join(CSRC, h) for h in ("swgb_kernels.cuh", "swgb_numeric.cuh", "swgb_adjoint.cuh", "swgb.map")] + \
+# The Blitter unit keeps IEEE subnormals (-ftz=false): the reference runs blit
+# routines on its queue thread, which does not set FTZ/DAZ.
+UNITS = [("swgb_draw.cu", ["-ftz=true"], "swgb_draw.o"), ("swgb_blit.cu", ["-ftz=false"], "swgb_blit.o")] + [
+    ("swgb_raster.cu", ["-ftz=true", "-DSWGB_RASTER_CF=%d" % cf], "swgb_raster_cf%d.o" % cf) for cf in range(4)]
+SOURCES = [os.path.join(CSRC, u) for u in ("swgb_draw.cu", "swgb_raster.cu", "swgb_blit.cu")]
+DEPS = SOURCES + [os.path.join(CSRC, h) for h in ("swgb_kernels.cuh", "swgb_numeric.cuh", "swgb_adjoint.cuh", "swgb_blit.h",
+                                                  "swgb.map")] + \
     [os.path.join(ROOT, "include", "swgb.h")]
 
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo", "-O3", "-std=c++17",
-              "-ftz=true", "-prec-div=true", "-prec-sqrt=true", "-fmad=false",
+              "-prec-div=true", "-prec-sqrt=true", "-fmad=false",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-diag-suppress", "177"]
 
 

@@ -41,6 +41,7 @@
 #include <unordered_map>
 #include <vector>
 
+#include "swgb_blit.h"
 #include "swgb_kernels.cuh"
 
 using namespace swgbk;
@@ -1710,6 +1711,211 @@ swgb_status swgb_draw_adjoint_batch(swgb_ctx *ctx, const swgb_pipeline_state *st
     if(n == 0) return SWGB_OK;
     cudaSetDevice(ctx->device);
     return draw_adjoint_batch(ctx, states, args, adjs, n);
+}
+
+// --------------------------------------------------------------------------
+// Blitter: clears, resolves, blits (kernels in swgb_blit.cu)
+// --------------------------------------------------------------------------
+
+namespace {
+
+struct BlitFormat {
+    bool colour;  // a colour format of the Blitter kernels
+    int kind;     // swgbb::BK_*
+    bool srgb;
+    int bytes;
+};
+
+BlitFormat blit_format(uint32_t f)
+{
+    switch(f)
+    {
+    case SWGB_FORMAT_R8G8B8A8_UNORM: return {true, swgbb::BK_RGBA8, false, 4};
+    case SWGB_FORMAT_R8G8B8A8_SRGB: return {true, swgbb::BK_RGBA8, true, 4};
+    case SWGB_FORMAT_B8G8R8A8_UNORM: return {true, swgbb::BK_BGRA8, false, 4};
+    case SWGB_FORMAT_B8G8R8A8_SRGB: return {true, swgbb::BK_BGRA8, true, 4};
+    case SWGB_FORMAT_R16G16B16A16_SFLOAT: return {true, swgbb::BK_RGBA16F, false, 8};
+    case SWGB_FORMAT_R32G32B32A32_SFLOAT: return {true, swgbb::BK_RGBA32F, false, 16};
+    case SWGB_FORMAT_D32_SFLOAT: return {false, -1, false, 4};
+    case SWGB_FORMAT_D16_UNORM: return {false, -1, false, 2};
+    case SWGB_FORMAT_S8_UINT: return {false, -1, false, 1};
+    default: return {false, -1, false, 0};
+    }
+}
+
+constexpr uint32_t MAX_IMAGE_DIM = 16384;  // vk::MAX_IMAGE_LEVELS_2D = 15 levels
+
+swgb_status check_image(const swgb_image *im, const char *what)
+{
+    const BlitFormat f = blit_format(im ? im->format : 0);
+    if(!im || !im->data) return set_error(SWGB_INVALID_ARG, what);
+    if(f.bytes == 0) return set_error(SWGB_UNSUPPORTED_STATE, "blitter: image format");
+    if(im->width == 0 || im->height == 0 || im->width > MAX_IMAGE_DIM || im->height > MAX_IMAGE_DIM)
+        return set_error(SWGB_INVALID_ARG, "blitter: image extent");
+    if(im->samples != 1 && im->samples != 4) return set_error(SWGB_UNSUPPORTED_STATE, "blitter: sample count");
+    const uint64_t b = (uint64_t)f.bytes;
+    if((uintptr_t)im->data % b || im->pitch_bytes % b || im->pitch_bytes < (uint64_t)im->width * b)
+        return set_error(SWGB_INVALID_ARG, "blitter: image base and row pitch must be texel-aligned, pitch >= width");
+    if(im->samples > 1 && (im->slice_bytes % b || im->slice_bytes < im->pitch_bytes * im->height))
+        return set_error(SWGB_INVALID_ARG, "blitter: sample-plane pitch");
+    return SWGB_OK;
+}
+
+}  // namespace
+
+swgb_status swgb_clear(swgb_ctx *ctx, const void *value, uint32_t value_format, const swgb_image *dst, const swgb_rect *area)
+{
+    if(!ctx || !value) return set_error(SWGB_INVALID_ARG, "null argument");
+    swgb_status s;
+    if((s = check_image(dst, "clear: dst")) != SWGB_OK) return s;
+    const BlitFormat f = blit_format(dst->format);
+    const uint32_t need = f.colour ? SWGB_FORMAT_R32G32B32A32_SFLOAT
+                          : dst->format == SWGB_FORMAT_S8_UINT ? SWGB_FORMAT_S8_UINT : SWGB_FORMAT_D32_SFLOAT;
+    if(value_format != need) return set_error(SWGB_INVALID_ARG, "clear: value format does not match the image");
+    swgb_rect a = area ? *area : swgb_rect{0, 0, dst->width, dst->height};
+    if(a.x < 0 || a.y < 0 || (uint64_t)a.x + a.width > dst->width || (uint64_t)a.y + a.height > dst->height)
+        return set_error(SWGB_INVALID_ARG, "clear: area outside the image");
+    if(a.width == 0 || a.height == 0) return SWGB_OK;
+    swgbb::ClearParams C = {};
+    C.dst = (uint8_t *)dst->data;
+    C.pitch = (int64_t)dst->pitch_bytes;
+    C.slice = (int64_t)dst->slice_bytes;
+    C.x = a.x;
+    C.y = a.y;
+    C.rows = (int)a.height;
+    C.planes = (int)dst->samples;
+    C.rowBytes = (int64_t)a.width * f.bytes;
+    C.bpp = f.bytes;
+    C.dstFormat = dst->format;
+    C.dstKind = f.kind;
+    C.dstSRGB = f.srgb;
+    // normalized formats clamp the value (Blitter.cpp:64-85)
+    C.normalized = (f.colour && f.kind != swgbb::BK_RGBA16F && f.kind != swgbb::BK_RGBA32F) || dst->format == SWGB_FORMAT_D16_UNORM;
+    if(value_format == SWGB_FORMAT_S8_UINT)
+        memcpy(&C.stencil, value, 4);
+    else
+        memcpy(C.value, value, value_format == SWGB_FORMAT_D32_SFLOAT ? 4 : 16);
+    cudaSetDevice(ctx->device);
+    cudaError_t e = cudaSuccess;
+    timed_launch(ctx, SWGB_KERNEL_BLIT, [&] { e = swgbb::launch_clear(C, ctx->stream); });
+    return cuda_check(e, "clear launch");
+}
+
+namespace {
+
+// Blitter::blit's setup (Blitter.cpp:1820-1895) of a 2D region, src samples
+// included (a resolve that misses the fast path is a NEAREST blit).
+swgb_status enqueue_blit(swgb_ctx *ctx, const swgb_image *src, const swgb_image *dst, swgb_blit_region r, bool filter)
+{
+    const BlitFormat sf = blit_format(src->format), df = blit_format(dst->format);
+    if(!sf.colour || !df.colour) return set_error(SWGB_UNSUPPORTED_STATE, "blit: colour formats only");
+    if(r.dst[0] > r.dst[2])
+    {
+        std::swap(r.src[0], r.src[2]);
+        std::swap(r.dst[0], r.dst[2]);
+    }
+    if(r.dst[1] > r.dst[3])
+    {
+        std::swap(r.src[1], r.src[3]);
+        std::swap(r.dst[1], r.dst[3]);
+    }
+    if(r.dst[0] < 0 || r.dst[1] < 0 || (uint32_t)r.dst[2] > dst->width || (uint32_t)r.dst[3] > dst->height)
+        return set_error(SWGB_INVALID_ARG, "blit: destination region outside the image");
+    if(r.dst[0] == r.dst[2] || r.dst[1] == r.dst[3]) return SWGB_OK;
+    const float widthRatio = static_cast<float>(r.src[2] - r.src[0]) / static_cast<float>(r.dst[2] - r.dst[0]);
+    const float heightRatio = static_cast<float>(r.src[3] - r.src[1]) / static_cast<float>(r.dst[3] - r.dst[1]);
+    const float x0 = r.src[0] + (0.5f - r.dst[0]) * widthRatio;
+    const float y0 = r.src[1] + (0.5f - r.dst[1]) * heightRatio;
+    swgbb::BlitParams P = {};
+    P.src = (const uint8_t *)src->data;
+    P.dst = (uint8_t *)dst->data;
+    P.sPitch = (int64_t)src->pitch_bytes;
+    P.sSlice = (int64_t)src->slice_bytes;
+    P.dPitch = (int64_t)dst->pitch_bytes;
+    P.srcKind = sf.kind;
+    P.dstKind = df.kind;
+    P.sBytes = sf.bytes;
+    P.dBytes = df.bytes;
+    P.srcSRGB = sf.srgb;
+    P.dstSRGB = df.srgb;
+    P.srcSamples = (int)src->samples;
+    P.filter = filter;
+    P.allowSRGB = filter || src->samples > 1 || sf.srgb != df.srgb;
+    P.clampToEdge = r.src[0] < 0 || r.src[1] < 0 || (uint32_t)r.src[2] > src->width || (uint32_t)r.src[3] > src->height ||
+                    (filter && (x0 < 0.5f || y0 < 0.5f));
+    P.x0 = x0;
+    P.y0 = y0;
+    P.w = widthRatio;
+    P.h = heightRatio;
+    P.x0d = r.dst[0];
+    P.x1d = r.dst[2];
+    P.y0d = r.dst[1];
+    P.y1d = r.dst[3];
+    P.sW = (int)src->width;
+    P.sH = (int)src->height;
+    cudaSetDevice(ctx->device);
+    cudaError_t e = cudaSuccess;
+    timed_launch(ctx, SWGB_KERNEL_BLIT, [&] { e = swgbb::launch_blit(P, ctx->stream); });
+    return cuda_check(e, "blit launch");
+}
+
+}  // namespace
+
+swgb_status swgb_resolve(swgb_ctx *ctx, const swgb_image *src, const swgb_image *dst, const swgb_resolve_region *region)
+{
+    if(!ctx) return set_error(SWGB_INVALID_ARG, "null argument");
+    swgb_status s;
+    if((s = check_image(src, "resolve: src")) != SWGB_OK || (s = check_image(dst, "resolve: dst")) != SWGB_OK) return s;
+    if(src->format != dst->format || !blit_format(src->format).colour)
+        return set_error(SWGB_INVALID_ARG, "resolve: src and dst must have the same colour format");
+    if(src->samples != 4 || dst->samples != 1) return set_error(SWGB_INVALID_ARG, "resolve: 4-sample src into single-sample dst");
+    swgb_resolve_region r = region ? *region : swgb_resolve_region{0, 0, 0, 0, src->width, src->height};
+    if(r.src_x < 0 || r.src_y < 0 || r.dst_x < 0 || r.dst_y < 0 || (uint64_t)r.src_x + r.width > src->width ||
+       (uint64_t)r.src_y + r.height > src->height || (uint64_t)r.dst_x + r.width > dst->width ||
+       (uint64_t)r.dst_y + r.height > dst->height)
+        return set_error(SWGB_INVALID_ARG, "resolve: region outside an image");
+    if(r.width == 0 || r.height == 0) return SWGB_OK;
+    // fastResolve (Blitter.cpp:2079-2205): whole images, R8G8B8A8_UNORM / B8G8R8A8_UNORM
+    const bool whole = r.src_x == 0 && r.src_y == 0 && r.dst_x == 0 && r.dst_y == 0 && r.width == src->width &&
+                       r.height == src->height && src->width == dst->width && src->height == dst->height;
+    if(whole && (src->format == SWGB_FORMAT_R8G8B8A8_UNORM || src->format == SWGB_FORMAT_B8G8R8A8_UNORM))
+    {
+        swgbb::ResolveParams R = {};
+        R.src = (const uint8_t *)src->data;
+        R.dst = (uint8_t *)dst->data;
+        R.sPitch = (int64_t)src->pitch_bytes;
+        R.sSlice = (int64_t)src->slice_bytes;
+        R.dPitch = (int64_t)dst->pitch_bytes;
+        R.width = (int)r.width;
+        R.height = (int)r.height;
+        R.vec16 = (uintptr_t)src->data % 16 == 0 && (uintptr_t)dst->data % 16 == 0 && src->pitch_bytes % 16 == 0 &&
+                  dst->pitch_bytes % 16 == 0 && src->slice_bytes % 16 == 0;
+        cudaSetDevice(ctx->device);
+        cudaError_t e = cudaSuccess;
+        timed_launch(ctx, SWGB_KERNEL_BLIT, [&] { e = swgbb::launch_resolve_bytes(R, ctx->stream); });
+        return cuda_check(e, "resolve launch");
+    }
+    // otherwise a NEAREST blit of the region, which averages the samples (Blitter.cpp:2052-2072)
+    swgb_blit_region b;
+    b.src[0] = r.src_x;
+    b.src[1] = r.src_y;
+    b.src[2] = r.src_x + (int32_t)r.width;
+    b.src[3] = r.src_y + (int32_t)r.height;
+    b.dst[0] = r.dst_x;
+    b.dst[1] = r.dst_y;
+    b.dst[2] = r.dst_x + (int32_t)r.width;
+    b.dst[3] = r.dst_y + (int32_t)r.height;
+    return enqueue_blit(ctx, src, dst, b, false);
+}
+
+swgb_status swgb_blit(swgb_ctx *ctx, const swgb_image *src, const swgb_image *dst, const swgb_blit_region *region, uint32_t filter)
+{
+    if(!ctx || !region) return set_error(SWGB_INVALID_ARG, "null argument");
+    swgb_status s;
+    if((s = check_image(src, "blit: src")) != SWGB_OK || (s = check_image(dst, "blit: dst")) != SWGB_OK) return s;
+    if(src->samples != 1 || dst->samples != 1) return set_error(SWGB_INVALID_ARG, "blit: single-sample images only");
+    if(filter != SWGB_FILTER_NEAREST && filter != SWGB_FILTER_LINEAR) return set_error(SWGB_INVALID_ARG, "blit: filter");
+    return enqueue_blit(ctx, src, dst, *region, filter == SWGB_FILTER_LINEAR);
 }
 
 swgb_status swgb_sync(swgb_ctx *ctx)

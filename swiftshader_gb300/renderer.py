@@ -93,7 +93,44 @@ class Renderer:
     def set_kernel_timing(self, enable):
         check(self._L.swgb_set_kernel_timing(self._ctx, 1 if enable else 0), "swgb_set_kernel_timing")
 
-    KERNEL_NAMES = ("vertex", "setup", "raster", "batch", "adjoint", "bin_order")
+    # --- sw::Blitter steps either side of a draw (swgb_clear / swgb_resolve /
+    # swgb_blit); images are abi.Image views, e.g. from image_view().
+
+    def clear_image(self, image, value):
+        """Blitter::clear of a whole image: value is an RGBA float sequence for
+        colour images, a float depth for D32_SFLOAT / D16_UNORM, an int for
+        S8_UINT stencil planes."""
+        self.clear_area(image, value, None)
+
+    def clear_area(self, image, value, area):
+        """Blitter::clear of area = (x, y, width, height) (None: whole image)."""
+        if image.format == abi.FORMAT_S8_UINT:
+            v, fmt = (C.c_uint32 * 4)(int(value), 0, 0, 0), abi.FORMAT_S8_UINT
+        elif image.format in (abi.FORMAT_D32_SFLOAT, abi.FORMAT_D16_UNORM):
+            v, fmt = (C.c_float * 4)(float(value), 0.0, 0.0, 0.0), abi.FORMAT_D32_SFLOAT
+        else:
+            v, fmt = (C.c_float * 4)(*[float(x) for x in value]), abi.FORMAT_R32G32B32A32_SFLOAT
+        r = C.byref(abi.Rect(*area)) if area is not None else None
+        check(self._L.swgb_clear(self._ctx, v, fmt, C.byref(image), r), "swgb_clear")
+
+    def resolve(self, src, dst, region=None):
+        """Blitter::resolve of a 4-sample image into a single-sample one;
+        region = (src_x, src_y, dst_x, dst_y, width, height) or None (whole)."""
+        r = C.byref(abi.ResolveRegion(*region)) if region is not None else None
+        check(self._L.swgb_resolve(self._ctx, C.byref(src), C.byref(dst), r), "swgb_resolve")
+
+    def blit(self, src, dst, src_box, dst_box, filter=abi.FILTER_LINEAR):
+        """Blitter::blit of src_box = (x0, y0, x1, y1) onto dst_box."""
+        reg = abi.BlitRegion((C.c_int32 * 4)(*src_box), (C.c_int32 * 4)(*dst_box))
+        check(self._L.swgb_blit(self._ctx, C.byref(src), C.byref(dst), C.byref(reg), int(filter)), "swgb_blit")
+
+    def generate_mipmaps(self, levels):
+        """Fills levels[1:] from levels[0] with one LINEAR blit per level, the
+        vkCmdBlitImage sequence applications record for mip generation."""
+        for a, b in zip(levels[:-1], levels[1:]):
+            self.blit(a, b, (0, 0, a.width, a.height), (0, 0, b.width, b.height), abi.FILTER_LINEAR)
+
+    KERNEL_NAMES = ("vertex", "setup", "raster", "batch", "adjoint", "bin_order", "blit")
 
     def kernel_times(self):
         """{kernel: (total ms, launches)} since the last call (synchronises)."""
@@ -210,6 +247,21 @@ class DeviceBatch:
         page, x, y = (int(v) for v in self.batch.place[i])
         s = int(self.batch.sides[i])
         return self.color[page, y:y + s, x:x + s], self.depth[page, y:y + s, x:x + s]
+
+
+def image_view(tensor, format, samples=1):
+    """abi.Image over a contiguous CUDA tensor shaped [H, W, C] (or [H, W] for
+    depth and stencil), or [samples, H, W, ...] for multisampled images."""
+    t = tensor
+    if samples > 1:
+        assert t.shape[0] == samples
+        h, w = t.shape[1], t.shape[2]
+    else:
+        h, w = t.shape[0], t.shape[1]
+    assert t.is_contiguous()
+    bpp = abi.TEXEL_BYTES[format]
+    pitch = w * bpp
+    return abi.Image(t.data_ptr(), format, w, h, samples, pitch, pitch * h)
 
 
 def torch_tensor(values, like):

@@ -24,6 +24,10 @@ STRUCTS = {
     "swgb_adjoint_args": abi.AdjointArgs,
     "swgb_raster_config": abi.RasterConfig,
     "swgb_stencil_op_state": abi.StencilOpState,
+    "swgb_image": abi.Image,
+    "swgb_rect": abi.Rect,
+    "swgb_resolve_region": abi.ResolveRegion,
+    "swgb_blit_region": abi.BlitRegion,
 }
 
 
@@ -72,7 +76,7 @@ def test_library_loads_and_exports_all_symbols(built_lib):
     for name in _lib.EXPORTS:
         assert name in exported, name
     L = _lib.load(built_lib)
-    assert L.swgb_abi_version() == 5
+    assert L.swgb_abi_version() == 6
 
 
 def test_host_side_errors_without_device(built_lib):
@@ -113,6 +117,11 @@ def test_host_side_errors_without_device(built_lib):
     # raster configuration: validated on the host
     assert L.swgb_ctx_set_raster_config(None, None) == abi.INVALID_ARG
     assert L.swgb_autotune(None, None, None, 0, 1, None, None, None) == abi.INVALID_ARG
+    # Blitter entry points: null context / arguments rejected on the host
+    img = abi.Image(None, abi.FORMAT_R8G8B8A8_UNORM, 4, 4, 1, 16, 64)
+    assert L.swgb_clear(None, None, 0, C.byref(img), None) == abi.INVALID_ARG
+    assert L.swgb_resolve(None, C.byref(img), C.byref(img), None) == abi.INVALID_ARG
+    assert L.swgb_blit(None, C.byref(img), C.byref(img), None, 0) == abi.INVALID_ARG
 
 
 def test_header_lists_the_bin_shapes():
