@@ -55,6 +55,8 @@ WORKLOADS = {
     "small": "1000 independent Gouraud triangles, 256x256 RGBA8 + D32F, depth LESS, no blend, no texture",
     "sphere": "adjoint: 20k-triangle uv-sphere, 512^2 RGBA32F, 1024^2 RGBA32F texture (forward + adjoint)",
     "views": "adjoint: views of a 100k-triangle noisy sphere, 512^2 4x MSAA RGBA16F, OVER (forward + adjoint)",
+    "blitter": "Blitter steps: 4x MSAA 4096^2 RGBA8 and 2048^2 RGBA16F resolves, clears of 4x MSAA 4096^2 "
+               "RGBA8 and D32F, 13-level LINEAR mip chain of an 8192^2 RGBA8 texture",
     "batch": "4096 independent draws, triangle counts log-uniform in [16, 65536], uniform clip-space triangles, "
              "square viewports with side uniform in {128,256,384,512} shelf-packed into 16384^2 RGBA8 + D32F "
              "atlas pages, each draw sampling its own 256^2 RGBA8 texture bilinearly, depth LESS, no blend",
@@ -584,6 +586,36 @@ def run_adjoint(args):
     print(json.dumps(line), flush=True)
 
 
+def run_blitter(args):
+    """--workload blitter: the clear / resolve / mip-chain timings alone, as
+    their own line (metric: GB/s of the mip chain, the others beside)."""
+    import torch
+    from swiftshader_gb300 import Renderer
+    world, rank, local = dist_env()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    r = Renderer(local, stream)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    res = measure_blitter(r, stream, flush, dev, steps=args.steps, warmup=args.warmup)
+    clk = clocks.stop()
+    if rank != 0:
+        return
+    mip = res["mip_chain_rgba8"]
+    line = {
+        "metric": "GB/s", "value": mip["achieved_gbs"], "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": mip["ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8 / f16 / f32 texels", "data": "synthetic (seeded generator)",
+        "config": {"workload": WORKLOADS["blitter"], "l2": "flushed before every timed step (256 MiB write)"},
+        "blitter": res, "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_batch(args):
     """--workload batch: the full 4096-draw atlas workload as the headline."""
     import numpy as np
@@ -730,6 +762,9 @@ def run_reference(args):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     oracle.build()
+    if args.workload == "blitter":
+        run_reference_blitter(args, oracle)
+        return
     scene = make_scene(args.workload)
     threads = os.cpu_count() or 1
     if args.workload == "batch":
@@ -757,6 +792,40 @@ def run_reference(args):
                                    "(reference JIT unbuildable here), %s" % platform.machine()},
         "e2e": {"value": round(value, 5), "unit": "Gfrag/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    print(json.dumps(line), flush=True)
+
+
+def run_reference_blitter(args, oracle):
+    """Reference arm of --workload blitter: the oracle's Blitter restatement
+    (one host thread) building the mip chain of a 2048^2 RGBA8 texture, a
+    bounded sample of the 8192^2 chain; GB/s of the same algorithmic bytes."""
+    import numpy as np
+    from swiftshader_gb300 import abi
+    levels, size = [], 2048
+    rng = np.random.default_rng(9)
+    while True:
+        levels.append(np.zeros((size, size, 4), np.uint8))
+        if size == 1:
+            break
+        size //= 2
+    levels[0][:] = rng.integers(0, 256, size=levels[0].shape, dtype=np.uint8)
+    nbytes = sum(a.nbytes for a in levels[:-1]) + sum(a.nbytes for a in levels[1:])
+    times = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        for a, c in zip(levels[:-1], levels[1:]):
+            oracle.blit(a, abi.FORMAT_R8G8B8A8_UNORM, c, abi.FORMAT_R8G8B8A8_UNORM, (0, 0, a.shape[1], a.shape[0]),
+                        (0, 0, c.shape[1], c.shape[0]), abi.FILTER_LINEAR)
+        if i >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    ms = statistics.median(times) * 1e3
+    v = round(nbytes / (ms * 1e-3) / 1e9, 3)
+    sample = "12-level LINEAR mip chain of a 2048^2 RGBA8 texture (bounded sample of the 8192^2 chain)"
+    line = {"impl": "reference", "metric": "GB/s", "value": v, "unit": "GB/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "config": {"workload": WORKLOADS["blitter"]},
+            "cpu_baseline": {"value": v, "unit": "GB/s", "cores": 1, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
@@ -807,6 +876,8 @@ def main():
         run_batch(args)
     elif args.workload in ("sphere", "views"):
         run_adjoint(args)
+    elif args.workload == "blitter":
+        run_blitter(args)
     else:
         run_ours(args)
 

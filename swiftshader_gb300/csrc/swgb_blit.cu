@@ -31,6 +31,7 @@ namespace {
 
 __host__ __device__ constexpr bool kind_unorm8(int k) { return k == BK_RGBA8 || k == BK_BGRA8; }
 __host__ __device__ constexpr bool kind_float(int k) { return k == BK_RGBA16F || k == BK_RGBA32F; }
+__host__ __device__ constexpr int kind_bytes(int k) { return kind_unorm8(k) ? 4 : (k == BK_RGBA16F ? 8 : 16); }
 
 // readFloat4 (Blitter.cpp:312-550): 8-bit formats as their byte values,
 // B8G8R8A8 swizzled to R, G, B, A (.zyxw); half floats through Reactor's
@@ -68,17 +69,21 @@ __device__ __forceinline__ uint32_t pack_unorm8(float c)
     return r < 0 ? 0u : (r > 255 ? 255u : (uint32_t)r);
 }
 
-// write (Blitter.cpp:553-1180), all four components written.
+// The same for a value known to lie in [0, 256): RoundInt in range, the
+// 16-bit saturation a no-op, only the clamp at 255 left.
+__device__ __forceinline__ uint32_t pack_unorm8_bounded(float c) { return (uint32_t)min(__float2int_rn(c), 255); }
+
+// write (Blitter.cpp:553-1180), all four components written.  BOUNDED: the
+// colour came from 8-bit texels (blends and sRGB round trips of values in
+// [0, 255] stay in [0, 256)).
+template<bool BOUNDED = false>
 __device__ __forceinline__ void write_texel(uint8_t *p, int kind, float4 c)
 {
+    auto pk = [](float v) { return BOUNDED ? pack_unorm8_bounded(v) : pack_unorm8(v); };
     switch(kind)
     {
-    case BK_RGBA8:
-        *(uint32_t *)p = pack_unorm8(c.x) | (pack_unorm8(c.y) << 8) | (pack_unorm8(c.z) << 16) | (pack_unorm8(c.w) << 24);
-        break;
-    case BK_BGRA8:
-        *(uint32_t *)p = pack_unorm8(c.z) | (pack_unorm8(c.y) << 8) | (pack_unorm8(c.x) << 16) | (pack_unorm8(c.w) << 24);
-        break;
+    case BK_RGBA8: *(uint32_t *)p = pk(c.x) | (pk(c.y) << 8) | (pk(c.z) << 16) | (pk(c.w) << 24); break;
+    case BK_BGRA8: *(uint32_t *)p = pk(c.z) | (pk(c.y) << 8) | (pk(c.x) << 16) | (pk(c.w) << 24); break;
     case BK_RGBA16F:
         *(uint2 *)p = make_uint2(reactor_float_to_half(c.x) | (reactor_float_to_half(c.y) << 16),
                                  reactor_float_to_half(c.z) | (reactor_float_to_half(c.w) << 16));
@@ -128,14 +133,38 @@ __device__ __forceinline__ float4 scale_and_clamp(float4 v, int srcKind, bool sr
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
+// The bilinear branch of Blitter::sample after its four reads
+// (Blitter.cpp:1625-1653): sRGB texels decoded when allowed, the blend
+// (c00 ix + c01 fx) iy + (c10 ix + c11 fx) fy, then ApplyScaleAndClamp.
+template<int SK, int DK>
+__device__ __forceinline__ float4 bilinear(const BlitParams &P, float4 c00, float4 c01, float4 c10, float4 c11, float fx, float fy)
+{
+    const bool convertSrc = P.allowSRGB && P.srcSRGB;
+    if(convertSrc)
+    {
+        c00 = scale_and_clamp(c00, SK, P.srcSRGB, DK, P.dstSRGB, P.allowSRGB, false);
+        c01 = scale_and_clamp(c01, SK, P.srcSRGB, DK, P.dstSRGB, P.allowSRGB, false);
+        c10 = scale_and_clamp(c10, SK, P.srcSRGB, DK, P.dstSRGB, P.allowSRGB, false);
+        c11 = scale_and_clamp(c11, SK, P.srcSRGB, DK, P.dstSRGB, P.allowSRGB, false);
+    }
+    const float ix = 1.0f - fx, iy = 1.0f - fy;
+    float4 color;
+    color.x = (c00.x * ix + c01.x * fx) * iy + (c10.x * ix + c11.x * fx) * fy;
+    color.y = (c00.y * ix + c01.y * fx) * iy + (c10.y * ix + c11.y * fx) * fy;
+    color.z = (c00.z * ix + c01.z * fx) * iy + (c10.z * ix + c11.z * fx) * fy;
+    color.w = (c00.w * ix + c01.w * fx) * iy + (c10.w * ix + c11.w * fx) * fy;
+    return scale_and_clamp(color, SK, P.srcSRGB, DK, P.dstSRGB, P.allowSRGB, convertSrc);
+}
+
 // Blitter::sample (Blitter.cpp:1497-1657), 2D: nearest texel (its samples
 // averaged for a resolve) or the bilinear blend of four.
-__device__ float4 sample(const BlitParams &P, float x, float y)
+template<int SK, int DK, bool FILTER>
+__device__ __forceinline__ float4 sample(const BlitParams &P, float x, float y)
 {
     const bool convertSrc = P.allowSRGB && P.srcSRGB;
     bool preScaled = false;
     float4 color;
-    if(!P.filter)
+    if(!FILTER)
     {
         int X = trunc_int(x), Y = trunc_int(y);
         if(P.clampToEdge)
@@ -145,21 +174,21 @@ __device__ float4 sample(const BlitParams &P, float x, float y)
         }
         X = clampi(X, 0, P.sW - 1);  // in range already unless the region is malformed
         Y = clampi(Y, 0, P.sH - 1);
-        const uint8_t *s = P.src + (int64_t)Y * P.sPitch + (int64_t)X * P.sBytes;
-        color = read_texel(s, P.srcKind);
+        const uint8_t *s = P.src + (int64_t)Y * P.sPitch + (int64_t)X * kind_bytes(SK);
+        color = read_texel(s, SK);
         if(P.srcSamples > 1)
         {
             if(convertSrc)
             {
-                color = scale_and_clamp(color, P.srcKind, P.srcSRGB, P.dstKind, P.dstSRGB, P.allowSRGB, false);
+                color = scale_and_clamp(color, SK, P.srcSRGB, DK, P.dstSRGB, P.allowSRGB, false);
                 preScaled = true;
             }
             float4 accum = color;
             for(int q = 1; q < P.srcSamples; q++)
             {
                 s += P.sSlice;
-                color = read_texel(s, P.srcKind);
-                if(convertSrc) color = scale_and_clamp(color, P.srcKind, P.srcSRGB, P.dstKind, P.dstSRGB, P.allowSRGB, false);
+                color = read_texel(s, SK);
+                if(convertSrc) color = scale_and_clamp(color, SK, P.srcSRGB, DK, P.dstSRGB, P.allowSRGB, false);
                 accum = make_float4(accum.x + color.x, accum.y + color.y, accum.z + color.z, accum.w + color.w);
             }
             color = mul4(accum, 1.0f / (float)P.srcSamples);
@@ -180,39 +209,72 @@ __device__ float4 sample(const BlitParams &P, float x, float y)
         Y1 = Y1 >= P.sH ? Y0 : Y1;
         const int rx0 = clampi(X0, 0, P.sW - 1), rx1 = clampi(X1, 0, P.sW - 1);
         const int ry0 = clampi(Y0, 0, P.sH - 1), ry1 = clampi(Y1, 0, P.sH - 1);
-        float4 c00 = read_texel(P.src + (int64_t)ry0 * P.sPitch + (int64_t)rx0 * P.sBytes, P.srcKind);
-        float4 c01 = read_texel(P.src + (int64_t)ry0 * P.sPitch + (int64_t)rx1 * P.sBytes, P.srcKind);
-        float4 c10 = read_texel(P.src + (int64_t)ry1 * P.sPitch + (int64_t)rx0 * P.sBytes, P.srcKind);
-        float4 c11 = read_texel(P.src + (int64_t)ry1 * P.sPitch + (int64_t)rx1 * P.sBytes, P.srcKind);
-        if(convertSrc)
-        {
-            c00 = scale_and_clamp(c00, P.srcKind, P.srcSRGB, P.dstKind, P.dstSRGB, P.allowSRGB, false);
-            c01 = scale_and_clamp(c01, P.srcKind, P.srcSRGB, P.dstKind, P.dstSRGB, P.allowSRGB, false);
-            c10 = scale_and_clamp(c10, P.srcKind, P.srcSRGB, P.dstKind, P.dstSRGB, P.allowSRGB, false);
-            c11 = scale_and_clamp(c11, P.srcKind, P.srcSRGB, P.dstKind, P.dstSRGB, P.allowSRGB, false);
-            preScaled = true;
-        }
-        const float fx = x0 - (float)X0, fy = y0 - (float)Y0;
-        const float ix = 1.0f - fx, iy = 1.0f - fy;
-        color.x = (c00.x * ix + c01.x * fx) * iy + (c10.x * ix + c11.x * fx) * fy;
-        color.y = (c00.y * ix + c01.y * fx) * iy + (c10.y * ix + c11.y * fx) * fy;
-        color.z = (c00.z * ix + c01.z * fx) * iy + (c10.z * ix + c11.z * fx) * fy;
-        color.w = (c00.w * ix + c01.w * fx) * iy + (c10.w * ix + c11.w * fx) * fy;
+        const float4 c00 = read_texel(P.src + (int64_t)ry0 * P.sPitch + (int64_t)rx0 * kind_bytes(SK), SK);
+        const float4 c01 = read_texel(P.src + (int64_t)ry0 * P.sPitch + (int64_t)rx1 * kind_bytes(SK), SK);
+        const float4 c10 = read_texel(P.src + (int64_t)ry1 * P.sPitch + (int64_t)rx0 * kind_bytes(SK), SK);
+        const float4 c11 = read_texel(P.src + (int64_t)ry1 * P.sPitch + (int64_t)rx1 * kind_bytes(SK), SK);
+        return bilinear<SK, DK>(P, c00, c01, c10, c11, x0 - (float)X0, y0 - (float)Y0);
     }
-    return scale_and_clamp(color, P.srcKind, P.srcSRGB, P.dstKind, P.dstSRGB, P.allowSRGB, preScaled);
+    return scale_and_clamp(color, SK, P.srcSRGB, DK, P.dstSRGB, P.allowSRGB, preScaled);
 }
 
 // The blit routine's pixel loop (Blitter.cpp:1714-1786): one thread per
-// destination pixel of the box.
+// destination pixel of the box, a warp per 32 pixels of a row; one kernel per
+// (source format, destination format, filter), so the per-texel format
+// switches fold away.
+template<int SK, int DK, bool FILTER>
 __global__ void __launch_bounds__(256) k_blit(BlitParams P)
 {
-    const int i = P.x0d + (int)(blockIdx.x * 16 + (threadIdx.x & 15));
-    const int j = P.y0d + (int)(blockIdx.y * 16 + (threadIdx.x >> 4));
+    const int i = P.x0d + (int)(blockIdx.x * 32 + (threadIdx.x & 31));
+    const int j = P.y0d + (int)(blockIdx.y * 8 + (threadIdx.x >> 5));
     if(i >= P.x1d || j >= P.y1d) return;
     const float x = P.x0 + (float)i * P.w;
     const float y = P.y0 + (float)j * P.h;
-    const float4 c = sample(P, x, y);
-    write_texel(P.dst + (int64_t)j * P.dPitch + (int64_t)i * P.dBytes, P.dstKind, c);
+    const float4 c = sample<SK, DK, FILTER>(P, x, y);
+    write_texel<kind_unorm8(SK)>(P.dst + (int64_t)j * P.dPitch + (int64_t)i * kind_bytes(DK), DK, c);
+}
+
+// A LINEAR blit of src box (0, 0, 2W, 2H) onto dst box (0, 0, W, H) inside
+// both images -- one mip level from the one above.  There the routine's
+// positions are exact: x = 1 + 2i, X0 = 2i, X1 = 2i + 1, fx = fy = 1/2, so the
+// blend above is evaluated on texels 2i, 2i + 1 of rows 2j, 2j + 1.  Each
+// thread makes two destination pixels from a 4 x 2 texel block (one 16-byte
+// load per row for 8-bit texels when the rows are 16-byte aligned).
+template<int SK, int DK>
+__global__ void __launch_bounds__(256) k_blit_half(BlitParams P)
+{
+    const int i0 = 2 * (int)(blockIdx.x * 32 + (threadIdx.x & 31));
+    const int j = (int)(blockIdx.y * 8 + (threadIdx.x >> 5));
+    if(i0 >= P.x1d || j >= P.y1d) return;
+    constexpr int B = kind_bytes(SK);
+    const uint8_t *r0 = P.src + (int64_t)(2 * j) * P.sPitch + (int64_t)(2 * i0) * B;
+    const uint8_t *r1 = r0 + P.sPitch;
+    const bool two = i0 + 1 < P.x1d;
+    float4 a[4], b[4];
+    if(kind_unorm8(SK) && two && P.vec16)
+    {
+        const uint4 u = *(const uint4 *)r0, v = *(const uint4 *)r1;
+        const uint32_t uu[4] = {u.x, u.y, u.z, u.w}, vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for(int k = 0; k < 4; k++)
+        {
+            a[k] = read_texel((const uint8_t *)&uu[k], SK);
+            b[k] = read_texel((const uint8_t *)&vv[k], SK);
+        }
+    }
+    else
+    {
+#pragma unroll
+        for(int k = 0; k < 4; k++)
+            if(k < 2 || two)
+            {
+                a[k] = read_texel(r0 + k * B, SK);
+                b[k] = read_texel(r1 + k * B, SK);
+            }
+    }
+    uint8_t *d = P.dst + (int64_t)j * P.dPitch + (int64_t)i0 * kind_bytes(DK);
+    write_texel<kind_unorm8(SK)>(d, DK, bilinear<SK, DK>(P, a[0], a[1], b[0], b[1], 0.5f, 0.5f));
+    if(two) write_texel<kind_unorm8(SK)>(d + kind_bytes(DK), DK, bilinear<SK, DK>(P, a[2], a[3], b[2], b[3], 0.5f, 0.5f));
 }
 
 // fastResolve (Blitter.cpp:2079-2205): per byte, the rounding-up average of
@@ -309,22 +371,21 @@ __device__ __forceinline__ void clear_row(const ClearParams &C, const uint8_t *t
     uint8_t *base = C.dst + (int64_t)plane * C.slice + (int64_t)(C.y + row) * C.pitch + (int64_t)C.x * C.bpp;
     const uintptr_t b0 = (uintptr_t)base, b1 = b0 + (uintptr_t)C.rowBytes;
     const uintptr_t a0 = (b0 + 15) & ~(uintptr_t)15, a1 = b1 & ~(uintptr_t)15;
-    const int tid = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const uintptr_t tid = threadIdx.x;
     if(a0 >= a1)
     {
         // the row fits between two boundaries: bytewise
-        for(uintptr_t a = b0 + tid; a < b1; a += (uintptr_t)gridDim.x * blockDim.x) *(uint8_t *)a = tex[a & 15];
+        for(uintptr_t a = b0 + tid; a < b1; a += blockDim.x) *(uint8_t *)a = tex[a & 15];
         return;
     }
-    if(blockIdx.x == 0)
-    {
-        if(b0 + threadIdx.x < a0) *(uint8_t *)(b0 + threadIdx.x) = tex[(b0 + threadIdx.x) & 15];
-        if(a1 + threadIdx.x < b1) *(uint8_t *)(a1 + threadIdx.x) = tex[(a1 + threadIdx.x) & 15];
-    }
+    if(b0 + tid < a0) *(uint8_t *)(b0 + tid) = tex[(b0 + tid) & 15];
+    if(a1 + tid < b1) *(uint8_t *)(a1 + tid) = tex[(a1 + tid) & 15];
     const uint4 pat = *(const uint4 *)tex;
-    for(uintptr_t a = a0 + (uintptr_t)tid * 16; a < a1; a += (uintptr_t)gridDim.x * blockDim.x * 16) *(uint4 *)a = pat;
+    for(uintptr_t a = a0 + tid * 16; a < a1; a += (uintptr_t)blockDim.x * 16) *(uint4 *)a = pat;
 }
 
+// One block per run of rows (grid-stride over rows x sample planes), its
+// threads striding each row in 16-byte chunks.
 __global__ void __launch_bounds__(256) k_clear(ClearParams C)
 {
     __shared__ __align__(16) uint8_t tex[16];
@@ -335,7 +396,22 @@ __global__ void __launch_bounds__(256) k_clear(ClearParams C)
         for(int k = 0; k < 16; k++) tex[k] = t[k % C.bpp];
     }
     __syncthreads();
-    for(int ry = (int)blockIdx.y; ry < C.rows * C.planes; ry += (int)gridDim.y) clear_row(C, tex, ry % C.rows, ry / C.rows);
+    for(int ry = (int)blockIdx.x; ry < C.rows * C.planes; ry += (int)gridDim.x) clear_row(C, tex, ry % C.rows, ry / C.rows);
+}
+
+using BlitKernel = void (*)(BlitParams);
+template<int SK, int DK>
+constexpr BlitKernel blit_kernel(bool filter) { return filter ? k_blit<SK, DK, true> : k_blit<SK, DK, false>; }
+template<int SK>
+BlitKernel blit_kernel(int dk, bool filter)
+{
+    switch(dk)
+    {
+    case BK_RGBA8: return blit_kernel<SK, BK_RGBA8>(filter);
+    case BK_BGRA8: return blit_kernel<SK, BK_BGRA8>(filter);
+    case BK_RGBA16F: return blit_kernel<SK, BK_RGBA16F>(filter);
+    default: return blit_kernel<SK, BK_RGBA32F>(filter);
+    }
 }
 
 }  // namespace
@@ -344,7 +420,24 @@ cudaError_t launch_blit(const BlitParams &P, cudaStream_t st)
 {
     const int w = P.x1d - P.x0d, h = P.y1d - P.y0d;
     if(w <= 0 || h <= 0) return cudaSuccess;
-    k_blit<<<dim3((w + 15) / 16, (h + 15) / 16), 256, 0, st>>>(P);
+    const bool f = P.filter != 0;
+    // the exact 2:1 reduction from the origin (mip generation), same format kinds
+    const bool half = f && !P.clampToEdge && P.x0 == 1.0f && P.y0 == 1.0f && P.w == 2.0f && P.h == 2.0f && P.x0d == 0 &&
+                      P.y0d == 0 && 2 * P.x1d <= P.sW && 2 * P.y1d <= P.sH && P.srcKind == P.dstKind;
+    if(half)
+    {
+        BlitKernel k = P.srcKind == BK_RGBA8 ? k_blit_half<BK_RGBA8, BK_RGBA8>
+                       : P.srcKind == BK_BGRA8 ? k_blit_half<BK_BGRA8, BK_BGRA8>
+                       : P.srcKind == BK_RGBA16F ? k_blit_half<BK_RGBA16F, BK_RGBA16F>
+                                                 : k_blit_half<BK_RGBA32F, BK_RGBA32F>;
+        k<<<dim3((w + 63) / 64, (h + 7) / 8), 256, 0, st>>>(P);
+        return cudaGetLastError();
+    }
+    BlitKernel k = P.srcKind == BK_RGBA8     ? blit_kernel<BK_RGBA8>(P.dstKind, f)
+                   : P.srcKind == BK_BGRA8   ? blit_kernel<BK_BGRA8>(P.dstKind, f)
+                   : P.srcKind == BK_RGBA16F ? blit_kernel<BK_RGBA16F>(P.dstKind, f)
+                                             : blit_kernel<BK_RGBA32F>(P.dstKind, f);
+    k<<<dim3((w + 31) / 32, (h + 7) / 8), 256, 0, st>>>(P);
     return cudaGetLastError();
 }
 
@@ -359,9 +452,8 @@ cudaError_t launch_resolve_bytes(const ResolveParams &R, cudaStream_t st)
 cudaError_t launch_clear(const ClearParams &C, cudaStream_t st)
 {
     if(C.rows <= 0 || C.rowBytes <= 0 || C.planes <= 0) return cudaSuccess;
-    const int64_t chunks = C.rowBytes / 16 + 1;
-    const unsigned gx = (unsigned)((chunks + 255) / 256);
-    k_clear<<<dim3(gx, (unsigned)std::min(C.rows * C.planes, 65535)), 256, 0, st>>>(C);
+    // 152 SMs x 8 resident blocks of 256 threads
+    k_clear<<<(unsigned)std::min(C.rows * C.planes, 152 * 8), 256, 0, st>>>(C);
     return cudaGetLastError();
 }
 

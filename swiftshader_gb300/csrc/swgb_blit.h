@@ -27,6 +27,7 @@ struct BlitParams {
     float x0, y0, w, h;
     int x0d, x1d, y0d, y1d;
     int sW, sH;
+    int vec16;  // source base and row pitch 16-byte aligned
 };
 
 // The byte-averaging 4-sample resolve of an 8-bit image.

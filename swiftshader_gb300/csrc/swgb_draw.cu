@@ -1853,6 +1853,7 @@ swgb_status enqueue_blit(swgb_ctx *ctx, const swgb_image *src, const swgb_image 
     P.y1d = r.dst[3];
     P.sW = (int)src->width;
     P.sH = (int)src->height;
+    P.vec16 = (uintptr_t)src->data % 16 == 0 && src->pitch_bytes % 16 == 0;
     cudaSetDevice(ctx->device);
     cudaError_t e = cudaSuccess;
     timed_launch(ctx, SWGB_KERNEL_BLIT, [&] { e = swgbb::launch_blit(P, ctx->stream); });

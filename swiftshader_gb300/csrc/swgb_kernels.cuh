@@ -842,9 +842,9 @@ __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
         }
     }
 
-    // ---- allocate span rows: block scan + one atomic per block ----------
-    __shared__ uint32_t sWarp[SETUP_THREADS / 32];
-    __shared__ unsigned long long sBase;
+    // ---- allocate span rows: warp scan + one atomic per warp -------------
+    // (no block barrier: warps that clip nothing go on to their span rows and
+    // planes while a clipping warp of the block is still busy)
     const uint32_t rows = cand ? (uint32_t)(yMax - yMin) : 0u;
     uint32_t incl = rows * (uint32_t)D.ms;
 #pragma unroll
@@ -853,21 +853,10 @@ __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
         uint32_t u = __shfl_up_sync(0xFFFFFFFFu, incl, o);
         if(lane >= o) incl += u;
     }
-    if(lane == 31) sWarp[warp] = incl;
-    __syncthreads();
-    if(threadIdx.x == 0)
-    {
-        uint32_t tot = 0;
-        for(int w = 0; w < SETUP_THREADS / 32; w++)
-        {
-            uint32_t c = sWarp[w];
-            sWarp[w] = tot;
-            tot += c;
-        }
-        sBase = tot ? atomicAdd(D.spanCount, (unsigned long long)tot) : 0ull;
-    }
-    __syncthreads();
-    const uint64_t off = (uint64_t)sBase + sWarp[warp] + (incl - rows * (uint32_t)D.ms);
+    unsigned long long warpBase = 0ull;
+    if(lane == 31 && incl) warpBase = atomicAdd(D.spanCount, (unsigned long long)incl);
+    warpBase = __shfl_sync(0xFFFFFFFFu, warpBase, 31);
+    const uint64_t off = (uint64_t)warpBase + (incl - rows * (uint32_t)D.ms);
 
     bool stored = false;
     if(cand && D.ms > 1)

@@ -83,12 +83,10 @@ __device__ __forceinline__ float reactor_half_to_float(uint32_t h)
     {
         if(m != 0)
         {
-            while((m & 0x400) == 0)
-            {
-                m <<= 1;
-                e -= 1;
-            }
-            fp32i |= (uint32_t)(((e + (127 - 15) + 1) << 23) | ((m & ~0x400) << 13));
+            // the reference shifts m left until bit 10 is set, decrementing e
+            // per step; s = clz(m) - 21 steps at once
+            const int32_t sh = __clz(m) - 21;
+            fp32i |= (uint32_t)(((127 - 15 + 1 - sh) << 23) | (((m << sh) & 0x3FF) << 13));
         }
     }
     else

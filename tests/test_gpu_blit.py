@@ -129,6 +129,11 @@ BLIT_CASES = [
     (abi.FORMAT_B8G8R8A8_SRGB, abi.FORMAT_R32G32B32A32_SFLOAT, (24, 24), (12, 12), (0, 0, 24, 24), (0, 0, 12, 12), 1),
     (abi.FORMAT_R32G32B32A32_SFLOAT, abi.FORMAT_B8G8R8A8_UNORM, (24, 24), (24, 24), (0, 0, 24, 24), (0, 0, 24, 24), 0),
     (abi.FORMAT_R16G16B16A16_SFLOAT, abi.FORMAT_R8G8B8A8_SRGB, (24, 24), (10, 14), (0, 0, 24, 24), (0, 0, 14, 10), 1),
+    # exact 2:1 reductions from the origin (the mip-level kernel): odd and even widths, every kind
+    (abi.FORMAT_B8G8R8A8_UNORM, abi.FORMAT_B8G8R8A8_UNORM, (48, 66), (24, 33), (0, 0, 66, 48), (0, 0, 33, 24), 1),
+    (abi.FORMAT_R32G32B32A32_SFLOAT, abi.FORMAT_R32G32B32A32_SFLOAT, (32, 34), (16, 17), (0, 0, 34, 32), (0, 0, 17, 16), 1),
+    (abi.FORMAT_R8G8B8A8_UNORM, abi.FORMAT_R8G8B8A8_SRGB, (32, 32), (16, 16), (0, 0, 32, 32), (0, 0, 16, 16), 1),
+    (abi.FORMAT_R8G8B8A8_UNORM, abi.FORMAT_R8G8B8A8_UNORM, (33, 35), (16, 17), (0, 0, 34, 32), (0, 0, 17, 16), 1),
 ]
 
 
