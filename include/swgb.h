@@ -124,6 +124,7 @@ typedef enum swgb_status {
 #define SWGB_ADDRESS_REPEAT 0
 #define SWGB_ADDRESS_MIRRORED_REPEAT 1
 #define SWGB_ADDRESS_CLAMP_TO_EDGE 2
+#define SWGB_ADDRESS_MIRROR_CLAMP_TO_EDGE 4 /* ADDRESSING_MIRRORONCE */
 
 /* The fixed shaders the path runs in place of SPIR-V modules.
  * VS_MVP_PASSTHROUGH: gl_Position = mvp * attribute[0] (OpMatrixTimesVector,

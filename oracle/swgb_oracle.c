@@ -917,6 +917,14 @@ static uint16_t address16(float uw, uint32_t mode)
         convert ^= mirror;
         return (uint16_t)convert;
     }
+    if(mode == SWGB_ADDRESS_MIRROR_CLAMP_TO_EDGE)
+    {
+        /* ADDRESSING_MIRRORONCE: Int4(Abs(u * 2^16)) - 0x8000 (wrapping int32),
+         * PackSigned to int16, + 0x8000 as uint16 */
+        int32_t convert = (int32_t)((uint32_t)trunc_int(fabsf(fmul(uw, 65536.0f))) - 0x8000u);
+        convert = convert < -32768 ? -32768 : (convert > 32767 ? 32767 : convert);
+        return (uint16_t)(convert + 0x8000);
+    }
     return (uint16_t)trunc_int(fmul(uw, 65536.0f)); /* wrap */
 }
 
@@ -1035,6 +1043,8 @@ static void address_float(const OSampler *s, float coord, uint32_t mode, int dim
         coord = fmul(2.0f, fabsf(fsub(coord, rintf(daz(coord)))));
         coord = fminr(coord, one);
     }
+    else if(mode == SWGB_ADDRESS_MIRROR_CLAMP_TO_EDGE)
+        coord = fminr(fabsf(daz(coord)), one);
     else
         coord = frac4(coord);
     coord = fmul(coord, (float)dim);

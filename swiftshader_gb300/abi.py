@@ -47,6 +47,7 @@ BLEND_OP_ADD, BLEND_OP_SUBTRACT, BLEND_OP_REVERSE_SUBTRACT, BLEND_OP_MIN, BLEND_
 FILTER_NEAREST, FILTER_LINEAR = 0, 1
 MIPMAP_MODE_NEAREST, MIPMAP_MODE_LINEAR = 0, 1
 ADDRESS_REPEAT, ADDRESS_MIRRORED_REPEAT, ADDRESS_CLAMP_TO_EDGE = 0, 1, 2
+ADDRESS_MIRROR_CLAMP_TO_EDGE = 4
 VS_MVP_PASSTHROUGH = 1
 FS_VCOLOR = 1
 FS_TEX_X_VCOLOR = 2

@@ -359,7 +359,10 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
         else return set_error(SWGB_UNSUPPORTED_STATE, "texture format");
         if(t.level_count < 1 || t.level_count > SWGB_MAX_MIP_LEVELS) return set_error(SWGB_INVALID_ARG, "texture level_count");
         if(t.mag_filter != t.min_filter) return set_error(SWGB_UNSUPPORTED_STATE, "mixed min/mag filters");
-        if(t.address_u > SWGB_ADDRESS_CLAMP_TO_EDGE || t.address_v > SWGB_ADDRESS_CLAMP_TO_EDGE) return set_error(SWGB_UNSUPPORTED_STATE, "address mode");
+        // REPEAT, MIRRORED_REPEAT, CLAMP_TO_EDGE, MIRROR_CLAMP_TO_EDGE (CLAMP_TO_BORDER is not implemented)
+        if(t.address_u > SWGB_ADDRESS_MIRROR_CLAMP_TO_EDGE || t.address_v > SWGB_ADDRESS_MIRROR_CLAMP_TO_EDGE ||
+           t.address_u == 3 || t.address_v == 3)
+            return set_error(SWGB_UNSUPPORTED_STATE, "address mode");
         D.levelCount = (int)t.level_count;
         for(uint32_t i = 0; i < t.level_count; i++)
         {
@@ -1124,7 +1127,10 @@ swgb_status bake_adjoint(const swgb_pipeline_state *st, const swgb_draw_args *a,
     if(D.depth16) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint needs a D32_SFLOAT depth attachment");
     if(D.depthBounds) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint: depth bounds test is not supported");
     if(D.stencilTest) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint: stencil test is not supported");
+    if(D.depthBias) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint: depth bias is not supported");
     if(D.fs == SWGB_FS_TEX_X_VCOLOR && !D.texFloat) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint needs a float texture");
+    if(D.fs == SWGB_FS_TEX_X_VCOLOR && (D.addrU == SWGB_ADDRESS_MIRROR_CLAMP_TO_EDGE || D.addrV == SWGB_ADDRESS_MIRROR_CLAMP_TO_EDGE))
+        return set_error(SWGB_UNSUPPORTED_STATE, "adjoint: MIRROR_CLAMP_TO_EDGE addressing is not supported");
     if(D.writeMask != 0xFu) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint needs color_write_mask 0xF");
     if(a->count > ADJ_TRI_MASK) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint: too many triangles");
     int over = 0;

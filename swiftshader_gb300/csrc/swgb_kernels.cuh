@@ -1088,11 +1088,16 @@ __global__ void __launch_bounds__(BIN_ORDER_THREADS) k_bin_order(const __grid_co
 // SamplerCore 16-bit path for R8G8B8A8_UNORM (src/Pipeline/SamplerCore.cpp)
 // ------------------------------------------------------------------------
 
-// address() 16-bit (SamplerCore.cpp:2399-2435)
+// address() 16-bit (SamplerCore.cpp:2399-2435).  MIRROR_CLAMP_TO_EDGE
+// (ADDRESSING_MIRRORONCE: Int4(Abs(u * 2^16)) - 0x8000, saturated to int16,
+// + 0x8000) equals CLAMP_TO_EDGE of |u| -- min(trunc(|u| 2^16), 0xFFFF) both
+// ways -- except for NaN, which it maps to 0xFFFF (the conversion gives
+// 0x80000000, the subtraction wraps it positive): NaN is taken as 1.
 __device__ __forceinline__ uint32_t address16(float uw, uint32_t mode)
 {
-    if(mode == SWGB_ADDRESS_CLAMP_TO_EDGE)
+    if(mode == SWGB_ADDRESS_CLAMP_TO_EDGE || mode == SWGB_ADDRESS_MIRROR_CLAMP_TO_EDGE)
     {
+        if(mode == SWGB_ADDRESS_MIRROR_CLAMP_TO_EDGE) uw = uw == uw ? fabsf(uw) : 1.0f;
         float c = rmin(rmax(uw, 0.0f), 65535.0f / 65536.0f);
         return (uint32_t)trunc_int(c * 65536.0f) & 0xFFFFu;
     }
@@ -1269,6 +1274,8 @@ __device__ __forceinline__ void address_float(const DrawParams &D, float coord, 
         coord = 2.0f * fabsf(coord - rintf(coord));
         coord = rmin(coord, one);
     }
+    else if(mode == SWGB_ADDRESS_MIRROR_CLAMP_TO_EDGE)
+        coord = rmin(fabsf(coord), one);
     else
         coord = rmin(coord - floorf(coord), one);  // Float4 Frac (LLVMReactor.cpp:3252-3275)
     coord = coord * (float)dim;

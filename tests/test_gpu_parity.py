@@ -50,9 +50,12 @@ def test_small_untextured_shapes(gpu_lib, n, w, h, seed):
     (False, abi.ADDRESS_REPEAT, False),
     (True, abi.ADDRESS_MIRRORED_REPEAT, False),
     (False, abi.ADDRESS_CLAMP_TO_EDGE, True),
+    (True, abi.ADDRESS_MIRROR_CLAMP_TO_EDGE, True),
+    (False, abi.ADDRESS_MIRROR_CLAMP_TO_EDGE, False),
 ])
 def test_textured_small(gpu_lib, mip, address, blend):
-    """16-bit UNORM8 filtering: trilinear / bilinear, REPEAT / CLAMP / MIRROR, blend on / off."""
+    """16-bit UNORM8 filtering: trilinear / bilinear, REPEAT / CLAMP / MIRROR /
+    MIRROR_CLAMP_TO_EDGE, blend on / off."""
     s = scenes.scene_textured_small(mip=mip, address=address, blend=blend)
     check_scene(s, gpu_lib)
 
@@ -172,6 +175,17 @@ def _float_variant(tex_fmt, color_fmt, blend, address, mip, seed=31):
     return s
 
 
+def test_mirror_clamp_nan_coordinates(gpu_lib):
+    """MIRROR_CLAMP_TO_EDGE maps a NaN coordinate to the last texel, as
+    ADDRESSING_MIRRORONCE's integer arithmetic does; some vertices carry NaN
+    texture coordinates."""
+    s = scenes.scene_textured_small(n_tris=120, width=64, height=48, mip=False, address=abi.ADDRESS_MIRROR_CLAMP_TO_EDGE,
+                                    seed_index=67)
+    s.vertices[::7, 8] = np.nan
+    s.vertices[3::11, 9] = np.nan
+    check_scene(s, gpu_lib)
+
+
 @pytest.mark.parametrize("tex_fmt,color_fmt,blend,address,mip", [
     (abi.FORMAT_R32G32B32A32_SFLOAT, abi.FORMAT_R32G32B32A32_SFLOAT, False, abi.ADDRESS_CLAMP_TO_EDGE, False),
     (abi.FORMAT_R32G32B32A32_SFLOAT, abi.FORMAT_R32G32B32A32_SFLOAT, True, abi.ADDRESS_REPEAT, True),
@@ -179,6 +193,8 @@ def _float_variant(tex_fmt, color_fmt, blend, address, mip, seed=31):
     (abi.FORMAT_R16G16B16A16_SFLOAT, abi.FORMAT_R32G32B32A32_SFLOAT, False, abi.ADDRESS_MIRRORED_REPEAT, True),
     (abi.FORMAT_R32G32B32A32_SFLOAT, abi.FORMAT_R8G8B8A8_UNORM, True, abi.ADDRESS_CLAMP_TO_EDGE, True),
     (abi.FORMAT_R8G8B8A8_UNORM, abi.FORMAT_R16G16B16A16_SFLOAT, True, abi.ADDRESS_REPEAT, True),
+    (abi.FORMAT_R32G32B32A32_SFLOAT, abi.FORMAT_R32G32B32A32_SFLOAT, True, abi.ADDRESS_MIRROR_CLAMP_TO_EDGE, True),
+    (abi.FORMAT_R16G16B16A16_SFLOAT, abi.FORMAT_R16G16B16A16_SFLOAT, False, abi.ADDRESS_MIRROR_CLAMP_TO_EDGE, False),
 ])
 def test_float_texture_and_attachment_formats(gpu_lib, tex_fmt, color_fmt, blend, address, mip):
     """fp32 SamplerCore path (RGBA16F / RGBA32F textures) and float colour

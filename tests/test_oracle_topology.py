@@ -172,3 +172,32 @@ def test_stencil_counts_fragments(oracle_mod):
     s.stencil = {"front": op, "back": op, "clear": 0}
     _, _, st, cnt = oracle_mod.render_stencil(s)
     assert int(st.astype(np.int64).sum()) == cnt["fragments_passed"] > 1000
+
+
+def test_mirror_clamp_to_edge_is_clamp_of_abs(oracle_mod):
+    """MIRROR_CLAMP_TO_EDGE (ADDRESSING_MIRRORONCE, SamplerCore.cpp:2418-2428,
+    2554-2558) addresses |u| with CLAMP_TO_EDGE's result: a draw whose texture
+    coordinates are negated renders under MIRROR_CLAMP_TO_EDGE exactly what
+    the original renders under CLAMP_TO_EDGE (negation is exact through the
+    plane equations and the interpolation), on the 16-bit and fp32 paths."""
+    from swiftshader_gb300 import abi, scenes
+    for fmt in (abi.FORMAT_R8G8B8A8_UNORM, abi.FORMAT_R32G32B32A32_SFLOAT):
+        a = scenes.scene_textured_small(n_tris=60, width=48, height=40, mip=True, address=abi.ADDRESS_CLAMP_TO_EDGE,
+                                        seed_index=66)
+        if fmt != abi.FORMAT_R8G8B8A8_UNORM:
+            a.texture_format = fmt
+            a.texture_levels = [lv.astype(np.float32) / 255.0 for lv in a.texture_levels]
+        b = scenes.scene_textured_small(n_tris=60, width=48, height=40, mip=True, address=abi.ADDRESS_MIRROR_CLAMP_TO_EDGE,
+                                        seed_index=66)
+        b.texture_format, b.texture_levels = a.texture_format, a.texture_levels
+        a.vertices[:, 8:10] = np.abs(a.vertices[:, 8:10])  # u, v >= 0: CLAMP_TO_EDGE of u is that of |-u|
+        b.vertices = a.vertices.copy()
+        b.vertices[:, 8:10] = -b.vertices[:, 8:10]
+        ca, da, _ = oracle_mod.render(a)
+        cb, db, _ = oracle_mod.render(b)
+        assert np.array_equal(da, db)
+        assert np.array_equal(ca, cb)
+        # and it differs from plain CLAMP_TO_EDGE of the negated coordinates
+        b.sampler = dict(b.sampler, address_u=abi.ADDRESS_CLAMP_TO_EDGE, address_v=abi.ADDRESS_CLAMP_TO_EDGE)
+        cc, _, _ = oracle_mod.render(b)
+        assert not np.array_equal(cc, ca)
