@@ -411,11 +411,14 @@ const RasterKernel &raster_kernel(int v)
 
 // Raster kernel index of a draw: its bin shape, colour format and samples.
 // Draws with D16_UNORM depth, depth bias, the depth bounds test, the stencil
-// test or an sRGB colour attachment run the kernels that carry the full
-// per-sample pipeline.
+// test, an sRGB colour attachment or an 8-bit texture addressed
+// MIRROR_CLAMP_TO_EDGE run the kernels that carry the full per-sample
+// pipeline.
 inline bool full_pipeline(const DrawParams &D)
 {
-    return D.depth16 || D.depthBias || D.depthBounds || D.stencilTest || D.colorSRGB;
+    const bool mirrorOnce16 = D.fs == SWGB_FS_TEX_X_VCOLOR && !D.texFloat &&
+                              (D.addrU == SWGB_ADDRESS_MIRROR_CLAMP_TO_EDGE || D.addrV == SWGB_ADDRESS_MIRROR_CLAMP_TO_EDGE);
+    return D.depth16 || D.depthBias || D.depthBounds || D.stencilTest || D.colorSRGB || mirrorOnce16;
 }
 inline int raster_variant(const DrawParams &D) { return raster_index(shape_index(D.binW, D.binH), D.hiz != 0, D.ms, D.cf, full_pipeline(D)); }
 

@@ -1092,12 +1092,14 @@ __global__ void __launch_bounds__(BIN_ORDER_THREADS) k_bin_order(const __grid_co
 // (ADDRESSING_MIRRORONCE: Int4(Abs(u * 2^16)) - 0x8000, saturated to int16,
 // + 0x8000) equals CLAMP_TO_EDGE of |u| -- min(trunc(|u| 2^16), 0xFFFF) both
 // ways -- except for NaN, which it maps to 0xFFFF (the conversion gives
-// 0x80000000, the subtraction wraps it positive): NaN is taken as 1.
+// 0x80000000, the subtraction wraps it positive): NaN is taken as 1.  Only
+// the full-pipeline raster variants (MIRROR_ONCE) carry that mode.
+template<bool MIRROR_ONCE>
 __device__ __forceinline__ uint32_t address16(float uw, uint32_t mode)
 {
-    if(mode == SWGB_ADDRESS_CLAMP_TO_EDGE || mode == SWGB_ADDRESS_MIRROR_CLAMP_TO_EDGE)
+    if(mode == SWGB_ADDRESS_CLAMP_TO_EDGE || (MIRROR_ONCE && mode == SWGB_ADDRESS_MIRROR_CLAMP_TO_EDGE))
     {
-        if(mode == SWGB_ADDRESS_MIRROR_CLAMP_TO_EDGE) uw = uw == uw ? fabsf(uw) : 1.0f;
+        if(MIRROR_ONCE && mode == SWGB_ADDRESS_MIRROR_CLAMP_TO_EDGE) uw = uw == uw ? fabsf(uw) : 1.0f;
         float c = rmin(rmax(uw, 0.0f), 65535.0f / 65536.0f);
         return (uint32_t)trunc_int(c * 65536.0f) & 0xFFFFu;
     }
@@ -1169,6 +1171,7 @@ __device__ __forceinline__ uint32_t texel_rgba8(const TexLevel &lv, uint32_t u, 
 }
 
 // sampleQuad2D for one lane, 16-bit channel values c << 8 (SamplerCore.cpp:668-909).
+template<bool MIRROR_ONCE>
 __device__ __forceinline__ void sample_quad_2d(const DrawParams &D, float u, float v, float lod, int second, uint32_t out[4], uint32_t &lvMask)
 {
     int ilod = D.mipLinear ? trunc_int(lod) : round_int(lod);  // selectMipmap (:2357-2379)
@@ -1176,8 +1179,8 @@ __device__ __forceinline__ void sample_quad_2d(const DrawParams &D, float u, flo
     li = li < 0 ? 0 : (li > D.levelCount - 1 ? D.levelCount - 1 : li);
     lvMask |= 1u << li;
     const TexLevel &lv = D.lv[li];
-    uint32_t uu = address16(u, D.addrU);
-    uint32_t vv = address16(v, D.addrV);
+    uint32_t uu = address16<MIRROR_ONCE>(u, D.addrU);
+    uint32_t vv = address16<MIRROR_ONCE>(v, D.addrV);
     if(!D.texLinear)
     {
         texel_components(D, __byte_perm(texel_rgba8(lv, uu, vv), 0u, texel_order(D)), out);
@@ -1233,6 +1236,7 @@ __device__ __forceinline__ float implicit_lod(const DrawParams &D, const float u
 
 // sampleTexture128 on the 16-bit path (SamplerCore.cpp:59-253) for lane 'lane'
 // of a quad; the result is scaled by 1 / 0xFF00 (getComponentScale).
+template<bool MIRROR_ONCE>
 __device__ __forceinline__ void sample_texture_lane(const DrawParams &D, float lod, float ul, float vl, float out[4],
                                                     uint32_t &lvMask)
 {
@@ -1242,7 +1246,7 @@ __device__ __forceinline__ void sample_texture_lane(const DrawParams &D, float l
     for(int second = 0; second < levels; second++)
     {
         uint32_t t[4];
-        sample_quad_2d(D, ul, vl, lod, second, t, lvMask);
+        sample_quad_2d<MIRROR_ONCE>(D, ul, vl, lod, second, t, lvMask);
 #pragma unroll
         for(int k = 0; k < 4; k++)
         {
@@ -1734,7 +1738,7 @@ __device__ __forceinline__ void shade_pixel(const DrawParams &D, const SH &S, in
         const float vl = i == 0 ? v[0] : (i == 1 ? v[1] : (i == 2 ? v[2] : v[3]));
         float t[4];
         if(D.texFloat) sample_float_lane(D, lod, ul, vl, t, lvMask);
-        else sample_texture_lane(D, lod, ul, vl, t, lvMask);
+        else sample_texture_lane<SH::kFull>(D, lod, ul, vl, t, lvMask);
 #pragma unroll
         for(int k = 0; k < 4; k++) c[k] = t[k] * c[k];
     }

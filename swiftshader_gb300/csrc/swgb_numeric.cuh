@@ -75,23 +75,15 @@ __device__ __forceinline__ float half_bits_to_float(uint32_t h)
 
 // Reactor's Float(Half) (src/Reactor/Reactor.cpp:3787-3815), used when the
 // blend reads an R16G16B16A16_SFLOAT attachment (a half inf/NaN reads as 65536+).
+// For a nonzero exponent the reference builds ((e + 112) << 23) | (m << 13),
+// which is the half's low 15 bits shifted by 13 plus 112 << 23 (exponent 31
+// included: it stays finite); for a zero exponent it normalises m, giving the
+// exact value m * 2^-24, a normal float (zero for m = 0).
 __device__ __forceinline__ float reactor_half_to_float(uint32_t h)
 {
-    int32_t e = (int32_t)((h >> 10) & 0x1Fu), m = (int32_t)(h & 0x3FFu);
-    uint32_t fp32i = ((h >> 15) & 1u) << 31;
-    if(e == 0)
-    {
-        if(m != 0)
-        {
-            // the reference shifts m left until bit 10 is set, decrementing e
-            // per step; s = clz(m) - 21 steps at once
-            const int32_t sh = __clz(m) - 21;
-            fp32i |= (uint32_t)(((127 - 15 + 1 - sh) << 23) | (((m << sh) & 0x3FF) << 13));
-        }
-    }
-    else
-        fp32i |= (uint32_t)(((e + (127 - 15)) << 23) | (m << 13));
-    return __uint_as_float(fp32i);
+    const uint32_t em = h & 0x7FFFu, sgn = (h & 0x8000u) << 16;
+    const uint32_t mag = em >= 0x400u ? (em << 13) + (112u << 23) : __float_as_uint((float)em * 5.9604644775390625e-8f);
+    return __uint_as_float(sgn | mag);
 }
 
 // Reactor's Half(Float) (src/Reactor/Reactor.cpp:3744-3770), used by

@@ -25,7 +25,15 @@ def host_image(rng, fmt, h, w, samples=1, denormals=False):
             a.reshape(-1)[::7] = np.float32(1e-39) * rng.integers(1, 100, size=a.reshape(-1)[::7].shape)
         return a
     if fmt == abi.FORMAT_R16G16B16A16_SFLOAT:
-        return rng.uniform(-0.25, 1.5, size=shape).astype(np.float16).view(np.uint16)
+        a = rng.uniform(-0.25, 1.5, size=shape).astype(np.float16).view(np.uint16)
+        if denormals:
+            # half subnormals, zeros of both signs, infinities and NaNs (Reactor
+            # reads exponent 31 as finite 65536+)
+            flat = a.reshape(-1)
+            flat[::5] = rng.integers(1, 0x400, size=flat[::5].shape) | (rng.integers(0, 2, size=flat[::5].shape) << 15)
+            flat[3::41] = rng.choice(np.array([0x0000, 0x8000, 0x7C00, 0xFC00, 0x7E00, 0x7C01], np.uint16),
+                                     size=flat[3::41].shape)
+        return a
     return rng.integers(0, np.iinfo(dt).max + 1, size=shape, dtype=np.int64).astype(dt)
 
 
