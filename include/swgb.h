@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-#define SWGB_ABI_VERSION 6
+#define SWGB_ABI_VERSION 7
 
 typedef enum swgb_status {
     SWGB_OK = 0,
@@ -124,7 +124,13 @@ typedef enum swgb_status {
 #define SWGB_ADDRESS_REPEAT 0
 #define SWGB_ADDRESS_MIRRORED_REPEAT 1
 #define SWGB_ADDRESS_CLAMP_TO_EDGE 2
+#define SWGB_ADDRESS_CLAMP_TO_BORDER 3
 #define SWGB_ADDRESS_MIRROR_CLAMP_TO_EDGE 4 /* ADDRESSING_MIRRORONCE */
+/* VkBorderColor (the float ones; the integer ones belong to integer formats) */
+#define SWGB_BORDER_COLOR_FLOAT_TRANSPARENT_BLACK 0
+#define SWGB_BORDER_COLOR_FLOAT_OPAQUE_BLACK 2
+#define SWGB_BORDER_COLOR_FLOAT_OPAQUE_WHITE 4
+#define SWGB_BORDER_COLOR_FLOAT_CUSTOM_EXT 1000287003u
 
 /* The fixed shaders the path runs in place of SPIR-V modules.
  * VS_MVP_PASSTHROUGH: gl_Position = mvp * attribute[0] (OpMatrixTimesVector,
@@ -178,6 +184,8 @@ typedef struct swgb_texture {
     uint32_t mag_filter, min_filter, mipmap_mode;
     uint32_t address_u, address_v;
     float mip_lod_bias, min_lod, max_lod;
+    uint32_t border_color;          /* SWGB_BORDER_COLOR_*: texels outside a CLAMP_TO_BORDER axis */
+    float custom_border_color[4];   /* VkSamplerCustomBorderColorCreateInfoEXT.float32 */
 } swgb_texture;
 
 /* VkStencilOpState */

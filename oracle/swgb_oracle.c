@@ -1045,9 +1045,30 @@ static void address_float(const OSampler *s, float coord, uint32_t mode, int dim
     }
     else if(mode == SWGB_ADDRESS_MIRROR_CLAMP_TO_EDGE)
         coord = fminr(fabsf(daz(coord)), one);
-    else
+    else if(mode != SWGB_ADDRESS_CLAMP_TO_BORDER) /* ADDRESSING_BORDER: unmapped */
         coord = frac4(coord);
     coord = fmul(coord, (float)dim);
+    if(mode == SWGB_ADDRESS_CLAMP_TO_BORDER)
+    {
+        /* point: Int4(Floor(coord)); linear: floor of coord - 0.5; then any
+         * coordinate outside [0, dim) becomes -1 (SamplerCore.cpp:2568-2612) */
+        if(!s->linearFilter)
+        {
+            *x0 = trunc_int(floorf(daz(coord)));
+            *f = 0.0f;
+        }
+        else
+        {
+            coord = fsub(coord, 0.5f);
+            float fl = floorf(daz(coord));
+            *x0 = trunc_int(fl);
+            *f = fsub(coord, fl);
+        }
+        *x1 = *x0 + 1;
+        if(*x0 < 0 || *x0 >= dim) *x0 = -1;
+        if(*x1 < 0 || *x1 >= dim) *x1 = -1;
+        return;
+    }
     if(!s->linearFilter)
     {
         *x0 = trunc_int(coord);
@@ -1074,12 +1095,48 @@ static void address_float(const OSampler *s, float coord, uint32_t mode, int dim
 
 static void texel_float(const swgb_texture *t, const swgb_texture_level *lv, int32_t index, float out[4])
 {
+    if(is_tex8(t->format))
+    {
+        /* an 8-bit texture on the 32-bit path (border addressing): the 16-bit
+         * sampleTexel's components as floats (SamplerCore.cpp:2215-2245) */
+        const uint8_t *p = (const uint8_t *)lv->buffer + (size_t)(uint32_t)index * 4;
+        const int bgra = t->format == SWGB_FORMAT_B8G8R8A8_UNORM || t->format == SWGB_FORMAT_B8G8R8A8_SRGB;
+        const int srgb = t->format == SWGB_FORMAT_R8G8B8A8_SRGB || t->format == SWGB_FORMAT_B8G8R8A8_SRGB;
+        for(int c = 0; c < 4; c++)
+        {
+            const uint8_t b = p[bgra ? bgra_byte(c) : c];
+            out[c] = (float)((srgb && c < 3) ? srgb_lut[b] : (uint16_t)(b << 8));
+        }
+        return;
+    }
     if(t->format == SWGB_FORMAT_R32G32B32A32_SFLOAT)
         memcpy(out, (const uint8_t *)lv->buffer + (size_t)(uint32_t)index * 16, 16);
     else
     {
         const uint16_t *p = (const uint16_t *)((const uint8_t *)lv->buffer + (size_t)(uint32_t)index * 8);
         for(int c = 0; c < 4; c++) out[c] = half_bits_to_float(p[c]);
+    }
+}
+
+/* sampleTexel of the 32-bit path (SamplerCore.cpp:2093-2110,1645-1677,
+ * 2290-2355): with border addressing, a texel whose coordinate is -1 (u, or
+ * v times the pitch, negative) is read at index 0 and replaced by the border
+ * colour, given in the path's units (scaled by getComponentScale()). */
+static void border_texel(const OSampler *s, const swgb_texture_level *lv, int32_t x, int32_t ypitch, float out[4])
+{
+    const int border = s->t->address_u == SWGB_ADDRESS_CLAMP_TO_BORDER || s->t->address_v == SWGB_ADDRESS_CLAMP_TO_BORDER;
+    const int valid = !border || (x | ypitch) >= 0;
+    texel_float(s->t, lv, valid ? x + ypitch : 0, out);
+    if(valid) return;
+    const float sc = is_tex8(s->t->format) ? 65280.0f : 1.0f;
+    switch(s->t->border_color)
+    {
+    case SWGB_BORDER_COLOR_FLOAT_OPAQUE_BLACK: out[0] = out[1] = out[2] = 0.0f; out[3] = sc; break;
+    case SWGB_BORDER_COLOR_FLOAT_OPAQUE_WHITE: out[0] = out[1] = out[2] = out[3] = sc; break;
+    case SWGB_BORDER_COLOR_FLOAT_CUSTOM_EXT:
+        for(int c = 0; c < 4; c++) out[c] = sc * s->t->custom_border_color[c];
+        break;
+    default: out[0] = out[1] = out[2] = out[3] = 0.0f; break;
     }
 }
 
@@ -1095,17 +1152,17 @@ static void sample_float_2d(const OSampler *s, float u, float v, float lod, int 
     address_float(s, v, s->t->address_v, (int)lv->height, &y0, &y1, &fv);
     int32_t pitch = (int32_t)lv->pitch_texels;
     y0 *= pitch;
-    if(!s->linearFilter)
-    {
-        texel_float(s->t, lv, x0 + y0, out);
-        return;
-    }
     y1 *= pitch;
     float c00[4], c10[4], c01[4], c11[4];
-    texel_float(s->t, lv, x0 + y0, c00);
-    texel_float(s->t, lv, x1 + y0, c10);
-    texel_float(s->t, lv, x0 + y1, c01);
-    texel_float(s->t, lv, x1 + y1, c11);
+    if(!s->linearFilter)
+    {
+        border_texel(s, lv, x0, y0, out);
+        return;
+    }
+    border_texel(s, lv, x0, y0, c00);
+    border_texel(s, lv, x1, y0, c10);
+    border_texel(s, lv, x0, y1, c01);
+    border_texel(s, lv, x1, y1, c11);
     for(int c = 0; c < 4; c++)
     {
         float a = fadd(c00[c], fmul(fu, fsub(c10[c], c00[c])));
@@ -1128,9 +1185,12 @@ static void sample_texture_quad(const OSampler *s, const float u[4], const float
         lod = fmaxr(lod, s->minLod);
         lod = fminr(lod, s->maxLod);
     }
-    if(!is_tex8(s->t->format))
+    const int border = s->t->address_u == SWGB_ADDRESS_CLAMP_TO_BORDER || s->t->address_v == SWGB_ADDRESS_CLAMP_TO_BORDER;
+    if(!is_tex8(s->t->format) || border)
     {
-        /* sampleFloatFilter (SamplerCore.cpp:1061-1083) */
+        /* sampleFloatFilter (SamplerCore.cpp:1061-1083); border addressing
+         * selects this 32-bit path for every format (:173-176), and 8-bit
+         * texels are normalized by 1 / 0xFF00 after it (:200-209) */
         float fr = fsub(daz(lod), floorf(daz(lod))); /* scalar Frac: lod - floor(lod) */
         for(int lane = 0; lane < 4; lane++)
         {
@@ -1142,7 +1202,7 @@ static void sample_texture_quad(const OSampler *s, const float u[4], const float
                 sample_float_2d(s, u[lane], v[lane], lod, 1, cc, lvMask);
                 for(int k = 0; k < 4; k++) c[k] = fadd(fmul(fsub(cc[k], c[k]), fr), c[k]);
             }
-            for(int k = 0; k < 4; k++) out[lane][k] = c[k];
+            for(int k = 0; k < 4; k++) out[lane][k] = is_tex8(s->t->format) ? fmul(c[k], 1.0f / 65280.0f) : c[k];
         }
         return;
     }

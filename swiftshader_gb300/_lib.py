@@ -82,7 +82,7 @@ def load(path=None):
     L.swgb_resolve.restype = C.c_int
     L.swgb_blit.argtypes = [C.c_void_p, C.POINTER(abi.Image), C.POINTER(abi.Image), C.POINTER(abi.BlitRegion), C.c_uint32]
     L.swgb_blit.restype = C.c_int
-    if L.swgb_abi_version() != 6:
+    if L.swgb_abi_version() != 7:
         raise OSError("libswgb ABI version mismatch")
     _lib = L
     return L

@@ -47,7 +47,10 @@ BLEND_OP_ADD, BLEND_OP_SUBTRACT, BLEND_OP_REVERSE_SUBTRACT, BLEND_OP_MIN, BLEND_
 FILTER_NEAREST, FILTER_LINEAR = 0, 1
 MIPMAP_MODE_NEAREST, MIPMAP_MODE_LINEAR = 0, 1
 ADDRESS_REPEAT, ADDRESS_MIRRORED_REPEAT, ADDRESS_CLAMP_TO_EDGE = 0, 1, 2
+ADDRESS_CLAMP_TO_BORDER = 3
 ADDRESS_MIRROR_CLAMP_TO_EDGE = 4
+BORDER_COLOR_FLOAT_TRANSPARENT_BLACK, BORDER_COLOR_FLOAT_OPAQUE_BLACK, BORDER_COLOR_FLOAT_OPAQUE_WHITE = 0, 2, 4
+BORDER_COLOR_FLOAT_CUSTOM_EXT = 1000287003
 VS_MVP_PASSTHROUGH = 1
 FS_VCOLOR = 1
 FS_TEX_X_VCOLOR = 2
@@ -76,7 +79,8 @@ class Texture(C.Structure):
                 ("levels", TextureLevel * MAX_MIP_LEVELS),
                 ("mag_filter", C.c_uint32), ("min_filter", C.c_uint32), ("mipmap_mode", C.c_uint32),
                 ("address_u", C.c_uint32), ("address_v", C.c_uint32),
-                ("mip_lod_bias", C.c_float), ("min_lod", C.c_float), ("max_lod", C.c_float)]
+                ("mip_lod_bias", C.c_float), ("min_lod", C.c_float), ("max_lod", C.c_float),
+                ("border_color", C.c_uint32), ("custom_border_color", C.c_float * 4)]
 
 
 class StencilOpState(C.Structure):

@@ -359,10 +359,36 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
         else return set_error(SWGB_UNSUPPORTED_STATE, "texture format");
         if(t.level_count < 1 || t.level_count > SWGB_MAX_MIP_LEVELS) return set_error(SWGB_INVALID_ARG, "texture level_count");
         if(t.mag_filter != t.min_filter) return set_error(SWGB_UNSUPPORTED_STATE, "mixed min/mag filters");
-        // REPEAT, MIRRORED_REPEAT, CLAMP_TO_EDGE, MIRROR_CLAMP_TO_EDGE (CLAMP_TO_BORDER is not implemented)
-        if(t.address_u > SWGB_ADDRESS_MIRROR_CLAMP_TO_EDGE || t.address_v > SWGB_ADDRESS_MIRROR_CLAMP_TO_EDGE ||
-           t.address_u == 3 || t.address_v == 3)
+        // REPEAT, MIRRORED_REPEAT, CLAMP_TO_EDGE, CLAMP_TO_BORDER, MIRROR_CLAMP_TO_EDGE
+        if(t.address_u > SWGB_ADDRESS_MIRROR_CLAMP_TO_EDGE || t.address_v > SWGB_ADDRESS_MIRROR_CLAMP_TO_EDGE)
             return set_error(SWGB_UNSUPPORTED_STATE, "address mode");
+        // border addressing takes the 32-bit filter path for every format
+        // (SamplerCore.cpp:173-176); the border texel is in that path's
+        // units: getComponentScale() = 0xFF00 for 8-bit textures, 1 for float
+        // ones (replaceBorderTexel, :2290-2355)
+        D.border = t.address_u == SWGB_ADDRESS_CLAMP_TO_BORDER || t.address_v == SWGB_ADDRESS_CLAMP_TO_BORDER;
+        D.floatPath = D.texFloat != 0 || D.border;
+        if(D.border)
+        {
+            const float sc = D.texFloat ? 1.0f : 65280.0f;
+            switch(t.border_color)
+            {
+            case SWGB_BORDER_COLOR_FLOAT_TRANSPARENT_BLACK:
+                for(int k = 0; k < 4; k++) D.borderColor[k] = 0.0f;
+                break;
+            case SWGB_BORDER_COLOR_FLOAT_OPAQUE_BLACK:
+                for(int k = 0; k < 3; k++) D.borderColor[k] = 0.0f;
+                D.borderColor[3] = sc;
+                break;
+            case SWGB_BORDER_COLOR_FLOAT_OPAQUE_WHITE:
+                for(int k = 0; k < 4; k++) D.borderColor[k] = sc;
+                break;
+            case SWGB_BORDER_COLOR_FLOAT_CUSTOM_EXT:
+                for(int k = 0; k < 4; k++) D.borderColor[k] = sc * t.custom_border_color[k];
+                break;
+            default: return set_error(SWGB_UNSUPPORTED_STATE, "border colour (float border colours only)");
+            }
+        }
         D.levelCount = (int)t.level_count;
         for(uint32_t i = 0; i < t.level_count; i++)
         {
@@ -411,14 +437,14 @@ const RasterKernel &raster_kernel(int v)
 
 // Raster kernel index of a draw: its bin shape, colour format and samples.
 // Draws with D16_UNORM depth, depth bias, the depth bounds test, the stencil
-// test, an sRGB colour attachment or an 8-bit texture addressed
-// MIRROR_CLAMP_TO_EDGE run the kernels that carry the full per-sample
-// pipeline.
+// test, an sRGB colour attachment, CLAMP_TO_BORDER addressing or an 8-bit
+// texture addressed MIRROR_CLAMP_TO_EDGE run the kernels that carry the full
+// per-sample pipeline.
 inline bool full_pipeline(const DrawParams &D)
 {
-    const bool mirrorOnce16 = D.fs == SWGB_FS_TEX_X_VCOLOR && !D.texFloat &&
+    const bool mirrorOnce16 = D.fs == SWGB_FS_TEX_X_VCOLOR && !D.floatPath &&
                               (D.addrU == SWGB_ADDRESS_MIRROR_CLAMP_TO_EDGE || D.addrV == SWGB_ADDRESS_MIRROR_CLAMP_TO_EDGE);
-    return D.depth16 || D.depthBias || D.depthBounds || D.stencilTest || D.colorSRGB || mirrorOnce16;
+    return D.depth16 || D.depthBias || D.depthBounds || D.stencilTest || D.colorSRGB || mirrorOnce16 || D.border;
 }
 inline int raster_variant(const DrawParams &D) { return raster_index(shape_index(D.binW, D.binH), D.hiz != 0, D.ms, D.cf, full_pipeline(D)); }
 
@@ -1132,8 +1158,9 @@ swgb_status bake_adjoint(const swgb_pipeline_state *st, const swgb_draw_args *a,
     if(D.stencilTest) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint: stencil test is not supported");
     if(D.depthBias) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint: depth bias is not supported");
     if(D.fs == SWGB_FS_TEX_X_VCOLOR && !D.texFloat) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint needs a float texture");
-    if(D.fs == SWGB_FS_TEX_X_VCOLOR && (D.addrU == SWGB_ADDRESS_MIRROR_CLAMP_TO_EDGE || D.addrV == SWGB_ADDRESS_MIRROR_CLAMP_TO_EDGE))
-        return set_error(SWGB_UNSUPPORTED_STATE, "adjoint: MIRROR_CLAMP_TO_EDGE addressing is not supported");
+    if(D.fs == SWGB_FS_TEX_X_VCOLOR && (D.addrU == SWGB_ADDRESS_MIRROR_CLAMP_TO_EDGE || D.addrV == SWGB_ADDRESS_MIRROR_CLAMP_TO_EDGE ||
+                                        D.border))
+        return set_error(SWGB_UNSUPPORTED_STATE, "adjoint: MIRROR_CLAMP_TO_EDGE / CLAMP_TO_BORDER addressing is not supported");
     if(D.writeMask != 0xFu) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint needs color_write_mask 0xF");
     if(a->count > ADJ_TRI_MASK) return set_error(SWGB_UNSUPPORTED_STATE, "adjoint: too many triangles");
     int over = 0;

@@ -135,6 +135,9 @@ struct DrawParams {
     int texSRGB;   // 8-bit texture with sRGB-encoded R, G, B (decoded through srgbLut)
     const uint16_t *srgbLut;  // sRGBtoLinearFF_FF00: 8-bit sRGB -> 16-bit linear (0xFF00 = 1.0)
     int texFloat; // 0: R8G8B8A8_UNORM texture (16-bit path), 1: RGBA16F, 2: RGBA32F (fp32 path)
+    int border;   // an axis addresses CLAMP_TO_BORDER: every texture takes the fp32 path
+    int floatPath;  // texFloat || border
+    float borderColor[4];  // the border texel in the fp32 path's units (scaled by 0xFF00 for 8-bit textures)
     uint8_t *color;
     uint32_t colorPitch;
     uint8_t *depth;
@@ -1280,9 +1283,27 @@ __device__ __forceinline__ void address_float(const DrawParams &D, float coord, 
     }
     else if(mode == SWGB_ADDRESS_MIRROR_CLAMP_TO_EDGE)
         coord = rmin(fabsf(coord), one);
-    else
+    else if(mode != SWGB_ADDRESS_CLAMP_TO_BORDER)  // a border axis keeps the coordinate
         coord = rmin(coord - floorf(coord), one);  // Float4 Frac (LLVMReactor.cpp:3252-3275)
     coord = coord * (float)dim;
+    if(mode == SWGB_ADDRESS_CLAMP_TO_BORDER)
+    {
+        // out-of-range texel coordinates become -1 and read the border
+        if(!D.texLinear)
+            x0 = trunc_int(floorf(coord));
+        else
+        {
+            coord = coord - 0.5f;
+            const float fl = floorf(coord);
+            x0 = trunc_int(fl);
+            f = coord - fl;
+        }
+        x1 = x0 + 1;
+        if(x0 < 0 || x0 >= dim) x0 = -1;
+        if(x1 < 0 || x1 >= dim) x1 = -1;
+        if(!D.texLinear) f = 0.0f;
+        return;
+    }
     if(!D.texLinear)
     {
         x0 = trunc_int(coord);
@@ -1309,13 +1330,23 @@ __device__ __forceinline__ void address_float(const DrawParams &D, float coord, 
 
 __device__ __forceinline__ float4 texel_float(const DrawParams &D, const TexLevel &lv, int32_t index)
 {
+    if(D.texFloat == 0)
+    {
+        // an 8-bit texture on the fp32 path (border addressing): the 16-bit
+        // path's components as floats (SamplerCore.cpp:2215-2245)
+        uint32_t c[4];
+        texel_components(D, __byte_perm(__ldg((const uint32_t *)lv.buf + (uint32_t)index), 0u, texel_order(D)), c);
+        return make_float4((float)c[0], (float)c[1], (float)c[2], (float)c[3]);
+    }
     if(D.texFloat == 2) return __ldg((const float4 *)lv.buf + (uint32_t)index);
     const uint2 h = __ldg((const uint2 *)lv.buf + (uint32_t)index);
     return make_float4(half_bits_to_float(h.x & 0xFFFFu), half_bits_to_float(h.x >> 16),
                        half_bits_to_float(h.y & 0xFFFFu), half_bits_to_float(h.y >> 16));
 }
 
-// sampleFloat2D for one lane (SamplerCore.cpp:1155-1248).
+// sampleFloat2D for one lane (SamplerCore.cpp:1155-1248).  BORDER: the
+// full-pipeline raster variants, which carry CLAMP_TO_BORDER addressing.
+template<bool BORDER>
 __device__ __forceinline__ float4 sample_float_2d(const DrawParams &D, float u, float v, float lod, int second, uint32_t &lvMask)
 {
     int ilod = D.mipLinear ? trunc_int(lod) : round_int(lod);
@@ -1328,6 +1359,28 @@ __device__ __forceinline__ float4 sample_float_2d(const DrawParams &D, float u, 
     address_float(D, u, D.addrU, (int)lv.w, x0, x1, fu);
     address_float(D, v, D.addrV, (int)lv.h, y0, y1, fv);
     const int32_t pitch = (int32_t)lv.pitch;
+    if(BORDER && D.border)
+    {
+        // sampleTexel with border addressing (SamplerCore.cpp:2093-2110,
+        // 1645-1677, 2290-2355): a texel with a -1 coordinate reads index 0
+        // and is replaced by the border colour
+        const float4 bc = make_float4(D.borderColor[0], D.borderColor[1], D.borderColor[2], D.borderColor[3]);
+        auto fetch = [&](int32_t x, int32_t y) {
+            const bool valid = x >= 0 && y >= 0;
+            const float4 t = texel_float(D, lv, valid ? x + y * pitch : 0);
+            return valid ? t : bc;
+        };
+        if(!D.texLinear) return fetch(x0, y0);
+        const float4 c00 = fetch(x0, y0), c10 = fetch(x1, y0), c01 = fetch(x0, y1), c11 = fetch(x1, y1);
+        float4 a, b, o;
+        a.x = c00.x + fu * (c10.x - c00.x); a.y = c00.y + fu * (c10.y - c00.y);
+        a.z = c00.z + fu * (c10.z - c00.z); a.w = c00.w + fu * (c10.w - c00.w);
+        b.x = c01.x + fu * (c11.x - c01.x); b.y = c01.y + fu * (c11.y - c01.y);
+        b.z = c01.z + fu * (c11.z - c01.z); b.w = c01.w + fu * (c11.w - c01.w);
+        o.x = a.x + fv * (b.x - a.x); o.y = a.y + fv * (b.y - a.y);
+        o.z = a.z + fv * (b.z - a.z); o.w = a.w + fv * (b.w - a.w);
+        return o;
+    }
     y0 *= pitch;
     if(!D.texLinear) return texel_float(D, lv, x0 + y0);
     y1 *= pitch;
@@ -1347,17 +1400,23 @@ __device__ __forceinline__ float4 sample_float_2d(const DrawParams &D, float u, 
 // Frac of the LOD (x86 SSE4.1: lod - floor(lod)).
 // Out of line: the raster kernels carry both filtering paths, and the fp32 one
 // inlined would crowd the UNORM8 path's code in the loop.
+template<bool BORDER>
 static __device__ __noinline__ void sample_float_lane(const DrawParams &D, float lod, float ul, float vl, float out[4], uint32_t &lvMask)
 {
-    float4 c = sample_float_2d(D, ul, vl, lod, 0, lvMask);
+    float4 c = sample_float_2d<BORDER>(D, ul, vl, lod, 0, lvMask);
     if(D.mipLinear)
     {
-        const float4 cc = sample_float_2d(D, ul, vl, lod, 1, lvMask);
+        const float4 cc = sample_float_2d<BORDER>(D, ul, vl, lod, 1, lvMask);
         const float fr = lod - floorf(lod);
         c.x = (cc.x - c.x) * fr + c.x;
         c.y = (cc.y - c.y) * fr + c.y;
         c.z = (cc.z - c.z) * fr + c.z;
         c.w = (cc.w - c.w) * fr + c.w;
+    }
+    if(BORDER && D.texFloat == 0)  // normalized 8-bit texels: 1 / getComponentScale() (SamplerCore.cpp:200-209)
+    {
+        const float s = 1.0f / 65280.0f;
+        c.x = c.x * s; c.y = c.y * s; c.z = c.z * s; c.w = c.w * s;
     }
     out[0] = c.x; out[1] = c.y; out[2] = c.z; out[3] = c.w;
 }
@@ -1737,7 +1796,7 @@ __device__ __forceinline__ void shade_pixel(const DrawParams &D, const SH &S, in
         const float ul = i == 0 ? u[0] : (i == 1 ? u[1] : (i == 2 ? u[2] : u[3]));
         const float vl = i == 0 ? v[0] : (i == 1 ? v[1] : (i == 2 ? v[2] : v[3]));
         float t[4];
-        if(D.texFloat) sample_float_lane(D, lod, ul, vl, t, lvMask);
+        if(D.floatPath) sample_float_lane<SH::kFull>(D, lod, ul, vl, t, lvMask);
         else sample_texture_lane<SH::kFull>(D, lod, ul, vl, t, lvMask);
 #pragma unroll
         for(int k = 0; k < 4; k++) c[k] = t[k] * c[k];

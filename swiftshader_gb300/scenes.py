@@ -11,6 +11,8 @@ R32G32B32A32_SFLOAT at 16, uv R32G32_SFLOAT at 32.
 from dataclasses import dataclass, field
 import math
 
+import ctypes
+
 import numpy as np
 
 from . import abi
@@ -370,6 +372,8 @@ def build_state(scene, color_ptr, depth_ptr, vertex_ptr, level_ptrs=None, color_
         for i, lv in enumerate(scene.texture_levels):
             t.levels[i] = abi.TextureLevel(level_ptrs[i], lv.shape[1], lv.shape[0], lv.shape[1], 0)
         for k, val in scene.sampler.items():
+            if k == "custom_border_color":
+                val = (ctypes.c_float * 4)(*val)
             setattr(t, k, val)
     st.precision_profile = abi.PRECISION_CMAKE
     return st

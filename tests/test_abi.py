@@ -76,7 +76,7 @@ def test_library_loads_and_exports_all_symbols(built_lib):
     for name in _lib.EXPORTS:
         assert name in exported, name
     L = _lib.load(built_lib)
-    assert L.swgb_abi_version() == 6
+    assert L.swgb_abi_version() == 7
 
 
 def test_host_side_errors_without_device(built_lib):

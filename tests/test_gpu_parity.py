@@ -175,6 +175,32 @@ def _float_variant(tex_fmt, color_fmt, blend, address, mip, seed=31):
     return s
 
 
+@pytest.mark.parametrize("tex_fmt", [abi.FORMAT_R8G8B8A8_UNORM, abi.FORMAT_B8G8R8A8_SRGB, abi.FORMAT_R16G16B16A16_SFLOAT,
+                                     abi.FORMAT_R32G32B32A32_SFLOAT])
+@pytest.mark.parametrize("border,linear,mixed", [
+    (abi.BORDER_COLOR_FLOAT_OPAQUE_WHITE, True, False),
+    (abi.BORDER_COLOR_FLOAT_TRANSPARENT_BLACK, False, False),
+    (abi.BORDER_COLOR_FLOAT_OPAQUE_BLACK, True, True),
+    (abi.BORDER_COLOR_FLOAT_CUSTOM_EXT, True, False),
+])
+def test_clamp_to_border(gpu_lib, tex_fmt, border, linear, mixed):
+    """CLAMP_TO_BORDER: every texture format takes the 32-bit filter path
+    (8-bit texels as their 16-bit-path values, normalized after filtering);
+    texels outside the image read the border colour scaled to that path's
+    units; trilinear / point; border on one axis and REPEAT on the other."""
+    s = _float_variant(tex_fmt, abi.FORMAT_R8G8B8A8_UNORM, True, abi.ADDRESS_CLAMP_TO_BORDER, linear) \
+        if tex_fmt in (abi.FORMAT_R16G16B16A16_SFLOAT, abi.FORMAT_R32G32B32A32_SFLOAT) else \
+        scenes.scene_textured_small(n_tris=200, width=96, height=72, mip=linear, address=abi.ADDRESS_CLAMP_TO_BORDER,
+                                    blend=True, seed_index=68)
+    s.texture_format = tex_fmt
+    s.sampler = dict(s.sampler, border_color=border, custom_border_color=(0.25, 0.5, 1.5, 0.75))
+    if not linear:
+        s.sampler.update(mag_filter=abi.FILTER_NEAREST, min_filter=abi.FILTER_NEAREST)
+    if mixed:
+        s.sampler["address_v"] = abi.ADDRESS_REPEAT
+    check_scene(s, gpu_lib)
+
+
 def test_mirror_clamp_nan_coordinates(gpu_lib):
     """MIRROR_CLAMP_TO_EDGE maps a NaN coordinate to the last texel, as
     ADDRESSING_MIRRORONCE's integer arithmetic does; some vertices carry NaN

@@ -201,3 +201,33 @@ def test_mirror_clamp_to_edge_is_clamp_of_abs(oracle_mod):
         b.sampler = dict(b.sampler, address_u=abi.ADDRESS_CLAMP_TO_EDGE, address_v=abi.ADDRESS_CLAMP_TO_EDGE)
         cc, _, _ = oracle_mod.render(b)
         assert not np.array_equal(cc, ca)
+
+
+def test_clamp_to_border_sampling(oracle_mod):
+    """CLAMP_TO_BORDER on the oracle's 32-bit path: point samples inside the
+    image return the texel (8-bit: b << 8 normalized by 1 / 0xFF00), outside
+    it the border colour (custom colours scaled by 0xFF00 and back)."""
+    import ctypes as C
+    from swiftshader_gb300 import abi
+    tex = np.arange(4 * 4 * 4, dtype=np.uint8).reshape(4, 4, 4) * 3
+    t = abi.Texture()
+    t.format = abi.FORMAT_R8G8B8A8_UNORM
+    t.level_count = 1
+    t.levels[0] = abi.TextureLevel(tex.ctypes.data, 4, 4, 4, 0)
+    t.mag_filter = t.min_filter = abi.FILTER_NEAREST
+    t.mipmap_mode = abi.MIPMAP_MODE_NEAREST
+    t.address_u = t.address_v = abi.ADDRESS_CLAMP_TO_BORDER
+    t.max_lod = 0.0
+    t.border_color = abi.BORDER_COLOR_FLOAT_CUSTOM_EXT
+    t.custom_border_color = (C.c_float * 4)(0.25, 0.5, 1.5, 0.75)
+    u = (C.c_float * 4)(0.125, 0.625, -0.1, 1.2)
+    v = (C.c_float * 4)(0.375, 0.875, 0.5, 0.5)
+    out = (C.c_float * 16)()
+    assert oracle_mod.lib().oracle_sample_quad(C.byref(t), u, v, out) == 0
+    o = np.array(out, np.float32).reshape(4, 4)
+    inv = np.float32(1.0) / np.float32(65280.0)
+    for lane, (x, y) in enumerate([(0, 1), (2, 3)]):
+        assert np.array_equal(o[lane], (tex[y, x].astype(np.float32) * np.float32(256)) * inv)
+    border = (np.float32(65280.0) * np.array([0.25, 0.5, 1.5, 0.75], np.float32)) * inv
+    assert np.array_equal(o[2], border) and np.array_equal(o[3], border)
+    assert abs(o[2][2] - 1.5) < 1e-6  # custom colours are not clamped
