@@ -49,6 +49,23 @@ def test_noalloc_matches_draw_twice(gpu_lib):
     assert np.array_equal(d.view(np.uint32), d_ref.view(np.uint32))
 
 
+def test_noalloc_full_pipeline_draw(gpu_lib):
+    """A draw that runs the full-pipeline raster variant through the fixed
+    scratch: D16_UNORM depth with depth bias, a B8G8R8A8_UNORM attachment,
+    a CLAMP_TO_BORDER texture with a custom border colour."""
+    L = gpu_lib
+    sc = scenes.scene_textured_small(n_tris=250, width=96, height=64, mip=True, address=abi.ADDRESS_CLAMP_TO_BORDER,
+                                     blend=True, seed_index=69)
+    sc.depth_format = abi.FORMAT_D16_UNORM
+    sc.depth_bias = (3.0, 1.0, 0.0)
+    sc.color_format = abi.FORMAT_B8G8R8A8_UNORM
+    sc.sampler = dict(sc.sampler, border_color=abi.BORDER_COLOR_FLOAT_CUSTOM_EXT, custom_border_color=(0.2, 0.4, 0.6, 0.8))
+    c_ref, d_ref = _ctx_render(sc)
+    c, d = _noalloc_render(L, sc)
+    assert np.array_equal(c, c_ref)
+    assert np.array_equal(np.ascontiguousarray(d).view(np.uint8), np.ascontiguousarray(d_ref).view(np.uint8))
+
+
 def test_noalloc_rejects_oversized_draws(gpu_lib):
     L = gpu_lib
     sc = scenes.scene_small(n_tris=8, width=32, height=32)
