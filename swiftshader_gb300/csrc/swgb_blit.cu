@@ -238,43 +238,52 @@ __global__ void __launch_bounds__(256) k_blit(BlitParams P)
 // both images -- one mip level from the one above.  There the routine's
 // positions are exact: x = 1 + 2i, X0 = 2i, X1 = 2i + 1, fx = fy = 1/2, so the
 // blend above is evaluated on texels 2i, 2i + 1 of rows 2j, 2j + 1.  Each
-// thread makes two destination pixels from a 4 x 2 texel block (one 16-byte
-// load per row for 8-bit texels when the rows are 16-byte aligned).
+// thread makes PX destination pixels from a 2PX x 2 texel block: four for
+// 8-bit texels (two 16-byte loads per row when the rows are 16-byte
+// aligned), two for float texels.
 template<int SK, int DK>
 __global__ void __launch_bounds__(256) k_blit_half(BlitParams P)
 {
-    const int i0 = 2 * (int)(blockIdx.x * 32 + (threadIdx.x & 31));
+    constexpr int PX = kind_unorm8(SK) ? 4 : 2;
+    constexpr int B = kind_bytes(SK);
+    const int i0 = PX * (int)(blockIdx.x * 32 + (threadIdx.x & 31));
     const int j = (int)(blockIdx.y * 8 + (threadIdx.x >> 5));
     if(i0 >= P.x1d || j >= P.y1d) return;
-    constexpr int B = kind_bytes(SK);
+    const int n = min(PX, P.x1d - i0);  // destination pixels of this thread
     const uint8_t *r0 = P.src + (int64_t)(2 * j) * P.sPitch + (int64_t)(2 * i0) * B;
     const uint8_t *r1 = r0 + P.sPitch;
-    const bool two = i0 + 1 < P.x1d;
-    float4 a[4], b[4];
-    if(kind_unorm8(SK) && two && P.vec16)
+    float4 a[2 * PX], b[2 * PX];
+    if(kind_unorm8(SK) && n == PX && P.vec16)
     {
-        const uint4 u = *(const uint4 *)r0, v = *(const uint4 *)r1;
-        const uint32_t uu[4] = {u.x, u.y, u.z, u.w}, vv[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-        for(int k = 0; k < 4; k++)
+        for(int h = 0; h < PX / 2; h++)
         {
-            a[k] = read_texel((const uint8_t *)&uu[k], SK);
-            b[k] = read_texel((const uint8_t *)&vv[k], SK);
+            const uint4 u = *(const uint4 *)(r0 + 16 * h), v = *(const uint4 *)(r1 + 16 * h);
+            const uint32_t uu[4] = {u.x, u.y, u.z, u.w}, vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for(int k = 0; k < 4; k++)
+            {
+                a[4 * h + k] = read_texel((const uint8_t *)&uu[k], SK);
+                b[4 * h + k] = read_texel((const uint8_t *)&vv[k], SK);
+            }
         }
     }
     else
     {
 #pragma unroll
-        for(int k = 0; k < 4; k++)
-            if(k < 2 || two)
+        for(int k = 0; k < 2 * PX; k++)
+            if(k < 2 * n)
             {
                 a[k] = read_texel(r0 + k * B, SK);
                 b[k] = read_texel(r1 + k * B, SK);
             }
     }
     uint8_t *d = P.dst + (int64_t)j * P.dPitch + (int64_t)i0 * kind_bytes(DK);
-    write_texel<kind_unorm8(SK)>(d, DK, bilinear<SK, DK>(P, a[0], a[1], b[0], b[1], 0.5f, 0.5f));
-    if(two) write_texel<kind_unorm8(SK)>(d + kind_bytes(DK), DK, bilinear<SK, DK>(P, a[2], a[3], b[2], b[3], 0.5f, 0.5f));
+#pragma unroll
+    for(int p = 0; p < PX; p++)
+        if(p < n)
+            write_texel<kind_unorm8(SK)>(d + p * kind_bytes(DK), DK,
+                                         bilinear<SK, DK>(P, a[2 * p], a[2 * p + 1], b[2 * p], b[2 * p + 1], 0.5f, 0.5f));
 }
 
 // fastResolve (Blitter.cpp:2079-2205): per byte, the rounding-up average of
@@ -430,7 +439,8 @@ cudaError_t launch_blit(const BlitParams &P, cudaStream_t st)
                        : P.srcKind == BK_BGRA8 ? k_blit_half<BK_BGRA8, BK_BGRA8>
                        : P.srcKind == BK_RGBA16F ? k_blit_half<BK_RGBA16F, BK_RGBA16F>
                                                  : k_blit_half<BK_RGBA32F, BK_RGBA32F>;
-        k<<<dim3((w + 63) / 64, (h + 7) / 8), 256, 0, st>>>(P);
+        const int px = (P.srcKind == BK_RGBA8 || P.srcKind == BK_BGRA8) ? 4 : 2;  // destination pixels per thread
+        k<<<dim3((w + 32 * px - 1) / (32 * px), (h + 7) / 8), 256, 0, st>>>(P);
         return cudaGetLastError();
     }
     BlitKernel k = P.srcKind == BK_RGBA8     ? blit_kernel<BK_RGBA8>(P.dstKind, f)
