@@ -286,6 +286,37 @@ __global__ void __launch_bounds__(256) k_blit_half(BlitParams P)
                                          bilinear<SK, DK>(P, a[2 * p], a[2 * p + 1], b[2 * p], b[2 * p + 1], 0.5f, 0.5f));
 }
 
+// The NEAREST blit a float-format resolve is (Blitter.cpp:1508-1545): at
+// scale 1 the sample position of destination pixel i is source texel
+// i + (srcOffset - dstOffset) exactly; its four samples are read, summed in
+// order, scaled by 1/4 and written -- no scale, clamp or sRGB step applies to
+// float formats.  Two pixels per thread for half floats (16-byte loads).
+template<int SK>
+__global__ void __launch_bounds__(256) k_resolve_float(BlitParams P, int dx, int dy)
+{
+    constexpr int PX = SK == BK_RGBA16F ? 2 : 1;
+    constexpr int B = kind_bytes(SK);
+    const int i0 = P.x0d + PX * (int)(blockIdx.x * 32 + (threadIdx.x & 31));
+    const int j = P.y0d + (int)(blockIdx.y * 8 + (threadIdx.x >> 5));
+    if(i0 >= P.x1d || j >= P.y1d) return;
+    const int n = min(PX, P.x1d - i0);
+    const uint8_t *s = P.src + (int64_t)(j + dy) * P.sPitch + (int64_t)(i0 + dx) * B;
+    uint8_t *d = P.dst + (int64_t)j * P.dPitch + (int64_t)i0 * B;
+#pragma unroll
+    for(int p = 0; p < PX; p++)
+        if(p < n)
+        {
+            float4 acc = read_texel(s + p * B, SK);
+#pragma unroll
+            for(int q = 1; q < 4; q++)
+            {
+                const float4 c = read_texel(s + p * B + q * P.sSlice, SK);
+                acc = make_float4(acc.x + c.x, acc.y + c.y, acc.z + c.z, acc.w + c.w);
+            }
+            write_texel(d + p * B, SK, mul4(acc, 1.0f / 4.0f));
+        }
+}
+
 // fastResolve (Blitter.cpp:2079-2205): per byte, the rounding-up average of
 // samples 0 and 1, of 2 and 3, then of the two (averageByte4 /
 // _mm_avg_epu8; __vavgu4 computes the same (a + b + 1) >> 1 per byte).
@@ -441,6 +472,18 @@ cudaError_t launch_blit(const BlitParams &P, cudaStream_t st)
                                                  : k_blit_half<BK_RGBA32F, BK_RGBA32F>;
         const int px = (P.srcKind == BK_RGBA8 || P.srcKind == BK_BGRA8) ? 4 : 2;  // destination pixels per thread
         k<<<dim3((w + 32 * px - 1) / (32 * px), (h + 7) / 8), 256, 0, st>>>(P);
+        return cudaGetLastError();
+    }
+    // a float-format 4-sample resolve at scale 1
+    if(!f && P.srcSamples == 4 && P.w == 1.0f && P.h == 1.0f && P.srcKind == P.dstKind && kind_float(P.srcKind))
+    {
+        const int dx = (int)floorf(P.x0), dy = (int)floorf(P.y0);  // srcOffset - dstOffset
+        const int px = P.srcKind == BK_RGBA16F ? 2 : 1;
+        const dim3 g((w + 32 * px - 1) / (32 * px), (h + 7) / 8);
+        if(P.srcKind == BK_RGBA16F)
+            k_resolve_float<BK_RGBA16F><<<g, 256, 0, st>>>(P, dx, dy);
+        else
+            k_resolve_float<BK_RGBA32F><<<g, 256, 0, st>>>(P, dx, dy);
         return cudaGetLastError();
     }
     BlitKernel k = P.srcKind == BK_RGBA8     ? blit_kernel<BK_RGBA8>(P.dstKind, f)
