@@ -78,6 +78,14 @@ def lib():
         L.oracle_vertex.argtypes = [C.POINTER(abi.PipelineState), C.POINTER(abi.DrawArgs), C.c_uint32,
                                     C.POINTER(C.c_float), C.POINTER(C.c_int32)]
         L.oracle_vertex.restype = C.c_int
+        L.oracle_triangle_inputs.argtypes = [C.POINTER(abi.PipelineState), C.POINTER(abi.DrawArgs), C.c_uint32,
+                                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.oracle_triangle_inputs.restype = C.c_int
+        L.oracle_setup_samples.argtypes = [C.POINTER(abi.PipelineState), C.POINTER(abi.DrawArgs), C.c_uint32,
+                                           C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
+        L.oracle_setup_samples.restype = C.c_int
+        L.oracle_set_interpolation_muladd.argtypes = [C.c_int]
+        L.oracle_set_interpolation_muladd.restype = None
         L.oracle_setup.argtypes = [C.POINTER(abi.PipelineState), C.POINTER(abi.DrawArgs), C.c_uint32,
                                    C.POINTER(C.c_int32), C.POINTER(C.c_uint16), C.c_int, C.POINTER(C.c_float)]
         L.oracle_setup.restype = C.c_int

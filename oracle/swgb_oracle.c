@@ -53,6 +53,17 @@ static inline float fsub(float a, float b) { return daz(daz(a) - daz(b)); }
 static inline float fmul(float a, float b) { return daz(daz(a) * daz(b)); }
 static inline float fdiv(float a, float b) { return daz(daz(a) / daz(b)); }
 static inline float ffma(float a, float b, float c) { return daz(fmaf(daz(a), daz(b), daz(c))); }
+
+/* Lowering of the mulAdd in QuadRasterizer::interpolate (QuadRasterizer.cpp:235-250,
+ * ShaderCore.cpp:714-722): Reactor's LLVM backend emits llvm.fmuladd, fused
+ * on an FMA host (the CMake profile this oracle restates, the default);
+ * Reactor's Subzero backend emits a multiply and an add
+ * (SubzeroReactor.cpp MulAdd).  The routine-level reference fixtures come
+ * from a Subzero build, so the tests that compare rasterised depth with them
+ * switch this to unfused (oracle_set_interpolation_muladd). */
+static int g_interp_fused = 1;
+static inline float interp_muladd(float a, float b, float c) { return g_interp_fused ? ffma(a, b, c) : fadd(fmul(a, b), c); }
+void oracle_set_interpolation_muladd(int fused) { g_interp_fused = fused != 0; }
 /* Comparisons see DAZ-flushed operands. */
 static inline int flt(float a, float b) { return daz(a) < daz(b); }
 static inline int fle(float a, float b) { return daz(a) <= daz(b); }
@@ -1227,6 +1238,7 @@ static void sample_texture_quad(const OSampler *s, const float u[4], const float
 
 swgb_status oracle_sample_quad(const swgb_texture *tex, const float u[4], const float v[4], float out[16])
 {
+    pthread_once(&srgb_once, srgb_init); /* sRGB textures decode through the table prepare() builds for draws */
     OSampler s;
     sampler_init(&s, tex);
     float o[4][4];
@@ -1481,7 +1493,7 @@ static void pixel_quad(const ODraw *d, const OSampler *smp, const OPrim *pr, int
                     xq = fsub(xq, SLX[q]); /* PixelRoutine.cpp:128-148 */
                 }
                 float Dz = fadd(pr->z.C, fmul(yq, pr->z.B));
-                z[q][i] = ffma(xq, pr->z.A, Dz);
+                z[q][i] = interp_muladd(xq, pr->z.A, Dz);
                 if(d->st->depth_bias_constant != 0.0f || d->st->depth_bias_slope != 0.0f)
                     z[q][i] = fadd(z[q][i], pr->zBias); /* PixelRoutine.cpp:141-144 */
             }
@@ -1490,7 +1502,7 @@ static void pixel_quad(const ODraw *d, const OSampler *smp, const OPrim *pr, int
     for(int i = 0; i < 4; i++)
     {
         float Dw = fadd(pr->w.C, fmul(yF[i], pr->w.B));
-        float w = ffma(xF[i], pr->w.A, Dw);
+        float w = interp_muladd(xF[i], pr->w.A, Dw);
         rhw[i] = fdiv(1.0f, w);
     }
     float vin[MAXV][4];
@@ -1498,7 +1510,7 @@ static void pixel_quad(const ODraw *d, const OSampler *smp, const OPrim *pr, int
         for(int i = 0; i < 4; i++)
         {
             float Dv = fadd(pr->V[k].C, fmul(yF[i], pr->V[k].B));
-            vin[k][i] = fmul(ffma(xF[i], pr->V[k].A, Dv), rhw[i]);
+            vin[k][i] = fmul(interp_muladd(xF[i], pr->V[k].A, Dv), rhw[i]);
         }
     /* Fixed fragment shader (PixelProgram::executeShader :138-241) */
     float c[4][4];
@@ -1940,4 +1952,86 @@ int oracle_setup(const swgb_pipeline_state *st, const swgb_draw_args *a, uint32_
     }
     free(buf);
     return vis;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Routine-level probes matched by the reference's own routines             */
+/* (oracle/refjit/refjit_harness.cpp)                                       */
+/* ------------------------------------------------------------------------ */
+
+#define ORACLE_VF (6 + MAXV)
+
+int oracle_triangle_inputs(const swgb_pipeline_state *st, const swgb_draw_args *a, uint32_t tri, float *vf, int32_t *vi,
+                           float *consts, int32_t *scissor)
+{
+    ODraw d;
+    if(prepare(&d, st, a) != SWGB_OK) return -1;
+    uint32_t k[3];
+    triangle_positions(st->topology, st->provoking_vertex == 0, tri, k);
+    for(int j = 0; j < 3; j++)
+    {
+        OVertex v;
+        memset(&v, 0, sizeof(v));
+        vertex_shade(&d, vertex_index(&d, k[j]), &v);
+        float *f = vf + j * ORACLE_VF;
+        f[0] = v.pos.x; f[1] = v.pos.y; f[2] = v.pos.z; f[3] = v.pos.w;
+        f[4] = v.pz; f[5] = v.pw;
+        for(int c = 0; c < MAXV; c++) f[6 + c] = c < d.nv ? v.v[c] : 0.0f;
+        vi[3 * j + 0] = v.X; vi[3 * j + 1] = v.Y; vi[3 * j + 2] = v.clipFlags;
+    }
+    consts[0] = d.WxF; consts[1] = d.HxF; consts[2] = d.X0xF; consts[3] = d.Y0xF;
+    consts[4] = d.depthRange; consts[5] = d.depthNear;
+    scissor[0] = d.sx0; scissor[1] = d.sx1; scissor[2] = d.sy0; scissor[3] = d.sy1;
+    return d.nv;
+}
+
+int oracle_setup_samples(const swgb_pipeline_state *st, const swgb_draw_args *a, uint32_t tri, int32_t *out_i, uint16_t *spans,
+                         int max_rows, float *out_f)
+{
+    ODraw d;
+    if(prepare(&d, st, a) != SWGB_OK) return -1;
+    OPrim pr;
+    memset(&pr, 0, sizeof(pr));
+    uint16_t *buf = (uint16_t *)calloc((size_t)8 * d.rows, sizeof(uint16_t));
+    if(!buf) return -1;
+    for(int q = 0; q < 4; q++)
+    {
+        pr.left[q] = buf + (size_t)2 * q * d.rows;
+        pr.right[q] = pr.left[q] + d.rows;
+    }
+    int clipped = 0;
+    int vis = process_triangle(&d, tri, &pr, NULL, &clipped);
+    out_i[0] = vis ? pr.yMin : 0;
+    out_i[1] = vis ? pr.yMax : 0;
+    out_i[2] = clipped;
+    out_i[3] = vis;
+    int rc = 0;
+    if(vis && spans)
+    {
+        int rows = pr.yMax - pr.yMin + 2;
+        if(rows > max_rows) rc = -1;
+        else
+            for(int q = 0; q < d.ms; q++)
+                for(int r = 0; r < rows; r++)
+                {
+                    int y = pr.yMin - 1 + r; /* left/right are indexed [y + 1] */
+                    spans[((size_t)q * max_rows + r) * 2 + 0] = pr.left[q][y + 1];
+                    spans[((size_t)q * max_rows + r) * 2 + 1] = pr.right[q][y + 1];
+                }
+    }
+    if(vis && out_f)
+    {
+        out_f[0] = pr.x0; out_f[1] = pr.y0;
+        out_f[2] = pr.z.A; out_f[3] = pr.z.B; out_f[4] = pr.z.C;
+        out_f[5] = pr.w.A; out_f[6] = pr.w.B; out_f[7] = pr.w.C;
+        for(int k = 0; k < d.nv; k++)
+        {
+            out_f[8 + 3 * k + 0] = pr.V[k].A;
+            out_f[8 + 3 * k + 1] = pr.V[k].B;
+            out_f[8 + 3 * k + 2] = pr.V[k].C;
+        }
+        out_f[8 + 3 * d.nv] = pr.zBias;
+    }
+    free(buf);
+    return rc == 0 ? vis : rc;
 }

@@ -64,6 +64,31 @@ int oracle_setup(const swgb_pipeline_state *state, const swgb_draw_args *args, u
  * exactly as SamplerCore::sampleTexture128 returns them. */
 swgb_status oracle_sample_quad(const swgb_texture *tex, const float u[4], const float v[4], float out[16]);
 
+/* Routine-level probes, compared with SwiftShader's own routines run by
+ * oracle/refjit (tests/test_oracle_reference_fixtures.py).
+ *
+ * oracle_triangle_inputs: what the setup stage receives for triangle tri, in
+ * the triangle's setBatchIndices order: vf[3 * 14] (per vertex: clip x, y, z,
+ * w, projected z, projected w, 8 varying components, zero past the draw's),
+ * vi[3 * 3] (projected X, Y, clip flags), consts = {WxF, HxF, X0xF, Y0xF,
+ * depthRange, depthNear}, scissor = {x0, x1, y0, y1}.  Returns the draw's
+ * varying component count, or -1.
+ *
+ * oracle_setup_samples: oracle_setup with every sample's outline:
+ * spans[(q * max_rows + r) * 2 + 0/1] = (left, right) of row yMin - 1 + r of
+ * sample q for rows yMin - 1 .. yMax, and out_f = {x0, y0, z.A, z.B, z.C, w.A,
+ * w.B, w.C, V[k].A, V[k].B, V[k].C ..., zBias}.  Returns visibility, or -1
+ * (max_rows too small or invalid state).
+ *
+ * oracle_set_interpolation_muladd: 1 (default) fuses the mulAdd of
+ * QuadRasterizer::interpolate as Reactor's LLVM backend does on an FMA host;
+ * 0 lowers it to a multiply and an add, as Reactor's Subzero backend does. */
+int oracle_triangle_inputs(const swgb_pipeline_state *state, const swgb_draw_args *args, uint32_t tri, float *vf, int32_t *vi,
+                           float *consts, int32_t *scissor);
+int oracle_setup_samples(const swgb_pipeline_state *state, const swgb_draw_args *args, uint32_t tri, int32_t *out_i,
+                         uint16_t *spans, int max_rows, float *out_f);
+void oracle_set_interpolation_muladd(int fused);
+
 #ifdef __cplusplus
 }
 #endif
