@@ -10,11 +10,15 @@ public call with host buffers: every step copies the scene (vertices, indices,
 texture chain) host->device from pinned memory and reads the colour + depth
 attachments back, inside the timed region.
 
+``value`` counts fragments passed (written after the depth test) per second;
+fragments tested are reported beside it as ``gfrag_tested_per_s``.
+
 The default line also carries
-  * "batched": the 4096-draw atlas workload with triangle counts log-uniform
-    in [16, 1024] (a reduced-size sample of the batch workload, stated in its
-    config), one swgb_draw_batch call per step against the same draws issued
-    one swgb_draw each;
+  * "batched": the full 4096-draw atlas workload (triangle counts
+    log-uniform in [16, 65536]), one swgb_draw_batch call per step against
+    the same draws issued one swgb_draw each (the per-draw raster
+    configuration picked on a seeded 256-draw sample, then timed on all
+    4096 draws);
   * "adjoint": forward and adjoint times (and their ratio) of the two adjoint
     workloads at full size -- the 20k-triangle sphere at 512^2 RGBA32F and 256
     views of the 100k-triangle noisy sphere at 512^2 4x MSAA -- through the
@@ -48,6 +52,8 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+DEFAULT_RUNS = 3
+
 WORKLOADS = {
     "heightfield": "1000x500-quad height field (1,000,000 tris, uint32 indices), 1920x1080 RGBA8 + D32F, "
                    "2048^2 RGBA8 12-level chain trilinear REPEAT, colour = texel * vertex colour, depth LESS, "
@@ -63,7 +69,6 @@ WORKLOADS = {
 }
 
 BATCH_FULL = dict(n_draws=4096, tri_min=16, tri_max=65536)
-BATCH_REDUCED = dict(n_draws=4096, tri_min=16, tri_max=1024)
 
 
 def make_scene(name):
@@ -238,7 +243,8 @@ def run_ours(args):
     ms_per_step = sum(step_ms) / len(step_ms)
     cnt = r.counters()
     frames = args.steps
-    frag_per_frame = cnt["fragments_tested"] / frames
+    frag_per_frame = cnt["fragments_passed"] / frames
+    tested_per_frame = cnt["fragments_tested"] / frames
     tri_per_frame = cnt["triangles_in"] / frames
     per_frame = {k: v // frames if k != "texture_levels_mask" else v for k, v in cnt.items()}
 
@@ -283,9 +289,10 @@ def run_ours(args):
     batched = None
     if args.workload == "heightfield" and not args.no_batched:
         del h_vert, h_idx, h_lv, h_color, h_depth
-        _, _, batched = measure_batch(r, stream, flush, BATCH_REDUCED, 3, 1, 2, dev, tune=not args.no_autotune)
-        batched["config"]["note"] = ("reduced-size sample of the batch workload (triangles log-uniform in "
-                                     "[16, 1024] instead of [16, 65536]); --workload batch runs the full one")
+        _, db, batched = measure_batch(r, stream, flush, BATCH_FULL, 3, 1, 1, dev, tune=not args.no_autotune,
+                                       pick_sample=256)
+        batched["config"]["workload"] = WORKLOADS["batch"]
+        del db
 
     blitter = None
     if args.workload == "heightfield" and not args.no_blitter:
@@ -325,8 +332,11 @@ def run_ours(args):
         "vs_baseline": None,
         "dtype": "f32 + int32 fixed point (RGBA8 / D32F out)",
         "data": "synthetic (seeded generator, swiftshader_gb300.scenes)",
-        "config": {"workload": WORKLOADS[args.workload], "l2": "flushed before every timed step (256 MiB write)",
-                   "parallelism": "replicas only" if world > 1 else "single GPU"},
+        "config": {"workload": WORKLOADS[args.workload]},
+        "l2": "flushed before every timed step (256 MiB write)",
+        "parallelism": "replicas only" if world > 1 else "single GPU",
+        "value_counts": "fragments passed (F_p: written after the depth test) per second",
+        "gfrag_tested_per_s": round(world * tested_per_frame / (ms_per_step * 1e-3) / 1e9, 4),
         "mtri_per_s": round(world * tri_per_frame / (ms_per_step * 1e-3) / 1e6, 2),
         "frame_counters": per_frame,
         "frame_algorithmic_bytes": frame_bytes,
@@ -441,17 +451,23 @@ def time_steps(stream, flush, steps, body):
 
 
 def autotune_summary(best, table):
-    return {"best": best, "candidates_ms": {"%s hiz%d" % (c["bin"], c["hiz"]): round(ms, 3) for c, ms in table},
-            "how": "swgb_autotune: one warm-up and one CUDA-event-timed run per candidate, attachments restored between"}
+    return {"best": best,
+            "candidates_ms": {"%s hiz%d" % (c["bin"], c["hiz"]): {k: round(v, 3) for k, v in t.items()}
+                              for c, t in table},
+            "how": "swgb_autotune: one warm-up and %d runs per candidate, each timed alone with CUDA events, "
+                   "attachments restored between; lowest median wins" % DEFAULT_RUNS}
 
 
-def measure_batch(r, stream, flush, params, steps, warmup, per_draw_steps, dev, world=1, rank=0, tune=True):
+def measure_batch(r, stream, flush, params, steps, warmup, per_draw_steps, dev, world=1, rank=0, tune=True,
+                  pick_sample=0):
     """Batched vs per-draw on the atlas workload: one swgb_draw_batch call per
     step against one swgb_draw per draw, same draws, same kernels' work.  The
     batched arm runs the raster configuration the autotuner picks for the
     batch; the per-draw arm runs the faster of that one and the default (16x16
-    bins, depth rejection on), each timed.  On N ranks each rank draws its
-    longest-processing-time-first share."""
+    bins, depth rejection on).  With pick_sample = 0 each candidate is timed
+    on all draws; with pick_sample = S the candidates are compared on a seeded
+    sample of S draws and only the faster one is timed on all draws.  On N
+    ranks each rank draws its longest-processing-time-first share."""
     from swiftshader_gb300 import DeviceBatch, scenes, shard
     b = scenes.scene_batch(**params)
     if world > 1:
@@ -481,15 +497,30 @@ def measure_batch(r, stream, flush, params, steps, warmup, per_draw_steps, dev, 
     launches = r.launch_count() - l0
     cnt = r.counters()
     per_draw_ms = {}
+    sample_ms = {}
     if per_draw_steps:
+        import numpy as np
         shapes = [best] + ([{"bin": "16x16", "hiz": 1}] if best != {"bin": "16x16", "hiz": 1} else [])
+        key = lambda c: "%s hiz%d" % (c["bin"], c["hiz"])
+        if pick_sample and pick_sample < b.n:
+            sample = sorted(np.random.Generator(np.random.PCG64(11)).permutation(b.n)[:pick_sample].tolist())
+            for c in shapes:
+                w, h = (int(x) for x in c["bin"].split("x"))
+                r.set_raster_config(w, h, bool(c["hiz"]))
+                db.clear()
+                db.draw_each(r, sample)
+                r.synchronize()
+                ts = time_steps(stream, flush, 3, lambda: db.draw_each(r, sample))
+                sample_ms[key(c)] = round(statistics.median(ts), 3)
+            shapes = [min(shapes, key=lambda c: sample_ms[key(c)])]
         for c in shapes:
             w, h = (int(x) for x in c["bin"].split("x"))
             r.set_raster_config(w, h, bool(c["hiz"]))
-            per_draw()
-            r.synchronize()
+            if not sample_ms:
+                per_draw()
+                r.synchronize()
             tp = time_steps(stream, flush, per_draw_steps, per_draw)
-            per_draw_ms["%s hiz%d" % (c["bin"], c["hiz"])] = round(sum(tp) / len(tp), 3)
+            per_draw_ms[key(c)] = round(sum(tp) / len(tp), 3)
         w, h = (int(x) for x in best["bin"].split("x"))
         r.set_raster_config(w, h, bool(best["hiz"]))
     r.synchronize()
@@ -502,6 +533,9 @@ def measure_batch(r, stream, flush, params, steps, warmup, per_draw_steps, dev, 
                    "atlas_pages": b.pages, "page": b.page_size, "texture": "256^2 RGBA8 per draw, bilinear"},
         "batched_ms_per_step": round(mb, 3), "per_draw_ms_per_step": round(mp, 3) if per_draw_steps else None,
         "per_draw_ms_by_config": per_draw_ms or None,
+        "per_draw_pick": ({"sample_draws": pick_sample, "sample_ms_by_config": sample_ms,
+                           "how": "per-draw configurations compared on a seeded sample of draws (median of 3); "
+                                  "the faster one timed on all draws"} if sample_ms else None),
         "speedup_vs_per_draw": round(mp / mb, 2) if per_draw_steps else None,
         "draws_per_s": round(b.n / (mb * 1e-3), 1), "per_draw_draws_per_s": round(b.n / (mp * 1e-3), 1) if per_draw_steps else None,
         "gfrag_per_s": round(per_step["fragments_tested"] / (mb * 1e-3) / 1e9, 3),
@@ -610,7 +644,8 @@ def run_blitter(args):
         "metric": "GB/s", "value": mip["achieved_gbs"], "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": mip["ms"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u8 / f16 / f32 texels", "data": "synthetic (seeded generator)",
-        "config": {"workload": WORKLOADS["blitter"], "l2": "flushed before every timed step (256 MiB write)"},
+        "config": {"workload": WORKLOADS["blitter"]},
+        "l2": "flushed before every timed step (256 MiB write)",
         "blitter": res, "clocks": clk,
     }
     print(json.dumps(line), flush=True)
@@ -688,10 +723,10 @@ def run_batch(args):
         "data": "synthetic (seeded generator, swiftshader_gb300.scenes.scene_batch)",
         "config": {"workload": WORKLOADS["batch"] if params == BATCH_FULL else
                    "%d independent draws, triangle counts log-uniform in [%d, %d], otherwise as the 4096-draw atlas "
-                   "workload" % (params["n_draws"], params["tri_min"], params["tri_max"]),
-                   "l2": "flushed before every timed step (256 MiB write)",
-                   "parallelism": ("draws split over ranks, longest-processing-time-first on triangles x viewport "
-                                   "area; no collective") if world > 1 else "single GPU"},
+                   "workload" % (params["n_draws"], params["tri_min"], params["tri_max"])},
+        "l2": "flushed before every timed step (256 MiB write)",
+        "parallelism": ("draws split over ranks, longest-processing-time-first on triangles x viewport "
+                        "area; no collective") if world > 1 else "single GPU",
         "batched": res,
         "kernels": {k: {"avg_ms": v[0] / max(1, v[1]), "launches": v[1]} for k, v in kt.items()},
         "roofline": {"kernel": "k_raster_batch", "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
@@ -743,7 +778,7 @@ def cpu_baseline(args, scene, bounded_s=12.0, threads=None):
     while True:
         _, _, cnt = oracle.render(scene, threads)
         frames += 1
-        frags += cnt["fragments_tested"]
+        frags += cnt["fragments_passed"]
         if time.perf_counter() - t0 >= bounded_s:
             break
     dt = time.perf_counter() - t0
@@ -777,7 +812,7 @@ def run_reference(args):
         t0 = time.perf_counter()
         _, _, cnt = oracle.render(scene, threads)
         t.append(time.perf_counter() - t0)
-        frags += cnt["fragments_tested"]
+        frags += cnt["fragments_passed"]
     ms = 1e3 * sum(t) / len(t)
     value = frags / sum(t) / 1e9
     line = {
@@ -786,7 +821,9 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 + int32 fixed point (RGBA8 / D32F out)",
         "data": "synthetic (seeded generator, swiftshader_gb300.scenes)",
-        "config": {"workload": WORKLOADS[args.workload], "parallelism": "host threads"},
+        "config": {"workload": WORKLOADS[args.workload]},
+        "parallelism": "host threads",
+        "value_counts": "fragments passed (F_p: written after the depth test) per second",
         "cpu_baseline": {"value": round(value, 5), "unit": "Gfrag/s", "cores": threads, "kind": "port",
                          "sample": "one full frame per step; the CPU restatement of the reference draw path "
                                    "(reference JIT unbuildable here), %s" % platform.machine()},
@@ -844,7 +881,8 @@ def run_reference_batch(args, b, world, threads):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 + int32 fixed point (RGBA8 / D32F out)",
         "data": "synthetic (seeded generator, swiftshader_gb300.scenes.scene_batch)",
-        "config": {"workload": WORKLOADS["batch"], "parallelism": "host threads"},
+        "config": {"workload": WORKLOADS["batch"]},
+        "parallelism": "host threads",
         "cpu_baseline": {"value": round(value, 3), "unit": "draws/s", "cores": threads, "kind": "port",
                          "sample": "per step: " + vals[-1]["sample"]},
         "e2e": {"value": round(value, 3), "unit": "draws/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

@@ -427,19 +427,25 @@ swgb_status swgb_ctx_get_raster_config(swgb_ctx *ctx, swgb_raster_config *config
 /* Autotuner of the raster configuration.  No counterpart in the reference.
  * It runs the n draws (one swgb_draw_batch when batched != 0, else one
  * swgb_draw each) under every candidate configuration -- each supported bin
- * shape, with hiz on and off -- one untimed warm-up run and one run timed
- * with CUDA events on the context's stream per candidate, and sets the
- * context's configuration to the fastest.  The attachment bytes the draws
- * can touch are copied to a temporary device buffer first and restored
- * before every run, so on return the attachments hold the draws' result
- * exactly once (as one swgb_draw_batch / n swgb_draw calls would leave them).
- * The temporary buffer is as large as those attachment bytes; it is freed
- * before returning.  ms[] (room for SWGB_AUTOTUNE_CANDIDATES entries, may be
- * NULL) receives each candidate's time and candidates[] (may be NULL) the
- * candidates, in the same order.  Synchronises the context's stream. */
+ * shape, with hiz on and off -- one untimed warm-up run and then `runs` runs
+ * (0 = SWGB_AUTOTUNE_DEFAULT_RUNS; at most SWGB_AUTOTUNE_MAX_RUNS), each
+ * timed alone with CUDA events on the context's stream, and sets the
+ * context's configuration to the candidate with the lowest median.  The
+ * attachment bytes the draws can touch are copied to a temporary device
+ * buffer first and restored before every run, so on return the attachments
+ * hold the draws' result exactly once (as one swgb_draw_batch / n swgb_draw
+ * calls would leave them).  The temporary buffer is as large as those
+ * attachment bytes; it is freed before returning.  ms[], ms_min[] and
+ * ms_max[] (room for SWGB_AUTOTUNE_CANDIDATES entries each, any may be NULL)
+ * receive each candidate's median, fastest and slowest run, and
+ * candidates[] (may be NULL) the candidates, in the same order.
+ * Synchronises the context's stream. */
 #define SWGB_AUTOTUNE_CANDIDATES 6
+#define SWGB_AUTOTUNE_DEFAULT_RUNS 3
+#define SWGB_AUTOTUNE_MAX_RUNS 15
 swgb_status swgb_autotune(swgb_ctx *ctx, const swgb_pipeline_state *states, const swgb_draw_args *args, uint32_t n,
-                          int batched, swgb_raster_config *best, swgb_raster_config *candidates, double *ms);
+                          int batched, uint32_t runs, swgb_raster_config *best, swgb_raster_config *candidates,
+                          double *ms, double *ms_min, double *ms_max);
 
 /* --- The Blitter steps either side of a draw: clears, multisample resolves
  * and scaled blits (mip generation is one LINEAR blit per level), for the

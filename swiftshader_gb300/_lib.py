@@ -74,7 +74,8 @@ def load(path=None):
     L.swgb_ctx_get_raster_config.argtypes = [C.c_void_p, C.POINTER(abi.RasterConfig)]
     L.swgb_ctx_get_raster_config.restype = C.c_int
     L.swgb_autotune.argtypes = [C.c_void_p, C.POINTER(abi.PipelineState), C.POINTER(abi.DrawArgs), C.c_uint32, C.c_int,
-                                C.POINTER(abi.RasterConfig), C.POINTER(abi.RasterConfig), C.POINTER(C.c_double)]
+                                C.c_uint32, C.POINTER(abi.RasterConfig), C.POINTER(abi.RasterConfig),
+                                C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.swgb_autotune.restype = C.c_int
     L.swgb_clear.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(abi.Image), C.POINTER(abi.Rect)]
     L.swgb_clear.restype = C.c_int

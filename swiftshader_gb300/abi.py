@@ -168,6 +168,8 @@ class RasterConfig(C.Structure):
 
 BIN_SHAPES = ((16, 16), (32, 16), (32, 32))
 AUTOTUNE_CANDIDATES = 6
+AUTOTUNE_DEFAULT_RUNS = 3
+AUTOTUNE_MAX_RUNS = 15
 
 
 class Image(C.Structure):

@@ -1567,9 +1567,12 @@ swgb_status swgb_ctx_get_raster_config(swgb_ctx *ctx, swgb_raster_config *config
 }
 
 swgb_status swgb_autotune(swgb_ctx *ctx, const swgb_pipeline_state *states, const swgb_draw_args *args, uint32_t n, int batched,
-                          swgb_raster_config *best, swgb_raster_config *candidates, double *ms)
+                          uint32_t runs, swgb_raster_config *best, swgb_raster_config *candidates, double *ms, double *ms_min,
+                          double *ms_max)
 {
     if(!ctx || (n && (!states || !args))) return set_error(SWGB_INVALID_ARG, "null argument");
+    if(runs == 0) runs = SWGB_AUTOTUNE_DEFAULT_RUNS;
+    if(runs > SWGB_AUTOTUNE_MAX_RUNS) return set_error(SWGB_INVALID_ARG, "swgb_autotune: runs above SWGB_AUTOTUNE_MAX_RUNS");
     cudaSetDevice(ctx->device);
     // Validate every draw first (bake has no side effects), and collect the
     // attachment byte ranges the draws can touch: every row of every sample
@@ -1647,7 +1650,7 @@ swgb_status swgb_autotune(swgb_ctx *ctx, const swgb_pipeline_state *states, cons
         }
         return SWGB_OK;
     };
-    double t[SWGB_AUTOTUNE_CANDIDATES] = {};
+    double t[SWGB_AUTOTUNE_CANDIDATES] = {}, tMin[SWGB_AUTOTUNE_CANDIDATES] = {}, tMax[SWGB_AUTOTUNE_CANDIDATES] = {};
     int bestK = 0;
     do
     {
@@ -1669,22 +1672,30 @@ swgb_status swgb_autotune(swgb_ctx *ctx, const swgb_pipeline_state *states, cons
         for(int k = 0; k < SWGB_AUTOTUNE_CANDIDATES && s == SWGB_OK; k++)
         {
             ctx->rasterConfig = cands[k];
-            for(int rep = 0; rep < 2 && s == SWGB_OK; rep++)
+            double samples[SWGB_AUTOTUNE_MAX_RUNS];
+            // run 0 warms up (module load, scratch growth, graph capture);
+            // runs 1..runs are timed one at a time
+            for(uint32_t rep = 0; rep <= runs && s == SWGB_OK; rep++)
             {
                 if((s = restore()) != SWGB_OK) break;
                 // the counters end as one run of the draws left them
                 if((s = cuda_check(cudaMemcpyAsync(ctx->counters, cntSave, CTX_COUNTERS * sizeof(unsigned long long), cudaMemcpyDeviceToDevice,
                                                    ctx->stream), "autotune counters")) != SWGB_OK)
                     break;
-                if(rep == 1) cudaEventRecord(e0, ctx->stream);
+                if(rep > 0) cudaEventRecord(e0, ctx->stream);
                 if((s = run()) != SWGB_OK) break;
-                if(rep == 1) cudaEventRecord(e1, ctx->stream);
+                if(rep == 0) continue;
+                cudaEventRecord(e1, ctx->stream);
+                float el = 0.0f;
+                if((s = cuda_check(cudaEventSynchronize(e1), "autotune sync")) != SWGB_OK) break;
+                cudaEventElapsedTime(&el, e0, e1);
+                samples[rep - 1] = el;
             }
             if(s != SWGB_OK) break;
-            float el = 0.0f;
-            if((s = cuda_check(cudaEventSynchronize(e1), "autotune sync")) != SWGB_OK) break;
-            cudaEventElapsedTime(&el, e0, e1);
-            t[k] = el;
+            std::sort(samples, samples + runs);
+            t[k] = (runs & 1) ? samples[runs / 2] : 0.5 * (samples[runs / 2 - 1] + samples[runs / 2]);
+            tMin[k] = samples[0];
+            tMax[k] = samples[runs - 1];
             if(t[k] < t[bestK]) bestK = k;
         }
     } while(false);
@@ -1705,6 +1716,8 @@ swgb_status swgb_autotune(swgb_ctx *ctx, const swgb_pipeline_state *states, cons
     {
         if(candidates) candidates[k] = cands[k];
         if(ms) ms[k] = t[k];
+        if(ms_min) ms_min[k] = tMin[k];
+        if(ms_max) ms_max[k] = tMax[k];
     }
     return SWGB_OK;
 }

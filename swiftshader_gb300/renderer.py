@@ -67,17 +67,45 @@ class Renderer:
         check(self._L.swgb_ctx_get_raster_config(self._ctx, C.byref(cfg)), "swgb_ctx_get_raster_config")
         return cfg.as_dict()
 
-    def autotune(self, states, args, batched=True):
-        """Runs the draws under every raster configuration (swgb_autotune),
-        keeps the fastest on this renderer and returns (best, [(config, ms)])."""
+    def autotune(self, states, args, batched=True, runs=abi.AUTOTUNE_DEFAULT_RUNS, table=None):
+        """Picks the raster configuration for these draws and keeps it on this
+        renderer; returns (best, [(config, {"median", "min", "max"})]).
+
+        With a tuning.TuningTable that already holds the draws' workload class
+        the recorded configuration is set without running anything (the
+        returned list is then the recorded one, and the attachments are not
+        touched).  Otherwise swgb_autotune runs the draws under every
+        candidate (one warm-up and `runs` timed runs each, the lowest median
+        wins, the attachments left as one run leaves them) and the result is
+        recorded in the table when one is given."""
         n = len(states)
         S = states if isinstance(states, C.Array) else (abi.PipelineState * n)(*states)
         A = args if isinstance(args, C.Array) else (abi.DrawArgs * n)(*args)
+        key = None
+        if table is not None:
+            from .tuning import workload_class
+            key = workload_class(S, A, batched)
+            hit = table.get(key)
+            if hit is not None:
+                w, h = (int(x) for x in hit["bin"].split("x"))
+                self.set_raster_config(w, h, bool(hit["hiz"]))
+                cands = []
+                for name, t in hit["candidates_ms"].items():
+                    shape, hz = name.split(" hiz")
+                    cands.append(({"bin": shape, "hiz": int(hz)}, t))
+                return {"bin": hit["bin"], "hiz": int(hit["hiz"])}, cands
         best = abi.RasterConfig()
         cands = (abi.RasterConfig * abi.AUTOTUNE_CANDIDATES)()
         ms = (C.c_double * abi.AUTOTUNE_CANDIDATES)()
-        check(self._L.swgb_autotune(self._ctx, S, A, n, 1 if batched else 0, C.byref(best), cands, ms), "swgb_autotune")
-        return best.as_dict(), [(c.as_dict(), float(t)) for c, t in zip(cands, ms)]
+        lo = (C.c_double * abi.AUTOTUNE_CANDIDATES)()
+        hi = (C.c_double * abi.AUTOTUNE_CANDIDATES)()
+        check(self._L.swgb_autotune(self._ctx, S, A, n, 1 if batched else 0, int(runs), C.byref(best), cands, ms, lo, hi),
+              "swgb_autotune")
+        res = [(c.as_dict(), {"median": float(t), "min": float(a), "max": float(b)})
+               for c, t, a, b in zip(cands, ms, lo, hi)]
+        if table is not None:
+            table.record(key, best.as_dict(), res)
+        return best.as_dict(), res
 
     def counters(self):
         c = abi.Counters()
@@ -238,8 +266,8 @@ class DeviceBatch:
     def draw_batch(self, renderer):
         renderer.draw_batch(self.states, self.args)
 
-    def draw_each(self, renderer):
-        for i in range(self.batch.n):
+    def draw_each(self, renderer, indices=None):
+        for i in (range(self.batch.n) if indices is None else indices):
             renderer.draw(self.states[i], self.args[i])
 
     def view(self, i):

@@ -116,7 +116,7 @@ def test_host_side_errors_without_device(built_lib):
     assert b"provoking" in L.swgb_last_error()
     # raster configuration: validated on the host
     assert L.swgb_ctx_set_raster_config(None, None) == abi.INVALID_ARG
-    assert L.swgb_autotune(None, None, None, 0, 1, None, None, None) == abi.INVALID_ARG
+    assert L.swgb_autotune(None, None, None, 0, 1, 0, None, None, None, None, None) == abi.INVALID_ARG
     # Blitter entry points: null context / arguments rejected on the host
     img = abi.Image(None, abi.FORMAT_R8G8B8A8_UNORM, 4, 4, 1, 16, 64)
     assert L.swgb_clear(None, None, 0, C.byref(img), None) == abi.INVALID_ARG
@@ -130,4 +130,6 @@ def test_header_lists_the_bin_shapes():
     for w, h in abi.BIN_SHAPES:
         assert "%dx%d" % (w, h) in text
     assert "#define SWGB_AUTOTUNE_CANDIDATES %d" % abi.AUTOTUNE_CANDIDATES in text
+    assert "#define SWGB_AUTOTUNE_DEFAULT_RUNS %d" % abi.AUTOTUNE_DEFAULT_RUNS in text
+    assert "#define SWGB_AUTOTUNE_MAX_RUNS %d" % abi.AUTOTUNE_MAX_RUNS in text
     assert abi.AUTOTUNE_CANDIDATES == 2 * len(abi.BIN_SHAPES)

@@ -121,15 +121,26 @@ def test_autotune_leaves_one_run(gpu_lib, batched):
     db.clear()
     torch.cuda.synchronize()
     r.reset_counters()
-    best, table = r.autotune(db.states, db.args, batched=batched)
+    from swiftshader_gb300.tuning import TuningTable, workload_class
+    tt = TuningTable()
+    best, table = r.autotune(db.states, db.args, batched=batched, runs=3, table=tt)
     r.synchronize()
     assert len(table) == abi.AUTOTUNE_CANDIDATES
-    assert all(ms > 0.0 for _, ms in table)
-    assert best == min(table, key=lambda e: e[1])[0]
+    assert all(0.0 < t["min"] <= t["median"] <= t["max"] for _, t in table)
+    assert best == min(table, key=lambda e: e[1]["median"])[0]
     assert r.raster_config() == best
     assert_bit_exact(db.depth.cpu().numpy(), d1, "depth")
     assert_bit_exact(db.color.cpu().numpy(), c1, "color")
     assert r.counters() == k1
+    # a table hit sets the recorded configuration without running the draws
+    assert workload_class(db.states, db.args, batched) in tt
+    r2 = Renderer(0)
+    r2.set_raster_config(16, 16, True) if best != {"bin": "16x16", "hiz": 1} else r2.set_raster_config(32, 32, False)
+    before = db.depth.clone()
+    best2, _ = r2.autotune(db.states, db.args, batched=batched, table=tt)
+    torch.cuda.synchronize()
+    assert best2 == best and r2.raster_config() == best
+    assert torch.equal(db.depth, before)
 
 
 @pytest.mark.parametrize("cfg", [(16, 16, True), (16, 16, False), (32, 16, True)], ids=lambda c: "%dx%d-hiz%d" % c)
