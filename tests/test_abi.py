@@ -2,6 +2,8 @@
 header (compiled with gcc), the exported symbols of libswgb.so, and host-side
 error handling that needs no device."""
 import ctypes as C
+
+import numpy as np
 import os
 import subprocess
 import sys
@@ -94,9 +96,11 @@ def test_host_side_errors_without_device(built_lib):
         assert status == abi.NO_DEVICE
     assert L.swgb_draw(None, None, None) == abi.INVALID_ARG
     assert L.swgb_sync(None) == abi.INVALID_ARG
-    # the allocation-free draw validates sizes before touching any device
+    # the allocation-free draw validates sizes before touching any device;
+    # every buffer pointer is null, which the host's state validation rejects
+    # as well, so no kernel can launch on these states
     sc = scenes.scene_small(n_tris=4, width=16, height=16)
-    st = scenes.build_state(sc, 1 << 20, 1 << 20, 1 << 20)
+    st = scenes.build_state(sc, None, None, None)
     a = scenes.build_args(sc)
     a.count = 40000
     assert L.swgb_draw_noalloc(C.byref(st), C.byref(a), None) == abi.INVALID_ARG
@@ -104,15 +108,24 @@ def test_host_side_errors_without_device(built_lib):
     # primitive restart runs only through swgb_draw: the batched and
     # allocation-free paths refuse it on the host
     rs = scenes.restart_scene(abi.TOPOLOGY_TRIANGLE_STRIP, n_indices=64)
-    rst = scenes.build_state(rs, 1 << 20, 1 << 20, 1 << 20)
-    ra = scenes.build_args(rs, 1 << 20)
+    rst = scenes.build_state(rs, None, None, None)
+    ra = scenes.build_args(rs, None)
     assert L.swgb_draw_noalloc(C.byref(rst), C.byref(ra), None) == abi.UNSUPPORTED_STATE
+    # swgb_plan_batch never launches anything (it only compares the byte
+    # ranges draws touch), so it gets real host buffers of the right sizes
+    cbuf, dbuf = scenes.clear_buffers(rs)
+    vbuf = np.ascontiguousarray(rs.vertices, np.float32)
+    ibuf = np.ascontiguousarray(rs.indices)
+    pst = scenes.build_state(rs, cbuf.ctypes.data, dbuf.ctypes.data, vbuf.ctypes.data)
+    pa = scenes.build_args(rs, ibuf.ctypes.data)
     segs = C.c_uint32()
-    assert L.swgb_plan_batch(C.byref(rst), C.byref(ra), 1, None, C.byref(segs)) == abi.UNSUPPORTED_STATE
-    ra.restart_index_count = 0
-    ra.count = 4
-    rst.provoking_vertex = 2
-    assert L.swgb_draw_noalloc(C.byref(rst), C.byref(ra), None) == abi.INVALID_ARG
+    assert L.swgb_plan_batch(C.byref(pst), C.byref(pa), 1, None, C.byref(segs)) == abi.UNSUPPORTED_STATE
+    # an out-of-range provoking-vertex mode fails the state validation every
+    # entry point shares (checked through the host-only planner)
+    pa.restart_index_count = 0
+    pa.count = 4
+    pst.provoking_vertex = 2
+    assert L.swgb_plan_batch(C.byref(pst), C.byref(pa), 1, None, C.byref(segs)) == abi.INVALID_ARG
     assert b"provoking" in L.swgb_last_error()
     # raster configuration: validated on the host
     assert L.swgb_ctx_set_raster_config(None, None) == abi.INVALID_ARG

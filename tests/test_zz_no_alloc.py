@@ -69,9 +69,7 @@ def test_noalloc_full_pipeline_draw(gpu_lib):
 def test_noalloc_rejects_oversized_draws(gpu_lib):
     L = gpu_lib
     sc = scenes.scene_small(n_tris=8, width=32, height=32)
-    st = abi.PipelineState()
-    a = abi.DrawArgs()
-    st = scenes.build_state(sc, 1 << 20, 1 << 20, 1 << 20)  # never dereferenced: rejected first
+    st = scenes.build_state(sc, None, None, None)  # null buffers: the host rejects the state too
     a = scenes.build_args(sc)
     a.count = 32769
     assert L.swgb_draw_noalloc(C.byref(st), C.byref(a), None) == abi.INVALID_ARG
