@@ -203,8 +203,14 @@ def run_ours(args):
             dist.barrier()
 
     # raster configuration chosen by the library's autotuner on this frame
+    # (or fixed by --raster-config)
     tune = None
-    if not args.no_autotune:
+    if args.raster_config:
+        wh, hz = args.raster_config.split(":")
+        w, h = (int(x) for x in wh.split("x"))
+        r.set_raster_config(w, h, bool(int(hz)))
+        tune = {"best": r.raster_config(), "how": "fixed by --raster-config"}
+    elif not args.no_autotune:
         ds.clear()
         tune = autotune_summary(*r.autotune([st], [a], batched=False))
 
@@ -903,6 +909,7 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint / forward timings")
     ap.add_argument("--no-blitter", action="store_true", help="skip the clear / resolve / mip-chain timings")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default raster configuration (16x16 bins, hiz on)")
+    ap.add_argument("--raster-config", default=None, help="fix the raster configuration, e.g. 16x16:0 (bins, hiz); no autotuning")
     ap.add_argument("--batch-draws", type=int, default=BATCH_FULL["n_draws"], help="--workload batch: draws")
     ap.add_argument("--batch-tri-max", type=int, default=BATCH_FULL["tri_max"], help="--workload batch: largest draw")
     ap.add_argument("--no-per-draw", action="store_true", help="--workload batch: skip the per-draw comparison")

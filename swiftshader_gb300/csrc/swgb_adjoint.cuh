@@ -70,7 +70,7 @@ struct AdjRegion {
 template<int MS>
 struct __align__(16) AdjShared {  // 16: the warps' copies sit back to back
     float depth[MS][BIN * BIN];  // replayed depth
-    float plane[PLANES][BATCH];
+    float4 planeA[BATCH][PLANES_STORED / 4];
     uint32_t span[BATCH][MS][BIN];
     int16_t qx0[BATCH][BIN / 2];
     uint16_t qpre[BATCH][BIN / 2 + 1];

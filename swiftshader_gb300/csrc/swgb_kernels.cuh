@@ -23,9 +23,9 @@ constexpr int BIN = 16;          // bin side in pixels; one warp owns one bin
 constexpr int RASTER_WARPS = 4;  // independent warps (bins) per raster block
 constexpr int RASTER_THREADS = 32 * RASTER_WARPS;
 constexpr int BATCH = 32;        // triangles staged per batch: one per lane
-constexpr int SUPER = 32;        // chunks per super-chunk box
+constexpr int SUPER = 64;        // chunks per super-chunk box
 constexpr int SETUP_THREADS = 256;
-constexpr int CHUNK = 64;        // triangles per chunk box
+constexpr int CHUNK = 32;        // triangles per chunk box (one setup warp)
 constexpr int MAX_POLY = 16;     // clipped polygon capacity (Polygon::B, src/Device/Polygon.hpp:45)
 
 // Bin shapes the raster kernels are built for (width x height in pixels); the
@@ -626,7 +626,6 @@ constexpr int PLANE_ZBIAS = 8 + 3 * PLANE_V;  // the triangle's depth bias (Prim
 constexpr int PLANES = PLANE_ZBIAS + 1;
 constexpr int PLANES_STORED = 28;  // PLANES rounded up to whole float4s
 
-__device__ __forceinline__ uint32_t select3(int o, uint32_t a, uint32_t b, uint32_t c) { return o == 0 ? a : (o == 1 ? b : c); }
 
 __device__ __forceinline__ float vary(const float4 &a, const float4 &b, int k)
 {
@@ -643,26 +642,31 @@ __device__ __forceinline__ float vary(const float4 &a, const float4 &b, int k)
     }
 }
 
-// Plane equations of triangle t from its post-transform vertices
-// (SetupRoutine.cpp:270-548): x0, y0 of the rotated first vertex, z (A, B, C),
-// w (A, B, C) and each varying (A, B, C), PLANES floats, unused ones zero.
-// The setup stage evaluates them once per triangle; the raster stage loads them
-// for every bin the triangle touches.
-__device__ __forceinline__ void triangle_planes(const DrawParams &D, uint32_t t, float p[PLANES_STORED])
+// Plane equations of a triangle (SetupRoutine.cpp:270-548) from its three
+// post-transform vertex records, v[k] = float4 k of the vertex (k = 0: clip
+// position, 1: X, Y, flags, projected z, 2: rhw + varyings 0-2, 3: varyings
+// 3-6): x0, y0 of the rotated first vertex, z (A, B, C), w (A, B, C) and each
+// varying (A, B, C), PLANES floats, unused ones zero.  The setup stage
+// evaluates them once per triangle; the raster stage loads them for every bin
+// the triangle touches.
+__device__ __forceinline__ float4 select3(int o, const float4 &a, const float4 &b, const float4 &c)
+{
+    return o == 0 ? a : (o == 1 ? b : c);
+}
+
+__device__ __forceinline__ void triangle_planes(const DrawParams &D, const float4 c[3], const float4 p[3], const float4 a[3],
+                                                const float4 b[3], float pl[PLANES_STORED])
 {
 #pragma unroll
-    for(int k = 0; k < PLANES_STORED; k++) p[k] = 0.0f;
-    uint32_t i0, i1, i2;
-    tri_slots(D, t, i0, i1, i2);
-    const float4 c0 = D.ptv[(size_t)i0 * 4], c1 = D.ptv[(size_t)i1 * 4], c2 = D.ptv[(size_t)i2 * 4];
+    for(int k = 0; k < PLANES_STORED; k++) pl[k] = 0.0f;
     // sort by minimum y, then maximum w (SetupRoutine.cpp:270-294)
     int o0 = 0, o1 = 1, o2 = 2, tt;
     {
-        float ym = rmin(rmin(c0.y, c1.y), c2.y);
-        if(ym == c1.y) { tt = o0; o0 = o1; o1 = o2; o2 = tt; }
-        if(ym == c2.y) { tt = o2; o2 = o1; o1 = o0; o0 = tt; }
+        float ym = rmin(rmin(c[0].y, c[1].y), c[2].y);
+        if(ym == c[1].y) { tt = o0; o0 = o1; o1 = o2; o2 = tt; }
+        if(ym == c[2].y) { tt = o2; o2 = o1; o1 = o0; o0 = tt; }
     }
-    const float cw0 = c0.w, cw1 = c1.w, cw2 = c2.w;
+    const float cw0 = c[0].w, cw1 = c[1].w, cw2 = c[2].w;
     {
         float w0 = o0 == 0 ? cw0 : (o0 == 1 ? cw1 : cw2);
         float w1 = o1 == 0 ? cw0 : (o1 == 1 ? cw1 : cw2);
@@ -671,26 +675,25 @@ __device__ __forceinline__ void triangle_planes(const DrawParams &D, uint32_t t,
         if(wm == w1) { tt = o0; o0 = o1; o1 = o2; o2 = tt; }
         if(wm == w2) { tt = o2; o2 = o1; o1 = o0; o0 = tt; }
     }
-    const uint32_t j0 = select3(o0, i0, i1, i2), j1 = select3(o1, i0, i1, i2), j2 = select3(o2, i0, i1, i2);
     const float w1 = o1 == 0 ? cw0 : (o1 == 1 ? cw1 : cw2);
     const float w2 = o2 == 0 ? cw0 : (o2 == 1 ? cw1 : cw2);
-    const float4 P0 = D.ptv[(size_t)j0 * 4 + 1], P1 = D.ptv[(size_t)j1 * 4 + 1], P2 = D.ptv[(size_t)j2 * 4 + 1];
-    const float4 A0 = D.ptv[(size_t)j0 * 4 + 2], A1 = D.ptv[(size_t)j1 * 4 + 2], A2 = D.ptv[(size_t)j2 * 4 + 2];
+    const float4 P0 = select3(o0, p[0], p[1], p[2]), P1 = select3(o1, p[0], p[1], p[2]), P2 = select3(o2, p[0], p[1], p[2]);
+    const float4 A0 = select3(o0, a[0], a[1], a[2]), A1 = select3(o1, a[0], a[1], a[2]), A2 = select3(o2, a[0], a[1], a[2]);
     const float rhw0 = A0.x;
     int32_t X0 = __float_as_int(P0.x), X1 = __float_as_int(P1.x), X2 = __float_as_int(P2.x);
     int32_t Y0 = __float_as_int(P0.y), Y1 = __float_as_int(P1.y), Y2 = __float_as_int(P2.y);
     const float inv = 1.0f / 256.0f;
-    p[0] = (float)X0 * inv;
-    p[1] = (float)Y0 * inv;
+    pl[0] = (float)X0 * inv;
+    pl[1] = (float)Y0 * inv;
     X1 -= X0; Y1 -= Y0; X2 -= X0; Y2 -= Y0;
     float x1 = (w1 * inv) * (float)X1, y1 = (w1 * inv) * (float)Y1;
     float x2 = (w2 * inv) * (float)X2, y2 = (w2 * inv) * (float)Y2;
-    float a = x1 * y2 - x2 * y1;
+    float ar = x1 * y2 - x2 * y1;
     float M0x = 0.0f, M0y = 0.0f, M1x = 0.0f, M1y = 0.0f, M2x = 0.0f, M2y = 0.0f;
     const float M0z = rhw0, M1z = 0.0f, M2z = 0.0f;
-    if(a != 0.0f)
+    if(ar != 0.0f)
     {
-        float A = 1.0f / a;
+        float A = 1.0f / ar;
         float Dd = A * rhw0;
         M0x = (y1 * w2 - y2 * w1) * Dd;
         M0y = (x2 * w1 - x1 * w2) * Dd;
@@ -699,18 +702,18 @@ __device__ __forceinline__ void triangle_planes(const DrawParams &D, uint32_t t,
         M2x = (-y1) * A;
         M2y = x1 * A;
     }
-    p[5] = (M0x + M1x) + M2x;
-    p[6] = (M0y + M1y) + M2y;
-    p[7] = (M0z + M1z) + M2z;
+    pl[5] = (M0x + M1x) + M2x;
+    pl[6] = (M0y + M1y) + M2y;
+    pl[7] = (M0z + M1z) + M2z;
     if(D.depthTest)
     {
         float z0 = P0.w, z1 = P1.w - z0, z2 = P2.w - z0;
         float fx1 = (float)X1 * inv, fy1 = (float)Y1 * inv;
         float fx2 = (float)X2 * inv, fy2 = (float)Y2 * inv;
         float Dz = D.depthRange / (fx1 * fy2 - fx2 * fy1);
-        p[2] = (fy2 * z1 - fy1 * z2) * Dz;
-        p[3] = (fx1 * z2 - fx2 * z1) * Dz;
-        p[4] = z0 * D.depthRange + D.depthNear;
+        pl[2] = (fy2 * z1 - fy1 * z2) * Dz;
+        pl[3] = (fx1 * z2 - fx2 * z1) * Dz;
+        pl[4] = z0 * D.depthRange + D.depthNear;
         // depth bias (SetupRoutine.cpp:417-476)
         if(D.biasConstant != 0.0f || D.biasSlope != 0.0f)
         {
@@ -723,34 +726,213 @@ __device__ __forceinline__ void triangle_planes(const DrawParams &D, uint32_t t,
                 {
                     // 2^(e - 23), e the largest exponent of the depths; the
                     // reference forms Z1, Z2 from the vertex differences
-                    const float Z0 = p[4], Z1 = z1 * D.depthRange + D.depthNear, Z2 = z2 * D.depthRange + D.depthNear;
+                    const float Z0 = pl[4], Z1 = z1 * D.depthRange + D.depthNear, Z2 = z2 * D.depthRange + D.depthNear;
                     const int e = max(max(__float_as_int(Z0) & 0x7F800000, __float_as_int(Z1) & 0x7F800000),
                                       __float_as_int(Z2) & 0x7F800000);
                     r = __int_as_float(e) * (1.0f / (1 << 23));
                 }
                 bias = r * D.biasConstant;
             }
-            if(D.biasSlope != 0.0f) bias += rmax(fabsf(p[2]), fabsf(p[3])) * D.biasSlope;
+            if(D.biasSlope != 0.0f) bias += rmax(fabsf(pl[2]), fabsf(pl[3])) * D.biasSlope;
             if(D.biasClamp != 0.0f) bias = D.biasClamp > 0.0f ? rmin(bias, D.biasClamp) : rmax(bias, D.biasClamp);
-            p[PLANE_ZBIAS] = bias;
+            pl[PLANE_ZBIAS] = bias;
         }
     }
-    float4 B0 = make_float4(0, 0, 0, 0), B1 = B0, B2 = B0;
-    if(D.nv > 3)
-    {
-        B0 = D.ptv[(size_t)j0 * 4 + 3]; B1 = D.ptv[(size_t)j1 * 4 + 3]; B2 = D.ptv[(size_t)j2 * 4 + 3];
-    }
+    const float4 B0 = select3(o0, b[0], b[1], b[2]), B1 = select3(o1, b[0], b[1], b[2]), B2 = select3(o2, b[0], b[1], b[2]);
 #pragma unroll
     for(int k = 0; k < PLANE_V; k++)
     {
         if(k >= D.nv) break;
         float v0 = vary(A0, B0, k), v1 = vary(A1, B1, k), v2 = vary(A2, B2, k);
-        p[8 + 3 * k + 0] = (v0 * M0x + v1 * M1x) + v2 * M2x;
-        p[8 + 3 * k + 1] = (v0 * M0y + v1 * M1y) + v2 * M2y;
-        p[8 + 3 * k + 2] = (v0 * M0z + v1 * M1z) + v2 * M2z;
+        pl[8 + 3 * k + 0] = (v0 * M0x + v1 * M1x) + v2 * M2x;
+        pl[8 + 3 * k + 1] = (v0 * M0y + v1 * M1y) + v2 * M2y;
+        pl[8 + 3 * k + 2] = (v0 * M0z + v1 * M1z) + v2 * M2z;
     }
 }
 
+// Clipped triangle (rare; out of line, its polygon arrays live in local
+// memory): Clipper::Clip, the reprojection of the clipped polygon
+// (SetupRoutine.cpp:125-145), its y range (:147-186) and x extent; a visible
+// polygon is stored in the draw's polygon scratch for the span stage and the
+// raster's edge walk.  Returns the vertex count (0: clipped away or empty y
+// range; -1: polygon scratch full).
+static __device__ __noinline__ int setup_clipped(const DrawParams &D, const float4 c0, const float4 c1, const float4 c2, int flagsOr,
+                                                 int32_t &yMin, int32_t &yMax, int32_t &xMinS, int32_t &xMaxS, uint32_t &slot)
+{
+    CVert P[MAX_POLY];
+    P[0] = {c0.x, c0.y, c0.z, c0.w};
+    P[1] = {c1.x, c1.y, c1.z, c1.w};
+    P[2] = {c2.x, c2.y, c2.z, c2.w};
+    const int n = clip_polygon(P, 3, flagsOr);
+    if(n < 3) return 0;
+    int32_t X[MAX_POLY], Y[MAX_POLY];
+    for(int i = 0; i < n; i++)
+    {
+        float w = P[i].w;
+        float rhw = w != 0.0f ? 1.0f / w : 1.0f;
+        X[i] = round_int(D.X0xF + (P[i].x * rhw) * D.WxF);
+        Y[i] = round_int(D.Y0xF + (P[i].y * rhw) * D.HxF);
+    }
+    yMin = Y[0]; yMax = Y[0]; xMinS = X[0]; xMaxS = X[0];
+    for(int i = 1; i < n; i++)
+    {
+        yMin = min(yMin, Y[i]); yMax = max(yMax, Y[i]);
+        xMinS = min(xMinS, X[i]); xMaxS = max(xMaxS, X[i]);
+    }
+    if(D.ms > 1)
+    {
+        yMin = max((yMin + Y_MIN_MS_OFFSET) >> 8, D.sy0);
+        yMax = min((yMax + Y_MAX_MS_OFFSET) >> 8, D.sy1);
+    }
+    else
+    {
+        yMin = max((yMin + 0xFF) >> 8, D.sy0);
+        yMax = min((yMax + 0xFF) >> 8, D.sy1);
+    }
+    if(yMin >= yMax) return 0;
+    slot = atomicAdd(D.polyCount, 1u);
+    if(slot >= D.polyCapacity)
+    {
+        atomicOr(D.error, ERR_POLY_OVERFLOW);
+        return -1;
+    }
+    for(int i = 0; i < n; i++) D.poly[(size_t)slot * MAX_POLY + i] = make_int2(X[i], Y[i]);
+    return n;
+}
+
+// Span rows of a stored clipped polygon (write_spans per sample, rows
+// [yMin, yMax)), and for one sample the trimmed range (SetupRoutine.cpp:243-264).
+static __device__ __noinline__ void spans_clipped(const DrawParams &D, uint32_t slot, int n, int dW, int32_t yMin, int32_t yMax,
+                                                  uint32_t *sp, int32_t &tMin, int32_t &tMax)
+{
+    int32_t X[MAX_POLY], Y[MAX_POLY];
+    for(int i = 0; i < n; i++)
+    {
+        const int2 q = D.poly[(size_t)slot * MAX_POLY + i];
+        X[i] = q.x; Y[i] = q.y;
+    }
+    const uint32_t rows = (uint32_t)(yMax - yMin);
+    tMin = yMin;
+    tMax = yMax;
+    if(D.ms > 1)
+    {
+        // one outline per sample, the polygon shifted by -Xf/-Yf; rows no edge
+        // writes stay empty and nothing is trimmed (SetupRoutine.cpp:188-240)
+        for(int q = 0; q < 4; q++)
+        {
+            uint32_t *s = sp + (uint64_t)q * rows;
+            for(uint32_t r = 0; r < rows; r++) s[r] = 0u;
+            int32_t Xq[MAX_POLY], Yq[MAX_POLY];
+            for(int i = 0; i < n; i++) { Xq[i] = X[i] - XF[q]; Yq[i] = Y[i] - YF[q]; }
+            write_spans(D, Xq, Yq, n, dW, yMin, s);
+        }
+        return;
+    }
+    write_spans(D, X, Y, n, dW, yMin, sp);
+    while(tMin < tMax)
+    {
+        const uint32_t s = sp[tMin - yMin];
+        if((s & 0xFFFFu) != (s >> 16)) break;
+        tMin++;
+    }
+    while(tMax > tMin)
+    {
+        const uint32_t s = sp[tMax - 1 - yMin];
+        if((s & 0xFFFFu) != (s >> 16)) break;
+        tMax--;
+    }
+}
+
+// Trimmed y range of a clipped polygon whose rows did not fit the span
+// scratch, by direct evaluation (k_raster then walks its edges itself).
+static __device__ __noinline__ void trim_clipped_unstored(const DrawParams &D, uint32_t slot, int n, int dW, int32_t &yMin, int32_t &yMax)
+{
+    int32_t X[MAX_POLY], Y[MAX_POLY];
+    for(int i = 0; i < n; i++)
+    {
+        const int2 q = D.poly[(size_t)slot * MAX_POLY + i];
+        X[i] = q.x; Y[i] = q.y;
+    }
+    int32_t l, r;
+    while(yMin < yMax)
+    {
+        span_at(D, X, Y, n, dW, yMin, l, r);
+        if(l != r) break;
+        yMin++;
+    }
+    while(yMax > yMin)
+    {
+        span_at(D, X, Y, n, dW, yMax - 1, l, r);
+        if(l != r) break;
+        yMax--;
+    }
+}
+
+// Span rows [yMin, yMax) of an unclipped triangle (X, Y snapped vertices,
+// shifted by the sample offset for 4x MSAA), row by row: each row's left and
+// right come from the edges covering it, walked by the reference's DDA
+// (SetupRoutine::edge, :550-621), and are stored as one word.  A triangle's
+// edges on one side cover disjoint rows, so this equals the reference's
+// edge-by-edge outline.  Rows no edge covers get the empty span 0 (only
+// sample outlines of 4x MSAA have them).  Returns the first and one past the
+// last row with left != right (the trim of :243-264; first = last = yMax when
+// every row is empty).
+__device__ __forceinline__ void spans_triangle(const DrawParams &D, int32_t X0, int32_t Y0, int32_t X1, int32_t Y1, int32_t X2,
+                                               int32_t Y2, int dW, int32_t yMin, int32_t yMax, uint32_t *sp, int32_t &first,
+                                               int32_t &last)
+{
+    // edges in the reference's order: edge i runs from vertex i+1-d to vertex i+d
+    EdgeDDA e[3];
+    bool ok[3];
+    int32_t ex[3], ed[3];
+    {
+        const int32_t Xs[3] = {X0, X1, X2}, Ys[3] = {Y0, Y1, Y2};
+#pragma unroll
+        for(int i = 0; i < 3; i++)
+        {
+            int ia = i + 1 - dW, ib = i + dW;
+            ia = ia == 3 ? 0 : ia;
+            ib = ib == 3 ? 0 : ib;
+            ok[i] = edge_setup(D, Xs[ia], Ys[ia], Xs[ib], Ys[ib], e[i]);
+            ex[i] = 0;
+            ed[i] = 0;
+            if(ok[i]) ex[i] = edge_x_at(e[i], e[i].yMin, &ed[i]);
+        }
+    }
+    first = yMax;
+    last = yMax;
+    int32_t lastNonEmpty = yMin - 1;
+    for(int32_t y = yMin; y < yMax; y++)
+    {
+        int32_t l = 0, r = 0;
+#pragma unroll
+        for(int i = 0; i < 3; i++)
+        {
+            if(ok[i] && y >= e[i].yMin && y < e[i].yMax)
+            {
+                const int32_t x = clamp_x(D, ex[i]);
+                if(e[i].right) r = x; else l = x;
+                ex[i] += e[i].Q;
+                ed[i] += e[i].R;
+                const int32_t of = (-ed[i]) >> 31;
+                ed[i] -= e[i].D & of;
+                ex[i] -= of;
+            }
+        }
+        sp[y - yMin] = (uint32_t)(l & 0xFFFF) | ((uint32_t)r << 16);
+        if(l != r)
+        {
+            if(first == yMax) first = y;
+            lastNonEmpty = y;
+        }
+    }
+    if(first < yMax) last = lastNonEmpty + 1;
+}
+
+// One SETUP_THREADS-triangle block of a draw (block index 'blk' within the
+// draw), one thread per triangle: trivial reject, culling, clipping, y range,
+// span rows (allocated per warp), pixel box, record and plane equations; per
+// warp the chunk box, the super-chunk box and the counters.  No block barrier.
 __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
 {
     const uint32_t t = blk * SETUP_THREADS + threadIdx.x;
@@ -760,74 +942,53 @@ __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
     int cntIn = 0, cntClip = 0, cntVis = 0;
     bool cand = false;
     int n = 3, dW = 1, frontBit = 0;
-    int32_t X[MAX_POLY + 1], Y[MAX_POLY + 1];
+    int32_t X0 = 0, X1 = 0, X2 = 0, Y0 = 0, Y1 = 0, Y2 = 0;
     int32_t yMin = 0, yMax = 0, xMinS = 0, xMaxS = 0;
+    uint32_t slot = 0, vs0 = 0, vs1 = 0, vs2 = 0;  // post-transform vertex slots
     if(t < D.count && tri_valid(D, t))
     {
         cntIn = 1;
-        uint32_t i0, i1, i2;
+        tri_slots(D, t, vs0, vs1, vs2);
         bool ok = true;
-        tri_slots(D, t, i0, i1, i2);
-        if(D.indexType != SWGB_INDEX_TYPE_NONE && (i0 >= D.vertexCount || i1 >= D.vertexCount || i2 >= D.vertexCount))
+        if(D.indexType != SWGB_INDEX_TYPE_NONE && (vs0 >= D.vertexCount || vs1 >= D.vertexCount || vs2 >= D.vertexCount))
         {
             atomicOr(D.error, ERR_INDEX_RANGE);
             ok = false;
         }
         if(ok)
         {
-            const float4 p0 = D.ptv[(size_t)i0 * 4 + 1], p1 = D.ptv[(size_t)i1 * 4 + 1], p2 = D.ptv[(size_t)i2 * 4 + 1];
-            const int f0 = __float_as_int(p0.z), f1 = __float_as_int(p1.z), f2 = __float_as_int(p2.z);
-            X[0] = __float_as_int(p0.x); X[1] = __float_as_int(p1.x); X[2] = __float_as_int(p2.x);
-            Y[0] = __float_as_int(p0.y); Y[1] = __float_as_int(p1.y); Y[2] = __float_as_int(p2.y);
+            float4 vp[3], vc[3];
+            vp[0] = D.ptv[(size_t)vs0 * 4 + 1]; vp[1] = D.ptv[(size_t)vs1 * 4 + 1]; vp[2] = D.ptv[(size_t)vs2 * 4 + 1];
+            vc[0] = D.ptv[(size_t)vs0 * 4]; vc[1] = D.ptv[(size_t)vs1 * 4]; vc[2] = D.ptv[(size_t)vs2 * 4];
+            const int f0 = __float_as_int(vp[0].z), f1 = __float_as_int(vp[1].z), f2 = __float_as_int(vp[2].z);
+            X0 = __float_as_int(vp[0].x); X1 = __float_as_int(vp[1].x); X2 = __float_as_int(vp[2].x);
+            Y0 = __float_as_int(vp[0].y); Y1 = __float_as_int(vp[1].y); Y2 = __float_as_int(vp[2].y);
             // setupSolidTriangles trivial reject (src/Device/Renderer.cpp:749-765)
             if((f0 & f1 & f2) == CLIP_FINITE)
             {
-                const float4 c0 = D.ptv[(size_t)i0 * 4], c1 = D.ptv[(size_t)i1 * 4], c2 = D.ptv[(size_t)i2 * 4];
                 const int flagsOr = f0 | f1 | f2;
-                bool keep = true;
-                CVert P[MAX_POLY];
-                if(flagsOr != CLIP_FINITE)
-                {
-                    cntClip = 1;
-                    P[0] = {c0.x, c0.y, c0.z, c0.w};
-                    P[1] = {c1.x, c1.y, c1.z, c1.w};
-                    P[2] = {c2.x, c2.y, c2.z, c2.w};
-                    n = clip_polygon(P, 3, flagsOr);
-                    keep = n >= 3;
-                }
-                if(keep)
-                {
-                    // Culling (SetupRoutine.cpp:73-120)
-                    float x0 = (float)X[0], x1 = (float)X[1], x2 = (float)X[2];
-                    float y0 = (float)Y[0], y1 = (float)Y[1], y2 = (float)Y[2];
-                    float A = ((y0 - y2) * x1 + (y2 - y1) * x0) + (y1 - y0) * x2;
-                    int32_t w0w1w2 = __float_as_int(c0.w) ^ __float_as_int(c1.w) ^ __float_as_int(c2.w);
-                    if(w0w1w2 < 0) A = -A;
-                    bool front = D.frontFace == SWGB_FRONT_FACE_COUNTER_CLOCKWISE ? (A >= 0.0f) : (A <= 0.0f);
-                    frontBit = front ? 1 : 0;
-                    if((D.cullMode & SWGB_CULL_FRONT) && front) keep = false;
-                    if((D.cullMode & SWGB_CULL_BACK) && !front) keep = false;
-                    dW = A > 0.0f ? 1 : 0;
-                }
+                cntClip = flagsOr != CLIP_FINITE;  // the triangle goes through the clipper (Renderer.cpp:758-765)
+                // Culling (SetupRoutine.cpp:73-120) on the triangle's own snapped
+                // vertices; it rejects a triangle the same whether or not the
+                // clipper ran first.
+                float x0 = (float)X0, x1 = (float)X1, x2 = (float)X2;
+                float y0 = (float)Y0, y1 = (float)Y1, y2 = (float)Y2;
+                float A = ((y0 - y2) * x1 + (y2 - y1) * x0) + (y1 - y0) * x2;
+                int32_t w0w1w2 = __float_as_int(vc[0].w) ^ __float_as_int(vc[1].w) ^ __float_as_int(vc[2].w);
+                if(w0w1w2 < 0) A = -A;
+                bool front = D.frontFace == SWGB_FRONT_FACE_COUNTER_CLOCKWISE ? (A >= 0.0f) : (A <= 0.0f);
+                frontBit = front ? 1 : 0;
+                bool keep = !((D.cullMode & SWGB_CULL_FRONT) && front) && !((D.cullMode & SWGB_CULL_BACK) && !front);
+                dW = A > 0.0f ? 1 : 0;
                 if(keep && cntClip)
                 {
-                    // reproject the clipped polygon (SetupRoutine.cpp:125-145)
-                    for(int i = 0; i < n; i++)
-                    {
-                        float w = P[i].w;
-                        float rhw = w != 0.0f ? 1.0f / w : 1.0f;
-                        X[i] = round_int(D.X0xF + (P[i].x * rhw) * D.WxF);
-                        Y[i] = round_int(D.Y0xF + (P[i].y * rhw) * D.HxF);
-                    }
+                    n = setup_clipped(D, vc[0], vc[1], vc[2], flagsOr, yMin, yMax, xMinS, xMaxS, slot);
+                    cand = n >= 3;
                 }
-                if(keep)
+                else if(keep)
                 {
-                    yMin = Y[0]; yMax = Y[0]; xMinS = X[0]; xMaxS = X[0];
-                    for(int i = 1; i < n; i++)
-                    {
-                        yMin = min(yMin, Y[i]); yMax = max(yMax, Y[i]);
-                        xMinS = min(xMinS, X[i]); xMaxS = max(xMaxS, X[i]);
-                    }
+                    yMin = min(min(Y0, Y1), Y2); yMax = max(max(Y0, Y1), Y2);
+                    xMinS = min(min(X0, X1), X2); xMaxS = max(max(X0, X1), X2);
                     // Vertical range (SetupRoutine.cpp:147-186)
                     if(D.ms > 1)
                     {
@@ -846,8 +1007,6 @@ __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
     }
 
     // ---- allocate span rows: warp scan + one atomic per warp -------------
-    // (no block barrier: warps that clip nothing go on to their span rows and
-    // planes while a clipping warp of the block is still busy)
     const uint32_t rows = cand ? (uint32_t)(yMax - yMin) : 0u;
     uint32_t incl = rows * (uint32_t)D.ms;
 #pragma unroll
@@ -862,105 +1021,85 @@ __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
     const uint64_t off = (uint64_t)warpBase + (incl - rows * (uint32_t)D.ms);
 
     bool stored = false;
-    if(cand && D.ms > 1)
+    if(cand)
     {
-        // 4x MSAA: one outline per sample, the polygon shifted by -Xf/-Yf
-        // (SetupRoutine.cpp:188-240); rows no edge writes stay empty and
-        // nothing is trimmed.
-        stored = off + (uint64_t)rows * 4 <= (uint64_t)D.spanCapacity;
-        if(stored)
+        stored = off + (uint64_t)rows * (uint32_t)D.ms <= (uint64_t)D.spanCapacity;
+        uint32_t *sp = D.spans + off;
+        int32_t tMin = yMin, tMax = yMax;
+        if(stored && cntClip)
+            spans_clipped(D, slot, n, dW, yMin, yMax, sp, tMin, tMax);
+        else if(stored && D.ms > 1)
         {
             for(int q = 0; q < 4; q++)
             {
-                uint32_t *sp = D.spans + off + (uint64_t)q * rows;
-                for(uint32_t r = 0; r < rows; r++) sp[r] = 0u;
-                int32_t Xq[MAX_POLY + 1], Yq[MAX_POLY + 1];
-                for(int i = 0; i < n; i++) { Xq[i] = X[i] - XF[q]; Yq[i] = Y[i] - YF[q]; }
-                write_spans(D, Xq, Yq, n, dW, yMin, sp);
+                int32_t f, l;
+                spans_triangle(D, X0 - XF[q], Y0 - YF[q], X1 - XF[q], Y1 - YF[q], X2 - XF[q], Y2 - YF[q], dW, yMin, yMax,
+                               sp + (uint64_t)q * rows, f, l);
             }
-            inf.spanOff = (uint32_t)off;
-            inf.rows = rows;
         }
-    }
-    else if(cand)
-    {
-        stored = off + rows <= (uint64_t)D.spanCapacity;
-        if(stored)
+        else if(stored)
+            spans_triangle(D, X0, Y0, X1, Y1, X2, Y2, dW, yMin, yMax, sp, tMin, tMax);
+        else if(D.ms > 1)
         {
-            uint32_t *sp = D.spans + off;
-            write_spans(D, X, Y, n, dW, yMin, sp);
-            // Trim empty rows at the top and bottom (SetupRoutine.cpp:243-264)
-            const int32_t y0 = yMin;
-            while(yMin < yMax)
-            {
-                uint32_t s = sp[yMin - y0];
-                if((s & 0xFFFFu) != (s >> 16)) break;
-                yMin++;
-            }
-            while(yMax > yMin)
-            {
-                uint32_t s = sp[yMax - 1 - y0];
-                if((s & 0xFFFFu) != (s >> 16)) break;
-                yMax--;
-            }
-            inf.spanOff = (uint32_t)(off + (uint64_t)(yMin - y0));
+            // span scratch full, 4x MSAA: nothing is trimmed (SetupRoutine.cpp:243);
+            // k_raster walks the edges itself for this triangle
         }
+        else if(cntClip)
+            trim_clipped_unstored(D, slot, n, dW, tMin, tMax);
         else
         {
             // span scratch full: trim by direct evaluation; k_raster walks the
             // edges itself for this triangle
+            const int32_t Xs[3] = {X0, X1, X2}, Ys[3] = {Y0, Y1, Y2};
             int32_t l, r;
-            while(yMin < yMax)
+            while(tMin < tMax)
             {
-                span_at(D, X, Y, n, dW, yMin, l, r);
+                span_at(D, Xs, Ys, 3, dW, tMin, l, r);
                 if(l != r) break;
-                yMin++;
+                tMin++;
             }
-            while(yMax > yMin)
+            while(tMax > tMin)
             {
-                span_at(D, X, Y, n, dW, yMax - 1, l, r);
+                span_at(D, Xs, Ys, 3, dW, tMax - 1, l, r);
                 if(l != r) break;
-                yMax--;
+                tMax--;
             }
         }
+        if(stored)
+        {
+            inf.spanOff = (uint32_t)(off + (uint64_t)(tMin - yMin));  // MSAA: tMin = yMin
+            inf.rows = rows;
+        }
+        yMin = tMin;
+        yMax = tMax;
     }
     if(cand && yMin < yMax)
     {
-        {
-            // pixel box: covered x satisfy ceil(Xmin/256) <= left <= x < right <= ceil(Xmax/256)
-            const int32_t pad = D.ms > 1 ? 96 : 0;  // farthest sample offset (Xf)
-            int32_t bx0 = max(D.sx0, (xMinS - pad + 0xFF) >> 8);
-            int32_t bx1 = max(bx0, min(D.sx1, (xMaxS + pad + 0xFF) >> 8));
-            {
-                cntVis = 1;
-                box = make_short4((short)bx0, (short)yMin, (short)bx1, (short)yMax);
-                inf.info = (uint32_t)n | ((uint32_t)dW << 5) | ((uint32_t)cntClip << 6) | ((uint32_t)stored << 7) | ((uint32_t)frontBit << 8);
-                if(!stored) inf.rows = 0;
-                if(cntClip)
-                {
-                    uint32_t slot = atomicAdd(D.polyCount, 1u);
-                    if(slot < D.polyCapacity)
-                    {
-                        inf.slot = slot;
-                        for(int i = 0; i < n; i++) D.poly[(size_t)slot * MAX_POLY + i] = make_int2(X[i], Y[i]);
-                    }
-                    else
-                    {
-                        atomicOr(D.error, ERR_POLY_OVERFLOW);
-                        cntVis = 0;
-                        box = make_short4(0, 0, 0, 0);
-                        inf.info = 0;
-                    }
-                }
-            }
-        }
+        // pixel box: covered x satisfy ceil(Xmin/256) <= left <= x < right <= ceil(Xmax/256)
+        const int32_t pad = D.ms > 1 ? 96 : 0;  // farthest sample offset (Xf)
+        int32_t bx0 = max(D.sx0, (xMinS - pad + 0xFF) >> 8);
+        int32_t bx1 = max(bx0, min(D.sx1, (xMaxS + pad + 0xFF) >> 8));
+        cntVis = 1;
+        box = make_short4((short)bx0, (short)yMin, (short)bx1, (short)yMax);
+        inf.info = (uint32_t)n | ((uint32_t)dW << 5) | ((uint32_t)cntClip << 6) | ((uint32_t)stored << 7) | ((uint32_t)frontBit << 8);
+        if(!stored) inf.rows = 0;
+        if(cntClip) inf.slot = slot;
     }
     D.triBox[t] = box;  // capacity is a whole number of setup blocks
     D.triInfo[t] = inf;
     if(cntVis)
     {
+        // the vertex records again (cached): kept out of registers across the span loop
+        float4 vc[3], vp[3], va[3], vb[3] = {make_float4(0, 0, 0, 0), make_float4(0, 0, 0, 0), make_float4(0, 0, 0, 0)};
+        vc[0] = D.ptv[(size_t)vs0 * 4]; vc[1] = D.ptv[(size_t)vs1 * 4]; vc[2] = D.ptv[(size_t)vs2 * 4];
+        vp[0] = D.ptv[(size_t)vs0 * 4 + 1]; vp[1] = D.ptv[(size_t)vs1 * 4 + 1]; vp[2] = D.ptv[(size_t)vs2 * 4 + 1];
+        va[0] = D.ptv[(size_t)vs0 * 4 + 2]; va[1] = D.ptv[(size_t)vs1 * 4 + 2]; va[2] = D.ptv[(size_t)vs2 * 4 + 2];
+        if(D.nv > 3)
+        {
+            vb[0] = D.ptv[(size_t)vs0 * 4 + 3]; vb[1] = D.ptv[(size_t)vs1 * 4 + 3]; vb[2] = D.ptv[(size_t)vs2 * 4 + 3];
+        }
         float pl[PLANES_STORED];
-        triangle_planes(D, t, pl);
+        triangle_planes(D, vc, vp, va, vb, pl);
         float4 *dst = D.planes + (size_t)t * (PLANES_STORED / 4);
 #pragma unroll
         for(int k = 0; k < PLANES_STORED / 4; k++)
@@ -979,7 +1118,7 @@ __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
         atomicAdd(&D.binDiff[yb * W + xb], 1);
     }
 
-    // ---- chunk boxes (64 triangles = 2 warps) and counters ------------------
+    // ---- per warp: chunk box (CHUNK = 32 triangles), super-chunk box, counters ----
     const bool has = cntVis != 0;
     int bx0 = has ? box.x : 0x7FFF, by0 = has ? box.y : 0x7FFF;
     int bx1 = has ? box.z : -0x8000, by1 = has ? box.w : -0x8000;
@@ -996,41 +1135,23 @@ __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
         cntClip += __shfl_xor_sync(0xFFFFFFFFu, cntClip, o);
         cntVis += __shfl_xor_sync(0xFFFFFFFFu, cntVis, o);
     }
-    __shared__ short4 sBox[SETUP_THREADS / 32];
-    __shared__ int sCnt[4][SETUP_THREADS / 32];
+    static_assert(CHUNK == 32, "one chunk box per warp");
+    const uint32_t chunk = blk * (SETUP_THREADS / CHUNK) + (uint32_t)warp;
     if(lane == 0)
     {
-        sBox[warp] = make_short4((short)bx0, (short)by0, (short)bx1, (short)by1);
-        sCnt[0][warp] = cntIn; sCnt[1][warp] = cntRej; sCnt[2][warp] = cntClip; sCnt[3][warp] = cntVis;
-    }
-    __syncthreads();
-    if(threadIdx.x < SETUP_THREADS / CHUNK)
-    {
-        const int w0 = threadIdx.x * (CHUNK / 32);
-        short4 b = sBox[w0];
-        for(int w = 1; w < CHUNK / 32; w++)
+        D.chunkBox[chunk] = make_short4((short)bx0, (short)by0, (short)bx1, (short)by1);
+        if(bx0 < bx1)
         {
-            short4 c = sBox[w0 + w];
-            b.x = min(b.x, c.x); b.y = min(b.y, c.y); b.z = max(b.z, c.z); b.w = max(b.w, c.w);
+            int4 *sb = D.superBox + chunk / SUPER;
+            atomicMin(&sb->x, bx0);
+            atomicMin(&sb->y, by0);
+            atomicMax(&sb->z, bx1);
+            atomicMax(&sb->w, by1);
         }
-        D.chunkBox[blk * (SETUP_THREADS / CHUNK) + threadIdx.x] = b;
-        if(b.x < b.z)
-        {
-            int4 *sb = D.superBox + blk / (SUPER * CHUNK / SETUP_THREADS);
-            atomicMin(&sb->x, (int)b.x);
-            atomicMin(&sb->y, (int)b.y);
-            atomicMax(&sb->z, (int)b.z);
-            atomicMax(&sb->w, (int)b.w);
-        }
-    }
-    if(threadIdx.x == 0)
-    {
-        int a = 0, b = 0, c = 0, d = 0;
-        for(int w = 0; w < SETUP_THREADS / 32; w++) { a += sCnt[0][w]; b += sCnt[1][w]; c += sCnt[2][w]; d += sCnt[3][w]; }
-        atomicAdd(&D.counters[0], (unsigned long long)a);
-        atomicAdd(&D.counters[1], (unsigned long long)b);
-        atomicAdd(&D.counters[2], (unsigned long long)c);
-        atomicAdd(&D.counters[3], (unsigned long long)d);
+        if(cntIn) atomicAdd(&D.counters[0], (unsigned long long)cntIn);
+        if(cntRej) atomicAdd(&D.counters[1], (unsigned long long)cntRej);
+        if(cntClip) atomicAdd(&D.counters[2], (unsigned long long)cntClip);
+        if(cntVis) atomicAdd(&D.counters[3], (unsigned long long)cntVis);
     }
 }
 
@@ -1165,12 +1286,73 @@ static __device__ __noinline__ void bilinear_srgb(const DrawParams &D, uint32_t 
     }
 }
 
-__device__ __forceinline__ uint32_t texel_rgba8(const TexLevel &lv, uint32_t u, uint32_t v)
+__device__ __forceinline__ uint32_t texel_index(const TexLevel &lv, uint32_t u, uint32_t v)
 {
     uint32_t xi = mulhi_u16(u, lv.w);
     uint32_t yi = mulhi_u16(v, lv.h);
-    int32_t index = (int32_t)(int16_t)xi + (int32_t)(int16_t)yi * (int32_t)(int16_t)lv.pitch;  // pmaddwd
-    return __ldg((const uint32_t *)lv.buf + (uint32_t)index);
+    return (uint32_t)((int32_t)(int16_t)xi + (int32_t)(int16_t)yi * (int32_t)(int16_t)lv.pitch);  // pmaddwd
+}
+
+__device__ __forceinline__ uint32_t texel_rgba8(const TexLevel &lv, uint32_t u, uint32_t v)
+{
+    return __ldg((const uint32_t *)lv.buf + texel_index(lv, u, v));
+}
+
+// bilinearInterpolate of four unsigned 8-bit texels (SamplerCore.cpp:516-575):
+// weights from the low 16 bits of u0 * width and v0 * height.
+__device__ __forceinline__ void bilinear8(const TexLevel &lv, uint32_t u0, uint32_t v0, uint32_t t00, uint32_t t10, uint32_t t01,
+                                          uint32_t t11, uint32_t out[4])
+{
+    uint32_t f0u = (u0 * lv.w) & 0xFFFFu, f0v = (v0 * lv.h) & 0xFFFFu;
+    uint32_t f1u = (~f0u) & 0xFFFFu, f1v = (~f0v) & 0xFFFFu;
+    uint32_t f0u0v = mulhi_u16(f0u, f0v), f1u0v = mulhi_u16(f1u, f0v);
+    uint32_t f0u1v = mulhi_u16(f0u, f1v), f1u1v = mulhi_u16(f1u, f1v);
+#pragma unroll
+    for(int c = 0; c < 4; c++)
+    {
+        uint32_t a = mulhi_u16(((t00 >> (8 * c)) & 0xFFu) << 8, f1u1v);
+        uint32_t b = mulhi_u16(((t10 >> (8 * c)) & 0xFFu) << 8, f0u1v);
+        uint32_t e = mulhi_u16(((t01 >> (8 * c)) & 0xFFu) << 8, f1u0v);
+        uint32_t g = mulhi_u16(((t11 >> (8 * c)) & 0xFFu) << 8, f0u0v);
+        out[c] = (((a + b) & 0xFFFFu) + ((e + g) & 0xFFFFu)) & 0xFFFFu;
+    }
+}
+
+// Both levels of a trilinear sample of a linear-filtered 8-bit texture
+// without sRGB decoding (sampleQuad2D at int(lod) and int(lod) + 1,
+// SamplerCore.cpp:324-379,668-909): the eight texel addresses first, then
+// the eight loads together, so the sample waits for memory once.
+template<bool MIRROR_ONCE>
+__device__ __forceinline__ void sample_trilinear8(const DrawParams &D, float u, float v, float lod, uint32_t c[4], uint32_t cc[4],
+                                                  uint32_t &lvMask)
+{
+    const int ilod = trunc_int(lod);  // selectMipmap, MIPMAP_LINEAR (:2357-2379)
+    const int top = D.levelCount - 1;
+    const int la = ilod < 0 ? 0 : (ilod > top ? top : ilod);
+    const int lb = ilod + 1 < 0 ? 0 : (ilod + 1 > top ? top : ilod + 1);
+    lvMask |= (1u << la) | (1u << lb);
+    const TexLevel &A = D.lv[la], &B = D.lv[lb];
+    const uint32_t uu = address16<MIRROR_ONCE>(u, D.addrU);
+    const uint32_t vv = address16<MIRROR_ONCE>(v, D.addrV);
+    const bool wu = D.addrU == SWGB_ADDRESS_REPEAT, wv = D.addrV == SWGB_ADDRESS_REPEAT;
+    const uint32_t au0 = offset_sample(uu, A.uHalf, wu, -1), av0 = offset_sample(vv, A.vHalf, wv, -1);
+    const uint32_t au1 = offset_sample(uu, A.uHalf, wu, +1), av1 = offset_sample(vv, A.vHalf, wv, +1);
+    const uint32_t bu0 = offset_sample(uu, B.uHalf, wu, -1), bv0 = offset_sample(vv, B.vHalf, wv, -1);
+    const uint32_t bu1 = offset_sample(uu, B.uHalf, wu, +1), bv1 = offset_sample(vv, B.vHalf, wv, +1);
+    const uint32_t *pa = (const uint32_t *)A.buf, *pb = (const uint32_t *)B.buf;
+    const uint32_t ia00 = texel_index(A, au0, av0), ia10 = texel_index(A, au1, av0);
+    const uint32_t ia01 = texel_index(A, au0, av1), ia11 = texel_index(A, au1, av1);
+    const uint32_t ib00 = texel_index(B, bu0, bv0), ib10 = texel_index(B, bu1, bv0);
+    const uint32_t ib01 = texel_index(B, bu0, bv1), ib11 = texel_index(B, bu1, bv1);
+    uint32_t ta00 = __ldg(pa + ia00), ta10 = __ldg(pa + ia10), ta01 = __ldg(pa + ia01), ta11 = __ldg(pa + ia11);
+    uint32_t tb00 = __ldg(pb + ib00), tb10 = __ldg(pb + ib10), tb01 = __ldg(pb + ib01), tb11 = __ldg(pb + ib11);
+    const uint32_t sel = texel_order(D);
+    ta00 = __byte_perm(ta00, 0u, sel); ta10 = __byte_perm(ta10, 0u, sel);
+    ta01 = __byte_perm(ta01, 0u, sel); ta11 = __byte_perm(ta11, 0u, sel);
+    tb00 = __byte_perm(tb00, 0u, sel); tb10 = __byte_perm(tb10, 0u, sel);
+    tb01 = __byte_perm(tb01, 0u, sel); tb11 = __byte_perm(tb11, 0u, sel);
+    bilinear8(A, au0, av0, ta00, ta10, ta01, ta11, c);
+    bilinear8(B, bu0, bv0, tb00, tb10, tb01, tb11, cc);
 }
 
 // sampleQuad2D for one lane, 16-bit channel values c << 8 (SamplerCore.cpp:668-909).
@@ -1201,25 +1383,14 @@ __device__ __forceinline__ void sample_quad_2d(const DrawParams &D, float u, flo
         t01 = __byte_perm(t01, 0u, sel);
         t11 = __byte_perm(t11, 0u, sel);
     }
-    // bilinearInterpolate, unsigned 8-bit components (:516-575)
-    uint32_t f0u = (u0 * lv.w) & 0xFFFFu, f0v = (v0 * lv.h) & 0xFFFFu;
-    uint32_t f1u = (~f0u) & 0xFFFFu, f1v = (~f0v) & 0xFFFFu;
-    uint32_t f0u0v = mulhi_u16(f0u, f0v), f1u0v = mulhi_u16(f1u, f0v);
-    uint32_t f0u1v = mulhi_u16(f0u, f1v), f1u1v = mulhi_u16(f1u, f1v);
     if(D.texSRGB)
     {
-        bilinear_srgb(D, t00, t10, t01, t11, f0u0v, f1u0v, f0u1v, f1u1v, out);
+        uint32_t f0u = (u0 * lv.w) & 0xFFFFu, f0v = (v0 * lv.h) & 0xFFFFu;
+        uint32_t f1u = (~f0u) & 0xFFFFu, f1v = (~f0v) & 0xFFFFu;
+        bilinear_srgb(D, t00, t10, t01, t11, mulhi_u16(f0u, f0v), mulhi_u16(f1u, f0v), mulhi_u16(f0u, f1v), mulhi_u16(f1u, f1v), out);
         return;
     }
-#pragma unroll
-    for(int c = 0; c < 4; c++)
-    {
-        uint32_t a = mulhi_u16(((t00 >> (8 * c)) & 0xFFu) << 8, f1u1v);
-        uint32_t b = mulhi_u16(((t10 >> (8 * c)) & 0xFFu) << 8, f0u1v);
-        uint32_t e = mulhi_u16(((t01 >> (8 * c)) & 0xFFu) << 8, f1u0v);
-        uint32_t g = mulhi_u16(((t11 >> (8 * c)) & 0xFFu) << 8, f0u0v);
-        out[c] = (((a + b) & 0xFFFFu) + ((e + g) & 0xFFFFu)) & 0xFFFFu;
-    }
+    bilinear8(lv, u0, v0, t00, t10, t01, t11, out);  // bilinearInterpolate, unsigned 8-bit components (:516-575)
 }
 
 // Implicit LOD of computeLod2D (SamplerCore.cpp:1376-1422) from lanes 0, 1, 2
@@ -1244,16 +1415,21 @@ __device__ __forceinline__ void sample_texture_lane(const DrawParams &D, float l
                                                     uint32_t &lvMask)
 {
     uint32_t c[4], cc[4] = {0u, 0u, 0u, 0u};
-    const int levels = D.mipLinear ? 2 : 1;
-#pragma unroll 1
-    for(int second = 0; second < levels; second++)
+    if(D.mipLinear && D.texLinear && !D.texSRGB)
+        sample_trilinear8<MIRROR_ONCE>(D, ul, vl, lod, c, cc, lvMask);
+    else
     {
-        uint32_t t[4];
-        sample_quad_2d<MIRROR_ONCE>(D, ul, vl, lod, second, t, lvMask);
-#pragma unroll
-        for(int k = 0; k < 4; k++)
+        const int levels = D.mipLinear ? 2 : 1;
+#pragma unroll 1
+        for(int second = 0; second < levels; second++)
         {
-            if(second) cc[k] = t[k]; else c[k] = t[k];
+            uint32_t t[4];
+            sample_quad_2d<MIRROR_ONCE>(D, ul, vl, lod, second, t, lvMask);
+#pragma unroll
+            for(int k = 0; k < 4; k++)
+            {
+                if(second) cc[k] = t[k]; else c[k] = t[k];
+            }
         }
     }
     if(D.mipLinear)  // sampleFilter trilinear blend (:324-379)
@@ -1601,11 +1777,26 @@ __host__ __device__ constexpr int color_words(int cf) { return cf_unorm8(cf) ? 1
 // kernel carries the whole per-sample pipeline -- D16_UNORM depth (the staged
 // depth then holds its integers), depth bias, the depth bounds test and the
 // stencil test; without it those paths are compiled out.
+// Shared-memory copies by the asynchronous copy unit (cp.async): the copy is
+// issued and the thread goes on; cp_async_wait_all waits for its own copies.
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((uint32_t)__cvta_generic_to_shared(smem)), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((uint32_t)__cvta_generic_to_shared(smem)), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
 template<int CF, int MS, int BW = BIN, int BH = BIN, bool FULL = false>
 struct __align__(16) RasterShared {  // 16: the warps' copies sit back to back and take float4 / uint4 accesses
     float depth[MS][BW * BH];
     uint32_t color[MS][BW * BH * color_words(CF)];
-    float plane[PLANES][BATCH];
+    float4 planeA[BATCH][PLANES_STORED / 4];  // the triangle's plane record, copied from the setup stage
     uint32_t span[BATCH][MS][BH];      // left | right << 16 per sample and bin row
     int16_t qx0[BATCH][BH / 2];        // first quad x per quad row of the triangle
     uint16_t qpre[BATCH][BH / 2 + 1];  // prefix of quads per quad row
@@ -1682,6 +1873,12 @@ __device__ __noinline__ void walk_spans_in_bin(const DrawParams &D, SH &S, int t
 template<class SH>
 __device__ int setup_batch_triangle(const DrawParams &D, SH &S, int ti, uint32_t t, int bx0, int by0)
 {
+    // the plane record first: it depends on t only, and arrives while the
+    // box, the record and the span rows are fetched
+    {
+        const float4 *pl = D.planes + (size_t)t * (PLANES_STORED / 4);
+        for(int v = 0; v < D.planeVec4; v++) cp_async16(&S.planeA[ti][v], pl + v);
+    }
     const short4 box = D.triBox[t];
     const TriInfo inf = D.triInfo[t];
     const int n = inf.info & 31, dW = (inf.info >> 5) & 1;
@@ -1694,8 +1891,8 @@ __device__ int setup_batch_triangle(const DrawParams &D, SH &S, int ti, uint32_t
 #pragma unroll
     for(int q = 0; q < MS; q++)
     {
-        S.span[ti][q][2 * qrA] = 0u;
-        S.span[ti][q][2 * qrB + 1] = 0u;
+        if(2 * qrA < rowLo - by0) S.span[ti][q][2 * qrA] = 0u;
+        if(2 * qrB + 1 >= rowHi - by0) S.span[ti][q][2 * qrB + 1] = 0u;
     }
     if(inf.info & 128)
     {
@@ -1703,7 +1900,7 @@ __device__ int setup_batch_triangle(const DrawParams &D, SH &S, int ti, uint32_t
         for(int q = 0; q < MS; q++)
         {
             const uint32_t *sp = D.spans + inf.spanOff + (size_t)q * inf.rows + (rowLo - box.y);
-            for(int y = rowLo; y < rowHi; y++) S.span[ti][q][y - by0] = __ldg(sp + (y - rowLo));
+            for(int y = rowLo; y < rowHi; y++) cp_async4(&S.span[ti][q][y - by0], sp + (y - rowLo));
         }
     }
     else
@@ -1711,6 +1908,7 @@ __device__ int setup_batch_triangle(const DrawParams &D, SH &S, int ti, uint32_t
         // span scratch was full at setup: walk the edges here (SetupRoutine::edge)
         walk_spans_in_bin(D, S, ti, t, inf, by0, rowLo, rowHi);
     }
+    cp_async_wait_all();
     // quad rows: x range of the row pair over all samples (QuadRasterizer.cpp:96-123), clipped to the bin
     int pre = 0;
     for(int qr = qrA; qr <= qrB; qr++)
@@ -1742,17 +1940,6 @@ __device__ int setup_batch_triangle(const DrawParams &D, SH &S, int ti, uint32_t
     S.qr0[ti] = (int8_t)qrA;
     S.nqr[ti] = (int8_t)(qrB - qrA + 1);
 
-    // plane equations, evaluated once per triangle by the setup stage
-    const float4 *pl = D.planes + (size_t)t * (PLANES_STORED / 4);
-#pragma unroll
-    for(int k = 0; k < PLANES_STORED / 4; k++)
-    {
-        const float4 v = __ldg(pl + k);  // past planeVec4: unused planes, never read
-        if(4 * k + 0 < PLANES) S.plane[4 * k + 0][ti] = v.x;
-        if(4 * k + 1 < PLANES) S.plane[4 * k + 1][ti] = v.y;
-        if(4 * k + 2 < PLANES) S.plane[4 * k + 2][ti] = v.z;
-        if(4 * k + 3 < PLANES) S.plane[4 * k + 3][ti] = v.w;
-    }
     return pre;
 }
 
@@ -1765,8 +1952,8 @@ template<int CF, class SH>
 __device__ __forceinline__ void shade_pixel(const DrawParams &D, const SH &S, int ti, int qx, int y, int i,
                                             float col[4], uint32_t &lvMask)
 {
-    const float x0p = S.plane[0][ti], y0p = S.plane[1][ti];
-    const float wA = S.plane[5][ti], wB = S.plane[6][ti], wC = S.plane[7][ti];
+    const float x0p = reinterpret_cast<const float *>(S.planeA[ti])[0], y0p = reinterpret_cast<const float *>(S.planeA[ti])[1];
+    const float wA = reinterpret_cast<const float *>(S.planeA[ti])[5], wB = reinterpret_cast<const float *>(S.planeA[ti])[6], wC = reinterpret_cast<const float *>(S.planeA[ti])[7];
     const float xFi = ((float)qx + (float)(i & 1)) - x0p;
     const float yFi = ((float)y + (float)(i >> 1)) - y0p;
     const float rhwI = 1.0f / mul_add(xFi, wA, wC + yFi * wB);
@@ -1774,13 +1961,13 @@ __device__ __forceinline__ void shade_pixel(const DrawParams &D, const SH &S, in
 #pragma unroll
     for(int k = 0; k < 4; k++)
     {
-        const float A = S.plane[8 + 3 * k][ti], B = S.plane[9 + 3 * k][ti], C = S.plane[10 + 3 * k][ti];
+        const float A = reinterpret_cast<const float *>(S.planeA[ti])[8 + 3 * k], B = reinterpret_cast<const float *>(S.planeA[ti])[9 + 3 * k], C = reinterpret_cast<const float *>(S.planeA[ti])[10 + 3 * k];
         c[k] = mul_add(xFi, A, C + yFi * B) * rhwI;
     }
     if(D.fs == SWGB_FS_TEX_X_VCOLOR)
     {
-        const float uA = S.plane[20][ti], uB = S.plane[21][ti], uC = S.plane[22][ti];
-        const float vA = S.plane[23][ti], vB = S.plane[24][ti], vC = S.plane[25][ti];
+        const float uA = reinterpret_cast<const float *>(S.planeA[ti])[20], uB = reinterpret_cast<const float *>(S.planeA[ti])[21], uC = reinterpret_cast<const float *>(S.planeA[ti])[22];
+        const float vA = reinterpret_cast<const float *>(S.planeA[ti])[23], vB = reinterpret_cast<const float *>(S.planeA[ti])[24], vC = reinterpret_cast<const float *>(S.planeA[ti])[25];
         float u[4], v[4];
 #pragma unroll
         for(int j = 0; j < 4; j++)
@@ -1945,15 +2132,15 @@ __device__ __forceinline__ int warp_incl_scan(int v, int lane)
 template<int MS, class SH>
 __device__ __forceinline__ float sample_depth(const DrawParams &D, const SH &S, int ti, int qx, int y, int i, int q)
 {
-    float xF = ((float)qx + (float)(i & 1)) - S.plane[0][ti];
-    float yF = ((float)y + (float)(i >> 1)) - S.plane[1][ti];
+    float xF = ((float)qx + (float)(i & 1)) - reinterpret_cast<const float *>(S.planeA[ti])[0];
+    float yF = ((float)y + (float)(i >> 1)) - reinterpret_cast<const float *>(S.planeA[ti])[1];
     if(MS > 1)
     {
         yF = yF + SLY[q];
         xF = xF - SLX[q];
     }
-    float z = mul_add(xF, S.plane[2][ti], S.plane[4][ti] + yF * S.plane[3][ti]);
-    if(SH::kFull && D.depthBias) z = z + S.plane[PLANE_ZBIAS][ti];  // PixelRoutine.cpp:141-144
+    float z = mul_add(xF, reinterpret_cast<const float *>(S.planeA[ti])[2], reinterpret_cast<const float *>(S.planeA[ti])[4] + yF * reinterpret_cast<const float *>(S.planeA[ti])[3]);
+    if(SH::kFull && D.depthBias) z = z + reinterpret_cast<const float *>(S.planeA[ti])[PLANE_ZBIAS];  // PixelRoutine.cpp:141-144
     return depth_value<SH::kFull>(D, rmin(rmax(z, D.minDepthClamp), D.maxDepthClamp));  // clampDepth
 }
 
@@ -1999,11 +2186,11 @@ template<class SH>
 __device__ __forceinline__ bool hiz_rejects(const DrawParams &D, const SH &S, int ti, uint32_t t, int bx0, int by0, float zb)
 {
     const short4 box = D.triBox[t];
-    const float x0p = S.plane[0][ti], y0p = S.plane[1][ti];
-    const float zA = S.plane[2][ti], zB = S.plane[3][ti], zC = S.plane[4][ti];
+    const float x0p = reinterpret_cast<const float *>(S.planeA[ti])[0], y0p = reinterpret_cast<const float *>(S.planeA[ti])[1];
+    const float zA = reinterpret_cast<const float *>(S.planeA[ti])[2], zB = reinterpret_cast<const float *>(S.planeA[ti])[3], zC = reinterpret_cast<const float *>(S.planeA[ti])[4];
     const float xFa = ((float)max((int)box.x, bx0) - 0.5f) - x0p, xFb = ((float)min((int)box.z, bx0 + SH::kBW) - 0.5f) - x0p;
     const float yFa = ((float)max((int)box.y, by0) - 0.5f) - y0p, yFb = ((float)min((int)box.w, by0 + SH::kBH) - 0.5f) - y0p;
-    const float bias = (SH::kFull && D.depthBias) ? S.plane[PLANE_ZBIAS][ti] : 0.0f;
+    const float bias = (SH::kFull && D.depthBias) ? reinterpret_cast<const float *>(S.planeA[ti])[PLANE_ZBIAS] : 0.0f;
     const float T = fabsf(zC) + fmaxf(fabsf(yFa), fabsf(yFb)) * fabsf(zB) + fmaxf(fabsf(xFa), fabsf(xFb)) * fabsf(zA) + fabsf(bias);
     const float margin = T * (1.0f / 1048576.0f) + 1e-30f;
     const uint32_t op = D.compareOp;
@@ -2144,15 +2331,33 @@ __device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared<CF, 
                 nQuads++;
                 if(earlyZ)
                 {
+                    // the quad's depth, as sample_depth computes it, with the
+                    // triangle's z plane read once: x and y relative to the
+                    // plane origin per column / row, z = MulAdd(x, A, C + y B)
                     const int lx = qx - bx0, ly = 2 * qrow, y = by0 + 2 * qrow;
+                    const float x0p = reinterpret_cast<const float *>(S.planeA[qti])[0], y0p = reinterpret_cast<const float *>(S.planeA[qti])[1];
+                    const float zA = reinterpret_cast<const float *>(S.planeA[qti])[2], zB = reinterpret_cast<const float *>(S.planeA[qti])[3], zC = reinterpret_cast<const float *>(S.planeA[qti])[4];
+                    const float zBias = (FULL && D.depthBias) ? reinterpret_cast<const float *>(S.planeA[qti])[PLANE_ZBIAS] : 0.0f;
+                    const float xc[2] = {(float)qx - x0p, ((float)qx + 1.0f) - x0p};
+                    const float yr[2] = {(float)y - y0p, ((float)y + 1.0f) - y0p};
                     int keep = 0;
 #pragma unroll
                     for(int q = 0; q < MS; q++)
 #pragma unroll
                         for(int i = 0; i < 4; i++)
-                            if((cMask >> (4 * q + i) & 1) &&
-                               depth_pass(D.compareOp, S.depth[q][(ly + (i >> 1)) * BW + lx + (i & 1)], sample_depth<MS>(D, S, qti, qx, y, i, q)))
-                                keep |= 1 << (4 * q + i);
+                        {
+                            if(!(cMask >> (4 * q + i) & 1)) continue;
+                            float xF = xc[i & 1], yF = yr[i >> 1];
+                            if(MS > 1)
+                            {
+                                yF = yF + SLY[q];
+                                xF = xF - SLX[q];
+                            }
+                            float z = mul_add(xF, zA, zC + yF * zB);
+                            if(FULL && D.depthBias) z = z + zBias;
+                            z = depth_value<FULL>(D, rmin(rmax(z, D.minDepthClamp), D.maxDepthClamp));
+                            if(depth_pass(D.compareOp, S.depth[q][(ly + (i >> 1)) * BW + lx + (i & 1)], z)) keep |= 1 << (4 * q + i);
+                        }
                     nTested += __popc(cMask & ~keep);
                     cMask = keep;
                 }
@@ -2277,17 +2482,37 @@ __device__ __forceinline__ void walk_bin(const DrawParams &D, SH &S, int bx0, in
         {
             const int sc = sb + __ffs(superHits) - 1;
             superHits &= superHits - 1;
-            const int c = sc * SUPER + lane;
-            unsigned chunkHits = __ballot_sync(0xFFFFFFFFu, c < D.nchunks && box_hits<BW, BH>(D.chunkBox[c], bx0, by0));
-            while(chunkHits)
-            {
-                const int chunk = sc * SUPER + __ffs(chunkHits) - 1;
-                chunkHits &= chunkHits - 1;
+            static_assert(SUPER % 32 == 0 && CHUNK == 32, "chunk boxes in ballots of 32, one triangle per lane");
 #pragma unroll
-                for(int half = 0; half < CHUNK / 32; half++)
+            for(int cw = 0; cw < SUPER; cw += 32)
+            {
+            const int c = sc * SUPER + cw + lane;
+            unsigned chunkHits = __ballot_sync(0xFFFFFFFFu, c < D.nchunks && box_hits<BW, BH>(D.chunkBox[c], bx0, by0));
+            // the triangle boxes of the next hit chunk are loaded while the
+            // current chunk is compacted (and its batches run)
+            int chunk = -1;
+            short4 tb = make_short4(0, 0, 0, 0);
+            if(chunkHits)
+            {
+                chunk = sc * SUPER + cw + __ffs(chunkHits) - 1;
+                chunkHits &= chunkHits - 1;
+                const uint32_t tri = (uint32_t)chunk * CHUNK + lane;
+                if(tri < D.count) tb = D.triBox[tri];
+            }
+            while(chunk >= 0)
+            {
+                int next = -1;
+                short4 nb = make_short4(0, 0, 0, 0);
+                if(chunkHits)
                 {
-                    const uint32_t tri = (uint32_t)chunk * CHUNK + half * 32 + lane;
-                    const bool th = tri < D.count && box_hits<BW, BH>(D.triBox[tri], bx0, by0);
+                    next = sc * SUPER + cw + __ffs(chunkHits) - 1;
+                    chunkHits &= chunkHits - 1;
+                    const uint32_t ntri = (uint32_t)next * CHUNK + lane;
+                    if(ntri < D.count) nb = D.triBox[ntri];
+                }
+                {
+                    const uint32_t tri = (uint32_t)chunk * CHUNK + lane;
+                    const bool th = tri < D.count && box_hits<BW, BH>(tb, bx0, by0);
                     const unsigned b = __ballot_sync(0xFFFFFFFFu, th);
                     if(th) S.triList[listCount + __popc(b & ((1u << lane) - 1u))] = (int)tri;
                     listCount += __popc(b);
@@ -2303,6 +2528,9 @@ __device__ __forceinline__ void walk_bin(const DrawParams &D, SH &S, int bx0, in
                         __syncwarp();
                     }
                 }
+                chunk = next;
+                tb = nb;
+            }
             }
         }
     }
@@ -2320,82 +2548,87 @@ __device__ __forceinline__ void raster_bin(const DrawParams &D, RasterShared<CF,
     const int bx0 = D.binX0 + (bin % D.binsX) * BW;
     const int by0 = D.binY0 + (bin / D.binsX) * BH;
 
-    // ---- stage the bin's depth and colour, every sample plane (16-byte segments) ----
-    for(int q = 0; q < MS; q++)
-    {
-        const uint8_t *dbase = D.depth + (size_t)q * D.depthSlice;
-        const uint8_t *cbase = D.color + (size_t)q * D.colorSlice;
-        for(int i = lane; i < BW * BH / 4; i += 32)
-        {
-            const int ly = i / (BW / 4), lx = (i % (BW / 4)) * 4;
-            const int px = bx0 + lx, py = by0 + ly;
-            float4 dz = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
-            if((D.depthTest || (FULL && D.depthBounds)) && py < D.sy1 && px < D.sx1)
-            {
-                const uint8_t *drow = dbase + (size_t)py * D.depthPitch;
-                if(FULL && D.depth16)
-                {
-                    // D16_UNORM: the stored integers as floats (readDepth16)
-                    uint32_t w0 = 0, w1 = 0;
-                    if(D.vec16 && px + 4 <= D.sx1)
-                    {
-                        const uint2 v = *(const uint2 *)(drow + (size_t)px * 2);
-                        w0 = v.x;
-                        w1 = v.y;
-                    }
-                    else
-                    {
-                        uint32_t h[4] = {0, 0, 0, 0};
-                        for(int k = 0; k < 4 && px + k < D.sx1; k++) h[k] = *(const uint16_t *)(drow + (size_t)(px + k) * 2);
-                        w0 = h[0] | h[1] << 16;
-                        w1 = h[2] | h[3] << 16;
-                    }
-                    dz = make_float4((float)(w0 & 0xFFFFu), (float)(w0 >> 16), (float)(w1 & 0xFFFFu), (float)(w1 >> 16));
-                }
-                else if(D.vec16 && px + 4 <= D.sx1)
-                    dz = *(const float4 *)(drow + (size_t)px * 4);
-                else
-                {
-                    float dv[4] = {1.0f, 1.0f, 1.0f, 1.0f};
-                    for(int k = 0; k < 4 && px + k < D.sx1; k++) dv[k] = *(const float *)(drow + (size_t)(px + k) * 4);
-                    dz = make_float4(dv[0], dv[1], dv[2], dv[3]);
-                }
-            }
-            *(float4 *)&S.depth[q][ly * BW + lx] = dz;
-        }
-        for(int i = lane; i < BW * BH * CW / 4; i += 32)
-        {
-            // 16-byte segment i of the bin's colour rows: 4 / CW pixels
-            const int ly = i / (BW * CW / 4), lx = (i % (BW * CW / 4)) * 4 / CW;
-            const int px = bx0 + lx, py = by0 + ly;
-            uint4 cc = make_uint4(0, 0, 0, 0);
-            if(py < D.sy1 && px < D.sx1)
-            {
-                const uint8_t *crow = cbase + (size_t)py * D.colorPitch + (size_t)px * 4 * CW;
-                if(D.vec16 && px + 4 / CW <= D.sx1)
-                    cc = *(const uint4 *)crow;
-                else
-                {
-                    uint32_t cv[4] = {0, 0, 0, 0};
-                    for(int k = 0; k < 4 && px + k / CW < D.sx1; k++) cv[k] = *(const uint32_t *)(crow + 4 * k);
-                    cc = make_uint4(cv[0], cv[1], cv[2], cv[3]);
-                }
-            }
-            *(uint4 *)&S.color[q][(ly * BW + lx) * CW] = cc;
-        }
-    }
-    if(FULL && D.stencilTest)
+    // The bin is staged when its first batch arrives: a bin no candidate
+    // reaches is neither read nor written back.
+    bool staged = false;
+    auto stage = [&]() {
+        // ---- stage the bin's depth and colour, every sample plane (16-byte segments) ----
         for(int q = 0; q < MS; q++)
         {
-            // the bin's stencil bytes (1 per pixel and sample plane)
-            const uint8_t *sbase = D.stencil + (size_t)q * D.stencilSlice;
-            for(int i = lane; i < BW * BH; i += 32)
+            const uint8_t *dbase = D.depth + (size_t)q * D.depthSlice;
+            const uint8_t *cbase = D.color + (size_t)q * D.colorSlice;
+            for(int i = lane; i < BW * BH / 4; i += 32)
             {
-                const int px = bx0 + i % BW, py = by0 + i / BW;
-                S.stencil[q][i] = (py < D.sy1 && px < D.sx1) ? sbase[(size_t)py * D.stencilPitch + px] : (uint8_t)0;
+                const int ly = i / (BW / 4), lx = (i % (BW / 4)) * 4;
+                const int px = bx0 + lx, py = by0 + ly;
+                float4 dz = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+                if((D.depthTest || (FULL && D.depthBounds)) && py < D.sy1 && px < D.sx1)
+                {
+                    const uint8_t *drow = dbase + (size_t)py * D.depthPitch;
+                    if(FULL && D.depth16)
+                    {
+                        // D16_UNORM: the stored integers as floats (readDepth16)
+                        uint32_t w0 = 0, w1 = 0;
+                        if(D.vec16 && px + 4 <= D.sx1)
+                        {
+                            const uint2 v = *(const uint2 *)(drow + (size_t)px * 2);
+                            w0 = v.x;
+                            w1 = v.y;
+                        }
+                        else
+                        {
+                            uint32_t h[4] = {0, 0, 0, 0};
+                            for(int k = 0; k < 4 && px + k < D.sx1; k++) h[k] = *(const uint16_t *)(drow + (size_t)(px + k) * 2);
+                            w0 = h[0] | h[1] << 16;
+                            w1 = h[2] | h[3] << 16;
+                        }
+                        dz = make_float4((float)(w0 & 0xFFFFu), (float)(w0 >> 16), (float)(w1 & 0xFFFFu), (float)(w1 >> 16));
+                    }
+                    else if(D.vec16 && px + 4 <= D.sx1)
+                        dz = *(const float4 *)(drow + (size_t)px * 4);
+                    else
+                    {
+                        float dv[4] = {1.0f, 1.0f, 1.0f, 1.0f};
+                        for(int k = 0; k < 4 && px + k < D.sx1; k++) dv[k] = *(const float *)(drow + (size_t)(px + k) * 4);
+                        dz = make_float4(dv[0], dv[1], dv[2], dv[3]);
+                    }
+                }
+                *(float4 *)&S.depth[q][ly * BW + lx] = dz;
+            }
+            for(int i = lane; i < BW * BH * CW / 4; i += 32)
+            {
+                // 16-byte segment i of the bin's colour rows: 4 / CW pixels
+                const int ly = i / (BW * CW / 4), lx = (i % (BW * CW / 4)) * 4 / CW;
+                const int px = bx0 + lx, py = by0 + ly;
+                uint4 cc = make_uint4(0, 0, 0, 0);
+                if(py < D.sy1 && px < D.sx1)
+                {
+                    const uint8_t *crow = cbase + (size_t)py * D.colorPitch + (size_t)px * 4 * CW;
+                    if(D.vec16 && px + 4 / CW <= D.sx1)
+                        cc = *(const uint4 *)crow;
+                    else
+                    {
+                        uint32_t cv[4] = {0, 0, 0, 0};
+                        for(int k = 0; k < 4 && px + k / CW < D.sx1; k++) cv[k] = *(const uint32_t *)(crow + 4 * k);
+                        cc = make_uint4(cv[0], cv[1], cv[2], cv[3]);
+                    }
+                }
+                *(uint4 *)&S.color[q][(ly * BW + lx) * CW] = cc;
             }
         }
-    __syncwarp();
+        if(FULL && D.stencilTest)
+            for(int q = 0; q < MS; q++)
+            {
+                // the bin's stencil bytes (1 per pixel and sample plane)
+                const uint8_t *sbase = D.stencil + (size_t)q * D.stencilSlice;
+                for(int i = lane; i < BW * BH; i += 32)
+                {
+                    const int px = bx0 + i % BW, py = by0 + i / BW;
+                    S.stencil[q][i] = (py < D.sy1 && px < D.sx1) ? sbase[(size_t)py * D.stencilPitch + px] : (uint8_t)0;
+                }
+            }
+        __syncwarp();
+    };
 
     // bit k: pixel lane + 32k of the bin lies inside the scissor (the depth bound's domain)
     uint32_t inMask = 0;
@@ -2409,7 +2642,15 @@ __device__ __forceinline__ void raster_bin(const DrawParams &D, RasterShared<CF,
         }
 
     // ---- candidates in primitive order, in batches of BATCH ----------------------
-    walk_bin(D, S, bx0, by0, [&](int nb) { raster_batch<CF, MS, BW, BH, HIZ, FULL>(D, S, nb, bx0, by0, inMask, nQuads, nTested, nPassed, lvMask); });
+    walk_bin(D, S, bx0, by0, [&](int nb) {
+        if(!staged)
+        {
+            stage();
+            staged = true;
+        }
+        raster_batch<CF, MS, BW, BH, HIZ, FULL>(D, S, nb, bx0, by0, inMask, nQuads, nTested, nPassed, lvMask);
+    });
+    if(!staged) return;  // untouched bin
 
     // ---- write the bin back, every sample plane ----------------------------------
     if(FULL && D.stencilWrite)
@@ -2585,7 +2826,7 @@ __global__ void __launch_bounds__(256) k_vertex_batch(const __grid_constant__ Ba
     }
 }
 
-__global__ void __launch_bounds__(SETUP_THREADS) k_setup_batch(const __grid_constant__ BatchPtrs B)
+__global__ void __launch_bounds__(SETUP_THREADS, 3) k_setup_batch(const __grid_constant__ BatchPtrs B)
 {
     const BatchView V(B.hdr);
     const BatchHeader &h = V.h;
@@ -2593,7 +2834,6 @@ __global__ void __launch_bounds__(SETUP_THREADS) k_setup_batch(const __grid_cons
     {
         const uint32_t d = find_draw(V.sStart, h.n, u);
         setup_body(V.draws[d], u - __ldg(V.sStart + d));
-        __syncthreads();  // the next unit reuses the block's shared memory
     }
 }
 

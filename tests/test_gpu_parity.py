@@ -155,6 +155,19 @@ def test_span_scratch_fallback(gpu_lib, monkeypatch, rows):
     monkeypatch.setenv("SWGB_SPAN_ROWS", rows if rows != "0" else "1")
     check_scene(scenes.scene_textured_small(n_tris=150, width=96, height=72), gpu_lib)
     check_scene(scenes.scene_heightfield(quads_x=60, quads_y=30, width=160, height=96, tex_size=64), gpu_lib)
+    # 4x MSAA outlines (never trimmed) and clipped polygons take the same fallback
+    s = scenes.scene_small(n_tris=300, width=72, height=56, seed_index=42)
+    s.samples = 4
+    check_scene(s, gpu_lib)
+    s = scenes.scene_small(n_tris=300, width=96, height=96, seed_index=22)
+    rng = np.random.Generator(np.random.PCG64(99))
+    v = s.vertices
+    v[:, 0:2] = rng.uniform(-3.0, 3.0, (v.shape[0], 2))
+    v[:, 2] = rng.uniform(-1.0, 2.0, v.shape[0])
+    v[:, 3] = rng.uniform(-0.5, 2.0, v.shape[0])
+    check_scene(s, gpu_lib)
+    s.samples = 4
+    check_scene(s, gpu_lib)
 
 
 def _float_variant(tex_fmt, color_fmt, blend, address, mip, seed=31):
