@@ -350,7 +350,11 @@ swgb_status swgb_plan_batch(const swgb_pipeline_state *states, const swgb_draw_a
  * the one array: calls whose work overlaps on the GPU (different streams, or
  * several host threads) race and corrupt each other; order them on one stream.
  * Device-side errors (an index >= vertex_count) drop the triangle silently,
- * as there is no context to report them through. */
+ * as there is no context to report them through.  The array's address is
+ * resolved once per device and kept for the life of the process, so a
+ * device reset (cudaDeviceReset) followed by more calls is not supported.
+ * Unlike swgb_draw, this path does not order the bins longest first: the
+ * result is the same, a large frame can take longer. */
 #define SWGB_NOALLOC_MAX_TRIANGLES 32768u
 #define SWGB_NOALLOC_MAX_VERTICES 98304u
 swgb_status swgb_draw_noalloc(const swgb_pipeline_state *state, const swgb_draw_args *args, void *stream);

@@ -449,29 +449,30 @@ __device__ __noinline__ void adj_interp(const DrawParams &D, const AdjParams &A,
     I.lod = D.minLod;
     if(D.fs == SWGB_FS_TEX_X_VCOLOR && I.ok && D.minLod != D.maxLod)
     {
-        // level of detail from lanes 0, 1, 2 of the pixel's quad, as the
-        // forward, in fp32 (it is held constant; only its value is used)
+        // level of detail from lanes 0, 1, 2 of the pixel's quad (it is held
+        // constant; only its value is used): the lanes' texture coordinates
+        // under the model in fp64, rounded to fp32, then the forward's fp32
+        // LOD arithmetic.  In fp32 throughout, the coordinate differences
+        // of a 2048^2 texture carried enough rounding to move the trilinear
+        // weights by ~1e-4.
         const int qx = px & ~1, qy = py & ~1;
-        const float3 K[3] = {make_float3((float)I.K[0].x, (float)I.K[0].y, (float)I.K[0].z),
-                             make_float3((float)I.K[1].x, (float)I.K[1].y, (float)I.K[1].z),
-                             make_float3((float)I.K[2].x, (float)I.K[2].y, (float)I.K[2].z)};
         float lu[4], lv[4];
 #pragma unroll
         for(int j = 0; j < 3; j++)
         {
             // w_i = d_k . K_i with d_k the lane's offset from vertex k's projection
             const double3 rd = pixel_ray(A, qx + (j & 1), qy + (j >> 1));
-            float w[3];
+            double w[3];
 #pragma unroll
             for(int i = 0; i < 3; i++)
             {
                 const int k = (i + 1) % 3;
-                const float dx = (float)(rd.x - T.proj[k].x), dy = (float)(rd.y - T.proj[k].y);
-                w[i] = dx * K[i].x + dy * K[i].y + (T.q[k].z != 0.0 ? 0.0f : K[i].z);
+                const double dx = rd.x - T.proj[k].x, dy = rd.y - T.proj[k].y;
+                w[i] = dx * I.K[i].x + dy * I.K[i].y + (T.q[k].z != 0.0 ? 0.0 : I.K[i].z);
             }
-            const float is = 1.0f / (w[0] + w[1] + w[2]);
-            lu[j] = (w[0] * T.var[0][4] + w[1] * T.var[1][4] + w[2] * T.var[2][4]) * is;
-            lv[j] = (w[0] * T.var[0][5] + w[1] * T.var[1][5] + w[2] * T.var[2][5]) * is;
+            const double ws = w[0] + w[1] + w[2];
+            lu[j] = (float)((w[0] * (double)T.var[0][4] + w[1] * (double)T.var[1][4] + w[2] * (double)T.var[2][4]) / ws);
+            lv[j] = (float)((w[0] * (double)T.var[0][5] + w[1] * (double)T.var[1][5] + w[2] * (double)T.var[2][5]) / ws);
         }
         lu[3] = lu[0];
         lv[3] = lv[0];

@@ -290,7 +290,8 @@ __global__ void __launch_bounds__(256) k_blit_half(BlitParams P)
 // scale 1 the sample position of destination pixel i is source texel
 // i + (srcOffset - dstOffset) exactly; its four samples are read, summed in
 // order, scaled by 1/4 and written -- no scale, clamp or sRGB step applies to
-// float formats.  Two pixels per thread for half floats (16-byte loads).
+// float formats.  Two pixels per thread for half floats, each sample of each
+// pixel read with its own texel-sized load.
 template<int SK>
 __global__ void __launch_bounds__(256) k_resolve_float(BlitParams P, int dx, int dy)
 {

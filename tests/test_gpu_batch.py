@@ -212,3 +212,32 @@ def test_batch_scratch_growth_recaptures(gpu_lib):
         assert_bit_exact(c, ref[0], "color")
         assert_bit_exact(d, ref[1], "depth")
         assert k == ref[2]
+
+
+def test_full_atlas_sample_against_oracle(gpu_lib):
+    """The full 4096-draw atlas workload (triangle counts log-uniform in
+    [16, 65536], 16384^2 pages) as one swgb_draw_batch, then a seeded sample
+    of its draws -- the largest ones included -- against the oracle drawing
+    each into its own framebuffer, bit for bit; and the batch's triangle
+    counter against the draws' total."""
+    import torch
+    from swiftshader_gb300 import DeviceBatch, Renderer
+    b = scenes.scene_batch()
+    db = DeviceBatch(b)
+    r = Renderer(0)
+    db.clear()
+    torch.cuda.synchronize()
+    r.reset_counters()
+    db.draw_batch(r)
+    r.synchronize()
+    cnt = r.counters()
+    assert cnt["triangles_in"] == int(b.tris.sum())
+    rng = np.random.Generator(np.random.PCG64(12))
+    sample = list(rng.choice(b.n, 16, replace=False)) + list(np.argsort(b.tris)[-2:])
+    for i in sample:
+        c_ref, d_ref, _ = render_oracle(b.draw_scene(int(i)), 8)
+        c, d = db.view(int(i))
+        assert_bit_exact(d.cpu().numpy(), d_ref, "depth of draw %d" % i)
+        assert_bit_exact(c.cpu().numpy(), c_ref, "colour of draw %d" % i)
+    del db
+    torch.cuda.empty_cache()
