@@ -77,7 +77,7 @@ struct swgb_ctx {
     uint16_t *srgbLut;     // sRGBtoLinearFF_FF00 on the device (256 entries)
     uint32_t *restart;     // primitive restart: per-position segment starts, then per-block carries
     size_t restartCap;
-    int *binDiff;          // longest-first bin order of single draws: difference array and order
+    int *binDiff;          // bin order of single draws: difference array, then the first chunk per bin
     size_t binDiffCap;
     uint32_t *binOrder;
     size_t binOrderCap;
@@ -569,6 +569,7 @@ swgb_status prepare_scratch(swgb_ctx *ctx, DrawParams &D, bool order = true)
         D.restartCarry = ctx->restart + D.count + nb;
     }
     D.binDiff = nullptr;
+    D.binFirst = nullptr;
     D.binOrder = nullptr;
     if(order && nbins > (size_t)ctx->rasterBlocks[raster_variant(D)] * RASTER_WARPS && cells * sizeof(int) <= BIN_ORDER_SMEM)
     {
@@ -579,9 +580,10 @@ swgb_status prepare_scratch(swgb_ctx *ctx, DrawParams &D, bool order = true)
                 return s;
             ctx->binOrderAttr = true;
         }
-        if((s = ensure(ctx->binDiff, ctx->binDiffCap, cells, "bin counts")) != SWGB_OK) return s;
+        if((s = ensure(ctx->binDiff, ctx->binDiffCap, cells + nbins, "bin counts")) != SWGB_OK) return s;
         if((s = ensure(ctx->binOrder, ctx->binOrderCap, nbins, "bin order")) != SWGB_OK) return s;
         D.binDiff = ctx->binDiff;
+        D.binFirst = ctx->binDiff + cells;
         D.binOrder = ctx->binOrder;
     }
     return SWGB_OK;

@@ -166,6 +166,7 @@ struct DrawParams {
     int nsuper;
     unsigned int *binQueue;  // next bin for the persistent raster warps
     int *binDiff;         // single draws: 2D difference array of triangle boxes over the bin grid, (binsY+1) x (binsX+1), or null
+    int *binFirst;        // single draws: per bin (binsY x binsX) the first chunk whose box reaches it, or null
     uint32_t *binOrder;   // single draws: bins longest first (k_bin_order), or null for raster order
     uint32_t *spans;      // left | right << 16 per triangle row
     unsigned long long *spanCount;
@@ -282,6 +283,8 @@ __global__ void k_vertex(const __grid_constant__ DrawParams D, uint32_t nverts)
         D.superBox[j] = make_int4(0x7FFFFFFF, 0x7FFFFFFF, (int)0x80000000, (int)0x80000000);
     if(D.binDiff)
         for(uint32_t j = i; j < (uint32_t)((D.binsX + 1) * (D.binsY + 1)); j += gridDim.x * blockDim.x) D.binDiff[j] = 0;
+    if(D.binFirst)
+        for(uint32_t j = i; j < (uint32_t)(D.binsX * D.binsY); j += gridDim.x * blockDim.x) D.binFirst[j] = 0x7FFFFFFF;
     if(i < nverts) vertex_body(D, i);
 }
 
@@ -1105,38 +1108,55 @@ __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
         for(int k = 0; k < PLANES_STORED / 4; k++)
             if(k < D.planeVec4) dst[k] = make_float4(pl[4 * k], pl[4 * k + 1], pl[4 * k + 2], pl[4 * k + 3]);
     }
-    if(D.binDiff && box.x < box.z && box.y < box.w)
+    if(D.binDiff)
     {
         // triangles per bin, for the raster's longest-first bin order: the
-        // box's bin rectangle into a 2D difference array (k_bin_order integrates)
-        const int W = D.binsX + 1;
-        const int xa = (box.x - D.binX0) / D.binW, xb = (box.z - 1 - D.binX0) / D.binW + 1;
-        const int ya = (box.y - D.binY0) / D.binH, yb = (box.w - 1 - D.binY0) / D.binH + 1;
-        atomicAdd(&D.binDiff[ya * W + xa], 1);
-        atomicAdd(&D.binDiff[ya * W + xb], -1);
-        atomicAdd(&D.binDiff[yb * W + xa], -1);
-        atomicAdd(&D.binDiff[yb * W + xb], 1);
+        // box's bin rectangle into a 2D difference array (k_bin_order
+        // integrates).  Neighbouring triangles share corners, so lanes adding
+        // to the same corner are merged first: one atomic per distinct corner.
+        const bool hasBox = box.x < box.z && box.y < box.w;
+        const unsigned act = __ballot_sync(0xFFFFFFFFu, hasBox);
+        if(hasBox)
+        {
+            const int W = D.binsX + 1;
+            const int xa = (box.x - D.binX0) / D.binW, xb = (box.z - 1 - D.binX0) / D.binW + 1;
+            const int ya = (box.y - D.binY0) / D.binH, yb = (box.w - 1 - D.binY0) / D.binH + 1;
+#pragma unroll
+            for(int c = 0; c < 4; c++)
+            {
+                // corners (xa, ya) +1, (xb, ya) -1, (xa, yb) -1, (xb, yb) +1
+                const int idx = (c < 2 ? ya : yb) * W + ((c == 0 || c == 2) ? xa : xb);
+                const unsigned peers = __match_any_sync(act, idx);
+                const int n = __popc(peers);
+                if(lane == __ffs(peers) - 1) atomicAdd(&D.binDiff[idx], (c == 0 || c == 3) ? n : -n);
+            }
+        }
     }
 
     // ---- per warp: chunk box (CHUNK = 32 triangles), super-chunk box, counters ----
     const bool has = cntVis != 0;
     int bx0 = has ? box.x : 0x7FFF, by0 = has ? box.y : 0x7FFF;
     int bx1 = has ? box.z : -0x8000, by1 = has ? box.w : -0x8000;
-    int cntRej = cntIn - cntVis;
-#pragma unroll
-    for(int o = 16; o > 0; o >>= 1)
-    {
-        bx0 = min(bx0, __shfl_xor_sync(0xFFFFFFFFu, bx0, o));
-        by0 = min(by0, __shfl_xor_sync(0xFFFFFFFFu, by0, o));
-        bx1 = max(bx1, __shfl_xor_sync(0xFFFFFFFFu, bx1, o));
-        by1 = max(by1, __shfl_xor_sync(0xFFFFFFFFu, by1, o));
-        cntIn += __shfl_xor_sync(0xFFFFFFFFu, cntIn, o);
-        cntRej += __shfl_xor_sync(0xFFFFFFFFu, cntRej, o);
-        cntClip += __shfl_xor_sync(0xFFFFFFFFu, cntClip, o);
-        cntVis += __shfl_xor_sync(0xFFFFFFFFu, cntVis, o);
-    }
+    bx0 = __reduce_min_sync(0xFFFFFFFFu, bx0);
+    by0 = __reduce_min_sync(0xFFFFFFFFu, by0);
+    bx1 = __reduce_max_sync(0xFFFFFFFFu, bx1);
+    by1 = __reduce_max_sync(0xFFFFFFFFu, by1);
+    const int cntRej = __reduce_add_sync(0xFFFFFFFFu, cntIn - cntVis);
+    cntIn = __reduce_add_sync(0xFFFFFFFFu, cntIn);
+    cntClip = __reduce_add_sync(0xFFFFFFFFu, cntClip);
+    cntVis = __reduce_add_sync(0xFFFFFFFFu, cntVis);
     static_assert(CHUNK == 32, "one chunk box per warp");
     const uint32_t chunk = blk * (SETUP_THREADS / CHUNK) + (uint32_t)warp;
+    if(D.binFirst && bx0 < bx1)
+    {
+        // first chunk reaching each bin, for the order's tie-break; a chunk
+        // spread over more than 256 bins leaves them to smaller chunks
+        const int xa = (bx0 - D.binX0) / D.binW, xb = (bx1 - 1 - D.binX0) / D.binW;
+        const int ya = (by0 - D.binY0) / D.binH, yb = (by1 - 1 - D.binY0) / D.binH;
+        const int w = xb - xa + 1, area = w * (yb - ya + 1);
+        if(area <= 256)
+            for(int i = lane; i < area; i += 32) atomicMin(&D.binFirst[(ya + i / w) * D.binsX + xa + i % w], (int)chunk);
+    }
     if(lane == 0)
     {
         D.chunkBox[chunk] = make_short4((short)bx0, (short)by0, (short)bx1, (short)by1);
@@ -1158,22 +1178,36 @@ __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
 #ifndef SWGB_RASTER_TU
 __global__ void __launch_bounds__(SETUP_THREADS) k_setup(const __grid_constant__ DrawParams D) { setup_body(D, blockIdx.x); }
 
-// Longest-first order of a draw's bins for the persistent raster warps (the
-// heaviest bins start first, so none starts last and holds the frame's tail):
+// Order of a draw's bins for the persistent raster warps.  Longest first:
 // the setup stage's difference array integrated in shared memory into
-// triangles per bin, then bins bucketed by the bit length of their count,
-// heaviest bucket first.  One block; the order inside a bucket is arbitrary,
-// as the bins are independent.
+// triangles per bin, bins bucketed by the bit length of their count, heaviest
+// bucket first, so no heavy bin starts last and holds the frame's tail.
+// Inside a bucket, bins reached earliest in the draw's triangle order go
+// first (64 sub-buckets of the first chunk index), which reads the setup
+// stage's oldest output first.  Measured on the 1M-triangle 1080p height
+// field, whose triangles are submitted bottom to top: k_raster took 1.311 ms
+// with an arbitrary order inside the buckets and 1.255 ms with this one; a
+// plain bottom-first order took 1.233 ms and a top-first one 1.59 ms, but on
+// 200k large random triangles the bottom-first order lost 6% to longest-first
+// and this one nothing.  One block; bins with the same key are independent.
 constexpr int BIN_ORDER_THREADS = 1024;
-__device__ __forceinline__ int bin_order_key(int c) { return c > 0 ? 32 - __clz(c) : 0; }
+constexpr int BIN_ORDER_SUB = 64;
+constexpr int BIN_ORDER_KEYS = 33 * BIN_ORDER_SUB;
+__device__ __forceinline__ int bin_order_key(int count, int first, int nchunks)
+{
+    const int len = count > 0 ? 32 - __clz(count) : 0;
+    const int sub = first == 0x7FFFFFFF ? BIN_ORDER_SUB - 1
+                                        : (int)(((long long)first * (BIN_ORDER_SUB - 1)) / max(1, nchunks));
+    return (32 - len) * BIN_ORDER_SUB + sub;
+}
 
 __global__ void __launch_bounds__(BIN_ORDER_THREADS) k_bin_order(const __grid_constant__ DrawParams D)
 {
     extern __shared__ int cnt[];  // (binsY + 1) x (binsX + 1)
-    __shared__ uint32_t hist[33], base[33];
+    __shared__ uint32_t hist[BIN_ORDER_KEYS];
     const int W = D.binsX + 1, H = D.binsY + 1, nb = D.binsX * D.binsY, tid = threadIdx.x;
     for(int i = tid; i < W * H; i += blockDim.x) cnt[i] = D.binDiff[i];
-    if(tid < 33) hist[tid] = 0;
+    for(int i = tid; i < BIN_ORDER_KEYS; i += blockDim.x) hist[i] = 0;
     __syncthreads();
     for(int r = tid; r < H; r += blockDim.x)
     {
@@ -1187,21 +1221,53 @@ __global__ void __launch_bounds__(BIN_ORDER_THREADS) k_bin_order(const __grid_co
         for(int y = 0; y < H; y++) cnt[y * W + c] = (acc += cnt[y * W + c]);
     }
     __syncthreads();
-    for(int b = tid; b < nb; b += blockDim.x) atomicAdd(&hist[bin_order_key(cnt[(b / D.binsX) * W + b % D.binsX])], 1u);
+    auto key = [&](int b) { return bin_order_key(cnt[(b / D.binsX) * W + b % D.binsX], D.binFirst[b], D.nchunks); };
+    for(int b = tid; b < nb; b += blockDim.x) atomicAdd(&hist[key(b)], 1u);
     __syncthreads();
-    if(tid == 0)
+    // exclusive scan of the histogram, 'per' consecutive entries per thread
+    __shared__ uint32_t warpSum[BIN_ORDER_THREADS / 32];
     {
-        uint32_t acc = 0;
-        for(int k = 32; k >= 0; k--)
+        const int per = (BIN_ORDER_KEYS + BIN_ORDER_THREADS - 1) / BIN_ORDER_THREADS;
+        uint32_t v[4] = {0, 0, 0, 0}, s = 0;
+        static_assert((BIN_ORDER_KEYS + BIN_ORDER_THREADS - 1) / BIN_ORDER_THREADS <= 4, "scan entries per thread");
+        for(int j = 0; j < per; j++)
         {
-            base[k] = acc;
-            acc += hist[k];
+            const int i = tid * per + j;
+            v[j] = i < BIN_ORDER_KEYS ? hist[i] : 0u;
+            s += v[j];
+        }
+        const int lane = tid & 31, warp = tid >> 5;
+        uint32_t incl = s;
+        for(int o = 1; o < 32; o <<= 1)
+        {
+            const uint32_t u = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if(lane >= o) incl += u;
+        }
+        if(lane == 31) warpSum[warp] = incl;
+        __syncthreads();
+        if(warp == 0)
+        {
+            uint32_t w = warpSum[lane], wi = w;
+            for(int o = 1; o < 32; o <<= 1)
+            {
+                const uint32_t u = __shfl_up_sync(0xFFFFFFFFu, wi, o);
+                if(lane >= o) wi += u;
+            }
+            warpSum[lane] = wi - w;
+        }
+        __syncthreads();
+        uint32_t run = warpSum[warp] + incl - s;
+        for(int j = 0; j < per; j++)
+        {
+            const int i = tid * per + j;
+            if(i < BIN_ORDER_KEYS) hist[i] = run;
+            run += v[j];
         }
     }
     __syncthreads();
     for(int b = tid; b < nb; b += blockDim.x)
     {
-        const uint32_t pos = atomicAdd(&base[bin_order_key(cnt[(b / D.binsX) * W + b % D.binsX])], 1u);
+        const uint32_t pos = atomicAdd(&hist[key(b)], 1u);
         D.binOrder[pos] = (uint32_t)b;
     }
 }
