@@ -1858,6 +1858,10 @@ __device__ __forceinline__ void cp_async_wait_all()
     asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
 }
 
+// A batch's live pixels are queued (at most 31 left over plus the 4 pixels of
+// each of a quad round's 32 quads) and shaded 32 at a time.
+constexpr int PIXQ = 31 + 4 * 32 + 1;
+
 template<int CF, int MS, int BW = BIN, int BH = BIN, bool FULL = false>
 struct __align__(16) RasterShared {  // 16: the warps' copies sit back to back and take float4 / uint4 accesses
     float depth[MS][BW * BH];
@@ -1869,6 +1873,7 @@ struct __align__(16) RasterShared {  // 16: the warps' copies sit back to back a
     int8_t qr0[BATCH];                 // first quad row of the triangle in the bin
     int8_t nqr[BATCH];                 // quad rows of the triangle in the bin
     int triList[2 * BATCH];
+    uint32_t pixq[PIXQ];               // live pixels waiting for shading, in primitive order (pix_entry)
     int8_t front[BATCH];               // the triangle faces front (stencil state [0]) or back ([1])
     uint8_t stencil[FULL ? MS : 1][FULL ? BW * BH : 4];  // the bin's stencil values (stencil test active)
     static constexpr int kSamples = MS;
@@ -2352,124 +2357,126 @@ __device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared<CF, 
     if(HIZ && earlyZ) cnt = hiz_pass<MS>(D, S, cnt, bx0, by0, inMask, lessType, nQuads, nTested);
     const int incl = warp_incl_scan(cnt, lane);
     const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-    for(int s0 = 0; s0 < total; s0 += 32)
+    // Quad rounds expand 32 quad slots each and append their live pixels to
+    // the queue S.pixq; pixel rounds take 32 queued pixels at a time (the
+    // rest after the last quad round).  A pixel queued but not yet resolved
+    // leaves the staged depth as it was, which only makes a later quad
+    // round's early test reject less.
+    int qn = 0;  // queued pixels (warp-uniform)
+    for(int s0 = 0;; s0 += 32)
     {
-        // ---- quad slot -> (triangle, quad) -> coverage, early depth ---------
-        const int slot = s0 + lane;
-        int src;
+        const bool drain = s0 >= total;
+        if(!drain)
         {
-            int lo = 0, hi = 31;  // smallest lane j with incl_j > slot
+            // ---- quad slot -> (triangle, quad) -> coverage, early depth ---------
+            const int slot = s0 + lane;
+            int src;
+            {
+                int lo = 0, hi = 31;  // smallest lane j with incl_j > slot
 #pragma unroll
-            for(int step = 0; step < 5; step++)
-            {
-                int mid = (lo + hi) >> 1;
-                int v = __shfl_sync(0xFFFFFFFFu, incl, mid);
-                if(v > slot) hi = mid; else lo = mid + 1;
-            }
-            src = lo;
-        }
-        const int sIncl = __shfl_sync(0xFFFFFFFFu, incl, src);
-        const int sCnt = __shfl_sync(0xFFFFFFFFu, cnt, src);
-        int cMask = 0, qti = src, qx = 0, qrow = 0;  // cMask bit 4q+i: sample q of lane i
-        if(slot < total)
-        {
-            const int local = slot - (sIncl - sCnt);
-            int k = 0;
-            const int nq = S.nqr[qti];
-            while(k < nq - 1 && (int)S.qpre[qti][k + 1] <= local) k++;
-            qrow = S.qr0[qti] + k;
-            qx = S.qx0[qti][k] + 2 * (local - (int)S.qpre[qti][k]);
-#pragma unroll
-            for(int q = 0; q < MS; q++)
-            {
-                const uint32_t sp0 = S.span[qti][q][2 * qrow], sp1 = S.span[qti][q][2 * qrow + 1];
-                const int l0 = sp0 & 0xFFFF, r0 = sp0 >> 16, l1 = sp1 & 0xFFFF, r1 = sp1 >> 16;
-                // per-lane coverage: left <= x < right (QuadRasterizer.cpp:184-209)
-                int m = 0;
-                if(qx >= l0 && qx < r0) m |= 1;
-                if(qx + 1 >= l0 && qx + 1 < r0) m |= 2;
-                if(qx >= l1 && qx < r1) m |= 4;
-                if(qx + 1 >= l1 && qx + 1 < r1) m |= 8;
-                cMask |= m << (4 * q);
-            }
-            if(cMask)
-            {
-                nQuads++;
-                if(earlyZ)
+                for(int step = 0; step < 5; step++)
                 {
-                    // the quad's depth, as sample_depth computes it, with the
-                    // triangle's z plane read once: x and y relative to the
-                    // plane origin per column / row, z = MulAdd(x, A, C + y B)
-                    const int lx = qx - bx0, ly = 2 * qrow, y = by0 + 2 * qrow;
-                    const float x0p = reinterpret_cast<const float *>(S.planeA[qti])[0], y0p = reinterpret_cast<const float *>(S.planeA[qti])[1];
-                    const float zA = reinterpret_cast<const float *>(S.planeA[qti])[2], zB = reinterpret_cast<const float *>(S.planeA[qti])[3], zC = reinterpret_cast<const float *>(S.planeA[qti])[4];
-                    const float zBias = (FULL && D.depthBias) ? reinterpret_cast<const float *>(S.planeA[qti])[PLANE_ZBIAS] : 0.0f;
-                    const float xc[2] = {(float)qx - x0p, ((float)qx + 1.0f) - x0p};
-                    const float yr[2] = {(float)y - y0p, ((float)y + 1.0f) - y0p};
-                    int keep = 0;
+                    int mid = (lo + hi) >> 1;
+                    int v = __shfl_sync(0xFFFFFFFFu, incl, mid);
+                    if(v > slot) hi = mid; else lo = mid + 1;
+                }
+                src = lo;
+            }
+            const int sIncl = __shfl_sync(0xFFFFFFFFu, incl, src);
+            const int sCnt = __shfl_sync(0xFFFFFFFFu, cnt, src);
+            int cMask = 0, qti = src, qx = 0, qrow = 0;  // cMask bit 4q+i: sample q of lane i
+            if(slot < total)
+            {
+                const int local = slot - (sIncl - sCnt);
+                int k = 0;
+                const int nq = S.nqr[qti];
+                while(k < nq - 1 && (int)S.qpre[qti][k + 1] <= local) k++;
+                qrow = S.qr0[qti] + k;
+                qx = S.qx0[qti][k] + 2 * (local - (int)S.qpre[qti][k]);
 #pragma unroll
-                    for(int q = 0; q < MS; q++)
+                for(int q = 0; q < MS; q++)
+                {
+                    const uint32_t sp0 = S.span[qti][q][2 * qrow], sp1 = S.span[qti][q][2 * qrow + 1];
+                    const int l0 = sp0 & 0xFFFF, r0 = sp0 >> 16, l1 = sp1 & 0xFFFF, r1 = sp1 >> 16;
+                    // per-lane coverage: left <= x < right (QuadRasterizer.cpp:184-209)
+                    int m = 0;
+                    if(qx >= l0 && qx < r0) m |= 1;
+                    if(qx + 1 >= l0 && qx + 1 < r0) m |= 2;
+                    if(qx >= l1 && qx < r1) m |= 4;
+                    if(qx + 1 >= l1 && qx + 1 < r1) m |= 8;
+                    cMask |= m << (4 * q);
+                }
+                if(cMask)
+                {
+                    nQuads++;
+                    if(earlyZ)
+                    {
+                        // the quad's depth, as sample_depth computes it, with the
+                        // triangle's z plane read once: x and y relative to the
+                        // plane origin per column / row, z = MulAdd(x, A, C + y B)
+                        const int lx = qx - bx0, ly = 2 * qrow, y = by0 + 2 * qrow;
+                        const float x0p = reinterpret_cast<const float *>(S.planeA[qti])[0], y0p = reinterpret_cast<const float *>(S.planeA[qti])[1];
+                        const float zA = reinterpret_cast<const float *>(S.planeA[qti])[2], zB = reinterpret_cast<const float *>(S.planeA[qti])[3], zC = reinterpret_cast<const float *>(S.planeA[qti])[4];
+                        const float zBias = (FULL && D.depthBias) ? reinterpret_cast<const float *>(S.planeA[qti])[PLANE_ZBIAS] : 0.0f;
+                        const float xc[2] = {(float)qx - x0p, ((float)qx + 1.0f) - x0p};
+                        const float yr[2] = {(float)y - y0p, ((float)y + 1.0f) - y0p};
+                        int keep = 0;
 #pragma unroll
-                        for(int i = 0; i < 4; i++)
-                        {
-                            if(!(cMask >> (4 * q + i) & 1)) continue;
-                            float xF = xc[i & 1], yF = yr[i >> 1];
-                            if(MS > 1)
+                        for(int q = 0; q < MS; q++)
+#pragma unroll
+                            for(int i = 0; i < 4; i++)
                             {
-                                yF = yF + SLY[q];
-                                xF = xF - SLX[q];
+                                if(!(cMask >> (4 * q + i) & 1)) continue;
+                                float xF = xc[i & 1], yF = yr[i >> 1];
+                                if(MS > 1)
+                                {
+                                    yF = yF + SLY[q];
+                                    xF = xF - SLX[q];
+                                }
+                                float z = mul_add(xF, zA, zC + yF * zB);
+                                if(FULL && D.depthBias) z = z + zBias;
+                                z = depth_value<FULL>(D, rmin(rmax(z, D.minDepthClamp), D.maxDepthClamp));
+                                if(depth_pass(D.compareOp, S.depth[q][(ly + (i >> 1)) * BW + lx + (i & 1)], z)) keep |= 1 << (4 * q + i);
                             }
-                            float z = mul_add(xF, zA, zC + yF * zB);
-                            if(FULL && D.depthBias) z = z + zBias;
-                            z = depth_value<FULL>(D, rmin(rmax(z, D.minDepthClamp), D.maxDepthClamp));
-                            if(depth_pass(D.compareOp, S.depth[q][(ly + (i >> 1)) * BW + lx + (i & 1)], z)) keep |= 1 << (4 * q + i);
-                        }
-                    nTested += __popc(cMask & ~keep);
-                    cMask = keep;
+                        nTested += __popc(cMask & ~keep);
+                        cMask = keep;
+                    }
                 }
             }
+            // ---- live pixels (any live sample) into the queue ---------------------
+            int pixMask = 0;
+#pragma unroll
+            for(int q = 0; q < MS; q++) pixMask |= (cMask >> (4 * q)) & 0xF;
+            const int np = __popc(pixMask);
+            const int pIncl = warp_incl_scan(np, lane);
+            int pos = qn + pIncl - np;
+#pragma unroll
+            for(int b = 0; b < 4; b++)
+                if(pixMask >> b & 1)
+                {
+                    int sm = 0;  // the pixel's live samples
+#pragma unroll
+                    for(int q = 0; q < MS; q++) sm |= ((cMask >> (4 * q + b)) & 1) << q;
+                    S.pixq[pos++] = (uint32_t)qti | (uint32_t)(qx - bx0) << 5 | (uint32_t)qrow << 11 | (uint32_t)b << 16 | (uint32_t)sm << 18;
+                }
+            qn += __shfl_sync(0xFFFFFFFFu, pIncl, 31);
+            __syncwarp();
         }
-        // ---- live pixels (any live sample), one per lane ----------------------
-        int pixMask = 0;
-#pragma unroll
-        for(int q = 0; q < MS; q++) pixMask |= (cMask >> (4 * q)) & 0xF;
-        const int np = __popc(pixMask);
-        const int pIncl = warp_incl_scan(np, lane);
-        const int pTotal = __shfl_sync(0xFFFFFFFFu, pIncl, 31);
-        for(int p0 = 0; p0 < pTotal; p0 += 32)
+        // ---- pixel rounds: 32 queued pixels, one per lane ---------------------
+        int done = 0;
+        while(qn - done >= 32 || (drain && qn > done))
         {
-            const int pix = p0 + lane;
-            int lo = 0, hi = 31;
-#pragma unroll
-            for(int step = 0; step < 5; step++)
-            {
-                int mid = (lo + hi) >> 1;
-                int v = __shfl_sync(0xFFFFFFFFu, pIncl, mid);
-                if(v > pix) hi = mid; else lo = mid + 1;
-            }
-            const int qq = lo;
-            const int qIncl = __shfl_sync(0xFFFFFFFFu, pIncl, qq);
-            const int qN = __shfl_sync(0xFFFFFFFFu, np, qq);
-            const int qPix = __shfl_sync(0xFFFFFFFFu, pixMask, qq);
-            const int qMask = __shfl_sync(0xFFFFFFFFu, cMask, qq);
-            const int qTi = __shfl_sync(0xFFFFFFFFu, qti, qq);
-            const int qX = __shfl_sync(0xFFFFFFFFu, qx, qq);
-            const int qRow = __shfl_sync(0xFFFFFFFFu, qrow, qq);
-            const bool valid = pix < pTotal;
-            int pidx = -1 - lane, i = 0;
+            const bool valid = lane < qn - done;
+            int pidx = -1 - lane, i = 0, sm = 0, qTi = 0, qX = 0, qRow = 0;
             float col[4] = {0.0f, 0.0f, 0.0f, 0.0f};
             if(valid)
             {
-                int nth = pix - (qIncl - qN);  // the nth set bit of the quad's pixel mask
-#pragma unroll
-                for(int b = 0; b < 4; b++)
-                {
-                    if(qPix >> b & 1)
-                    {
-                        if(nth == 0) i = b;
-                        nth--;
-                    }
-                }
+                const uint32_t e = S.pixq[done + lane];
+                qTi = (int)(e & 31u);
+                qX = bx0 + (int)((e >> 5) & 63u);
+                qRow = (int)((e >> 11) & 31u);
+                i = (int)((e >> 16) & 3u);
+                sm = (int)((e >> 18) & 15u);
                 pidx = (2 * qRow + (i >> 1)) * BW + (qX - bx0) + (i & 1);
                 shade_pixel<CF>(D, S, qTi, qX, by0 + 2 * qRow, i, col, lvMask);
             }
@@ -2483,7 +2490,7 @@ __device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared<CF, 
                 {
 #pragma unroll
                     for(int q = 0; q < MS; q++)
-                        if(qMask >> (4 * q + i) & 1)
+                        if(sm >> q & 1)
                         {
                             const float z = D.depthTest ? sample_depth<MS>(D, S, qTi, qX, by0 + 2 * qRow, i, q) : 0.0f;
                             rop_pixel<CF>(D, S, qTi, q, pidx, z, col, nTested, nPassed);
@@ -2493,6 +2500,18 @@ __device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared<CF, 
                 __syncwarp();
                 pend = __ballot_sync(0xFFFFFFFFu, mine && ((pend >> lane) & 1));
             }
+            done += min(32, qn - done);
+        }
+        if(drain) break;
+        if(done)
+        {
+            // the leftover (< 32) moves to the front
+            const int rem = qn - done;
+            const uint32_t v = lane < rem ? S.pixq[done + lane] : 0u;
+            __syncwarp();
+            if(lane < rem) S.pixq[lane] = v;
+            __syncwarp();
+            qn = rem;
         }
     }
     __syncwarp();
