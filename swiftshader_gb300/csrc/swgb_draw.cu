@@ -326,6 +326,13 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
     D.blendAlpha = D.srcC == SWGB_BLEND_SRC_ALPHA && D.dstC == SWGB_BLEND_ONE_MINUS_SRC_ALPHA && D.opC == SWGB_BLEND_OP_ADD &&
                    D.srcA == SWGB_BLEND_SRC_ALPHA && D.dstA == SWGB_BLEND_ONE_MINUS_SRC_ALPHA && D.opA == SWGB_BLEND_OP_ADD;
     D.writeMask = st->color_write_mask & 0xFu;
+    {
+        // B8G8R8A8 stores R in byte 2 and B in byte 0
+        const bool bgra = st->color_format == SWGB_FORMAT_B8G8R8A8_UNORM || st->color_format == SWGB_FORMAT_B8G8R8A8_SRGB;
+        D.writeBytes = 0;
+        for(int c = 0; c < 4; c++)
+            if(D.writeMask & (1u << c)) D.writeBytes |= 0xFFu << (8 * (bgra && c != 3 ? 2 - c : c));
+    }
     D.ms = (int)st->sample_count;
     D.colorSlice = st->color_slice_bytes;
     D.depthSlice = st->depth_slice_bytes;

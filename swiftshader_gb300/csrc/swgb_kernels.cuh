@@ -125,6 +125,7 @@ struct DrawParams {
     uint32_t srcC, dstC, opC, srcA, dstA, opA;
     int blendAlpha;  // SRC_ALPHA / ONE_MINUS_SRC_ALPHA / ADD on colour and alpha
     uint32_t writeMask;
+    uint32_t writeBytes;  // UNORM8 attachments: writeMask as a byte mask of the stored texel
     int fs;
     int ms;       // samples per pixel: 1 or 4
     uint64_t colorSlice, depthSlice;  // bytes between sample planes
@@ -2150,17 +2151,18 @@ __device__ __forceinline__ void rop_pixel(const DrawParams &D, SH &S, int ti, in
         // way out, and its write-mask bits with them (:2138-2143); sRGB
         // attachments encode R, G, B before the clamp (:1965-1970)
         if(SH::kFull && D.colorSRGB) srgb_encode3(out);
-        uint32_t packed = CF == CF_BGRA8 ? __byte_perm(color[idx], 0u, 0x3012u) : color[idx];
+        // clamped to [0, 1] (a NaN to 0), v * 255 rounds to 0..255: RoundInt's
+        // out-of-range value and PackUnsigned's saturation never apply
+        uint32_t fresh = 0;
 #pragma unroll
         for(int c = 0; c < 4; c++)
         {
-            float v = rmin(rmax(out[c], 0.0f), 1.0f);
-            int32_t r = round_int(v * 255.0f);
-            int32_t s16 = (int32_t)(int16_t)r;
-            uint32_t b = s16 < 0 ? 0u : (s16 > 255 ? 255u : (uint32_t)s16);  // PackUnsigned
-            if(D.writeMask & (1u << c)) packed = (packed & ~(0xFFu << (8 * c))) | (b << (8 * c));
+            const float v = rmin(rmax(out[c], 0.0f), 1.0f);
+            fresh |= (uint32_t)__float2int_rn(v * 255.0f) << (8 * c);
         }
-        color[idx] = CF == CF_BGRA8 ? __byte_perm(packed, 0u, 0x3012u) : packed;
+        if(CF == CF_BGRA8) fresh = __byte_perm(fresh, 0u, 0x3012u);
+        const uint32_t keep = D.writeBytes;  // bytes of the stored texel in its own order
+        color[idx] = keep == 0xFFFFFFFFu ? fresh : (color[idx] & ~keep) | (fresh & keep);
     }
     else if(CF == CF_RGBA16F)
     {
@@ -2481,12 +2483,13 @@ __device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared<CF, 
                 shade_pixel<CF>(D, S, qTi, qX, by0 + 2 * qRow, i, col, lvMask);
             }
             // ordered resolve: among lanes on the same pixel, lowest lane first
-            unsigned pend = __ballot_sync(0xFFFFFFFFu, valid);
-            while(pend)
+            // (rank = earlier lanes on the lane's pixel)
+            const unsigned peers = __match_any_sync(0xFFFFFFFFu, pidx);
+            const int rank = __popc(peers & ((1u << lane) - 1u));
+            const int maxRank = __reduce_max_sync(0xFFFFFFFFu, (unsigned)rank);
+            for(int rr = 0; rr <= maxRank; rr++)
             {
-                const bool mine = (pend >> lane) & 1;
-                const unsigned peers = __match_any_sync(0xFFFFFFFFu, mine ? pidx : -1 - lane);
-                if(mine && (__ffs(peers) - 1) == lane)
+                if(valid && rank == rr)
                 {
 #pragma unroll
                     for(int q = 0; q < MS; q++)
@@ -2495,10 +2498,8 @@ __device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared<CF, 
                             const float z = D.depthTest ? sample_depth<MS>(D, S, qTi, qX, by0 + 2 * qRow, i, q) : 0.0f;
                             rop_pixel<CF>(D, S, qTi, q, pidx, z, col, nTested, nPassed);
                         }
-                    pend &= ~(1u << lane);
                 }
                 __syncwarp();
-                pend = __ballot_sync(0xFFFFFFFFu, mine && ((pend >> lane) & 1));
             }
             done += min(32, qn - done);
         }
