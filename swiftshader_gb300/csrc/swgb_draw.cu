@@ -81,6 +81,10 @@ struct swgb_ctx {
     size_t binDiffCap;
     uint32_t *binOrder;
     size_t binOrderCap;
+    uint32_t *binList;        // candidate lists of single draws' bins, then their counts
+    size_t binListCap;
+    uint32_t binListPerBin;   // entries per bin list (0: no lists)
+    uint32_t binListMinTris;  // draws with fewer triangles walk their bins in k_raster
     bool binOrderAttr;
     int rasterBlocks[NRASTER];  // persistent raster grid per kernel variant: SMs x resident blocks per SM
     swgb_raster_config rasterConfig;  // bin shape and depth rejection of single-sample draws
@@ -523,6 +527,9 @@ void timed_launch(swgb_ctx *ctx, int kind, F &&launch)
 }
 
 constexpr size_t BIN_ORDER_SMEM = 200 * 1024;  // bin grids up to 51200 cells are ordered
+constexpr uint32_t BIN_LIST_MIN_TRIANGLES = 4096;    // smaller draws walk their bins in k_raster
+constexpr uint32_t BIN_LIST_DEFAULT = 1024;          // candidates per bin list
+constexpr size_t BIN_LIST_BYTES = (size_t)256 << 20;  // all of a draw's bin lists
 
 // Grows the context's scratch for draw D and points D at it; with order, also
 // the scratch of the longest-first bin order when it applies.
@@ -578,6 +585,22 @@ swgb_status prepare_scratch(swgb_ctx *ctx, DrawParams &D, bool order = true)
     D.binDiff = nullptr;
     D.binFirst = nullptr;
     D.binOrder = nullptr;
+    D.binList = nullptr;
+    D.binListCount = nullptr;
+    D.binListCap = 0;
+    if(order && ctx->binListPerBin && D.count >= ctx->binListMinTris && nbins > 0)
+    {
+        // per-bin candidate lists, BIN_LIST_BYTES at most in all
+        size_t per = ctx->binListPerBin;
+        if(nbins * per * sizeof(uint32_t) > BIN_LIST_BYTES) per = (BIN_LIST_BYTES / (nbins * sizeof(uint32_t))) & ~(size_t)31;
+        if(per >= 32)
+        {
+            if((s = ensure(ctx->binList, ctx->binListCap, nbins * per + nbins, "bin lists")) != SWGB_OK) return s;
+            D.binList = ctx->binList;
+            D.binListCount = ctx->binList + nbins * per;
+            D.binListCap = (uint32_t)per;
+        }
+    }
     if(order && nbins > (size_t)ctx->rasterBlocks[raster_variant(D)] * RASTER_WARPS && cells * sizeof(int) <= BIN_ORDER_SMEM)
     {
         if(!ctx->binOrderAttr)
@@ -625,6 +648,11 @@ swgb_status enqueue(swgb_ctx *ctx, DrawParams &D)
     {
         const size_t smem = (size_t)(D.binsX + 1) * (D.binsY + 1) * sizeof(int);
         timed_launch(ctx, SWGB_KERNEL_BIN_ORDER, [&] { k_bin_order<<<1, BIN_ORDER_THREADS, smem, ctx->stream>>>(D); });
+    }
+    if(D.binList)
+    {
+        const uint32_t blocks = (uint32_t)((D.binsX * D.binsY + BIN_LIST_WARPS - 1) / BIN_LIST_WARPS);
+        timed_launch(ctx, SWGB_KERNEL_BIN_ORDER, [&] { k_bin_list<<<blocks, 32 * BIN_LIST_WARPS, 0, ctx->stream>>>(D); });
     }
     if(D.binsX > 0 && D.binsY > 0)
     {
@@ -1404,6 +1432,12 @@ swgb_status swgb_ctx_create(int device, void *stream, swgb_ctx **out)
         c->ownStream = true;
     }
     if(const char *lim = getenv("SWGB_SPAN_ROWS")) c->spanRowsLimit = strtoull(lim, nullptr, 10);
+    // bin lists: SWGB_BIN_LIST entries per bin (0: none), for draws of at
+    // least SWGB_BIN_LIST_MIN triangles
+    c->binListPerBin = BIN_LIST_DEFAULT;
+    c->binListMinTris = BIN_LIST_MIN_TRIANGLES;
+    if(const char *lim = getenv("SWGB_BIN_LIST")) c->binListPerBin = (uint32_t)strtoul(lim, nullptr, 10);
+    if(const char *lim = getenv("SWGB_BIN_LIST_MIN")) c->binListMinTris = (uint32_t)strtoul(lim, nullptr, 10);
     if((s = cuda_check(cudaMalloc((void **)&c->polyCount, sizeof(uint32_t)), "polyCount")) != SWGB_OK ||
        (s = cuda_check(cudaMalloc((void **)&c->spanCount, sizeof(unsigned long long)), "spanCount")) != SWGB_OK ||
        (s = cuda_check(cudaMalloc((void **)&c->binQueue, sizeof(unsigned int)), "binQueue")) != SWGB_OK ||
@@ -1438,6 +1472,7 @@ swgb_status swgb_ctx_destroy(swgb_ctx *c)
     cudaFree(c->restart);
     cudaFree(c->srgbLut);
     cudaFree(c->binOrder);
+    cudaFree(c->binList);
     cudaFree(c->triBox);
     cudaFree(c->triInfo);
     cudaFree(c->planes);

@@ -170,6 +170,21 @@ def test_span_scratch_fallback(gpu_lib, monkeypatch, rows):
     check_scene(s, gpu_lib)
 
 
+@pytest.mark.parametrize("per_bin", ["32", "4096", "0"])
+def test_bin_list_paths(gpu_lib, monkeypatch, per_bin):
+    """Bins rasterised from k_bin_list's candidate lists, by their own walk
+    (lists off, or more candidates than a list holds), or a mix of both: same
+    bits.  Lists are forced on for these small draws (32 entries per bin
+    overflows some of their bins)."""
+    monkeypatch.setenv("SWGB_BIN_LIST_MIN", "1")
+    monkeypatch.setenv("SWGB_BIN_LIST", per_bin)
+    check_scene(scenes.scene_textured_small(n_tris=400, width=96, height=72), gpu_lib)
+    check_scene(scenes.scene_heightfield(quads_x=60, quads_y=30, width=160, height=96, tex_size=64), gpu_lib)
+    s = scenes.scene_small(n_tris=600, width=72, height=56, seed_index=42)
+    s.samples = 4
+    check_scene(s, gpu_lib)
+
+
 def _float_variant(tex_fmt, color_fmt, blend, address, mip, seed=31):
     """Random textured triangles with float textures / float attachments."""
     s = scenes.scene_textured_small(n_tris=180, width=80, height=64, tex_size=32, mip=mip, address=address,
