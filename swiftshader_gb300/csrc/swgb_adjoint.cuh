@@ -71,9 +71,9 @@ template<int MS>
 struct __align__(16) AdjShared {  // 16: the warps' copies sit back to back
     float depth[MS][BIN * BIN];  // replayed depth
     float4 planeA[BATCH][PLANES_STORED / 4];
-    uint32_t span[BATCH][MS][BIN];
-    int16_t qx0[BATCH][BIN / 2];
-    uint16_t qpre[BATCH][BIN / 2 + 1];
+    uint32_t span[BATCH][MS][BIN + 1];  // padded as in RasterShared
+    int16_t qx0[BATCH][BIN / 2 + 2];
+    uint16_t qpre[BATCH][BIN / 2 + 3];
     int8_t qr0[BATCH];
     int8_t nqr[BATCH];
     int8_t front[BATCH];  // facing (unused: the adjoint takes no stencil)

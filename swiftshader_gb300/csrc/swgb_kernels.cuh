@@ -1951,9 +1951,11 @@ struct __align__(16) RasterShared {  // 16: the warps' copies sit back to back a
     float depth[MS][BW * BH];
     uint32_t color[MS][BW * BH * color_words(CF)];
     float4 planeA[BATCH][PLANES_STORED / 4];  // the triangle's plane record, copied from the setup stage
-    uint32_t span[BATCH][MS][BH];      // left | right << 16 per sample and bin row
-    int16_t qx0[BATCH][BH / 2];        // first quad x per quad row of the triangle
-    uint16_t qpre[BATCH][BH / 2 + 1];  // prefix of quads per quad row
+    // per-triangle rows padded to odd word strides: lanes reading different
+    // triangles' rows fall in different banks
+    uint32_t span[BATCH][MS][BH + 1];  // left | right << 16 per sample and bin row
+    int16_t qx0[BATCH][BH / 2 + 2];    // first quad x per quad row of the triangle
+    uint16_t qpre[BATCH][BH / 2 + 3];  // prefix of quads per quad row
     int8_t qr0[BATCH];                 // first quad row of the triangle in the bin
     int8_t nqr[BATCH];                 // quad rows of the triangle in the bin
     int triList[2 * BATCH];
@@ -2107,22 +2109,26 @@ template<int CF, class SH>
 __device__ __forceinline__ void shade_pixel(const DrawParams &D, const SH &S, int ti, int qx, int y, int i,
                                             float col[4], uint32_t &lvMask)
 {
-    const float x0p = reinterpret_cast<const float *>(S.planeA[ti])[0], y0p = reinterpret_cast<const float *>(S.planeA[ti])[1];
-    const float wA = reinterpret_cast<const float *>(S.planeA[ti])[5], wB = reinterpret_cast<const float *>(S.planeA[ti])[6], wC = reinterpret_cast<const float *>(S.planeA[ti])[7];
+    // the plane record in 16-byte pieces: x0 y0 zA zB | zC wA wB wC | then A, B, C
+    // of each varying from float 8
+    const float4 p0 = S.planeA[ti][0], p1 = S.planeA[ti][1];
+    const float x0p = p0.x, y0p = p0.y;
+    const float wA = p1.y, wB = p1.z, wC = p1.w;
     const float xFi = ((float)qx + (float)(i & 1)) - x0p;
     const float yFi = ((float)y + (float)(i >> 1)) - y0p;
     const float rhwI = 1.0f / mul_add(xFi, wA, wC + yFi * wB);
     float c[4];
-#pragma unroll
-    for(int k = 0; k < 4; k++)
     {
-        const float A = reinterpret_cast<const float *>(S.planeA[ti])[8 + 3 * k], B = reinterpret_cast<const float *>(S.planeA[ti])[9 + 3 * k], C = reinterpret_cast<const float *>(S.planeA[ti])[10 + 3 * k];
-        c[k] = mul_add(xFi, A, C + yFi * B) * rhwI;
+        const float4 p2 = S.planeA[ti][2], p3 = S.planeA[ti][3], p4 = S.planeA[ti][4];
+        const float cA[4] = {p2.x, p2.w, p3.z, p4.y}, cB[4] = {p2.y, p3.x, p3.w, p4.z}, cC[4] = {p2.z, p3.y, p4.x, p4.w};
+#pragma unroll
+        for(int k = 0; k < 4; k++) c[k] = mul_add(xFi, cA[k], cC[k] + yFi * cB[k]) * rhwI;
     }
     if(D.fs == SWGB_FS_TEX_X_VCOLOR)
     {
-        const float uA = reinterpret_cast<const float *>(S.planeA[ti])[20], uB = reinterpret_cast<const float *>(S.planeA[ti])[21], uC = reinterpret_cast<const float *>(S.planeA[ti])[22];
-        const float vA = reinterpret_cast<const float *>(S.planeA[ti])[23], vB = reinterpret_cast<const float *>(S.planeA[ti])[24], vC = reinterpret_cast<const float *>(S.planeA[ti])[25];
+        const float4 p5 = S.planeA[ti][5], p6 = S.planeA[ti][6];
+        const float uA = p5.x, uB = p5.y, uC = p5.z;
+        const float vA = p5.w, vB = p6.x, vC = p6.y;
         float u[4], v[4];
 #pragma unroll
         for(int j = 0; j < 4; j++)
@@ -2288,14 +2294,15 @@ __device__ __forceinline__ int warp_incl_scan(int v, int lane)
 template<int MS, class SH>
 __device__ __forceinline__ float sample_depth(const DrawParams &D, const SH &S, int ti, int qx, int y, int i, int q)
 {
-    float xF = ((float)qx + (float)(i & 1)) - reinterpret_cast<const float *>(S.planeA[ti])[0];
-    float yF = ((float)y + (float)(i >> 1)) - reinterpret_cast<const float *>(S.planeA[ti])[1];
+    const float4 p0 = S.planeA[ti][0];
+    float xF = ((float)qx + (float)(i & 1)) - p0.x;
+    float yF = ((float)y + (float)(i >> 1)) - p0.y;
     if(MS > 1)
     {
         yF = yF + SLY[q];
         xF = xF - SLX[q];
     }
-    float z = mul_add(xF, reinterpret_cast<const float *>(S.planeA[ti])[2], reinterpret_cast<const float *>(S.planeA[ti])[4] + yF * reinterpret_cast<const float *>(S.planeA[ti])[3]);
+    float z = mul_add(xF, p0.z, S.planeA[ti][1].x + yF * p0.w);
     if(SH::kFull && D.depthBias) z = z + reinterpret_cast<const float *>(S.planeA[ti])[PLANE_ZBIAS];  // PixelRoutine.cpp:141-144
     return depth_value<SH::kFull>(D, rmin(rmax(z, D.minDepthClamp), D.maxDepthClamp));  // clampDepth
 }
@@ -2503,8 +2510,8 @@ __device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared<CF, 
                         // triangle's z plane read once: x and y relative to the
                         // plane origin per column / row, z = MulAdd(x, A, C + y B)
                         const int lx = qx - bx0, ly = 2 * qrow, y = by0 + 2 * qrow;
-                        const float x0p = reinterpret_cast<const float *>(S.planeA[qti])[0], y0p = reinterpret_cast<const float *>(S.planeA[qti])[1];
-                        const float zA = reinterpret_cast<const float *>(S.planeA[qti])[2], zB = reinterpret_cast<const float *>(S.planeA[qti])[3], zC = reinterpret_cast<const float *>(S.planeA[qti])[4];
+                        const float4 p0 = S.planeA[qti][0];
+                        const float x0p = p0.x, y0p = p0.y, zA = p0.z, zB = p0.w, zC = S.planeA[qti][1].x;
                         const float zBias = (FULL && D.depthBias) ? reinterpret_cast<const float *>(S.planeA[qti])[PLANE_ZBIAS] : 0.0f;
                         const float xc[2] = {(float)qx - x0p, ((float)qx + 1.0f) - x0p};
                         const float yr[2] = {(float)y - y0p, ((float)y + 1.0f) - y0p};
