@@ -875,36 +875,34 @@ static __device__ __noinline__ void trim_clipped_unstored(const DrawParams &D, u
     }
 }
 
-// Span rows [yMin, yMax) of an unclipped triangle (X, Y snapped vertices,
-// shifted by the sample offset for 4x MSAA), row by row: each row's left and
-// right come from the edges covering it, walked by the reference's DDA
-// (SetupRoutine::edge, :550-621), and are stored as one word.  A triangle's
-// edges on one side cover disjoint rows, so this equals the reference's
-// edge-by-edge outline.  Rows no edge covers get the empty span 0 (only
-// sample outlines of 4x MSAA have them).  Returns the first and one past the
-// last row with left != right (the trim of :243-264; first = last = yMax when
-// every row is empty).
-__device__ __forceinline__ void spans_triangle(const DrawParams &D, int32_t X0, int32_t Y0, int32_t X1, int32_t Y1, int32_t X2,
-                                               int32_t Y2, int dW, int32_t yMin, int32_t yMax, uint32_t *sp, int32_t &first,
-                                               int32_t &last)
+// Span rows [yMin, yMax) of an N-vertex outline in registers -- an unclipped
+// triangle (shifted by the sample offset for 4x MSAA) or a clipped polygon of
+// at most 4 vertices -- row by row: each row's left and right come from the
+// edges covering it, walked by the reference's DDA (SetupRoutine::edge,
+// :550-621), and are stored as one word.  The edges on one side of a convex
+// outline cover disjoint rows, so this equals the reference's edge-by-edge
+// outline.  Rows no edge covers get the empty span 0 (only sample outlines of
+// 4x MSAA have them).  Returns the first and one past the last row with
+// left != right (the trim of :243-264; first = last = yMax when every row is
+// empty).
+template<int N>
+__device__ __forceinline__ void spans_outline(const DrawParams &D, const int32_t (&Xs)[N], const int32_t (&Ys)[N], int dW, int32_t yMin,
+                                              int32_t yMax, uint32_t *sp, int32_t &first, int32_t &last)
 {
     // edges in the reference's order: edge i runs from vertex i+1-d to vertex i+d
-    EdgeDDA e[3];
-    bool ok[3];
-    int32_t ex[3], ed[3];
-    {
-        const int32_t Xs[3] = {X0, X1, X2}, Ys[3] = {Y0, Y1, Y2};
+    EdgeDDA e[N];
+    bool ok[N];
+    int32_t ex[N], ed[N];
 #pragma unroll
-        for(int i = 0; i < 3; i++)
-        {
-            int ia = i + 1 - dW, ib = i + dW;
-            ia = ia == 3 ? 0 : ia;
-            ib = ib == 3 ? 0 : ib;
-            ok[i] = edge_setup(D, Xs[ia], Ys[ia], Xs[ib], Ys[ib], e[i]);
-            ex[i] = 0;
-            ed[i] = 0;
-            if(ok[i]) ex[i] = edge_x_at(e[i], e[i].yMin, &ed[i]);
-        }
+    for(int i = 0; i < N; i++)
+    {
+        int ia = i + 1 - dW, ib = i + dW;
+        ia = ia == N ? 0 : ia;
+        ib = ib == N ? 0 : ib;
+        ok[i] = edge_setup(D, Xs[ia], Ys[ia], Xs[ib], Ys[ib], e[i]);
+        ex[i] = 0;
+        ed[i] = 0;
+        if(ok[i]) ex[i] = edge_x_at(e[i], e[i].yMin, &ed[i]);
     }
     first = yMax;
     last = yMax;
@@ -913,7 +911,7 @@ __device__ __forceinline__ void spans_triangle(const DrawParams &D, int32_t X0, 
     {
         int32_t l = 0, r = 0;
 #pragma unroll
-        for(int i = 0; i < 3; i++)
+        for(int i = 0; i < N; i++)
         {
             if(ok[i] && y >= e[i].yMin && y < e[i].yMax)
             {
@@ -936,10 +934,95 @@ __device__ __forceinline__ void spans_triangle(const DrawParams &D, int32_t X0, 
     if(first < yMax) last = lastNonEmpty + 1;
 }
 
+__device__ __forceinline__ void spans_triangle(const DrawParams &D, int32_t X0, int32_t Y0, int32_t X1, int32_t Y1, int32_t X2,
+                                               int32_t Y2, int dW, int32_t yMin, int32_t yMax, uint32_t *sp, int32_t &first,
+                                               int32_t &last)
+{
+    const int32_t Xs[3] = {X0, X1, X2}, Ys[3] = {Y0, Y1, Y2};
+    spans_outline<3>(D, Xs, Ys, dW, yMin, yMax, sp, first, last);
+}
+
+// Clipped triangle whose vertices lie outside one clip plane only (plane k of
+// Clipper::Clip's order): that plane's Sutherland-Hodgman pass (clipNear ..
+// clipBottom, src/Device/Clipper.cpp:32-265) on the three vertices in
+// registers -- each vertex i emits itself when inside and the crossing of
+// edge (i, i+1) when the edge crosses, in the pass's order -- then the
+// reprojection, y range and x extent as setup_clipped.  The polygon (at most
+// 4 vertices, X/Y) stays in registers for the span rows and is also stored
+// in the polygon scratch for the raster's fallback.  Returns the vertex count
+// (0: clipped away or empty y range; -1: polygon scratch full).
+static __device__ __forceinline__ int setup_clipped_one(const DrawParams &D, const float4 c0, const float4 c1, const float4 c2, int k,
+                                                        int32_t &yMin, int32_t &yMax, int32_t &xMinS, int32_t &xMaxS, uint32_t &slot,
+                                                        int32_t (&X)[4], int32_t (&Y)[4])
+{
+    const CVert P[3] = {{c0.x, c0.y, c0.z, c0.w}, {c1.x, c1.y, c1.z, c1.w}, {c2.x, c2.y, c2.z, c2.w}};
+    float d[3];
+#pragma unroll
+    for(int i = 0; i < 3; i++) d[i] = plane_dist(P[i], k);
+    // emitted vertices in order: P_i when inside, then E_i when edge (i, i+1) crosses
+    bool inP[3], inE[3];
+    CVert E[3];
+    int posP[3], posE[3], t = 0;
+#pragma unroll
+    for(int i = 0; i < 3; i++)
+    {
+        const int j = i == 2 ? 0 : i + 1;
+        inP[i] = d[i] >= 0.0f;
+        inE[i] = inP[i] ? d[j] < 0.0f : d[j] > 0.0f;
+        E[i] = inP[i] ? clip_edge(P[i], P[j], d[i], d[j]) : clip_edge(P[j], P[i], d[j], d[i]);
+        posP[i] = t;
+        t += inP[i] ? 1 : 0;
+        posE[i] = t;
+        t += inE[i] ? 1 : 0;
+    }
+    const int n = t;
+    if(n < 3) return 0;
+#pragma unroll
+    for(int m = 0; m < 4; m++)
+    {
+        CVert v = P[0];
+#pragma unroll
+        for(int i = 0; i < 3; i++)
+        {
+            if(inP[i] && posP[i] == m) v = P[i];
+            if(inE[i] && posE[i] == m) v = E[i];
+        }
+        const float rhw = v.w != 0.0f ? 1.0f / v.w : 1.0f;
+        X[m] = round_int(D.X0xF + (v.x * rhw) * D.WxF);
+        Y[m] = round_int(D.Y0xF + (v.y * rhw) * D.HxF);
+    }
+    if(n == 3)
+    {
+        X[3] = X[2];
+        Y[3] = Y[2];
+    }
+    yMin = min(min(Y[0], Y[1]), min(Y[2], Y[3]));
+    yMax = max(max(Y[0], Y[1]), max(Y[2], Y[3]));
+    xMinS = min(min(X[0], X[1]), min(X[2], X[3]));
+    xMaxS = max(max(X[0], X[1]), max(X[2], X[3]));
+    yMin = max((yMin + 0xFF) >> 8, D.sy0);
+    yMax = min((yMax + 0xFF) >> 8, D.sy1);
+    if(yMin >= yMax) return 0;
+    slot = atomicAdd(D.polyCount, 1u);
+    if(slot >= D.polyCapacity)
+    {
+        atomicOr(D.error, ERR_POLY_OVERFLOW);
+        return -1;
+    }
+#pragma unroll
+    for(int m = 0; m < 4; m++)
+        if(m < n) D.poly[(size_t)slot * MAX_POLY + m] = make_int2(X[m], Y[m]);
+    return n;
+}
+
 // One SETUP_THREADS-triangle block of a draw (block index 'blk' within the
 // draw), one thread per triangle: trivial reject, culling, clipping, y range,
 // span rows (allocated per warp), pixel box, record and plane equations; per
 // warp the chunk box, the super-chunk box and the counters.  No block barrier.
+// CLIP_ONE: triangles clipped by one plane take setup_clipped_one (the
+// batched kernel, whose draw records live in global memory, leaves it out:
+// it would spill there).
+template<bool CLIP_ONE>
 __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
 {
     const uint32_t t = blk * SETUP_THREADS + threadIdx.x;
@@ -952,6 +1035,8 @@ __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
     int32_t X0 = 0, X1 = 0, X2 = 0, Y0 = 0, Y1 = 0, Y2 = 0;
     int32_t yMin = 0, yMax = 0, xMinS = 0, xMaxS = 0;
     uint32_t slot = 0, vs0 = 0, vs1 = 0, vs2 = 0;  // post-transform vertex slots
+    int32_t X3 = 0, Y3 = 0;  // fourth vertex of a polygon clipped by one plane
+    bool clipOne = false;    // the polygon (X0..X3, Y0..Y3) came from setup_clipped_one
     if(t < D.count && tri_valid(D, t))
     {
         cntIn = 1;
@@ -987,7 +1072,21 @@ __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
                 frontBit = front ? 1 : 0;
                 bool keep = !((D.cullMode & SWGB_CULL_FRONT) && front) && !((D.cullMode & SWGB_CULL_BACK) && !front);
                 dW = A > 0.0f ? 1 : 0;
-                if(keep && cntClip)
+                const int planes = flagsOr & CLIP_FRUSTUM;
+                if(CLIP_ONE && keep && cntClip && D.ms == 1 && (planes & (planes - 1)) == 0)
+                {
+                    // one plane (the common case: triangles across a side of the
+                    // view): the clipper's single pass in registers
+                    const int k = planes == CLIP_NEAR ? 0 : planes == CLIP_FAR ? 1 : planes == CLIP_LEFT ? 2 :
+                                  planes == CLIP_RIGHT ? 3 : planes == CLIP_TOP ? 4 : 5;
+                    int32_t PX[4], PY[4];
+                    n = setup_clipped_one(D, vc[0], vc[1], vc[2], k, yMin, yMax, xMinS, xMaxS, slot, PX, PY);
+                    cand = n >= 3;
+                    clipOne = true;
+                    X0 = PX[0]; X1 = PX[1]; X2 = PX[2]; X3 = PX[3];
+                    Y0 = PY[0]; Y1 = PY[1]; Y2 = PY[2]; Y3 = PY[3];
+                }
+                else if(keep && cntClip)
                 {
                     n = setup_clipped(D, vc[0], vc[1], vc[2], flagsOr, yMin, yMax, xMinS, xMaxS, slot);
                     cand = n >= 3;
@@ -1033,7 +1132,14 @@ __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
         stored = off + (uint64_t)rows * (uint32_t)D.ms <= (uint64_t)D.spanCapacity;
         uint32_t *sp = D.spans + off;
         int32_t tMin = yMin, tMax = yMax;
-        if(stored && cntClip)
+        if(stored && clipOne && n == 4)
+        {
+            const int32_t Xs[4] = {X0, X1, X2, X3}, Ys[4] = {Y0, Y1, Y2, Y3};
+            spans_outline<4>(D, Xs, Ys, dW, yMin, yMax, sp, tMin, tMax);
+        }
+        else if(stored && clipOne)
+            spans_triangle(D, X0, Y0, X1, Y1, X2, Y2, dW, yMin, yMax, sp, tMin, tMax);
+        else if(stored && cntClip)
             spans_clipped(D, slot, n, dW, yMin, yMax, sp, tMin, tMax);
         else if(stored && D.ms > 1)
         {
@@ -1180,7 +1286,7 @@ __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
 }
 
 #ifndef SWGB_RASTER_TU
-__global__ void __launch_bounds__(SETUP_THREADS) k_setup(const __grid_constant__ DrawParams D) { setup_body(D, blockIdx.x); }
+__global__ void __launch_bounds__(SETUP_THREADS) k_setup(const __grid_constant__ DrawParams D) { setup_body<true>(D, blockIdx.x); }
 
 // Order of a draw's bins for the persistent raster warps.  Longest first:
 // the setup stage's difference array integrated in shared memory into
@@ -3012,7 +3118,7 @@ __global__ void __launch_bounds__(SETUP_THREADS, 3) k_setup_batch(const __grid_c
     for(uint32_t u = blockIdx.x; u < h.sblocks; u += gridDim.x)
     {
         const uint32_t d = find_draw(V.sStart, h.n, u);
-        setup_body(V.draws[d], u - __ldg(V.sStart + d));
+        setup_body<false>(V.draws[d], u - __ldg(V.sStart + d));
     }
 }
 
