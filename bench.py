@@ -228,7 +228,9 @@ def run_ours(args):
     time.sleep(0.3)
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    r.set_kernel_timing(True)
+    # live event pairs around k_raster only (the roofline's kernel); the
+    # other kernels' times come from an untimed pass after the timed region
+    r.set_kernel_timing(True, kinds=["raster"])
     barrier()
     torch.cuda.synchronize()
     launches0 = r.launch_count()
@@ -245,9 +247,17 @@ def run_ours(args):
     r.set_kernel_timing(False)
     ktimes = r.kernel_times()
     clk = clocks.stop()
+    cnt = r.counters()
+    # every kernel of the same frames, each launch timed (outside the timed region)
+    r.set_kernel_timing(True)
+    for i in range(args.steps):
+        flush.fill_(i & 0xFF)
+        ds.clear()
+        r.draw(st, a)
+    r.set_kernel_timing(False)
+    ktimes_all = r.kernel_times()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     ms_per_step = sum(step_ms) / len(step_ms)
-    cnt = r.counters()
     frames = args.steps
     frag_per_frame = cnt["fragments_passed"] / frames
     tested_per_frame = cnt["fragments_tested"] / frames
@@ -323,7 +333,7 @@ def run_ours(args):
     rast_ms, rast_n = ktimes.get("raster", (0.0, 0))
     rast_avg = rast_ms / max(1, rast_n)
     achieved = raster_bytes / (rast_avg * 1e-3) / 1e9 if rast_avg > 0 else 0.0
-    kernels = {k: {"avg_ms": v[0] / max(1, v[1]), "launches": v[1]} for k, v in ktimes.items()}
+    kernels = {k: {"avg_ms": v[0] / max(1, v[1]), "launches": v[1]} for k, v in ktimes_all.items()}
     value = world * frag_per_frame / (ms_per_step * 1e-3) / 1e9
     line = {
         "metric": "Gfrag/s",
@@ -348,6 +358,8 @@ def run_ours(args):
         "frame_algorithmic_bytes": frame_bytes,
         "frame_achieved_gbs": round(frame_bytes / (ms_per_step * 1e-3) / 1e9, 1),
         "kernels": kernels,
+        "kernels_how": "k_raster (the roofline) timed by CUDA events inside the timed region; every kernel, "
+                       "each launch between events, in an untimed pass of the same frames",
         "roofline": {"kernel": "k_raster", "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "algorithmic_bytes_per_launch": raster_bytes, "traffic": None},

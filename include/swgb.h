@@ -523,10 +523,13 @@ swgb_status swgb_reset_counters(swgb_ctx *ctx);
 uint64_t swgb_launch_count(swgb_ctx *ctx);
 
 /* Kernel timing for benchmarks: with enable = 1 the context records a CUDA
- * event pair on its stream around every kernel launch.  swgb_get_kernel_times
- * synchronises, sums the elapsed milliseconds per kernel kind
- * (SWGB_KERNEL_*) into ms[] and the launch counts into launches[], then
+ * event pair on its stream around every kernel launch; with enable =
+ * SWGB_KERNEL_TIMING_KINDS(mask) only around launches of the kinds whose bit
+ * (1 << SWGB_KERNEL_*) is in mask (each pair costs the stream a little time).
+ * swgb_get_kernel_times synchronises, sums the elapsed milliseconds per kernel
+ * kind (SWGB_KERNEL_*) into ms[] and the launch counts into launches[], then
  * forgets the recorded pairs. */
+#define SWGB_KERNEL_TIMING_KINDS(mask) (0x10000 | ((mask) & 0xFFFF))
 #define SWGB_KERNEL_VERTEX 0
 #define SWGB_KERNEL_SETUP 1
 #define SWGB_KERNEL_RASTER 2

@@ -53,6 +53,8 @@ using namespace swgbk;
 struct swgb_ctx {
     int device;
     cudaStream_t stream;
+    cudaStream_t side;            // second stream: k_bin_order beside k_bin_list
+    cudaEvent_t sideFork, sideJoin;
     bool ownStream;
     float4 *ptv;
     size_t ptvCap;
@@ -93,6 +95,7 @@ struct swgb_ctx {
     uint64_t launches;
     bool rasterAttr;
     bool timing;
+    uint32_t timingKinds;  // bit k: launches of kind k get an event pair while timing
     std::vector<cudaEvent_t> *evFree;           // recycled events
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> *evPairs;
     struct BatchState *batch;                   // batched-draw scratch, descriptors and graphs
@@ -508,20 +511,22 @@ cudaEvent_t take_event(swgb_ctx *ctx)
 
 // Launch helper: records a CUDA event pair around the launch when timing is on.
 template<typename F>
-void timed_launch(swgb_ctx *ctx, int kind, F &&launch)
+void timed_launch(swgb_ctx *ctx, int kind, F &&launch, cudaStream_t on = nullptr)
 {
     cudaEvent_t a = nullptr, b = nullptr;
-    if(ctx->timing)
+    const bool timed = ctx->timing && (ctx->timingKinds >> kind & 1u);
+    if(!on) on = ctx->stream;
+    if(timed)
     {
         a = take_event(ctx);
         b = take_event(ctx);
-        cudaEventRecord(a, ctx->stream);
+        cudaEventRecord(a, on);
     }
     launch();
     ctx->launches++;
-    if(ctx->timing)
+    if(timed)
     {
-        cudaEventRecord(b, ctx->stream);
+        cudaEventRecord(b, on);
         ctx->evPairs->push_back({kind, {a, b}});
     }
 }
@@ -644,15 +649,29 @@ swgb_status enqueue(swgb_ctx *ctx, DrawParams &D)
     timed_launch(ctx, SWGB_KERNEL_VERTEX, [&] { k_vertex<<<(nv + 255) / 256, 256, 0, ctx->stream>>>(D, nv); });
     const uint32_t setupBlocks = (uint32_t)((D.count + SETUP_THREADS - 1) / SETUP_THREADS);
     timed_launch(ctx, SWGB_KERNEL_SETUP, [&] { k_setup<<<setupBlocks, SETUP_THREADS, 0, ctx->stream>>>(D); });
+    // the bin order (one block) and the bin lists depend on the setup stage
+    // only: with both, the order runs on the side stream beside the lists
+    const bool fork = D.binOrder && D.binList && ctx->side;
+    if(fork)
+    {
+        cudaEventRecord(ctx->sideFork, ctx->stream);
+        cudaStreamWaitEvent(ctx->side, ctx->sideFork, 0);
+    }
     if(D.binOrder)
     {
         const size_t smem = (size_t)(D.binsX + 1) * (D.binsY + 1) * sizeof(int);
-        timed_launch(ctx, SWGB_KERNEL_BIN_ORDER, [&] { k_bin_order<<<1, BIN_ORDER_THREADS, smem, ctx->stream>>>(D); });
+        cudaStream_t on = fork ? ctx->side : ctx->stream;
+        timed_launch(ctx, SWGB_KERNEL_BIN_ORDER, [&] { k_bin_order<<<1, BIN_ORDER_THREADS, smem, on>>>(D); }, on);
     }
     if(D.binList)
     {
         const uint32_t blocks = (uint32_t)((D.binsX * D.binsY + BIN_LIST_WARPS - 1) / BIN_LIST_WARPS);
         timed_launch(ctx, SWGB_KERNEL_BIN_ORDER, [&] { k_bin_list<<<blocks, 32 * BIN_LIST_WARPS, 0, ctx->stream>>>(D); });
+    }
+    if(fork)
+    {
+        cudaEventRecord(ctx->sideJoin, ctx->side);
+        cudaStreamWaitEvent(ctx->stream, ctx->sideJoin, 0);
     }
     if(D.binsX > 0 && D.binsY > 0)
     {
@@ -1431,6 +1450,15 @@ swgb_status swgb_ctx_create(int device, void *stream, swgb_ctx **out)
         if((s = cuda_check(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream")) != SWGB_OK) { delete c; return s; }
         c->ownStream = true;
     }
+    if(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+       cudaEventCreateWithFlags(&c->sideFork, cudaEventDisableTiming) != cudaSuccess ||
+       cudaEventCreateWithFlags(&c->sideJoin, cudaEventDisableTiming) != cudaSuccess)
+    {
+        // without them the bin order runs on the context's stream
+        cudaGetLastError();
+        if(c->side) cudaStreamDestroy(c->side);
+        c->side = nullptr;
+    }
     if(const char *lim = getenv("SWGB_SPAN_ROWS")) c->spanRowsLimit = strtoull(lim, nullptr, 10);
     // bin lists: SWGB_BIN_LIST entries per bin (0: none), for draws of at
     // least SWGB_BIN_LIST_MIN triangles
@@ -1486,6 +1514,13 @@ swgb_status swgb_ctx_destroy(swgb_ctx *c)
     cudaFree(c->counters);
     cudaFree(c->error);
     if(c->ownStream && c->stream) cudaStreamDestroy(c->stream);
+    if(c->side)
+    {
+        cudaStreamSynchronize(c->side);
+        cudaStreamDestroy(c->side);
+    }
+    if(c->sideFork) cudaEventDestroy(c->sideFork);
+    if(c->sideJoin) cudaEventDestroy(c->sideJoin);
     if(c->evPairs)
         for(auto &p : *c->evPairs)
         {
@@ -2062,6 +2097,7 @@ swgb_status swgb_set_kernel_timing(swgb_ctx *ctx, int enable)
 {
     if(!ctx) return SWGB_INVALID_ARG;
     ctx->timing = enable != 0;
+    ctx->timingKinds = (enable & 0x10000) ? (uint32_t)(enable & 0xFFFF) : 0xFFFFu;
     return SWGB_OK;
 }
 

@@ -1390,7 +1390,7 @@ __global__ void __launch_bounds__(BIN_ORDER_THREADS) k_bin_order(const __grid_co
 // bin's candidates 32 at a time.  A bin with more than binListCap candidates
 // stops there with a count above the capacity, and the raster walks it
 // itself.  The triangle boxes of up to four hit chunks are loaded together.
-// On the 1M-triangle 1080p height field this took 21 us and made k_raster
+// On the 1M-triangle 1080p height field this took ~60 us and made k_raster
 // 1.09 -> 1.015 ms.
 constexpr int BIN_LIST_WARPS = 8;
 __global__ void __launch_bounds__(32 * BIN_LIST_WARPS) k_bin_list(const __grid_constant__ DrawParams D)

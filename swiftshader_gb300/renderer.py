@@ -118,8 +118,13 @@ class Renderer:
     def launch_count(self):
         return int(self._L.swgb_launch_count(self._ctx))
 
-    def set_kernel_timing(self, enable):
-        check(self._L.swgb_set_kernel_timing(self._ctx, 1 if enable else 0), "swgb_set_kernel_timing")
+    def set_kernel_timing(self, enable, kinds=None):
+        """Event pairs around every kernel launch (enable), or only around the
+        launches of the kernel kinds named in kinds (KERNEL_NAMES)."""
+        v = 1 if enable else 0
+        if enable and kinds is not None:
+            v = 0x10000 | sum(1 << self.KERNEL_NAMES.index(k) for k in kinds)  # SWGB_KERNEL_TIMING_KINDS
+        check(self._L.swgb_set_kernel_timing(self._ctx, v), "swgb_set_kernel_timing")
 
     # --- sw::Blitter steps either side of a draw (swgb_clear / swgb_resolve /
     # swgb_blit); images are abi.Image views, e.g. from image_view().
@@ -203,11 +208,11 @@ class DeviceScene:
         self.d16 = scene.depth_format == abi.FORMAT_D16_UNORM
         self.depth = torch.empty(dshape, dtype=torch.int16 if self.d16 else torch.float32, device=self.device)
         self.stencil = None if scene.stencil is None else torch.empty(dshape, dtype=torch.uint8, device=self.device)
+        self._clear_rgba = None
         self.clear()
 
     def clear(self):
-        import torch
-        self.color[...] = torch.tensor(self.scene.clear_color, dtype=self.color.dtype, device=self.device)
+        self.color[...] = device_value(self, "_clear_rgba", self.scene.clear_color, self.color)
         if self.d16:
             self.depth.fill_(int(np.array(scenes.depth_clear_value(self.scene)).view(np.int16)))
         else:
@@ -260,7 +265,7 @@ class DeviceBatch:
             self.args[i] = scenes.build_args(sc)
 
     def clear(self):
-        self.color[...] = torch_tensor(self.batch.clear_color, self.color)
+        self.color[...] = device_value(self, "_clear_rgba", self.batch.clear_color, self.color)
         self.depth.fill_(self.batch.clear_depth)
 
     def draw_batch(self, renderer):
@@ -290,6 +295,18 @@ def image_view(tensor, format, samples=1):
     bpp = abi.TEXEL_BYTES[format]
     pitch = w * bpp
     return abi.Image(t.data_ptr(), format, w, h, samples, pitch, pitch * h)
+
+
+def device_value(owner, attr, values, like):
+    """values as a device tensor like 'like', kept on owner.attr and made again
+    only when values change: a clear then copies on the device alone, with no
+    host-to-device copy in the stream."""
+    key = (tuple(values), like.dtype, like.device)
+    cached = getattr(owner, attr, None)
+    if cached is None or cached[0] != key:
+        cached = (key, torch_tensor(values, like))
+        setattr(owner, attr, cached)
+    return cached[1]
 
 
 def torch_tensor(values, like):
