@@ -14,28 +14,45 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libswgb_oracle.so")
+# the timing build: FPU flush-to-zero mode instead of the software flush, -O3;
+# used only to time the CPU baseline, after its frame is compared with LIB's
+LIB_TIMING = os.path.join(BUILD, "libswgb_oracle_timing.so")
 SRC = os.path.join(HERE, "swgb_oracle.c")
 SRC_BLIT = os.path.join(HERE, "swgb_oracle_blit.c")
 CFLAGS = ["-O2", "-fPIC", "-shared", "-std=c11", "-fwrapv", "-ffp-contract=off", "-fno-fast-math",
           "-Wall", "-Wextra"]
 
 _lib = None
+_lib_timing = None
 
 
-def build(force=False):
+def build(force=False, timing=False):
     os.makedirs(BUILD, exist_ok=True)
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(
+    out = LIB_TIMING if timing else LIB
+    if not force and os.path.exists(out) and os.path.getmtime(out) >= max(
             os.path.getmtime(SRC), os.path.getmtime(SRC_BLIT), os.path.getmtime(os.path.join(HERE, "swgb_oracle.h")),
             os.path.getmtime(os.path.join(os.path.dirname(HERE), "include", "swgb.h"))):
-        return LIB
-    tmp = LIB + ".tmp%d" % os.getpid()
-    subprocess.check_call(["gcc"] + CFLAGS + ["-o", tmp, SRC, SRC_BLIT, "-lm", "-lpthread"])
-    os.replace(tmp, LIB)
-    return LIB
+        return out
+    tmp = out + ".tmp%d" % os.getpid()
+    flags = [f if f != "-O2" else "-O3" for f in CFLAGS] + ["-DSWGB_ORACLE_HW_FLUSH"] if timing else CFLAGS
+    subprocess.check_call(["gcc"] + flags + ["-o", tmp, SRC, SRC_BLIT, "-lm", "-lpthread"])
+    os.replace(tmp, out)
+    return out
 
 
-def lib():
-    global _lib
+def lib(timing=False):
+    """The checker build, or with timing=True the timing build."""
+    global _lib, _lib_timing
+    if timing:
+        if _lib_timing is None:
+            from swiftshader_gb300 import abi
+            L = C.CDLL(build(timing=True))
+            L.oracle_draw.argtypes = [C.POINTER(abi.PipelineState), C.POINTER(abi.DrawArgs), C.c_int,
+                                      C.POINTER(abi.Counters)]
+            L.oracle_draw.restype = C.c_int
+            L.oracle_timing_build.restype = C.c_int
+            _lib_timing = L
+        return _lib_timing
     if _lib is None:
         import sys
         sys.path.insert(0, os.path.dirname(HERE))
@@ -166,10 +183,10 @@ def host_state(scene, color, depth, stencil=None):
     return st, args, keep
 
 
-def render(scene, nthreads=1, color=None, depth=None, stencil=None):
+def render(scene, nthreads=1, color=None, depth=None, stencil=None, timing=False):
     """Runs one draw of 'scene' on the CPU oracle; returns (color, depth, counters dict).
     A scene with a stencil state draws into 'stencil' (a fresh cleared one when
-    None; render_stencil returns it)."""
+    None; render_stencil returns it).  timing=True runs the timing build."""
     from swiftshader_gb300 import abi, scenes
     if color is None or depth is None:
         color, depth = scenes.clear_buffers(scene)
@@ -177,7 +194,7 @@ def render(scene, nthreads=1, color=None, depth=None, stencil=None):
         stencil = scenes.stencil_buffer(scene)
     st, args, keep = host_state(scene, color, depth, stencil)
     cnt = abi.Counters()
-    s = lib().oracle_draw(C.byref(st), C.byref(args), nthreads, C.byref(cnt))
+    s = lib(timing).oracle_draw(C.byref(st), C.byref(args), nthreads, C.byref(cnt))
     if s != 0:
         raise RuntimeError("oracle_draw failed: %s" % abi.STATUS_NAMES.get(s, s))
     del keep

@@ -85,7 +85,12 @@ def raster(st, vf, vi, consts, scissor, ntri, nv):
     """Reference rasteriser + shaderless pixel routine over all triangles of a
     draw (the depth / stencil attachments of st are host arrays updated in
     place); returns (visible, clipped, occlusion samples)."""
-    counts = np.zeros(3, np.uint64)
+    return raster_timed(st, vf, vi, consts, scissor, ntri, nv)[:3]
+
+
+def raster_timed(st, vf, vi, consts, scissor, ntri, nv):
+    """raster() plus the nanoseconds of its setup loop and of the pixel routine."""
+    counts = np.zeros(5, np.uint64)
     r = lib().refjit_raster(C.byref(st), consts.ctypes.data, scissor.ctypes.data, vf.ctypes.data, vi.ctypes.data,
                             ntri, nv, counts.ctypes.data)
     if r != 0:

@@ -18,7 +18,9 @@
  *                      src/Pipeline/PixelRoutine.cpp) of a pipeline without a
  *                      fragment shader (spirvShader == nullptr: coverage, depth
  *                      bias, depth clamp, depth bounds, stencil, depth test and
- *                      write, occlusion count), one cluster, primitive order.
+ *                      write, occlusion count), one cluster, primitive order;
+ *                      counts[] = {visible, clipped, occlusion samples,
+ *                      nanoseconds of the setup loop, of the pixel routine}.
  *
  * The vertex stage (VertexRoutine + the MVP shader) and the draw constants
  * (Renderer::draw) stay the oracle's: the caller passes the oracle's vertex
@@ -45,6 +47,7 @@
 
 #include "swgb.h"
 
+#include <chrono>
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
@@ -543,6 +546,7 @@ int refjit_raster(const swgb_pipeline_state *st, const float *consts, const int3
 	prims.reserve((size_t)ntri * ms);
 	std::vector<sw::Primitive> one(ms);
 	uint64_t visible = 0, clippedN = 0;
+	const auto t0 = std::chrono::steady_clock::now();
 	for(int t = 0; t < ntri; t++)
 	{
 		fill_vertex(tri->v0, vf + (3 * t + 0) * kVF, vi + (3 * t + 0) * kVI, nv);
@@ -559,10 +563,15 @@ int refjit_raster(const swgb_pipeline_state *st, const float *consts, const int3
 	}
 	// the pixel routine walks `count` primitives of stride ms * sizeof(Primitive)
 	// (QuadRasterizer.cpp:71-100, one cluster covers every row)
+	const auto t1 = std::chrono::steady_clock::now();
 	if(visible) proutine(env().dev(), prims.data(), (int)visible, 0, 1, data.get());
+	const auto t2 = std::chrono::steady_clock::now();
 	counts[0] = visible;
 	counts[1] = clippedN;
 	counts[2] = data->occlusion[0];
+	// nanoseconds of the setup loop and of the pixel routine's call
+	counts[3] = (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(t1 - t0).count();
+	counts[4] = (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(t2 - t1).count();
 	return 0;
 }
 

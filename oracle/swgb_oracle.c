@@ -11,7 +11,11 @@
  * reference routine it restates.  The reference's JIT code is x86 Reactor;
  * its numeric semantics (src/Reactor/LLVMReactor.cpp) are restated:
  *   - all float math with FTZ+DAZ (worker threads, src/System/SwiftConfig.cpp:136-139),
- *     emulated in software so the oracle gives the same bits on x86 and Arm;
+ *     emulated in software so the oracle gives the same bits on x86 and Arm
+ *     (the checker build); the timing build (-DSWGB_ORACLE_HW_FLUSH, used only
+ *     to time the CPU baseline) sets the FPU's flush-to-zero mode through
+ *     fenv.h on x86-64 and AArch64 instead, as the reference's worker threads
+ *     do, and its frames are compared with the checker build's before timing;
  *   - fused multiply-add only where Reactor emits MulAdd/mulAdd;
  *   - RoundInt = cvtss2si/cvtps2dq (half-even, INT_MIN when out of range),
  *     RoundIntClamped = nearbyint + fptosi.sat, Int(Float) = cvttss2si;
@@ -26,6 +30,7 @@
  */
 #include "swgb_oracle.h"
 
+#include <fenv.h>
 #include <math.h>
 #include <pthread.h>
 #include <stdint.h>
@@ -42,11 +47,34 @@ static inline uint32_t f2u(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
 static inline float u2f(uint32_t u) { float f; memcpy(&f, &u, 4); return f; }
 
 /* DAZ on inputs / FTZ on results: a subnormal becomes a zero of the same sign. */
+#if defined(SWGB_ORACLE_HW_FLUSH) && (defined(__x86_64__) || defined(__aarch64__))
+#define ORACLE_HW_FLUSH 1
+/* The FPU flushes subnormal inputs and results (hw_flush_on). */
+static inline float daz(float x) { return x; }
+#else
 static inline float daz(float x)
 {
     uint32_t u = f2u(x);
     if((u & 0x7F800000u) == 0) return u2f(u & 0x80000000u);
     return x;
+}
+#endif
+
+/* Timing build: the calling thread's FPU in flush-to-zero mode (MXCSR FTZ +
+ * DAZ on x86-64, FPCR.FZ on AArch64), as the reference sets it on its worker
+ * threads; new threads inherit it.  The checker build leaves the FPU alone. */
+static void hw_flush_on(fenv_t *saved)
+{
+    fegetenv(saved);
+#ifdef ORACLE_HW_FLUSH
+    fenv_t e = *saved;
+#if defined(__x86_64__)
+    e.__mxcsr |= 0x8040u;
+#else
+    e.__fpcr |= 1u << 24;
+#endif
+    fesetenv(&e);
+#endif
 }
 static inline float fadd(float a, float b) { return daz(daz(a) + daz(b)); }
 static inline float fsub(float a, float b) { return daz(daz(a) - daz(b)); }
@@ -1886,14 +1914,31 @@ static swgb_status draw_impl(const swgb_pipeline_state *st, const swgb_draw_args
 
 swgb_status oracle_draw(const swgb_pipeline_state *st, const swgb_draw_args *a, int nthreads, swgb_counters *cnt)
 {
-    return draw_impl(st, a, nthreads, cnt, NULL, NULL, 0);
+    fenv_t saved;
+    hw_flush_on(&saved);
+    const swgb_status s = draw_impl(st, a, nthreads, cnt, NULL, NULL, 0);
+    fesetenv(&saved);
+    return s;
 }
 
 swgb_status oracle_draw_visibility(const swgb_pipeline_state *st, const swgb_draw_args *a, int nthreads, swgb_counters *cnt,
                                    uint32_t *vis, uint32_t *visLen, int visCap)
 {
     if(!vis || !visLen || visCap < 1) return SWGB_INVALID_ARG;
-    return draw_impl(st, a, nthreads, cnt, vis, visLen, visCap);
+    fenv_t saved;
+    hw_flush_on(&saved);
+    const swgb_status s = draw_impl(st, a, nthreads, cnt, vis, visLen, visCap);
+    fesetenv(&saved);
+    return s;
+}
+
+int oracle_timing_build(void)
+{
+#ifdef ORACLE_HW_FLUSH
+    return 1;
+#else
+    return 0;
+#endif
 }
 
 /* ------------------------------------------------------------------------ */

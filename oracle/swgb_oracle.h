@@ -35,6 +35,10 @@ swgb_status oracle_draw(const swgb_pipeline_state *state, const swgb_draw_args *
 swgb_status oracle_draw_visibility(const swgb_pipeline_state *state, const swgb_draw_args *args, int nthreads, swgb_counters *cnt,
                                    uint32_t *vis, uint32_t *visLen, int visCap);
 
+/* 1 in the timing build (FPU flush-to-zero mode instead of the software
+ * flush; used only to time the CPU baseline), 0 in the checker build. */
+int oracle_timing_build(void);
+
 /* Primitive-level probes, exported so the reference's Reactor known-answer
  * vectors (tests/ReactorUnitTests/ReactorUnitTests.cpp) can pin them. */
 int32_t oracle_round_int(float x);         /* RoundInt: cvtss2si, half-even, INT_MIN on overflow */
