@@ -211,12 +211,12 @@ def run_ours(args):
         r.set_raster_config(w, h, bool(int(hz)))
         tune = {"best": r.raster_config(), "how": "fixed by --raster-config"}
     elif not args.no_autotune:
-        ds.clear()
+        ds.clear(r)
         tune = autotune_summary(*r.autotune([st], [a], batched=False))
 
     # warm-up
     for _ in range(args.warmup):
-        ds.clear()
+        ds.clear(r)
         r.draw(st, a)
     r.synchronize()
     r.reset_counters()
@@ -237,7 +237,7 @@ def run_ours(args):
     for i in range(args.steps):
         flush.fill_(i & 0xFF)  # L2 flush, outside the step's events
         starts[i].record(stream)
-        ds.clear()
+        ds.clear(r)
         r.draw(st, a)
         ends[i].record(stream)
     r.synchronize()
@@ -252,7 +252,7 @@ def run_ours(args):
     r.set_kernel_timing(True)
     for i in range(args.steps):
         flush.fill_(i & 0xFF)
-        ds.clear()
+        ds.clear(r)
         r.draw(st, a)
     r.set_kernel_timing(False)
     ktimes_all = r.kernel_times()
@@ -281,7 +281,7 @@ def run_ours(args):
             ds.indices.copy_(h_idx, non_blocking=True)
         for d_l, h_l in zip(ds.levels, h_lv):
             d_l.copy_(h_l, non_blocking=True)
-        ds.clear()
+        ds.clear(r)
         r.draw(st, a)
         h_color.copy_(ds.color, non_blocking=True)
         h_depth.copy_(ds.depth, non_blocking=True)

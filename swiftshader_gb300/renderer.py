@@ -211,7 +211,26 @@ class DeviceScene:
         self._clear_rgba = None
         self.clear()
 
-    def clear(self):
+    # colour formats whose clear value the Blitter clear takes exactly as
+    # normalised floats (UNORM8: byte / 255 rounds back to the byte)
+    _BLITTER_CLEAR = {abi.FORMAT_R8G8B8A8_UNORM: 255.0, abi.FORMAT_B8G8R8A8_UNORM: 255.0,
+                      abi.FORMAT_R32G32B32A32_SFLOAT: 1.0}
+
+    def clear(self, renderer=None):
+        """Clears the attachments to the scene's clear values: with a renderer
+        through the library's Blitter clear (swgb_clear, one kernel per
+        attachment), else by torch fills."""
+        sc = self.scene
+        scale = self._BLITTER_CLEAR.get(sc.color_format)
+        if renderer is not None and scale is not None and not self.d16 and self.stencil is None:
+            # clear_color holds the attachment's bytes in memory order; the
+            # Blitter clear takes R, G, B, A (B8G8R8A8 stores B first)
+            cc = list(sc.clear_color)
+            if sc.color_format == abi.FORMAT_B8G8R8A8_UNORM:
+                cc = [cc[2], cc[1], cc[0], cc[3]]
+            renderer.clear_image(image_view(self.color, sc.color_format, sc.samples), [v / scale for v in cc])
+            renderer.clear_image(image_view(self.depth, abi.FORMAT_D32_SFLOAT, sc.samples), sc.clear_depth)
+            return
         self.color[...] = device_value(self, "_clear_rgba", self.scene.clear_color, self.color)
         if self.d16:
             self.depth.fill_(int(np.array(scenes.depth_clear_value(self.scene)).view(np.int16)))

@@ -201,3 +201,36 @@ def test_blitter_errors(rend):
     with pytest.raises(SwgbError):
         rend.clear_image(img, (0, 0, 0, 0))
     rend.synchronize()
+
+
+@pytest.mark.parametrize("fmt,samples", [(abi.FORMAT_R8G8B8A8_UNORM, 1), (abi.FORMAT_B8G8R8A8_UNORM, 1),
+                                         (abi.FORMAT_R32G32B32A32_SFLOAT, 1), (abi.FORMAT_R8G8B8A8_UNORM, 4)])
+def test_scene_clear_through_blitter(gpu_lib, fmt, samples):
+    """DeviceScene.clear(renderer) (the library's Blitter clear, which the
+    benchmark's frames use) leaves the attachments exactly as the torch fills
+    of DeviceScene.clear() do, and a draw after it gives the same bits."""
+    import torch
+    from swiftshader_gb300 import DeviceScene, Renderer, scenes
+    s = scenes.scene_heightfield(quads_x=60, quads_y=30, width=160, height=96, tex_size=64)
+    s.color_format = fmt
+    s.samples = samples
+    if fmt == abi.FORMAT_R32G32B32A32_SFLOAT:
+        s.clear_color = (0.1, 0.2, 0.3, 0.4)
+    r = Renderer(0)
+    ds = DeviceScene(s)
+    torch.cuda.synchronize()
+    ref_c, ref_d = ds.color.clone(), ds.depth.clone()
+    ds.color.fill_(7)
+    ds.depth.fill_(-3.0)
+    ds.clear(r)
+    r.synchronize()
+    assert torch.equal(ds.color, ref_c)
+    assert torch.equal(ds.depth.view(torch.int32), ref_d.view(torch.int32))
+    r.draw(ds.state(), ds.args())
+    r.synchronize()
+    c1, d1 = ds.color.clone(), ds.depth.clone()
+    ds.clear()
+    r.draw(ds.state(), ds.args())
+    r.synchronize()
+    assert torch.equal(ds.color, c1)
+    assert torch.equal(ds.depth.view(torch.int32), d1.view(torch.int32))
