@@ -2990,24 +2990,26 @@ __device__ __forceinline__ void raster_bin(const DrawParams &D, RasterShared<CF,
 }
 
 // Shared memory of a raster block and the blocks one SM holds with it, at
-// most 5: the register budget follows from that (65536 / (blocks x
-// threads) = 102 registers), enough for the raster loop without spills; a
-// 6-block bound (80 registers, spilling) measured 5% slower on the 1M-triangle
-// frame.
+// most 4 without hierarchical depth rejection and 5 with it: the register
+// budget follows from that (65536 / (blocks x threads): 128 and 102
+// registers).  Measured on the 1M-triangle frame (no rejection): 4 blocks
+// 0.954 ms against 1.010 for 5 (96 registers) and 0.952 for 3; on the full
+// atlas's 16x16 rejection variant 5 blocks 1150 ms against 1172 for 4 and
+// 1345 for 3; a 6-block bound (80 registers, spilling) lost 5% earlier.
 template<int CF, int MS, int BW, int BH, bool FULL>
 constexpr size_t raster_smem()
 {
     static_assert(sizeof(RasterShared<CF, MS, BW, BH, FULL>) % 16 == 0, "each warp's shared block starts 16-byte aligned");
     return RASTER_WARPS * sizeof(RasterShared<CF, MS, BW, BH, FULL>);
 }
-template<int CF, int MS, int BW, int BH, bool FULL>
+template<int CF, int MS, int BW, int BH, bool FULL, bool HIZ = false>
 constexpr int raster_min_blocks()
 {
-    return (int)std::min<size_t>(5, std::max<size_t>(1, (size_t)(228 * 1024) / (raster_smem<CF, MS, BW, BH, FULL>() + 1024)));
+    return (int)std::min<size_t>(HIZ ? 5 : 4, std::max<size_t>(1, (size_t)(228 * 1024) / (raster_smem<CF, MS, BW, BH, FULL>() + 1024)));
 }
 
 template<int CF, int MS, int BW, int BH, bool HIZ, bool FULL>
-__global__ void __launch_bounds__(RASTER_THREADS, (raster_min_blocks<CF, MS, BW, BH, FULL>())) k_raster(const __grid_constant__ DrawParams D)
+__global__ void __launch_bounds__(RASTER_THREADS, (raster_min_blocks<CF, MS, BW, BH, FULL, HIZ>())) k_raster(const __grid_constant__ DrawParams D)
 {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -3125,7 +3127,7 @@ __global__ void __launch_bounds__(SETUP_THREADS, 3) k_setup_batch(const __grid_c
 #endif  // SWGB_RASTER_TU
 
 template<int CF, int MS, int BW, int BH, bool HIZ, bool FULL>
-__global__ void __launch_bounds__(RASTER_THREADS, (raster_min_blocks<CF, MS, BW, BH, FULL>())) k_raster_batch(const __grid_constant__ BatchPtrs B)
+__global__ void __launch_bounds__(RASTER_THREADS, (raster_min_blocks<CF, MS, BW, BH, FULL, HIZ>())) k_raster_batch(const __grid_constant__ BatchPtrs B)
 {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
