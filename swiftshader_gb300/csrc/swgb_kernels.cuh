@@ -1126,20 +1126,24 @@ __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
     warpBase = __shfl_sync(0xFFFFFFFFu, warpBase, 31);
     const uint64_t off = (uint64_t)warpBase + (incl - rows * (uint32_t)D.ms);
 
+    // a warp holding a 4-vertex polygon clipped by one plane writes every
+    // outline of its lanes with the 4-edge writer in one pass: a triangle is the
+    // 4-vertex outline with its last vertex repeated (the repeated vertex makes
+    // an edge of zero height, which writes no row)
+    const bool quad = cand && clipOne && n == 4;
+    const bool warpQuad = __any_sync(0xFFFFFFFFu, quad);
     bool stored = false;
     if(cand)
     {
         stored = off + (uint64_t)rows * (uint32_t)D.ms <= (uint64_t)D.spanCapacity;
         uint32_t *sp = D.spans + off;
         int32_t tMin = yMin, tMax = yMax;
-        if(stored && clipOne && n == 4)
+        if(stored && warpQuad && (!cntClip || clipOne) && D.ms == 1)
         {
-            const int32_t Xs[4] = {X0, X1, X2, X3}, Ys[4] = {Y0, Y1, Y2, Y3};
+            const int32_t Xs[4] = {X0, X1, X2, quad ? X3 : X2}, Ys[4] = {Y0, Y1, Y2, quad ? Y3 : Y2};
             spans_outline<4>(D, Xs, Ys, dW, yMin, yMax, sp, tMin, tMax);
         }
-        else if(stored && clipOne)
-            spans_triangle(D, X0, Y0, X1, Y1, X2, Y2, dW, yMin, yMax, sp, tMin, tMax);
-        else if(stored && cntClip)
+        else if(stored && cntClip && !clipOne)
             spans_clipped(D, slot, n, dW, yMin, yMax, sp, tMin, tMax);
         else if(stored && D.ms > 1)
         {
