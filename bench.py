@@ -556,7 +556,10 @@ def measure_batch(r, stream, flush, params, steps, warmup, per_draw_steps, dev, 
                                   "the faster one timed on all draws"} if sample_ms else None),
         "speedup_vs_per_draw": round(mp / mb, 2) if per_draw_steps else None,
         "draws_per_s": round(b.n / (mb * 1e-3), 1), "per_draw_draws_per_s": round(b.n / (mp * 1e-3), 1) if per_draw_steps else None,
-        "gfrag_per_s": round(per_step["fragments_tested"] / (mb * 1e-3) / 1e9, 3),
+        "gfrag_passed_per_s": round(per_step["fragments_passed"] / (mb * 1e-3) / 1e9, 3),
+        "gfrag_tested_per_s": round(per_step["fragments_tested"] / (mb * 1e-3) / 1e9, 3),
+        "tested_how": "samples tested against depth, including those of whole triangles the hierarchical depth "
+                      "rejection counts from their span rows without expanding them (the oracle's count)",
         "mtri_per_s": round(per_step["triangles_in"] / (mb * 1e-3) / 1e6, 2),
         "gpu_launches_per_step": launches / steps, "steps": steps, "per_draw_steps": per_draw_steps,
         "counters_per_step": per_step, "raster_config": tuned,
