@@ -66,6 +66,25 @@ def test_noalloc_full_pipeline_draw(gpu_lib):
     assert np.array_equal(np.ascontiguousarray(d).view(np.uint8), np.ascontiguousarray(d_ref).view(np.uint8))
 
 
+def test_noalloc_allocates_nothing(gpu_lib):
+    """After a first call (module loading and the one-time lookups), further
+    calls leave the device's free memory exactly as it was."""
+    import torch
+    from swiftshader_gb300 import DeviceScene
+    L = gpu_lib
+    sc = scenes.scene_heightfield(quads_x=120, quads_y=60, width=320, height=180, tex_size=256)
+    ds = DeviceScene(sc)
+    st, a = ds.state(), ds.args()
+    assert L.swgb_draw_noalloc(C.byref(st), C.byref(a), None) == abi.OK, L.swgb_last_error()
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(3):
+        ds.clear()
+        assert L.swgb_draw_noalloc(C.byref(st), C.byref(a), None) == abi.OK, L.swgb_last_error()
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+
+
 def test_noalloc_rejects_oversized_draws(gpu_lib):
     L = gpu_lib
     sc = scenes.scene_small(n_tris=8, width=32, height=32)
