@@ -265,26 +265,35 @@ def run_ours(args):
     per_frame = {k: v // frames if k != "texture_levels_mask" else v for k, v in cnt.items()}
 
     # ---- end to end through the API with host buffers --------------------
-    pin = lambda arr: torch.from_numpy(arr).pin_memory()
-    import numpy as np
-    h_vert = pin(np.ascontiguousarray(scene.vertices))
-    h_idx = None if scene.indices is None else pin(scenes.index_bytes(scene))
-    h_lv = [pin(np.ascontiguousarray(l)) for l in scene.texture_levels]
-    h_color = torch.empty(ds.color.shape, dtype=ds.color.dtype).pin_memory()
-    h_depth = torch.empty(ds.depth.shape, dtype=ds.depth.dtype).pin_memory()
-    h2d = h_vert.numel() * 4 + (0 if h_idx is None else h_idx.numel()) + sum(l.numel() for l in h_lv)
-    d2h = h_color.numel() * h_color.element_size() + h_depth.numel() * 4
+    # the scene's geometry (vertices, indices) and texture levels sit in two
+    # regions of the DeviceScene's allocation and its attachments in a third.
+    # Per step: the geometry, then the textures, uploaded from pinned memory on
+    # a copy stream; the draw waits for the geometry and lets only its raster
+    # stage wait for the textures (swgb_draw_args.raster_wait_event), so the
+    # texture upload runs beside vertex processing, setup and binning; one
+    # read-back of colour and depth.
+    h_geo = ds.geometry_region.cpu().pin_memory()
+    h_tex = ds.texture_region.cpu().pin_memory()
+    h_out = torch.empty(ds.outputs().shape, dtype=torch.uint8).pin_memory()
+    h2d = h_geo.numel() + h_tex.numel()
+    d2h = h_out.numel()
+    copy_stream = torch.cuda.Stream(dev)
+    ev_geo, ev_tex = torch.cuda.Event(), torch.cuda.Event()
+    ev_tex.record(copy_stream)
+    a_e2e = ds.args()
+    a_e2e.raster_wait_event = ev_tex.cuda_event
 
     def e2e_step():
-        ds.vertices.copy_(h_vert, non_blocking=True)
-        if h_idx is not None:
-            ds.indices.copy_(h_idx, non_blocking=True)
-        for d_l, h_l in zip(ds.levels, h_lv):
-            d_l.copy_(h_l, non_blocking=True)
+        copy_stream.wait_stream(stream)  # after the previous step's use of the inputs
+        with torch.cuda.stream(copy_stream):
+            ds.geometry_region.copy_(h_geo, non_blocking=True)
+            ev_geo.record(copy_stream)
+            ds.texture_region.copy_(h_tex, non_blocking=True)
+            ev_tex.record(copy_stream)
         ds.clear(r)
-        r.draw(st, a)
-        h_color.copy_(ds.color, non_blocking=True)
-        h_depth.copy_(ds.depth, non_blocking=True)
+        stream.wait_event(ev_geo)
+        r.draw(st, a_e2e)
+        h_out.copy_(ds.outputs(), non_blocking=True)
 
     for _ in range(max(1, args.warmup)):
         e2e_step()
@@ -304,7 +313,7 @@ def run_ours(args):
     # batched vs per-draw on the reduced-size atlas workload (free the frame first)
     batched = None
     if args.workload == "heightfield" and not args.no_batched:
-        del h_vert, h_idx, h_lv, h_color, h_depth
+        del h_geo, h_tex, h_out
         _, db, batched = measure_batch(r, stream, flush, BATCH_FULL, 3, 1, 1, dev, tune=not args.no_autotune,
                                        pick_sample=256)
         batched["config"]["workload"] = WORKLOADS["batch"]

@@ -281,6 +281,13 @@ typedef struct swgb_draw_args {
      * swgb_draw takes it; swgb_draw_batch and swgb_draw_noalloc return
      * SWGB_UNSUPPORTED_STATE.  0: no restart, count triangles. */
     uint32_t restart_index_count;
+    /* Optional cudaEvent_t the caller records on another stream after the
+     * last write the draw's texture levels depend on (an upload, a mip-chain
+     * blit): the draw waits for it (cudaStreamWaitEvent on the context's
+     * stream) only before its raster stage, so vertex processing, setup and
+     * binning run while the textures arrive.  NULL: no wait.  swgb_draw_batch
+     * and swgb_draw_noalloc wait for it before their first kernel. */
+    void *raster_wait_event;
 } swgb_draw_args;
 
 /* Device-side counters of one draw (the reference keeps occlusion counts per

@@ -132,7 +132,7 @@ class DrawArgs(C.Structure):
         ("instance_id", C.c_int32), ("layer", C.c_int32),
         ("render_area_x", C.c_int32), ("render_area_y", C.c_int32),
         ("render_area_width", C.c_uint32), ("render_area_height", C.c_uint32),
-        ("restart_index_count", C.c_uint32),
+        ("restart_index_count", C.c_uint32), ("raster_wait_event", C.c_void_p),
     ]
 
 

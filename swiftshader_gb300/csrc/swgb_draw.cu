@@ -632,7 +632,7 @@ void apply_config(const swgb_ctx *ctx, DrawParams &D)
     D.hiz = (int)ctx->rasterConfig.hiz;
 }
 
-swgb_status enqueue(swgb_ctx *ctx, DrawParams &D)
+swgb_status enqueue(swgb_ctx *ctx, DrawParams &D, cudaEvent_t rasterWait = nullptr)
 {
     if(D.count == 0) return SWGB_OK;  // Renderer.cpp:187
     swgb_status s;
@@ -677,6 +677,8 @@ swgb_status enqueue(swgb_ctx *ctx, DrawParams &D)
     {
         uint32_t blocks = (uint32_t)((D.binsX * D.binsY + RASTER_WARPS - 1) / RASTER_WARPS);
         if(blocks > (uint32_t)ctx->rasterBlocks[raster_variant(D)]) blocks = (uint32_t)ctx->rasterBlocks[raster_variant(D)];
+        // the textures may still be arriving on another stream
+        if(rasterWait) cudaStreamWaitEvent(ctx->stream, rasterWait, 0);
         timed_launch(ctx, SWGB_KERNEL_RASTER, [&] { launch_raster(D, blocks, ctx->stream); });
     }
     return cuda_check(cudaGetLastError(), "kernel launch");
@@ -1560,7 +1562,7 @@ swgb_status swgb_draw(swgb_ctx *ctx, const swgb_pipeline_state *st, const swgb_d
     if(D.count == 0) return SWGB_OK;
     apply_config(ctx, D);
     cudaSetDevice(ctx->device);
-    return enqueue(ctx, D);
+    return enqueue(ctx, D, (cudaEvent_t)args->raster_wait_event);
 }
 
 // The allocation-free variant of swgb_draw: the same validation, baking and
@@ -1603,6 +1605,7 @@ swgb_status swgb_draw_noalloc(const swgb_pipeline_state *st, const swgb_draw_arg
     D.binQueue = (unsigned int *)(w + 76);
     D.error = (int *)(w + 80);
     cudaStream_t st0 = (cudaStream_t)stream;
+    if(args->raster_wait_event) cudaStreamWaitEvent(st0, (cudaEvent_t)args->raster_wait_event, 0);
     // The array keeps the previous call's contents: the counters and the error
     // word are cleared here, the queue heads and super-chunk boxes by k_vertex.
     if((s = cuda_check(cudaMemsetAsync(w, 0, NA_WORDS_BYTES, st0), "clear scratch words")) != SWGB_OK) return s;
@@ -1625,6 +1628,8 @@ swgb_status swgb_draw_batch(swgb_ctx *ctx, const swgb_pipeline_state *states, co
     if(!ctx || (!states && n) || (!args && n)) return set_error(SWGB_INVALID_ARG, "null argument");
     if(n == 0) return SWGB_OK;
     cudaSetDevice(ctx->device);
+    for(uint32_t i = 0; i < n; i++)
+        if(args[i].raster_wait_event) cudaStreamWaitEvent(ctx->stream, (cudaEvent_t)args[i].raster_wait_event, 0);
     return draw_batch(ctx, states, args, n);
 }
 
@@ -1653,6 +1658,8 @@ swgb_status swgb_autotune(swgb_ctx *ctx, const swgb_pipeline_state *states, cons
     if(runs == 0) runs = SWGB_AUTOTUNE_DEFAULT_RUNS;
     if(runs > SWGB_AUTOTUNE_MAX_RUNS) return set_error(SWGB_INVALID_ARG, "swgb_autotune: runs above SWGB_AUTOTUNE_MAX_RUNS");
     cudaSetDevice(ctx->device);
+    for(uint32_t i = 0; i < n; i++)  // textures still arriving: wait before the first run
+        if(args[i].raster_wait_event) cudaStreamWaitEvent(ctx->stream, (cudaEvent_t)args[i].raster_wait_event, 0);
     // Validate every draw first (bake has no side effects), and collect the
     // attachment byte ranges the draws can touch: every row of every sample
     // plane of the colour and depth attachments, merged.

@@ -249,6 +249,8 @@ void fill_args(unsigned int count, int baseVertex, uint32_t firstVertex, const v
 	out.render_area_width = renderArea.extent.width;
 	out.render_area_height = renderArea.extent.height;
 	out.restart_index_count = restartIndexCount;
+	// the queue has already ordered every texture write before the draw
+	out.raster_wait_event = nullptr;
 }
 
 }  // namespace swgb_bridge

@@ -190,26 +190,98 @@ class Renderer:
 
 class DeviceScene:
     """A scene's buffers resident in device memory (torch tensors), plus the
-    C-ABI state that points at them."""
+    C-ABI state that points at them.
+
+    All of them live in one device allocation (``arena``): the draw's inputs
+    first (vertices and indices, ``geometry_region``; texture levels,
+    ``texture_region``), then the attachments (colour, depth, stencil;
+    ``outputs()``), each 256-byte aligned.  A caller that re-uploads the inputs
+    and reads the attachments back every frame makes few, large copies, and can
+    upload the textures while the draw's first stages run
+    (``swgb_draw_args.raster_wait_event``)."""
+
+    ALIGN = 256
 
     def __init__(self, scene, device="cuda"):
         import torch
         self.scene = scene
         self.device = torch.device(device)
-        self.vertices = torch.from_numpy(np.ascontiguousarray(scene.vertices)).to(self.device)
-        self.indices = None if scene.indices is None else torch.from_numpy(scenes.index_bytes(scene)).to(self.device)
-        self.levels = [torch.from_numpy(np.ascontiguousarray(l)).to(self.device) for l in scene.texture_levels]
         cdtype = {abi.FORMAT_R8G8B8A8_UNORM: torch.uint8, abi.FORMAT_B8G8R8A8_UNORM: torch.uint8,
                   abi.FORMAT_R8G8B8A8_SRGB: torch.uint8, abi.FORMAT_B8G8R8A8_SRGB: torch.uint8,
                   abi.FORMAT_R32G32B32A32_SFLOAT: torch.float32, abi.FORMAT_R16G16B16A16_SFLOAT: torch.float16}[scene.color_format]
         cshape, dshape = scenes.attachment_shapes(scene)
-        self.color = torch.empty(cshape, dtype=cdtype, device=self.device)
         # D16_UNORM attachments live in int16 tensors (the same bits; torch has no uint16 arithmetic)
         self.d16 = scene.depth_format == abi.FORMAT_D16_UNORM
-        self.depth = torch.empty(dshape, dtype=torch.int16 if self.d16 else torch.float32, device=self.device)
-        self.stencil = None if scene.stencil is None else torch.empty(dshape, dtype=torch.uint8, device=self.device)
+        ddtype = torch.int16 if self.d16 else torch.float32
+        up = lambda n: (n + self.ALIGN - 1) // self.ALIGN * self.ALIGN
+        inputs = [np.ascontiguousarray(scene.vertices)]
+        if scene.indices is not None:
+            inputs.append(scenes.index_bytes(scene))
+        inputs += [np.ascontiguousarray(l) for l in scene.texture_levels]
+        off, where = 0, []
+        first_level = len(inputs) - len(scene.texture_levels)
+        self.texture_offset = None
+        for i, a in enumerate(inputs):
+            if i == first_level:
+                self.texture_offset = off  # geometry before it, texture levels from it
+            where.append(off)
+            off = up(off + a.nbytes)
+        self.input_bytes = off
+        if self.texture_offset is None:
+            self.texture_offset = off
+        esize = lambda dt: torch.empty((), dtype=dt).element_size()
+        outputs = [(cshape, cdtype), (dshape, ddtype)] + ([(dshape, torch.uint8)] if scene.stencil is not None else [])
+        for shape, dt in outputs:
+            where.append(off)
+            off = up(off + int(np.prod(shape)) * esize(dt))
+        self.arena = torch.empty(off, dtype=torch.uint8, device=self.device)
+        host = np.zeros(self.input_bytes, np.uint8)
+        for a, o in zip(inputs, where):
+            host[o:o + a.nbytes] = a.reshape(-1).view(np.uint8)
+        self.arena[:self.input_bytes].copy_(torch.from_numpy(host))
+
+        def view(o, shape, dt):
+            n = int(np.prod(shape)) * esize(dt)
+            return self.arena[o:o + n].view(dt).view(shape)
+
+        tdt = {np.dtype(np.float32): torch.float32, np.dtype(np.float16): torch.float16, np.dtype(np.uint8): torch.uint8}
+        k = 0
+        self.vertices = view(where[k], inputs[k].shape, tdt[inputs[k].dtype])
+        k += 1
+        self.indices = None
+        if scene.indices is not None:
+            self.indices = view(where[k], inputs[k].shape, torch.uint8)
+            k += 1
+        self.levels = []
+        for _ in scene.texture_levels:
+            a = inputs[k]
+            self.levels.append(view(where[k], a.shape, tdt[a.dtype]))
+            k += 1
+        self.color = view(where[k], cshape, cdtype)
+        self.depth = view(where[k + 1], dshape, ddtype)
+        self.stencil = view(where[k + 2], dshape, torch.uint8) if scene.stencil is not None else None
+        self.output_region = (where[k], off)
         self._clear_rgba = None
         self.clear()
+
+    @property
+    def input_region(self):
+        """The arena's input bytes (vertices, indices, texture levels)."""
+        return self.arena[:self.input_bytes]
+
+    @property
+    def geometry_region(self):
+        """The input bytes of vertices and indices."""
+        return self.arena[:self.texture_offset]
+
+    @property
+    def texture_region(self):
+        """The input bytes of the texture levels."""
+        return self.arena[self.texture_offset:self.input_bytes]
+
+    def outputs(self):
+        """The arena's attachment bytes (colour, depth, stencil)."""
+        return self.arena[self.output_region[0]:self.output_region[1]]
 
     # colour formats whose clear value the Blitter clear takes exactly as
     # normalised floats (UNORM8: byte / 255 rounds back to the byte)

@@ -517,3 +517,35 @@ def test_stencil_with_bounds_and_d16(gpu_lib):
     s.clear_depth = 0.7
     s.depth_format = abi.FORMAT_D16_UNORM
     check_stencil_scene(s)
+
+
+def test_raster_waits_for_texture_event(gpu_lib):
+    """swgb_draw_args.raster_wait_event: textures uploaded on another stream
+    that is kept busy first; the draw's raster stage waits for the event, so
+    the frame equals the one drawn with the textures already in place (a
+    raster that ran early would read the zeroed texture levels)."""
+    import torch
+    from swiftshader_gb300 import DeviceScene, Renderer
+    s = scenes.scene_textured_small(n_tris=300, width=96, height=72)
+    c_ref, d_ref, _ = render_gpu(s)
+    r = Renderer(0)
+    ds = DeviceScene(s)
+    host_tex = ds.texture_region.cpu().pin_memory()
+    ds.texture_region.zero_()
+    busy = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    side = torch.cuda.Stream()
+    ev = torch.cuda.Event()
+    with torch.cuda.stream(side):
+        for i in range(20):
+            busy.fill_(i)
+        ds.texture_region.copy_(host_tex, non_blocking=True)
+        ev.record(side)
+    a = ds.args()
+    a.raster_wait_event = ev.cuda_event
+    ds.clear(r)
+    r.draw(ds.state(), a)
+    r.synchronize()
+    torch.cuda.synchronize()
+    assert_bit_exact(ds.color.cpu().numpy(), c_ref, "color")
+    assert_bit_exact(ds.depth_numpy(), d_ref, "depth")
