@@ -542,7 +542,7 @@ uint64_t swgb_launch_count(swgb_ctx *ctx);
 #define SWGB_KERNEL_RASTER 2
 #define SWGB_KERNEL_BATCH 3 /* one graph replay of a batch segment (three kernels) */
 #define SWGB_KERNEL_ADJOINT 4
-#define SWGB_KERNEL_BIN_ORDER 5 /* longest-first bin order of a single draw */
+#define SWGB_KERNEL_BIN_ORDER 5 /* binning of a single draw: bin order and bin lists */
 #define SWGB_KERNEL_BLIT 6      /* swgb_clear / swgb_resolve / swgb_blit */
 #define SWGB_KERNEL_KINDS 8
 swgb_status swgb_set_kernel_timing(swgb_ctx *ctx, int enable);

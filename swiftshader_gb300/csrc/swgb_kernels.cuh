@@ -1,6 +1,6 @@
 // swgb_kernels.cuh -- device code of the draw hot path (sm_103a), shared by
-// the translation units of libswgb: swgb_draw.cu (vertex, setup and adjoint
-// kernels, host side, C-ABI) and swgb_raster.cu (the raster kernel variants,
+// the translation units of libswgb: swgb_draw.cu (vertex, setup, binning and
+// adjoint kernels, host side, C-ABI) and swgb_raster.cu (the raster kernel variants,
 // compiled once per colour format and linked into the same library).
 // SWGB_RASTER_TU leaves out everything but the raster stage.
 #ifndef SWGB_KERNELS_CUH
