@@ -427,6 +427,8 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
         D.mipLinear = t.mipmap_mode == SWGB_MIPMAP_MODE_LINEAR;
         D.addrU = t.address_u;
         D.addrV = t.address_v;
+        D.texRepeatTrilinear = t.format == SWGB_FORMAT_R8G8B8A8_UNORM && !D.floatPath && D.texLinear && D.mipLinear &&
+                               D.addrU == SWGB_ADDRESS_REPEAT && D.addrV == SWGB_ADDRESS_REPEAT;
     }
     set_bins(D, BIN, BIN);
     D.nchunks = (int)((D.count + CHUNK - 1) / CHUNK);
