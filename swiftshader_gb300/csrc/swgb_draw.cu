@@ -429,6 +429,8 @@ swgb_status bake(const swgb_pipeline_state *st, const swgb_draw_args *a, DrawPar
         D.addrV = t.address_v;
         D.texRepeatTrilinear = t.format == SWGB_FORMAT_R8G8B8A8_UNORM && !D.floatPath && D.texLinear && D.mipLinear &&
                                D.addrU == SWGB_ADDRESS_REPEAT && D.addrV == SWGB_ADDRESS_REPEAT;
+        for(uint32_t i = 0; i < t.level_count && D.texRepeatTrilinear; i++)
+            if(t.levels[i].width >= 32768 || t.levels[i].height >= 32768 || t.levels[i].pitch_texels >= 32768) D.texRepeatTrilinear = 0;
     }
     set_bins(D, BIN, BIN);
     D.nchunks = (int)((D.count + CHUNK - 1) / CHUNK);

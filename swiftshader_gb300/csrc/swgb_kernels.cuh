@@ -1616,19 +1616,25 @@ __device__ __forceinline__ void sample_trilinear8(const DrawParams &D, float u, 
     }
 }
 
-// sample_trilinear8 for the common state -- R8G8B8A8_UNORM, REPEAT on u and
-// v -- with the address modes and the texel order fixed: address16 of REPEAT
-// and the wrapping offsetSample inline (the same arithmetic).  Compiled into
-// the raster variants without depth rejection only (TEXFAST): on the 1M-
-// triangle height field it took k_raster from 0.951 to 0.914 ms, while in the
-// rejection variants the second sampler copy cost the atlas 3%.
-__device__ __forceinline__ void sample_trilinear8_repeat(const DrawParams &D, float u, float v, float lod, uint32_t c[4],
-                                                         uint32_t cc[4], uint32_t &lvMask)
+// sample_trilinear8 plus the trilinear blend and the 1/0xFF00 scale for the
+// common state -- R8G8B8A8_UNORM, REPEAT on u and v, every level below 2^15
+// texels wide, high and pitched -- with the address modes and the texel order
+// fixed: address16 of REPEAT and the wrapping offsetSample inline (the same
+// arithmetic), and the level choice and texel index without the out-of-range
+// paths that state excludes.  Compiled into the raster variants without depth
+// rejection only (TEXFAST): on the 1M-triangle height field it took k_raster
+// from 0.951 to 0.898 ms, while in the rejection variants the second sampler
+// copy cost the atlas 3%.
+__device__ __forceinline__ void sample_trilinear8_repeat(const DrawParams &D, float u, float v, float lod, float out[4],
+                                                         uint32_t &lvMask)
 {
-    const int ilod = trunc_int(lod);
+    // lod comes from implicit_lod: its selects return minLod or maxLod for a
+    // NaN or out-of-range value, and the host clamps both into [0, 13] (a NaN
+    // bound truncates to level 0), so ilod is never negative
+    const int ilod = __float2int_rz(lod);
     const int top = D.levelCount - 1;
-    const int la = ilod < 0 ? 0 : (ilod > top ? top : ilod);
-    const int lb = ilod + 1 < 0 ? 0 : (ilod + 1 > top ? top : ilod + 1);
+    const int la = ilod > top ? top : ilod;
+    const int lb = ilod + 1 > top ? top : ilod + 1;
     lvMask |= (1u << la) | (1u << lb);
     const TexLevel &A = D.lv[la], &B = D.lv[lb];
     const uint32_t uu = (uint32_t)trunc_int(u * 65536.0f) & 0xFFFFu;
@@ -1637,13 +1643,24 @@ __device__ __forceinline__ void sample_trilinear8_repeat(const DrawParams &D, fl
     const uint32_t au1 = (uu + A.uHalf) & 0xFFFFu, av1 = (vv + A.vHalf) & 0xFFFFu;
     const uint32_t bu0 = (uu - B.uHalf) & 0xFFFFu, bv0 = (vv - B.vHalf) & 0xFFFFu;
     const uint32_t bu1 = (uu + B.uHalf) & 0xFFFFu, bv1 = (vv + B.vHalf) & 0xFFFFu;
+    // texel_index with width, height and pitch below 2^15 (the state's
+    // condition): MulHigh by the width / height, and the 16-bit row product,
+    // never leave the int16 range
+    const uint32_t axa0 = au0 * A.w >> 16, axa1 = au1 * A.w >> 16, aya0 = (av0 * A.h >> 16) * A.pitch, aya1 = (av1 * A.h >> 16) * A.pitch;
+    const uint32_t bxa0 = bu0 * B.w >> 16, bxa1 = bu1 * B.w >> 16, bya0 = (bv0 * B.h >> 16) * B.pitch, bya1 = (bv1 * B.h >> 16) * B.pitch;
     const uint32_t *pa = (const uint32_t *)A.buf, *pb = (const uint32_t *)B.buf;
-    const uint32_t ta00 = __ldg(pa + texel_index(A, au0, av0)), ta10 = __ldg(pa + texel_index(A, au1, av0));
-    const uint32_t ta01 = __ldg(pa + texel_index(A, au0, av1)), ta11 = __ldg(pa + texel_index(A, au1, av1));
-    const uint32_t tb00 = __ldg(pb + texel_index(B, bu0, bv0)), tb10 = __ldg(pb + texel_index(B, bu1, bv0));
-    const uint32_t tb01 = __ldg(pb + texel_index(B, bu0, bv1)), tb11 = __ldg(pb + texel_index(B, bu1, bv1));
+    const uint32_t ta00 = __ldg(pa + axa0 + aya0), ta10 = __ldg(pa + axa1 + aya0);
+    const uint32_t ta01 = __ldg(pa + axa0 + aya1), ta11 = __ldg(pa + axa1 + aya1);
+    const uint32_t tb00 = __ldg(pb + bxa0 + bya0), tb10 = __ldg(pb + bxa1 + bya0);
+    const uint32_t tb01 = __ldg(pb + bxa0 + bya1), tb11 = __ldg(pb + bxa1 + bya1);
+    uint32_t c[4], cc[4];
     bilinear8(A, au0, av0, ta00, ta10, ta01, ta11, c);
     bilinear8(B, bu0, bv0, tb00, tb10, tb01, tb11, cc);
+    const uint32_t utri = (uint32_t)__float2int_rz(lod * 65536.0f) & 0xFFFFu;  // sampleFilter trilinear blend (:324-379)
+    const float scale = 1.0f / 65280.0f;
+#pragma unroll
+    for(int j = 0; j < 4; j++)
+        out[j] = __uint2float_rn(((c[j] * (utri ^ 0xFFFFu) >> 16) + (cc[j] * utri >> 16)) & 0xFFFFu) * scale;
 }
 
 // sampleQuad2D for one lane, 16-bit channel values c << 8 (SamplerCore.cpp:668-909).
@@ -1705,10 +1722,13 @@ template<bool MIRROR_ONCE, bool TEXFAST = false>
 __device__ __forceinline__ void sample_texture_lane(const DrawParams &D, float lod, float ul, float vl, float out[4],
                                                     uint32_t &lvMask)
 {
-    uint32_t c[4], cc[4] = {0u, 0u, 0u, 0u};
     if(TEXFAST && !MIRROR_ONCE && D.texRepeatTrilinear)
-        sample_trilinear8_repeat(D, ul, vl, lod, c, cc, lvMask);
-    else if(D.mipLinear && D.texLinear && !D.texSRGB)
+    {
+        sample_trilinear8_repeat(D, ul, vl, lod, out, lvMask);
+        return;
+    }
+    uint32_t c[4], cc[4] = {0u, 0u, 0u, 0u};
+    if(D.mipLinear && D.texLinear && !D.texSRGB)
         sample_trilinear8<MIRROR_ONCE>(D, ul, vl, lod, c, cc, lvMask);
     else
     {
