@@ -268,52 +268,21 @@ def run_ours(args):
     # the scene's geometry (vertices, indices) and texture levels sit in two
     # regions of the DeviceScene's allocation and its attachments in a third.
     # Per step: the geometry, then the textures, uploaded from pinned memory on
-    # a copy stream; the draw waits for the geometry and lets only its raster
-    # stage wait for the textures (swgb_draw_args.raster_wait_event), so the
-    # texture upload runs beside vertex processing, setup and binning; one
-    # read-back of colour and depth.
+    # an upload stream; the draw waits for the geometry and lets only its
+    # raster stage wait for the textures (swgb_draw_args.raster_wait_event),
+    # so the texture upload runs beside vertex processing, setup and binning;
+    # one read-back of colour and depth.
     h_geo = ds.geometry_region.cpu().pin_memory()
     h_tex = ds.texture_region.cpu().pin_memory()
-    h_out = torch.empty(ds.outputs().shape, dtype=torch.uint8).pin_memory()
     h2d = h_geo.numel() + h_tex.numel()
-    d2h = h_out.numel()
-    copy_stream = torch.cuda.Stream(dev)
-    ev_geo, ev_tex = torch.cuda.Event(), torch.cuda.Event()
-    ev_tex.record(copy_stream)
-    a_e2e = ds.args()
-    a_e2e.raster_wait_event = ev_tex.cuda_event
-
-    def e2e_step():
-        copy_stream.wait_stream(stream)  # after the previous step's use of the inputs
-        with torch.cuda.stream(copy_stream):
-            ds.geometry_region.copy_(h_geo, non_blocking=True)
-            ev_geo.record(copy_stream)
-            ds.texture_region.copy_(h_tex, non_blocking=True)
-            ev_tex.record(copy_stream)
-        ds.clear(r)
-        stream.wait_event(ev_geo)
-        r.draw(st, a_e2e)
-        h_out.copy_(ds.outputs(), non_blocking=True)
-
-    for _ in range(max(1, args.warmup)):
-        e2e_step()
-    torch.cuda.synchronize()
-    e_starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    e_ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    barrier()
-    for i in range(args.steps):
-        flush.fill_(i & 0xFF)
-        e_starts[i].record(stream)
-        e2e_step()
-        e_ends[i].record(stream)
-    torch.cuda.synchronize()
-    barrier()
-    e2e_ms = sum(s.elapsed_time(e) for s, e in zip(e_starts, e_ends)) / args.steps
+    d2h = ds.outputs().numel()
+    e2e_ms, e2e_seq_ms = measure_e2e(r, stream, flush, [ds, DeviceScene(scene, dev)], h_geo, h_tex,
+                                     args.steps, args.warmup, barrier)
 
     # batched vs per-draw on the reduced-size atlas workload (free the frame first)
     batched = None
     if args.workload == "heightfield" and not args.no_batched:
-        del h_geo, h_tex, h_out
+        del h_geo, h_tex
         _, db, batched = measure_batch(r, stream, flush, BATCH_FULL, 3, 1, 1, dev, tune=not args.no_autotune,
                                        pick_sample=256)
         batched["config"]["workload"] = WORKLOADS["batch"]
@@ -329,7 +298,7 @@ def run_ours(args):
                          "views": measure_adjoint(r, stream, flush, dev, "views", steps=2, warmup=1)}
 
     # max over ranks
-    ms_per_step, e2e_ms = max_over_ranks([ms_per_step, e2e_ms], dev)
+    ms_per_step, e2e_ms, e2e_seq_ms = max_over_ranks([ms_per_step, e2e_ms, e2e_seq_ms], dev)
 
     if rank != 0:
         if world > 1:
@@ -373,7 +342,13 @@ def run_ours(args):
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "algorithmic_bytes_per_launch": raster_bytes, "traffic": None},
         "e2e": {"value": round(world * frag_per_frame / (e2e_ms * 1e-3) / 1e9, 4), "unit": "Gfrag/s",
-                "ms_per_step": round(e2e_ms, 4), "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                "ms_per_step": round(e2e_ms, 4), "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "how": "two frames in flight (two DeviceScenes): step i uploads its geometry and textures on "
+                       "an upload stream while step i-1 renders, and reads its colour and depth back on a "
+                       "read-back stream while step i+1 renders; L2 flushed inside every step; "
+                       "K steps between one pair of events, fill and drain included",
+                "sequential_ms_per_step": round(e2e_seq_ms, 4),
+                "sequential_value": round(world * frag_per_frame / (e2e_seq_ms * 1e-3) / 1e9, 4)},
         "gpu_launches": int(launches),
         "clocks": clk,
         "raster_config": tune,
@@ -399,6 +374,103 @@ def run_ours(args):
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def measure_e2e(r, stream, flush, dss, h_geo, h_tex, steps, warmup, barrier):
+    """Per-step milliseconds of the frame through the API with host buffers:
+    (pipelined, sequential).
+
+    Sequential: one frame at a time -- upload, clear, draw, read-back, the
+    next step after the read-back.  Pipelined: two frames in flight on two
+    DeviceScenes (``dss``); step i's uploads (upload stream) wait only until
+    the draw of step i-2 has read that scene's inputs, its clear waits until
+    the read-back of step i-2 has left that scene's attachments, and its
+    read-back (read-back stream) runs while step i+1 renders.  Every step
+    flushes L2 on the draw stream before its clear, inside the timed region;
+    the pipelined K steps are timed between one pair of events, including the
+    first upload and the last read-back."""
+    import torch
+    dev = stream.device
+    up, down = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+    sts = [d.state() for d in dss]
+    h_out = [torch.empty(d.outputs().shape, dtype=torch.uint8).pin_memory() for d in dss]
+    ev_geo = [torch.cuda.Event() for _ in dss]
+    ev_tex = [torch.cuda.Event() for _ in dss]
+    ev_drawn = [torch.cuda.Event() for _ in dss]
+    ev_read = [torch.cuda.Event() for _ in dss]
+    argl = []
+    for d, e in zip(dss, ev_tex):
+        e.record(up)  # a recorded event before the first draw refers to it
+        a = d.args()
+        a.raster_wait_event = e.cuda_event
+        argl.append(a)
+    torch.cuda.synchronize()
+
+    def upload(b):
+        d = dss[b]
+        up.wait_event(ev_drawn[b])  # the draw two steps back has read these inputs
+        with torch.cuda.stream(up):
+            d.geometry_region.copy_(h_geo, non_blocking=True)
+            ev_geo[b].record(up)
+            d.texture_region.copy_(h_tex, non_blocking=True)
+            ev_tex[b].record(up)
+
+    def render(i, b):
+        d = dss[b]
+        flush.fill_(i & 0xFF)
+        stream.wait_event(ev_read[b])  # the read-back two steps back has left the attachments
+        d.clear(r)
+        stream.wait_event(ev_geo[b])
+        r.draw(sts[b], argl[b])
+        ev_drawn[b].record(stream)
+
+    def read_back(b):
+        down.wait_event(ev_drawn[b])
+        with torch.cuda.stream(down):
+            h_out[b].copy_(dss[b].outputs(), non_blocking=True)
+            ev_read[b].record(down)
+
+    def pipelined(n):
+        for i in range(n):
+            b = i & 1
+            upload(b)
+            render(i, b)
+            read_back(b)
+        stream.wait_stream(down)
+
+    def sequential_step(i):
+        upload(0)
+        render(i, 0)
+        read_back(0)
+        stream.wait_stream(down)
+
+    for i in range(max(1, warmup)):
+        sequential_step(i)
+    pipelined(max(2, warmup))
+    torch.cuda.synchronize()
+    # sequential: per-step event pairs
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    barrier()
+    for i in range(steps):
+        starts[i].record(stream)
+        sequential_step(i)
+        ends[i].record(stream)
+    torch.cuda.synchronize()
+    seq_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / steps
+    # pipelined: one event pair around all steps
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    t0.record(stream)
+    pipelined(steps)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    # both scenes rendered the same frame as the device-resident steps
+    for b in range(len(dss)):
+        assert torch.equal(h_out[b], h_out[0]), "pipelined frames differ"
+    return t0.elapsed_time(t1) / steps, seq_ms
 
 
 def measure_blitter(r, stream, flush, dev, steps=5, warmup=3):
