@@ -593,6 +593,7 @@ swgb_status prepare_scratch(swgb_ctx *ctx, DrawParams &D, bool order = true)
     }
     D.binDiff = nullptr;
     D.binFirst = nullptr;
+    D.binCost = nullptr;
     D.binOrder = nullptr;
     D.binList = nullptr;
     D.binListCount = nullptr;
@@ -619,10 +620,12 @@ swgb_status prepare_scratch(swgb_ctx *ctx, DrawParams &D, bool order = true)
                 return s;
             ctx->binOrderAttr = true;
         }
-        if((s = ensure(ctx->binDiff, ctx->binDiffCap, cells + nbins, "bin counts")) != SWGB_OK) return s;
+        if((s = ensure(ctx->binDiff, ctx->binDiffCap, 2 * cells + nbins, "bin counts")) != SWGB_OK) return s;
         if((s = ensure(ctx->binOrder, ctx->binOrderCap, nbins, "bin order")) != SWGB_OK) return s;
         D.binDiff = ctx->binDiff;
         D.binFirst = ctx->binDiff + cells;
+        // the area estimate needs a second grid in the order kernel's shared memory
+        if(2 * cells * sizeof(int) <= BIN_ORDER_SMEM) D.binCost = reinterpret_cast<uint32_t *>(ctx->binDiff + cells + nbins);
         D.binOrder = ctx->binOrder;
     }
     return SWGB_OK;
@@ -663,7 +666,7 @@ swgb_status enqueue(swgb_ctx *ctx, DrawParams &D, cudaEvent_t rasterWait = nullp
     }
     if(D.binOrder)
     {
-        const size_t smem = (size_t)(D.binsX + 1) * (D.binsY + 1) * sizeof(int);
+        const size_t smem = (size_t)(D.binsX + 1) * (D.binsY + 1) * sizeof(int) * (D.binCost ? 2 : 1);
         cudaStream_t on = fork ? ctx->side : ctx->stream;
         timed_launch(ctx, SWGB_KERNEL_BIN_ORDER, [&] { k_bin_order<<<1, BIN_ORDER_THREADS, smem, on>>>(D); }, on);
     }

@@ -169,6 +169,8 @@ struct DrawParams {
     unsigned int *binQueue;  // next bin for the persistent raster warps
     int *binDiff;         // single draws: 2D difference array of triangle boxes over the bin grid, (binsY+1) x (binsX+1), or null
     int *binFirst;        // single draws: per bin (binsY x binsX) the first chunk whose box reaches it, or null
+    uint32_t *binCost;    // single draws: 2D difference array, like binDiff, of each chunk's triangle area spread
+                          // evenly over its box's bins, or null
     uint32_t *binOrder;   // single draws: bins longest first (k_bin_order), or null for raster order
     uint32_t *binList;       // single draws: per bin its candidate triangles in primitive order (binListCap each), or null
     uint32_t *binListCount;  // candidates per bin; above binListCap the raster walks the bin itself
@@ -290,6 +292,8 @@ __global__ void k_vertex(const __grid_constant__ DrawParams D, uint32_t nverts)
         for(uint32_t j = i; j < (uint32_t)((D.binsX + 1) * (D.binsY + 1)); j += gridDim.x * blockDim.x) D.binDiff[j] = 0;
     if(D.binFirst)
         for(uint32_t j = i; j < (uint32_t)(D.binsX * D.binsY); j += gridDim.x * blockDim.x) D.binFirst[j] = 0x7FFFFFFF;
+    if(D.binCost)
+        for(uint32_t j = i; j < (uint32_t)((D.binsX + 1) * (D.binsY + 1)); j += gridDim.x * blockDim.x) D.binCost[j] = 0u;
     if(i < nverts) vertex_body(D, i);
 }
 
@@ -1038,6 +1042,7 @@ __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
     uint32_t slot = 0, vs0 = 0, vs1 = 0, vs2 = 0;  // post-transform vertex slots
     int32_t X3 = 0, Y3 = 0;  // fourth vertex of a polygon clipped by one plane
     bool clipOne = false;    // the polygon (X0..X3, Y0..Y3) came from setup_clipped_one
+    float area2 = 0.0f;      // |doubled area| of the snapped triangle, 1/256-pixel units squared
     if(t < D.count && tri_valid(D, t))
     {
         cntIn = 1;
@@ -1069,6 +1074,7 @@ __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
                 float A = ((y0 - y2) * x1 + (y2 - y1) * x0) + (y1 - y0) * x2;
                 int32_t w0w1w2 = __float_as_int(vc[0].w) ^ __float_as_int(vc[1].w) ^ __float_as_int(vc[2].w);
                 if(w0w1w2 < 0) A = -A;
+                area2 = fabsf(A);
                 bool front = D.frontFace == SWGB_FRONT_FACE_COUNTER_CLOCKWISE ? (A >= 0.0f) : (A <= 0.0f);
                 frontBit = front ? 1 : 0;
                 bool keep = !((D.cullMode & SWGB_CULL_FRONT) && front) && !((D.cullMode & SWGB_CULL_BACK) && !front);
@@ -1262,6 +1268,28 @@ __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
     cntVis = __reduce_add_sync(0xFFFFFFFFu, cntVis);
     static_assert(CHUNK == 32, "one chunk box per warp");
     const uint32_t chunk = blk * (SETUP_THREADS / CHUNK) + (uint32_t)warp;
+    if(D.binCost && bx0 < bx1)
+    {
+        // the chunk's triangle area (each triangle's capped by its box) spread
+        // evenly over the bins of the chunk box: a cost estimate for the bin
+        // order, one difference-array update per corner
+        uint32_t a = 0u;
+        if(cntVis)
+        {
+            const uint32_t boxPx = (uint32_t)(box.z - box.x) * (uint32_t)(box.w - box.y);
+            a = min((uint32_t)(area2 * (0.5f / 65536.0f)), boxPx);
+        }
+        a = __reduce_add_sync(0xFFFFFFFFu, a);
+        const int W = D.binsX + 1;
+        const int xa = (bx0 - D.binX0) / D.binW, xb = (bx1 - 1 - D.binX0) / D.binW + 1;
+        const int ya = (by0 - D.binY0) / D.binH, yb = (by1 - 1 - D.binY0) / D.binH + 1;
+        const uint32_t w = a / (uint32_t)((xb - xa) * (yb - ya));
+        if(w && lane < 4)
+        {
+            const int idx = (lane < 2 ? ya : yb) * W + ((lane == 0 || lane == 2) ? xa : xb);
+            atomicAdd(&D.binCost[idx], (lane == 0 || lane == 3) ? w : 0u - w);
+        }
+    }
     if(D.binFirst && bx0 < bx1)
     {
         // first chunk reaching each bin, for the order's tie-break; a chunk
@@ -1293,58 +1321,112 @@ __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
 #ifndef SWGB_RASTER_TU
 __global__ void __launch_bounds__(SETUP_THREADS) k_setup(const __grid_constant__ DrawParams D) { setup_body<true>(D, blockIdx.x); }
 
-// Order of a draw's bins for the persistent raster warps.  Longest first:
-// the setup stage's difference array integrated in shared memory into
-// triangles per bin, bins bucketed by the bit length of their count, heaviest
-// bucket first, so no heavy bin starts last and holds the frame's tail.
-// Inside a bucket, bins reached earliest in the draw's triangle order go
-// first (64 sub-buckets of the first chunk index), which reads the setup
-// stage's oldest output first.  Measured on the 1M-triangle 1080p height
-// field, whose triangles are submitted bottom to top: k_raster took 1.311 ms
-// with an arbitrary order inside the buckets and 1.255 ms with this one; a
-// plain bottom-first order took 1.233 ms and a top-first one 1.59 ms, but on
-// 200k large random triangles the bottom-first order lost 6% to longest-first
-// and this one nothing.  One block; bins with the same key are independent.
+// Order of a draw's bins for the persistent raster warps.  Longest first, by
+// an estimated cost: the setup stage's two difference arrays integrated in
+// shared memory into triangles per bin and spread triangle area per bin, the
+// cost = area + triangles x (the draw's area per triangle), bucketed in
+// eighth-octave steps, heaviest bucket first, so no heavy bin starts last and
+// holds the frame's tail.  A bin's raster time follows its shaded fragments
+// more than its triangle count (on the 1M-triangle 1080p height field,
+// triangles + passed fragments explain 96% of the variance of the per-bin
+// times, triangles alone 45%); the area is the part of that known before the
+// raster.  Inside a bucket, bins reached earliest in the draw's triangle order
+// go first (16 sub-buckets of the first chunk index), which reads the setup
+// stage's oldest output first.  Measured on that frame: k_raster 0.896 ms with
+// bit-length buckets of the triangle count (warps then finished between 0.76
+// and 0.93 ms of the instrumented kernel: heavy bins started late), 0.833 ms
+// with the cost; earlier, with count buckets, an arbitrary order inside the
+// buckets had cost 4% against the first-touch one.  One block; bins with the
+// same key are independent.
 constexpr int BIN_ORDER_THREADS = 1024;
-constexpr int BIN_ORDER_SUB = 64;
-constexpr int BIN_ORDER_KEYS = 33 * BIN_ORDER_SUB;
-__device__ __forceinline__ int bin_order_key(int count, int first, int nchunks)
+constexpr int BIN_ORDER_SUB = 16;
+constexpr int BIN_ORDER_FINE = 33 * 8;  // eighth-octave steps of a 32-bit cost
+constexpr int BIN_ORDER_KEYS = BIN_ORDER_FINE * BIN_ORDER_SUB;
+__device__ __forceinline__ int bin_order_key(uint32_t cost, int first, int nchunks)
 {
-    const int len = count > 0 ? 32 - __clz(count) : 0;
+    const int len = cost > 0u ? 32 - __clz(cost) : 0;
+    const int frac = len > 3 ? (int)((cost >> (len - 4)) & 7u) : (int)((cost << (4 - len)) & 7u);
     const int sub = first == 0x7FFFFFFF ? BIN_ORDER_SUB - 1
                                         : (int)(((long long)first * (BIN_ORDER_SUB - 1)) / max(1, nchunks));
-    return (32 - len) * BIN_ORDER_SUB + sub;
+    return (BIN_ORDER_FINE - 1 - (len * 8 + frac)) * BIN_ORDER_SUB + sub;
 }
 
 __global__ void __launch_bounds__(BIN_ORDER_THREADS) k_bin_order(const __grid_constant__ DrawParams D)
 {
-    extern __shared__ int cnt[];  // (binsY + 1) x (binsX + 1)
+    extern __shared__ int cnt[];  // (binsY + 1) x (binsX + 1), then as many cost cells with binCost
     __shared__ uint32_t hist[BIN_ORDER_KEYS];
+    __shared__ unsigned long long tot[2];
     const int W = D.binsX + 1, H = D.binsY + 1, nb = D.binsX * D.binsY, tid = threadIdx.x;
-    for(int i = tid; i < W * H; i += blockDim.x) cnt[i] = D.binDiff[i];
+    uint32_t *cost = reinterpret_cast<uint32_t *>(cnt + W * H);
+    for(int i = tid; i < W * H; i += blockDim.x)
+    {
+        cnt[i] = D.binDiff[i];
+        if(D.binCost) cost[i] = D.binCost[i];
+    }
     for(int i = tid; i < BIN_ORDER_KEYS; i += blockDim.x) hist[i] = 0;
+    if(tid < 2) tot[tid] = 0ull;
     __syncthreads();
     for(int r = tid; r < H; r += blockDim.x)
     {
         int acc = 0;
-        for(int x = 0; x < W; x++) cnt[r * W + x] = (acc += cnt[r * W + x]);
+        uint32_t cacc = 0u;
+        for(int x = 0; x < W; x++)
+        {
+            cnt[r * W + x] = (acc += cnt[r * W + x]);
+            if(D.binCost) cost[r * W + x] = (cacc += cost[r * W + x]);
+        }
     }
     __syncthreads();
     for(int c = tid; c < W; c += blockDim.x)
     {
         int acc = 0;
-        for(int y = 0; y < H; y++) cnt[y * W + c] = (acc += cnt[y * W + c]);
+        uint32_t cacc = 0u;
+        for(int y = 0; y < H; y++)
+        {
+            cnt[y * W + c] = (acc += cnt[y * W + c]);
+            if(D.binCost) cost[y * W + c] = (cacc += cost[y * W + c]);
+        }
     }
     __syncthreads();
-    auto key = [&](int b) { return bin_order_key(cnt[(b / D.binsX) * W + b % D.binsX], D.binFirst[b], D.nchunks); };
+    // cost of a bin: its spread triangle area plus its triangle count weighted
+    // by the draw's mean area per triangle and bin (equal shares over the
+    // draw), or the count alone without the area array
+    float perTri = 0.0f;
+    if(D.binCost)
+    {
+        unsigned long long sc = 0ull, sa = 0ull;
+        for(int b = tid; b < nb; b += blockDim.x)
+        {
+            const int c = (b / D.binsX) * W + b % D.binsX;
+            sc += (unsigned long long)max(cnt[c], 0);
+            sa += cost[c];
+        }
+        for(int o = 16; o > 0; o >>= 1)
+        {
+            sc += __shfl_xor_sync(0xFFFFFFFFu, sc, o);
+            sa += __shfl_xor_sync(0xFFFFFFFFu, sa, o);
+        }
+        if((tid & 31) == 0)
+        {
+            atomicAdd(&tot[0], sc);
+            atomicAdd(&tot[1], sa);
+        }
+        __syncthreads();
+        perTri = tot[0] ? (float)tot[1] / (float)tot[0] : 0.0f;
+    }
+    auto key = [&](int b) {
+        const int c = (b / D.binsX) * W + b % D.binsX;
+        const float v = (float)max(cnt[c], 0) * (D.binCost ? perTri : 1.0f) + (D.binCost ? (float)cost[c] : 0.0f);
+        return bin_order_key(v >= 2147483648.0f ? 0x80000000u : (uint32_t)v, D.binFirst[b], D.nchunks);
+    };
     for(int b = tid; b < nb; b += blockDim.x) atomicAdd(&hist[key(b)], 1u);
     __syncthreads();
     // exclusive scan of the histogram, 'per' consecutive entries per thread
     __shared__ uint32_t warpSum[BIN_ORDER_THREADS / 32];
     {
         const int per = (BIN_ORDER_KEYS + BIN_ORDER_THREADS - 1) / BIN_ORDER_THREADS;
-        uint32_t v[4] = {0, 0, 0, 0}, s = 0;
-        static_assert((BIN_ORDER_KEYS + BIN_ORDER_THREADS - 1) / BIN_ORDER_THREADS <= 4, "scan entries per thread");
+        uint32_t v[8] = {0, 0, 0, 0, 0, 0, 0, 0}, s = 0;
+        static_assert((BIN_ORDER_KEYS + BIN_ORDER_THREADS - 1) / BIN_ORDER_THREADS <= 8, "scan entries per thread");
         for(int j = 0; j < per; j++)
         {
             const int i = tid * per + j;
