@@ -1095,7 +1095,12 @@ __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
                 }
                 else if(keep && cntClip)
                 {
-                    n = setup_clipped(D, vc[0], vc[1], vc[2], flagsOr, yMin, yMax, xMinS, xMaxS, slot);
+                    // through temporaries: a local whose address reaches an
+                    // out-of-line call lives in local memory on every path
+                    int32_t a0 = yMin, a1 = yMax, a2 = xMinS, a3 = xMaxS;
+                    uint32_t a4 = slot;
+                    n = setup_clipped(D, vc[0], vc[1], vc[2], flagsOr, a0, a1, a2, a3, a4);
+                    yMin = a0; yMax = a1; xMinS = a2; xMaxS = a3; slot = a4;
                     cand = n >= 3;
                 }
                 else if(keep)
@@ -1151,7 +1156,11 @@ __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
             spans_outline<4>(D, Xs, Ys, dW, yMin, yMax, sp, tMin, tMax);
         }
         else if(stored && cntClip && !clipOne)
-            spans_clipped(D, slot, n, dW, yMin, yMax, sp, tMin, tMax);
+        {
+            int32_t a0 = tMin, a1 = tMax;  // temporaries, as above
+            spans_clipped(D, slot, n, dW, yMin, yMax, sp, a0, a1);
+            tMin = a0; tMax = a1;
+        }
         else if(stored && D.ms > 1)
         {
             for(int q = 0; q < 4; q++)
@@ -1169,7 +1178,11 @@ __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
             // k_raster walks the edges itself for this triangle
         }
         else if(cntClip)
-            trim_clipped_unstored(D, slot, n, dW, tMin, tMax);
+        {
+            int32_t a0 = tMin, a1 = tMax;
+            trim_clipped_unstored(D, slot, n, dW, a0, a1);
+            tMin = a0; tMax = a1;
+        }
         else
         {
             // span scratch full: trim by direct evaluation; k_raster walks the
@@ -1777,7 +1790,10 @@ __device__ __forceinline__ void sample_quad_2d(const DrawParams &D, float u, flo
     {
         uint32_t f0u = (u0 * lv.w) & 0xFFFFu, f0v = (v0 * lv.h) & 0xFFFFu;
         uint32_t f1u = (~f0u) & 0xFFFFu, f1v = (~f0v) & 0xFFFFu;
-        bilinear_srgb(D, t00, t10, t01, t11, mulhi_u16(f0u, f0v), mulhi_u16(f1u, f0v), mulhi_u16(f0u, f1v), mulhi_u16(f1u, f1v), out);
+        uint32_t o[4];  // a temporary: the caller's array stays in registers
+        bilinear_srgb(D, t00, t10, t01, t11, mulhi_u16(f0u, f0v), mulhi_u16(f1u, f0v), mulhi_u16(f0u, f1v), mulhi_u16(f1u, f1v), o);
+#pragma unroll
+        for(int k = 0; k < 4; k++) out[k] = o[k];
         return;
     }
     bilinear8(lv, u0, v0, t00, t10, t01, t11, out);  // bilinearInterpolate, unsigned 8-bit components (:516-575)
@@ -2389,7 +2405,16 @@ __device__ __forceinline__ void shade_pixel(const DrawParams &D, const SH &S, in
         const float ul = i == 0 ? u[0] : (i == 1 ? u[1] : (i == 2 ? u[2] : u[3]));
         const float vl = i == 0 ? v[0] : (i == 1 ? v[1] : (i == 2 ? v[2] : v[3]));
         float t[4];
-        if(D.floatPath) sample_float_lane<SH::kFull>(D, lod, ul, vl, t, lvMask);
+        if(D.floatPath)
+        {
+            // temporaries: t and lvMask stay in registers on the UNORM8 path
+            float tf[4];
+            uint32_t lm = 0u;
+            sample_float_lane<SH::kFull>(D, lod, ul, vl, tf, lm);
+            lvMask |= lm;
+#pragma unroll
+            for(int k = 0; k < 4; k++) t[k] = tf[k];
+        }
         else sample_texture_lane<SH::kFull, TEXFAST>(D, lod, ul, vl, t, lvMask);
 #pragma unroll
         for(int k = 0; k < 4; k++) c[k] = t[k] * c[k];
@@ -2448,7 +2473,13 @@ __device__ __forceinline__ void rop_pixel(const DrawParams &D, SH &S, int ti, in
             const uint32_t old = CF == CF_BGRA8 ? __byte_perm(color[idx], 0u, 0x3012u) : color[idx];
 #pragma unroll
             for(int c = 0; c < 4; c++) dst[c] = (float)(((old >> (8 * c)) & 0xFFu) * 257u) * (1.0f / 0xFFFF);
-            if(SH::kFull && D.colorSRGB) srgb_decode3(dst);  // sRGBtoLinear on R, G, B (:1822-1827)
+            if(SH::kFull && D.colorSRGB)
+            {
+                float v[4] = {dst[0], dst[1], dst[2], dst[3]};
+                srgb_decode3(v);  // sRGBtoLinear on R, G, B (:1822-1827)
+#pragma unroll
+                for(int k = 0; k < 4; k++) dst[k] = v[k];
+            }
         }
         else if(CF == CF_RGBA16F)
         {
@@ -2472,7 +2503,19 @@ __device__ __forceinline__ void rop_pixel(const DrawParams &D, SH &S, int ti, in
             for(int c = 0; c < 4; c++) out[c] = col[c] * a + dst[c] * oma;
         }
         else
-            blend_generic(D, col, dst, out);
+        {
+            // temporaries: col, dst and out stay in registers on the common path
+            float gc[4], gd[4], go[4];
+#pragma unroll
+            for(int k = 0; k < 4; k++)
+            {
+                gc[k] = col[k];
+                gd[k] = dst[k];
+            }
+            blend_generic(D, gc, gd, go);
+#pragma unroll
+            for(int k = 0; k < 4; k++) out[k] = go[k];
+        }
     }
     else
     {
@@ -2484,7 +2527,13 @@ __device__ __forceinline__ void rop_pixel(const DrawParams &D, SH &S, int ti, in
         // packed in R, G, B, A byte order; B8G8R8A8 swaps R and B back on the
         // way out, and its write-mask bits with them (:2138-2143); sRGB
         // attachments encode R, G, B before the clamp (:1965-1970)
-        if(SH::kFull && D.colorSRGB) srgb_encode3(out);
+        if(SH::kFull && D.colorSRGB)
+        {
+            float v[4] = {out[0], out[1], out[2], out[3]};
+            srgb_encode3(v);
+#pragma unroll
+            for(int k = 0; k < 4; k++) out[k] = v[k];
+        }
         // clamped to [0, 1] (a NaN to 0), v * 255 rounds to 0..255: RoundInt's
         // out-of-range value and PackUnsigned's saturation never apply
         uint32_t fresh = 0;
@@ -2677,9 +2726,13 @@ __device__ __noinline__ int hiz_pass(const DrawParams &D, const SH &S, int cnt, 
 // at once.
 template<int CF, int MS, int BW, int BH, bool HIZ, bool FULL>
 __device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared<CF, MS, BW, BH, FULL> &S, int nb, int bx0, int by0, uint32_t inMask,
-                                          unsigned long long &nQuads, unsigned long long &nTested,
-                                          unsigned long long &nPassed, uint32_t &lvMask)
+                                          unsigned long long &nQuadsIo, unsigned long long &nTestedIo,
+                                          unsigned long long &nPassedIo, uint32_t &lvMaskIo)
 {
+    // the counters in registers for the batch: no out-of-line call takes
+    // their address, and the queue's shared-memory stores cannot alias them
+    unsigned long long nQuads = nQuadsIo, nTested = nTestedIo, nPassed = nPassedIo;
+    uint32_t lvMask = lvMaskIo;
     const int lane = threadIdx.x & 31;
     int cnt = 0;
     if(lane < nb) cnt = setup_batch_triangle(D, S, lane, (uint32_t)S.triList[lane], bx0, by0);
@@ -2691,7 +2744,13 @@ __device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared<CF, 
     const bool lessType = D.compareOp == SWGB_COMPARE_LESS || D.compareOp == SWGB_COMPARE_LESS_OR_EQUAL;
     const bool earlyZ = D.depthTest && (!FULL || D.earlyDepthOK) &&
                         (lessType || D.compareOp == SWGB_COMPARE_GREATER || D.compareOp == SWGB_COMPARE_GREATER_OR_EQUAL);
-    if(HIZ && earlyZ) cnt = hiz_pass<MS>(D, S, cnt, bx0, by0, inMask, lessType, nQuads, nTested);
+    if(HIZ && earlyZ)
+    {
+        unsigned long long hq = 0ull, ht = 0ull;
+        cnt = hiz_pass<MS>(D, S, cnt, bx0, by0, inMask, lessType, hq, ht);
+        nQuads += hq;
+        nTested += ht;
+    }
     const int incl = warp_incl_scan(cnt, lane);
     const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
     // Quad rounds expand 32 quad slots each and append their live pixels to
@@ -2853,6 +2912,10 @@ __device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared<CF, 
             qn = rem;
         }
     }
+    nQuadsIo = nQuads;
+    nTestedIo = nTested;
+    nPassedIo = nPassed;
+    lvMaskIo = lvMask;
     __syncwarp();
 }
 
