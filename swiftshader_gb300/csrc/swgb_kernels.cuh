@@ -2701,9 +2701,13 @@ __device__ __forceinline__ void covered_counts(const SH &S, int ti, int bx0, uin
 // Whole triangles behind the bin are counted, not expanded: returns the lane's
 // quad slot count, 0 when its triangle is rejected.
 template<int MS, class SH>
-__device__ __noinline__ int hiz_pass(const DrawParams &D, const SH &S, int cnt, int bx0, int by0, uint32_t inMask, bool lessType,
+__device__ __noinline__ int hiz_pass(const DrawParams &D, int cnt, int bx0, int by0, uint32_t inMask, bool lessType,
                                      unsigned long long &nQuads, unsigned long long &nTested)
 {
+    // the warp's staging block from the kernel's dynamic shared memory (as
+    // k_raster lays it out), so that it is addressed as shared memory here
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    const SH &S = reinterpret_cast<const SH *>(smem_raw)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
     if(!__any_sync(0xFFFFFFFFu, cnt > 0)) return cnt;
     const float zb = bin_depth_bound<MS>(S, inMask, lessType);
@@ -2747,7 +2751,7 @@ __device__ __forceinline__ void raster_batch_body(const DrawParams &D, RasterSha
     if(HIZ && earlyZ)
     {
         unsigned long long hq = 0ull, ht = 0ull;
-        cnt = hiz_pass<MS>(D, S, cnt, bx0, by0, inMask, lessType, hq, ht);
+        cnt = hiz_pass<MS, RasterShared<CF, MS, BW, BH, FULL>>(D, cnt, bx0, by0, inMask, lessType, hq, ht);
         nQuads += hq;
         nTested += ht;
     }
@@ -2924,15 +2928,20 @@ __device__ __forceinline__ void raster_batch_body(const DrawParams &D, RasterSha
 // their kernels, the 32x16 and 16x16 rejection variants on the full atlas
 // took 1343 and 1706 ms instead of 882 and 1164; this wrapper under another
 // name measured 4% slower on the atlas with the same registers and stack).
+// Out of line it finds the warp's staging block in the dynamic shared memory
+// itself, rather than taking it as a (generic) reference: atlas 884 -> 870 ms.
 // Inlined, the single-sample common variants address the staged bin as
 // shared memory throughout (out of line it arrives as a generic pointer) and
 // allocate their registers with the bin loop: on the 1M-triangle height
 // field k_raster took 0.680 ms instead of 0.744.
 template<int CF, int MS, int BW, int BH, bool HIZ, bool FULL>
-__device__ __noinline__ void raster_batch(const DrawParams &D, RasterShared<CF, MS, BW, BH, FULL> &S, int nb, int bx0, int by0,
-                                                  uint32_t inMask, unsigned long long &nQuads, unsigned long long &nTested,
-                                                  unsigned long long &nPassed, uint32_t &lvMask)
+__device__ __noinline__ void raster_batch(const DrawParams &D, int nb, int bx0, int by0, uint32_t inMask, unsigned long long &nQuads,
+                                          unsigned long long &nTested, unsigned long long &nPassed, uint32_t &lvMask)
 {
+    // the warp's staging block from the kernel's dynamic shared memory (as
+    // k_raster lays it out), so that it is addressed as shared memory here
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    RasterShared<CF, MS, BW, BH, FULL> &S = reinterpret_cast<RasterShared<CF, MS, BW, BH, FULL> *>(smem_raw)[threadIdx.x >> 5];
     raster_batch_body<CF, MS, BW, BH, HIZ, FULL>(D, S, nb, bx0, by0, inMask, nQuads, nTested, nPassed, lvMask);
 }
 
@@ -3137,7 +3146,7 @@ __device__ __forceinline__ void raster_bin(const DrawParams &D, RasterShared<CF,
         if constexpr(!HIZ && MS == 1 && !FULL)
             raster_batch_body<CF, MS, BW, BH, HIZ, FULL>(D, S, nb, bx0, by0, inMask, nQuads, nTested, nPassed, lvMask);
         else
-            raster_batch<CF, MS, BW, BH, HIZ, FULL>(D, S, nb, bx0, by0, inMask, nQuads, nTested, nPassed, lvMask);
+            raster_batch<CF, MS, BW, BH, HIZ, FULL>(D, nb, bx0, by0, inMask, nQuads, nTested, nPassed, lvMask);
     };
     const uint32_t listed = D.binList ? __ldg(D.binListCount + bin) : 0xFFFFFFFFu;
     if(listed <= D.binListCap)
