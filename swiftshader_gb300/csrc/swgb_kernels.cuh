@@ -3221,10 +3221,13 @@ __device__ __forceinline__ void raster_bin(const DrawParams &D, RasterShared<CF,
 }
 
 // Shared memory of a raster block and the blocks one SM holds with it, at
-// most 4 without hierarchical depth rejection and 5 with it: the register
-// budget follows from that (65536 / (blocks x threads): 128 and 102
-// registers).  Measured on the 1M-triangle frame (no rejection): 4 blocks
-// 0.954 ms against 1.010 for 5 (96 registers) and 0.952 for 3; on the full
+// most 5 for the single-sample variants of the common pixel pipeline and
+// those with hierarchical depth rejection, 4 for the rest: the register
+// budget follows from that (65536 / (blocks x threads): 102 and 128
+// registers).  Measured on the 1M-triangle frame (no rejection): with the
+// batch loop out of line, 4 blocks 0.954 ms against 1.010 for 5 (96
+// registers) and 0.952 for 3; with it inlined (92 registers at 5 blocks, no
+// spills) 5 blocks 0.662 ms against 0.681 for 4 and 0.675 for 3.  On the full
 // atlas's 16x16 rejection variant 5 blocks 1150 ms against 1172 for 4 and
 // 1345 for 3; a 6-block bound (80 registers, spilling) lost 5% earlier.
 template<int CF, int MS, int BW, int BH, bool FULL>
@@ -3236,7 +3239,8 @@ constexpr size_t raster_smem()
 template<int CF, int MS, int BW, int BH, bool FULL, bool HIZ = false>
 constexpr int raster_min_blocks()
 {
-    return (int)std::min<size_t>(HIZ ? 5 : 4, std::max<size_t>(1, (size_t)(228 * 1024) / (raster_smem<CF, MS, BW, BH, FULL>() + 1024)));
+    return (int)std::min<size_t>(HIZ || (MS == 1 && !FULL) ? 5 : 4,
+                                 std::max<size_t>(1, (size_t)(228 * 1024) / (raster_smem<CF, MS, BW, BH, FULL>() + 1024)));
 }
 
 template<int CF, int MS, int BW, int BH, bool HIZ, bool FULL>
