@@ -143,17 +143,29 @@ def test_autotune_leaves_one_run(gpu_lib, batched):
     assert torch.equal(db.depth, before)
 
 
+def clustered_scene(n, width, height, seed):
+    s = scenes.scene_small(n_tris=n, width=width, height=height, seed_index=seed)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    v = s.vertices
+    centers = rng.uniform(-1.0, 1.0, (n, 2)) ** 3  # denser towards the middle
+    v[:, 0:2] = (np.repeat(centers, 3, axis=0) + rng.uniform(-0.03, 0.03, (3 * n, 2))).astype(np.float32)
+    return s
+
+
 @pytest.mark.parametrize("cfg", [(16, 16, True), (16, 16, False), (32, 16, True)], ids=lambda c: "%dx%d-hiz%d" % c)
 def test_longest_first_bin_order(gpu_lib, cfg):
-    """Frames with more bins than resident raster warps take the longest-first
-    bin order (per-bin triangle counts from the setup stage): small triangles
-    clustered unevenly over a 1920x1088 frame, empty bins included."""
-    s = scenes.scene_small(n_tris=20000, width=1920, height=1088, seed_index=71)
-    rng = np.random.Generator(np.random.PCG64(71))
-    v = s.vertices
-    centers = rng.uniform(-1.0, 1.0, (20000, 2)) ** 3  # denser towards the middle
-    v[:, 0:2] = (np.repeat(centers, 3, axis=0) + rng.uniform(-0.03, 0.03, (60000, 2))).astype(np.float32)
-    check_config(s, cfg)
+    """Frames with more bins than resident raster warps take the heaviest-first
+    bin order (per-bin triangle counts and spread triangle area from the setup
+    stage): small triangles clustered unevenly over a 1920x1088 frame, empty
+    bins included."""
+    check_config(clustered_scene(20000, 1920, 1088, 71), cfg)
+
+
+def test_bin_order_by_count_only(gpu_lib):
+    """A bin grid too large for both difference arrays in the order kernel's
+    shared memory (171 x 171 cells of 16x16 bins) orders by triangle count
+    alone."""
+    check_config(clustered_scene(20000, 2720, 2720, 73), (16, 16, False))
 
 
 @pytest.mark.parametrize("cfg", [(16, 16, True), (32, 32, True)], ids=lambda c: "%dx%d" % c[:2])
