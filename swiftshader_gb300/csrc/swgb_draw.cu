@@ -621,12 +621,16 @@ swgb_status prepare_scratch(swgb_ctx *ctx, DrawParams &D, bool order = true)
             ctx->binOrderAttr = true;
         }
         if((s = ensure(ctx->binDiff, ctx->binDiffCap, 2 * cells + nbins, "bin counts")) != SWGB_OK) return s;
-        if((s = ensure(ctx->binOrder, ctx->binOrderCap, nbins, "bin order")) != SWGB_OK) return s;
+        // entries of up to two halves per bin, and their count
+        if((s = ensure(ctx->binOrder, ctx->binOrderCap, 2 * nbins + 1, "bin order")) != SWGB_OK) return s;
         D.binDiff = ctx->binDiff;
         D.binFirst = ctx->binDiff + cells;
         // the area estimate needs a second grid in the order kernel's shared memory
         if(2 * cells * sizeof(int) <= BIN_ORDER_SMEM) D.binCost = reinterpret_cast<uint32_t *>(ctx->binDiff + cells + nbins);
         D.binOrder = ctx->binOrder;
+        D.rasterWarps = ctx->rasterBlocks[raster_variant(D)] * RASTER_WARPS;
+        // half bins: the single-sample variants of the common pixel pipeline
+        D.binSplit = D.ms == 1 && !D.hiz && !full_pipeline(D);
     }
     return SWGB_OK;
 }

@@ -171,7 +171,10 @@ struct DrawParams {
     int *binFirst;        // single draws: per bin (binsY x binsX) the first chunk whose box reaches it, or null
     uint32_t *binCost;    // single draws: 2D difference array, like binDiff, of each chunk's triangle area spread
                           // evenly over its box's bins, or null
-    uint32_t *binOrder;   // single draws: bins longest first (k_bin_order), or null for raster order
+    uint32_t *binOrder;   // single draws: bins heaviest first (k_bin_order; entry = bin | part << 30, part 1 / 2
+                          // the top / bottom half of a split bin; the entry count at [2 x bins]), or null
+    uint32_t rasterWarps; // resident raster warps of the draw's variant (the split threshold)
+    int binSplit;         // the variant rasterises half bins: the order may split its heaviest bins
     uint32_t *binList;       // single draws: per bin its candidate triangles in primitive order (binListCap each), or null
     uint32_t *binListCount;  // candidates per bin; above binListCap the raster walks the bin itself
     uint32_t binListCap;
@@ -1404,15 +1407,15 @@ __global__ void __launch_bounds__(BIN_ORDER_THREADS) k_bin_order(const __grid_co
     // cost of a bin: its spread triangle area plus its triangle count weighted
     // by the draw's mean area per triangle and bin (equal shares over the
     // draw), or the count alone without the area array
-    float perTri = 0.0f;
-    if(D.binCost)
+    __shared__ uint32_t nSplit;
+    if(tid == 0) nSplit = 0u;
     {
         unsigned long long sc = 0ull, sa = 0ull;
         for(int b = tid; b < nb; b += blockDim.x)
         {
             const int c = (b / D.binsX) * W + b % D.binsX;
             sc += (unsigned long long)max(cnt[c], 0);
-            sa += cost[c];
+            if(D.binCost) sa += cost[c];
         }
         for(int o = 16; o > 0; o >>= 1)
         {
@@ -1425,14 +1428,31 @@ __global__ void __launch_bounds__(BIN_ORDER_THREADS) k_bin_order(const __grid_co
             atomicAdd(&tot[1], sa);
         }
         __syncthreads();
-        perTri = tot[0] ? (float)tot[1] / (float)tot[0] : 0.0f;
     }
-    auto key = [&](int b) {
+    const float perTri = D.binCost && tot[0] ? (float)tot[1] / (float)tot[0] : 0.0f;
+    auto value = [&](int b) {
         const int c = (b / D.binsX) * W + b % D.binsX;
-        const float v = (float)max(cnt[c], 0) * (D.binCost ? perTri : 1.0f) + (D.binCost ? (float)cost[c] : 0.0f);
+        return (float)max(cnt[c], 0) * (D.binCost ? perTri : 1.0f) + (D.binCost ? (float)cost[c] : 0.0f);
+    };
+    auto key = [&](int b, float v) {
         return bin_order_key(v >= 2147483648.0f ? 0x80000000u : (uint32_t)v, D.binFirst[b], D.nchunks);
     };
-    for(int b = tid; b < nb; b += blockDim.x) atomicAdd(&hist[key(b)], 1u);
+    // A bin whose cost exceeds 3/4 of a resident warp's mean share would hold
+    // the frame's end on its own: it is queued as two halves (its top and its
+    // bottom rows), each ordered by half the cost.
+    const float total = D.binCost ? 2.0f * (float)tot[1] : (float)tot[0];
+    const float splitAt = D.binSplit && D.rasterWarps ? 0.75f * total / (float)D.rasterWarps : 3.0e38f;
+    for(int b = tid; b < nb; b += blockDim.x)
+    {
+        const float v = value(b);
+        if(v > splitAt)
+        {
+            atomicAdd(&hist[key(b, 0.5f * v)], 2u);
+            atomicAdd(&nSplit, 1u);
+        }
+        else
+            atomicAdd(&hist[key(b, v)], 1u);
+    }
     __syncthreads();
     // exclusive scan of the histogram, 'per' consecutive entries per thread
     __shared__ uint32_t warpSum[BIN_ORDER_THREADS / 32];
@@ -1477,9 +1497,20 @@ __global__ void __launch_bounds__(BIN_ORDER_THREADS) k_bin_order(const __grid_co
     __syncthreads();
     for(int b = tid; b < nb; b += blockDim.x)
     {
-        const uint32_t pos = atomicAdd(&hist[key(b)], 1u);
-        D.binOrder[pos] = (uint32_t)b;
+        const float v = value(b);
+        if(v > splitAt)
+        {
+            const uint32_t pos = atomicAdd(&hist[key(b, 0.5f * v)], 2u);
+            D.binOrder[pos] = (uint32_t)b | 1u << 30;
+            D.binOrder[pos + 1] = (uint32_t)b | 2u << 30;
+        }
+        else
+        {
+            const uint32_t pos = atomicAdd(&hist[key(b, v)], 1u);
+            D.binOrder[pos] = (uint32_t)b;
+        }
     }
+    if(tid == 0) D.binOrder[2 * nb] = (uint32_t)nb + nSplit;
 }
 
 // Candidate lists of a single draw's bins: one warp per bin walks the
@@ -2290,7 +2321,7 @@ __device__ __noinline__ void walk_spans_in_bin(const DrawParams &D, SH &S, int t
 // quad rows, and its plane equations (SetupRoutine.cpp:270-548).  Returns the
 // number of quad slots it expands to.
 template<class SH>
-__device__ int setup_batch_triangle(const DrawParams &D, SH &S, int ti, uint32_t t, int bx0, int by0)
+__device__ int setup_batch_triangle(const DrawParams &D, SH &S, int ti, uint32_t t, int bx0, int by0, int w0 = 0, int w1 = SH::kBH)
 {
     // the plane record first: it depends on t only, and arrives while the
     // box, the record and the span rows are fetched
@@ -2303,7 +2334,14 @@ __device__ int setup_batch_triangle(const DrawParams &D, SH &S, int ti, uint32_t
     const int n = inf.info & 31, dW = (inf.info >> 5) & 1;
     S.front[ti] = (int8_t)((inf.info >> 8) & 1);
     constexpr int BW = SH::kBW, BH = SH::kBH;
-    const int rowLo = max((int)box.y, by0), rowHi = min((int)box.w, by0 + BH);  // bin rows of the triangle
+    // bin rows of the triangle, inside the rows [w0, w1) this warp takes (even)
+    const int rowLo = max((int)box.y, by0 + w0), rowHi = min((int)box.w, by0 + w1);
+    if(rowLo >= rowHi)
+    {
+        cp_async_wait_all();  // the plane record's copy lands before the slot is reused
+        S.nqr[ti] = 0;
+        return 0;
+    }
     const int qrA = (rowLo - by0) >> 1, qrB = (rowHi - 1 - by0) >> 1;            // quad rows [qrA, qrB]
     constexpr int MS = SH::kSamples;
     // rows outside [rowLo, rowHi) but inside the quad rows are empty
@@ -2732,7 +2770,7 @@ __device__ __noinline__ int hiz_pass(const DrawParams &D, int cnt, int bx0, int 
 template<int CF, int MS, int BW, int BH, bool HIZ, bool FULL>
 __device__ __forceinline__ void raster_batch_body(const DrawParams &D, RasterShared<CF, MS, BW, BH, FULL> &S, int nb, int bx0, int by0,
                                              uint32_t inMask, unsigned long long &nQuadsIo, unsigned long long &nTestedIo,
-                                             unsigned long long &nPassedIo, uint32_t &lvMaskIo)
+                                             unsigned long long &nPassedIo, uint32_t &lvMaskIo, int w0 = 0, int w1 = BH)
 {
     // the counters in registers for the batch: no out-of-line call takes
     // their address, and the queue's shared-memory stores cannot alias them
@@ -2740,7 +2778,7 @@ __device__ __forceinline__ void raster_batch_body(const DrawParams &D, RasterSha
     uint32_t lvMask = lvMaskIo;
     const int lane = threadIdx.x & 31;
     int cnt = 0;
-    if(lane < nb) cnt = setup_batch_triangle(D, S, lane, (uint32_t)S.triList[lane], bx0, by0);
+    if(lane < nb) cnt = setup_batch_triangle(D, S, lane, (uint32_t)S.triList[lane], bx0, by0, w0, w1);
     __syncwarp();
     // Depth only moves one way under LESS/LESS_OR_EQUAL (down) and GREATER/
     // GREATER_OR_EQUAL (up) with clamped, never-NaN fragment depth, so a
@@ -3054,13 +3092,16 @@ __device__ __forceinline__ void walk_bin(const DrawParams &D, SH &S, int bx0, in
 // One bin of a draw: stage its depth and colour, walk the candidates in
 // primitive order in batches, write the bin back.
 template<int CF, int MS, int BW, int BH, bool HIZ, bool FULL>
-__device__ __forceinline__ void raster_bin(const DrawParams &D, RasterShared<CF, MS, BW, BH, FULL> &S, int bin, unsigned long long &nQuads,
+__device__ __forceinline__ void raster_bin(const DrawParams &D, RasterShared<CF, MS, BW, BH, FULL> &S, int bin, int part, unsigned long long &nQuads,
                                            unsigned long long &nTested, unsigned long long &nPassed, uint32_t &lvMask)
 {
     const int lane = threadIdx.x & 31;
     constexpr int CW = color_words(CF);
     const int bx0 = D.binX0 + (bin % D.binsX) * BW;
     const int by0 = D.binY0 + (bin / D.binsX) * BH;
+    // rows [w0, w1) of the bin: all, or the top / bottom half of a split bin
+    // (the other half's warp stages and writes back its own rows)
+    const int w0 = part == 2 ? BH / 2 : 0, w1 = part == 1 ? BH / 2 : BH;
 
     // The bin is staged when its first batch arrives: a bin no candidate
     // reaches is neither read nor written back.
@@ -3074,6 +3115,7 @@ __device__ __forceinline__ void raster_bin(const DrawParams &D, RasterShared<CF,
             for(int i = lane; i < BW * BH / 4; i += 32)
             {
                 const int ly = i / (BW / 4), lx = (i % (BW / 4)) * 4;
+                if(ly < w0 || ly >= w1) continue;
                 const int px = bx0 + lx, py = by0 + ly;
                 float4 dz = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
                 if((D.depthTest || (FULL && D.depthBounds)) && py < D.sy1 && px < D.sx1)
@@ -3113,6 +3155,7 @@ __device__ __forceinline__ void raster_bin(const DrawParams &D, RasterShared<CF,
             {
                 // 16-byte segment i of the bin's colour rows: 4 / CW pixels
                 const int ly = i / (BW * CW / 4), lx = (i % (BW * CW / 4)) * 4 / CW;
+                if(ly < w0 || ly >= w1) continue;
                 const int px = bx0 + lx, py = by0 + ly;
                 uint4 cc = make_uint4(0, 0, 0, 0);
                 if(py < D.sy1 && px < D.sx1)
@@ -3163,7 +3206,7 @@ __device__ __forceinline__ void raster_bin(const DrawParams &D, RasterShared<CF,
             staged = true;
         }
         if constexpr(!HIZ && MS == 1 && !FULL)
-            raster_batch_body<CF, MS, BW, BH, HIZ, FULL>(D, S, nb, bx0, by0, inMask, nQuads, nTested, nPassed, lvMask);
+            raster_batch_body<CF, MS, BW, BH, HIZ, FULL>(D, S, nb, bx0, by0, inMask, nQuads, nTested, nPassed, lvMask, w0, w1);
         else
             raster_batch<CF, MS, BW, BH, HIZ, FULL>(D, nb, bx0, by0, inMask, nQuads, nTested, nPassed, lvMask);
     };
@@ -3192,7 +3235,8 @@ __device__ __forceinline__ void raster_bin(const DrawParams &D, RasterShared<CF,
             for(int i = lane; i < BW * BH; i += 32)
             {
                 const int px = bx0 + i % BW, py = by0 + i / BW;
-                if(py >= D.sy0 && py < D.sy1 && px >= D.sx0 && px < D.sx1) sbase[(size_t)py * D.stencilPitch + px] = S.stencil[q][i];
+                if(py >= D.sy0 && py < D.sy1 && px >= D.sx0 && px < D.sx1 && i / BW >= w0 && i / BW < w1)
+                    sbase[(size_t)py * D.stencilPitch + px] = S.stencil[q][i];
             }
         }
     for(int q = 0; q < MS; q++)
@@ -3204,7 +3248,7 @@ __device__ __forceinline__ void raster_bin(const DrawParams &D, RasterShared<CF,
             if(!D.depthWrite) break;
             const int ly = i / (BW / 4), lx = (i % (BW / 4)) * 4;
             const int px = bx0 + lx, py = by0 + ly;
-            if(py >= D.sy1 || px >= D.sx1 || py < D.sy0) continue;
+            if(py >= D.sy1 || px >= D.sx1 || py < D.sy0 || ly < w0 || ly >= w1) continue;
             uint8_t *drow = dbase + (size_t)py * D.depthPitch;
             if(FULL && D.depth16)
             {
@@ -3227,7 +3271,7 @@ __device__ __forceinline__ void raster_bin(const DrawParams &D, RasterShared<CF,
         {
             const int ly = i / (BW * CW / 4), lx = (i % (BW * CW / 4)) * 4 / CW;
             const int px = bx0 + lx, py = by0 + ly;
-            if(py >= D.sy1 || px >= D.sx1 || py < D.sy0) continue;
+            if(py >= D.sy1 || px >= D.sx1 || py < D.sy0 || ly < w0 || ly >= w1) continue;
             uint8_t *crow = cbase + (size_t)py * D.colorPitch + (size_t)px * 4 * CW;
             if(D.vec16 && px + 4 / CW <= D.sx1 && px >= D.sx0)
                 *(uint4 *)crow = *(const uint4 *)&S.color[q][(ly * BW + lx) * CW];
@@ -3269,18 +3313,20 @@ __global__ void __launch_bounds__(RASTER_THREADS, (raster_min_blocks<CF, MS, BW,
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     RasterShared<CF, MS, BW, BH, FULL> &S = reinterpret_cast<RasterShared<CF, MS, BW, BH, FULL> *>(smem_raw)[warp];
     const int nbins = D.binsX * D.binsY;
+    // queue entries: the bins, or with an order its entries (split bins twice)
+    const int entries = D.binOrder ? (int)__ldg(D.binOrder + 2 * nbins) : nbins;
     unsigned long long nQuads = 0, nTested = 0, nPassed = 0;
     uint32_t lvMask = 0;
     // Persistent warps: each takes the next bin from the queue until it drains,
     // so a slow bin never holds idle warps of its block.
     for(;;)
     {
-        int bin = 0;
-        if(lane == 0) bin = (int)atomicAdd(D.binQueue, 1u);
-        bin = __shfl_sync(0xFFFFFFFFu, bin, 0);
-        if(bin >= nbins) break;
-        if(D.binOrder) bin = (int)__ldg(D.binOrder + bin);
-        raster_bin<CF, MS, BW, BH, HIZ, FULL>(D, S, bin, nQuads, nTested, nPassed, lvMask);
+        int item = 0;
+        if(lane == 0) item = (int)atomicAdd(D.binQueue, 1u);
+        item = __shfl_sync(0xFFFFFFFFu, item, 0);
+        if(item >= entries) break;
+        const uint32_t e = D.binOrder ? __ldg(D.binOrder + item) : (uint32_t)item;
+        raster_bin<CF, MS, BW, BH, HIZ, FULL>(D, S, (int)(e & 0x3FFFFFFFu), (int)(e >> 30), nQuads, nTested, nPassed, lvMask);
     }
     flush_counters(D.counters, nQuads, nTested, nPassed, lvMask);
 }
@@ -3397,7 +3443,7 @@ __global__ void __launch_bounds__(RASTER_THREADS, (raster_min_blocks<CF, MS, BW,
         bin = __shfl_sync(0xFFFFFFFFu, bin, 0);
         if(bin >= h.bins) break;
         const uint32_t d = find_draw(V.bStart, h.n, bin);
-        raster_bin<CF, MS, BW, BH, HIZ, FULL>(V.draws[d], S, (int)(bin - __ldg(V.bStart + d)), nQuads, nTested, nPassed, lvMask);
+        raster_bin<CF, MS, BW, BH, HIZ, FULL>(V.draws[d], S, (int)(bin - __ldg(V.bStart + d)), 0, nQuads, nTested, nPassed, lvMask);
     }
     flush_counters(B.counters, nQuads, nTested, nPassed, lvMask);
 }
