@@ -1439,7 +1439,10 @@ __global__ void __launch_bounds__(BIN_ORDER_THREADS) k_bin_order(const __grid_co
     };
     // A bin whose cost exceeds 3/4 of a resident warp's mean share would hold
     // the frame's end on its own: it is queued as two halves (its top and its
-    // bottom rows), each ordered by half the cost.
+    // bottom rows), each ordered by half the cost.  On the 1M-triangle 1080p
+    // height field the heaviest bin alone took longer than the warps' mean
+    // load (0.73 vs 0.58 ms, instrumented); splitting at 3/4 took k_raster
+    // 0.659 -> 0.636 ms (at 1/2: 0.670, at 1: 0.664).
     const float total = D.binCost ? 2.0f * (float)tot[1] : (float)tot[0];
     const float splitAt = D.binSplit && D.rasterWarps ? 0.75f * total / (float)D.rasterWarps : 3.0e38f;
     for(int b = tid; b < nb; b += blockDim.x)
