@@ -900,7 +900,8 @@ __device__ __forceinline__ void spans_outline(const DrawParams &D, const int32_t
     // edges in the reference's order: edge i runs from vertex i+1-d to vertex i+d
     EdgeDDA e[N];
     bool ok[N];
-    int32_t ex[N], ed[N];
+    int32_t ex[N], ed[N], y0[N];
+    uint32_t nr[N];
 #pragma unroll
     for(int i = 0; i < N; i++)
     {
@@ -911,6 +912,10 @@ __device__ __forceinline__ void spans_outline(const DrawParams &D, const int32_t
         ex[i] = 0;
         ed[i] = 0;
         if(ok[i]) ex[i] = edge_x_at(e[i], e[i].yMin, &ed[i]);
+        // rows of the edge as one unsigned range test: y - yMin < rows (none
+        // for an edge that writes no row)
+        y0[i] = ok[i] ? e[i].yMin : 0;
+        nr[i] = ok[i] ? (uint32_t)(e[i].yMax - e[i].yMin) : 0u;
     }
     first = yMax;
     last = yMax;
@@ -921,7 +926,7 @@ __device__ __forceinline__ void spans_outline(const DrawParams &D, const int32_t
 #pragma unroll
         for(int i = 0; i < N; i++)
         {
-            if(ok[i] && y >= e[i].yMin && y < e[i].yMax)
+            if((uint32_t)(y - y0[i]) < nr[i])
             {
                 const int32_t x = clamp_x(D, ex[i]);
                 if(e[i].right) r = x; else l = x;
