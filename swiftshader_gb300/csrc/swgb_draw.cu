@@ -541,7 +541,8 @@ constexpr uint32_t BIN_LIST_DEFAULT = 1024;          // candidates per bin list
 constexpr size_t BIN_LIST_BYTES = (size_t)256 << 20;  // all of a draw's bin lists
 
 // Grows the context's scratch for draw D and points D at it; with order, also
-// the scratch of the longest-first bin order when it applies.
+// the scratch of the heaviest-first bin order (and of its split bins) when it
+// applies.
 swgb_status prepare_scratch(swgb_ctx *ctx, DrawParams &D, bool order = true)
 {
     swgb_status s;

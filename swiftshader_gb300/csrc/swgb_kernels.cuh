@@ -1252,7 +1252,7 @@ __device__ __forceinline__ void setup_body(const DrawParams &D, uint32_t blk)
     }
     if(D.binDiff)
     {
-        // triangles per bin, for the raster's longest-first bin order: the
+        // triangles per bin, for the raster's heaviest-first bin order: the
         // box's bin rectangle into a 2D difference array (k_bin_order
         // integrates).  Neighbouring triangles share corners, so lanes adding
         // to the same corner are merged first: one atomic per distinct corner.
@@ -3097,8 +3097,9 @@ __device__ __forceinline__ void walk_bin(const DrawParams &D, SH &S, int bx0, in
     if(listCount > 0) batch(listCount);
 }
 
-// One bin of a draw: stage its depth and colour, walk the candidates in
-// primitive order in batches, write the bin back.
+// One bin of a draw (part 0), or the top (1) / bottom (2) half of its rows:
+// stage its depth and colour, walk the candidates in primitive order in
+// batches, write the bin back.
 template<int CF, int MS, int BW, int BH, bool HIZ, bool FULL>
 __device__ __forceinline__ void raster_bin(const DrawParams &D, RasterShared<CF, MS, BW, BH, FULL> &S, int bin, int part, unsigned long long &nQuads,
                                            unsigned long long &nTested, unsigned long long &nPassed, uint32_t &lvMask)
@@ -3325,8 +3326,9 @@ __global__ void __launch_bounds__(RASTER_THREADS, (raster_min_blocks<CF, MS, BW,
     const int entries = D.binOrder ? (int)__ldg(D.binOrder + 2 * nbins) : nbins;
     unsigned long long nQuads = 0, nTested = 0, nPassed = 0;
     uint32_t lvMask = 0;
-    // Persistent warps: each takes the next bin from the queue until it drains,
-    // so a slow bin never holds idle warps of its block.
+    // Persistent warps: each takes the next queue entry (a bin, or half of a
+    // split one) until the queue drains, so a slow bin never holds idle warps
+    // of its block.
     for(;;)
     {
         int item = 0;
