@@ -360,7 +360,7 @@ swgb_status swgb_plan_batch(const swgb_pipeline_state *states, const swgb_draw_a
  * as there is no context to report them through.  The array's address is
  * resolved once per device and kept for the life of the process, so a
  * device reset (cudaDeviceReset) followed by more calls is not supported.
- * Unlike swgb_draw, this path does not order the bins longest first: the
+ * Unlike swgb_draw, this path does not order the bins heaviest first: the
  * result is the same, a large frame can take longer. */
 #define SWGB_NOALLOC_MAX_TRIANGLES 32768u
 #define SWGB_NOALLOC_MAX_VERTICES 98304u
