@@ -161,6 +161,21 @@ def test_longest_first_bin_order(gpu_lib, cfg):
     check_config(clustered_scene(20000, 1920, 1088, 71), cfg)
 
 
+@pytest.mark.parametrize("fmt", [abi.FORMAT_R8G8B8A8_UNORM, abi.FORMAT_R32G32B32A32_SFLOAT], ids=["rgba8", "rgba32f"])
+def test_split_bins_with_offsets(gpu_lib, fmt):
+    """Bins heavy enough to be queued as their top and bottom halves
+    (triangles clustered in the middle of the frame), under a viewport and a
+    scissor that are not aligned to the bins, with 8-bit and float colour
+    attachments (each half stages and writes back only its rows)."""
+    s = clustered_scene(20000, 1920, 1088, 75)
+    s.viewport = (13, -7, 1900, 1080)
+    s.scissor = (5, 11, 1890, 1060)
+    if fmt != abi.FORMAT_R8G8B8A8_UNORM:
+        s.color_format = fmt
+        s.clear_color = (0.0, 0.0, 0.0, 0.0)
+    check_config(s, (16, 16, False))
+
+
 def test_bin_order_by_count_only(gpu_lib):
     """A bin grid too large for both difference arrays in the order kernel's
     shared memory (171 x 171 cells of 16x16 bins) orders by triangle count
