@@ -1447,7 +1447,7 @@ __global__ void __launch_bounds__(BIN_ORDER_THREADS) k_bin_order(const __grid_co
     // bottom rows), each ordered by half the cost.  On the 1M-triangle 1080p
     // height field the heaviest bin alone took longer than the warps' mean
     // load (0.73 vs 0.58 ms, instrumented); splitting at 3/4 took k_raster
-    // 0.659 -> 0.636 ms (at 1/2: 0.670, at 1: 0.664).
+    // 0.659 -> 0.636 ms (at 1/2: 0.670, 0.65: 0.649, 0.85: 0.648, 1: 0.664).
     const float total = D.binCost ? 2.0f * (float)tot[1] : (float)tot[0];
     const float splitAt = D.binSplit && D.rasterWarps ? 0.75f * total / (float)D.rasterWarps : 3.0e38f;
     for(int b = tid; b < nb; b += blockDim.x)
