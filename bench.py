@@ -382,6 +382,20 @@ def run_ours(args):
                 tj = json.load(f)
             if tj.get("workload") == args.workload:
                 line["roofline"]["traffic"] = tj["bytes_per_launch"]
+                # the issue-side bound the kernel runs against: its warp
+                # instructions per launch (the same ncu capture) over the live
+                # launch time, against one instruction per scheduler (4 per
+                # SM) per cycle at the SM clock sampled during the timed steps
+                inst = tj.get("warp_instructions_per_launch")
+                mhz = (clk or {}).get("sm_mhz") or (clk or {}).get("sm_max_mhz")
+                if inst and mhz and rast_avg > 0:
+                    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+                    ach = inst / (rast_avg * 1e-3) / 1e9
+                    peak_i = sms * 4 * mhz * 1e6 / 1e9
+                    line["roofline"]["issue"] = {"warp_instructions_per_launch": inst, "achieved": round(ach, 1),
+                                                 "peak": round(peak_i, 1), "unit": "G warp instructions/s",
+                                                 "frac": round(ach / peak_i, 4),
+                                                 "how": "%d SMs x 4 schedulers x %g MHz; instructions from ncu" % (sms, mhz)}
         except Exception:
             pass
     if batched is not None:
